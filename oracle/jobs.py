@@ -1,0 +1,180 @@
+"""Job files for the checkers: the reference's own classes (oracle/_ref/ref_harness)
+and the C restatement (oracle/_build/sfxc_oracle) take identical jobs and write
+identical output files, so one job can be run through both and compared.
+
+Test infrastructure only (tests/, golden-fixture generation, the CPU baseline).
+The reference harness needs the reference checkout (oracle/build_ref.py) and so
+runs only where that checkout exists; the restatement builds anywhere with gcc.
+"""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+from . import build_ref, build_oracle
+
+
+def harness():
+    exe = build_ref.build()
+    if exe is None:
+        raise RuntimeError("reference checkout not available; the reference harness cannot be built")
+    return exe
+
+
+def restatement():
+    return build_oracle.build()
+
+
+_EXE = {"reference": harness, "oracle": restatement}
+
+
+def _write_job(path, lines):
+    with open(path, "w") as f:
+        for key, *vals in lines:
+            f.write(key + " " + " ".join(str(v) for v in vals) + "\n")
+
+
+def _run(mode, lines, out, workdir, impl):
+    job = os.path.join(workdir, mode + ".job")
+    _write_job(job, lines)
+    r = subprocess.run([_EXE[impl](), mode, job, out], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("%s %s failed (%d): %s%s" % (impl, mode, r.returncode, r.stdout, r.stderr))
+
+
+def delays(del_bytes, start_ticks, stop_ticks, sample_rate, bits, probes=(), clock=None, impl="reference"):
+    """Input_node_tasklet delay list for one interval + spline probes.
+
+    Returns (list of (ticks, bytes, remaining_samples), list of
+    (ticks, delay, rate, phase, amplitude)).
+    """
+    with tempfile.TemporaryDirectory() as d:
+        delf = os.path.join(d, "st.del")
+        open(delf, "wb").write(del_bytes)
+        lines = [("delfile", delf), ("start_ticks", start_ticks), ("stop_ticks", stop_ticks),
+                 ("sample_rate", sample_rate), ("bits_per_sample", bits)]
+        if clock is not None:
+            lines.append(("clock",) + tuple(clock))
+        lines += [("probe", p) for p in probes]
+        out = os.path.join(d, "out.txt")
+        _run("delays", lines, out, d, impl)
+        dl, pr = [], []
+        for line in open(out):
+            v = line.split()
+            if v[0] == "P":
+                pr.append((int(v[1]),) + tuple(float(x) for x in v[2:]))
+            else:
+                dl.append((int(v[0]), int(v[1]), int(v[2])))
+        return dl, pr
+
+
+def protocol(blocks, slices, sample_rate, bits, integr_time_us, station_number=0, impl="reference"):
+    """Input_node_data_writer protocol bytes for each slice.
+
+    blocks: list of (start_ticks, bytes, [(invalid_begin, nr_invalid), ...])
+    slices: list of (start_ticks, stop_ticks, nr_samples, delay_list)
+    """
+    with tempfile.TemporaryDirectory() as d:
+        blob = os.path.join(d, "blocks.bin")
+        offs = []
+        with open(blob, "wb") as f:
+            pos = 0
+            for st, data, inv in blocks:
+                f.write(bytes(data))
+                offs.append((st, pos, len(data), inv))
+                pos += len(data)
+        lines = [("sample_rate", sample_rate), ("bits_per_sample", bits),
+                 ("integr_time_us", integr_time_us), ("station_number", station_number),
+                 ("blockfile", blob)]
+        for st, pos, n, inv in offs:
+            flat = [x for pair in inv for x in pair]
+            lines.append(("block", st, pos, n, *flat))
+        for k, (s0, s1, ns, dl) in enumerate(slices):
+            dpath = os.path.join(d, "dl%d.txt" % k)
+            with open(dpath, "w") as f:
+                for t, b, r in dl:
+                    f.write("%d %d %d\n" % (t, b, r))
+            lines.append(("slice", s0, s1, ns))
+            lines.append(("dlist", dpath))
+        out = os.path.join(d, "proto.bin")
+        _run("protocol", lines, out, d, impl)
+        raw = open(out, "rb").read()
+        res, p = [], 0
+        while p < len(raw):
+            n = int(np.frombuffer(raw[p:p + 8], dtype=np.uint64)[0])
+            res.append(raw[p + 8:p + 8 + n])
+            p += 8 + n
+        return res
+
+
+def extract(words_bytes, word_bytes, bits, nsamples, tracks, impl="reference"):
+    """Channel_extractor_5 output per subband (bytes)."""
+    with tempfile.TemporaryDirectory() as d:
+        inf = os.path.join(d, "in.bin")
+        open(inf, "wb").write(bytes(words_bytes))
+        lines = [("word_bytes", word_bytes), ("bits_per_sample", bits), ("nsamples", nsamples),
+                 ("infile", inf)] + [("subband", *t) for t in tracks]
+        out = os.path.join(d, "out.bin")
+        _run("extract", lines, out, d, impl)
+        raw = open(out, "rb").read()
+        per = nsamples * len(tracks[0]) // 8
+        return [raw[i * per:(i + 1) * per] for i in range(len(tracks))]
+
+
+def correlate(job, dump=False, impl="reference", precision=32):
+    """Run Bit2float_worker -> Delay_correction -> Correlation_core(_pulsar).
+
+    job: dict with keys of the harness 'correlate' mode (see ref_harness.cc);
+    'del_bytes' (list per station), 'protocols' (list per stream of a list of
+    per-integration byte strings).  Returns dict with cor bytes, stats lines,
+    tsys bytes and (dump=True) per-integration unpacked/rows arrays.
+    """
+    with tempfile.TemporaryDirectory() as d:
+        lines = []
+        for k, db in enumerate(job["del_bytes"]):
+            p = os.path.join(d, "st%d.del" % k)
+            open(p, "wb").write(db)
+            lines.append(("delfile", p))
+        for key in ["experiment_start_ticks", "start_ticks", "integration_time_us",
+                    "sub_integration_time_us", "number_channels", "fft_size_delaycor",
+                    "fft_size_correlation", "sample_rate", "channel_freq", "bandwidth", "sideband",
+                    "frequency_nr", "polarisation", "cross_polarize", "reference_station", "window",
+                    "source", "integration_nr", "n_integrations"]:
+            lines.append((key, job[key]))
+        for k, s in enumerate(job["streams"]):
+            lines.append(("stream",) + tuple(s))
+            p = os.path.join(d, "proto%d.bin" % k)
+            with open(p, "wb") as f:
+                for chunk in job["protocols"][k]:
+                    f.write(np.uint64(len(chunk)).tobytes())
+                    f.write(bytes(chunk))
+            lines.append(("protocol", p))
+        if "pulsar" in job:
+            lines.append(("pulsar",) + tuple(job["pulsar"]))
+            for pc in job["polyco"]:
+                lines.append(("polyco",) + tuple(pc))
+        if dump:
+            lines.append(("dump", 1))
+        if precision != 32:
+            lines.append(("precision", precision))
+        outdir = os.path.join(d, "out")
+        os.makedirs(outdir)
+        _run("correlate", lines, outdir, d, impl)
+        res = {"cor": open(os.path.join(outdir, "out.cor"), "rb").read(),
+               "stats": open(os.path.join(outdir, "stats.txt")).read(),
+               "tsys": open(os.path.join(outdir, "tsys.bin"), "rb").read()}
+        p64 = os.path.join(outdir, "out64.bin")
+        if os.path.exists(p64):
+            res["vis64"] = np.fromfile(p64, dtype=np.complex128)
+        if dump:
+            un, rows = {}, {}
+            for it in range(int(job["n_integrations"])):
+                for k in range(len(job["streams"])):
+                    un[(it, k)] = np.fromfile(os.path.join(outdir, "unpacked_i%d_s%d.f32" % (it, k)),
+                                              dtype=np.float32)
+                    rows[(it, k)] = np.fromfile(os.path.join(outdir, "rows_i%d_s%d.c64" % (it, k)),
+                                                dtype=np.complex64)
+            res["unpacked"] = un
+            res["rows"] = rows
+        return res

@@ -1,0 +1,559 @@
+// Checker harness: drives the REFERENCE's own correlator-node classes
+// (compiled from the reference sources by oracle/build_ref.py) on one job and
+// writes their outputs to files.  Test infrastructure only: it generates the
+// golden fixtures under tests/golden/ and pins the C restatement in
+// oracle/sfxc_oracle.c.  Nothing in the product links or runs it.
+//
+// Modes
+//   correlate <job> <outdir>  Bit2float_worker -> Delay_correction ->
+//                             Correlation_core(_pulsar), wired as in
+//                             Correlator_node::hook_added_data_reader
+//                             (sfxc/src/correlator_node.cc:213-249) and polled
+//                             as in Correlator_node::correlate (263-296).
+//   delays <job> <outfile>    Input_node_tasklet::get_delay/get_delays as
+//                             called by add_time_interval
+//                             (sfxc/src/input_node_tasklet.cc:103-128,235-282).
+//   protocol <job> <outfile>  Input_node_data_writer::do_task producing the
+//                             correlator-node byte protocol
+//                             (sfxc/src/input_node_data_writer.cc:107-229).
+//   extract <job> <outfile>   Channel_extractor_5 (sfxc/src/channel_extractor_5.cc).
+//
+// Job files are "key value..." text lines (written by tests/golden/make_golden.py
+// and oracle/refrun.py).
+#define private public
+#define protected public
+#include "bit2float_worker.h"
+#include "bit_statistics.h"
+#include "channel_extractor_5.h"
+#include "control_parameters.h"
+#include "correlation_core.h"
+#include "correlation_core_pulsar.h"
+#include "correlator_node_types.h"
+#include "data_writer.h"
+#include "delay_correction.h"
+#include "delay_table_akima.h"
+#include "input_node_data_writer.h"
+#include "input_node_tasklet.h"
+#undef private
+#undef protected
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <new>
+#include <sstream>
+#include <string>
+#include <vector>
+
+struct ShimMessage {
+  int tag;
+  std::vector<char> bytes;
+};
+extern std::vector<ShimMessage> g_shim_messages;
+
+typedef std::map<std::string, std::vector<std::string> > Kv;
+
+static void die(const std::string &m) {
+  std::fprintf(stderr, "ref_harness: %s\n", m.c_str());
+  std::exit(2);
+}
+
+// Reads "key v1 v2 ..." lines.  Repeated keys get an index suffix "#k".
+static Kv read_job(const char *path) {
+  std::ifstream in(path);
+  if (!in) die(std::string("cannot open ") + path);
+  Kv kv;
+  std::map<std::string, int> count;
+  std::string line;
+  while (std::getline(in, line)) {
+    if (line.empty() || line[0] == '#') continue;
+    std::istringstream ss(line);
+    std::string key, v;
+    ss >> key;
+    std::vector<std::string> vals;
+    while (ss >> v) vals.push_back(v);
+    std::ostringstream k2;
+    k2 << key << "#" << count[key]++;
+    kv[k2.str()] = vals;
+    if (count[key] == 1) kv[key] = vals;
+  }
+  return kv;
+}
+
+static const std::vector<std::string> &get(const Kv &kv, const std::string &k) {
+  Kv::const_iterator it = kv.find(k);
+  if (it == kv.end()) die("missing key " + k);
+  return it->second;
+}
+static int geti(const Kv &kv, const std::string &k, int i = 0) { return std::atoi(get(kv, k)[i].c_str()); }
+static long long getll(const Kv &kv, const std::string &k, int i = 0) { return std::atoll(get(kv, k)[i].c_str()); }
+static double getd(const Kv &kv, const std::string &k, int i = 0) { return std::strtod(get(kv, k)[i].c_str(), 0); }
+static bool has(const Kv &kv, const std::string &k) { return kv.find(k) != kv.end(); }
+static int count_key(const Kv &kv, const std::string &k) {
+  int n = 0;
+  while (true) {
+    std::ostringstream s;
+    s << k << "#" << n;
+    if (!has(kv, s.str())) return n;
+    n++;
+  }
+}
+static std::string idx(const std::string &k, int i) {
+  std::ostringstream s;
+  s << k << "#" << i;
+  return s.str();
+}
+
+static std::vector<char> read_file(const std::string &path) {
+  std::ifstream in(path.c_str(), std::ios::binary);
+  if (!in) die("cannot open " + path);
+  return std::vector<char>((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+}
+static void write_file(const std::string &path, const void *p, size_t n) {
+  FILE *f = std::fopen(path.c_str(), "wb");
+  if (!f) die("cannot write " + path);
+  if (n) std::fwrite(p, 1, n, f);
+  std::fclose(f);
+}
+
+// Time from "ticks" (int64 clock ticks at 512 MHz since MJD 51544).
+static Time ticks_time(long long ticks) {
+  Time t;
+  t.set_clock_ticks(ticks);
+  return t;
+}
+
+class Memory_writer : public Data_writer {
+ public:
+  std::vector<char> bytes;
+  bool can_write() { return true; }
+
+ private:
+  size_t do_put_bytes(size_t n, const char *buf) {
+    bytes.insert(bytes.end(), buf, buf + n);
+    return n;
+  }
+};
+
+// Builds a Delay_table for one station: job keys "delfile#k", optional
+// "clock#k offset rate epoch_ticks".
+static Delay_table load_delay_table(const Kv &kv, int st) {
+  Delay_table t;
+  t.open(get(kv, idx("delfile", st))[0].c_str());
+  if (has(kv, idx("clock", st))) {
+    const std::vector<std::string> &c = get(kv, idx("clock", st));
+    t.set_clock_offset(std::strtod(c[0].c_str(), 0), Time(), std::strtod(c[1].c_str(), 0),
+                       ticks_time(std::atoll(c[2].c_str())));
+  }
+  return t;
+}
+
+// ---------------------------------------------------------------- delays ---
+static int mode_delays(const Kv &kv, const char *outfile) {
+  Delay_table table = load_delay_table(kv, 0);
+  long long start_ticks = getll(kv, "start_ticks");
+  long long stop_ticks = getll(kv, "stop_ticks");
+  int sample_rate = geti(kv, "sample_rate");
+  int bps = geti(kv, "bits_per_sample");
+
+  // The tasklet is only used for its delay members; its reader/writer
+  // members are never touched by get_delay/get_delays.
+  void *mem = std::calloc(1, sizeof(Input_node_tasklet));
+  Input_node_tasklet *t = static_cast<Input_node_tasklet *>(mem);
+  new (&t->delay_table) Delay_table();
+  new (&t->akima_delays) Delay_table_akima();
+  t->delay_table.add_scans(table);
+  t->sample_rate = sample_rate;
+  t->bits_per_sample = bps;
+
+  Time start_time = ticks_time(start_ticks), stop_time = ticks_time(stop_ticks);
+  // add_time_interval (sfxc/src/input_node_tasklet.cc:103-115)
+  t->akima_delays = t->delay_table.create_akima_spline(start_time, stop_time - start_time);
+  std::vector<Delay> list;
+  list.push_back(t->get_delay(start_time));
+  start_time.set_sample_rate(sample_rate);
+  stop_time.set_sample_rate(sample_rate);
+  int64_t nsamples = stop_time.diff_samples(start_time);
+  t->get_delays(start_time, nsamples, list);
+
+  FILE *f = std::fopen(outfile, "w");
+  for (size_t i = 0; i < list.size(); i++)
+    std::fprintf(f, "%lld %d %d\n", (long long)list[i].time.get_clock_ticks(), list[i].bytes,
+                 list[i].remaining_samples);
+  // Also record spline evaluations at requested probe times (delay, rate, phase, amplitude).
+  int np = count_key(kv, "probe");
+  for (int i = 0; i < np; i++) {
+    Time pt = ticks_time(getll(kv, idx("probe", i)));
+    std::fprintf(f, "P %lld %.17g %.17g %.17g %.17g\n", (long long)pt.get_clock_ticks(),
+                 t->akima_delays.delay(pt), t->akima_delays.rate(pt), t->akima_delays.phase(pt),
+                 t->akima_delays.amplitude(pt));
+  }
+  std::fclose(f);
+  return 0;
+}
+
+// -------------------------------------------------------------- protocol ---
+// Input_node_data_writer over in-memory channel blocks.
+//   sample_rate, bits_per_sample, integr_time_us, station_number
+//   blockfile <path> ; blocks "block#k start_ticks offset size [inv_begin n]..."
+//   delays <path to delay list from mode_delays>
+//   slice#k start_ticks stop_ticks nr_samples
+static int mode_protocol(const Kv &kv, const char *outfile) {
+  Input_node_parameters param;
+  int sample_rate = geti(kv, "sample_rate");
+  int bps = geti(kv, "bits_per_sample");
+  param.integr_time = Time((double)geti(kv, "integr_time_us"));
+  param.phasecal_integr_time = Time();
+  Input_node_parameters::Channel_parameters ch;
+  ch.bits_per_sample = bps;
+  ch.sideband = 'U';
+  ch.polarisation = 'R';
+  ch.frequency_number = 0;
+  for (int b = 0; b < bps; b++) ch.tracks.push_back(b);
+  param.channels.push_back(ch);
+  param.track_bit_rate = sample_rate;  // sample_rate() = track_bit_rate * subsamples_per_sample
+  param.n_tracks = bps;
+  param.frame_size = -1;
+  if (param.sample_rate() != sample_rate || param.bits_per_sample() != bps)
+    die("Input_node_parameters accessors disagree with the job");
+
+  Input_node_data_writer &w = *new Input_node_data_writer();
+  Input_node_data_writer::Input_buffer_ptr q(new Input_node_data_writer::Input_buffer());
+  w.connect_to(q);
+  w.set_parameters(0, param, geti(kv, "station_number"));
+
+  std::vector<char> data = read_file(get(kv, "blockfile")[0]);
+  // Pools are leaked on purpose: the reference pools assert at destruction
+  // that every element came back, and the writer still holds some at exit.
+  Input_node_types::Data_memory_pool &pool = *new Input_node_types::Data_memory_pool(count_key(kv, "block") + 4);
+  int nb = count_key(kv, "block");
+  for (int b = 0; b < nb; b++) {
+    const std::vector<std::string> &v = get(kv, idx("block", b));
+    Input_node_types::Channel_buffer_element e;
+    e.start_time = ticks_time(std::atoll(v[0].c_str()));
+    size_t off = std::atoll(v[1].c_str()), size = std::atoll(v[2].c_str());
+    e.channel_data = pool.allocate();
+    e.channel_data.data().data.assign(data.begin() + off, data.begin() + off + size);
+    for (size_t k = 3; k + 1 < v.size(); k += 2) {
+      Input_node_types::Invalid_block ib;
+      ib.invalid_begin = std::atoi(v[k].c_str());
+      ib.nr_invalid = std::atoi(v[k + 1].c_str());
+      e.invalid.push_back(ib);
+    }
+    q->push(e);
+  }
+
+  Delay_memory_pool &dpool = *new Delay_memory_pool(count_key(kv, "slice") + 2);
+  std::vector<boost::shared_ptr<Memory_writer> > writers;
+  int ns = count_key(kv, "slice");
+  for (int s = 0; s < ns; s++) {
+    const std::vector<std::string> &v = get(kv, idx("slice", s));
+    Time start = ticks_time(std::atoll(v[0].c_str())), stop = ticks_time(std::atoll(v[1].c_str()));
+    // Delay list for this slice: "dlist#s" file from mode_delays
+    std::ifstream din(get(kv, idx("dlist", s))[0].c_str());
+    Delay_memory_pool_element de = dpool.allocate();
+    de.data().resize(0);
+    std::string line;
+    while (std::getline(din, line)) {
+      if (line.empty() || line[0] == 'P') continue;
+      std::istringstream ss(line);
+      long long tk;
+      Delay d;
+      ss >> tk >> d.bytes >> d.remaining_samples;
+      d.time = ticks_time(tk);
+      d.time.set_sample_rate(sample_rate);
+      de.data().push_back(d);
+    }
+    start.set_sample_rate(sample_rate);
+    stop.set_sample_rate(sample_rate);
+    w.add_delay(de);
+    w.add_time_interval(start, stop);
+    boost::shared_ptr<Memory_writer> mw(new Memory_writer());
+    writers.push_back(mw);
+    w.add_timeslice(mw, std::atoll(v[2].c_str()));
+  }
+  int guard = 0;
+  while (w.has_work()) {
+    w.do_task();
+    if (++guard > 100000000) die("protocol writer did not terminate");
+  }
+  std::vector<char> all;
+  FILE *f = std::fopen(outfile, "wb");
+  for (size_t s = 0; s < writers.size(); s++) {
+    uint64_t n = writers[s]->bytes.size();
+    std::fwrite(&n, 8, 1, f);
+    if (n) std::fwrite(&writers[s]->bytes[0], 1, n, f);
+  }
+  std::fclose(f);
+  return 0;
+}
+
+// --------------------------------------------------------------- extract ---
+//   word_bytes N, bits_per_sample, nsamples, infile, subband#k track...
+static int mode_extract(const Kv &kv, const char *outfile) {
+  int N = geti(kv, "word_bytes");
+  int bps = geti(kv, "bits_per_sample");
+  int nsamples = geti(kv, "nsamples");
+  std::vector<char> in = read_file(get(kv, "infile")[0]);
+  std::vector<std::vector<int> > tracks;
+  int nsub = count_key(kv, "subband");
+  for (int s = 0; s < nsub; s++) {
+    const std::vector<std::string> &v = get(kv, idx("subband", s));
+    std::vector<int> t;
+    for (size_t k = 0; k < v.size(); k++) t.push_back(std::atoi(v[k].c_str()));
+    tracks.push_back(t);
+  }
+  int fan_out = tracks[0].size();
+  if ((int)in.size() < nsamples * N) die("extract input too short");
+  Channel_extractor_5 ex;
+  ex.initialise(tracks, N, nsamples, bps);
+  std::vector<std::vector<unsigned char> > out(nsub, std::vector<unsigned char>(nsamples * fan_out / 8 + 8));
+  std::vector<unsigned char *> ptrs(nsub);
+  for (int s = 0; s < nsub; s++) ptrs[s] = &out[s][0];
+  ex.extract((unsigned char *)&in[0], &ptrs[0]);
+  FILE *f = std::fopen(outfile, "wb");
+  for (int s = 0; s < nsub; s++) std::fwrite(&out[s][0], 1, nsamples * fan_out / 8, f);
+  std::fclose(f);
+  return 0;
+}
+
+// ------------------------------------------------------------- correlate ---
+struct Stream_chain {
+  bit_statistics_ptr stats;
+  Correlator_node_types::Channel_circular_input_buffer *ring;
+  Bit2float_worker_sptr b2f;
+  Correlator_node_types::Channel_queue_ptr b2f_to_dc;  // harness tap between the stages
+  boost::shared_ptr<Delay_correction> dc;
+  Delay_correction::Output_buffer_ptr dc_to_core;
+  std::vector<char> protocol;
+  size_t protocol_pos;
+  std::vector<float> unpacked;          // all bit2float output of the current integration
+  std::vector<std::complex<float> > rows;  // all Delay_correction rows (stride M+4)
+};
+
+static void push_bytes(Correlator_node_types::Channel_circular_input_buffer *r, const char *p, size_t n) {
+  if (n > r->bytes_free()) die("protocol larger than the correlator-node ring buffer");
+  for (size_t i = 0; i < n; i++) r->data[(r->write + i) % r->size] = p[i];
+  r->write += n;
+}
+
+static int mode_correlate(const Kv &kv, const char *outdir) {
+  const int nstreams = count_key(kv, "stream");
+  const int nstations = count_key(kv, "delfile");
+  const bool dump = has(kv, "dump") && geti(kv, "dump") != 0;
+  const int n_int = geti(kv, "n_integrations");
+  const int M = geti(kv, "fft_size_correlation");
+
+  std::vector<Delay_table> tables;
+  for (int s = 0; s < nstations; s++) tables.push_back(load_delay_table(kv, s));
+
+  Correlation_parameters p;
+  p.experiment_start = ticks_time(getll(kv, "experiment_start_ticks"));
+  p.integration_time = Time((double)getll(kv, "integration_time_us"));
+  p.sub_integration_time = Time((double)getll(kv, "sub_integration_time_us"));
+  p.number_channels = geti(kv, "number_channels");
+  p.fft_size_delaycor = geti(kv, "fft_size_delaycor");
+  p.fft_size_correlation = M;
+  p.slice_offset = 1;
+  p.sample_rate = geti(kv, "sample_rate");
+  p.channel_freq = getll(kv, "channel_freq");
+  p.bandwidth = geti(kv, "bandwidth");
+  p.sideband = get(kv, "sideband")[0][0];
+  p.frequency_nr = geti(kv, "frequency_nr");
+  p.polarisation = get(kv, "polarisation")[0][0];
+  p.cross_polarize = geti(kv, "cross_polarize") != 0;
+  p.reference_station = geti(kv, "reference_station");
+  p.window = geti(kv, "window");
+  std::memset(p.source, 0, sizeof(p.source));
+  std::strncpy(p.source, get(kv, "source")[0].c_str(), 10);
+  p.n_phase_centers = 1;
+  p.pulsar_binning = has(kv, "pulsar") ? 1 : 0;
+  p.pulsar_parameters = 0;
+  p.mask_parameters = 0;
+  std::vector<int> stream_station_index;  // delay table per stream
+  for (int i = 0; i < nstreams; i++) {
+    const std::vector<std::string> &v = get(kv, idx("stream", i));
+    // station_number station_stream sample_rate channel_freq bandwidth sideband pol bps LO_offset tsys_freq table_index
+    Correlation_parameters::Station_parameters sp;
+    sp.station_number = std::atoi(v[0].c_str());
+    sp.station_stream = std::atoi(v[1].c_str());
+    sp.sample_rate = std::atoi(v[2].c_str());
+    sp.channel_freq = std::atoll(v[3].c_str());
+    sp.bandwidth = std::atoi(v[4].c_str());
+    sp.sideband = v[5][0];
+    sp.polarisation = v[6][0];
+    sp.bits_per_sample = std::atoi(v[7].c_str());
+    sp.LO_offset = std::strtod(v[8].c_str(), 0);
+    sp.tsys_freq = std::atoi(v[9].c_str());
+    stream_station_index.push_back(std::atoi(v[10].c_str()));
+    p.station_streams.push_back(sp);
+  }
+
+  Pulsar_parameters::Pulsar pulsar;
+  if (p.pulsar_binning) {
+    const std::vector<std::string> &v = get(kv, "pulsar");  // nbins gate_start gate_stop
+    std::memset(pulsar.name, 0, sizeof(pulsar.name));
+    std::strncpy(pulsar.name, p.source, 10);
+    pulsar.nbins = std::atoi(v[0].c_str());
+    pulsar.interval.start = std::strtod(v[1].c_str(), 0);
+    pulsar.interval.stop = std::strtod(v[2].c_str(), 0);
+    int npc = count_key(kv, "polyco");
+    for (int k = 0; k < npc; k++) {
+      // tmid DM ref_phase ref_freq obs_freq coef...
+      const std::vector<std::string> &c = get(kv, idx("polyco", k));
+      Pulsar_parameters::Polyco_params pp;
+      std::memset(&pp, 0, (char *)&pp.coef - (char *)&pp);
+      pp.tmid = std::strtod(c[0].c_str(), 0);
+      pp.DM = std::strtod(c[1].c_str(), 0);
+      pp.ref_phase = std::strtod(c[2].c_str(), 0);
+      pp.ref_freq = std::strtod(c[3].c_str(), 0);
+      pp.obs_freq = std::strtod(c[4].c_str(), 0);
+      for (size_t j = 5; j < c.size(); j++) pp.coef.push_back(std::strtod(c[j].c_str(), 0));
+      pp.n_coef = pp.coef.size();
+      pulsar.polyco_params.push_back(pp);
+    }
+  }
+
+  // Build the per-stream chains (Correlator_node::hook_added_data_reader).
+  int max_stream = 0;
+  for (int i = 0; i < nstreams; i++) max_stream = std::max(max_stream, (int)p.station_streams[i].station_stream);
+  std::vector<Stream_chain> chains(max_stream + 1);
+  boost::shared_ptr<Correlation_core> core_normal(new Correlation_core());
+  boost::shared_ptr<Correlation_core_pulsar> core_pulsar(new Correlation_core_pulsar());
+  Correlation_core *core = p.pulsar_binning ? (Correlation_core *)core_pulsar.get() : core_normal.get();
+  boost::shared_ptr<Memory_writer> out(new Memory_writer());
+  core->set_data_writer(out);
+  const size_t ring_size = has(kv, "ring_bytes") ? (size_t)getll(kv, "ring_bytes") : (size_t)37100000;
+  for (int i = 0; i < nstreams; i++) {
+    int s = p.station_streams[i].station_stream;
+    Stream_chain &c = chains[s];
+    c.stats = bit_statistics_ptr(new bit_statistics());
+    c.ring = new Correlator_node_types::Channel_circular_input_buffer(ring_size);
+    c.b2f = Bit2float_worker::new_sptr(s, c.stats);
+    c.b2f->connect_to(c.ring);
+    c.b2f_to_dc = Correlator_node_types::Channel_queue_ptr(new Correlator_node_types::Channel_queue());
+    c.dc = boost::shared_ptr<Delay_correction>(new Delay_correction(s));
+    c.dc->connect_to(c.b2f_to_dc);
+    c.dc_to_core = Delay_correction::Output_buffer_ptr(new Delay_correction::Output_buffer());
+    core->connect_to(s, c.stats, c.dc_to_core);
+    core->connect_to(s, c.b2f->get_invalid());
+    c.protocol = read_file(get(kv, idx("protocol", i))[0]);
+    c.protocol_pos = 0;
+  }
+
+  std::string od(outdir);
+  FILE *tsys_f = std::fopen((od + "/tsys.bin").c_str(), "wb");
+  FILE *stats_f = std::fopen((od + "/stats.txt").c_str(), "w");
+  for (int it = 0; it < n_int; it++) {
+    p.integration_nr = geti(kv, "integration_nr") + it;
+    p.slice_nr = p.integration_nr;
+    p.start_time = ticks_time(getll(kv, "start_ticks") + (long long)it * p.integration_time.get_clock_ticks());
+    p.stop_time = p.start_time + p.integration_time;
+    for (int i = 0; i < nstreams; i++) {
+      p.station_streams[i].start_time = p.start_time;
+      p.station_streams[i].stop_time = p.stop_time;
+    }
+    // Correlator_node::set_parameters (sfxc/src/correlator_node.cc:311-406)
+    std::vector<Delay_table_akima> akima(max_stream + 1);
+    std::vector<std::vector<double> > uvw(max_stream + 1, std::vector<double>(3, 0.0));
+    for (int i = 0; i < nstreams; i++) {
+      int s = p.station_streams[i].station_stream;
+      akima[s] = tables[stream_station_index[i]].create_akima_spline(p.start_time, p.integration_time);
+    }
+    if (p.pulsar_binning)
+      core_pulsar->set_parameters(p, pulsar, akima, uvw, 0);
+    else
+      core_normal->set_parameters(p, akima, uvw, 0);
+    for (int i = 0; i < nstreams; i++) {
+      int s = p.station_streams[i].station_stream;
+      chains[s].dc->set_parameters(p, akima[s]);
+      chains[s].b2f->set_new_parameters(p, akima[s]);
+      chains[s].unpacked.clear();
+      chains[s].rows.clear();
+    }
+    // Feed this integration's protocol (length-prefixed per integration).
+    for (int i = 0; i < nstreams; i++) {
+      int s = p.station_streams[i].station_stream;
+      Stream_chain &c = chains[s];
+      if (c.protocol_pos + 8 > c.protocol.size()) die("protocol file exhausted");
+      uint64_t n;
+      std::memcpy(&n, &c.protocol[c.protocol_pos], 8);
+      c.protocol_pos += 8;
+      push_bytes(c.ring, &c.protocol[c.protocol_pos], n);
+      c.protocol_pos += n;
+    }
+    // Poll like the bit2float thread + main thread (single-threaded).
+    long guard = 0;
+    while (!core->finished()) {
+      bool work = false;
+      for (int i = 0; i < nstreams; i++) {
+        Stream_chain &c = chains[p.station_streams[i].station_stream];
+        while (c.b2f->has_work()) {
+          c.b2f->do_task();
+          work = true;
+        }
+        // Tap: copy bit2float output, then hand the element to Delay_correction.
+        Correlator_node_types::Channel_queue_ptr src = c.b2f->get_output_buffer();
+        while (!src->empty()) {
+          Correlator_node_types::Channel_memory_pool_element e = src->front_and_pop();
+          if (dump) c.unpacked.insert(c.unpacked.end(), &e.data().data[0], &e.data().data[0] + e.data().data.size());
+          c.b2f_to_dc->push(e);
+        }
+        while (c.dc->has_work()) {
+          c.dc->do_task();
+          work = true;
+        }
+        Delay_correction::Output_buffer_ptr dsrc = c.dc->get_output_buffer();
+        while (!dsrc->empty()) {
+          Delay_correction::Output_buffer_element e = dsrc->front_and_pop();
+          if (dump) c.rows.insert(c.rows.end(), &e->data[0], &e->data[0] + e->data.size());
+          c.dc_to_core->push(e);
+        }
+      }
+      while (core->has_work() && !core->finished()) {
+        core->do_task();
+        work = true;
+      }
+      if (!work && ++guard > 1000) die("pipeline stalled (protocol shorter than the integration?)");
+    }
+    // Statistics as the core saw them at integration end.
+    for (int i = 0; i < nstreams; i++) {
+      Stream_chain &c = chains[p.station_streams[i].station_stream];
+      int *lv = c.stats->get_statistics();
+      int *ts = c.stats->get_tsys();
+      std::fprintf(stats_f, "%d %d %d %d %d %d %d %d %d %d %d\n", it, lv[0], lv[1], lv[2], lv[3], lv[4],
+                   ts[0], ts[1], ts[2], ts[3], (int)c.b2f->get_invalid()->size());
+      std::vector<Bit2float_worker::Invalid> *inv = c.b2f->get_invalid();
+      for (size_t k = 0; k < inv->size(); k++)
+        std::fprintf(stats_f, "I %d %d %d\n", i, (*inv)[k].start, (*inv)[k].n_invalid);
+      if (dump) {
+        std::ostringstream a, b;
+        a << od << "/unpacked_i" << it << "_s" << i << ".f32";
+        b << od << "/rows_i" << it << "_s" << i << ".c64";
+        write_file(a.str(), c.unpacked.empty() ? 0 : &c.unpacked[0], c.unpacked.size() * 4);
+        write_file(b.str(), c.rows.empty() ? 0 : &c.rows[0], c.rows.size() * 8);
+      }
+    }
+    for (size_t m = 0; m < g_shim_messages.size(); m++)
+      std::fwrite(&g_shim_messages[m].bytes[0], 1, g_shim_messages[m].bytes.size(), tsys_f);
+    g_shim_messages.clear();
+  }
+  std::fclose(tsys_f);
+  std::fclose(stats_f);
+  write_file(od + "/out.cor", out->bytes.empty() ? 0 : &out->bytes[0], out->bytes.size());
+  return 0;
+}
+
+int main(int argc, char **argv) {
+  if (argc != 4) die("usage: ref_harness correlate|delays|protocol|extract <job> <out>");
+  Kv kv = read_job(argv[2]);
+  std::string m(argv[1]);
+  if (m == "correlate") return mode_correlate(kv, argv[3]);
+  if (m == "delays") return mode_delays(kv, argv[3]);
+  if (m == "protocol") return mode_protocol(kv, argv[3]);
+  if (m == "extract") return mode_extract(kv, argv[3]);
+  die("unknown mode " + m);
+  return 2;
+}

@@ -1,0 +1,266 @@
+"""Seeded synthetic VLBI station data: delay tables, quantised samples, VDIF frames.
+
+The reference ships no station recordings, so every workload is generated.
+Signal model (one subband, one polarisation):
+
+    x_i(t) = g_i * [ sqrt(rho) * Re{ a(T) exp(-2 pi i f_lo tau_i(T)) } + sqrt(1-rho) * n_i(t) ]
+
+where a is the analytic signal of a white band-limited Gaussian sky signal s,
+T solves T + tau_i(T) = t (the station sees the wavefront tau_i later), n_i is
+independent white noise, and f_lo is the subband's sky frequency at baseband
+zero.  Correlating x_i at t = T + tau_i(T) -- which is what the correlator's
+integer shift plus fractional-delay / fringe-rotation do with the delay table
+written here -- recovers the common signal with a stationary phase.
+
+Samples are quantised like a VLBI digitiser: 2-bit offset-binary codes at
+thresholds {-0.98 sigma, 0, +0.98 sigma} (codes 0..3 map to -7,-2,+2,+7 in the
+reference's unpack tables, sfxc/src/bit2float_worker.cc:4-10), or 1-bit sign
+codes.
+"""
+from __future__ import annotations
+
+import math
+import struct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import timebase
+
+THRESH_2BIT = 0.98
+
+
+# --------------------------------------------------------------------------
+# delay tables (.del files; layout of sfxc/utils/delay/generate_delay_model_calc.c:440-467,636-642,
+# read by Delay_table::open, sfxc/src/delay_table_akima.cc:238-372)
+# --------------------------------------------------------------------------
+@dataclass
+class DelayPoly:
+    """tau(t) = sum_k c[k] * (t - t0)^k seconds, t in seconds of day; phase and amplitude columns."""
+    coeffs: tuple = (0.0,)
+    t0: float = 0.0
+    phase_coeffs: tuple = (0.0,)
+    amp: float = 1.0
+
+    def delay(self, sec_of_day):
+        x = np.asarray(sec_of_day, dtype=np.float64) - self.t0
+        r = np.zeros_like(x)
+        for c in reversed(self.coeffs):
+            r = r * x + c
+        return r
+
+    def phase(self, sec_of_day):
+        x = np.asarray(sec_of_day, dtype=np.float64) - self.t0
+        r = np.zeros_like(x)
+        for c in reversed(self.phase_coeffs):
+            r = r * x + c
+        return r
+
+
+def del_file_bytes(station: str, scans) -> bytes:
+    """scans: list of (source, mjd, sec_start, n_rows, DelayPoly) with 1-s row spacing."""
+    out = bytearray()
+    name = station.encode()[:2].ljust(2, b"\0") + b"\0"
+    out += struct.pack("<i", 3) + name
+    for source, mjd, sec_start, n_rows, poly in scans:
+        src = source.encode()[:80].ljust(80, b" ") + b"\0"
+        out += src + struct.pack("<i", mjd)
+        for k in range(n_rows):
+            sec = float(sec_start + k)
+            d = float(poly.delay(sec))
+            ph = float(poly.phase(sec))
+            out += struct.pack("<7d", sec, 0.0, 0.0, 0.0, d, ph, poly.amp)
+        out += struct.pack("<7d", *([0.0] * 7))
+    return bytes(out)
+
+
+# --------------------------------------------------------------------------
+# signal generation
+# --------------------------------------------------------------------------
+@dataclass
+class StationSignal:
+    poly: DelayPoly
+    gain: float = 1.0
+    sideband: str = "U"
+
+
+@dataclass
+class SubbandSignal:
+    """Synthesis parameters shared by all stations of one subband/polarisation."""
+    sample_rate: int
+    f_lo: float                 # sky frequency of baseband zero (Hz)
+    rho: float = 0.01           # correlated power fraction
+    seed: int = 0
+    tones: list = field(default_factory=list)   # [(baseband_freq_hz, amplitude_in_sigma)], common RFI
+
+
+def _inverse_delay_time(t_abs, poly: DelayPoly, mjd_sec_offset: float):
+    """Solve T + tau(T) = t (seconds of day) by fixed-point iteration."""
+    T = t_abs - poly.delay(t_abs)
+    for _ in range(4):
+        T = t_abs - poly.delay(T)
+    return T
+
+
+def generate_station_samples(sub: SubbandSignal, stations: list, start_sec_of_day: float,
+                             n_samples: int, block: int = 8192, pad: int = 512):
+    """Real-valued station signals x_i(t) (float32 arrays, unit-ish variance).
+
+    start_sec_of_day: time of sample 0 (identical for all stations: the
+    recording start).  The common sky signal is drawn on a grid wide enough to
+    cover every station's shift.
+    """
+    sr = sub.sample_rate
+    rng = np.random.Generator(np.random.PCG64(sub.seed))
+    t_samples = start_sec_of_day + np.arange(n_samples, dtype=np.float64) / sr
+    # total shift range (samples) to size the sky-signal grid
+    max_tau = max(float(np.max(np.abs(st.poly.delay(t_samples[[0, -1]])))) for st in stations)
+    margin = int(max_tau * sr) + 4 * pad + block
+    n_sky = n_samples + 2 * margin
+    sky = rng.standard_normal(n_sky).astype(np.float64)
+    sky0 = margin  # sky index of T = start_sec_of_day
+    out = []
+    for si, st in enumerate(stations):
+        nrng = np.random.Generator(np.random.PCG64(sub.seed * 1000 + 17 + si))
+        x = np.empty(n_samples, dtype=np.float64)
+        for b0 in range(0, n_samples, block):
+            b1 = min(n_samples, b0 + block)
+            t = t_samples[b0:b1]
+            T = _inverse_delay_time(t, st.poly, 0.0)
+            # sample position of T on the sky grid (fractional)
+            pos = (T - start_sec_of_day) * sr + sky0
+            centre = 0.5 * (pos[0] + pos[-1])
+            shift = centre - (b0 + (b1 - b0 - 1) * 0.5 + sky0)
+            ishift = int(math.floor(shift))
+            frac = shift - ishift
+            lo = b0 + sky0 + ishift - pad
+            seg = sky[lo:lo + (b1 - b0) + 2 * pad]
+            L = seg.size
+            F = np.fft.rfft(seg)
+            f = np.arange(F.size) / L
+            # analytic signal of the segment, advanced by frac samples
+            A = np.zeros(L, dtype=np.complex128)
+            A[:F.size] = F * 2.0
+            A[0] = F[0]
+            if L % 2 == 0:
+                A[L // 2] = F[L // 2]
+            A[:F.size] *= np.exp(2j * np.pi * f * frac)
+            a = np.fft.ifft(A)[pad:pad + (b1 - b0)]
+            # small residual drift of the shift across the block: linear correction
+            resid = pos - (np.arange(b0, b1) + sky0 + shift)
+            # derivative approximation of a for the residual (first order)
+            da = np.gradient(a)
+            a = a + da * resid
+            phase = -2.0 * np.pi * sub.f_lo * st.poly.delay(T)
+            sig = np.real(a * np.exp(1j * phase))
+            noise = nrng.standard_normal(b1 - b0)
+            xs = math.sqrt(sub.rho) * sig + math.sqrt(1.0 - sub.rho) * noise
+            for (ftone, amp) in sub.tones:
+                xs = xs + amp * np.cos(2 * np.pi * ftone * (t - start_sec_of_day))
+            x[b0:b1] = st.gain * xs
+        out.append(x.astype(np.float32))
+    return out
+
+
+def quantise(x: np.ndarray, bits: int) -> np.ndarray:
+    """Digitiser codes (uint8): 2-bit offset binary at +-0.98 sigma, or 1-bit sign."""
+    sigma = float(np.std(x.astype(np.float64)))
+    if bits == 2:
+        t = THRESH_2BIT * sigma
+        return (np.digitize(x, [-t, 0.0, t])).astype(np.uint8)
+    if bits == 1:
+        return (x >= 0).astype(np.uint8)
+    raise ValueError("bits must be 1 or 2")
+
+
+def pack_codes(codes: np.ndarray, bits: int) -> np.ndarray:
+    """Channel stream bytes: samples packed LSB-first (first sample in the lowest bits)."""
+    spb = 8 // bits
+    n = codes.size - codes.size % spb
+    c = codes[:n].astype(np.uint8).reshape(-1, spb)
+    out = np.zeros(c.shape[0], dtype=np.uint8)
+    for k in range(spb):
+        out |= (c[:, k] << (k * bits)).astype(np.uint8)
+    return out
+
+
+def unpack_codes(stream: np.ndarray, bits: int) -> np.ndarray:
+    spb = 8 // bits
+    mask = (1 << bits) - 1
+    s = np.asarray(stream, dtype=np.uint8)
+    return np.stack([(s >> (k * bits)) & mask for k in range(spb)], axis=1).reshape(-1)
+
+
+# --------------------------------------------------------------------------
+# VDIF framing (sfxc/include/vdif_reader.h:36-61)
+# --------------------------------------------------------------------------
+VDIF_HEADER_BYTES = 32
+
+
+def vdif_ref_epoch(mjd: int) -> tuple:
+    """(ref_epoch, mjd of that epoch): half-years since 2000 containing mjd."""
+    best = (0, timebase.mjd_from_date(1, 1, 2000))
+    for e in range(0, 64):
+        y = 2000 + e // 2
+        m = 1 + 6 * (e % 2)
+        em = timebase.mjd_from_date(1, m, y)
+        if em <= mjd:
+            best = (e, em)
+    return best
+
+
+def vdif_header(sec_from_epoch: int, frame_in_second: int, ref_epoch: int, frame_bytes: int,
+                log2_nchan: int, bits: int, thread_id: int = 0, station_id: int = 0,
+                invalid: bool = False) -> bytes:
+    w0 = (sec_from_epoch & 0x3FFFFFFF) | ((1 if invalid else 0) << 31)
+    w1 = (frame_in_second & 0xFFFFFF) | ((ref_epoch & 0x3F) << 24)
+    w2 = ((frame_bytes // 8) & 0xFFFFFF) | ((log2_nchan & 0x1F) << 24)
+    w3 = (station_id & 0xFFFF) | ((thread_id & 0x3FF) << 16) | (((bits - 1) & 0x1F) << 26)
+    return struct.pack("<8I", w0, w1, w2, w3, 0, 0, 0, 0)
+
+
+def vdif_words_from_codes(chan_codes: list, bits: int) -> np.ndarray:
+    """Interleave per-channel codes into 32-bit VDIF words.
+
+    With C channels of b bits, a word carries 32/(C*b) samples of every
+    channel; sample k of channel c sits at bit ((k*C)+c)*b.
+    """
+    C = len(chan_codes)
+    per_word = 32 // (C * bits)
+    if per_word < 1:
+        raise ValueError("more bits per sample period than one word")
+    n = min(c.size for c in chan_codes)
+    n -= n % per_word
+    words = np.zeros(n // per_word, dtype=np.uint32)
+    for c in range(C):
+        cc = chan_codes[c][:n].astype(np.uint32).reshape(-1, per_word)
+        for k in range(per_word):
+            words |= cc[:, k] << np.uint32(((k * C) + c) * bits)
+    return words
+
+
+def vdif_file_bytes(words: np.ndarray, *, payload_bytes: int, sample_rate: int, nchan: int, bits: int,
+                    start_mjd: int, start_sec_of_day: int, invalid_frames=(), thread_id=0,
+                    station_id=0) -> bytes:
+    """Frame a word stream into VDIF frames (32-B header + payload).
+
+    Sample 0 must fall on an integer second (start_sec_of_day) so that frame
+    numbers restart at 0 each second.
+    """
+    ref_epoch, epoch_mjd = vdif_ref_epoch(start_mjd)
+    words_per_frame = payload_bytes // 4
+    samples_per_frame = payload_bytes * 8 // (bits * nchan)
+    frames_per_second = sample_rate // samples_per_frame
+    nframes = words.size // words_per_frame
+    log2_nchan = int(round(math.log2(nchan)))
+    inv = set(invalid_frames)
+    payload = words[: nframes * words_per_frame].reshape(nframes, words_per_frame)
+    out = bytearray()
+    sec0 = (start_mjd - epoch_mjd) * 86400 + start_sec_of_day
+    for f in range(nframes):
+        sec = sec0 + f // frames_per_second
+        fn = f % frames_per_second
+        out += vdif_header(sec, fn, ref_epoch, payload_bytes + VDIF_HEADER_BYTES, log2_nchan, bits,
+                           thread_id, station_id, f in inv)
+        out += payload[f].tobytes()
+    return bytes(out)
