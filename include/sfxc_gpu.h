@@ -1,0 +1,205 @@
+/*
+ * sfxc_gpu.h -- C ABI of the GB300 correlator-node path.
+ *
+ * Drop-in boundary for the reference's in-process correlator-node task
+ * interface (paths relative to the reference project):
+ *
+ *   Correlator_node::set_parameters / receive_parameters
+ *       sfxc/src/correlator_node.cc:298-406            -> sfxc_gpu_set_parameters
+ *   Correlator_node_data_reader_tasklet -> Channel_circular_input_buffer
+ *       sfxc/src/correlator_node_data_reader_tasklet.cc:28-109,
+ *       sfxc/include/correlator_node_types.h:14-31     -> sfxc_gpu_push_protocol
+ *   Bit2float_worker + Delay_correction + Correlation_core(_pulsar)::do_task
+ *   until finished(), integration_write via Data_writer::put_bytes, tsys_write
+ *       sfxc/src/correlator_node.cc:263-296, sfxc/include/delay_correction.h:39-55,
+ *       sfxc/include/correlation_core.h:27-59,
+ *       sfxc/include/correlation_core_pulsar.h:10-16,
+ *       sfxc/include/data_writer.h:28                  -> sfxc_gpu_run_integration
+ *   Input_node_tasklet::get_delay / get_delays (add_time_interval)
+ *       sfxc/src/input_node_tasklet.cc:103-128,235-282 -> sfxc_gpu_delay_list
+ *   Input_node_data_writer::do_task (byte protocol to the correlator node)
+ *       sfxc/src/input_node_data_writer.cc:107-229,389-500 -> sfxc_gpu_write_protocol
+ *   Channel_extractor_5::extract (bit gather into per-subband streams)
+ *       sfxc/src/channel_extractor_5.cc:27-99          -> sfxc_gpu_extract_channels
+ *
+ * Conventions: plain pointers and sizes; every call returns 0 or a negative
+ * status (SFXC_GPU_E*), with a message from sfxc_gpu_last_error().  Input
+ * buffers belong to the caller and are not referenced after a call returns.
+ * One host thread drives one context; a context owns one CUDA stream on one
+ * device.  The library has no CPU fallback: without a usable GPU,
+ * sfxc_gpu_create fails.
+ */
+#ifndef SFXC_GPU_H
+#define SFXC_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SFXC_GPU_OK 0
+#define SFXC_GPU_EINVAL (-1)   /* bad parameters */
+#define SFXC_GPU_EDELTAB (-2)  /* malformed delay table */
+#define SFXC_GPU_EDELAY (-3)   /* delay model does not cover the request */
+#define SFXC_GPU_EPROTO (-4)   /* malformed input protocol */
+#define SFXC_GPU_ESTREAM (-5)  /* input ended before the integration was complete */
+#define SFXC_GPU_ESTATE (-6)   /* call out of order */
+#define SFXC_GPU_ECUDA (-10)   /* CUDA runtime error */
+
+/* X-step arithmetic */
+#define SFXC_GPU_X_FP32 0      /* FP32 spectra, FP32 CUDA-core multiply-accumulate */
+#define SFXC_GPU_X_TC_HILO 1   /* FP16 hi+lo spectra, tensor-core products, FP32 accumulation */
+
+typedef struct sfxc_gpu_ctx sfxc_gpu_ctx;
+
+typedef struct {
+  int32_t device; /* CUDA device ordinal */
+  int32_t x_mode; /* SFXC_GPU_X_* */
+} sfxc_gpu_config;
+
+/* Correlation_parameters::Station_parameters (sfxc/include/control_parameters.h:125-142) */
+typedef struct {
+  int32_t station_number;
+  int32_t station_stream;
+  int32_t sample_rate;
+  int32_t bandwidth;
+  int32_t bits_per_sample;
+  int32_t tsys_freq;
+  int64_t channel_freq;
+  char sideband;     /* 'U' or 'L' */
+  char polarisation; /* 'R' or 'L' */
+  char pad_[2];
+  int32_t delay_table; /* index into sfxc_correlation_params.delay_tables */
+  double lo_offset;
+} sfxc_station_stream;
+
+/* A station delay table: the bytes of its .del file (layout of
+ * sfxc/utils/delay/generate_delay_model_calc.c:440-467) and the clock model of
+ * Delay_table::set_clock_offset (sfxc/src/delay_table_akima.cc:221-229). */
+typedef struct {
+  const uint8_t *del_bytes;
+  size_t del_size;
+  double clock_offset;
+  double clock_rate;
+  int64_t clock_epoch_ticks;
+} sfxc_delay_table;
+
+/* Pulsar_parameters::Polyco_params (sfxc/include/control_parameters.h:74-90) */
+typedef struct {
+  double tmid, dm, ref_phase, ref_freq, obs_freq;
+  int32_t n_coef;
+  const double *coef;
+} sfxc_polyco;
+
+/* Correlation_parameters (sfxc/include/control_parameters.h:117-182).  Times
+ * are clock ticks at 512 MHz since MJD 51544 (the reference's Time). */
+typedef struct {
+  int64_t experiment_start_ticks;
+  int64_t start_ticks;             /* start of the first integration */
+  int64_t integration_time_us;
+  int64_t sub_integration_time_us;
+  int32_t number_channels;
+  int32_t fft_size_delaycor;
+  int32_t fft_size_correlation;
+  int32_t sample_rate;
+  int32_t bandwidth;
+  int32_t frequency_nr;
+  int64_t channel_freq;
+  char sideband;
+  char polarisation;
+  char pad_[2];
+  int32_t cross_polarize;
+  int32_t reference_station;
+  int32_t window;                  /* SFXC_WINDOW_* ids of sfxc/include/utils.h */
+  int32_t integration_nr;
+  int32_t n_streams;
+  const sfxc_station_stream *streams;
+  int32_t n_delay_tables;
+  const sfxc_delay_table *delay_tables;
+  /* pulsar binning (Correlation_core_pulsar); pulsar_nbins == 0 disables it */
+  int32_t pulsar_nbins;            /* Pulsar::nbins (one off-pulse bin is added) */
+  double gate_start, gate_stop;    /* Pulsar::interval */
+  int32_t n_polyco;
+  const sfxc_polyco *polyco;
+} sfxc_correlation_params;
+
+sfxc_gpu_ctx *sfxc_gpu_create(const sfxc_gpu_config *config);
+void sfxc_gpu_destroy(sfxc_gpu_ctx *ctx);
+const char *sfxc_gpu_last_error(const sfxc_gpu_ctx *ctx);
+/* Message of the last failed context-free call (create, delay list, protocol). */
+const char *sfxc_gpu_global_error(void);
+
+/* Set up a job (one subband, one or more integrations). */
+int sfxc_gpu_set_parameters(sfxc_gpu_ctx *ctx, const sfxc_correlation_params *params);
+
+/* Append correlator-node protocol bytes (HEADER_DATA/INVALID/DELAY/ENDSTREAM
+ * records, sfxc/include/utils.h:39-42) for stream index `stream` (position in
+ * params.streams): the bytes of the next integration. */
+int sfxc_gpu_push_protocol(sfxc_gpu_ctx *ctx, int32_t stream, const uint8_t *bytes, size_t n);
+
+/* Output sink, the Data_writer::put_bytes of the reference.  kind 0: bytes of
+ * the correlator output slice (file index, timeslice/uvw/statistics headers,
+ * baseline headers and visibilities, byte-identical layout to
+ * Correlation_core::integration_write); kind 1: one tsys record per stream
+ * (the packed message of Correlation_core::tsys_write).  Return 0 to go on. */
+typedef int (*sfxc_output_sink)(void *user, int32_t kind, const void *data, size_t n);
+
+/* Correlate the next integration of the job (all streams must have pushed). */
+int sfxc_gpu_run_integration(sfxc_gpu_ctx *ctx, sfxc_output_sink sink, void *user);
+
+/* Inspection of the last integration (for verification).  Copies stream
+ * `stream`'s unpacked samples (n_blocks * fft_size_delaycor floats, the
+ * output of Bit2float_worker) or its delay-corrected spectra (rows of
+ * fft_size_correlation + 1 complex values, the output of Delay_correction). */
+int sfxc_gpu_copy_unpacked(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
+int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
+/* Per-kernel device time (ms) of the last integration, CUDA events on the
+ * context's stream: [0] unpack+fringe, [1] windowed FFT, [2] X-step,
+ * [3] statistics+normalisation, [4] total. */
+int sfxc_gpu_last_timings(const sfxc_gpu_ctx *ctx, float *ms5);
+
+/* Integer delay list of one interval (Input_node_tasklet::add_time_interval):
+ * writes up to `capacity` entries (ticks, bytes, remaining samples) and
+ * returns the count (or a negative status). */
+int sfxc_gpu_delay_list(const sfxc_delay_table *table, int64_t start_ticks, int64_t stop_ticks, int32_t sample_rate,
+                        int32_t bits_per_sample, int64_t *ticks, int32_t *bytes, int32_t *remaining,
+                        int32_t capacity);
+
+/* Input-node byte protocol for consecutive slices of one channel.
+ * Channel blocks: start ticks, byte size and invalid runs (begin, n) of each
+ * block of the channel stream `stream` (blocks stored back to back).  Slices:
+ * start/stop ticks, sample count and delay list (as returned by
+ * sfxc_gpu_delay_list).  Output: slice k's bytes at out + out_offsets[k],
+ * length out_offsets[k+1] - out_offsets[k]; returns the total byte count, or
+ * the needed capacity as a negative-free count when out is NULL. */
+typedef struct {
+  int64_t start_ticks;
+  int32_t size;
+  int32_t n_invalid;
+  const int32_t *invalid; /* 2*n_invalid: begin, n */
+} sfxc_channel_block;
+typedef struct {
+  int64_t start_ticks, stop_ticks, nr_samples;
+  int32_t n_delays;
+  const int64_t *delay_ticks;
+  const int32_t *delay_bytes;
+  const int32_t *delay_remaining;
+} sfxc_slice;
+int64_t sfxc_gpu_write_protocol(const uint8_t *stream, int32_t n_blocks, const sfxc_channel_block *blocks,
+                                int32_t n_slices, const sfxc_slice *slices, int32_t sample_rate,
+                                int32_t bits_per_sample, int64_t integration_time_us, uint8_t *out,
+                                int64_t capacity, int64_t *out_offsets);
+
+/* Channel extraction on the GPU: `nwords` input words of `word_bytes` bytes
+ * (host memory); subband s takes tracks tracks[s*fan_out .. +fan_out) (bit
+ * positions within a word, first track = high bit of a sample code).  Writes
+ * nwords*fan_out/8 bytes per subband, back to back, into `out` (host). */
+int sfxc_gpu_extract_channels(sfxc_gpu_ctx *ctx, const uint8_t *words, int64_t nwords, int32_t word_bytes,
+                              int32_t bits_per_sample, int32_t n_subbands, int32_t fan_out, const int32_t *tracks,
+                              uint8_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

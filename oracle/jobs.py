@@ -177,4 +177,10 @@ def correlate(job, dump=False, impl="reference", precision=32):
                                                 dtype=np.complex64)
             res["unpacked"] = un
             res["rows"] = rows
+            bp = os.path.join(outdir, "bins_i0.i32")
+            if "pulsar" in job and os.path.exists(bp):
+                K = int(job["fft_size_correlation"]) + 1
+                res["bins"] = np.concatenate([
+                    np.fromfile(os.path.join(outdir, "bins_i%d.i32" % it), dtype=np.int32).reshape(-1, K)
+                    for it in range(int(job["n_integrations"]))])
         return res

@@ -536,6 +536,29 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
         write_file(b.str(), c.rows.empty() ? 0 : &c.rows[0], c.rows.size() * 8);
       }
     }
+    if (dump && p.pulsar_binning) {
+      // The reference's own bin table of this integration: dedisperse_buffer()
+      // recomputed per FFT after the integration (its scratch buffer is zero,
+      // so the accumulators are unchanged), plus its phase constants.
+      std::ostringstream a;
+      a << od << "/bins_i" << it << ".i32";
+      FILE *bf = std::fopen(a.str().c_str(), "wb");
+      const int nr = core_pulsar->number_ffts_in_integration;
+      for (int r = 0; r < nr; r++) {
+        core_pulsar->current_fft = r;
+        core_pulsar->dedisperse_buffer();
+        std::fwrite(&core_pulsar->bins[0], 4, core_pulsar->bins.size(), bf);
+      }
+      core_pulsar->current_fft = nr;
+      std::fclose(bf);
+      std::ostringstream b;
+      b << od << "/pulsar_i" << it << ".txt";
+      FILE *pf = std::fopen(b.str().c_str(), "w");
+      std::fprintf(pf, "%.17g %.17g %.17g\n", core_pulsar->start_phase, core_pulsar->fft_duration,
+                   p.start_time.get_mjd());
+      for (size_t q = 0; q < core_pulsar->offsets.size(); q++) std::fprintf(pf, "%.17g\n", core_pulsar->offsets[q]);
+      std::fclose(pf);
+    }
     for (size_t m = 0; m < g_shim_messages.size(); m++)
       std::fwrite(&g_shim_messages[m].bytes[0], 1, g_shim_messages[m].bytes.size(), tsys_f);
     g_shim_messages.clear();

@@ -1741,11 +1741,17 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
       double tmid = pc0[0], DM = pc0[1], ref_phase = pc0[2], ref_freq = pc0[3], obs_freq = pc0[4];
       int N = (int)pc0[5];
       const double *coef = pc0 + 6;
+      /* The reference is built with -O2 -ffast-math (sfxc/configure.ac:31); GCC
+         reassociates (start_mjd - tmid) + fft_duration/us_per_day into
+         (start_mjd + fft_duration/us_per_day) - tmid.  Start MJDs carry ~6e-7 s
+         of FP64 resolution, so the association moves the pulsar phase by up to
+         ~1e-5 cycles; the compiled reference's order is restated here (checked
+         against its own dumped start phase and bin table). */
       double DT;
       if (j.window == WINDOW_NONE)
-        DT = ((start_mjd - tmid) + fft_duration / (2 * us_per_day)) * 1440;
+        DT = ((start_mjd + fft_duration / (2 * us_per_day)) - tmid) * 1440;
       else
-        DT = ((start_mjd - tmid) + fft_duration / us_per_day) * 1440;
+        DT = ((start_mjd + fft_duration / us_per_day) - tmid) * 1440;
       double start_phase = 0;
       for (int q = N - 1; q > 0; q--) start_phase = (start_phase + coef[q]) * DT;
       start_phase += (ref_phase - floor(ref_phase)) + DT * 60 * ref_freq + coef[0];
@@ -1757,8 +1763,11 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
       for (int q = N - 1; q > 1; q--) freq = (freq + q * coef[q]) * DT;
       freq = (freq + coef[1]) / 60 + ref_freq;
       double *offsets = xmalloc(K * 8);
-      for (int q = 0; q < K; q++)
-        offsets[q] = 4148.808 * DM * (1 / pow(base_freq + q * dfreq, 2) - inv_freq_obs2) * freq;
+      /* same build: 4148.808*DM*(...)*freq is evaluated as (4148.808*DM)*((...)*freq) */
+      for (int q = 0; q < K; q++) {
+        const double x = base_freq + q * dfreq;
+        offsets[q] = (4148.808 * DM) * ((1 / (x * x) - inv_freq_obs2) * freq);
+      }
       double len = j.gate1 - j.gate0;
       int nbins = j.nbins;
       double *acc = xmalloc((size_t)nbins * nbl * K * 2 * sizeof(double));

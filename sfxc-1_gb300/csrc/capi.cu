@@ -1,0 +1,870 @@
+// C ABI of the correlator-node path (include/sfxc_gpu.h): job setup, per-
+// integration planning on the host, kernel launches on one CUDA stream, and
+// the byte layout of the correlator output (Correlation_core::integration_write,
+// sfxc/src/correlation_core.cc:316-477; headers sfxc/include/output_header.h:100-148).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "host.hpp"
+#include "kernels.hpp"
+#include "sfxc_gpu.h"
+
+using namespace sfxc;
+
+namespace {
+
+thread_local std::string g_error;
+
+struct CudaError : Error {
+  CudaError(cudaError_t e, const char *what)
+      : Error(SFXC_GPU_ECUDA, std::string(what) + ": " + cudaGetErrorString(e)) {}
+};
+#define CK(x)                                  \
+  do {                                         \
+    cudaError_t e_ = (x);                      \
+    if (e_ != cudaSuccess) throw CudaError(e_, #x); \
+  } while (0)
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  void *ensure(size_t n) {
+    if (n > cap) {
+      if (p) cudaFree(p);
+      p = nullptr;
+      cap = 0;
+      CK(cudaMalloc(&p, n));
+      cap = n;
+    }
+    return p;
+  }
+  template <class T>
+  T *as() const { return reinterpret_cast<T *>(p); }
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+struct StreamCtx {
+  std::vector<Record> recs;
+  StreamUnpackState ust;
+  std::vector<uint8_t> chunk;
+  bool pushed = false;
+  UnpackPlan plan;
+  BitStats stats{};
+  Spline sp;
+  int n_blocks = 0, nfft_max = 0, rot = 0, hop = 0;
+  DevBuf src, segs, stat_rng, spline, hist;
+};
+
+struct Polyco {
+  double tmid, dm, ref_phase, ref_freq, obs_freq;
+  std::vector<double> coef;
+};
+
+// Host-side per-launch tables uploaded once per job.
+struct JobTables {
+  std::vector<int> blmap, tiles, blpairs;
+  int npad = 0, ntiles = 0;
+};
+
+}  // namespace
+
+struct sfxc_gpu_ctx {
+  int device = 0, x_mode = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[6] = {};
+  float timings[5] = {};
+  std::string err;
+  bool have_job = false;
+  // job
+  sfxc_correlation_params p{};
+  std::vector<StationStream> streams;
+  std::vector<DelayTable> tables;
+  std::vector<int> stream_table;
+  std::vector<Polyco> polyco;
+  int current_integration = 0;
+  std::vector<StreamCtx> sc;
+  std::vector<Baseline> bl;
+  JobTables jt;
+  int M = 0, K = 0, Nd = 0, kpad = 0, nffts = 0, nsub = 0, nbins = 1;
+  // device
+  DevBuf streamdev, tw256, window, twrot, ts, spec, acc, out, norms, flagfac, blmap, tiles, blpairs, items, bins,
+      offsets;
+  int tw_rot_n = 0, window_n = 0, window_type = -1;
+  std::vector<StreamDev> hsd;
+};
+
+namespace {
+
+int fail(sfxc_gpu_ctx *c, const Error &e) {
+  if (c) c->err = e.msg;
+  g_error = e.msg;
+  return e.code;
+}
+
+void upload(DevBuf &b, const void *src, size_t n, cudaStream_t st) {
+  b.ensure(n ? n : 16);
+  if (n) CK(cudaMemcpyAsync(b.p, src, n, cudaMemcpyHostToDevice, st));
+}
+
+// Twiddle tables exp(-2 pi i m / n), computed in double and rounded once.
+void twiddles(std::vector<float2> &v, int n) {
+  for (int m = 0; m < n; m++) {
+    double a = -2.0 * M_PI * (double)m / (double)n;
+    v.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
+  }
+}
+
+// Delay_correction::create_window (sfxc/src/delay_correction.cc:300-341)
+std::vector<float> make_window(int type, int n) {
+  std::vector<float> w(n);
+  for (int i = 0; i < n; i++) {
+    double v = 0;
+    switch (type) {
+      case WINDOW_NONE: v = i < n / 2 ? 1 : 0; break;
+      case WINDOW_RECT: v = (i >= n / 4 && i < 3 * n / 4) ? 1 : 0; break;
+      case WINDOW_COS: v = std::sin(M_PI * i / (n - 1)); break;
+      case WINDOW_HAMMING: v = 0.54 - 0.46 * std::cos(2 * M_PI * i / (n - 1)); break;
+      case WINDOW_HANN: v = 0.5 * (1 - std::cos(2 * M_PI * i / (n - 1))); break;
+      default: throw Error(SFXC_GPU_EINVAL, "invalid window function");
+    }
+    w[i] = (float)v;
+  }
+  return w;
+}
+
+template <class T>
+void put(std::vector<uint8_t> &o, const T &v) {
+  const uint8_t *p = reinterpret_cast<const uint8_t *>(&v);
+  o.insert(o.end(), p, p + sizeof(T));
+}
+
+void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
+  if (!p || p->n_streams <= 0 || !p->streams) throw Error(SFXC_GPU_EINVAL, "no streams");
+  if (p->fft_size_delaycor != kNd) throw Error(SFXC_GPU_EINVAL, "fft_size_delaycor must be 256");
+  if (p->number_channels != p->fft_size_correlation)
+    throw Error(SFXC_GPU_EINVAL, "spectral reduction (number_channels != fft_size_correlation) is not supported");
+  if (p->fft_size_correlation < kNd || (p->fft_size_correlation & (p->fft_size_correlation - 1)))
+    throw Error(SFXC_GPU_EINVAL, "fft_size_correlation must be a power of two >= 256");
+  if (p->window < WINDOW_NONE || p->window > WINDOW_HANN) throw Error(SFXC_GPU_EINVAL, "invalid window");
+  if (p->n_delay_tables <= 0 || !p->delay_tables) throw Error(SFXC_GPU_EINVAL, "no delay tables");
+  c->p = *p;
+  c->p.streams = nullptr;
+  c->p.delay_tables = nullptr;
+  c->p.polyco = nullptr;
+  c->tables.clear();
+  for (int i = 0; i < p->n_delay_tables; i++) {
+    const sfxc_delay_table &t = p->delay_tables[i];
+    if (!t.del_bytes || t.del_size < 4) throw Error(SFXC_GPU_EDELTAB, "empty delay table");
+    DelayTable dt = DelayTable::parse(t.del_bytes, t.del_size);
+    dt.clock_offset = t.clock_offset;
+    dt.clock_rate = t.clock_rate;
+    dt.clock_epoch = t.clock_epoch_ticks;
+    c->tables.push_back(std::move(dt));
+  }
+  c->streams.clear();
+  c->stream_table.clear();
+  for (int i = 0; i < p->n_streams; i++) {
+    const sfxc_station_stream &s = p->streams[i];
+    if (s.bits_per_sample != 1 && s.bits_per_sample != 2) throw Error(SFXC_GPU_EINVAL, "bits_per_sample must be 1 or 2");
+    if (s.sample_rate <= 0 || s.bandwidth <= 0) throw Error(SFXC_GPU_EINVAL, "bad stream sample rate or bandwidth");
+    if (s.delay_table < 0 || s.delay_table >= p->n_delay_tables) throw Error(SFXC_GPU_EINVAL, "bad delay table index");
+    if (s.station_stream != i) throw Error(SFXC_GPU_EINVAL, "station_stream must equal the stream's position");
+    if (s.bits_per_sample == 2 && s.tsys_freq <= 0) throw Error(SFXC_GPU_EINVAL, "tsys_freq must be positive");
+    StationStream ss{s.station_number, s.station_stream, s.sample_rate, s.bandwidth, s.bits_per_sample, s.tsys_freq,
+                     s.channel_freq, s.sideband, s.polarisation, s.lo_offset};
+    c->streams.push_back(ss);
+    c->stream_table.push_back(s.delay_table);
+  }
+  c->polyco.clear();
+  c->nbins = 1;
+  if (p->pulsar_nbins > 0) {
+    if (p->n_polyco <= 0 || !p->polyco) throw Error(SFXC_GPU_EINVAL, "pulsar binning without polyco");
+    for (int i = 0; i < p->n_polyco; i++) {
+      const sfxc_polyco &q = p->polyco[i];
+      if (q.n_coef < 2 || !q.coef) throw Error(SFXC_GPU_EINVAL, "polyco needs at least two coefficients");
+      c->polyco.push_back(Polyco{q.tmid, q.dm, q.ref_phase, q.ref_freq, q.obs_freq,
+                                 std::vector<double>(q.coef, q.coef + q.n_coef)});
+    }
+    c->nbins = p->pulsar_nbins + 1;
+  }
+  c->M = p->fft_size_correlation;
+  c->K = c->M + 1;
+  c->Nd = p->fft_size_delaycor;
+  c->kpad = c->M + 4;
+  const int nr = nr_ffts_per_integration_slice((double)p->integration_time_us, p->sample_rate, c->M);
+  c->nffts = nr - (p->window != WINDOW_NONE ? 1 : 0);
+  c->nsub = nr_ffts_per_integration_slice((double)p->sub_integration_time_us, p->sample_rate, c->M);
+  if (c->nffts <= 0) throw Error(SFXC_GPU_EINVAL, "integration shorter than two FFTs");
+  c->sc.clear();
+  c->sc.resize(p->n_streams);
+  for (int i = 0; i < p->n_streams; i++) {
+    StreamCtx &s = c->sc[i];
+    const StationStream &ss = c->streams[i];
+    const int nfft_min = std::max(c->M / c->Nd, 1);
+    s.nfft_max = (int)(((uint64_t)std::max(kCorrelatorBufferSize / c->Nd, nfft_min) * (uint64_t)ss.sample_rate) /
+                       p->sample_rate);
+    s.n_blocks = (int)(((uint64_t)(c->M / c->Nd) * nr * (uint64_t)ss.sample_rate) / p->sample_rate);
+    s.rot = (int)(((uint64_t)2 * c->M * (uint64_t)ss.sample_rate) / p->sample_rate);
+    s.hop = s.rot / 2;
+    if (s.rot & (s.rot - 1)) throw Error(SFXC_GPU_EINVAL, "FFT length per stream must be a power of two");
+    if (s.rot > 16384) throw Error(SFXC_GPU_EINVAL, "FFT lengths above 16384 samples are not supported yet");
+    if (s.rot != 2 * c->M) throw Error(SFXC_GPU_EINVAL, "mixed sample rates within a job are not supported yet");
+  }
+  c->bl = create_baselines(c->streams, p->reference_station);
+  // stream-pair tiles of the X-step and the map pair -> baseline
+  JobTables &jt = c->jt;
+  const int N = p->n_streams;
+  jt.npad = (N + 3) / 4 * 4;
+  jt.blmap.assign((size_t)jt.npad * jt.npad, -1);
+  jt.blpairs.clear();
+  for (size_t b = 0; b < c->bl.size(); b++) {
+    const int a = c->bl[b].a, bb = c->bl[b].b;
+    const int i = std::min(a, bb), j = std::max(a, bb);
+    jt.blmap[(size_t)i * jt.npad + j] = (int)(b << 1) | (a > bb ? 1 : 0);
+    jt.blpairs.push_back(a);
+    jt.blpairs.push_back(bb);
+  }
+  jt.tiles.clear();
+  const int T4 = jt.npad / 4;
+  for (int I = 0; I < T4; I++)
+    for (int J = I; J < T4; J++) {
+      bool used = false;
+      for (int p_ = 0; p_ < 4; p_++)
+        for (int q = 0; q < 4; q++) used |= jt.blmap[(size_t)(4 * I + p_) * jt.npad + 4 * J + q] >= 0;
+      if (used) {
+        jt.tiles.push_back(I);
+        jt.tiles.push_back(J);
+      }
+    }
+  jt.ntiles = (int)jt.tiles.size() / 2;
+  if (xcorr_tpw(jt.ntiles) < 0) throw Error(SFXC_GPU_EINVAL, "too many streams for the X-step tiling (max 48 tiles)");
+  upload(c->blmap, jt.blmap.data(), jt.blmap.size() * 4, c->st);
+  upload(c->tiles, jt.tiles.data(), jt.tiles.size() * 4, c->st);
+  upload(c->blpairs, jt.blpairs.data(), jt.blpairs.size() * 4, c->st);
+  // twiddle tables: 256/128 for the block stage, rot and rot/2 for the windowed FFT
+  std::vector<float2> tw;
+  twiddles(tw, 256);
+  twiddles(tw, 128);
+  upload(c->tw256, tw.data(), tw.size() * sizeof(float2), c->st);
+  const int rot = c->sc[0].rot;
+  std::vector<float2> twr;
+  twiddles(twr, rot);
+  twiddles(twr, rot / 2);
+  upload(c->twrot, twr.data(), twr.size() * sizeof(float2), c->st);
+  std::vector<float> win = make_window(p->window, rot);
+  upload(c->window, win.data(), win.size() * 4, c->st);
+  CK(cudaStreamSynchronize(c->st));
+  c->current_integration = 0;
+  c->have_job = true;
+}
+
+// Delay_correction output chunking (sfxc/src/delay_correction.cc:31-36) and the
+// sub-integration dumps of Correlation_core::do_task (correlation_core.cc:48-72):
+// returns the row ranges accumulated between dumps.
+std::vector<std::pair<int, int>> subint_ranges(const sfxc_gpu_ctx *c) {
+  const StreamCtx &s = c->sc[0];
+  std::vector<std::pair<int, int>> r;
+  int tb = 0, cur = 0, start = 0, next_sub = 1;
+  const int minus = c->p.window != WINDOW_NONE ? 1 : 0;
+  for (int c0 = 0; c0 < s.n_blocks; c0 += s.nfft_max) {
+    const int nb = std::min(s.nfft_max, s.n_blocks - c0);
+    const int nc = (nb * c->Nd + tb) / s.hop - minus;
+    tb += nb * c->Nd - nc * s.hop;
+    if (nc <= 0) continue;
+    cur += nc;
+    if (cur == c->nffts || (c->nsub > 0 && cur >= next_sub * c->nsub)) {
+      r.push_back({start, cur});
+      start = cur;
+      if (cur != c->nffts) next_sub++;
+    }
+  }
+  if (start != c->nffts) r.push_back({start, c->nffts});
+  return r;
+}
+
+void serialize_integration(sfxc_gpu_ctx *c, const std::vector<float2> &vis, int32_t source_nr,
+                           const std::vector<std::pair<int64_t, int64_t>> &nfl, std::vector<uint8_t> &o) {
+  const int N = (int)c->streams.size();
+  const int nbl = (int)c->bl.size();
+  put(o, source_nr);
+  std::vector<int> stations;
+  std::set<int> seen;
+  for (int i = 0; i < N; i++)
+    if (seen.insert(c->streams[i].station_number).second) stations.push_back(c->streams[i].station_number);
+  put(o, (int32_t)(c->p.integration_nr + c->current_integration));
+  put(o, (int32_t)nbl);
+  put(o, (int32_t)stations.size());
+  put(o, (int32_t)N);
+  for (int s : stations) {
+    put(o, (int32_t)s);
+    put(o, (int32_t)0);
+    const double uvw[3] = {0, 0, 0};  // the UVW model is not part of this path
+    for (double v : uvw) put(o, v);
+  }
+  for (int i = 0; i < N; i++) {
+    o.push_back((uint8_t)c->streams[i].station_number);
+    o.push_back((uint8_t)c->p.frequency_nr);
+    o.push_back((uint8_t)(c->p.sideband == 'L' ? 0 : 1));
+    o.push_back((uint8_t)(c->streams[i].polarisation == 'R' ? 0 : 1));
+    int lv[5];
+    c->sc[i].stats.levels(lv);
+    int32_t l[5];
+    if (c->streams[i].bits == 2) {
+      l[0] = lv[0]; l[1] = lv[1]; l[2] = lv[2]; l[3] = lv[3];
+    } else {
+      l[0] = 0; l[1] = lv[0]; l[2] = lv[1]; l[3] = 0;
+    }
+    l[4] = lv[4];
+    for (int k = 0; k < 5; k++) put(o, l[k]);
+  }
+  const int64_t total = (int64_t)c->nffts * c->M;
+  const size_t K = (size_t)c->M + 1;
+  for (int b = 0; b < nbl; b++) {
+    int lv[5];
+    c->sc[c->bl[b].a].stats.levels(lv);
+    int64_t w = c->bl[b].a == c->bl[b].b ? total - lv[4] : total - lv[4] - nfl[b].first;
+    put(o, (int32_t)std::max<int64_t>(w, 0));
+    o.push_back((uint8_t)c->streams[c->bl[b].a].station_number);
+    o.push_back((uint8_t)c->streams[c->bl[b].b].station_number);
+    o.push_back((uint8_t)((c->streams[c->bl[b].a].polarisation == 'R' ? 0 : 1) |
+                          ((c->streams[c->bl[b].b].polarisation == 'R' ? 0 : 1) << 1) |
+                          ((c->p.sideband == 'U' ? 1 : 0) << 2) | ((c->p.frequency_nr & 31) << 3)));
+    o.push_back((uint8_t)' ');
+    const uint8_t *d = reinterpret_cast<const uint8_t *>(vis.data() + (size_t)b * K);
+    o.insert(o.end(), d, d + K * sizeof(float2));
+  }
+}
+
+int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
+  if (!c->have_job) throw Error(SFXC_GPU_ESTATE, "no parameters set");
+  const int N = (int)c->streams.size();
+  for (int i = 0; i < N; i++)
+    if (!c->sc[i].pushed) throw Error(SFXC_GPU_ESTATE, "a stream has no input for this integration");
+  const ticks_t tint = time_from_usec((double)c->p.integration_time_us);
+  const ticks_t start = c->p.start_ticks + (ticks_t)c->current_integration * tint;
+  const int M = c->M, K = c->K, kpad = c->kpad, nbl = (int)c->bl.size();
+  cudaStream_t st = c->st;
+  // ---- host planning per stream (Bit2float_worker state machine replica)
+  c->hsd.assign(N, StreamDev{});
+  std::vector<int4> items;
+  for (int i = 0; i < N; i++) {
+    StreamCtx &s = c->sc[i];
+    const StationStream &ss = c->streams[i];
+    s.sp = Spline::create(c->tables[c->stream_table[i]], start, tint);
+    std::vector<Record> recs(s.recs.begin() + (long)s.ust.rec, s.recs.end());
+    std::vector<Record> fresh = parse_protocol(s.chunk.data(), s.chunk.size(), 0);
+    recs.insert(recs.end(), fresh.begin(), fresh.end());
+    s.ust.rec = 0;
+    s.recs.swap(recs);
+    s.plan = plan_unpack(s.recs, s.ust, s.n_blocks, s.nfft_max, c->Nd, ss.bits, ss.sample_rate, ss.tsys_freq,
+                         s.sp.delay(start));
+    upload(s.src, s.chunk.data(), s.chunk.size(), st);
+    if (s.plan.segs.empty()) s.plan.segs.push_back(Segment{0, s.n_blocks * c->Nd, -1});
+    upload(s.segs, s.plan.segs.data(), s.plan.segs.size() * sizeof(Segment), st);
+    upload(s.stat_rng, s.plan.stats.data(), s.plan.stats.size() * sizeof(StatRange), st);
+    std::vector<double> spl;
+    spl.insert(spl.end(), s.sp.x.begin(), s.sp.x.end());
+    for (int k = 0; k < 3; k++) {
+      spl.insert(spl.end(), s.sp.y[k].begin(), s.sp.y[k].end());
+      spl.insert(spl.end(), s.sp.b[k].begin(), s.sp.b[k].end());
+      spl.insert(spl.end(), s.sp.c[k].begin(), s.sp.c[k].end());
+      spl.insert(spl.end(), s.sp.d[k].begin(), s.sp.d[k].end());
+    }
+    upload(s.spline, spl.data(), spl.size() * 8, st);
+    s.hist.ensure(512 * 8);
+    CK(cudaMemsetAsync(s.hist.p, 0, 512 * 8, st));
+    StreamDev &d = c->hsd[i];
+    d.src = s.src.as<uint8_t>();
+    d.segs = s.segs.as<DevSegment>();
+    d.nsegs = (int)s.plan.segs.size();
+    d.bits = ss.bits;
+    d.stats = s.stat_rng.as<DevStatRange>();
+    d.nstats = (int)s.plan.stats.size();
+    d.tsys_t0 = s.plan.tsys.t0;
+    d.tsys_period = s.plan.tsys.period;
+    d.tsys_on0 = s.plan.tsys.on0;
+    d.tsys_two_bit = s.plan.tsys.two_bit;
+    d.spline = s.spline.as<double>();
+    d.spline_n = s.sp.n;
+    d.scan_begin = s.sp.scan_begin;
+    d.clock_epoch = s.sp.clock_epoch;
+    d.clock_offset = s.sp.clock_offset;
+    d.clock_rate = s.sp.clock_rate;
+    d.start_ticks = start;
+    d.tps = ticks_per_sample(ss.sample_rate);
+    d.n_blocks = s.n_blocks;
+    const ticks_t fft_len = time_from_usec((double)c->Nd / (ss.sample_rate / 1000000));
+    d.fft_len_ticks = fft_len;
+    d.half_len_ticks = time_div(fft_len, 2);
+    d.fft_len_sec = time_sec_of_day(fft_len);
+    d.sample_rate = ss.sample_rate;
+    d.bandwidth = ss.bandwidth;
+    d.oversamp = (int)std::round(ss.sample_rate / (2 * (double)ss.bandwidth));
+    d.sideband = ss.sideband == 'L' ? -1 : 1;
+    d.center_freq = ss.channel_freq + d.sideband * ss.bandwidth * 0.5 + ss.lo_offset;
+    d.lo_offset = ss.lo_offset;
+    const double dt = time_diff(start, c->p.experiment_start_ticks);
+    double sp0 = ss.lo_offset * (dt - std::trunc(dt)) + (ss.lo_offset - std::trunc(ss.lo_offset)) * std::trunc(dt);
+    d.start_phase = sp0 - std::floor(sp0);
+    d.rot = s.rot;
+    d.flip = c->p.sideband != ss.sideband;
+    int64_t delta, freq = ss.channel_freq;  // delay_correction.cc:226-241
+    if (c->p.sideband != ss.sideband) freq += (int64_t)d.sideband * ss.bandwidth;
+    delta = c->p.sideband == 'L' ? freq - c->p.channel_freq : c->p.channel_freq - freq;
+    if (delta > 0) {
+      d.output_offset = (int)(delta * 2 * M / c->p.sample_rate);
+      d.temp_fft_offset = 0;
+    } else {
+      d.output_offset = 0;
+      d.temp_fft_offset = (int)(-delta * 2 * M / c->p.sample_rate);
+    }
+    d.hist = s.hist.as<unsigned long long>();
+    for (int r = 0; r < (int)s.plan.stats.size(); r++) {
+      const StatRange &sr = s.plan.stats[r];
+      for (int off = 0; off < sr.n; off += 4096) items.push_back(make_int4(i, r, off, std::min(4096, sr.n - off)));
+    }
+    s.chunk.clear();
+    s.pushed = false;
+  }
+  // ---- flagged samples and normalisation factors (host)
+  std::vector<const std::vector<InvalidRun> *> inv;
+  for (int i = 0; i < N; i++) inv.push_back(&c->sc[i].plan.invalid);
+  std::vector<std::pair<int64_t, int64_t>> nfl;
+  find_invalid(c->streams, c->p.sample_rate, c->bl, inv, nfl);
+  const int64_t total = (int64_t)c->nffts * M;
+  std::vector<double> flagfac(nbl, 1.0);
+  auto inv_level = [&](int i) {  // bit_statistics::get_statistics()[4]
+    return (int)(((uint64_t)c->p.sample_rate * (uint64_t)(int64_t)(int)c->sc[i].plan.n_invalid) /
+                 (uint64_t)c->streams[i].sample_rate);
+  };
+  for (int b = N; b < nbl; b++) {
+    const int64_t v1 = total - inv_level(c->bl[b].a), v2 = total - inv_level(c->bl[b].b);
+    const double n1 = v1 > 0 ? 1 - nfl[b].first * 1. / v1 : 1;
+    const double n2 = v2 > 0 ? 1 - nfl[b].second * 1. / v2 : 1;
+    double n = n1 * n2;
+    if (n < 0.01) n = 1;
+    flagfac[b] = n;
+  }
+  upload(c->flagfac, flagfac.data(), flagfac.size() * 8, st);
+  upload(c->streamdev, c->hsd.data(), c->hsd.size() * sizeof(StreamDev), st);
+  upload(c->items, items.data(), items.size() * sizeof(int4), st);
+  // ---- device work
+  const size_t accn = (size_t)c->nbins * nbl * kpad;
+  c->acc.ensure(accn * sizeof(float2));
+  CK(cudaMemsetAsync(c->acc.p, 0, accn * sizeof(float2), st));
+  CK(cudaEventRecord(c->ev[0], st));
+  launch_bitstat(c->streamdev.as<StreamDev>(), c->items.as<int4>(), (int)items.size(), st);
+  CK(cudaGetLastError());
+  const bool pulsar = c->nbins > 1;
+  std::vector<std::pair<int, int>> ranges;
+  if (pulsar)
+    ranges.push_back({0, c->nffts});  // no sub-integrations in Correlation_core_pulsar
+  else
+    ranges = subint_ranges(c);
+  int max_rows = 0;
+  for (auto &r : ranges) max_rows = std::max(max_rows, r.second - r.first);
+  const int minus = c->p.window != WINDOW_NONE ? 0 : -1;  // one extra hop for overlapping windows
+  const int hop = c->sc[0].hop;
+  const bool chunked = hop % kNd == 0;
+  if (!chunked) {
+    ranges.assign(1, {0, c->nffts});
+    max_rows = c->nffts;
+  }
+  int max_blocks = 0;
+  for (int i = 0; i < N; i++) max_blocks = std::max(max_blocks, chunked ? (max_rows + 2) * hop / kNd : c->sc[i].n_blocks);
+  c->ts.ensure((size_t)N * max_blocks * kNd * sizeof(float));
+  const bool tc = c->x_mode == SFXC_GPU_X_TC_HILO;
+  c->spec.ensure((size_t)N * max_rows * kpad * sizeof(float2));
+  float t_f1 = 0, t_f2 = 0, t_x = 0;
+  // pulsar setup (Correlation_core_pulsar::set_parameters, correlation_core_pulsar.cc:46-95)
+  double psr_start_phase = 0, psr_rate = 0, fft_duration = 0;
+  if (pulsar) {
+    const double us_per_day = (double)((int64_t)24 * 60 * 60 * 1000000);
+    const double start_mjd = time_mjd(start);
+    fft_duration = ((double)M * 1000000) / c->p.sample_rate;
+    size_t closest = 0;
+    double diff = std::fabs(c->polyco[0].tmid - start_mjd);
+    for (size_t i = 1; i < c->polyco.size(); i++) {
+      double nd = std::fabs(c->polyco[i].tmid - start_mjd);
+      if (nd < diff) {
+        diff = nd;
+        closest = i;
+      }
+    }
+    const Polyco &pc = c->polyco[closest];
+    // Association of the reference as built with its own flags (-O2 -ffast-math,
+    // sfxc/configure.ac:31): GCC evaluates (start_mjd - tmid) + fft_duration/us_per_day
+    // as (start_mjd + fft_duration/us_per_day) - tmid.  The FP64 start MJD has
+    // ~6e-7 s resolution, so the association moves the phase by up to ~1e-5
+    // cycles and decides bins near a gate edge.
+    double DT = c->p.window == WINDOW_NONE ? ((start_mjd + fft_duration / (2 * us_per_day)) - pc.tmid) * 1440
+                                           : ((start_mjd + fft_duration / us_per_day) - pc.tmid) * 1440;
+    const int nc = (int)pc.coef.size();
+    double sp = 0;
+    for (int i = nc - 1; i > 0; i--) sp = (sp + pc.coef[i]) * DT;
+    sp += (pc.ref_phase - std::floor(pc.ref_phase)) + DT * 60 * pc.ref_freq + pc.coef[0];
+    psr_start_phase = sp;
+    psr_rate = pc.coef[1] + 60 * pc.ref_freq;
+    const int sb = c->p.sideband == 'L' ? -1 : 1;
+    const double base_freq = c->p.channel_freq * 1e-6;
+    const double dfreq = sb * c->p.sample_rate * 1e-6 / (2 * M);
+    const double inv2 = 1 / (pc.obs_freq * pc.obs_freq);
+    double freq = 0;
+    for (int i = nc - 1; i > 1; i--) freq = (freq + i * pc.coef[i]) * DT;
+    freq = (freq + pc.coef[1]) / 60 + pc.ref_freq;
+    std::vector<double> off(K);
+    for (int i = 0; i < K; i++) {  // (4148.808*DM)*((...)*freq): the same build's association
+      const double x = base_freq + i * dfreq;
+      off[i] = (4148.808 * pc.dm) * ((1 / (x * x) - inv2) * freq);
+    }
+    upload(c->offsets, off.data(), off.size() * 8, st);
+    c->bins.ensure((size_t)max_rows * K * sizeof(int16_t));
+  }
+  cudaEvent_t e0, e1, e2, e3;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventCreate(&e2));
+  CK(cudaEventCreate(&e3));
+  for (auto &rg : ranges) {
+    const int r0 = rg.first, r1 = rg.second, nrows = r1 - r0;
+    // block range of each stream for rows [r0, r1) (plus the overlapping half window)
+    for (int i = 0; i < N; i++) {
+      StreamDev &d = c->hsd[i];
+      const int b0 = chunked ? r0 * c->sc[i].hop / kNd : 0;
+      const int b1 = chunked ? std::min(c->sc[i].n_blocks, (r1 + 1 + minus) * c->sc[i].hop / kNd) : c->sc[i].n_blocks;
+      d.ts = c->ts.as<float>() + (size_t)i * max_blocks * kNd;
+      d.block0 = b0;
+      d.n_blocks = b1 - b0;
+    }
+    upload(c->streamdev, c->hsd.data(), c->hsd.size() * sizeof(StreamDev), st);
+    CK(cudaEventRecord(e0, st));
+    launch_fstep_block(c->streamdev.as<StreamDev>(), N, max_blocks, c->tw256.as<float2>(), st);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(e1, st));
+    const int nper = c->p.window == WINDOW_NONE ? c->sc[0].hop : c->sc[0].rot;
+    launch_window_fft(c->streamdev.as<StreamDev>(), N, 0, nrows, max_rows, c->window.as<float>(),
+                      c->twrot.as<float2>(), c->sc[0].rot, nper, M, kpad, c->spec.p, false, 1.0f, st);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(e2, st));
+    if (pulsar) {
+      launch_pulsar(c->spec.as<float2>(), max_rows, kpad, N, c->jt.npad, nrows, K, c->tiles.as<int>(), c->jt.ntiles,
+                    c->blmap.as<int>(), nbl, psr_start_phase, psr_rate, fft_duration, c->offsets.as<double>(),
+                    c->p.gate_start, c->p.gate_stop, c->nbins, c->bins.as<int16_t>(), c->acc.as<float2>(), st);
+    } else {
+      launch_xcorr_f32(c->spec.as<float2>(), max_rows, kpad, N, c->jt.npad, 0, nrows, K, c->tiles.as<int>(),
+                       c->jt.ntiles, c->blmap.as<int>(), c->acc.as<float2>(), st);
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(e3, st));
+    CK(cudaEventSynchronize(e3));
+    float a, b, x;
+    CK(cudaEventElapsedTime(&a, e0, e1));
+    CK(cudaEventElapsedTime(&b, e1, e2));
+    CK(cudaEventElapsedTime(&x, e2, e3));
+    t_f1 += a;
+    t_f2 += b;
+    t_x += x;
+  }
+  (void)tc;
+  // restore the whole-integration time base for inspection calls
+  for (int i = 0; i < N; i++) {
+    c->hsd[i].block0 = 0;
+    c->hsd[i].n_blocks = c->sc[i].n_blocks;
+  }
+  // ---- normalisation and statistics
+  CK(cudaEventRecord(e0, st));
+  c->norms.ensure((size_t)N * 8);
+  c->out.ensure((size_t)c->nbins * nbl * K * sizeof(float2));
+  for (int bin = 0; bin < c->nbins; bin++)
+    launch_normalize(c->acc.as<float2>() + (size_t)bin * nbl * kpad, kpad, M, N, nbl, c->blpairs.as<int>(),
+                     c->norms.as<double>(), c->flagfac.as<double>(), c->out.as<float2>() + (size_t)bin * nbl * K, st);
+  CK(cudaGetLastError());
+  std::vector<float2> vis((size_t)c->nbins * nbl * K);
+  CK(cudaMemcpyAsync(vis.data(), c->out.p, vis.size() * sizeof(float2), cudaMemcpyDeviceToHost, st));
+  std::vector<unsigned long long> hist((size_t)N * 512);
+  for (int i = 0; i < N; i++)
+    CK(cudaMemcpyAsync(hist.data() + (size_t)i * 512, c->sc[i].hist.p, 512 * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaEventRecord(e1, st));
+  CK(cudaStreamSynchronize(st));
+  float tn;
+  CK(cudaEventElapsedTime(&tn, e0, e1));
+  float tall;
+  CK(cudaEventElapsedTime(&tall, c->ev[0], e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  cudaEventDestroy(e3);
+  c->timings[0] = t_f1;
+  c->timings[1] = t_f2;
+  c->timings[2] = t_x;
+  c->timings[3] = tn;
+  c->timings[4] = tall;
+  for (int i = 0; i < N; i++) {
+    BitStats &bs = c->sc[i].stats;
+    for (int k = 0; k < 256; k++) {
+      bs.on[k] = (int64_t)hist[(size_t)i * 512 + k];
+      bs.off[k] = (int64_t)hist[(size_t)i * 512 + 256 + k];
+    }
+    bs.n_invalid = c->sc[i].plan.n_invalid;
+    bs.bits = c->streams[i].bits;
+    bs.sample_rate = c->streams[i].sample_rate;
+    bs.base_sample_rate = c->p.sample_rate;
+  }
+  // ---- output bytes (integration_write per bin) and tsys records
+  std::vector<uint8_t> o;
+  for (int bin = 0; bin < c->nbins; bin++) {
+    std::vector<float2> v(vis.begin() + (size_t)bin * nbl * K, vis.begin() + (size_t)(bin + 1) * nbl * K);
+    serialize_integration(c, v, pulsar ? bin : 0, nfl, o);
+  }
+  if (sink && sink(user, 0, o.data(), o.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
+  for (int i = 0; i < N; i++) {
+    std::vector<uint8_t> t;
+    t.push_back((uint8_t)c->streams[i].station_number);
+    t.push_back((uint8_t)c->p.frequency_nr);
+    t.push_back((uint8_t)(c->p.sideband == 'L' ? 0 : 1));
+    t.push_back((uint8_t)(c->streams[i].polarisation == 'R' ? 0 : 1));
+    int ts[4];
+    c->sc[i].stats.tsys(ts);
+    put(t, (int64_t)start);
+    for (int k = 0; k < 4; k++) put(t, (int64_t)ts[k]);
+    if (sink && sink(user, 1, t.data(), t.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
+  }
+  c->current_integration++;
+  return SFXC_GPU_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ C entry points
+extern "C" {
+
+sfxc_gpu_ctx *sfxc_gpu_create(const sfxc_gpu_config *config) {
+  std::unique_ptr<sfxc_gpu_ctx> c(new sfxc_gpu_ctx());
+  try {
+    if (config) {
+      c->device = config->device;
+      c->x_mode = config->x_mode;
+    }
+    if (c->x_mode != SFXC_GPU_X_FP32 && c->x_mode != SFXC_GPU_X_TC_HILO) throw Error(SFXC_GPU_EINVAL, "bad x_mode");
+    int n = 0;
+    CK(cudaGetDeviceCount(&n));
+    if (c->device < 0 || c->device >= n) throw Error(SFXC_GPU_EINVAL, "no such CUDA device");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    for (auto &e : c->ev) CK(cudaEventCreate(&e));
+  } catch (const Error &e) {
+    g_error = e.msg;
+    return nullptr;
+  }
+  return c.release();
+}
+
+void sfxc_gpu_destroy(sfxc_gpu_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  for (auto &e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+const char *sfxc_gpu_last_error(const sfxc_gpu_ctx *c) { return c ? c->err.c_str() : g_error.c_str(); }
+const char *sfxc_gpu_global_error(void) { return g_error.c_str(); }
+
+int sfxc_gpu_set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
+  if (!c) return SFXC_GPU_EINVAL;
+  try {
+    CK(cudaSetDevice(c->device));
+    c->have_job = false;
+    set_parameters(c, p);
+    return SFXC_GPU_OK;
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
+int sfxc_gpu_push_protocol(sfxc_gpu_ctx *c, int32_t stream, const uint8_t *bytes, size_t n) {
+  if (!c) return SFXC_GPU_EINVAL;
+  if (!c->have_job) return fail(c, Error(SFXC_GPU_ESTATE, "no parameters set"));
+  if (stream < 0 || stream >= (int)c->sc.size()) return fail(c, Error(SFXC_GPU_EINVAL, "bad stream index"));
+  if (n && !bytes) return fail(c, Error(SFXC_GPU_EINVAL, "null input"));
+  StreamCtx &s = c->sc[stream];
+  s.chunk.insert(s.chunk.end(), bytes, bytes + n);
+  s.pushed = true;
+  return SFXC_GPU_OK;
+}
+
+int sfxc_gpu_run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
+  if (!c) return SFXC_GPU_EINVAL;
+  try {
+    CK(cudaSetDevice(c->device));
+    return run_integration(c, sink, user);
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
+int sfxc_gpu_copy_unpacked(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n) {
+  if (!c || !c->have_job) return SFXC_GPU_ESTATE;
+  if (stream < 0 || stream >= (int)c->sc.size()) return fail(c, Error(SFXC_GPU_EINVAL, "bad stream index"));
+  try {
+    const StreamCtx &s = c->sc[stream];
+    const size_t need = (size_t)s.n_blocks * c->Nd;
+    if (n < need) throw Error(SFXC_GPU_EINVAL, "output buffer too small");
+    StreamDev d = c->hsd[stream];
+    DevBuf sd, dout;
+    dout.ensure(need * sizeof(float));
+    upload(sd, &d, sizeof(StreamDev), c->st);
+    launch_unpack(sd.as<StreamDev>(), 1, s.n_blocks, dout.as<float>(), c->st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, dout.p, need * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return (int)need;
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
+int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n) {
+  if (!c || !c->have_job) return SFXC_GPU_ESTATE;
+  if (stream < 0 || stream >= (int)c->sc.size()) return fail(c, Error(SFXC_GPU_EINVAL, "bad stream index"));
+  try {
+    // recompute the spectra of the whole last integration into a scratch buffer
+    const StreamCtx &s = c->sc[stream];
+    const size_t rows = (size_t)c->nffts, K = (size_t)c->M + 1;
+    if (n < rows * K * 2) throw Error(SFXC_GPU_EINVAL, "output buffer too small");
+    StreamDev d = c->hsd[stream];
+    d.block0 = 0;
+    d.n_blocks = s.n_blocks;
+    DevBuf ts, spec, sd;
+    ts.ensure((size_t)s.n_blocks * kNd * sizeof(float));
+    spec.ensure(rows * c->kpad * sizeof(float2));
+    d.ts = ts.as<float>();
+    upload(sd, &d, sizeof(StreamDev), c->st);
+    launch_fstep_block(sd.as<StreamDev>(), 1, s.n_blocks, c->tw256.as<float2>(), c->st);
+    const int nper = c->p.window == WINDOW_NONE ? s.hop : s.rot;
+    launch_window_fft(sd.as<StreamDev>(), 1, 0, (int)rows, (int)rows, c->window.as<float>(), c->twrot.as<float2>(),
+                      s.rot, nper, c->M, c->kpad, spec.p, false, 1.0f, c->st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy2DAsync(out, K * sizeof(float2), spec.p, c->kpad * sizeof(float2), K * sizeof(float2), rows,
+                         cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return (int)(rows * K * 2);
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
+int sfxc_gpu_extract_channels(sfxc_gpu_ctx *c, const uint8_t *words, int64_t nwords, int32_t word_bytes,
+                              int32_t bits, int32_t n_subbands, int32_t fan_out, const int32_t *tracks, uint8_t *out) {
+  if (!c) return SFXC_GPU_EINVAL;
+  try {
+    if (!words || !tracks || !out || nwords <= 0 || word_bytes <= 0 || n_subbands <= 0)
+      throw Error(SFXC_GPU_EINVAL, "bad arguments");
+    if (fan_out <= 0 || fan_out > 8 || 8 % fan_out || (bits != 1 && bits != 2) || fan_out % bits)
+      throw Error(SFXC_GPU_EINVAL, "fan_out must divide 8 and be a multiple of bits_per_sample");
+    for (int i = 0; i < n_subbands * fan_out; i++)
+      if (tracks[i] < 0 || tracks[i] >= word_bytes * 8) throw Error(SFXC_GPU_EINVAL, "track outside the word");
+    const int spb = 8 / fan_out;
+    if (nwords % spb) throw Error(SFXC_GPU_EINVAL, "word count must be a multiple of 8/fan_out");
+    CK(cudaSetDevice(c->device));
+    const int64_t nout = nwords / spb;
+    DevBuf din, dtr, dout;
+    upload(din, words, (size_t)(nwords * word_bytes), c->st);
+    upload(dtr, tracks, (size_t)n_subbands * fan_out * 4, c->st);
+    dout.ensure((size_t)(nout * n_subbands));
+    launch_extract(din.as<uint8_t>(), nout, word_bytes, bits, n_subbands, fan_out, dtr.as<int>(), dout.as<uint8_t>(),
+                   c->st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, dout.p, (size_t)(nout * n_subbands), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return SFXC_GPU_OK;
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
+int sfxc_gpu_last_timings(const sfxc_gpu_ctx *c, float *ms5) {
+  if (!c || !ms5) return SFXC_GPU_EINVAL;
+  for (int i = 0; i < 5; i++) ms5[i] = c->timings[i];
+  return SFXC_GPU_OK;
+}
+
+int sfxc_gpu_delay_list(const sfxc_delay_table *table, int64_t start, int64_t stop, int32_t sample_rate, int32_t bits,
+                        int64_t *ticks, int32_t *bytes, int32_t *remaining, int32_t capacity) {
+  try {
+    if (!table || !table->del_bytes) throw Error(SFXC_GPU_EINVAL, "no delay table");
+    if (bits != 1 && bits != 2) throw Error(SFXC_GPU_EINVAL, "bits_per_sample must be 1 or 2");
+    if (stop <= start) throw Error(SFXC_GPU_EINVAL, "empty interval");
+    DelayTable t = DelayTable::parse(table->del_bytes, table->del_size);
+    t.clock_offset = table->clock_offset;
+    t.clock_rate = table->clock_rate;
+    t.clock_epoch = table->clock_epoch_ticks;
+    Spline sp = Spline::create(t, start, stop - start);
+    std::vector<Delay> d = interval_delays(sp, start, stop, sample_rate, bits);
+    for (size_t i = 0; i < d.size() && (int)i < capacity; i++) {
+      ticks[i] = d[i].time;
+      bytes[i] = d[i].bytes;
+      remaining[i] = d[i].rem;
+    }
+    return (int)d.size();
+  } catch (const Error &e) {
+    g_error = e.msg;
+    return e.code;
+  }
+}
+
+int64_t sfxc_gpu_write_protocol(const uint8_t *stream, int32_t n_blocks, const sfxc_channel_block *blocks,
+                                int32_t n_slices, const sfxc_slice *slices, int32_t sample_rate, int32_t bits,
+                                int64_t integration_time_us, uint8_t *out, int64_t capacity, int64_t *offsets) {
+  try {
+    if (!stream || !blocks || !slices || n_blocks < 0 || n_slices < 0) throw Error(SFXC_GPU_EINVAL, "bad arguments");
+    std::vector<ChannelBlock> cb(n_blocks);
+    int64_t off = 0;
+    for (int i = 0; i < n_blocks; i++) {
+      cb[i].start = blocks[i].start_ticks;
+      cb[i].size = blocks[i].size;
+      cb[i].src_offset = off;
+      off += blocks[i].size;
+      for (int k = 0; k < blocks[i].n_invalid; k++)
+        cb[i].invalid.push_back(InvalidRun{blocks[i].invalid[2 * k], blocks[i].invalid[2 * k + 1]});
+    }
+    std::vector<SliceRequest> sl(n_slices);
+    for (int i = 0; i < n_slices; i++) {
+      sl[i].start = slices[i].start_ticks;
+      sl[i].stop = slices[i].stop_ticks;
+      sl[i].nr_samples = slices[i].nr_samples;
+      for (int k = 0; k < slices[i].n_delays; k++)
+        sl[i].delays.push_back(Delay{slices[i].delay_ticks[k], slices[i].delay_bytes[k], slices[i].delay_remaining[k]});
+      if (sl[i].delays.empty()) throw Error(SFXC_GPU_EINVAL, "slice without delays");
+    }
+    auto recs = write_protocol(cb, sl, sample_rate, bits, (double)integration_time_us);
+    int64_t total = 0;
+    std::vector<uint8_t> buf;
+    for (int i = 0; i < n_slices; i++) {
+      buf.clear();
+      serialize_protocol(recs[i], stream, buf);
+      if (offsets) offsets[i] = total;
+      if (out) {
+        if (total + (int64_t)buf.size() > capacity) throw Error(SFXC_GPU_EINVAL, "output buffer too small");
+        std::memcpy(out + total, buf.data(), buf.size());
+      }
+      total += (int64_t)buf.size();
+    }
+    if (offsets) offsets[n_slices] = total;
+    return total;
+  } catch (const Error &e) {
+    g_error = e.msg;
+    return e.code;
+  }
+}
+
+}  // extern "C"

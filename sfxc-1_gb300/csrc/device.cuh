@@ -1,0 +1,189 @@
+// Device-side structures and helpers shared by the correlator-node kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+namespace sfxc {
+
+constexpr int kNd = 256;  // fft_size_delaycor handled by the fused block kernel
+
+// One plan segment: output samples [out0, out0+n) come from source bit src_bit
+// onward (bits per sample apart); src_bit < 0 means zeros (invalid or an
+// inserted sample).  Same layout as host.hpp's Segment.
+struct DevSegment {
+  int32_t out0, n;
+  int64_t src_bit;
+};
+struct DevStatRange {
+  int64_t src_byte;
+  int32_t n, cidx;
+};
+
+// Per-stream parameters of the F-step kernels (one integration).
+struct StreamDev {
+  const uint8_t *src;          // source bytes (protocol buffer or channel stream)
+  const DevSegment *segs;      // unpack plan
+  int32_t nsegs;
+  int32_t bits;
+  const DevStatRange *stats;   // counted-byte ranges
+  int32_t nstats;
+  int32_t tsys_t0, tsys_period, tsys_on0, tsys_two_bit;
+  // delay model: spline over n nodes: x | (y b c d) x3 columns, 13n doubles
+  const double *spline;
+  int32_t spline_n;
+  int64_t scan_begin, clock_epoch;
+  double clock_offset, clock_rate;
+  // time base
+  int64_t start_ticks;         // integration start
+  int32_t tps;                 // ticks per sample
+  int32_t n_blocks;            // blocks handled by this launch, starting at block0
+  int32_t block0;              // first block (index within the integration)
+  int64_t fft_len_ticks, half_len_ticks;
+  double fft_len_sec;
+  // channel setup (Delay_correction::set_parameters)
+  int32_t sample_rate, bandwidth, oversamp, sideband;  // sideband +1 / -1
+  double center_freq, lo_offset, start_phase;
+  // windowed FFT stage
+  int32_t rot, flip, output_offset, temp_fft_offset;
+  // outputs
+  float *ts;                   // fringe-stopped series, n_blocks*256 floats
+  unsigned long long *hist;    // 512 counters: [on|off][byte]
+};
+
+// --------------------------------------------------------------------------
+// FP64 Akima evaluation with the same operation order as the host (no FMA
+// contraction) so that integer delays agree bit for bit.
+__device__ __forceinline__ int spline_index(const double *x, int n, double v) {
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    int i = (hi + lo) >> 1;
+    if (x[i] > v)
+      hi = i;
+    else
+      lo = i;
+  }
+  return lo;
+}
+__device__ __forceinline__ double spline_eval(const double *sp, int n, int col, double v) {
+  const double *x = sp;
+  const double *y = sp + n + col * 4 * n;
+  const double *b = y + n, *c = y + 2 * n, *d = y + 3 * n;
+  int i = spline_index(x, n, v);
+  double dx = __dsub_rn(v, x[i]);
+  double t = __dadd_rn(c[i], __dmul_rn(d[i], dx));
+  t = __dadd_rn(b[i], __dmul_rn(dx, t));
+  return __dadd_rn(y[i], __dmul_rn(dx, t));
+}
+__device__ __forceinline__ double time_diff_dev(int64_t a, int64_t b) {
+  return __ddiv_rn((double)(a - b), 512000000.0);
+}
+__device__ __forceinline__ double stream_delay(const StreamDev &s, int64_t t) {
+  double r = spline_eval(s.spline, s.spline_n, 0, time_diff_dev(t, s.scan_begin));
+  double drift = __dadd_rn(s.clock_offset, __dmul_rn(time_diff_dev(t, s.clock_epoch), s.clock_rate));
+  return __dadd_rn(r, drift);
+}
+__device__ __forceinline__ double stream_phase(const StreamDev &s, int64_t t) {
+  return spline_eval(s.spline, s.spline_n, 1, time_diff_dev(t, s.scan_begin));
+}
+__device__ __forceinline__ double stream_amplitude(const StreamDev &s, int64_t t) {
+  return spline_eval(s.spline, s.spline_n, 2, time_diff_dev(t, s.scan_begin));
+}
+
+// --------------------------------------------------------------------------
+// Stockham auto-sort FFT (radix 4, one radix-2 stage when log2 N is odd),
+// natural order in and out, ping-pong between two buffers.  `tw` holds
+// exp(-2 pi i m / N) for m < N.  Threads [tid, tid+nthreads) cooperate; the
+// caller supplies the barrier (warp or CTA).
+template <int SIGN>
+__device__ __forceinline__ float2 cmul_tw(float2 a, float2 w) {
+  // a * w (SIGN<0) or a * conj(w) (SIGN>0)
+  float wi = SIGN < 0 ? w.y : -w.y;
+  return make_float2(a.x * w.x - a.y * wi, a.x * wi + a.y * w.x);
+}
+
+template <int SIGN, typename Sync>
+__device__ float2 *stockham(float2 *a, float2 *b, int N, const float2 *tw, int tid, int nthreads, Sync sync) {
+  int Ns = 1;
+  int lg = 31 - __clz(N);
+  if (lg & 1) {  // one radix-2 stage first
+    for (int j = tid; j < N / 2; j += nthreads) {
+      float2 v0 = a[j], v1 = a[j + N / 2];
+      b[2 * j] = make_float2(v0.x + v1.x, v0.y + v1.y);
+      b[2 * j + 1] = make_float2(v0.x - v1.x, v0.y - v1.y);
+    }
+    sync();
+    float2 *t = a;
+    a = b;
+    b = t;
+    Ns = 2;
+  }
+  for (; Ns < N; Ns *= 4) {
+    const int q = N / 4;
+    const int twstep = N / (Ns * 4);
+    for (int j = tid; j < q; j += nthreads) {
+      const int k = j % Ns;
+      float2 v0 = a[j], v1 = a[j + q], v2 = a[j + 2 * q], v3 = a[j + 3 * q];
+      if (Ns > 1) {
+        const int m = k * twstep;
+        v1 = cmul_tw<SIGN>(v1, tw[m]);
+        v2 = cmul_tw<SIGN>(v2, tw[2 * m]);
+        v3 = cmul_tw<SIGN>(v3, tw[3 * m]);
+      }
+      float2 a0 = make_float2(v0.x + v2.x, v0.y + v2.y);
+      float2 a1 = make_float2(v0.x - v2.x, v0.y - v2.y);
+      float2 a2 = make_float2(v1.x + v3.x, v1.y + v3.y);
+      float2 d = make_float2(v1.x - v3.x, v1.y - v3.y);
+      // a3 = d * (-i) for the forward transform, d * (+i) for the backward
+      float2 a3 = SIGN < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
+      const int o = (j / Ns) * Ns * 4 + k;
+      b[o] = make_float2(a0.x + a2.x, a0.y + a2.y);
+      b[o + Ns] = make_float2(a1.x + a3.x, a1.y + a3.y);
+      b[o + 2 * Ns] = make_float2(a0.x - a2.x, a0.y - a2.y);
+      b[o + 3 * Ns] = make_float2(a1.x - a3.x, a1.y - a3.y);
+    }
+    sync();
+    float2 *t = a;
+    a = b;
+    b = t;
+  }
+  return a;
+}
+
+struct WarpSync {
+  __device__ void operator()() const { __syncwarp(); }
+};
+struct BlockSync {
+  __device__ void operator()() const { __syncthreads(); }
+};
+
+// Unpacked sample `o` (index within the integration) through the plan;
+// `si` is a segment cursor that only moves forward for increasing `o`.
+__device__ __forceinline__ float gather_sample(const StreamDev &s, int o, int &si) {
+  while (si + 1 < s.nsegs && s.segs[si].out0 + s.segs[si].n <= o) si++;
+  const DevSegment sg = s.segs[si];
+  if (sg.src_bit < 0 || o < sg.out0 || o >= sg.out0 + sg.n) return 0.0f;
+  const int64_t bit = sg.src_bit + (int64_t)(o - sg.out0) * s.bits;
+  const int code = (__ldg(s.src + (bit >> 3)) >> (bit & 7)) & ((1 << s.bits) - 1);
+  // Bit2float_worker lookup tables (sfxc/src/bit2float_worker.cc:4-10)
+  return s.bits == 2 ? (code == 0 ? -7.f : code == 1 ? -2.f : code == 2 ? 2.f : 7.f) : (code ? 5.f : -5.f);
+}
+// First segment whose range can contain sample o (binary search on out0).
+__device__ __forceinline__ int find_segment(const StreamDev &s, int o) {
+  int lo = 0, hi = s.nsegs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (s.segs[mid].out0 <= o)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// Accumulator element written by the X kernels and read by normalisation.
+struct VisLayout {
+  int32_t nbl, kpad;  // baselines, padded channel count
+};
+
+}  // namespace sfxc

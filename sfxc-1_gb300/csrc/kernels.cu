@@ -1,0 +1,550 @@
+// CUDA kernels of the correlator-node path (sm_103a).
+//
+//   fstep_block_kernel   unpack (plan segments + 1/2-bit lookup) -> rfft(256)
+//                        -> fractional-delay phase ramp -> complex ifft(256)
+//                        -> fringe rotation; one warp per 256-sample block.
+//                        Delay_correction::fractional_bit_shift / fringe_stopping
+//                        (sfxc/src/delay_correction.cc:82-184) on the unpacked
+//                        samples of Bit2float_worker (sfxc/src/bit2float_worker.cc:327-425).
+//   window_fft_kernel    window, sideband flip, real FFT of 2M samples, channel
+//                        selection (delay_correction.cc:57-75); one CTA per row.
+//   bitstat_kernel       byte histograms with cal-diode on/off split
+//                        (bit_statistics.cc:36-47, bit2float_worker.cc:341-346).
+//   xcorr_f32_kernel     X-step on CUDA cores, 4x4 stream tiles per thread
+//                        (Correlation_core::integration_step, correlation_core.cc:241-273).
+//   pulsar_bins_kernel / xcorr_f32_pulsar  bin per (FFT, channel) in FP64 and binned
+//                        accumulation (correlation_core_pulsar.cc:210-238).
+//   norm_* kernels       Correlation_core::integration_normalize (275-314).
+#include <cstdio>
+
+#include "device.cuh"
+#include "kernels.hpp"
+
+namespace sfxc {
+
+// ------------------------------------------------------------------------
+// F-step, stage 1: one warp per block of 256 samples.
+// tw holds exp(-2 pi i m / 256) for m < 256 followed by exp(-2 pi i m / 128) for m < 128.
+__global__ void __launch_bounds__(256) fstep_block_kernel(const StreamDev *__restrict__ streams,
+                                                         const float2 *__restrict__ tw) {
+  __shared__ float2 sbuf[8][2][kNd];
+  __shared__ float2 stw[kNd + kNd / 2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < kNd + kNd / 2; i += blockDim.x) stw[i] = tw[i];
+  __syncthreads();
+  const StreamDev &s = streams[blockIdx.y];
+  const int bl = blockIdx.x * 8 + warp;
+  if (bl >= s.n_blocks) return;
+  const int b = s.block0 + bl;  // block index within the integration
+  float2 *A = sbuf[warp][0], *B = sbuf[warp][1];
+  float *xa = reinterpret_cast<float *>(A);
+
+  // ---- FP64 block parameters, one spline evaluation per lane
+  const int64_t ct = s.start_ticks + (int64_t)b * kNd * s.tps;
+  double v = 0.0;
+  if (lane == 0) v = stream_delay(s, ct + s.half_len_ticks);
+  else if (lane == 1) v = stream_delay(s, ct);
+  else if (lane == 2) v = stream_delay(s, ct + s.fft_len_ticks);
+  else if (lane == 3) v = stream_phase(s, ct);
+  else if (lane == 4) v = stream_phase(s, ct + s.fft_len_ticks);
+  else if (lane == 5) v = stream_amplitude(s, ct + s.half_len_ticks);
+  const double delay_c = __shfl_sync(0xffffffffu, v, 0);
+  const double delay_0 = __shfl_sync(0xffffffffu, v, 1);
+  const double delay_1 = __shfl_sync(0xffffffffu, v, 2);
+  const double phase_0 = __shfl_sync(0xffffffffu, v, 3);
+  const double phase_1 = __shfl_sync(0xffffffffu, v, 4);
+  const double ampl = __shfl_sync(0xffffffffu, v, 5);
+
+  // fractional delay at the block centre (delay_correction.cc:40-47, 97-103)
+  const double dis = __dmul_rn(delay_c, (double)s.sample_rate);
+  const int integer_delay = (int)floor(__dadd_rn(dis, 0.5));
+  const double frac = dis - integer_delay;
+  const double tmp1 = -2.0 * M_PI * frac / s.sample_rate;
+  const double tmp2 = M_PI * (integer_delay & (4 * s.oversamp - 1)) / (2 * s.oversamp);
+  const double cterm = tmp2 - tmp1 * 0.5 * s.bandwidth;
+  const double lterm = tmp1 * ((double)s.sample_rate / kNd);
+  // fringe phase over the block (delay_correction.cc:139-160)
+  const double mult = -s.sideband * 2.0 * M_PI;
+  const double lo_phase = s.start_phase + s.lo_offset * time_diff_dev(ct, s.start_ticks);
+  double phi = s.center_freq * delay_0 + lo_phase + phase_0 / (2 * M_PI);
+  const double floor_phi = floor(phi);
+  phi = mult * (phi - floor_phi);
+  double phi_end = s.center_freq * delay_1 + lo_phase + s.fft_len_sec * s.lo_offset + phase_1 / (2 * M_PI);
+  phi_end = mult * (phi_end - floor_phi);
+  const float dphi = (float)((phi_end - phi) / kNd);
+  const float phi0 = (float)phi;
+  const float amp = (float)ampl;
+  // phase ramp start reduced to [0, 2pi) in FP64 before the FP32 per-bin ramp
+  const float c32 = (float)(cterm - 2.0 * M_PI * floor(cterm / (2.0 * M_PI)));
+  const float l32 = (float)lterm;
+
+  // ---- unpack 256 samples through the plan
+  {
+    const int o0 = b * kNd;
+    int si = find_segment(s, o0);
+    for (int q = 0; q < 8; q++) {
+      const int n = lane + 32 * q;
+      xa[n] = gather_sample(s, o0 + n, si);
+    }
+  }
+  __syncwarp();
+  // ---- rfft(256) via a 128-point complex FFT of (x[2n], x[2n+1])
+  float2 *Z = stockham<-1>(A, B, kNd / 2, stw + kNd, lane, 32, WarpSync());
+  float2 *G = (Z == A) ? B : A;
+  for (int k = lane; k <= kNd / 2; k += 32) {
+    const float2 zk = Z[k & (kNd / 2 - 1)];
+    const float2 zc = Z[(kNd / 2 - k) & (kNd / 2 - 1)];
+    const float er = 0.5f * (zk.x + zc.x), ei = 0.5f * (zk.y - zc.y);
+    const float orr = 0.5f * (zk.y + zc.y), oi = -0.5f * (zk.x - zc.x);
+    const float2 w = stw[k & (kNd - 1)];
+    float fr = er + (orr * w.x - oi * w.y);
+    float fi = ei + (orr * w.y + oi * w.x);
+    if (k == 0 || k == kNd / 2) {  // DC and Nyquist halved
+      fr *= 0.5f;
+      fi *= 0.5f;
+    }
+    float sn, cs;
+    sincosf(fmaf((float)k, l32, c32), &sn, &cs);
+    // F * (cos phi, -sin phi)
+    G[k] = make_float2(fr * cs + fi * sn, fi * cs - fr * sn);
+  }
+  for (int k = kNd / 2 + 1 + lane; k < kNd; k += 32) G[k] = make_float2(0.f, 0.f);
+  __syncwarp();
+  float2 *Y = stockham<+1>(G, Z, kNd, stw, lane, 32, WarpSync());
+  // ---- fringe rotation and store
+  float *out = s.ts + (int64_t)bl * kNd;
+  for (int q = 0; q < 8; q++) {
+    const int n = lane + 32 * q;
+    float sn, cs;
+    sincosf(fmaf((float)n, dphi, phi0), &sn, &cs);
+    const float2 z = Y[n];
+    out[n] = z.x * (amp * cs) + z.y * (amp * sn);
+  }
+}
+
+// Unpacked samples only (inspection of the Bit2float_worker output).
+__global__ void unpack_kernel(const StreamDev *__restrict__ streams, float *__restrict__ out) {
+  const StreamDev &s = streams[blockIdx.y];
+  const int o0 = (s.block0 + blockIdx.x) * kNd;
+  if ((int)blockIdx.x >= s.n_blocks) return;
+  int si = find_segment(s, o0 + threadIdx.x);
+  out[(int64_t)blockIdx.x * kNd + threadIdx.x] = gather_sample(s, o0 + threadIdx.x, si);
+}
+
+// Channel extraction: output byte `ob` of subband s packs spb = 8/fan_out
+// samples, first sample in the lowest bits; sample j reads word ob*spb+j.
+// Bit placement follows Channel_extractor_5 (sfxc/src/channel_extractor_5.cc:40-58,
+// 67-99): track t of a sample lands at low_bit << ((t+1) % bits) with low_bit
+// starting at 1 << (8 - fan_out) and advancing by `bits` per complete sample,
+// and each earlier sample is shifted down by fan_out per later sample.
+__global__ void extract_kernel(const uint8_t *__restrict__ in, int64_t nout, int N, int bits, int fan_out,
+                               const int *__restrict__ tracks, uint8_t *__restrict__ out) {
+  const int64_t ob = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int sb = blockIdx.y;
+  if (ob >= nout) return;
+  const int spb = 8 / fan_out;
+  unsigned byte = 0;
+  for (int j = 0; j < spb; j++) {
+    const uint8_t *w = in + (ob * spb + j) * N;
+    unsigned v = 0, low_bit = 1u << (8 - fan_out);
+    for (int t = 0; t < fan_out; t++) {
+      const int tr = tracks[sb * fan_out + t];
+      if ((w[tr >> 3] >> (tr & 7)) & 1) v |= low_bit << ((t + 1) % bits);
+      if ((t + 1) % bits == 0) low_bit <<= bits;
+    }
+    byte |= (v >> ((spb - 1 - j) * fan_out)) & 0xffu;
+  }
+  out[(int64_t)sb * nout + ob] = (uint8_t)byte;
+}
+
+// ------------------------------------------------------------------------
+// F-step, stage 2: windowed real FFT of rot samples per output row.
+template <int OUT_TC>
+__global__ void __launch_bounds__(512) window_fft_kernel(const StreamDev *__restrict__ streams, int row0,
+                                                        int nrows_total, const float *__restrict__ window,
+                                                        const float2 *__restrict__ tw_rot, int nper, int M,
+                                                        int kpad, void *__restrict__ spec_out, float tc_scale) {
+  extern __shared__ float2 dsm[];
+  const StreamDev &s = streams[blockIdx.y];
+  const int r = row0 + blockIdx.x;
+  const int rot = s.rot, half = rot / 2, hop = rot / 2;
+  float2 *A = dsm, *B = dsm + half;
+  float *xa = reinterpret_cast<float *>(A);
+  const float *ts = s.ts + (int64_t)r * hop;
+  for (int i = threadIdx.x; i < rot; i += blockDim.x) {
+    float v = i < nper ? ts[i] * window[i] : 0.0f;
+    if (s.flip && (i & 1)) v = -v;
+    xa[i] = v;
+  }
+  __syncthreads();
+  // tw_rot holds exp(-2 pi i m / rot) for m < rot, followed by the table of the
+  // half-length transform, exp(-2 pi i m / (rot/2)) for m < rot/2.
+  float2 *Z = stockham<-1>(A, B, half, tw_rot + rot, threadIdx.x, blockDim.x, BlockSync());
+  const int stride = kpad;
+  for (int i = threadIdx.x; i <= M; i += blockDim.x) {
+    const int q = s.output_offset + i - s.temp_fft_offset;
+    float fr = 0.f, fi = 0.f;
+    if (q >= 0 && q <= half) {
+      const float2 zk = Z[q & (half - 1)];
+      const float2 zc = Z[(half - q) & (half - 1)];
+      const float er = 0.5f * (zk.x + zc.x), ei = 0.5f * (zk.y - zc.y);
+      const float orr = 0.5f * (zk.y + zc.y), oi = -0.5f * (zk.x - zc.x);
+      const float2 w = tw_rot[q & (rot - 1)];
+      fr = er + (orr * w.x - oi * w.y);
+      fi = ei + (orr * w.y + oi * w.x);
+    }
+    const int64_t idx = ((int64_t)blockIdx.y * nrows_total + r) * stride + i;
+    if (OUT_TC) {
+      const float sr_ = fr * tc_scale, si_ = fi * tc_scale;
+      const __half hr = __float2half_rn(sr_), hi_ = __float2half_rn(si_);
+      const __half lr = __float2half_rn(sr_ - __half2float(hr)), li = __float2half_rn(si_ - __half2float(hi_));
+      __half2 *o = reinterpret_cast<__half2 *>(spec_out) + idx * 2;
+      o[0] = __halves2half2(hr, hi_);
+      o[1] = __halves2half2(lr, li);
+    } else {
+      reinterpret_cast<float2 *>(spec_out)[idx] = make_float2(fr, fi);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// Bit statistics over counted-byte ranges.  Work items: (stream, range, offset).
+__global__ void bitstat_kernel(const StreamDev *__restrict__ streams, const int4 *__restrict__ items, int nitems) {
+  __shared__ unsigned int h[512];
+  for (int i = threadIdx.x; i < 512; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  const int4 it = items[blockIdx.x];  // x = stream, y = range index, z = offset in range, w = count
+  const StreamDev &s = streams[it.x];
+  const DevStatRange rg = s.stats[it.y];
+  for (int j = threadIdx.x; j < it.w; j += blockDim.x) {
+    const int off = it.z + j;
+    const unsigned byte = __ldg(s.src + rg.src_byte + off);
+    int on = 1;
+    if (s.tsys_two_bit) {
+      const int64_t c = (int64_t)rg.cidx + off;
+      on = s.tsys_on0;
+      if (s.tsys_t0 > 0 && c >= s.tsys_t0) {
+        const int64_t flips = s.tsys_period > 0 ? 1 + (c - s.tsys_t0) / s.tsys_period : 1;
+        on ^= (int)(flips & 1);
+      }
+    }
+    atomicAdd(&h[(on ? 0 : 256) + byte], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 512; i += blockDim.x)
+    if (h[i]) atomicAdd(&s.hist[i], (unsigned long long)h[i]);
+}
+
+// ------------------------------------------------------------------------
+// X-step on CUDA cores.  spec: [stream][row][kpad] complex64.  Each thread owns
+// one channel and TPW tiles of 4x4 stream pairs (i in tile row I, j in tile
+// column J, I <= J); blmap[i*npad+j] gives (baseline << 1 | conj) or -1.
+template <int TPW>
+__global__ void __launch_bounds__(384, 1) xcorr_f32_kernel(const float2 *__restrict__ spec, int nrows_total, int kpad,
+                                                        int nstreams, int npad, int r0, int r1, int K,
+                                                        const int *__restrict__ tiles, int ntiles,
+                                                        const int *__restrict__ blmap, float2 *__restrict__ acc) {
+  extern __shared__ float2 xs[];  // [npad][32] for one row
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int k = blockIdx.x * 32 + lane;
+  float2 a[TPW][4][4];
+#pragma unroll
+  for (int t = 0; t < TPW; t++)
+#pragma unroll
+    for (int p = 0; p < 4; p++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) a[t][p][q] = make_float2(0.f, 0.f);
+  int ti[TPW], tj[TPW];
+#pragma unroll
+  for (int t = 0; t < TPW; t++) {
+    const int tile = warp + t * nwarps;
+    ti[t] = tile < ntiles ? tiles[2 * tile] : -1;
+    tj[t] = tile < ntiles ? tiles[2 * tile + 1] : -1;
+  }
+  for (int r = r0; r < r1; r++) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < npad * 32; e += blockDim.x) {
+      const int st = e >> 5, kk = blockIdx.x * 32 + (e & 31);
+      float2 v = make_float2(0.f, 0.f);
+      if (st < nstreams && kk < K) v = spec[((int64_t)st * nrows_total + r) * kpad + kk];
+      xs[e] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < TPW; t++) {
+      if (ti[t] < 0) continue;
+      float2 xi[4], xj[4];
+#pragma unroll
+      for (int p = 0; p < 4; p++) {
+        xi[p] = xs[(ti[t] * 4 + p) * 32 + lane];
+        xj[p] = xs[(tj[t] * 4 + p) * 32 + lane];
+      }
+#pragma unroll
+      for (int p = 0; p < 4; p++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          // x_i * conj(x_j)
+          a[t][p][q].x += xi[p].x * xj[q].x + xi[p].y * xj[q].y;
+          a[t][p][q].y += xi[p].y * xj[q].x - xi[p].x * xj[q].y;
+        }
+    }
+  }
+  if (k >= K) return;
+#pragma unroll
+  for (int t = 0; t < TPW; t++) {
+    if (ti[t] < 0) continue;
+#pragma unroll
+    for (int p = 0; p < 4; p++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int i = ti[t] * 4 + p, j = tj[t] * 4 + q;
+        const int m = blmap[i * npad + j];
+        if (m < 0) continue;
+        float2 *dst = acc + (int64_t)(m >> 1) * kpad + k;
+        const float2 v = a[t][p][q];
+        float2 o = *dst;
+        o.x += v.x;
+        o.y += (m & 1) ? -v.y : v.y;
+        *dst = o;
+      }
+  }
+}
+
+// ------------------------------------------------------------------------
+// Pulsar bins (Correlation_core_pulsar::dedisperse_buffer) in FP64, evaluated
+// with the reference's operation order so that every bin matches.
+__global__ void pulsar_bins_kernel(int nrows, int K, double start_phase, double rate_term, double fft_duration,
+                                   const double *__restrict__ offsets, double g0, double g1, int nbins,
+                                   int16_t *__restrict__ bins) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (k >= K || r >= nrows) return;
+  const double us_per_day = 86400000000.0;
+  // start_phase + (coef[1] + 60 F0) * fft_duration * current_fft * 1440 / us_per_day
+  double ph = __dmul_rn(rate_term, fft_duration);
+  ph = __dmul_rn(ph, (double)r);
+  ph = __dmul_rn(ph, 1440.0);
+  ph = __ddiv_rn(ph, us_per_day);
+  ph = __dadd_rn(start_phase, ph);
+  double p = __dsub_rn(ph, offsets[k]);
+  p = __dsub_rn(p, floor(p));
+  const double len = __dsub_rn(g1, g0);
+  int bin;
+  if (p >= g0) {
+    bin = p < g1 ? (int)__ddiv_rn(__dmul_rn(__dsub_rn(p, g0), (double)(nbins - 1)), len) + 1 : 0;
+  } else if (__dadd_rn(p, 1.0) < g1) {
+    bin = (int)__ddiv_rn(__dmul_rn(__dsub_rn(__dadd_rn(p, 1.0), g0), (double)(nbins - 1)), len) + 1;
+  } else {
+    bin = 0;
+  }
+  bins[(int64_t)r * K + k] = (int16_t)bin;
+}
+
+// Binned X-step: like xcorr_f32_kernel, but each thread keeps its register
+// tile while its channel's bin is unchanged and adds it into acc[bin] when
+// the bin changes (each (bin, baseline, channel) has a single owner thread).
+template <int TPW>
+__global__ void __launch_bounds__(384, 1) xcorr_f32_pulsar_kernel(
+    const float2 *__restrict__ spec, int nrows_total, int kpad, int nstreams, int npad, int r0, int r1, int K,
+    const int *__restrict__ tiles, int ntiles, const int *__restrict__ blmap, int nbl, const int16_t *__restrict__ bins,
+    float2 *__restrict__ acc) {
+  extern __shared__ float2 xs[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int k = blockIdx.x * 32 + lane;
+  float2 a[TPW][4][4];
+  int ti[TPW], tj[TPW];
+#pragma unroll
+  for (int t = 0; t < TPW; t++) {
+    const int tile = warp + t * nwarps;
+    ti[t] = tile < ntiles ? tiles[2 * tile] : -1;
+    tj[t] = tile < ntiles ? tiles[2 * tile + 1] : -1;
+#pragma unroll
+    for (int p = 0; p < 4; p++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) a[t][p][q] = make_float2(0.f, 0.f);
+  }
+  auto flush = [&](int bin) {
+    if (k >= K || bin < 0) return;
+#pragma unroll
+    for (int t = 0; t < TPW; t++) {
+      if (ti[t] < 0) continue;
+#pragma unroll
+      for (int p = 0; p < 4; p++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const int m = blmap[(ti[t] * 4 + p) * npad + tj[t] * 4 + q];
+          if (m >= 0) {
+            float2 *dst = acc + ((int64_t)bin * nbl + (m >> 1)) * kpad + k;
+            float2 o = *dst;
+            o.x += a[t][p][q].x;
+            o.y += (m & 1) ? -a[t][p][q].y : a[t][p][q].y;
+            *dst = o;
+          }
+          a[t][p][q] = make_float2(0.f, 0.f);
+        }
+    }
+  };
+  int cur = -1;
+  for (int r = r0; r < r1; r++) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < npad * 32; e += blockDim.x) {
+      const int st = e >> 5, kk = blockIdx.x * 32 + (e & 31);
+      float2 v = make_float2(0.f, 0.f);
+      if (st < nstreams && kk < K) v = spec[((int64_t)st * nrows_total + r) * kpad + kk];
+      xs[e] = v;
+    }
+    __syncthreads();
+    const int bin = k < K ? bins[(int64_t)r * K + k] : -1;
+    if (bin != cur) {
+      flush(cur);
+      cur = bin;
+    }
+#pragma unroll
+    for (int t = 0; t < TPW; t++) {
+      if (ti[t] < 0) continue;
+      float2 xi[4], xj[4];
+#pragma unroll
+      for (int p = 0; p < 4; p++) {
+        xi[p] = xs[(ti[t] * 4 + p) * 32 + lane];
+        xj[p] = xs[(tj[t] * 4 + p) * 32 + lane];
+      }
+#pragma unroll
+      for (int p = 0; p < 4; p++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          a[t][p][q].x += xi[p].x * xj[q].x + xi[p].y * xj[q].y;
+          a[t][p][q].y += xi[p].y * xj[q].x - xi[p].x * xj[q].y;
+        }
+    }
+  }
+  flush(cur);
+}
+
+// ------------------------------------------------------------------------
+// Normalisation.  norms[i] = max(1, sum_k Re acc[auto_i][k] / M) in FP64.
+__global__ void norm_autos_kernel(const float2 *__restrict__ acc, int kpad, int M, int nstreams, double *norms) {
+  __shared__ double red[256];
+  const int i = blockIdx.x;
+  double s = 0.0;
+  for (int k = threadIdx.x; k <= M; k += blockDim.x) s += (double)acc[(int64_t)i * kpad + k].x;
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double n = red[0] / M;
+    norms[i] = n < 1 ? 1 : n;
+  }
+}
+
+// out[b][k] (compact M+1) = normalised visibility; flagfac[b] = N1*N2 (crosses).
+__global__ void normalize_kernel(const float2 *__restrict__ acc, int kpad, int M, int nstreams, int nbl,
+                                 const int *__restrict__ bl, const double *__restrict__ norms,
+                                 const double *__restrict__ flagfac, float2 *__restrict__ out) {
+  const int b = blockIdx.y;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k > M) return;
+  const float2 v = acc[(int64_t)b * kpad + k];
+  float2 o;
+  if (b < nstreams) {
+    o = make_float2((float)((double)v.x / norms[b]), 0.f);
+  } else {
+    const double n = flagfac[b];
+    const float norm = (float)sqrt(n * norms[bl[2 * b]] * norms[bl[2 * b + 1]]);
+    o = make_float2(v.x / norm, v.y / norm);
+  }
+  out[(int64_t)b * (M + 1) + k] = o;
+}
+
+// ------------------------------------------------------------------------
+// launchers
+void launch_fstep_block(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256,
+                        cudaStream_t st) {
+  dim3 grid((max_blocks + 7) / 8, nstreams);
+  fstep_block_kernel<<<grid, 256, 0, st>>>(d_streams, tw256);
+}
+
+void launch_unpack(const StreamDev *d_streams, int nstreams, int max_blocks, float *out, cudaStream_t st) {
+  unpack_kernel<<<dim3(max_blocks, nstreams), kNd, 0, st>>>(d_streams, out);
+}
+
+void launch_extract(const uint8_t *in, int64_t nout, int N, int bits, int nsub, int fan_out, const int *tracks,
+                    uint8_t *out, cudaStream_t st) {
+  extract_kernel<<<dim3((unsigned)((nout + 255) / 256), nsub), 256, 0, st>>>(in, nout, N, bits, fan_out, tracks, out);
+}
+
+void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
+                       const float *window, const float2 *tw_rot, int rot, int nper, int M, int kpad, void *spec,
+                       bool tc, float tc_scale, cudaStream_t st) {
+  dim3 grid(nrows, nstreams);
+  const size_t smem = (size_t)rot * sizeof(float2);  // two buffers of rot/2
+  if (tc) {
+    cudaFuncSetAttribute(window_fft_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    window_fft_kernel<1><<<grid, 512, smem, st>>>(d_streams, row0, nrows_total, window, tw_rot, nper, M, kpad, spec,
+                                                  tc_scale);
+  } else {
+    cudaFuncSetAttribute(window_fft_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    window_fft_kernel<0><<<grid, 512, smem, st>>>(d_streams, row0, nrows_total, window, tw_rot, nper, M, kpad, spec,
+                                                  tc_scale);
+  }
+}
+
+void launch_bitstat(const StreamDev *d_streams, const int4 *d_items, int nitems, cudaStream_t st) {
+  if (nitems > 0) bitstat_kernel<<<nitems, 256, 0, st>>>(d_streams, d_items, nitems);
+}
+
+static int xcorr_threads(int ntiles, int tpw) {
+  int warps = (ntiles + tpw - 1) / tpw;
+  if (warps < 1) warps = 1;
+  return warps * 32;
+}
+
+int xcorr_tpw(int ntiles) {
+  // registers per thread grow with TPW: the smallest TPW that fits 12 warps
+  for (int t = 1; t <= 4; t++)
+    if ((ntiles + t - 1) / t <= 12) return t;
+  return -1;
+}
+
+void launch_xcorr_f32(const float2 *spec, int nrows_total, int kpad, int nstreams, int npad, int r0, int r1, int K,
+                      const int *tiles, int ntiles, const int *blmap, float2 *acc, cudaStream_t st) {
+  const int tpw = xcorr_tpw(ntiles);
+  const int threads = xcorr_threads(ntiles, tpw);
+  const dim3 grid((K + 31) / 32);
+  const size_t smem = (size_t)npad * 32 * sizeof(float2);
+  switch (tpw) {
+    case 1: xcorr_f32_kernel<1><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, r0, r1, K, tiles, ntiles, blmap, acc); break;
+    case 2: xcorr_f32_kernel<2><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, r0, r1, K, tiles, ntiles, blmap, acc); break;
+    case 3: xcorr_f32_kernel<3><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, r0, r1, K, tiles, ntiles, blmap, acc); break;
+    default: xcorr_f32_kernel<4><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, r0, r1, K, tiles, ntiles, blmap, acc); break;
+  }
+}
+
+void launch_pulsar(const float2 *spec, int nrows_total, int kpad, int nstreams, int npad, int nrows, int K,
+                   const int *tiles, int ntiles, const int *blmap, int nbl, double start_phase, double rate_term,
+                   double fft_duration, const double *offsets, double g0, double g1, int nbins, int16_t *bins,
+                   float2 *acc, cudaStream_t st) {
+  pulsar_bins_kernel<<<dim3((K + 127) / 128, nrows), 128, 0, st>>>(nrows, K, start_phase, rate_term, fft_duration,
+                                                                  offsets, g0, g1, nbins, bins);
+  const int tpw = xcorr_tpw(ntiles);
+  const int threads = xcorr_threads(ntiles, tpw);
+  const dim3 grid((K + 31) / 32);
+  const size_t smem = (size_t)npad * 32 * sizeof(float2);
+  switch (tpw) {
+    case 1: xcorr_f32_pulsar_kernel<1><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, 0, nrows, K, tiles, ntiles, blmap, nbl, bins, acc); break;
+    case 2: xcorr_f32_pulsar_kernel<2><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, 0, nrows, K, tiles, ntiles, blmap, nbl, bins, acc); break;
+    case 3: xcorr_f32_pulsar_kernel<3><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, 0, nrows, K, tiles, ntiles, blmap, nbl, bins, acc); break;
+    default: xcorr_f32_pulsar_kernel<4><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, 0, nrows, K, tiles, ntiles, blmap, nbl, bins, acc); break;
+  }
+}
+
+void launch_normalize(const float2 *acc, int kpad, int M, int nstreams, int nbl, const int *bl, double *norms,
+                      const double *flagfac, float2 *out, cudaStream_t st) {
+  norm_autos_kernel<<<nstreams, 256, 0, st>>>(acc, kpad, M, nstreams, norms);
+  normalize_kernel<<<dim3((M + 1 + 255) / 256, nbl), 256, 0, st>>>(acc, kpad, M, nstreams, nbl, bl, norms, flagfac,
+                                                                    out);
+}
+
+}  // namespace sfxc

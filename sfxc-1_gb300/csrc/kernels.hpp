@@ -1,0 +1,29 @@
+// Launch wrappers of the correlator-node kernels (kernels.cu, xcorr_tc.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace sfxc {
+
+void launch_fstep_block(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256_128,
+                        cudaStream_t st);
+void launch_unpack(const StreamDev *d_streams, int nstreams, int max_blocks, float *out, cudaStream_t st);
+void launch_extract(const uint8_t *in, int64_t nout, int N, int bits, int nsub, int fan_out, const int *tracks,
+                    uint8_t *out, cudaStream_t st);
+void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
+                       const float *window, const float2 *tw_rot, int rot, int nper, int M, int kpad, void *spec,
+                       bool tc, float tc_scale, cudaStream_t st);
+void launch_bitstat(const StreamDev *d_streams, const int4 *d_items, int nitems, cudaStream_t st);
+int xcorr_tpw(int ntiles);
+void launch_xcorr_f32(const float2 *spec, int nrows_total, int kpad, int nstreams, int npad, int r0, int r1, int K,
+                      const int *tiles, int ntiles, const int *blmap, float2 *acc, cudaStream_t st);
+void launch_pulsar(const float2 *spec, int nrows_total, int kpad, int nstreams, int npad, int nrows, int K,
+                   const int *tiles, int ntiles, const int *blmap, int nbl, double start_phase, double rate_term,
+                   double fft_duration, const double *offsets, double g0, double g1, int nbins, int16_t *bins,
+                   float2 *acc, cudaStream_t st);
+void launch_normalize(const float2 *acc, int kpad, int M, int nstreams, int nbl, const int *bl, double *norms,
+                      const double *flagfac, float2 *out, cudaStream_t st);
+
+}  // namespace sfxc

@@ -1,0 +1,214 @@
+"""Host-side interface of the GB300 correlator-node path.
+
+Mirrors the reference's correlator-node task interface: a
+`CorrelatorNode` takes the Correlation_parameters of a job (set_parameters,
+sfxc/src/correlator_node.cc:311-406), receives each stream's byte protocol as
+the input-node writer produced it (push_protocol; the reference's
+Channel_circular_input_buffer), and correlates one integration at a time,
+handing the output bytes to a writer (Data_writer::put_bytes) and the tsys
+records to the output node.  Errors raise SfxcError with the library's
+status code, where the reference would abort (sfxc/src/utils.cc:44-90).
+
+Input-node helpers (`delay_list`, `write_protocol`, `extract_channels`)
+expose Input_node_tasklet::get_delays, Input_node_data_writer and the channel
+extractor through the same library.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import lib as L
+
+
+def _bytes_ptr(b):
+    arr = (C.c_uint8 * len(b)).from_buffer_copy(b) if len(b) else (C.c_uint8 * 1)()
+    return arr
+
+
+class CorrelatorNode:
+    """One CUDA context on one device.  x_mode: L.X_FP32 or L.X_TC_HILO."""
+
+    def __init__(self, device=0, x_mode=L.X_FP32):
+        self._lib = L.load()
+        cfg = L.Config(device, x_mode)
+        self._h = self._lib.sfxc_gpu_create(C.byref(cfg))
+        if not self._h:
+            raise L.SfxcError(L.ECUDA, self._lib.sfxc_gpu_global_error().decode())
+        self._keep = []
+
+    def close(self):
+        if self._h:
+            self._lib.sfxc_gpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc < 0:
+            raise L.SfxcError(rc, self._lib.sfxc_gpu_last_error(self._h).decode())
+        return rc
+
+    # ------------------------------------------------------------------
+    def set_parameters(self, job):
+        """job: dict with the keys of oracle/jobs.correlate (the same dicts
+        drive the reference checker, the C restatement and this library)."""
+        keep = []
+        tables = (L.DelayTable * len(job["del_bytes"]))()
+        for k, db in enumerate(job["del_bytes"]):
+            buf = _bytes_ptr(db)
+            keep.append(buf)
+            clock = job.get("clocks", [None] * len(job["del_bytes"]))[k]
+            off, rate, epoch = clock if clock is not None else (0.0, 0.0, 0)
+            tables[k] = L.DelayTable(C.cast(buf, C.POINTER(C.c_uint8)), len(db), off, rate, epoch)
+        streams = (L.StationStream * len(job["streams"]))()
+        for i, s in enumerate(job["streams"]):
+            (station_number, station_stream, sr, cf, bw, sb, pol, bits, lo, tsys_freq, table) = s
+            streams[i] = L.StationStream(station_number, station_stream, sr, bw, bits, tsys_freq, cf,
+                                         sb.encode(), pol.encode(), b"\0\0", table, lo)
+        p = L.CorrelationParams()
+        p.experiment_start_ticks = job["experiment_start_ticks"]
+        p.start_ticks = job["start_ticks"]
+        p.integration_time_us = job["integration_time_us"]
+        p.sub_integration_time_us = job["sub_integration_time_us"]
+        p.number_channels = job["number_channels"]
+        p.fft_size_delaycor = job["fft_size_delaycor"]
+        p.fft_size_correlation = job["fft_size_correlation"]
+        p.sample_rate = job["sample_rate"]
+        p.bandwidth = job["bandwidth"]
+        p.frequency_nr = job["frequency_nr"]
+        p.channel_freq = job["channel_freq"]
+        p.sideband = job["sideband"].encode()
+        p.polarisation = job["polarisation"].encode()
+        p.cross_polarize = job["cross_polarize"]
+        p.reference_station = job["reference_station"]
+        p.window = job["window"]
+        p.integration_nr = job["integration_nr"]
+        p.n_streams = len(job["streams"])
+        p.streams = streams
+        p.n_delay_tables = len(job["del_bytes"])
+        p.delay_tables = tables
+        if "pulsar" in job:
+            nb, g0, g1 = job["pulsar"]
+            p.pulsar_nbins = int(nb)
+            p.gate_start = float(g0)
+            p.gate_stop = float(g1)
+            pcs = (L.Polyco * len(job["polyco"]))()
+            for k, pc in enumerate(job["polyco"]):
+                coef = (C.c_double * (len(pc) - 5))(*pc[5:])
+                keep.append(coef)
+                pcs[k] = L.Polyco(pc[0], pc[1], pc[2], pc[3], pc[4], len(pc) - 5, coef)
+            p.n_polyco = len(job["polyco"])
+            p.polyco = pcs
+            keep.append(pcs)
+        keep += [tables, streams]
+        self._check(self._lib.sfxc_gpu_set_parameters(self._h, C.byref(p)))
+        self._keep = keep
+        self.nstreams = len(job["streams"])
+        self.job = job
+
+    def push_protocol(self, stream, data):
+        buf = _bytes_ptr(data)
+        self._check(self._lib.sfxc_gpu_push_protocol(self._h, stream, buf, len(data)))
+
+    def run_integration(self):
+        """Returns (output bytes, [tsys record bytes per stream])."""
+        out, tsys = [], []
+
+        def sink(user, kind, data, n):
+            b = C.string_at(data, n)
+            (out if kind == 0 else tsys).append(b)
+            return 0
+
+        cb = L.SINK(sink)
+        self._check(self._lib.sfxc_gpu_run_integration(self._h, cb, None))
+        return b"".join(out), tsys
+
+    def correlate(self, job):
+        """Run every integration of a job dict; returns (cor bytes, tsys bytes)."""
+        self.set_parameters(job)
+        cor, tsys = [], []
+        for it in range(int(job["n_integrations"])):
+            for k in range(self.nstreams):
+                self.push_protocol(k, job["protocols"][k][it])
+            o, t = self.run_integration()
+            cor.append(o)
+            tsys += t
+        return b"".join(cor), b"".join(tsys)
+
+    def unpacked(self, stream, n):
+        out = np.empty(n, dtype=np.float32)
+        self._check(self._lib.sfxc_gpu_copy_unpacked(self._h, stream, out.ctypes.data, n))
+        return out
+
+    def spectra(self, stream, nrows, nchan):
+        out = np.empty((nrows, nchan + 1), dtype=np.complex64)
+        self._check(self._lib.sfxc_gpu_copy_spectra(self._h, stream, out.ctypes.data, out.size * 2))
+        return out
+
+    def timings(self):
+        t = (C.c_float * 5)()
+        self._check(self._lib.sfxc_gpu_last_timings(self._h, t))
+        return {"unpack_fringe_ms": t[0], "window_fft_ms": t[1], "xstep_ms": t[2], "normalise_ms": t[3],
+                "total_ms": t[4]}
+
+    def extract_channels(self, words, word_bytes, bits, tracks):
+        """Channel_extractor semantics on the GPU.  tracks: list per subband."""
+        nsub, fan_out = len(tracks), len(tracks[0])
+        flat = (C.c_int32 * (nsub * fan_out))(*[t for tr in tracks for t in tr])
+        w = np.ascontiguousarray(np.frombuffer(bytes(words), dtype=np.uint8))
+        nwords = w.size // word_bytes
+        out = np.empty(nsub * (nwords * fan_out // 8), dtype=np.uint8)
+        self._check(self._lib.sfxc_gpu_extract_channels(self._h, w.ctypes.data, nwords, word_bytes, bits, nsub,
+                                                        fan_out, flat, out.ctypes.data))
+        per = nwords * fan_out // 8
+        return [out[i * per:(i + 1) * per].tobytes() for i in range(nsub)]
+
+
+def delay_list(del_bytes, start_ticks, stop_ticks, sample_rate, bits, clock=(0.0, 0.0, 0), capacity=1 << 20):
+    lib = L.load()
+    buf = _bytes_ptr(del_bytes)
+    t = L.DelayTable(C.cast(buf, C.POINTER(C.c_uint8)), len(del_bytes), clock[0], clock[1], clock[2])
+    ticks = (C.c_int64 * capacity)()
+    by = (C.c_int32 * capacity)()
+    rem = (C.c_int32 * capacity)()
+    n = lib.sfxc_gpu_delay_list(C.byref(t), start_ticks, stop_ticks, sample_rate, bits, ticks, by, rem, capacity)
+    if n < 0:
+        raise L.SfxcError(n, lib.sfxc_gpu_global_error().decode())
+    return [(ticks[i], by[i], rem[i]) for i in range(n)]
+
+
+def write_protocol(blocks, slices, sample_rate, bits, integration_time_us):
+    """blocks: [(start_ticks, bytes, [(begin, n), ...])]; slices: [(start, stop, nr_samples, delays)].
+    Returns the protocol bytes of each slice."""
+    lib = L.load()
+    stream = b"".join(bytes(b[1]) for b in blocks)
+    keep = []
+    cb = (L.ChannelBlock * len(blocks))()
+    for i, (st, data, inv) in enumerate(blocks):
+        arr = (C.c_int32 * max(1, 2 * len(inv)))(*[x for pr in inv for x in pr])
+        keep.append(arr)
+        cb[i] = L.ChannelBlock(st, len(data), len(inv), arr)
+    sl = (L.Slice * len(slices))()
+    for i, (s0, s1, ns, dl) in enumerate(slices):
+        tk = (C.c_int64 * len(dl))(*[d[0] for d in dl])
+        by = (C.c_int32 * len(dl))(*[d[1] for d in dl])
+        rm = (C.c_int32 * len(dl))(*[d[2] for d in dl])
+        keep += [tk, by, rm]
+        sl[i] = L.Slice(s0, s1, ns, len(dl), tk, by, rm)
+    sbuf = _bytes_ptr(stream)
+    offs = (C.c_int64 * (len(slices) + 1))()
+    need = lib.sfxc_gpu_write_protocol(sbuf, len(blocks), cb, len(slices), sl, sample_rate, bits,
+                                       integration_time_us, None, 0, offs)
+    if need < 0:
+        raise L.SfxcError(int(need), lib.sfxc_gpu_global_error().decode())
+    out = (C.c_uint8 * max(1, need))()
+    n = lib.sfxc_gpu_write_protocol(sbuf, len(blocks), cb, len(slices), sl, sample_rate, bits,
+                                    integration_time_us, out, need, offs)
+    if n < 0:
+        raise L.SfxcError(int(n), lib.sfxc_gpu_global_error().decode())
+    raw = bytes(out)[:n]
+    return [raw[offs[i]:offs[i + 1]] for i in range(len(slices))]

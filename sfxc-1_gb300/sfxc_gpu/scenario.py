@@ -1,0 +1,176 @@
+"""Seeded synthetic correlator jobs: delay tables, channel streams and input-node
+protocols for a set of station streams, packaged as the job dicts consumed by
+CorrelatorNode.correlate (and by the checkers in oracle/, which take the same
+dicts).
+
+A scenario describes one subband job: stations with delay polynomials and
+gains, the streams (station x polarisation) with their sampling, and the
+correlation setup.  Channel data are generated per polarisation with a common
+sky signal (synth.generate_station_samples), quantised, packed LSB-first and
+cut into input-node blocks; optional invalid runs mark blocks like invalid
+VDIF frames.  The integer delays and the byte protocol come from pluggable
+functions so the same scenario can be run through the reference's own input
+node (oracle/jobs.py), the C restatement or this library.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import synth, timebase
+
+
+@dataclass
+class Station:
+    name: str
+    number: int
+    poly: synth.DelayPoly
+    gain: float = 1.0
+
+
+@dataclass
+class Scenario:
+    stations: list
+    pols: tuple = ("R",)
+    sample_rate: int = 32_000_000
+    bandwidth: int = 16_000_000
+    bits: int = 2
+    channel_freq: int = 1_600_000_000
+    sideband: str = "U"
+    station_sidebands: dict = field(default_factory=dict)  # station number -> sideband
+    nchan: int = 512
+    window: int = 4
+    integration_us: int = 15625
+    sub_integration_us: int = 125000
+    n_integrations: int = 2
+    lead_us: int = 4000                 # recording start -> first integration
+    rho: float = 0.05
+    seed: int = 1
+    tones: list = field(default_factory=list)
+    block_bytes: int = 32000            # channel bytes per input-node block
+    invalid: dict = field(default_factory=dict)  # (station number, pol) -> [(block, begin, n)]
+    mjd: int = 60000
+    sec0: int = 36000                   # recording start, seconds of day
+    lo_offset: float = 0.0
+    tsys_freq: int = 80
+    reference_station: int = -1
+    frequency_nr: int = 0
+
+    def streams(self):
+        """(station index, pol) in correlator order: stations outer, pols inner."""
+        return [(si, pol) for si in range(len(self.stations)) for pol in self.pols]
+
+
+def del_tables(sc: Scenario):
+    return [synth.del_file_bytes(st.name[:2], [("SRC", sc.mjd, sc.sec0 - 20, 140, st.poly)]) for st in sc.stations]
+
+
+def channel_streams(sc: Scenario, fast_random=False):
+    """Packed channel bytes per stream, covering the job plus delay margins."""
+    sr, bits = sc.sample_rate, sc.bits
+    int_samples = sc.integration_us * sr // 1_000_000
+    span = sc.lead_us * sr // 1_000_000 + sc.n_integrations * int_samples
+    max_tau = max(abs(float(st.poly.delay(sc.sec0 + sc.lead_us * 1e-6))) for st in sc.stations)
+    tail = int(max_tau * sr) + 4 * (sc.block_bytes * 8 // bits)
+    nsamp = span + tail
+    spb_block = sc.block_bytes * 8 // bits
+    nsamp = (nsamp + spb_block - 1) // spb_block * spb_block
+    out = {}
+    for pi, pol in enumerate(sc.pols):
+        if fast_random:
+            rng = np.random.Generator(np.random.PCG64(sc.seed * 7919 + pi))
+            for si in range(len(sc.stations)):
+                out[(si, pol)] = rng.integers(0, 256, size=nsamp * bits // 8, dtype=np.uint8)
+            continue
+        sub = synth.SubbandSignal(sample_rate=sr, f_lo=float(sc.channel_freq), rho=sc.rho,
+                                  seed=sc.seed * 100 + pi, tones=list(sc.tones))
+        sigs = [synth.StationSignal(st.poly, st.gain) for st in sc.stations]
+        xs = synth.generate_station_samples(sub, sigs, float(sc.sec0), nsamp)
+        for si, x in enumerate(xs):
+            out[(si, pol)] = synth.pack_codes(synth.quantise(x, bits), bits)
+    return out, nsamp
+
+
+def blocks_of(sc: Scenario, stream_bytes, key):
+    """Input-node blocks of one channel stream: (start ticks, bytes, invalid runs)."""
+    rec0 = timebase.ticks_from_mjd_sec(sc.mjd, sc.sec0)
+    tps = timebase.ticks_per_sample(sc.sample_rate)
+    spb_block = sc.block_bytes * 8 // sc.bits
+    nb = len(stream_bytes) // sc.block_bytes
+    inv = {}
+    for (b, begin, n) in sc.invalid.get((sc.stations[key[0]].number, key[1]), []):
+        inv.setdefault(b, []).append((begin, n))
+    return [(rec0 + b * spb_block * tps, bytes(stream_bytes[b * sc.block_bytes:(b + 1) * sc.block_bytes]),
+             inv.get(b, [])) for b in range(nb)]
+
+
+def job_timing(sc: Scenario):
+    rec0 = timebase.ticks_from_mjd_sec(sc.mjd, sc.sec0)
+    start = rec0 + timebase.ticks_from_usec(sc.lead_us)
+    tint = timebase.ticks_from_usec(sc.integration_us)
+    nr = timebase.nr_ffts_per_integration_slice(sc.integration_us, sc.sample_rate, max(256, sc.nchan))
+    slice_samples = nr * max(256, sc.nchan)
+    return rec0, start, tint, slice_samples
+
+
+def build_job(sc: Scenario, delay_fn, protocol_fn, fast_random=False):
+    """Complete job dict.  delay_fn(del_bytes, s0, s1, sample_rate, bits) -> delay list;
+    protocol_fn(blocks, slices, sample_rate, bits, integration_us) -> [bytes per slice]."""
+    dels = del_tables(sc)
+    chans, _ = channel_streams(sc, fast_random=fast_random)
+    rec0, start, tint, slice_samples = job_timing(sc)
+    streams, protos = [], []
+    for k, (si, pol) in enumerate(sc.streams()):
+        st = sc.stations[si]
+        slices = []
+        for it in range(sc.n_integrations):
+            s0 = start + it * tint
+            s1 = s0 + tint
+            slices.append((s0, s1, slice_samples, delay_fn(dels[si], s0, s1, sc.sample_rate, sc.bits)))
+        blocks = blocks_of(sc, chans[(si, pol)], (si, pol))
+        protos.append(protocol_fn(blocks, slices, sc.sample_rate, sc.bits, sc.integration_us))
+        sb = sc.station_sidebands.get(st.number, sc.sideband)
+        # A station recording the job's sky band in the other sideband has its LO
+        # at the opposite band edge (Delay_correction::set_parameters then finds
+        # a zero channel offset, sfxc/src/delay_correction.cc:226-241).
+        cf = sc.channel_freq
+        if sb != sc.sideband:
+            cf += sc.bandwidth if sc.sideband == "U" else -sc.bandwidth
+        streams.append((st.number, k, sc.sample_rate, cf, sc.bandwidth, sb, pol, sc.bits,
+                        sc.lo_offset, sc.tsys_freq, si))
+    return dict(del_bytes=dels, experiment_start_ticks=rec0, start_ticks=start,
+                integration_time_us=sc.integration_us, sub_integration_time_us=sc.sub_integration_us,
+                number_channels=sc.nchan, fft_size_delaycor=256, fft_size_correlation=max(256, sc.nchan),
+                sample_rate=sc.sample_rate, channel_freq=sc.channel_freq, bandwidth=sc.bandwidth,
+                sideband=sc.sideband, frequency_nr=sc.frequency_nr, polarisation=sc.pols[0],
+                cross_polarize=1 if len(sc.pols) > 1 else 0, reference_station=sc.reference_station,
+                window=sc.window, source="SRC", integration_nr=0, n_integrations=sc.n_integrations,
+                streams=streams, protocols=protos)
+
+
+def c1_plain(integration_us=15625, n_integrations=2, seed=1):
+    """The plain CPU-runnable configuration, shortened: 2 stations, 1 subband of
+    16 MHz at 32 MS/s, 2-bit, single pol; station 2 delayed by 37.25 samples
+    with a rate of 1e-7 s/s; sky frequency 1.6 GHz; 512 channels."""
+    sr = 32_000_000
+    st = [Station("Aa", 0, synth.DelayPoly(coeffs=(0.0,), t0=36000.0)),
+          Station("Bb", 1, synth.DelayPoly(coeffs=(37.25 / sr, 1e-7), t0=36000.0))]
+    return Scenario(stations=st, sample_rate=sr, bandwidth=16_000_000, bits=2, channel_freq=1_600_000_000,
+                    nchan=512, integration_us=integration_us, n_integrations=n_integrations, rho=0.01,
+                    seed=seed)
+
+
+def cubic_stations(n, seed, max_delay=15e-3, max_rate=3e-6, t0=36000.0, gains=None):
+    """n stations with seeded cubic delay polynomials (|tau| <= max_delay, |rate| <= max_rate)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(n):
+        c0 = rng.uniform(-max_delay, max_delay)
+        c1 = rng.uniform(-max_rate, max_rate)
+        c2 = rng.uniform(-1e-9, 1e-9)
+        c3 = rng.uniform(-1e-13, 1e-13)
+        g = 1.0 if gains is None else gains[i]
+        out.append(Station("S%d" % i, i, synth.DelayPoly(coeffs=(c0, c1, c2, c3), t0=t0), g))
+    return out

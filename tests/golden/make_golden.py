@@ -1,0 +1,127 @@
+"""Generate the golden fixtures in tests/golden/ from the reference's own classes.
+
+Run here, where the reference checkout exists:  python tests/golden/make_golden.py
+The reference correlator-node classes are compiled by oracle/build_ref.py and
+driven by oracle/ref_harness.cc; inputs are seeded synthetic scenarios
+(sfxc_gpu.scenario).  Each fixture stores the inputs the reference consumed
+(delay tables, channel streams) and what it produced: integer delay lists,
+digests of the input-node protocol bytes and of the unpacked samples, a sample of the delay-
+corrected spectra, the correlator output bytes, statistics and tsys records.
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "sfxc-1_gb300"))
+sys.path.insert(0, ROOT)
+
+from oracle import jobs  # noqa: E402
+from sfxc_gpu import scenario, synth  # noqa: E402
+
+
+def ref_delays(*a):
+    return jobs.delays(*a)[0]
+
+
+def scenarios():
+    out = {}
+    out["c1_plain"] = scenario.c1_plain(integration_us=15625, n_integrations=2, seed=1)
+    # three stations x two polarisations, large delay rates (integer-delay changes inside
+    # the integrations), one lower-sideband station (sideband flip), invalid runs
+    st = scenario.cubic_stations(3, seed=11, max_delay=2e-3, max_rate=3e-5)
+    out["multi"] = scenario.Scenario(
+        stations=st, pols=("R", "L"), sample_rate=64_000_000, bandwidth=32_000_000, bits=2,
+        channel_freq=4_800_000_000, station_sidebands={2: "L"}, nchan=256, integration_us=4000,
+        n_integrations=3, sub_integration_us=1000, lead_us=3000, rho=0.05, seed=5, block_bytes=2000,
+        invalid={(1, "R"): [(6, 100, 300)], (0, "L"): [(9, 0, 2000), (10, 0, 500)]})
+    # 1-bit streams
+    st1 = scenario.cubic_stations(2, seed=3, max_delay=1e-3, max_rate=1e-5)
+    out["onebit"] = scenario.Scenario(
+        stations=st1, sample_rate=32_000_000, bandwidth=16_000_000, bits=1, channel_freq=1_400_000_000,
+        nchan=512, integration_us=8000, n_integrations=2, rho=0.1, seed=9, block_bytes=4000)
+    # pulsar binning
+    stp = scenario.cubic_stations(2, seed=21, max_delay=1e-4, max_rate=1e-6)
+    out["pulsar"] = scenario.Scenario(
+        stations=stp, sample_rate=32_000_000, bandwidth=16_000_000, bits=2, channel_freq=1_400_000_000,
+        nchan=256, integration_us=8000, n_integrations=1, rho=0.05, seed=13, block_bytes=8000)
+    return out
+
+
+# two polycos (the closer one is used), non-zero phase polynomial
+PULSAR = dict(nbins=8, gate=(0.2, 0.9),
+              polyco=[(60000.0 + 36000.0 / 86400 - 0.01, 56.8, 0.25, 1 / 0.0334, 1400.0,
+                       0.013, 0.0021, 1.3e-5, -2.2e-7, 4e-9) + (0.0,) * 7,
+                      (60000.0 + 36000.0 / 86400 + 0.2, 56.8, 0.5, 1 / 0.0334, 1400.0) + (0.0,) * 12])
+
+
+def make(name, sc):
+    dels = scenario.del_tables(sc)
+    chans, _ = scenario.channel_streams(sc)
+    rec0, start, tint, slice_samples = scenario.job_timing(sc)
+    rec = {"del_bytes": np.array([np.frombuffer(d, np.uint8) for d in dels], dtype=object)}
+    job = scenario.build_job(sc, ref_delays, jobs.protocol)
+    if name == "pulsar":
+        job["pulsar"] = (PULSAR["nbins"],) + PULSAR["gate"]
+        job["polyco"] = PULSAR["polyco"]
+    res = jobs.correlate(job, dump=True)
+    keys = sc.streams()
+    for k, key in enumerate(keys):
+        si = key[0]
+        rec["chan_%d" % k] = chans[key]
+        for it in range(sc.n_integrations):
+            s0 = start + it * tint
+            dl = ref_delays(dels[si], s0, s0 + tint, sc.sample_rate, sc.bits)
+            rec["delays_%d_%d" % (k, it)] = np.array(dl, dtype=np.int64)
+            pb = job["protocols"][k][it]
+            rec["proto_sha_%d_%d" % (k, it)] = np.frombuffer(hashlib.sha256(pb).digest(), np.uint8)
+            rec["proto_len_%d_%d" % (k, it)] = np.array(len(pb))
+            un = res["unpacked"][(it, k)]
+            rec["unpacked_sha_%d_%d" % (k, it)] = np.frombuffer(hashlib.sha256(un.tobytes()).digest(), np.uint8)
+            rec["unpacked_head_%d_%d" % (k, it)] = un[:4096]
+            rows = res["rows"][(it, k)].reshape(-1, job["fft_size_correlation"] + 4)
+            pick = sorted(set([0, 1, rows.shape[0] // 2, rows.shape[0] - 1]))
+            rec["rows_idx_%d_%d" % (k, it)] = np.array(pick)
+            rec["rows_%d_%d" % (k, it)] = rows[pick, :job["fft_size_correlation"] + 1]
+    if "pulsar" in job:
+        rec["bins"] = res["bins"].astype(np.int8)
+    rec["cor"] = np.frombuffer(res["cor"], np.uint8)
+    rec["tsys"] = np.frombuffer(res["tsys"], np.uint8)
+    rec["stats"] = np.frombuffer(res["stats"].encode(), np.uint8)
+    meta = {k: v for k, v in job.items() if k not in ("del_bytes", "protocols")}
+    meta["block_bytes"] = sc.block_bytes
+    meta["rec0"] = rec0
+    meta["slice_samples"] = slice_samples
+    meta["nblocks"] = [len(chans[key]) // sc.block_bytes for key in keys]
+    meta["invalid"] = {"%d,%s" % k: v for k, v in sc.invalid.items()}
+    rec["meta"] = np.array(repr(meta))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **rec)
+    print(name, "cor bytes", len(res["cor"]))
+
+
+def make_extract():
+    # 16 channels x 2 bits in 32-bit words (VDIF multi-channel layout), reference tracks
+    rng = np.random.Generator(np.random.PCG64(77))
+    words = rng.integers(0, 2**32, size=8000, dtype=np.uint64).astype(np.uint32)
+    tracks = [[2 * c + 1, 2 * c] for c in range(16)]
+    out16 = jobs.extract(words.tobytes(), 4, 2, words.size, tracks)
+    # 8 channels x 2 bits with fan-out 4 (two samples per channel per 32-bit word)
+    tracks8 = [[2 * c + 1, 2 * c, 2 * c + 17, 2 * c + 16] for c in range(8)]
+    out8 = jobs.extract(words.tobytes(), 4, 2, words.size, tracks8)
+    # 1-bit, 32 tracks in pairs of fan-out 2 (Mark5B-like bitstreams)
+    tracks1 = [[c, c + 16] for c in range(16)]
+    out1 = jobs.extract(words.tobytes(), 4, 1, words.size, tracks1)
+    np.savez_compressed(os.path.join(HERE, "extract.npz"), words=words,
+                        tracks16=np.array(tracks16 := tracks), out16=np.frombuffer(b"".join(out16), np.uint8),
+                        tracks8=np.array(tracks8), out8=np.frombuffer(b"".join(out8), np.uint8),
+                        tracks1=np.array(tracks1), out1=np.frombuffer(b"".join(out1), np.uint8))
+    print("extract done")
+
+
+if __name__ == "__main__":
+    make_extract()
+    for name, sc in scenarios().items():
+        make(name, sc)

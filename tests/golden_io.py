@@ -1,0 +1,126 @@
+"""Loading of the golden fixtures (tests/golden/*.npz) and helpers to compare
+correlator outputs.  Test infrastructure."""
+import ast
+import hashlib
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ["c1_plain", "multi", "onebit", "pulsar"]
+
+
+class Golden:
+    def __init__(self, name):
+        self.name = name
+        self.z = np.load(os.path.join(GOLDEN, name + ".npz"), allow_pickle=True)
+        self.meta = ast.literal_eval(str(self.z["meta"]))
+        self.dels = [bytes(np.asarray(d, dtype=np.uint8)) for d in self.z["del_bytes"]]
+        self.nstreams = len(self.meta["streams"])
+        self.nint = int(self.meta["n_integrations"])
+
+    def blocks(self, k):
+        m = self.meta
+        chan = np.asarray(self.z["chan_%d" % k], dtype=np.uint8)
+        bb = m["block_bytes"]
+        s = m["streams"][k]
+        bits, sr = s[7], s[2]
+        tps = int(round(512e6 / sr))
+        spb_block = bb * 8 // bits
+        inv = {}
+        key = "%d,%s" % (s[0], s[6])
+        for (b, begin, n) in m["invalid"].get(key, []):
+            inv.setdefault(b, []).append((begin, n))
+        nb = len(chan) // bb
+        return [(m["rec0"] + b * spb_block * tps, chan[b * bb:(b + 1) * bb].tobytes(), inv.get(b, []))
+                for b in range(nb)]
+
+    def delays(self, k, it):
+        return [tuple(int(x) for x in row) for row in self.z["delays_%d_%d" % (k, it)]]
+
+    def slices(self, k):
+        m = self.meta
+        tint = int(round(m["integration_time_us"] * 512))
+        out = []
+        for it in range(self.nint):
+            s0 = m["start_ticks"] + it * tint
+            out.append((s0, s0 + tint, m["slice_samples"], self.delays(k, it)))
+        return out
+
+    def protocol_ok(self, k, it, data):
+        sha = bytes(np.asarray(self.z["proto_sha_%d_%d" % (k, it)], dtype=np.uint8))
+        return hashlib.sha256(data).digest() == sha and len(data) == int(self.z["proto_len_%d_%d" % (k, it)])
+
+    def job(self, protocol_fn):
+        """Job dict with protocols regenerated by protocol_fn and checked by digest."""
+        m = self.meta
+        job = {k: v for k, v in m.items()}
+        job["del_bytes"] = self.dels
+        protos = []
+        for k in range(self.nstreams):
+            s = m["streams"][k]
+            pr = protocol_fn(self.blocks(k), self.slices(k), s[2], s[7], m["integration_time_us"])
+            for it in range(self.nint):
+                assert self.protocol_ok(k, it, pr[it]), "protocol of stream %d integration %d differs" % (k, it)
+            protos.append(pr)
+        job["protocols"] = protos
+        return job
+
+    def unpacked_sha(self, k, it):
+        return bytes(np.asarray(self.z["unpacked_sha_%d_%d" % (k, it)], dtype=np.uint8))
+
+    @property
+    def cor(self):
+        return bytes(np.asarray(self.z["cor"], dtype=np.uint8))
+
+    @property
+    def tsys(self):
+        return bytes(np.asarray(self.z["tsys"], dtype=np.uint8))
+
+    @property
+    def stats(self):
+        return bytes(np.asarray(self.z["stats"], dtype=np.uint8)).decode()
+
+
+def parse_cor(data, nchan):
+    """Split correlator output bytes into header bytes and visibility arrays.
+
+    Returns (headers: bytes, vis: list of complex64 arrays, one per baseline
+    and slice, in file order)."""
+    hdr = bytearray()
+    vis = []
+    p = 0
+    while p < len(data):
+        hdr += data[p:p + 4]  # file index
+        p += 4
+        ts = np.frombuffer(data[p:p + 16], dtype=np.int32)
+        hdr += data[p:p + 16]
+        p += 16
+        nbl, nuvw, nstat = int(ts[1]), int(ts[2]), int(ts[3])
+        n = nuvw * 32 + nstat * 24
+        hdr += data[p:p + n]
+        p += n
+        for _ in range(nbl):
+            hdr += data[p:p + 8]
+            p += 8
+            vis.append(np.frombuffer(data[p:p + (nchan + 1) * 8], dtype=np.complex64).copy())
+            p += (nchan + 1) * 8
+    return bytes(hdr), vis
+
+
+def rel_err(a, b):
+    nb = np.linalg.norm(b)
+    if nb == 0:
+        return float(np.linalg.norm(a))
+    return float(np.linalg.norm(a - b) / nb)
+
+
+def compare_cor(got, want, nchan, tol):
+    """Headers byte-identical; every visibility vector within relative L2 `tol`."""
+    hg, vg = parse_cor(got, nchan)
+    hw, vw = parse_cor(want, nchan)
+    assert hg == hw, "output headers differ"
+    assert len(vg) == len(vw)
+    worst = max(rel_err(a, b) for a, b in zip(vg, vw))
+    assert worst <= tol, "visibility error %.3g exceeds %.3g" % (worst, tol)
+    return worst

@@ -1,0 +1,74 @@
+"""The C-ABI library without a GPU: it loads, exports every function that
+include/sfxc_gpu.h declares, and its host-side input-node functions (integer
+delay lists, byte protocol) reproduce the reference's golden outputs bit for
+bit.  No kernel runs here."""
+import os
+import re
+
+import pytest
+
+from golden_io import CASES, Golden
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "sfxc_gpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = set(re.findall(r"\b(sfxc_gpu_\w+)\s*\(", text))
+    return sorted(n for n in names if not n.startswith("sfxc_gpu_ctx"))
+
+
+def test_exports_every_declared_symbol(sfxc_lib):
+    names = declared_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(sfxc_lib, n), n
+    from sfxc_gpu import lib
+    assert sorted(lib.EXPORTS) == names
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_delay_lists(case, sfxc_lib):
+    from sfxc_gpu import correlator
+    g = Golden(case)
+    for k in range(g.nstreams):
+        s = g.meta["streams"][k]
+        for s0, s1, _, dl in g.slices(k):
+            assert correlator.delay_list(g.dels[s[10]], s0, s1, s[2], s[7]) == dl
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_protocol_bytes(case, sfxc_lib):
+    from sfxc_gpu import correlator
+    g = Golden(case)
+    g.job(correlator.write_protocol)  # asserts the digest of every slice
+
+
+def test_delay_list_errors(sfxc_lib):
+    from sfxc_gpu import correlator, lib
+    g = Golden("c1_plain")
+    s0, s1, _, _ = g.slices(0)[0]
+    with pytest.raises(lib.SfxcError) as e:
+        correlator.delay_list(g.dels[0], s1, s0, 32_000_000, 2)
+    assert e.value.code == lib.EINVAL
+    with pytest.raises(lib.SfxcError) as e:
+        correlator.delay_list(g.dels[0], s0, s1, 32_000_000, 3)
+    assert e.value.code == lib.EINVAL
+    far = s0 + 3600 * 512_000_000
+    with pytest.raises(lib.SfxcError) as e:
+        correlator.delay_list(g.dels[0], far, far + 512_000_000, 32_000_000, 2)
+    assert e.value.code == lib.EDELAY
+    with pytest.raises(lib.SfxcError) as e:
+        correlator.delay_list(b"\x03\x00\x00\x00ab\x00", s0, s1, 32_000_000, 2)
+    assert e.value.code == lib.EDELTAB
+
+
+def test_no_cpu_fallback(sfxc_lib):
+    """Without a usable GPU the library refuses to create a context."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from sfxc_gpu import correlator, lib
+    with pytest.raises(lib.SfxcError):
+        correlator.CorrelatorNode(0)
