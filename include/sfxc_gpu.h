@@ -154,10 +154,11 @@ int sfxc_gpu_run_integration(sfxc_gpu_ctx *ctx, sfxc_output_sink sink, void *use
  * fft_size_correlation + 1 complex values, the output of Delay_correction). */
 int sfxc_gpu_copy_unpacked(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
 int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
-/* Per-kernel device time (ms) of the last integration, CUDA events on the
- * context's stream: [0] unpack+fringe, [1] windowed FFT, [2] X-step,
- * [3] statistics+normalisation, [4] total. */
-int sfxc_gpu_last_timings(const sfxc_gpu_ctx *ctx, float *ms5);
+/* Device time (ms) of the last integration, CUDA events on the context's
+ * stream: [0] unpack+fringe, [1] windowed FFT, [2] X-step, [3] normalisation
+ * and result copies, [4] total from the first kernel to the last copy;
+ * [5] number of kernel launches. */
+int sfxc_gpu_last_timings(const sfxc_gpu_ctx *ctx, float *out6);
 
 /* Integer delay list of one interval (Input_node_tasklet::add_time_interval):
  * writes up to `capacity` entries (ticks, bytes, remaining samples) and

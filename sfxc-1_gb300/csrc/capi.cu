@@ -53,7 +53,8 @@ struct DevBuf {
 struct StreamCtx {
   std::vector<Record> recs;
   StreamUnpackState ust;
-  std::vector<uint8_t> chunk;
+  std::vector<Record> pending;  // records of the bytes pushed for the next integration
+  int64_t dev_bytes = 0;        // bytes of that input already on the device
   bool pushed = false;
   UnpackPlan plan;
   BitStats stats{};
@@ -79,7 +80,8 @@ struct sfxc_gpu_ctx {
   int device = 0, x_mode = 0;
   cudaStream_t st = nullptr;
   cudaEvent_t ev[6] = {};
-  float timings[5] = {};
+  float timings[6] = {};
+  std::vector<cudaEvent_t> evpool;
   std::string err;
   bool have_job = false;
   // job
@@ -359,13 +361,12 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     const StationStream &ss = c->streams[i];
     s.sp = Spline::create(c->tables[c->stream_table[i]], start, tint);
     std::vector<Record> recs(s.recs.begin() + (long)s.ust.rec, s.recs.end());
-    std::vector<Record> fresh = parse_protocol(s.chunk.data(), s.chunk.size(), 0);
-    recs.insert(recs.end(), fresh.begin(), fresh.end());
+    recs.insert(recs.end(), s.pending.begin(), s.pending.end());
+    s.pending.clear();
     s.ust.rec = 0;
     s.recs.swap(recs);
     s.plan = plan_unpack(s.recs, s.ust, s.n_blocks, s.nfft_max, c->Nd, ss.bits, ss.sample_rate, ss.tsys_freq,
                          s.sp.delay(start));
-    upload(s.src, s.chunk.data(), s.chunk.size(), st);
     if (s.plan.segs.empty()) s.plan.segs.push_back(Segment{0, s.n_blocks * c->Nd, -1});
     upload(s.segs, s.plan.segs.data(), s.plan.segs.size() * sizeof(Segment), st);
     upload(s.stat_rng, s.plan.stats.data(), s.plan.stats.size() * sizeof(StatRange), st);
@@ -430,7 +431,6 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       const StatRange &sr = s.plan.stats[r];
       for (int off = 0; off < sr.n; off += 4096) items.push_back(make_int4(i, r, off, std::min(4096, sr.n - off)));
     }
-    s.chunk.clear();
     s.pushed = false;
   }
   // ---- flagged samples and normalisation factors (host)
@@ -527,11 +527,15 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     upload(c->offsets, off.data(), off.size() * 8, st);
     c->bins.ensure((size_t)max_rows * K * sizeof(int16_t));
   }
-  cudaEvent_t e0, e1, e2, e3;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
-  CK(cudaEventCreate(&e2));
-  CK(cudaEventCreate(&e3));
+  // four events per chunk (+2 for normalisation), recorded without host syncs
+  const size_t nev = ranges.size() * 4 + 2;
+  while (c->evpool.size() < nev) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    c->evpool.push_back(e);
+  }
+  int launches = items.empty() ? 0 : 1;
+  size_t ev = 0;
   for (auto &rg : ranges) {
     const int r0 = rg.first, r1 = rg.second, nrows = r1 - r0;
     // block range of each stream for rows [r0, r1) (plus the overlapping half window)
@@ -544,15 +548,15 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       d.n_blocks = b1 - b0;
     }
     upload(c->streamdev, c->hsd.data(), c->hsd.size() * sizeof(StreamDev), st);
-    CK(cudaEventRecord(e0, st));
+    CK(cudaEventRecord(c->evpool[ev], st));
     launch_fstep_block(c->streamdev.as<StreamDev>(), N, max_blocks, c->tw256.as<float2>(), st);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(e1, st));
+    CK(cudaEventRecord(c->evpool[ev + 1], st));
     const int nper = c->p.window == WINDOW_NONE ? c->sc[0].hop : c->sc[0].rot;
     launch_window_fft(c->streamdev.as<StreamDev>(), N, 0, nrows, max_rows, c->window.as<float>(),
                       c->twrot.as<float2>(), c->sc[0].rot, nper, M, kpad, c->spec.p, false, 1.0f, st);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(e2, st));
+    CK(cudaEventRecord(c->evpool[ev + 2], st));
     if (pulsar) {
       launch_pulsar(c->spec.as<float2>(), max_rows, kpad, N, c->jt.npad, nrows, K, c->tiles.as<int>(), c->jt.ntiles,
                     c->blmap.as<int>(), nbl, psr_start_phase, psr_rate, fft_duration, c->offsets.as<double>(),
@@ -562,15 +566,9 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
                        c->jt.ntiles, c->blmap.as<int>(), c->acc.as<float2>(), st);
     }
     CK(cudaGetLastError());
-    CK(cudaEventRecord(e3, st));
-    CK(cudaEventSynchronize(e3));
-    float a, b, x;
-    CK(cudaEventElapsedTime(&a, e0, e1));
-    CK(cudaEventElapsedTime(&b, e1, e2));
-    CK(cudaEventElapsedTime(&x, e2, e3));
-    t_f1 += a;
-    t_f2 += b;
-    t_x += x;
+    CK(cudaEventRecord(c->evpool[ev + 3], st));
+    ev += 4;
+    launches += pulsar ? 4 : 3;
   }
   (void)tc;
   // restore the whole-integration time base for inspection calls
@@ -579,7 +577,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     c->hsd[i].n_blocks = c->sc[i].n_blocks;
   }
   // ---- normalisation and statistics
-  CK(cudaEventRecord(e0, st));
+  CK(cudaEventRecord(c->evpool[ev], st));
   c->norms.ensure((size_t)N * 8);
   c->out.ensure((size_t)c->nbins * nbl * K * sizeof(float2));
   for (int bin = 0; bin < c->nbins; bin++)
@@ -591,16 +589,22 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   std::vector<unsigned long long> hist((size_t)N * 512);
   for (int i = 0; i < N; i++)
     CK(cudaMemcpyAsync(hist.data() + (size_t)i * 512, c->sc[i].hist.p, 512 * 8, cudaMemcpyDeviceToHost, st));
-  CK(cudaEventRecord(e1, st));
+  CK(cudaEventRecord(c->evpool[ev + 1], st));
+  launches += 2 * c->nbins;
   CK(cudaStreamSynchronize(st));
-  float tn;
-  CK(cudaEventElapsedTime(&tn, e0, e1));
-  float tall;
-  CK(cudaEventElapsedTime(&tall, c->ev[0], e1));
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaEventDestroy(e2);
-  cudaEventDestroy(e3);
+  for (size_t q = 0; q + 4 <= ev; q += 4) {
+    float a, b, x;
+    CK(cudaEventElapsedTime(&a, c->evpool[q], c->evpool[q + 1]));
+    CK(cudaEventElapsedTime(&b, c->evpool[q + 1], c->evpool[q + 2]));
+    CK(cudaEventElapsedTime(&x, c->evpool[q + 2], c->evpool[q + 3]));
+    t_f1 += a;
+    t_f2 += b;
+    t_x += x;
+  }
+  float tn, tall;
+  CK(cudaEventElapsedTime(&tn, c->evpool[ev], c->evpool[ev + 1]));
+  CK(cudaEventElapsedTime(&tall, c->ev[0], c->evpool[ev + 1]));
+  c->timings[5] = (float)launches;
   c->timings[0] = t_f1;
   c->timings[1] = t_f2;
   c->timings[2] = t_x;
@@ -672,6 +676,7 @@ void sfxc_gpu_destroy(sfxc_gpu_ctx *c) {
   if (c->st) cudaStreamSynchronize(c->st);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
+  for (auto &e : c->evpool) cudaEventDestroy(e);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -697,9 +702,28 @@ int sfxc_gpu_push_protocol(sfxc_gpu_ctx *c, int32_t stream, const uint8_t *bytes
   if (stream < 0 || stream >= (int)c->sc.size()) return fail(c, Error(SFXC_GPU_EINVAL, "bad stream index"));
   if (n && !bytes) return fail(c, Error(SFXC_GPU_EINVAL, "null input"));
   StreamCtx &s = c->sc[stream];
-  s.chunk.insert(s.chunk.end(), bytes, bytes + n);
-  s.pushed = true;
-  return SFXC_GPU_OK;
+  try {
+    CK(cudaSetDevice(c->device));
+    // records refer to the bytes by their offset in the stream's device buffer
+    std::vector<Record> recs = parse_protocol(bytes, n, s.dev_bytes);
+    const size_t need = (size_t)(s.dev_bytes + (int64_t)n);
+    if (need > s.src.cap) {  // grow, keeping what this integration already pushed
+      DevBuf grown;
+      grown.ensure(std::max(need, s.src.cap * 3 / 2));
+      if (s.dev_bytes) CK(cudaMemcpyAsync(grown.p, s.src.p, (size_t)s.dev_bytes, cudaMemcpyDeviceToDevice, c->st));
+      std::swap(grown.p, s.src.p);
+      std::swap(grown.cap, s.src.cap);
+      CK(cudaStreamSynchronize(c->st));
+    }
+    if (n) CK(cudaMemcpyAsync(s.src.as<uint8_t>() + s.dev_bytes, bytes, n, cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));  // the caller may reuse its buffer on return
+    s.dev_bytes += (int64_t)n;
+    s.pending.insert(s.pending.end(), recs.begin(), recs.end());
+    s.pushed = true;
+    return SFXC_GPU_OK;
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
 }
 
 int sfxc_gpu_run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
@@ -792,9 +816,10 @@ int sfxc_gpu_extract_channels(sfxc_gpu_ctx *c, const uint8_t *words, int64_t nwo
   }
 }
 
-int sfxc_gpu_last_timings(const sfxc_gpu_ctx *c, float *ms5) {
+int sfxc_gpu_last_timings(const sfxc_gpu_ctx *c, float *ms6) {
+  float *ms5 = ms6;
   if (!c || !ms5) return SFXC_GPU_EINVAL;
-  for (int i = 0; i < 5; i++) ms5[i] = c->timings[i];
+  for (int i = 0; i < 6; i++) ms5[i] = c->timings[i];
   return SFXC_GPU_OK;
 }
 

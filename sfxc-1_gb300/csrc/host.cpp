@@ -438,11 +438,9 @@ UnpackPlan plan_unpack(const std::vector<Record> &recs, StreamUnpackState &st, i
   st.invalid_left = 0;
   st.sample_in_byte = 0;
   int cur_delay = -1;
-  int64_t src = 0;  // payload position of the current data record (the reference's read pointer)
-  if (st.state == S_DATA || (st.state == S_PURGE && st.bytes_left > 0)) {
-    if (st.rec == 0 || recs[st.rec - 1].type != HEADER_DATA) throw Error(-4, "inconsistent carried-over state");
-    src = recs[st.rec - 1].src + st.rec_off;
-  }
+  // payload position of the current data record (the reference's read pointer);
+  // an integration always starts in IDLE or PURGE, so no payload carries over
+  int64_t src = 0;
   plan.tsys.two_bit = bits == 2;
   plan.tsys.on0 = 1;
   if (bits == 2) {

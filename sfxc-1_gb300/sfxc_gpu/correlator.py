@@ -150,10 +150,10 @@ class CorrelatorNode:
         return out
 
     def timings(self):
-        t = (C.c_float * 5)()
+        t = (C.c_float * 6)()
         self._check(self._lib.sfxc_gpu_last_timings(self._h, t))
         return {"unpack_fringe_ms": t[0], "window_fft_ms": t[1], "xstep_ms": t[2], "normalise_ms": t[3],
-                "total_ms": t[4]}
+                "total_ms": t[4], "launches": int(t[5])}
 
     def extract_channels(self, words, word_bytes, bits, tracks):
         """Channel_extractor semantics on the GPU.  tracks: list per subband."""
@@ -179,6 +179,43 @@ def delay_list(del_bytes, start_ticks, stop_ticks, sample_rate, bits, clock=(0.0
     if n < 0:
         raise L.SfxcError(n, lib.sfxc_gpu_global_error().decode())
     return [(ticks[i], by[i], rem[i]) for i in range(n)]
+
+
+_BLOCK_DTYPE = np.dtype([("start", "<i8"), ("size", "<i4"), ("ninv", "<i4"), ("inv", "<u8")])
+
+
+def write_protocol_stream(stream, block_bytes, block_starts, slices, sample_rate, bits, integration_time_us,
+                          alloc=None):
+    """write_protocol for a whole channel stream held in one array (blocks of
+    `block_bytes` back to back, starting at `block_starts`, no invalid runs).
+    `alloc(n)` may supply the output buffer (e.g. pinned memory); returns one
+    uint8 array view per slice."""
+    lib = L.load()
+    stream = np.ascontiguousarray(stream, dtype=np.uint8)
+    nb = len(block_starts)
+    cb = np.zeros(nb, dtype=_BLOCK_DTYPE)
+    cb["start"] = block_starts
+    cb["size"] = block_bytes
+    keep = []
+    sl = (L.Slice * len(slices))()
+    for i, (s0, s1, ns, dl) in enumerate(slices):
+        tk = (C.c_int64 * len(dl))(*[d[0] for d in dl])
+        by = (C.c_int32 * len(dl))(*[d[1] for d in dl])
+        rm = (C.c_int32 * len(dl))(*[d[2] for d in dl])
+        keep += [tk, by, rm]
+        sl[i] = L.Slice(s0, s1, ns, len(dl), tk, by, rm)
+    offs = (C.c_int64 * (len(slices) + 1))()
+    cbp = C.cast(cb.ctypes.data, C.POINTER(L.ChannelBlock))
+    need = lib.sfxc_gpu_write_protocol(stream.ctypes.data, nb, cbp, len(slices), sl, sample_rate, bits,
+                                       integration_time_us, None, 0, offs)
+    if need < 0:
+        raise L.SfxcError(int(need), lib.sfxc_gpu_global_error().decode())
+    out = alloc(int(need)) if alloc else np.empty(int(need), dtype=np.uint8)
+    n = lib.sfxc_gpu_write_protocol(stream.ctypes.data, nb, cbp, len(slices), sl, sample_rate, bits,
+                                    integration_time_us, out.ctypes.data, need, offs)
+    if n < 0:
+        raise L.SfxcError(int(n), lib.sfxc_gpu_global_error().decode())
+    return [out[offs[i]:offs[i + 1]] for i in range(len(slices))]
 
 
 def write_protocol(blocks, slices, sample_rate, bits, integration_time_us):

@@ -150,6 +150,44 @@ def build_job(sc: Scenario, delay_fn, protocol_fn, fast_random=False):
                 streams=streams, protocols=protos)
 
 
+def build_job_bulk(sc: Scenario, alloc=None):
+    """Large jobs: uniformly random 2-bit/1-bit codes generated per stream and
+    turned straight into protocol bytes by the library's input-node writer
+    (no per-block Python objects).  alloc(n) may supply the protocol buffers
+    (pinned host memory for end-to-end timing).  No invalid runs."""
+    from . import correlator
+    dels = del_tables(sc)
+    rec0, start, tint, slice_samples = job_timing(sc)
+    sr, bits = sc.sample_rate, sc.bits
+    tps = timebase.ticks_per_sample(sr)
+    spb_block = sc.block_bytes * 8 // bits
+    max_tau = max(abs(float(st.poly.delay(sc.sec0 + sc.lead_us * 1e-6))) for st in sc.stations)
+    span = sc.lead_us * sr // 1_000_000 + sc.n_integrations * (sc.integration_us * sr // 1_000_000)
+    nsamp = span + int(max_tau * sr) + 4 * spb_block
+    nblocks = (nsamp + spb_block - 1) // spb_block
+    starts = rec0 + np.arange(nblocks, dtype=np.int64) * spb_block * tps
+    streams, protos = [], []
+    for k, (si, pol) in enumerate(sc.streams()):
+        st = sc.stations[si]
+        rng = np.random.Generator(np.random.PCG64(sc.seed * 7919 + k))
+        data = rng.integers(0, 256, size=nblocks * sc.block_bytes, dtype=np.uint8)
+        slices = []
+        for it in range(sc.n_integrations):
+            s0 = start + it * tint
+            slices.append((s0, s0 + tint, slice_samples, correlator.delay_list(dels[si], s0, s0 + tint, sr, bits)))
+        protos.append(correlator.write_protocol_stream(data, sc.block_bytes, starts, slices, sr, bits,
+                                                       sc.integration_us, alloc=alloc))
+        streams.append((st.number, k, sr, sc.channel_freq, sc.bandwidth, sc.sideband, pol, bits, sc.lo_offset,
+                        sc.tsys_freq, si))
+    return dict(del_bytes=dels, experiment_start_ticks=rec0, start_ticks=start,
+                integration_time_us=sc.integration_us, sub_integration_time_us=sc.sub_integration_us,
+                number_channels=sc.nchan, fft_size_delaycor=256, fft_size_correlation=max(256, sc.nchan),
+                sample_rate=sr, channel_freq=sc.channel_freq, bandwidth=sc.bandwidth, sideband=sc.sideband,
+                frequency_nr=sc.frequency_nr, polarisation=sc.pols[0], cross_polarize=1 if len(sc.pols) > 1 else 0,
+                reference_station=sc.reference_station, window=sc.window, source="SRC", integration_nr=0,
+                n_integrations=sc.n_integrations, streams=streams, protocols=protos)
+
+
 def c1_plain(integration_us=15625, n_integrations=2, seed=1):
     """The plain CPU-runnable configuration, shortened: 2 stations, 1 subband of
     16 MHz at 32 MS/s, 2-bit, single pol; station 2 delayed by 37.25 samples

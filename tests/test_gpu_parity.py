@@ -95,15 +95,43 @@ def test_larger_job_vs_oracle(gpu_node):
     compare_cor(cor, ref["cor"], 4096, FP32_TOL)
 
 
+def record_boundaries(data):
+    """Offsets at which the correlator-node protocol records end."""
+    out, p = [], 0
+    while p < len(data):
+        h = data[p]
+        if h == 0:
+            p += 3 + (data[p + 1] | data[p + 2] << 8)
+        elif h == 1:
+            p += 3
+        elif h == 2:
+            p += 2
+        else:
+            p += 1
+        out.append(p)
+    return out
+
+
 def test_errors_leave_context_usable(gpu_node):
     from sfxc_gpu import correlator, lib
     g = Golden("c1_plain")
     job = g.job(correlator.write_protocol)
+    proto = job["protocols"][0][0]
     gpu_node.set_parameters(job)
-    gpu_node.push_protocol(0, job["protocols"][0][0][:1000])  # short input
+    # a record cut in the middle is malformed input
+    with pytest.raises(lib.SfxcError) as e:
+        gpu_node.push_protocol(0, proto[:1000])
+    assert e.value.code == lib.EPROTO
+    # whole records that end before the integration is complete: input ended early
+    gpu_node.set_parameters(job)
+    cut = [b for b in record_boundaries(proto) if b < len(proto) // 2][-1]
+    gpu_node.push_protocol(0, proto[:cut])
     gpu_node.push_protocol(1, job["protocols"][1][0])
     with pytest.raises(lib.SfxcError) as e:
         gpu_node.run_integration()
     assert e.value.code == lib.ESTREAM
+    with pytest.raises(lib.SfxcError) as e:
+        gpu_node.push_protocol(7, proto)
+    assert e.value.code == lib.EINVAL
     cor, _ = gpu_node.correlate(job)  # a fresh job on the same context works
     compare_cor(cor, g.cor, 512, FP32_TOL)
