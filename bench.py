@@ -196,7 +196,7 @@ def run_gpu(args):
         return
     value = total * args.steps * world / (dev_total / 1e3) / 1e9
     e2e = total * args.steps * world / wall / 1e9
-    in_bytes = sum(sum(b.numel() for b in j["pinned"]) for j in jobs)
+    in_bytes = sum(sum(b.size for b in j["pinned"]) for j in jobs)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Gsamples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dev_total / args.steps, 3), "higher_is_better": True,

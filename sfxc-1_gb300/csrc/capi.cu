@@ -97,7 +97,7 @@ struct sfxc_gpu_ctx {
   int M = 0, K = 0, Nd = 0, kpad = 0, nffts = 0, nsub = 0, nbins = 1;
   // device
   DevBuf streamdev, tw256, window, twrot, ts, spec, acc, out, norms, flagfac, blmap, tiles, blpairs, items, bins,
-      offsets;
+      offsets, derr;
   int tw_rot_n = 0, window_n = 0, window_type = -1;
   std::vector<StreamDev> hsd;
 };
@@ -247,6 +247,8 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
     }
   jt.ntiles = (int)jt.tiles.size() / 2;
   if (xcorr_tpw(jt.ntiles) < 0) throw Error(SFXC_GPU_EINVAL, "too many streams for the X-step tiling (max 48 tiles)");
+  if (c->x_mode == SFXC_GPU_X_TC_HILO && N > 32)
+    throw Error(SFXC_GPU_EINVAL, "the tensor-core X-step takes at most 32 streams per job");
   upload(c->blmap, jt.blmap.data(), jt.blmap.size() * 4, c->st);
   upload(c->tiles, jt.tiles.data(), jt.tiles.size() * 4, c->st);
   upload(c->blpairs, jt.blpairs.data(), jt.blpairs.size() * 4, c->st);
@@ -480,8 +482,14 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   int max_blocks = 0;
   for (int i = 0; i < N; i++) max_blocks = std::max(max_blocks, chunked ? (max_rows + 2) * hop / kNd : c->sc[i].n_blocks);
   c->ts.ensure((size_t)N * max_blocks * kNd * sizeof(float));
-  const bool tc = c->x_mode == SFXC_GPU_X_TC_HILO;
+  // tensor-core X-step for normal correlation of up to 32 inputs; the spectra
+  // are scaled by a power of two before the FP16 hi/lo split so that typical
+  // magnitudes sit near 1 (|X| ~ sqrt(2M * 0.375 * E[x^2]) for a Hann window)
+  const bool tc_x = c->x_mode == SFXC_GPU_X_TC_HILO && !pulsar;
+  const float tc_scale = std::ldexp(1.0f, -(int)std::lround(0.5 * std::log2(2.0 * M * 10.0)));
   c->spec.ensure((size_t)N * max_rows * kpad * sizeof(float2));
+  c->derr.ensure(sizeof(int));
+  CK(cudaMemsetAsync(c->derr.p, 0, sizeof(int), st));
   float t_f1 = 0, t_f2 = 0, t_x = 0;
   // pulsar setup (Correlation_core_pulsar::set_parameters, correlation_core_pulsar.cc:46-95)
   double psr_start_phase = 0, psr_rate = 0, fft_duration = 0;
@@ -554,10 +562,13 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     CK(cudaEventRecord(c->evpool[ev + 1], st));
     const int nper = c->p.window == WINDOW_NONE ? c->sc[0].hop : c->sc[0].rot;
     launch_window_fft(c->streamdev.as<StreamDev>(), N, 0, nrows, max_rows, c->window.as<float>(),
-                      c->twrot.as<float2>(), c->sc[0].rot, nper, M, kpad, c->spec.p, false, 1.0f, st);
+                      c->twrot.as<float2>(), c->sc[0].rot, nper, M, kpad, c->spec.p, tc_x, tc_scale, st);
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->evpool[ev + 2], st));
-    if (pulsar) {
+    if (tc_x) {
+      launch_xcorr_tc(c->spec.p, max_rows, kpad, N, nrows, K, c->blmap.as<int>(), c->jt.npad,
+                      1.0f / (tc_scale * tc_scale), c->acc.as<float2>(), c->derr.as<int>(), st);
+    } else if (pulsar) {
       launch_pulsar(c->spec.as<float2>(), max_rows, kpad, N, c->jt.npad, nrows, K, c->tiles.as<int>(), c->jt.ntiles,
                     c->blmap.as<int>(), nbl, psr_start_phase, psr_rate, fft_duration, c->offsets.as<double>(),
                     c->p.gate_start, c->p.gate_stop, c->nbins, c->bins.as<int16_t>(), c->acc.as<float2>(), st);
@@ -570,7 +581,6 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     ev += 4;
     launches += pulsar ? 4 : 3;
   }
-  (void)tc;
   // restore the whole-integration time base for inspection calls
   for (int i = 0; i < N; i++) {
     c->hsd[i].block0 = 0;
@@ -589,9 +599,12 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   std::vector<unsigned long long> hist((size_t)N * 512);
   for (int i = 0; i < N; i++)
     CK(cudaMemcpyAsync(hist.data() + (size_t)i * 512, c->sc[i].hist.p, 512 * 8, cudaMemcpyDeviceToHost, st));
+  int dev_err = 0;
+  CK(cudaMemcpyAsync(&dev_err, c->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaEventRecord(c->evpool[ev + 1], st));
   launches += 2 * c->nbins;
   CK(cudaStreamSynchronize(st));
+  if (dev_err) throw Error(SFXC_GPU_ECUDA, "tensor-core X-step timed out waiting for its MMAs");
   for (size_t q = 0; q + 4 <= ev; q += 4) {
     float a, b, x;
     CK(cudaEventElapsedTime(&a, c->evpool[q], c->evpool[q + 1]));
