@@ -2,6 +2,7 @@
 // integration planning on the host, kernel launches on one CUDA stream, and
 // the byte layout of the correlator output (Correlation_core::integration_write,
 // sfxc/src/correlation_core.cc:316-477; headers sfxc/include/output_header.h:100-148).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -60,7 +61,7 @@ struct StreamCtx {
   BitStats stats{};
   Spline sp;
   int n_blocks = 0, nfft_max = 0, rot = 0, hop = 0;
-  DevBuf src, segs, stat_rng, spline, hist;
+  DevBuf src, segs, stat_rng, spline, hist, bparams, bamp;
 };
 
 struct Polyco {
@@ -429,6 +430,9 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       d.temp_fft_offset = (int)(-delta * 2 * M / c->p.sample_rate);
     }
     d.hist = s.hist.as<unsigned long long>();
+    d.phase_zero = std::all_of(s.sp.y[1].begin(), s.sp.y[1].end(), [](double v) { return v == 0.0; });
+    d.amp_one = std::all_of(s.sp.y[2].begin(), s.sp.y[2].end(), [](double v) { return v == 1.0; });
+    d.no_clock = s.sp.clock_offset == 0.0 && s.sp.clock_rate == 0.0;
     for (int r = 0; r < (int)s.plan.stats.size(); r++) {
       const StatRange &sr = s.plan.stats[r];
       for (int off = 0; off < sr.n; off += 4096) items.push_back(make_int4(i, r, off, std::min(4096, sr.n - off)));
@@ -490,6 +494,10 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   c->spec.ensure((size_t)N * max_rows * kpad * sizeof(float2));
   c->derr.ensure(sizeof(int));
   CK(cudaMemsetAsync(c->derr.p, 0, sizeof(int), st));
+  for (int i = 0; i < N; i++) {
+    c->sc[i].bparams.ensure((size_t)max_blocks * sizeof(float4));
+    c->sc[i].bamp.ensure((size_t)max_blocks * sizeof(float));
+  }
   float t_f1 = 0, t_f2 = 0, t_x = 0;
   // pulsar setup (Correlation_core_pulsar::set_parameters, correlation_core_pulsar.cc:46-95)
   double psr_start_phase = 0, psr_rate = 0, fft_duration = 0;
@@ -552,6 +560,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       const int b0 = chunked ? r0 * c->sc[i].hop / kNd : 0;
       const int b1 = chunked ? std::min(c->sc[i].n_blocks, (r1 + 1 + minus) * c->sc[i].hop / kNd) : c->sc[i].n_blocks;
       d.ts = c->ts.as<float>() + (size_t)i * max_blocks * kNd;
+      d.bparams = c->sc[i].bparams.as<float4>();
+      d.bamp = c->sc[i].bamp.as<float>();
       d.block0 = b0;
       d.n_blocks = b1 - b0;
     }
@@ -579,7 +589,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->evpool[ev + 3], st));
     ev += 4;
-    launches += pulsar ? 4 : 3;
+    launches += pulsar ? 5 : 4;
   }
   // restore the whole-integration time base for inspection calls
   for (int i = 0; i < N; i++) {
@@ -781,10 +791,14 @@ int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n)
     StreamDev d = c->hsd[stream];
     d.block0 = 0;
     d.n_blocks = s.n_blocks;
-    DevBuf ts, spec, sd;
+    DevBuf ts, spec, sd, bp, ba;
     ts.ensure((size_t)s.n_blocks * kNd * sizeof(float));
     spec.ensure(rows * c->kpad * sizeof(float2));
+    bp.ensure((size_t)s.n_blocks * sizeof(float4));
+    ba.ensure((size_t)s.n_blocks * sizeof(float));
     d.ts = ts.as<float>();
+    d.bparams = bp.as<float4>();
+    d.bamp = ba.as<float>();
     upload(sd, &d, sizeof(StreamDev), c->st);
     launch_fstep_block(sd.as<StreamDev>(), 1, s.n_blocks, c->tw256.as<float2>(), c->st);
     const int nper = c->p.window == WINDOW_NONE ? s.hop : s.rot;

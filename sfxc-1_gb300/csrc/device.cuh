@@ -46,6 +46,14 @@ struct StreamDev {
   double center_freq, lo_offset, start_phase;
   // windowed FFT stage
   int32_t rot, flip, output_offset, temp_fft_offset;
+  // delay-model shortcuts, exact: an all-zero phase column evaluates to 0.0,
+  // an all-one amplitude column to 1.0, a zero clock model to a zero drift
+  int32_t phase_zero, amp_one, no_clock;
+  // per-block parameters of this launch's blocks (block_params_kernel):
+  // {phase-ramp start (rad, [0,2pi)), ramp step per bin, fringe phase at the
+  // block start, fringe phase step per sample}, and the amplitude
+  float4 *bparams;
+  float *bamp;
   // outputs
   float *ts;                   // fringe-stopped series, n_blocks*256 floats
   unsigned long long *hist;    // 512 counters: [on|off][byte]
@@ -80,6 +88,7 @@ __device__ __forceinline__ double time_diff_dev(int64_t a, int64_t b) {
 }
 __device__ __forceinline__ double stream_delay(const StreamDev &s, int64_t t) {
   double r = spline_eval(s.spline, s.spline_n, 0, time_diff_dev(t, s.scan_begin));
+  if (s.no_clock) return __dadd_rn(r, 0.0);
   double drift = __dadd_rn(s.clock_offset, __dmul_rn(time_diff_dev(t, s.clock_epoch), s.clock_rate));
   return __dadd_rn(r, drift);
 }

@@ -38,45 +38,9 @@ __global__ void __launch_bounds__(256) fstep_block_kernel(const StreamDev *__res
   const int b = s.block0 + bl;  // block index within the integration
   float2 *A = sbuf[warp][0], *B = sbuf[warp][1];
   float *xa = reinterpret_cast<float *>(A);
-
-  // ---- FP64 block parameters, one spline evaluation per lane
-  const int64_t ct = s.start_ticks + (int64_t)b * kNd * s.tps;
-  double v = 0.0;
-  if (lane == 0) v = stream_delay(s, ct + s.half_len_ticks);
-  else if (lane == 1) v = stream_delay(s, ct);
-  else if (lane == 2) v = stream_delay(s, ct + s.fft_len_ticks);
-  else if (lane == 3) v = stream_phase(s, ct);
-  else if (lane == 4) v = stream_phase(s, ct + s.fft_len_ticks);
-  else if (lane == 5) v = stream_amplitude(s, ct + s.half_len_ticks);
-  const double delay_c = __shfl_sync(0xffffffffu, v, 0);
-  const double delay_0 = __shfl_sync(0xffffffffu, v, 1);
-  const double delay_1 = __shfl_sync(0xffffffffu, v, 2);
-  const double phase_0 = __shfl_sync(0xffffffffu, v, 3);
-  const double phase_1 = __shfl_sync(0xffffffffu, v, 4);
-  const double ampl = __shfl_sync(0xffffffffu, v, 5);
-
-  // fractional delay at the block centre (delay_correction.cc:40-47, 97-103)
-  const double dis = __dmul_rn(delay_c, (double)s.sample_rate);
-  const int integer_delay = (int)floor(__dadd_rn(dis, 0.5));
-  const double frac = dis - integer_delay;
-  const double tmp1 = -2.0 * M_PI * frac / s.sample_rate;
-  const double tmp2 = M_PI * (integer_delay & (4 * s.oversamp - 1)) / (2 * s.oversamp);
-  const double cterm = tmp2 - tmp1 * 0.5 * s.bandwidth;
-  const double lterm = tmp1 * ((double)s.sample_rate / kNd);
-  // fringe phase over the block (delay_correction.cc:139-160)
-  const double mult = -s.sideband * 2.0 * M_PI;
-  const double lo_phase = s.start_phase + s.lo_offset * time_diff_dev(ct, s.start_ticks);
-  double phi = s.center_freq * delay_0 + lo_phase + phase_0 / (2 * M_PI);
-  const double floor_phi = floor(phi);
-  phi = mult * (phi - floor_phi);
-  double phi_end = s.center_freq * delay_1 + lo_phase + s.fft_len_sec * s.lo_offset + phase_1 / (2 * M_PI);
-  phi_end = mult * (phi_end - floor_phi);
-  const float dphi = (float)((phi_end - phi) / kNd);
-  const float phi0 = (float)phi;
-  const float amp = (float)ampl;
-  // phase ramp start reduced to [0, 2pi) in FP64 before the FP32 per-bin ramp
-  const float c32 = (float)(cterm - 2.0 * M_PI * floor(cterm / (2.0 * M_PI)));
-  const float l32 = (float)lterm;
+  const float4 prm = s.bparams[bl];  // block_params_kernel
+  const float c32 = prm.x, l32 = prm.y, phi0 = prm.z, dphi = prm.w;
+  const float amp = s.bamp[bl];
 
   // ---- unpack 256 samples through the plan
   {
@@ -91,7 +55,15 @@ __global__ void __launch_bounds__(256) fstep_block_kernel(const StreamDev *__res
   // ---- rfft(256) via a 128-point complex FFT of (x[2n], x[2n+1])
   float2 *Z = stockham<-1>(A, B, kNd / 2, stw + kNd, lane, 32, WarpSync());
   float2 *G = (Z == A) ? B : A;
+  // phase ramp exp(-i (c + k l)) for k = lane + 32 q: one sincos for the
+  // lane's first bin and one for the 32-bin step, then complex rotations
+  float rs, rc, ss, sc;
+  sincosf(fmaf((float)lane, l32, c32), &rs, &rc);
+  sincosf(32.0f * l32, &ss, &sc);
   for (int k = lane; k <= kNd / 2; k += 32) {
+    const float cs = rc, sn = rs;
+    rc = cs * sc - sn * ss;
+    rs = sn * sc + cs * ss;
     const float2 zk = Z[k & (kNd / 2 - 1)];
     const float2 zc = Z[(kNd / 2 - k) & (kNd / 2 - 1)];
     const float er = 0.5f * (zk.x + zc.x), ei = 0.5f * (zk.y - zc.y);
@@ -103,8 +75,6 @@ __global__ void __launch_bounds__(256) fstep_block_kernel(const StreamDev *__res
       fr *= 0.5f;
       fi *= 0.5f;
     }
-    float sn, cs;
-    sincosf(fmaf((float)k, l32, c32), &sn, &cs);
     // F * (cos phi, -sin phi)
     G[k] = make_float2(fr * cs + fi * sn, fi * cs - fr * sn);
   }
@@ -113,13 +83,56 @@ __global__ void __launch_bounds__(256) fstep_block_kernel(const StreamDev *__res
   float2 *Y = stockham<+1>(G, Z, kNd, stw, lane, 32, WarpSync());
   // ---- fringe rotation and store
   float *out = s.ts + (int64_t)bl * kNd;
+  sincosf(fmaf((float)lane, dphi, phi0), &rs, &rc);
+  sincosf(32.0f * dphi, &ss, &sc);
+  rs *= amp;
+  rc *= amp;
   for (int q = 0; q < 8; q++) {
     const int n = lane + 32 * q;
-    float sn, cs;
-    sincosf(fmaf((float)n, dphi, phi0), &sn, &cs);
     const float2 z = Y[n];
-    out[n] = z.x * (amp * cs) + z.y * (amp * sn);
+    out[n] = z.x * rc + z.y * rs;
+    const float c2 = rc * sc - rs * ss;
+    rs = rs * sc + rc * ss;
+    rc = c2;
   }
+}
+
+// Per-block FP64 parameters of the F-step, one thread per 256-sample block
+// (all lanes busy on the reduced-rate FP64 pipe).  Follows
+// Delay_correction::do_task / fractional_bit_shift / fringe_stopping
+// (sfxc/src/delay_correction.cc:40-47, 97-103, 139-160): the integer and
+// fractional delay at the block centre, the fringe phase at the block start
+// and its linear step over the block, the amplitude at the centre.  The
+// phases leave FP64 only after reduction to one turn.
+__global__ void block_params_kernel(const StreamDev *__restrict__ streams) {
+  const StreamDev &s = streams[blockIdx.y];
+  const int bl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (bl >= s.n_blocks) return;
+  const int b = s.block0 + bl;
+  const int64_t ct = s.start_ticks + (int64_t)b * kNd * s.tps;
+  const double delay_c = stream_delay(s, ct + s.half_len_ticks);
+  const double delay_0 = stream_delay(s, ct);
+  const double delay_1 = stream_delay(s, ct + s.fft_len_ticks);
+  const double phase_0 = s.phase_zero ? 0.0 : stream_phase(s, ct);
+  const double phase_1 = s.phase_zero ? 0.0 : stream_phase(s, ct + s.fft_len_ticks);
+  const double ampl = s.amp_one ? 1.0 : stream_amplitude(s, ct + s.half_len_ticks);
+  const double dis = __dmul_rn(delay_c, (double)s.sample_rate);
+  const int integer_delay = (int)floor(__dadd_rn(dis, 0.5));
+  const double frac = dis - integer_delay;
+  const double tmp1 = -2.0 * M_PI * frac / s.sample_rate;
+  const double tmp2 = M_PI * (integer_delay & (4 * s.oversamp - 1)) / (2 * s.oversamp);
+  const double cterm = tmp2 - tmp1 * 0.5 * s.bandwidth;
+  const double lterm = tmp1 * ((double)s.sample_rate / kNd);
+  const double mult = -s.sideband * 2.0 * M_PI;
+  const double lo_phase = s.start_phase + s.lo_offset * time_diff_dev(ct, s.start_ticks);
+  double phi = s.center_freq * delay_0 + lo_phase + phase_0 / (2 * M_PI);
+  const double floor_phi = floor(phi);
+  phi = mult * (phi - floor_phi);
+  double phi_end = s.center_freq * delay_1 + lo_phase + s.fft_len_sec * s.lo_offset + phase_1 / (2 * M_PI);
+  phi_end = mult * (phi_end - floor_phi);
+  s.bparams[bl] = make_float4((float)(cterm - 2.0 * M_PI * floor(cterm / (2.0 * M_PI))), (float)lterm, (float)phi,
+                              (float)((phi_end - phi) / kNd));
+  s.bamp[bl] = (float)ampl;
 }
 
 // Unpacked samples only (inspection of the Bit2float_worker output).
@@ -462,6 +475,7 @@ __global__ void normalize_kernel(const float2 *__restrict__ acc, int kpad, int M
 // launchers
 void launch_fstep_block(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256,
                         cudaStream_t st) {
+  block_params_kernel<<<dim3((max_blocks + 127) / 128, nstreams), 128, 0, st>>>(d_streams);
   dim3 grid((max_blocks + 7) / 8, nstreams);
   fstep_block_kernel<<<grid, 256, 0, st>>>(d_streams, tw256);
 }
