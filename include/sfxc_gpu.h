@@ -154,6 +154,24 @@ int sfxc_gpu_run_integration(sfxc_gpu_ctx *ctx, sfxc_output_sink sink, void *use
  * fft_size_correlation + 1 complex values, the output of Delay_correction). */
 int sfxc_gpu_copy_unpacked(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
 int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
+/* sfxc_gpu_copy_spectra without any allocation.  This call has no
+ * counterpart in the reference; it exists for callers that cannot allocate
+ * device memory when they inspect a stream: code running while a CUDA graph
+ * is captured (cudaMalloc/cudaFree cannot be captured), real-time loops that
+ * cannot wait on the allocator, and hosts that carve up GPU memory once at
+ * start-up.  Its scratch -- the fringe-stopped samples, the per-block delay
+ * parameters, the stream descriptor and the spectra before the copy out --
+ * lives in one static device array of 16.2 MiB that every GPU loading the
+ * library holds until the process exits.  Limits: at most 8192 blocks of
+ * fft_size_delaycor samples (2,097,152 samples) per stream and integration,
+ * and at most 2^20 values of nffts x (fft_size_correlation + 4); larger
+ * requests return SFXC_GPU_EINVAL and touch nothing.  The first call on a
+ * device resolves the array's device address (cudaGetSymbolAddress) and
+ * should come before any stream capture.  All calls share the array and it
+ * keeps the last call's contents (each call writes every element it reads);
+ * calls that overlap on the GPU -- from different contexts or threads --
+ * race on it.  Arguments and result as sfxc_gpu_copy_spectra. */
+int sfxc_gpu_copy_spectra_noalloc(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
 /* Device time (ms) of the last integration, CUDA events on the context's
  * stream: [0] unpack+fringe, [1] windowed FFT, [2] X-step, [3] normalisation
  * and result copies, [4] total from the first kernel to the last copy;

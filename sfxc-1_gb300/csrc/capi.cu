@@ -6,7 +6,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <set>
 #include <string>
 #include <vector>
@@ -806,6 +808,94 @@ int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n)
                       s.rot, nper, c->M, c->kpad, spec.p, false, 1.0f, c->st);
     CK(cudaGetLastError());
     CK(cudaMemcpy2DAsync(out, K * sizeof(float2), spec.p, c->kpad * sizeof(float2), K * sizeof(float2), rows,
+                         cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return (int)(rows * K * 2);
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free spectra inspection.  Some callers cannot allocate device
+// memory at the moment they want to look at a stream's delay-corrected
+// spectra: code running while a CUDA graph is being captured on the stream
+// (cudaMalloc/cudaFree are not capturable), real-time correlator loops whose
+// latency budget has no room for allocator synchronisation, and hosts that
+// hand the GPU's memory out once at start-up.  sfxc_gpu_copy_spectra_noalloc
+// does the work of sfxc_gpu_copy_spectra with its scratch (fringe-stopped
+// series, per-block delay parameters, the stream descriptor and the spectra
+// before the copy out) in one file-scope device array of fixed size instead
+// of fresh allocations.
+namespace {
+constexpr int kNoallocMaxBlocks = 8192;                 // 2,097,152 samples of one stream and integration
+constexpr size_t kNoallocMaxSpectra = (size_t)1 << 20;  // rows x (fft_size_correlation + 4) complex values
+constexpr size_t kNoallocTsOff = 0;
+constexpr size_t kNoallocParOff = kNoallocTsOff + (size_t)kNoallocMaxBlocks * kNd * sizeof(float);
+constexpr size_t kNoallocAmpOff = kNoallocParOff + (size_t)kNoallocMaxBlocks * sizeof(float4);
+constexpr size_t kNoallocDescOff = kNoallocAmpOff + (size_t)kNoallocMaxBlocks * sizeof(float);
+constexpr size_t kNoallocSpecOff = kNoallocDescOff + 1024;
+constexpr size_t kNoallocBytes = kNoallocSpecOff + kNoallocMaxSpectra * sizeof(float2);  // 16.2 MiB
+static_assert(sizeof(StreamDev) <= 1024, "stream descriptor slot too small");
+
+// Held by every GPU that loads the library until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+std::mutex g_noalloc_mu;
+std::map<int, unsigned char *> g_noalloc_addr;  // device ordinal -> device address of the array
+
+// Device address of the array on `device` (current device), resolved once
+// per device: in host code the array's name only stands in for the symbol.
+unsigned char *noalloc_scratch(int device) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  auto it = g_noalloc_addr.find(device);
+  if (it != g_noalloc_addr.end()) return it->second;
+  void *ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess || !ptr) throw CudaError(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+  g_noalloc_addr[device] = static_cast<unsigned char *>(ptr);
+  return static_cast<unsigned char *>(ptr);
+}
+}  // namespace
+
+extern "C" {
+
+int sfxc_gpu_copy_spectra_noalloc(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n) {
+  if (!c || !c->have_job) return SFXC_GPU_ESTATE;
+  if (stream < 0 || stream >= (int)c->sc.size()) return fail(c, Error(SFXC_GPU_EINVAL, "bad stream index"));
+  try {
+    const StreamCtx &s = c->sc[stream];
+    const size_t rows = (size_t)c->nffts, K = (size_t)c->M + 1;
+    if (!out || n < rows * K * 2) throw Error(SFXC_GPU_EINVAL, "output buffer too small");
+    if (s.n_blocks > kNoallocMaxBlocks)
+      throw Error(SFXC_GPU_EINVAL, "integration of " + std::to_string(s.n_blocks) +
+                                       " blocks exceeds the static scratch (at most " +
+                                       std::to_string(kNoallocMaxBlocks) + " blocks of 256 samples per stream)");
+    if (rows * (size_t)c->kpad > kNoallocMaxSpectra)
+      throw Error(SFXC_GPU_EINVAL, "spectra of " + std::to_string(rows * (size_t)c->kpad) +
+                                       " values exceed the static scratch (at most " +
+                                       std::to_string(kNoallocMaxSpectra) + " complex values)");
+    CK(cudaSetDevice(c->device));
+    unsigned char *base = noalloc_scratch(c->device);
+    StreamDev d = c->hsd[stream];
+    d.block0 = 0;
+    d.n_blocks = s.n_blocks;
+    d.ts = reinterpret_cast<float *>(base + kNoallocTsOff);
+    d.bparams = reinterpret_cast<float4 *>(base + kNoallocParOff);
+    d.bamp = reinterpret_cast<float *>(base + kNoallocAmpOff);
+    StreamDev *dd = reinterpret_cast<StreamDev *>(base + kNoallocDescOff);
+    float2 *spec = reinterpret_cast<float2 *>(base + kNoallocSpecOff);
+    // every scratch element read below is written first by the same call, so
+    // nothing is cleared; the descriptor copy is ordered on the context stream
+    CK(cudaMemcpyAsync(dd, &d, sizeof(StreamDev), cudaMemcpyHostToDevice, c->st));
+    launch_fstep_block(dd, 1, s.n_blocks, c->tw256.as<float2>(), c->st);
+    const int nper = c->p.window == WINDOW_NONE ? s.hop : s.rot;
+    launch_window_fft(dd, 1, 0, (int)rows, (int)rows, c->window.as<float>(), c->twrot.as<float2>(), s.rot, nper, c->M,
+                      c->kpad, spec, false, 1.0f, c->st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy2DAsync(out, K * sizeof(float2), spec, c->kpad * sizeof(float2), K * sizeof(float2), rows,
                          cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     return (int)(rows * K * 2);

@@ -149,6 +149,12 @@ class CorrelatorNode:
         self._check(self._lib.sfxc_gpu_copy_spectra(self._h, stream, out.ctypes.data, out.size * 2))
         return out
 
+    def spectra_noalloc(self, stream, nrows, nchan):
+        """spectra() through the allocation-free entry point (static device scratch)."""
+        out = np.empty((nrows, nchan + 1), dtype=np.complex64)
+        self._check(self._lib.sfxc_gpu_copy_spectra_noalloc(self._h, stream, out.ctypes.data, out.size * 2))
+        return out
+
     def timings(self):
         t = (C.c_float * 6)()
         self._check(self._lib.sfxc_gpu_last_timings(self._h, t))

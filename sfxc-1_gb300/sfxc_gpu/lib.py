@@ -17,7 +17,7 @@ EXPORTS = [
     "sfxc_gpu_create", "sfxc_gpu_destroy", "sfxc_gpu_last_error", "sfxc_gpu_global_error",
     "sfxc_gpu_set_parameters", "sfxc_gpu_push_protocol", "sfxc_gpu_run_integration",
     "sfxc_gpu_copy_unpacked", "sfxc_gpu_copy_spectra", "sfxc_gpu_last_timings", "sfxc_gpu_delay_list",
-    "sfxc_gpu_write_protocol", "sfxc_gpu_extract_channels",
+    "sfxc_gpu_write_protocol", "sfxc_gpu_extract_channels", "sfxc_gpu_copy_spectra_noalloc",
 ]
 
 
@@ -92,6 +92,7 @@ def load(path=None):
     lib.sfxc_gpu_run_integration.argtypes = [C.c_void_p, SINK, C.c_void_p]
     lib.sfxc_gpu_copy_unpacked.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]
     lib.sfxc_gpu_copy_spectra.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]
+    lib.sfxc_gpu_copy_spectra_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]
     lib.sfxc_gpu_last_timings.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     lib.sfxc_gpu_delay_list.argtypes = [C.POINTER(DelayTable), C.c_int64, C.c_int64, C.c_int32, C.c_int32,
                                         C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
