@@ -99,66 +99,7 @@ __device__ __forceinline__ double stream_amplitude(const StreamDev &s, int64_t t
   return spline_eval(s.spline, s.spline_n, 2, time_diff_dev(t, s.scan_begin));
 }
 
-// --------------------------------------------------------------------------
-// Stockham auto-sort FFT (radix 4, one radix-2 stage when log2 N is odd),
-// natural order in and out, ping-pong between two buffers.  `tw` holds
-// exp(-2 pi i m / N) for m < N.  Threads [tid, tid+nthreads) cooperate; the
-// caller supplies the barrier (warp or CTA).
-template <int SIGN>
-__device__ __forceinline__ float2 cmul_tw(float2 a, float2 w) {
-  // a * w (SIGN<0) or a * conj(w) (SIGN>0)
-  float wi = SIGN < 0 ? w.y : -w.y;
-  return make_float2(a.x * w.x - a.y * wi, a.x * wi + a.y * w.x);
-}
-
-template <int SIGN, typename Sync>
-__device__ float2 *stockham(float2 *a, float2 *b, int N, const float2 *tw, int tid, int nthreads, Sync sync) {
-  int Ns = 1;
-  int lg = 31 - __clz(N);
-  if (lg & 1) {  // one radix-2 stage first
-    for (int j = tid; j < N / 2; j += nthreads) {
-      float2 v0 = a[j], v1 = a[j + N / 2];
-      b[2 * j] = make_float2(v0.x + v1.x, v0.y + v1.y);
-      b[2 * j + 1] = make_float2(v0.x - v1.x, v0.y - v1.y);
-    }
-    sync();
-    float2 *t = a;
-    a = b;
-    b = t;
-    Ns = 2;
-  }
-  for (; Ns < N; Ns *= 4) {
-    const int q = N / 4;
-    const int twstep = N / (Ns * 4);
-    for (int j = tid; j < q; j += nthreads) {
-      const int k = j % Ns;
-      float2 v0 = a[j], v1 = a[j + q], v2 = a[j + 2 * q], v3 = a[j + 3 * q];
-      if (Ns > 1) {
-        const int m = k * twstep;
-        v1 = cmul_tw<SIGN>(v1, tw[m]);
-        v2 = cmul_tw<SIGN>(v2, tw[2 * m]);
-        v3 = cmul_tw<SIGN>(v3, tw[3 * m]);
-      }
-      float2 a0 = make_float2(v0.x + v2.x, v0.y + v2.y);
-      float2 a1 = make_float2(v0.x - v2.x, v0.y - v2.y);
-      float2 a2 = make_float2(v1.x + v3.x, v1.y + v3.y);
-      float2 d = make_float2(v1.x - v3.x, v1.y - v3.y);
-      // a3 = d * (-i) for the forward transform, d * (+i) for the backward
-      float2 a3 = SIGN < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
-      const int o = (j / Ns) * Ns * 4 + k;
-      b[o] = make_float2(a0.x + a2.x, a0.y + a2.y);
-      b[o + Ns] = make_float2(a1.x + a3.x, a1.y + a3.y);
-      b[o + 2 * Ns] = make_float2(a0.x - a2.x, a0.y - a2.y);
-      b[o + 3 * Ns] = make_float2(a1.x - a3.x, a1.y - a3.y);
-    }
-    sync();
-    float2 *t = a;
-    a = b;
-    b = t;
-  }
-  return a;
-}
-
+// Barriers for the register FFT (fft_reg.cuh): a warp or the whole CTA.
 struct WarpSync {
   __device__ void operator()() const { __syncwarp(); }
 };

@@ -1,0 +1,199 @@
+// Register-resident FFT building blocks for the F-step kernels.
+//
+// A transform of N = 2^LOGN complex points is done by T = N/16 cooperating
+// threads that each hold 16 values in registers.  Passes are radix-16
+// Stockham steps (and one final radix-2/4/8 step when LOGN is not a multiple
+// of 4) computed in registers; between passes the values go through one
+// shared buffer of N + N/16 float2.  The padded index i + i/16 keeps both
+// access patterns of a pass -- unit stride across threads and stride 16
+// within a thread -- free of shared-memory bank conflicts.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace sfxc {
+
+__device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * w (SIGN < 0) or a * conj(w) (SIGN > 0), w = exp(-2 pi i m / N) from a table
+template <int SIGN>
+__device__ __forceinline__ float2 cmulw(float2 a, float2 w) {
+  const float wi = SIGN < 0 ? w.y : -w.y;
+  return make_float2(a.x * w.x - a.y * wi, a.x * wi + a.y * w.x);
+}
+// d * (-i) for the forward transform, d * (+i) for the backward one
+template <int SIGN>
+__device__ __forceinline__ float2 rot90(float2 d) {
+  return SIGN < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
+}
+// multiplication by exp(SIGN 2 pi i m / 16) for the constant twiddles of the 16-point kernel
+template <int SIGN, int M>
+__device__ __forceinline__ float2 w16(float2 a) {
+  constexpr float C1 = 0.92387953251128674f, S1 = 0.38268343236508978f, R2 = 0.70710678118654752f;
+  constexpr int m = M & 15;
+  if constexpr (m == 0) {
+    return a;
+  } else if constexpr (m == 4) {
+    return rot90<SIGN>(a);
+  } else if constexpr (m == 8) {
+    return make_float2(-a.x, -a.y);
+  } else if constexpr (m == 12) {
+    return rot90<-SIGN>(a);
+  } else {
+    static_assert(m == 1 || m == 2 || m == 3 || m == 6 || m == 9, "twiddle not needed");
+    // cos and the sine of the forward (negative) exponent
+    constexpr float c = m == 1 ? C1 : m == 2 ? R2 : m == 3 ? S1 : m == 6 ? -R2 : -C1;
+    constexpr float sn = m == 1 ? -S1 : m == 2 ? -R2 : m == 3 ? -C1 : m == 6 ? -R2 : S1;
+    return cmul(a, make_float2(c, SIGN < 0 ? sn : -sn));
+  }
+}
+
+template <int SIGN>
+__device__ __forceinline__ void dft2(float2 &a, float2 &b) {
+  const float2 t = a;
+  a = cadd(t, b);
+  b = csub(t, b);
+}
+// in-place 4-point DFT of (a0, a1, a2, a3), outputs in natural order
+template <int SIGN>
+__device__ __forceinline__ void dft4(float2 &a0, float2 &a1, float2 &a2, float2 &a3) {
+  const float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = rot90<SIGN>(csub(a1, a3));
+  a0 = cadd(t0, t2);
+  a2 = csub(t0, t2);
+  a1 = cadd(t1, t3);
+  a3 = csub(t1, t3);
+}
+template <int SIGN>
+__device__ __forceinline__ void dft8(float2 *v) {
+  float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+  float2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  dft4<SIGN>(e0, e1, e2, e3);
+  dft4<SIGN>(o0, o1, o2, o3);
+  o1 = w16<SIGN, 2>(o1);
+  o2 = w16<SIGN, 4>(o2);
+  o3 = w16<SIGN, 6>(o3);
+  v[0] = cadd(e0, o0);
+  v[4] = csub(e0, o0);
+  v[1] = cadd(e1, o1);
+  v[5] = csub(e1, o1);
+  v[2] = cadd(e2, o2);
+  v[6] = csub(e2, o2);
+  v[3] = cadd(e3, o3);
+  v[7] = csub(e3, o3);
+}
+// 16-point DFT as 4 x 4: x[n1 + 4 n2] -> X[k1 + 4 k2]
+template <int SIGN>
+__device__ __forceinline__ void dft16(float2 (&v)[16]) {
+#pragma unroll
+  for (int n1 = 0; n1 < 4; n1++) dft4<SIGN>(v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]);
+  // v[n1 + 4 k1] = y[n1][k1]; twiddle W16^(n1 k1)
+  v[5] = w16<SIGN, 1>(v[5]);
+  v[9] = w16<SIGN, 2>(v[9]);
+  v[13] = w16<SIGN, 3>(v[13]);
+  v[6] = w16<SIGN, 2>(v[6]);
+  v[10] = w16<SIGN, 4>(v[10]);
+  v[14] = w16<SIGN, 6>(v[14]);
+  v[7] = w16<SIGN, 3>(v[7]);
+  v[11] = w16<SIGN, 6>(v[11]);
+  v[15] = w16<SIGN, 9>(v[15]);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) dft4<SIGN>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+  // v[4 k1 + k2] = X[k1 + 4 k2]: transpose into natural order
+  float2 o[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++)
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++) o[k1 + 4 * k2] = v[4 * k1 + k2];
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = o[i];
+}
+
+// v[r] *= W^(r m) for r = 1..15, W = exp(-/+ 2 pi i / N) from the table
+// tw[j] = exp(-2 pi i j / N); four table reads, at most three products each.
+template <int SIGN>
+__device__ __forceinline__ void twiddle16(float2 (&v)[16], const float2 *__restrict__ tw, int m) {
+  const float2 w1 = __ldg(tw + m), w2 = __ldg(tw + 2 * m), w4 = __ldg(tw + 4 * m), w8 = __ldg(tw + 8 * m);
+  const float2 w3 = cmul(w1, w2), w5 = cmul(w4, w1), w6 = cmul(w4, w2), w7 = cmul(w4, w3);
+  const float2 w[8] = {make_float2(1.f, 0.f), w1, w2, w3, w4, w5, w6, w7};
+#pragma unroll
+  for (int r = 1; r < 8; r++) v[r] = cmulw<SIGN>(v[r], w[r]);
+  v[8] = cmulw<SIGN>(v[8], w8);
+#pragma unroll
+  for (int r = 9; r < 16; r++) v[r] = cmulw<SIGN>(v[r], cmul(w8, w[r - 8]));
+}
+
+// Transform of N = 2^LOGN points by T = N/16 threads (t = 0..T-1).
+// In: v[r] = x[t + r T].  `sm`: this transform's buffer of padi(N) float2.
+// `tw`: exp(-2 pi i j / N) for j < N.  `sync` is the barrier over all threads
+// sharing the barrier (warp or CTA); every one of them must call this.
+// Out (TO_SMEM): X[k] at sm[padi(k)], visible after the final barrier.
+// Out (!TO_SMEM, LOGN % 4 == 0 only): v[r] = X[t + r T]; sm is free again
+// once every thread has returned (the caller syncs before reusing it).
+template <int SIGN, int LOGN, bool TO_SMEM, typename Sync>
+__device__ __forceinline__ void fft_reg(float2 (&v)[16], float2 *sm, int t, const float2 *__restrict__ tw,
+                                        Sync sync) {
+  constexpr int N = 1 << LOGN, T = N / 16, NR16 = LOGN / 4, LAST = LOGN % 4;
+  static_assert(NR16 >= 1, "at least 16 points");
+  static_assert(TO_SMEM || LAST == 0, "register output needs a final radix-16 pass");
+  int Ns = 1;
+#pragma unroll
+  for (int p = 0; p < NR16; p++) {
+    if (p > 0) {
+#pragma unroll
+      for (int r = 0; r < 16; r++) v[r] = sm[padi(t + r * T)];
+      sync();
+      const int k = t & (Ns - 1);
+      twiddle16<SIGN>(v, tw, k * (N / (16 * Ns)));
+    }
+    dft16<SIGN>(v);
+    if (p == NR16 - 1 && LAST == 0 && !TO_SMEM) return;  // v[r] = X[t + r T]
+    const int base = (t - (t & (Ns - 1))) * 16 + (t & (Ns - 1));
+#pragma unroll
+    for (int r = 0; r < 16; r++) sm[padi(base + r * Ns)] = v[r];
+    sync();
+    Ns *= 16;
+  }
+  if constexpr (LAST > 0) {
+    constexpr int R = 1 << LAST, G = 16 / R, Q = N / R;  // Ns == Q here
+#pragma unroll
+    for (int g = 0; g < G; g++)
+#pragma unroll
+      for (int r = 0; r < R; r++) v[g * R + r] = sm[padi(t + g * T + r * Q)];
+    sync();
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+      const int j = t + g * T;
+      float2 *u = v + g * R;
+      if constexpr (R == 2) {
+        u[1] = cmulw<SIGN>(u[1], __ldg(tw + j));
+        dft2<SIGN>(u[0], u[1]);
+      } else if constexpr (R == 4) {
+        const float2 w1 = __ldg(tw + j), w2 = __ldg(tw + 2 * j);
+        u[1] = cmulw<SIGN>(u[1], w1);
+        u[2] = cmulw<SIGN>(u[2], w2);
+        u[3] = cmulw<SIGN>(u[3], cmul(w1, w2));
+        dft4<SIGN>(u[0], u[1], u[2], u[3]);
+      } else {
+        const float2 w1 = __ldg(tw + j), w2 = __ldg(tw + 2 * j), w4 = __ldg(tw + 4 * j);
+        const float2 w3 = cmul(w1, w2);
+        u[1] = cmulw<SIGN>(u[1], w1);
+        u[2] = cmulw<SIGN>(u[2], w2);
+        u[3] = cmulw<SIGN>(u[3], w3);
+        u[4] = cmulw<SIGN>(u[4], w4);
+        u[5] = cmulw<SIGN>(u[5], cmul(w4, w1));
+        u[6] = cmulw<SIGN>(u[6], cmul(w4, w2));
+        u[7] = cmulw<SIGN>(u[7], cmul(w4, w3));
+        dft8<SIGN>(u);
+      }
+#pragma unroll
+      for (int r = 0; r < R; r++) sm[padi(j + r * Q)] = u[r];
+    }
+    sync();
+  }
+}
+
+}  // namespace sfxc

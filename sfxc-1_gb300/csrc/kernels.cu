@@ -2,12 +2,13 @@
 //
 //   fstep_block_kernel   unpack (plan segments + 1/2-bit lookup) -> rfft(256)
 //                        -> fractional-delay phase ramp -> complex ifft(256)
-//                        -> fringe rotation; one warp per 256-sample block.
+//                        -> fringe rotation; 16 threads per pair of blocks.
 //                        Delay_correction::fractional_bit_shift / fringe_stopping
 //                        (sfxc/src/delay_correction.cc:82-184) on the unpacked
 //                        samples of Bit2float_worker (sfxc/src/bit2float_worker.cc:327-425).
 //   window_fft_kernel    window, sideband flip, real FFT of 2M samples, channel
-//                        selection (delay_correction.cc:57-75); one CTA per row.
+//                        selection (delay_correction.cc:57-75); M/16 threads per row.
+// Both FFT stages are the register-resident radix-16 transforms of fft_reg.cuh.
 //   bitstat_kernel       byte histograms with cal-diode on/off split
 //                        (bit_statistics.cc:36-47, bit2float_worker.cc:341-346).
 //   xcorr_f32_kernel     X-step on CUDA cores, 4x4 stream tiles per thread
@@ -18,82 +19,102 @@
 #include <cstdio>
 
 #include "device.cuh"
+#include "fft_reg.cuh"
 #include "kernels.hpp"
 
 namespace sfxc {
 
 // ------------------------------------------------------------------------
-// F-step, stage 1: one warp per block of 256 samples.
-// tw holds exp(-2 pi i m / 256) for m < 256 followed by exp(-2 pi i m / 128) for m < 128.
+// F-step, stage 1: 16 threads per pair of 256-sample blocks, 32 blocks per CTA.
+// One forward 256-point complex FFT of x_b + i x_{b+1} gives both real
+// spectra (X[k] +/- conj X[256-k]); per block: DC and Nyquist halved, phase
+// ramp exp(-i (c + k l)) on k <= 128, upper half zero, inverse 256-point FFT,
+// fringe rotation of the real part.  tw holds exp(-2 pi i m / 256), m < 256.
 __global__ void __launch_bounds__(256) fstep_block_kernel(const StreamDev *__restrict__ streams,
                                                          const float2 *__restrict__ tw) {
-  __shared__ float2 sbuf[8][2][kNd];
-  __shared__ float2 stw[kNd + kNd / 2];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < kNd + kNd / 2; i += blockDim.x) stw[i] = tw[i];
-  __syncthreads();
+  __shared__ float2 sbuf[16][kNd + kNd / 16];
+  const int t = threadIdx.x & 15, grp = threadIdx.x >> 4;
   const StreamDev &s = streams[blockIdx.y];
-  const int bl = blockIdx.x * 8 + warp;
-  if (bl >= s.n_blocks) return;
-  const int b = s.block0 + bl;  // block index within the integration
-  float2 *A = sbuf[warp][0], *B = sbuf[warp][1];
-  float *xa = reinterpret_cast<float *>(A);
-  const float4 prm = s.bparams[bl];  // block_params_kernel
-  const float c32 = prm.x, l32 = prm.y, phi0 = prm.z, dphi = prm.w;
-  const float amp = s.bamp[bl];
+  const int first = blockIdx.x * 32;  // first block of the CTA
+  if (first + (threadIdx.x >> 5) * 4 >= s.n_blocks) return;  // whole warps only (warp barriers below)
+  const int bl0 = first + grp * 2;
+  const bool ok0 = bl0 < s.n_blocks, ok1 = bl0 + 1 < s.n_blocks;
+  float2 *sm = sbuf[grp];
+  float2 v[16];
+  {  // unpack the two blocks through the plan
+    const int o0 = (s.block0 + bl0) * kNd;
+    int si = ok0 ? find_segment(s, o0) : 0;
+#pragma unroll
+    for (int r = 0; r < 16; r++) v[r].x = ok0 ? gather_sample(s, o0 + t + 16 * r, si) : 0.0f;
+#pragma unroll
+    for (int r = 0; r < 16; r++) v[r].y = ok1 ? gather_sample(s, o0 + kNd + t + 16 * r, si) : 0.0f;
+  }
+  fft_reg<-1, 8, true>(v, sm, t, tw, WarpSync());
 
-  // ---- unpack 256 samples through the plan
-  {
-    const int o0 = b * kNd;
-    int si = find_segment(s, o0);
-    for (int q = 0; q < 8; q++) {
-      const int n = lane + 32 * q;
-      xa[n] = gather_sample(s, o0 + n, si);
+  // split, halve DC/Nyquist, phase ramp; block 0 into v, block 1 into g1
+  const float4 p0 = ok0 ? s.bparams[bl0] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 p1 = ok1 ? s.bparams[bl0 + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+  float a_s, a_c, as_s, as_c, b_s, b_c, bs_s, bs_c;
+  sincosf(fmaf((float)t, p0.y, p0.x), &a_s, &a_c);
+  sincosf(16.0f * p0.y, &as_s, &as_c);
+  sincosf(fmaf((float)t, p1.y, p1.x), &b_s, &b_c);
+  sincosf(16.0f * p1.y, &bs_s, &bs_c);
+  float2 g1[9];
+#pragma unroll
+  for (int r = 0; r < 9; r++) {
+    const int k = t + 16 * r;
+    float2 f0 = make_float2(0.f, 0.f), f1 = make_float2(0.f, 0.f);
+    if (r < 8 || t == 0) {
+      const float2 xk = sm[padi(k & (kNd - 1))], xm = sm[padi((kNd - k) & (kNd - 1))];
+      const float h = (k == 0 || k == kNd / 2) ? 0.25f : 0.5f;  // 1/2 of the split, DC and Nyquist halved again
+      const float er = h * (xk.x + xm.x), ei = h * (xk.y - xm.y);
+      const float orr = h * (xk.y + xm.y), oi = -h * (xk.x - xm.x);
+      // F * (cos phi, -sin phi)
+      f0 = make_float2(er * a_c + ei * a_s, ei * a_c - er * a_s);
+      f1 = make_float2(orr * b_c + oi * b_s, oi * b_c - orr * b_s);
     }
+    v[r] = f0;
+    g1[r] = f1;
+    float c2 = a_c * as_c - a_s * as_s;
+    a_s = a_s * as_c + a_c * as_s;
+    a_c = c2;
+    c2 = b_c * bs_c - b_s * bs_s;
+    b_s = b_s * bs_c + b_c * bs_s;
+    b_c = c2;
   }
+#pragma unroll
+  for (int r = 9; r < 16; r++) v[r] = make_float2(0.f, 0.f);
   __syncwarp();
-  // ---- rfft(256) via a 128-point complex FFT of (x[2n], x[2n+1])
-  float2 *Z = stockham<-1>(A, B, kNd / 2, stw + kNd, lane, 32, WarpSync());
-  float2 *G = (Z == A) ? B : A;
-  // phase ramp exp(-i (c + k l)) for k = lane + 32 q: one sincos for the
-  // lane's first bin and one for the 32-bin step, then complex rotations
-  float rs, rc, ss, sc;
-  sincosf(fmaf((float)lane, l32, c32), &rs, &rc);
-  sincosf(32.0f * l32, &ss, &sc);
-  for (int k = lane; k <= kNd / 2; k += 32) {
-    const float cs = rc, sn = rs;
-    rc = cs * sc - sn * ss;
-    rs = sn * sc + cs * ss;
-    const float2 zk = Z[k & (kNd / 2 - 1)];
-    const float2 zc = Z[(kNd / 2 - k) & (kNd / 2 - 1)];
-    const float er = 0.5f * (zk.x + zc.x), ei = 0.5f * (zk.y - zc.y);
-    const float orr = 0.5f * (zk.y + zc.y), oi = -0.5f * (zk.x - zc.x);
-    const float2 w = stw[k & (kNd - 1)];
-    float fr = er + (orr * w.x - oi * w.y);
-    float fi = ei + (orr * w.y + oi * w.x);
-    if (k == 0 || k == kNd / 2) {  // DC and Nyquist halved
-      fr *= 0.5f;
-      fi *= 0.5f;
+
+  // per block: inverse FFT (result in registers, v[r] = z[t + 16 r]), fringe rotation, store
+#pragma unroll 1
+  for (int h = 0; h < 2; h++) {
+    if (h == 1) {
+#pragma unroll
+      for (int r = 0; r < 9; r++) v[r] = g1[r];
+#pragma unroll
+      for (int r = 9; r < 16; r++) v[r] = make_float2(0.f, 0.f);
     }
-    // F * (cos phi, -sin phi)
-    G[k] = make_float2(fr * cs + fi * sn, fi * cs - fr * sn);
-  }
-  for (int k = kNd / 2 + 1 + lane; k < kNd; k += 32) G[k] = make_float2(0.f, 0.f);
-  __syncwarp();
-  float2 *Y = stockham<+1>(G, Z, kNd, stw, lane, 32, WarpSync());
-  // ---- fringe rotation and store
-  float *out = s.ts + (int64_t)bl * kNd;
-  sincosf(fmaf((float)lane, dphi, phi0), &rs, &rc);
-  sincosf(32.0f * dphi, &ss, &sc);
-  rs *= amp;
-  rc *= amp;
-  for (int q = 0; q < 8; q++) {
-    const int n = lane + 32 * q;
-    const float2 z = Y[n];
-    out[n] = z.x * rc + z.y * rs;
-    const float c2 = rc * sc - rs * ss;
-    rs = rs * sc + rc * ss;
-    rc = c2;
+    fft_reg<+1, 8, false>(v, sm, t, tw, WarpSync());
+    const int bl = bl0 + h;
+    if (bl < s.n_blocks) {
+      const float4 prm = h ? p1 : p0;
+      const float amp = s.bamp[bl];
+      float rs, rc, ss, sc;
+      sincosf(fmaf((float)t, prm.w, prm.z), &rs, &rc);
+      sincosf(16.0f * prm.w, &ss, &sc);
+      rs *= amp;
+      rc *= amp;
+      float *out = s.ts + (int64_t)bl * kNd + t;
+#pragma unroll
+      for (int r = 0; r < 16; r++) {
+        out[16 * r] = v[r].x * rc + v[r].y * rs;
+        const float c2 = rc * sc - rs * ss;
+        rs = rs * sc + rc * ss;
+        rc = c2;
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -171,56 +192,78 @@ __global__ void extract_kernel(const uint8_t *__restrict__ in, int64_t nout, int
 }
 
 // ------------------------------------------------------------------------
-// F-step, stage 2: windowed real FFT of rot samples per output row.
-template <int OUT_TC>
-__global__ void __launch_bounds__(512) window_fft_kernel(const StreamDev *__restrict__ streams, int row0,
-                                                        int nrows_total, const float *__restrict__ window,
-                                                        const float2 *__restrict__ tw_rot, int nper, int M,
-                                                        int kpad, void *__restrict__ spec_out, float tc_scale) {
+// F-step, stage 2: windowed real FFT of rot = 2N samples per output row as an
+// N-point complex FFT (N = 2^LOGN) of (x[2e], x[2e+1]) by N/16 threads, G rows
+// per CTA; the first pass reads the samples straight from HBM.
+template <int LOGN>
+struct WinShape {
+  static constexpr int N = 1 << LOGN, T = N / 16, G = T < 256 ? 256 / T : 1, THREADS = T * G;
+  static constexpr size_t SMEM = (size_t)G * (N + N / 16) * sizeof(float2);
+};
+
+template <int LOGN, int OUT_TC>
+__global__ void __launch_bounds__(WinShape<LOGN>::THREADS) window_fft_kernel(
+    const StreamDev *__restrict__ streams, int row0, int nrows, int nrows_total, const float *__restrict__ window,
+    const float2 *__restrict__ tw_rot, int nper, int M, int kpad, void *__restrict__ spec_out, float tc_scale) {
+  using S = WinShape<LOGN>;
+  constexpr int N = S::N, T = S::T;
   extern __shared__ float2 dsm[];
+  const int t = threadIdx.x % T, g = threadIdx.x / T;
   const StreamDev &s = streams[blockIdx.y];
-  const int r = row0 + blockIdx.x;
-  const int rot = s.rot, half = rot / 2, hop = rot / 2;
-  float2 *A = dsm, *B = dsm + half;
-  float *xa = reinterpret_cast<float *>(A);
-  const float *ts = s.ts + (int64_t)r * hop;
-  for (int i = threadIdx.x; i < rot; i += blockDim.x) {
-    float v = i < nper ? ts[i] * window[i] : 0.0f;
-    if (s.flip && (i & 1)) v = -v;
-    xa[i] = v;
+  const int rr = blockIdx.x * S::G + g;
+  const bool ok = rr < nrows;
+  const int r = row0 + rr;
+  float2 *sm = dsm + g * (N + N / 16);
+  const int rot = 2 * N;
+  float2 v[16];
+  {
+    const float *ts = s.ts + (int64_t)r * N;  // hop = rot / 2
+    const float sgn = s.flip ? -1.0f : 1.0f;  // sideband flip negates odd samples
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      const int i = 2 * (t + q * T);
+      float2 x = make_float2(0.f, 0.f);
+      if (ok && i + 1 < nper) {
+        const float2 a = *reinterpret_cast<const float2 *>(ts + i);
+        const float2 w = __ldg(reinterpret_cast<const float2 *>(window + i));
+        x = make_float2(a.x * w.x, sgn * (a.y * w.y));
+      } else if (ok && i < nper) {
+        x.x = ts[i] * window[i];
+      }
+      v[q] = x;
+    }
   }
-  __syncthreads();
-  // tw_rot holds exp(-2 pi i m / rot) for m < rot, followed by the table of the
-  // half-length transform, exp(-2 pi i m / (rot/2)) for m < rot/2.
-  float2 *Z = stockham<-1>(A, B, half, tw_rot + rot, threadIdx.x, blockDim.x, BlockSync());
-  const int stride = kpad;
-  for (int i = threadIdx.x; i <= M; i += blockDim.x) {
+  // tw_rot holds exp(-2 pi i m / rot) for m < rot, followed by exp(-2 pi i m / N) for m < N.
+  fft_reg<-1, LOGN, true>(v, sm, t, tw_rot + rot, BlockSync());
+  if (!ok) return;
+  for (int i = t; i <= M; i += T) {
     const int q = s.output_offset + i - s.temp_fft_offset;
     float fr = 0.f, fi = 0.f;
-    if (q >= 0 && q <= half) {
-      const float2 zk = Z[q & (half - 1)];
-      const float2 zc = Z[(half - q) & (half - 1)];
+    if (q >= 0 && q <= N) {
+      const float2 zk = sm[padi(q & (N - 1))];
+      const float2 zc = sm[padi((N - q) & (N - 1))];
       const float er = 0.5f * (zk.x + zc.x), ei = 0.5f * (zk.y - zc.y);
       const float orr = 0.5f * (zk.y + zc.y), oi = -0.5f * (zk.x - zc.x);
-      const float2 w = tw_rot[q & (rot - 1)];
+      const float2 w = __ldg(tw_rot + (q & (rot - 1)));
       fr = er + (orr * w.x - oi * w.y);
       fi = ei + (orr * w.y + oi * w.x);
     }
-    const int64_t idx = ((int64_t)blockIdx.y * nrows_total + r) * stride + i;
+    const int64_t idx = ((int64_t)blockIdx.y * nrows_total + r) * kpad + i;
     if (OUT_TC) {
       const float sr_ = fr * tc_scale, si_ = fi * tc_scale;
       const __half hr = __float2half_rn(sr_), hi_ = __float2half_rn(si_);
       const __half lr = __float2half_rn(sr_ - __half2float(hr)), li = __float2half_rn(si_ - __half2float(hi_));
-      __half2 *o = reinterpret_cast<__half2 *>(spec_out) + idx * 2;
-      o[0] = __halves2half2(hr, hi_);
-      o[1] = __halves2half2(lr, li);
+      const __half2 h0 = __halves2half2(hr, hi_), h1 = __halves2half2(lr, li);
+      uint2 u;
+      u.x = *reinterpret_cast<const unsigned *>(&h0);
+      u.y = *reinterpret_cast<const unsigned *>(&h1);
+      reinterpret_cast<uint2 *>(spec_out)[idx] = u;
     } else {
       reinterpret_cast<float2 *>(spec_out)[idx] = make_float2(fr, fi);
     }
   }
 }
 
-// ------------------------------------------------------------------------
 // Bit statistics over counted-byte ranges.  Work items: (stream, range, offset).
 __global__ void bitstat_kernel(const StreamDev *__restrict__ streams, const int4 *__restrict__ items, int nitems) {
   __shared__ unsigned int h[512];
@@ -476,7 +519,7 @@ __global__ void normalize_kernel(const float2 *__restrict__ acc, int kpad, int M
 void launch_fstep_block(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256,
                         cudaStream_t st) {
   block_params_kernel<<<dim3((max_blocks + 127) / 128, nstreams), 128, 0, st>>>(d_streams);
-  dim3 grid((max_blocks + 7) / 8, nstreams);
+  dim3 grid((max_blocks + 31) / 32, nstreams);
   fstep_block_kernel<<<grid, 256, 0, st>>>(d_streams, tw256);
 }
 
@@ -489,20 +532,49 @@ void launch_extract(const uint8_t *in, int64_t nout, int N, int bits, int nsub, 
   extract_kernel<<<dim3((unsigned)((nout + 255) / 256), nsub), 256, 0, st>>>(in, nout, N, bits, fan_out, tracks, out);
 }
 
+template <int LOGN, int OUT_TC>
+static void window_fft_launch(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
+                              const float *window, const float2 *tw_rot, int nper, int M, int kpad, void *spec,
+                              float tc_scale, cudaStream_t st) {
+  using S = WinShape<LOGN>;
+  dim3 grid((nrows + S::G - 1) / S::G, nstreams);
+  cudaFuncSetAttribute(window_fft_kernel<LOGN, OUT_TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+  window_fft_kernel<LOGN, OUT_TC><<<grid, S::THREADS, S::SMEM, st>>>(d_streams, row0, nrows, nrows_total, window,
+                                                                      tw_rot, nper, M, kpad, spec, tc_scale);
+}
+
+template <int OUT_TC>
+static void window_fft_dispatch(int logn, const StreamDev *d_streams, int nstreams, int row0, int nrows,
+                                int nrows_total, const float *window, const float2 *tw_rot, int nper, int M, int kpad,
+                                void *spec, float tc_scale, cudaStream_t st) {
+  switch (logn) {
+#define SFXC_WIN_CASE(L)                                                                                         \
+  case L:                                                                                                        \
+    window_fft_launch<L, OUT_TC>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad, \
+                                 spec, tc_scale, st);                                                            \
+    break;
+    SFXC_WIN_CASE(8)
+    SFXC_WIN_CASE(9)
+    SFXC_WIN_CASE(10)
+    SFXC_WIN_CASE(11)
+    SFXC_WIN_CASE(12)
+    SFXC_WIN_CASE(13)
+#undef SFXC_WIN_CASE
+    default:
+      break;  // sizes outside 2^9..2^14 samples are rejected by set_parameters
+  }
+}
+
 void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                        const float *window, const float2 *tw_rot, int rot, int nper, int M, int kpad, void *spec,
                        bool tc, float tc_scale, cudaStream_t st) {
-  dim3 grid(nrows, nstreams);
-  const size_t smem = (size_t)rot * sizeof(float2);  // two buffers of rot/2
-  if (tc) {
-    cudaFuncSetAttribute(window_fft_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    window_fft_kernel<1><<<grid, 512, smem, st>>>(d_streams, row0, nrows_total, window, tw_rot, nper, M, kpad, spec,
-                                                  tc_scale);
-  } else {
-    cudaFuncSetAttribute(window_fft_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    window_fft_kernel<0><<<grid, 512, smem, st>>>(d_streams, row0, nrows_total, window, tw_rot, nper, M, kpad, spec,
-                                                  tc_scale);
-  }
+  const int logn = 30 - __builtin_clz((unsigned)rot);  // log2(rot / 2)
+  if (tc)
+    window_fft_dispatch<1>(logn, d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad, spec,
+                           tc_scale, st);
+  else
+    window_fft_dispatch<0>(logn, d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad, spec,
+                           tc_scale, st);
 }
 
 void launch_bitstat(const StreamDev *d_streams, const int4 *d_items, int nitems, cudaStream_t st) {
