@@ -153,13 +153,22 @@ def run_gpu(args):
     for n, j in zip(nodes, jobs):
         n.set_parameters(j)
 
+    host_ms = {"set_parameters": 0.0, "push_protocol": 0.0, "run_integration": 0.0}
+
     def step():
         dev_ms, launches, out_bytes = 0.0, 0, 0
         for n, j in zip(nodes, jobs):
+            t0 = time.perf_counter()
             n.set_parameters(j)  # each step correlates the job's integration afresh
+            t1 = time.perf_counter()
             for k, buf in enumerate(j["pinned"]):
                 n._check(n._lib.sfxc_gpu_push_protocol(n._h, k, C.c_void_p(buf.ctypes.data), buf.size))
+            t2 = time.perf_counter()
             o, _ = n.run_integration()
+            t3 = time.perf_counter()
+            host_ms["set_parameters"] += (t1 - t0) * 1e3
+            host_ms["push_protocol"] += (t2 - t1) * 1e3
+            host_ms["run_integration"] += (t3 - t2) * 1e3
             out_bytes += len(o)
             t = n.timings()
             dev_ms += t["total_ms"]
@@ -171,6 +180,8 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    for k in host_ms:
+        host_ms[k] = 0.0
     clocks = ClockSampler()
     clocks.start()
     t0 = time.perf_counter()
@@ -211,6 +222,7 @@ def run_gpu(args):
         "gpu_launches": launches,
         "clocks": clk,
         "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in per_kernel.items() if k != "launches"},
+        "host_call_ms_per_step": {k: round(v / args.steps, 3) for k, v in host_ms.items()},
         "real_time_factor": round(e2e / (total / (args.integration_us / 1e6) / 1e9), 2),
     }
     line["roofline"] = roofline(args, per_kernel, total)

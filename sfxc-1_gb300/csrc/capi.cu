@@ -250,7 +250,7 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
     }
   jt.ntiles = (int)jt.tiles.size() / 2;
   if (xcorr_tpw(jt.ntiles) < 0) throw Error(SFXC_GPU_EINVAL, "too many streams for the X-step tiling (max 48 tiles)");
-  if (c->x_mode == SFXC_GPU_X_TC_HILO && N > 32)
+  if (c->x_mode == SFXC_GPU_X_TC_HILO && N > kTcSlots)
     throw Error(SFXC_GPU_EINVAL, "the tensor-core X-step takes at most 32 streams per job");
   upload(c->blmap, jt.blmap.data(), jt.blmap.size() * 4, c->st);
   upload(c->tiles, jt.tiles.data(), jt.tiles.size() * 4, c->st);
@@ -493,7 +493,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   // magnitudes sit near 1 (|X| ~ sqrt(2M * 0.375 * E[x^2]) for a Hann window)
   const bool tc_x = c->x_mode == SFXC_GPU_X_TC_HILO && !pulsar;
   const float tc_scale = std::ldexp(1.0f, -(int)std::lround(0.5 * std::log2(2.0 * M * 10.0)));
-  c->spec.ensure((size_t)N * max_rows * kpad * sizeof(float2));
+  // FP32 spectra: [stream][row][kpad]; TC spectra: [row][kpad][32 stream slots], 8 bytes each
+  c->spec.ensure((size_t)(tc_x ? kTcSlots : N) * max_rows * kpad * sizeof(float2));
   c->derr.ensure(sizeof(int));
   CK(cudaMemsetAsync(c->derr.p, 0, sizeof(int), st));
   for (int i = 0; i < N; i++) {
@@ -578,8 +579,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->evpool[ev + 2], st));
     if (tc_x) {
-      launch_xcorr_tc(c->spec.p, max_rows, kpad, N, nrows, K, c->blmap.as<int>(), c->jt.npad,
-                      1.0f / (tc_scale * tc_scale), c->acc.as<float2>(), c->derr.as<int>(), st);
+      CK(launch_xcorr_tc(c->spec.p, nrows, kpad, K, c->blmap.as<int>(), c->jt.npad, 1.0f / (tc_scale * tc_scale),
+                         c->acc.as<float2>(), c->derr.as<int>(), st));
     } else if (pulsar) {
       launch_pulsar(c->spec.as<float2>(), max_rows, kpad, N, c->jt.npad, nrows, K, c->tiles.as<int>(), c->jt.ntiles,
                     c->blmap.as<int>(), nbl, psr_start_phase, psr_rate, fft_duration, c->offsets.as<double>(),
@@ -731,7 +732,8 @@ int sfxc_gpu_push_protocol(sfxc_gpu_ctx *c, int32_t stream, const uint8_t *bytes
     CK(cudaSetDevice(c->device));
     // records refer to the bytes by their offset in the stream's device buffer
     std::vector<Record> recs = parse_protocol(bytes, n, s.dev_bytes);
-    const size_t need = (size_t)(s.dev_bytes + (int64_t)n);
+    // 8 spare bytes: the unpack reads whole 32-bit words, one past the last sample
+    const size_t need = (size_t)(s.dev_bytes + (int64_t)n) + 8;
     if (need > s.src.cap) {  // grow, keeping what this integration already pushed
       DevBuf grown;
       grown.ensure(std::max(need, s.src.cap * 3 / 2));

@@ -7,6 +7,7 @@
 namespace sfxc {
 
 constexpr int kNd = 256;  // fft_size_delaycor handled by the fused block kernel
+constexpr int kTcSlots = 32;  // stream slots per (row, channel) of the tensor-core spectra layout
 
 // One plan segment: output samples [out0, out0+n) come from source bit src_bit
 // onward (bits per sample apart); src_bit < 0 means zeros (invalid or an
@@ -106,6 +107,13 @@ struct WarpSync {
 struct BlockSync {
   __device__ void operator()() const { __syncthreads(); }
 };
+
+// 2-bit code -> sample value, the Bit2float_worker table (sfxc/src/bit2float_worker.cc:4-10):
+// 0 -> -7, 1 -> -2, 2 -> +2, 3 -> +7.
+__device__ __forceinline__ float code_value2(uint32_t c) {
+  const float mag = ((c ^ (c >> 1)) & 1) ? 2.0f : 7.0f;
+  return (c & 2) ? mag : -mag;
+}
 
 // Unpacked sample `o` (index within the integration) through the plan;
 // `si` is a segment cursor that only moves forward for increasing `o`.

@@ -30,7 +30,7 @@ namespace sfxc {
 // spectra (X[k] +/- conj X[256-k]); per block: DC and Nyquist halved, phase
 // ramp exp(-i (c + k l)) on k <= 128, upper half zero, inverse 256-point FFT,
 // fringe rotation of the real part.  tw holds exp(-2 pi i m / 256), m < 256.
-__global__ void __launch_bounds__(256) fstep_block_kernel(const StreamDev *__restrict__ streams,
+__global__ void __launch_bounds__(256, 4) fstep_block_kernel(const StreamDev *__restrict__ streams,
                                                          const float2 *__restrict__ tw) {
   __shared__ float2 sbuf[16][kNd + kNd / 16];
   const int t = threadIdx.x & 15, grp = threadIdx.x >> 4;
@@ -44,10 +44,46 @@ __global__ void __launch_bounds__(256) fstep_block_kernel(const StreamDev *__res
   {  // unpack the two blocks through the plan
     const int o0 = (s.block0 + bl0) * kNd;
     int si = ok0 ? find_segment(s, o0) : 0;
+    const DevSegment sg = s.segs[si];
+    if (ok1 && sg.src_bit >= 0 && o0 >= sg.out0 && o0 + 2 * kNd <= sg.out0 + sg.n) {
+      // common case: both blocks inside one segment of recorded samples, so
+      // sample t + 16 r (r < 32 over the pair) sits at bit p + 16 r * bits of
+      // the stream; whole 32-bit words and funnel shifts, no segment walk
+      // (the input buffer has spare bytes after the last sample)
+      const uint32_t *w = reinterpret_cast<const uint32_t *>(s.src);
+      const int64_t bit0 = sg.src_bit + (int64_t)(o0 - sg.out0) * s.bits;
+      if (s.bits == 2) {
+        const int64_t p = bit0 + 2 * t;
+        const int64_t w0 = p >> 5;
+        const uint32_t sh = (uint32_t)p & 31;
+        uint32_t lo = __ldg(w + w0);
 #pragma unroll
-    for (int r = 0; r < 16; r++) v[r].x = ok0 ? gather_sample(s, o0 + t + 16 * r, si) : 0.0f;
+        for (int r = 0; r < 32; r++) {
+          const uint32_t hi = __ldg(w + w0 + r + 1);
+          const float x = code_value2(__funnelshift_r(lo, hi, sh) & 3);
+          if (r < 16)
+            v[r].x = x;
+          else
+            v[r - 16].y = x;
+          lo = hi;
+        }
+      } else {
 #pragma unroll
-    for (int r = 0; r < 16; r++) v[r].y = ok1 ? gather_sample(s, o0 + kNd + t + 16 * r, si) : 0.0f;
+        for (int r = 0; r < 32; r++) {
+          const int64_t p = bit0 + t + 16 * r;
+          const float x = ((__ldg(w + (p >> 5)) >> (p & 31)) & 1) ? 5.0f : -5.0f;
+          if (r < 16)
+            v[r].x = x;
+          else
+            v[r - 16].y = x;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < 16; r++) v[r].x = ok0 ? gather_sample(s, o0 + t + 16 * r, si) : 0.0f;
+#pragma unroll
+      for (int r = 0; r < 16; r++) v[r].y = ok1 ? gather_sample(s, o0 + kNd + t + 16 * r, si) : 0.0f;
+    }
   }
   fft_reg<-1, 8, true>(v, sm, t, tw, WarpSync());
 
@@ -193,32 +229,65 @@ __global__ void extract_kernel(const uint8_t *__restrict__ in, int64_t nout, int
 
 // ------------------------------------------------------------------------
 // F-step, stage 2: windowed real FFT of rot = 2N samples per output row as an
-// N-point complex FFT (N = 2^LOGN) of (x[2e], x[2e+1]) by N/16 threads, G rows
-// per CTA; the first pass reads the samples straight from HBM.
-template <int LOGN>
+// N-point complex FFT (N = 2^LOGN) of (x[2e], x[2e+1]) by T = N/16 threads.
+// A CTA of 1024 threads transforms SPC streams x RPC rows (one group of T
+// threads each); the first pass reads the samples straight from HBM.  For
+// the tensor-core layout ([row][channel][32 stream slots] x 8 B) one thread
+// then writes the SPC streams of a channel as one contiguous 8*SPC-byte piece
+// (a whole 32-byte sector for SPC = 4).
+template <int LOGN, int SPCMAX>
 struct WinShape {
-  static constexpr int N = 1 << LOGN, T = N / 16, G = T < 256 ? 256 / T : 1, THREADS = T * G;
-  static constexpr size_t SMEM = (size_t)G * (N + N / 16) * sizeof(float2);
+  static constexpr int N = 1 << LOGN, T = N / 16;
+  static constexpr int SPC = T * SPCMAX <= 1024 ? SPCMAX : 1024 / T;  // streams per CTA
+  static constexpr int RPC = T < 256 ? 256 / T : 1;                   // rows per CTA
+  static constexpr int THREADS = SPC * RPC * T;
+  static constexpr int BUF = N + N / 16;  // padded FFT buffer (float2) of one group
+  static constexpr size_t SMEM = (size_t)SPC * RPC * BUF * sizeof(float2);
+  static_assert(THREADS <= 1024, "at most 1024 threads");
 };
 
-template <int LOGN, int OUT_TC>
-__global__ void __launch_bounds__(WinShape<LOGN>::THREADS) window_fft_kernel(
-    const StreamDev *__restrict__ streams, int row0, int nrows, int nrows_total, const float *__restrict__ window,
-    const float2 *__restrict__ tw_rot, int nper, int M, int kpad, void *__restrict__ spec_out, float tc_scale) {
-  using S = WinShape<LOGN>;
-  constexpr int N = S::N, T = S::T;
+__device__ __forceinline__ uint2 tc_split(float fr, float fi, float tc_scale) {
+  const float sr_ = fr * tc_scale, si_ = fi * tc_scale;
+  const __half hr = __float2half_rn(sr_), hi_ = __float2half_rn(si_);
+  const __half lr = __float2half_rn(sr_ - __half2float(hr)), li = __float2half_rn(si_ - __half2float(hi_));
+  const __half2 h0 = __halves2half2(hr, hi_), h1 = __halves2half2(lr, li);
+  return make_uint2(*reinterpret_cast<const unsigned *>(&h0), *reinterpret_cast<const unsigned *>(&h1));
+}
+
+// Channel i of one group's transform Z (natural order, padded): the real-FFT
+// split for output bin q = output_offset + i - temp_fft_offset (zero outside 0..N).
+template <int N>
+__device__ __forceinline__ float2 real_bin(const float2 *Z, const float2 *__restrict__ tw_rot, int q) {
+  if (q < 0 || q > N) return make_float2(0.f, 0.f);
+  const float2 zk = Z[padi(q & (N - 1))];
+  const float2 zc = Z[padi((N - q) & (N - 1))];
+  const float er = 0.5f * (zk.x + zc.x), ei = 0.5f * (zk.y - zc.y);
+  const float orr = 0.5f * (zk.y + zc.y), oi = -0.5f * (zk.x - zc.x);
+  const float2 w = __ldg(tw_rot + q);  // q <= N < rot
+  return make_float2(er + (orr * w.x - oi * w.y), ei + (orr * w.y + oi * w.x));
+}
+
+template <int LOGN, int OUT_TC, int SPCMAX>
+__global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinShape<LOGN, SPCMAX>::THREADS) window_fft_kernel(
+    const StreamDev *__restrict__ streams, int nstreams, int row0, int nrows, int nrows_total,
+    const float *__restrict__ window, const float2 *__restrict__ tw_rot, int nper, int M, int kpad,
+    void *__restrict__ spec_out, float tc_scale) {
+  using S = WinShape<LOGN, SPCMAX>;
+  constexpr int N = S::N, T = S::T, SPC = S::SPC, RPC = S::RPC;
   extern __shared__ float2 dsm[];
   const int t = threadIdx.x % T, g = threadIdx.x / T;
-  const StreamDev &s = streams[blockIdx.y];
-  const int rr = blockIdx.x * S::G + g;
-  const bool ok = rr < nrows;
-  const int r = row0 + rr;
-  float2 *sm = dsm + g * (N + N / 16);
+  const int nsg = (nstreams + SPC - 1) / SPC;
+  const int sg = blockIdx.x % nsg, rg = blockIdx.x / nsg;  // stream group fastest
+  const int gs = g % SPC, gr = g / SPC;
+  const int stream = sg * SPC + gs, rr = rg * RPC + gr;
+  const bool ok = stream < nstreams && rr < nrows;
+  float2 *sm = dsm + g * S::BUF;
   const int rot = 2 * N;
   float2 v[16];
   {
-    const float *ts = s.ts + (int64_t)r * N;  // hop = rot / 2
-    const float sgn = s.flip ? -1.0f : 1.0f;  // sideband flip negates odd samples
+    const StreamDev &s = streams[ok ? stream : 0];
+    const float *ts = s.ts + (int64_t)(row0 + rr) * N;  // hop = rot / 2
+    const float sgn = s.flip ? -1.0f : 1.0f;            // sideband flip negates odd samples
 #pragma unroll
     for (int q = 0; q < 16; q++) {
       const int i = 2 * (t + q * T);
@@ -235,35 +304,53 @@ __global__ void __launch_bounds__(WinShape<LOGN>::THREADS) window_fft_kernel(
   }
   // tw_rot holds exp(-2 pi i m / rot) for m < rot, followed by exp(-2 pi i m / N) for m < N.
   fft_reg<-1, LOGN, true>(v, sm, t, tw_rot + rot, BlockSync());
-  if (!ok) return;
-  for (int i = t; i <= M; i += T) {
-    const int q = s.output_offset + i - s.temp_fft_offset;
-    float fr = 0.f, fi = 0.f;
-    if (q >= 0 && q <= N) {
-      const float2 zk = sm[padi(q & (N - 1))];
-      const float2 zc = sm[padi((N - q) & (N - 1))];
-      const float er = 0.5f * (zk.x + zc.x), ei = 0.5f * (zk.y - zc.y);
-      const float orr = 0.5f * (zk.y + zc.y), oi = -0.5f * (zk.x - zc.x);
-      const float2 w = __ldg(tw_rot + (q & (rot - 1)));
-      fr = er + (orr * w.x - oi * w.y);
-      fi = ei + (orr * w.y + oi * w.x);
+
+  if (OUT_TC) {
+    int shift[SPC];
+#pragma unroll
+    for (int j = 0; j < SPC; j++) {
+      const int st = min(sg * SPC + j, nstreams - 1);
+      shift[j] = streams[st].output_offset - streams[st].temp_fft_offset;
     }
-    const int64_t idx = ((int64_t)blockIdx.y * nrows_total + r) * kpad + i;
-    if (OUT_TC) {
-      const float sr_ = fr * tc_scale, si_ = fi * tc_scale;
-      const __half hr = __float2half_rn(sr_), hi_ = __float2half_rn(si_);
-      const __half lr = __float2half_rn(sr_ - __half2float(hr)), li = __float2half_rn(si_ - __half2float(hi_));
-      const __half2 h0 = __halves2half2(hr, hi_), h1 = __halves2half2(lr, li);
-      uint2 u;
-      u.x = *reinterpret_cast<const unsigned *>(&h0);
-      u.y = *reinterpret_cast<const unsigned *>(&h1);
-      reinterpret_cast<uint2 *>(spec_out)[idx] = u;
-    } else {
-      reinterpret_cast<float2 *>(spec_out)[idx] = make_float2(fr, fi);
+#pragma unroll 1
+    for (int r = 0; r < RPC; r++) {
+      const int row = rg * RPC + r;
+      if (row >= nrows) break;
+      uint2 *dst = reinterpret_cast<uint2 *>(spec_out) + ((int64_t)(row0 + row) * kpad) * kTcSlots + sg * SPC;
+      for (int i = threadIdx.x; i <= M; i += S::THREADS) {
+        uint2 o[SPC];
+#pragma unroll
+        for (int j = 0; j < SPC; j++) {
+          const float2 f = real_bin<N>(dsm + (r * SPC + j) * S::BUF, tw_rot, shift[j] + i);
+          o[j] = tc_split(f.x, f.y, tc_scale);
+        }
+        uint2 *p = dst + (int64_t)i * kTcSlots;
+        if constexpr (SPC == 1) {
+          *p = o[0];
+        } else if constexpr (SPC == 4) {
+          asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(o[0].x), "r"(o[0].y),
+                       "r"(o[1].x), "r"(o[1].y), "r"(o[2].x), "r"(o[2].y), "r"(o[3].x), "r"(o[3].y)
+                       : "memory");
+        } else {
+          static_assert(SPC == 2, "1, 2 or 4 streams per CTA");
+          *reinterpret_cast<uint4 *>(p) = make_uint4(o[0].x, o[0].y, o[1].x, o[1].y);
+        }
+      }
+    }
+  } else {
+#pragma unroll 1
+    for (int gg = 0; gg < SPC * RPC; gg++) {
+      const int st = sg * SPC + gg % SPC, row = rg * RPC + gg / SPC;
+      if (st >= nstreams || row >= nrows) continue;
+      const int shift = streams[st].output_offset - streams[st].temp_fft_offset;
+      float2 *dst = reinterpret_cast<float2 *>(spec_out) + ((int64_t)st * nrows_total + row0 + row) * kpad;
+      for (int i = threadIdx.x; i <= M; i += S::THREADS)
+        dst[i] = real_bin<N>(dsm + gg * S::BUF, tw_rot, shift + i);
     }
   }
 }
 
+// ------------------------------------------------------------------------
 // Bit statistics over counted-byte ranges.  Work items: (stream, range, offset).
 __global__ void bitstat_kernel(const StreamDev *__restrict__ streams, const int4 *__restrict__ items, int nitems) {
   __shared__ unsigned int h[512];
@@ -532,26 +619,29 @@ void launch_extract(const uint8_t *in, int64_t nout, int N, int bits, int nsub, 
   extract_kernel<<<dim3((unsigned)((nout + 255) / 256), nsub), 256, 0, st>>>(in, nout, N, bits, fan_out, tracks, out);
 }
 
-template <int LOGN, int OUT_TC>
+template <int LOGN, int OUT_TC, int SPCMAX>
 static void window_fft_launch(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                               const float *window, const float2 *tw_rot, int nper, int M, int kpad, void *spec,
                               float tc_scale, cudaStream_t st) {
-  using S = WinShape<LOGN>;
-  dim3 grid((nrows + S::G - 1) / S::G, nstreams);
-  cudaFuncSetAttribute(window_fft_kernel<LOGN, OUT_TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
-  window_fft_kernel<LOGN, OUT_TC><<<grid, S::THREADS, S::SMEM, st>>>(d_streams, row0, nrows, nrows_total, window,
-                                                                      tw_rot, nper, M, kpad, spec, tc_scale);
+  using S = WinShape<LOGN, SPCMAX>;
+  const unsigned grid = (unsigned)((nrows + S::RPC - 1) / S::RPC) * (unsigned)((nstreams + S::SPC - 1) / S::SPC);
+  auto kern = window_fft_kernel<LOGN, OUT_TC, SPCMAX>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+  kern<<<grid, S::THREADS, S::SMEM, st>>>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad,
+                                          spec, tc_scale);
 }
 
 template <int OUT_TC>
 static void window_fft_dispatch(int logn, const StreamDev *d_streams, int nstreams, int row0, int nrows,
                                 int nrows_total, const float *window, const float2 *tw_rot, int nper, int M, int kpad,
                                 void *spec, float tc_scale, cudaStream_t st) {
+  // four streams per CTA: a whole 32-byte sector per channel in the TC layout
+  // (two streams per CTA measured the same, one stream 30 % slower)
   switch (logn) {
-#define SFXC_WIN_CASE(L)                                                                                         \
-  case L:                                                                                                        \
-    window_fft_launch<L, OUT_TC>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad, \
-                                 spec, tc_scale, st);                                                            \
+#define SFXC_WIN_CASE(L)                                                                                            \
+  case L:                                                                                                           \
+    window_fft_launch<L, OUT_TC, 4>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad, \
+                                    spec, tc_scale, st);                                                            \
     break;
     SFXC_WIN_CASE(8)
     SFXC_WIN_CASE(9)

@@ -24,8 +24,9 @@ void launch_pulsar(const float2 *spec, int nrows_total, int kpad, int nstreams, 
                    double fft_duration, const double *offsets, double g0, double g1, int nbins, int16_t *bins,
                    float2 *acc, cudaStream_t st);
 size_t xcorr_tc_smem_bytes();
-void launch_xcorr_tc(const void *spec, int nrows_total, int kpad, int nstreams, int nrows, int K, const int *blmap,
-                     int npad, float inv_scale2, float2 *acc, int *err, cudaStream_t st);
+// TC spectra: [row][channel (kpad)][32 stream slots] of 4 FP16 (hi.re, hi.im, lo.re, lo.im).
+cudaError_t launch_xcorr_tc(const void *spec, int nrows, int kpad, int K, const int *blmap, int npad,
+                            float inv_scale2, float2 *acc, int *err, cudaStream_t st);
 void launch_normalize(const float2 *acc, int kpad, int M, int nstreams, int nbl, const int *bl, double *norms,
                       const double *flagfac, float2 *out, cudaStream_t st);
 

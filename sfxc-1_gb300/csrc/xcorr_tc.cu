@@ -12,15 +12,27 @@
 // parts, i.e. the compensated product, and the epilogue forms
 //   Re V(a,b) = G[2a][2b] + G[2a+1][2b+1],  Im V(a,b) = G[2a+1][2b] - G[2a][2b+1].
 //
-// CTA: 4 channels (4 x 128 TMEM columns), 256 threads.  K-tiles of 64 FFTs,
-// double buffered in shared memory in the canonical MN-major 128-byte-swizzle
-// layout (per channel: two 64-component atoms of 64 rows x 128 B).  All
-// threads stage a tile (global loads, swizzled stores, async-proxy fence);
-// thread 0 issues 4 channels x 4 MMAs (K = 16 each) and commits them to the
-// stage's mbarrier.  Waits are bounded: on timeout the CTA records an error,
+// Spectra layout (written by the windowed FFT): [row][channel][32 stream
+// slots][hi.re, hi.im, lo.re, lo.im] as FP16, i.e. 256 B per (row, channel),
+// so one channel's K-tile of 64 rows is two 128-byte-wide MN-major atoms
+// (stream slots 0-15 and 16-31), each 64 rows x 128 B.  The M index of a
+// component is 4 * stream + {hi.re, hi.im, lo.re, lo.im}; summing the four
+// hi/lo combinations gives the compensated product, and the epilogue forms
+//   Re V(a,b) = sum over re-re and im-im pairs,  Im V(a,b) = im-re minus re-im
+// with lane shuffles over the 4 TMEM lanes (D rows) of one stream.
+//
+// CTA: 4 channels (4 x 128 TMEM columns), 256 threads, warp-specialised:
+// thread 0 streams K-tiles with TMA (cp.async.bulk.tensor, 128-byte swizzle,
+// 8 boxes of 8 KB per 64 KB stage, 3 stages); thread 32 issues 4 channels x 4
+// MMAs (K = 16) per stage and commits them to the stage's "empty" barrier;
+// after the last tile all 8 warps read TMEM (two channels per warp quarter)
+// and add the visibilities to the accumulator.  Every wait is bounded: on
+// timeout the CTA records an error, waits (bounded) for its loads in flight,
 // skips its output, frees its TMEM and returns.
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_fp16.h>
+#include <cudaTypedefs.h>
 
 #include "device.cuh"
 #include "kernels.hpp"
@@ -30,9 +42,10 @@ namespace {
 
 constexpr int kChan = 4;        // channels per CTA
 constexpr int kRowsK = 64;      // FFT rows per K-tile
+constexpr int kStages = 3;
 constexpr int kThreads = 256;
 constexpr int kAtomBytes = kRowsK * 128;      // one 64-component atom of a K-tile
-constexpr int kChanTile = 2 * kAtomBytes;     // hi + lo atoms of one channel
+constexpr int kChanTile = 2 * kAtomBytes;     // both atoms (stream slots 0-15, 16-31) of one channel
 constexpr int kStageBytes = kChan * kChanTile;  // 64 KB per stage
 constexpr unsigned long long kSpinLimit = 200000000ull;
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s
@@ -119,27 +132,30 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// Byte offset of component m (0..127) at K-row k in one channel's tile.
-__device__ __forceinline__ uint32_t tile_offset(int m, int k) {
-  const int atom = m >> 6, mm = m & 63;
-  return (uint32_t)(atom * kAtomBytes + (k >> 3) * 1024 + (k & 7) * 128 + ((((mm >> 3) ^ (k & 7))) << 4) +
-                    (mm & 7) * 2);
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// One TMA box {64 halves, 1, 64 rows} = 8 KB at coordinates (0, c1, c2).
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c1, int c2, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
-    xcorr_tc_kernel(const uint2 *__restrict__ spec, int nrows_total, int kpad, int nstreams, int nrows, int K,
-                    const int *__restrict__ blmap, int npad, float inv_scale2, float2 *__restrict__ acc,
-                    int *__restrict__ err) {
+    xcorr_tc_kernel(const __grid_constant__ CUtensorMap tmap, int nrows, int K, int kpad, const int *__restrict__ blmap,
+                    int npad, float inv_scale2, float2 *__restrict__ acc, int *__restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  // 1024-B aligned dynamic shared memory: two stages, then epilogue staging
-  uint8_t *base = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
-  uint8_t *stage[2] = {base, base + kStageBytes};
-  float *stg = reinterpret_cast<float *>(base);  // reused after the MMAs: [128][65]
-  __shared__ uint64_t mbar[2];
+  uint8_t *base = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);  // 128-byte swizzle wants 1 KB
+  __shared__ uint64_t full[kStages], empty[kStages], done;
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int k0 = blockIdx.x * kChan;
+  const int nkt = (nrows + kRowsK - 1) / kRowsK;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&tmem_base))
@@ -147,8 +163,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
+    for (int s = 0; s < kStages; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
     failed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -156,96 +175,93 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
-  const uint32_t idesc = idesc_f16(128, 128);
-  const int nkt = (nrows + kRowsK - 1) / kRowsK;
+  volatile int *vfailed = &failed;
 
-  for (int kt = 0; kt < nkt; kt++) {
-    const int s = kt & 1;
-    if (kt >= 2) {
-      if (!mbar_wait(&mbar[s], ((kt - 2) >> 1) & 1)) failed = 1;
-    }
-    __syncthreads();
-    if (failed) break;
-    // ---- stage the K-tile: (stream, row) pairs, 4 channels x (hi, lo) each
-    uint8_t *st = stage[s];
-    for (int e = tid; e < 32 * kRowsK; e += kThreads) {
-      const int sidx = e & 31, r = e >> 5;
-      const int row = kt * kRowsK + r;
-      uint2 v[kChan];
-#pragma unroll
-      for (int c = 0; c < kChan; c++) v[c] = make_uint2(0u, 0u);
-      if (sidx < nstreams && row < nrows) {
-        const uint2 *src = spec + ((int64_t)sidx * nrows_total + row) * kpad + k0;
-#pragma unroll
-        for (int c = 0; c < kChan; c++)
-          if (k0 + c < K) v[c] = src[c];
+  if (tid == 0) {
+    // ---- TMA producer
+    int last[kStages];
+    for (int s = 0; s < kStages; s++) last[s] = -1;
+    for (int kt = 0; kt < nkt; kt++) {
+      const int s = kt % kStages, n = kt / kStages;
+      if (n > 0 && !mbar_wait(&empty[s], (n - 1) & 1)) {
+        *vfailed = 1;
+        break;
       }
+      if (*vfailed) break;
+      mbar_expect_tx(&full[s], kStageBytes);
+      uint8_t *st = base + s * kStageBytes;
 #pragma unroll
-      for (int c = 0; c < kChan; c++) {
-        uint8_t *t = st + c * kChanTile;
-        *reinterpret_cast<uint32_t *>(t + tile_offset(2 * sidx, r)) = v[c].x;       // hi re, hi im
-        *reinterpret_cast<uint32_t *>(t + tile_offset(64 + 2 * sidx, r)) = v[c].y;  // lo re, lo im
-      }
+      for (int c = 0; c < kChan; c++)
+#pragma unroll
+        for (int a = 0; a < 2; a++)
+          tma_load_3d(st + c * kChanTile + a * kAtomBytes, &tmap, 2 * (k0 + c) + a, kt * kRowsK, &full[s]);
+      last[s] = kt;
     }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
+    // loads still in flight land before the CTA may exit
+    for (int s = 0; s < kStages; s++)
+      if (last[s] >= 0 && !mbar_wait(&full[s], (last[s] / kStages) & 1)) *vfailed = 1;
+  } else if (tid == 32) {
+    // ---- MMA issuer
+    const uint32_t idesc = idesc_f16(128, 128);
+    for (int kt = 0; kt < nkt; kt++) {
+      const int s = kt % kStages, n = kt / kStages;
+      if (!mbar_wait(&full[s], n & 1)) {
+        *vfailed = 1;
+        break;
+      }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t st = smem_u32(base + s * kStageBytes);
 #pragma unroll
       for (int c = 0; c < kChan; c++) {
-        const uint32_t a0 = smem_u32(st + c * kChanTile);
 #pragma unroll
         for (int ks = 0; ks < kRowsK / 16; ks++) {
-          // 16 K-rows = two 8-row groups of 1024 B; atoms (hi, lo) kAtomBytes apart
-          const uint64_t d = smem_desc(a0 + ks * 2048, kAtomBytes, 1024);
+          // 16 K-rows = two 8-row groups of 1024 B; M atoms kAtomBytes apart
+          const uint64_t d = smem_desc(st + c * kChanTile + ks * 2048, kAtomBytes, 1024);
           mma_f16(tmem + c * 128, d, d, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
         }
       }
-      mma_commit(&mbar[s]);
+      mma_commit(&empty[s]);
     }
+    mma_commit(&done);  // arrives once every MMA issued above has completed
   }
-  // ---- wait for the last tile's MMAs (the commit covers all earlier ones)
-  if (!failed && nkt > 0) {
-    if (!mbar_wait(&mbar[(nkt - 1) & 1], ((nkt - 1) >> 1) & 1)) failed = 1;
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  if (!mbar_wait(&done, 0)) *vfailed = 1;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (failed) {
+  __syncthreads();
+  if (*vfailed) {
     if (tid == 0) atomicExch(err, 1);
-  } else {
-    // ---- epilogue per channel: quadrant sums via shared memory, then baselines
-    for (int c = 0; c < kChan; c++) {
-      const int k = k0 + c;
-      if (warp < 4) {
-        const int m = warp * 32 + lane;  // TMEM lane = D row
-        float lo[32], hi[32];
-        for (int q0 = 0; q0 < 64; q0 += 32) {
-          const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + c * 128;
-          tmem_ld32(ta + q0, lo);
-          tmem_ld32(ta + 64 + q0, hi);
+  } else if (nkt > 0) {
+    // ---- epilogue: warp quarter q reads D rows 32q..32q+31, two channels per warp
+    const int q = warp & 3, m = q * 32 + lane, a = m >> 2, p = m & 3;
+#pragma unroll 1
+    for (int cc = 0; cc < 2; cc++) {
+      const int c = (warp >> 2) * 2 + cc, k = k0 + c;
+#pragma unroll 1
+      for (int j = 0; j < 4; j++) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + c * 128 + j * 32, v);
 #pragma unroll
-          for (int q = 0; q < 32; q++) stg[m * 65 + q0 + q] = lo[q] + hi[q];
+        for (int bb = 0; bb < 8; bb++) {
+          const float A = v[4 * bb] + v[4 * bb + 2], B = v[4 * bb + 1] + v[4 * bb + 3];
+          // row component p: 0 hi.re, 1 hi.im, 2 lo.re, 3 lo.im; columns likewise
+          float re = (p & 1) ? B : A, im = (p & 1) ? A : -B;
+          re += __shfl_xor_sync(0xffffffffu, re, 1);
+          im += __shfl_xor_sync(0xffffffffu, im, 1);
+          re += __shfl_xor_sync(0xffffffffu, re, 2);
+          im += __shfl_xor_sync(0xffffffffu, im, 2);
+          const int b = j * 8 + bb;
+          if (p == 0 && k < K && a < npad && b < npad) {
+            const int mapv = __ldg(blmap + a * npad + b);
+            if (mapv >= 0) {
+              float2 *dst = acc + (int64_t)(mapv >> 1) * kpad + k;
+              float2 o = *dst;
+              o.x += re * inv_scale2;
+              o.y += ((mapv & 1) ? -im : im) * inv_scale2;
+              *dst = o;
+            }
+          }
         }
       }
-      __syncthreads();
-      if (k < K) {
-        for (int p = tid; p < npad * npad; p += kThreads) {
-          const int i = p / npad, j = p % npad;
-          const int mapv = blmap[i * npad + j];
-          if (mapv < 0 || i >= 32 || j >= 32) continue;
-          auto G = [&](int a, int b) { return stg[a * 65 + b] + stg[(a + 64) * 65 + b]; };
-          const float re = (G(2 * i, 2 * j) + G(2 * i + 1, 2 * j + 1)) * inv_scale2;
-          float im = (G(2 * i + 1, 2 * j) - G(2 * i, 2 * j + 1)) * inv_scale2;
-          if (mapv & 1) im = -im;
-          float2 *dst = acc + (int64_t)(mapv >> 1) * kpad + k;
-          float2 o = *dst;
-          o.x += re;
-          o.y += im;
-          *dst = o;
-        }
-      }
-      __syncthreads();
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -258,15 +274,43 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 }  // namespace
 
-size_t xcorr_tc_smem_bytes() { return 2 * (size_t)kStageBytes + 1024; }
+size_t xcorr_tc_smem_bytes() { return kStages * (size_t)kStageBytes + 1024; }
 
-void launch_xcorr_tc(const void *spec, int nrows_total, int kpad, int nstreams, int nrows, int K, const int *blmap,
-                     int npad, float inv_scale2, float2 *acc, int *err, cudaStream_t st) {
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against libcuda).
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+cudaError_t launch_xcorr_tc(const void *spec, int nrows, int kpad, int K, const int *blmap, int npad,
+                            float inv_scale2, float2 *acc, int *err, cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+  if (!enc) return cudaErrorNotSupported;
+  // halves of one 128-byte atom row; (channel, atom) pairs 128 B apart; rows kpad * 256 B apart
+  alignas(64) CUtensorMap map;
+  const cuuint64_t dims[3] = {64, (cuuint64_t)2 * kpad, (cuuint64_t)nrows};
+  const cuuint64_t strides[2] = {128, (cuuint64_t)kpad * 256};
+  const cuuint32_t box[3] = {64, 1, (cuuint32_t)kRowsK};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<void *>(spec), dims, strides, box, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
   const size_t smem = xcorr_tc_smem_bytes();
-  cudaFuncSetAttribute(xcorr_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  xcorr_tc_kernel<<<(K + kChan - 1) / kChan, kThreads, smem, st>>>(reinterpret_cast<const uint2 *>(spec),
-                                                                  nrows_total, kpad, nstreams, nrows, K, blmap, npad,
-                                                                  inv_scale2, acc, err);
+  cudaError_t e = cudaFuncSetAttribute(xcorr_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  xcorr_tc_kernel<<<(K + kChan - 1) / kChan, kThreads, smem, st>>>(map, nrows, K, kpad, blmap, npad, inv_scale2, acc,
+                                                                  err);
+  return cudaGetLastError();
 }
 
 }  // namespace sfxc
