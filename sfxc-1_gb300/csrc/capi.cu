@@ -730,8 +730,6 @@ int sfxc_gpu_push_protocol(sfxc_gpu_ctx *c, int32_t stream, const uint8_t *bytes
   StreamCtx &s = c->sc[stream];
   try {
     CK(cudaSetDevice(c->device));
-    // records refer to the bytes by their offset in the stream's device buffer
-    std::vector<Record> recs = parse_protocol(bytes, n, s.dev_bytes);
     // 8 spare bytes: the unpack reads whole 32-bit words, one past the last sample
     const size_t need = (size_t)(s.dev_bytes + (int64_t)n) + 8;
     if (need > s.src.cap) {  // grow, keeping what this integration already pushed
@@ -742,7 +740,17 @@ int sfxc_gpu_push_protocol(sfxc_gpu_ctx *c, int32_t stream, const uint8_t *bytes
       std::swap(grown.cap, s.src.cap);
       CK(cudaStreamSynchronize(c->st));
     }
+    // the copy runs while the records are parsed; bytes past dev_bytes only
+    // count once the parse has succeeded
     if (n) CK(cudaMemcpyAsync(s.src.as<uint8_t>() + s.dev_bytes, bytes, n, cudaMemcpyHostToDevice, c->st));
+    std::vector<Record> recs;
+    try {
+      // records refer to the bytes by their offset in the stream's device buffer
+      recs = parse_protocol(bytes, n, s.dev_bytes);
+    } catch (...) {
+      cudaStreamSynchronize(c->st);  // the caller owns the buffer again on return
+      throw;
+    }
     CK(cudaStreamSynchronize(c->st));  // the caller may reuse its buffer on return
     s.dev_bytes += (int64_t)n;
     s.pending.insert(s.pending.end(), recs.begin(), recs.end());
