@@ -33,9 +33,27 @@ struct CudaError : Error {
     if (e_ != cudaSuccess) throw CudaError(e_, #x); \
   } while (0)
 
+// Device buffer that only grows.  Move-only: freeing device memory
+// synchronises the whole device, so buffers are kept and handed on (swap)
+// rather than freed between jobs.
 struct DevBuf {
   void *p = nullptr;
   size_t cap = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept : p(o.p), cap(o.cap) {
+    o.p = nullptr;
+    o.cap = 0;
+  }
+  DevBuf &operator=(DevBuf &&o) noexcept {
+    swap(o);
+    return *this;
+  }
+  void swap(DevBuf &o) noexcept {
+    std::swap(p, o.p);
+    std::swap(cap, o.cap);
+  }
   void *ensure(size_t n) {
     if (n > cap) {
       if (p) cudaFree(p);
@@ -64,6 +82,15 @@ struct StreamCtx {
   Spline sp;
   int n_blocks = 0, nfft_max = 0, rot = 0, hop = 0;
   DevBuf src, segs, stat_rng, spline, hist, bparams, bamp;
+  void take_buffers(StreamCtx &o) {
+    src.swap(o.src);
+    segs.swap(o.segs);
+    stat_rng.swap(o.stat_rng);
+    spline.swap(o.spline);
+    hist.swap(o.hist);
+    bparams.swap(o.bparams);
+    bamp.swap(o.bamp);
+  }
 };
 
 struct Polyco {
@@ -207,8 +234,12 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
   c->nffts = nr - (p->window != WINDOW_NONE ? 1 : 0);
   c->nsub = nr_ffts_per_integration_slice((double)p->sub_integration_time_us, p->sample_rate, c->M);
   if (c->nffts <= 0) throw Error(SFXC_GPU_EINVAL, "integration shorter than two FFTs");
-  c->sc.clear();
-  c->sc.resize(p->n_streams);
+  {  // fresh stream state; the device buffers of the previous job are reused
+    std::vector<StreamCtx> prev;
+    prev.swap(c->sc);
+    c->sc.resize(p->n_streams);
+    for (size_t i = 0; i < prev.size() && i < c->sc.size(); i++) c->sc[i].take_buffers(prev[i]);
+  }
   for (int i = 0; i < p->n_streams; i++) {
     StreamCtx &s = c->sc[i];
     const StationStream &ss = c->streams[i];

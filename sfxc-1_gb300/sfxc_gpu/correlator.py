@@ -115,17 +115,21 @@ class CorrelatorNode:
         self._check(self._lib.sfxc_gpu_push_protocol(self._h, stream, buf, len(data)))
 
     def run_integration(self):
-        """Returns (output bytes, [tsys record bytes per stream])."""
+        """Returns (output bytes (bytes or bytearray), [tsys record bytes per stream])."""
         out, tsys = [], []
 
         def sink(user, kind, data, n):
-            b = C.string_at(data, n)
-            (out if kind == 0 else tsys).append(b)
+            # the copy is a foreign call (ctypes.memmove), so other threads
+            # driving other contexts keep the interpreter meanwhile
+            b = bytearray(n)
+            if n:
+                C.memmove((C.c_char * n).from_buffer(b), data, n)
+            (out if kind == 0 else tsys).append(bytes(b) if kind else b)
             return 0
 
         cb = L.SINK(sink)
         self._check(self._lib.sfxc_gpu_run_integration(self._h, cb, None))
-        return b"".join(out), tsys
+        return (out[0] if len(out) == 1 else b"".join(out)), tsys
 
     def correlate(self, job):
         """Run every integration of a job dict; returns (cor bytes, tsys bytes)."""
