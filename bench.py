@@ -266,9 +266,10 @@ def run_gpu(args):
 
 def roofline(args, per_kernel, total):
     """Dominant kernel against the measured HBM copy bandwidth.  Algorithmic
-    bytes per input sample: X-step reads (M+1)/M complex64 spectra = 8.002 B;
-    windowed FFT reads 4 B (fringe-stopped series) and writes 8.002 B; the
-    unpack+fringe stage reads 0.25 B and writes 4 B."""
+    bytes per input sample: the X-step reads (M+1)/M spectrum values of 8 B
+    (FP16 hi+lo or complex64) = 8.002 B; the windowed FFT reads 4 B
+    (fringe-stopped series) and writes 8.002 B; the unpack+fringe stage reads
+    0.25 B of 2-bit codes and writes 4 B."""
     try:
         peak = json.load(open(PEAKS))["hbm_gbs"]
         src = "measured"

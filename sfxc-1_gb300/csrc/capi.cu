@@ -46,10 +46,6 @@ struct DevBuf {
     o.p = nullptr;
     o.cap = 0;
   }
-  DevBuf &operator=(DevBuf &&o) noexcept {
-    swap(o);
-    return *this;
-  }
   void swap(DevBuf &o) noexcept {
     std::swap(p, o.p);
     std::swap(cap, o.cap);
@@ -623,7 +619,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->evpool[ev + 3], st));
     ev += 4;
-    launches += pulsar ? 5 : 4;
+    launches += pulsar ? 5 : 4;  // parameters, blocks, window FFT, (pulsar bins,) X-step
   }
   // restore the whole-integration time base for inspection calls
   for (int i = 0; i < N; i++) {

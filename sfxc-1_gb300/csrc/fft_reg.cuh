@@ -139,21 +139,25 @@ __device__ __forceinline__ void fft_reg(float2 (&v)[16], float2 *sm, int t, cons
   constexpr int N = 1 << LOGN, T = N / 16, NR16 = LOGN / 4, LAST = LOGN % 4;
   static_assert(NR16 >= 1, "at least 16 points");
   static_assert(TO_SMEM || LAST == 0, "register output needs a final radix-16 pass");
+  // T, Q and every stride Ns >= 16 are multiples of 16, and the Ns = 1 pass
+  // writes 16 consecutive entries from a multiple of 16, so each padded index
+  // is padi(base) plus a compile-time offset (padi(x + 16 m) = padi(x) + 17 m)
+  const int rbase = padi(t);
   int Ns = 1;
 #pragma unroll
   for (int p = 0; p < NR16; p++) {
     if (p > 0) {
 #pragma unroll
-      for (int r = 0; r < 16; r++) v[r] = sm[padi(t + r * T)];
+      for (int r = 0; r < 16; r++) v[r] = sm[rbase + r * (T + T / 16)];
       sync();
       const int k = t & (Ns - 1);
       twiddle16<SIGN>(v, tw, k * (N / (16 * Ns)));
     }
     dft16<SIGN>(v);
     if (p == NR16 - 1 && LAST == 0 && !TO_SMEM) return;  // v[r] = X[t + r T]
-    const int base = (t - (t & (Ns - 1))) * 16 + (t & (Ns - 1));
+    const int wbase = padi((t - (t & (Ns - 1))) * 16 + (t & (Ns - 1)));
 #pragma unroll
-    for (int r = 0; r < 16; r++) sm[padi(base + r * Ns)] = v[r];
+    for (int r = 0; r < 16; r++) sm[wbase + r * (Ns + Ns / 16)] = v[r];
     sync();
     Ns *= 16;
   }
@@ -162,7 +166,7 @@ __device__ __forceinline__ void fft_reg(float2 (&v)[16], float2 *sm, int t, cons
 #pragma unroll
     for (int g = 0; g < G; g++)
 #pragma unroll
-      for (int r = 0; r < R; r++) v[g * R + r] = sm[padi(t + g * T + r * Q)];
+      for (int r = 0; r < R; r++) v[g * R + r] = sm[rbase + g * (T + T / 16) + r * (Q + Q / 16)];
     sync();
 #pragma unroll
     for (int g = 0; g < G; g++) {
@@ -190,7 +194,7 @@ __device__ __forceinline__ void fft_reg(float2 (&v)[16], float2 *sm, int t, cons
         dft8<SIGN>(u);
       }
 #pragma unroll
-      for (int r = 0; r < R; r++) sm[padi(j + r * Q)] = u[r];
+      for (int r = 0; r < R; r++) sm[rbase + g * (T + T / 16) + r * (Q + Q / 16)] = u[r];
     }
     sync();
   }

@@ -16,6 +16,7 @@
 //   pulsar_bins_kernel / xcorr_f32_pulsar  bin per (FFT, channel) in FP64 and binned
 //                        accumulation (correlation_core_pulsar.cc:210-238).
 //   norm_* kernels       Correlation_core::integration_normalize (275-314).
+#include <algorithm>
 #include <cstdio>
 
 #include "device.cuh"
@@ -25,21 +26,21 @@
 namespace sfxc {
 
 // ------------------------------------------------------------------------
-// F-step, stage 1: 16 threads per pair of 256-sample blocks, 32 blocks per CTA.
-// One forward 256-point complex FFT of x_b + i x_{b+1} gives both real
-// spectra (X[k] +/- conj X[256-k]); per block: DC and Nyquist halved, phase
-// ramp exp(-i (c + k l)) on k <= 128, upper half zero, inverse 256-point FFT,
+// F-step, stage 1: 16 threads per pair of 256-sample blocks.  One forward
+// 256-point complex FFT of x_b + i x_{b+1} gives both real spectra
+// (X[k] +/- conj X[256-k]); per block: DC and Nyquist halved, phase ramp
+// exp(-i (c + k l)) on k <= 128, upper half zero, inverse 256-point FFT,
 // fringe rotation of the real part.  tw holds exp(-2 pi i m / 256), m < 256.
-__global__ void __launch_bounds__(256, 4) fstep_block_kernel(const StreamDev *__restrict__ streams,
-                                                         const float2 *__restrict__ tw) {
-  __shared__ float2 sbuf[16][kNd + kNd / 16];
-  const int t = threadIdx.x & 15, grp = threadIdx.x >> 4;
-  const StreamDev &s = streams[blockIdx.y];
-  const int first = blockIdx.x * 32;  // first block of the CTA
-  if (first + (threadIdx.x >> 5) * 4 >= s.n_blocks) return;  // whole warps only (warp barriers below)
-  const int bl0 = first + grp * 2;
+//
+// Pair (bl0, bl0 + 1) of a stream's blocks (indices from the stream's block0)
+// by the 16 threads t = 0..15 of a half warp, with a scratch of
+// kNd + kNd / 16 float2; blocks at or past n_blocks give no output.  The
+// result goes through store(block, sample, value).  Both half warps of a warp
+// must call this together (warp barriers).
+template <class Store>
+__device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, float2 *sm,
+                                           const float2 *__restrict__ tw, Store store) {
   const bool ok0 = bl0 < s.n_blocks, ok1 = bl0 + 1 < s.n_blocks;
-  float2 *sm = sbuf[grp];
   float2 v[16];
   {  // unpack the two blocks through the plan
     const int o0 = (s.block0 + bl0) * kNd;
@@ -141,10 +142,9 @@ __global__ void __launch_bounds__(256, 4) fstep_block_kernel(const StreamDev *__
       sincosf(16.0f * prm.w, &ss, &sc);
       rs *= amp;
       rc *= amp;
-      float *out = s.ts + (int64_t)bl * kNd + t;
 #pragma unroll
       for (int r = 0; r < 16; r++) {
-        out[16 * r] = v[r].x * rc + v[r].y * rs;
+        store(bl, t + 16 * r, v[r].x * rc + v[r].y * rs);
         const float c2 = rc * sc - rs * ss;
         rs = rs * sc + rc * ss;
         rc = c2;
@@ -152,6 +152,20 @@ __global__ void __launch_bounds__(256, 4) fstep_block_kernel(const StreamDev *__
     }
     __syncwarp();
   }
+}
+
+// F-step stage 1 as its own kernel (fringe-stopped samples to s.ts): 16
+// pairs of blocks per CTA of 256 threads.
+__global__ void __launch_bounds__(256, 4) fstep_block_kernel(const StreamDev *__restrict__ streams,
+                                                         const float2 *__restrict__ tw) {
+  __shared__ float2 sbuf[16][kNd + kNd / 16];
+  const int t = threadIdx.x & 15, grp = threadIdx.x >> 4;
+  const StreamDev &s = streams[blockIdx.y];
+  const int first = blockIdx.x * 32;  // first block of the CTA
+  if (first + (threadIdx.x >> 5) * 4 >= s.n_blocks) return;  // whole warps only (warp barriers)
+  float *ts = s.ts;
+  fstep_pair(s, first + grp * 2, t, sbuf[grp], tw,
+             [ts](int bl, int n, float x) { ts[(int64_t)bl * kNd + n] = x; });
 }
 
 // Per-block FP64 parameters of the F-step, one thread per 256-sample block
@@ -229,33 +243,23 @@ __global__ void extract_kernel(const uint8_t *__restrict__ in, int64_t nout, int
 
 // ------------------------------------------------------------------------
 // F-step, stage 2: windowed real FFT of rot = 2N samples per output row as an
-// N-point complex FFT (N = 2^LOGN) of (x[2e], x[2e+1]) by T = N/16 threads.
-// A CTA of 1024 threads transforms SPC streams x RPC rows (one group of T
-// threads each); the first pass reads the samples straight from HBM.  For
-// the tensor-core layout ([row][channel][32 stream slots] x 8 B) one thread
-// then writes the SPC streams of a channel as one contiguous 8*SPC-byte piece
-// (a whole 32-byte sector for SPC = 4).
-template <int LOGN, int SPCMAX>
-struct WinShape {
-  static constexpr int N = 1 << LOGN, T = N / 16;
-  static constexpr int SPC = T * SPCMAX <= 1024 ? SPCMAX : 1024 / T;  // streams per CTA
-  static constexpr int RPC = T < 256 ? 256 / T : 1;                   // rows per CTA
-  static constexpr int THREADS = SPC * RPC * T;
-  static constexpr int BUF = N + N / 16;  // padded FFT buffer (float2) of one group
-  static constexpr size_t SMEM = (size_t)SPC * RPC * BUF * sizeof(float2);
-  static_assert(THREADS <= 1024, "at most 1024 threads");
-};
+// N-point complex FFT (N = 2^LOGN) of (x[2e], x[2e+1]) by T = N/16 threads,
+// then the real-FFT split and the channel selection.  For the tensor-core
+// layout ([row][channel][32 stream slots] x 8 B) one thread writes up to four
+// streams of a channel as one contiguous piece (a whole 32-byte sector for
+// four streams).
 
-__device__ __forceinline__ uint2 tc_split(float fr, float fi, float tc_scale) {
-  const float sr_ = fr * tc_scale, si_ = fi * tc_scale;
-  const __half hr = __float2half_rn(sr_), hi_ = __float2half_rn(si_);
-  const __half lr = __float2half_rn(sr_ - __half2float(hr)), li = __float2half_rn(si_ - __half2float(hi_));
-  const __half2 h0 = __halves2half2(hr, hi_), h1 = __halves2half2(lr, li);
-  return make_uint2(*reinterpret_cast<const unsigned *>(&h0), *reinterpret_cast<const unsigned *>(&h1));
+// FP16 hi = fp16(s x), lo = fp16(s x - hi) of a complex value (packed conversions).
+__device__ __forceinline__ uint2 tc_split(float2 f, float tc_scale) {
+  const float2 sv = make_float2(f.x * tc_scale, f.y * tc_scale);
+  const __half2 h = __float22half2_rn(sv);
+  const float2 hb = __half22float2(h);
+  const __half2 l = __float22half2_rn(make_float2(sv.x - hb.x, sv.y - hb.y));
+  return make_uint2(*reinterpret_cast<const unsigned *>(&h), *reinterpret_cast<const unsigned *>(&l));
 }
 
-// Channel i of one group's transform Z (natural order, padded): the real-FFT
-// split for output bin q = output_offset + i - temp_fft_offset (zero outside 0..N).
+// Channel i of one transform Z (natural order, padded): the real-FFT split
+// for output bin q = output_offset + i - temp_fft_offset (zero outside 0..N).
 template <int N>
 __device__ __forceinline__ float2 real_bin(const float2 *Z, const float2 *__restrict__ tw_rot, int q) {
   if (q < 0 || q > N) return make_float2(0.f, 0.f);
@@ -267,86 +271,154 @@ __device__ __forceinline__ float2 real_bin(const float2 *Z, const float2 *__rest
   return make_float2(er + (orr * w.x - oi * w.y), ei + (orr * w.y + oi * w.x));
 }
 
-template <int LOGN, int OUT_TC, int SPCMAX>
-__global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinShape<LOGN, SPCMAX>::THREADS) window_fft_kernel(
-    const StreamDev *__restrict__ streams, int nstreams, int row0, int nrows, int nrows_total,
-    const float *__restrict__ window, const float2 *__restrict__ tw_rot, int nper, int M, int kpad,
-    void *__restrict__ spec_out, float tc_scale) {
-  using S = WinShape<LOGN, SPCMAX>;
-  constexpr int N = S::N, T = S::T, SPC = S::SPC, RPC = S::RPC;
-  extern __shared__ float2 dsm[];
-  const int t = threadIdx.x % T, g = threadIdx.x / T;
-  const int nsg = (nstreams + SPC - 1) / SPC;
-  const int sg = blockIdx.x % nsg, rg = blockIdx.x / nsg;  // stream group fastest
-  const int gs = g % SPC, gr = g / SPC;
-  const int stream = sg * SPC + gs, rr = rg * RPC + gr;
-  const bool ok = stream < nstreams && rr < nrows;
-  float2 *sm = dsm + g * S::BUF;
-  const int rot = 2 * N;
-  float2 v[16];
-  {
-    const StreamDev &s = streams[ok ? stream : 0];
-    const float *ts = s.ts + (int64_t)(row0 + rr) * N;  // hop = rot / 2
-    const float sgn = s.flip ? -1.0f : 1.0f;            // sideband flip negates odd samples
-#pragma unroll
-    for (int q = 0; q < 16; q++) {
-      const int i = 2 * (t + q * T);
-      float2 x = make_float2(0.f, 0.f);
-      if (ok && i + 1 < nper) {
-        const float2 a = *reinterpret_cast<const float2 *>(ts + i);
-        const float2 w = __ldg(reinterpret_cast<const float2 *>(window + i));
-        x = make_float2(a.x * w.x, sgn * (a.y * w.y));
-      } else if (ok && i < nper) {
-        x.x = ts[i] * window[i];
-      }
-      v[q] = x;
-    }
-  }
-  // tw_rot holds exp(-2 pi i m / rot) for m < rot, followed by exp(-2 pi i m / N) for m < N.
-  fft_reg<-1, LOGN, true>(v, sm, t, tw_rot + rot, BlockSync());
+// Bins q and N - q of one transform together (0 <= q <= N/2): both read
+// Z[q] and Z[N - q], and with E, O the even and odd parts and w = tw_rot[q],
+// X[q] = E + O w and X[N - q] = conj(E - O w) (tw_rot[N - q] = -conj w).
+template <int N>
+__device__ __forceinline__ void real_bin_pair(const float2 *Z, float2 w, int q, float2 &xq, float2 &xnq) {
+  const float2 zk = Z[padi(q & (N - 1))];
+  const float2 zc = Z[padi((N - q) & (N - 1))];
+  const float er = 0.5f * (zk.x + zc.x), ei = 0.5f * (zk.y - zc.y);
+  const float orr = 0.5f * (zk.y + zc.y), oi = -0.5f * (zk.x - zc.x);
+  const float owr = orr * w.x - oi * w.y, owi = orr * w.y + oi * w.x;
+  xq = make_float2(er + owr, ei + owi);
+  xnq = make_float2(er - owr, owi - ei);
+}
 
-  if (OUT_TC) {
-    int shift[SPC];
+// First-pass inputs v[qq] = complex element t + qq T of the windowed row:
+// samples i = 2 e, 2 e + 1 from sample(i) (a float2), times the window, odd
+// samples negated for a sideband flip, zero from nper on.
+template <int T, class Sample>
+__device__ __forceinline__ void window_load(float2 (&v)[16], int t, bool ok, int nper, float sgn,
+                                            const float *__restrict__ window, Sample sample) {
 #pragma unroll
-    for (int j = 0; j < SPC; j++) {
-      const int st = min(sg * SPC + j, nstreams - 1);
-      shift[j] = streams[st].output_offset - streams[st].temp_fft_offset;
+  for (int qq = 0; qq < 16; qq++) {
+    const int i = 2 * (t + qq * T);
+    float2 x = make_float2(0.f, 0.f);
+    if (ok && i + 1 < nper) {
+      const float2 a = sample(i);
+      const float2 w = __ldg(reinterpret_cast<const float2 *>(window + i));
+      x = make_float2(a.x * w.x, sgn * (a.y * w.y));
+    } else if (ok && i < nper) {
+      x.x = sample(i).x * window[i];
     }
+    v[qq] = x;
+  }
+}
+
+// Output row `row` of the NS streams sg0 + j (j < NS) whose transforms are at
+// Z + j * BUF; threads tid = 0..nthr-1 share the channels 0..M.
+template <int N, int NS, int OUT_TC>
+__device__ __forceinline__ void store_row(const float2 *Z, int BUF, const StreamDev *__restrict__ streams,
+                                          int nstreams, int sg0, int row, int nrows_total, int M, int kpad,
+                                          const float2 *__restrict__ tw_rot, void *__restrict__ spec_out,
+                                          float tc_scale, int tid, int nthr) {
+  if (OUT_TC) {
+    constexpr int W = NS < 4 ? NS : 4;  // streams per store
+    auto put = [](uint2 *p, const uint2 (&o)[W]) {
+      if constexpr (W == 1) {
+        *p = o[0];
+      } else if constexpr (W == 2) {
+        *reinterpret_cast<uint4 *>(p) = make_uint4(o[0].x, o[0].y, o[1].x, o[1].y);
+      } else {
+        asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(o[0].x), "r"(o[0].y),
+                     "r"(o[1].x), "r"(o[1].y), "r"(o[2].x), "r"(o[2].y), "r"(o[3].x), "r"(o[3].y)
+                     : "memory");
+      }
+    };
 #pragma unroll 1
-    for (int r = 0; r < RPC; r++) {
-      const int row = rg * RPC + r;
-      if (row >= nrows) break;
-      uint2 *dst = reinterpret_cast<uint2 *>(spec_out) + ((int64_t)(row0 + row) * kpad) * kTcSlots + sg * SPC;
-      for (int i = threadIdx.x; i <= M; i += S::THREADS) {
-        uint2 o[SPC];
+    for (int j0 = 0; j0 < NS && sg0 + j0 < nstreams; j0 += W) {
+      int shift[W];
+      bool aligned = M == N;  // every stream's channel i is its bin i
 #pragma unroll
-        for (int j = 0; j < SPC; j++) {
-          const float2 f = real_bin<N>(dsm + (r * SPC + j) * S::BUF, tw_rot, shift[j] + i);
-          o[j] = tc_split(f.x, f.y, tc_scale);
+      for (int j = 0; j < W; j++) {
+        const int st = min(sg0 + j0 + j, nstreams - 1);
+        shift[j] = streams[st].output_offset - streams[st].temp_fft_offset;
+        aligned = aligned && shift[j] == 0;
+      }
+      uint2 *dst = reinterpret_cast<uint2 *>(spec_out) + (int64_t)row * kpad * kTcSlots + sg0 + j0;
+      if (aligned) {
+        for (int i = tid; i <= N / 2; i += nthr) {
+          const float2 w = __ldg(tw_rot + i);
+          uint2 a[W], b[W];
+#pragma unroll
+          for (int j = 0; j < W; j++) {
+            float2 xq, xnq;
+            real_bin_pair<N>(Z + (j0 + j) * BUF, w, i, xq, xnq);
+            a[j] = tc_split(xq, tc_scale);
+            b[j] = tc_split(xnq, tc_scale);
+          }
+          put(dst + (int64_t)i * kTcSlots, a);
+          if (i < N / 2) put(dst + (int64_t)(N - i) * kTcSlots, b);
         }
-        uint2 *p = dst + (int64_t)i * kTcSlots;
-        if constexpr (SPC == 1) {
-          *p = o[0];
-        } else if constexpr (SPC == 4) {
-          asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(o[0].x), "r"(o[0].y),
-                       "r"(o[1].x), "r"(o[1].y), "r"(o[2].x), "r"(o[2].y), "r"(o[3].x), "r"(o[3].y)
-                       : "memory");
-        } else {
-          static_assert(SPC == 2, "1, 2 or 4 streams per CTA");
-          *reinterpret_cast<uint4 *>(p) = make_uint4(o[0].x, o[0].y, o[1].x, o[1].y);
+      } else {
+        for (int i = tid; i <= M; i += nthr) {
+          uint2 o[W];
+#pragma unroll
+          for (int j = 0; j < W; j++) o[j] = tc_split(real_bin<N>(Z + (j0 + j) * BUF, tw_rot, shift[j] + i), tc_scale);
+          put(dst + (int64_t)i * kTcSlots, o);
         }
       }
     }
   } else {
 #pragma unroll 1
-    for (int gg = 0; gg < SPC * RPC; gg++) {
-      const int st = sg * SPC + gg % SPC, row = rg * RPC + gg / SPC;
-      if (st >= nstreams || row >= nrows) continue;
+    for (int j = 0; j < NS && sg0 + j < nstreams; j++) {
+      const int st = sg0 + j;
       const int shift = streams[st].output_offset - streams[st].temp_fft_offset;
-      float2 *dst = reinterpret_cast<float2 *>(spec_out) + ((int64_t)st * nrows_total + row0 + row) * kpad;
-      for (int i = threadIdx.x; i <= M; i += S::THREADS)
-        dst[i] = real_bin<N>(dsm + gg * S::BUF, tw_rot, shift + i);
+      float2 *dst = reinterpret_cast<float2 *>(spec_out) + ((int64_t)st * nrows_total + row) * kpad;
+      if (shift == 0 && M == N) {
+        for (int i = tid; i <= N / 2; i += nthr) {
+          float2 xq, xnq;
+          real_bin_pair<N>(Z + j * BUF, __ldg(tw_rot + i), i, xq, xnq);
+          dst[i] = xq;
+          if (i < N / 2) dst[N - i] = xnq;
+        }
+      } else {
+        for (int i = tid; i <= M; i += nthr) dst[i] = real_bin<N>(Z + j * BUF, tw_rot, shift + i);
+      }
     }
+  }
+}
+
+// Stage 2 as its own kernel, reading the fringe-stopped samples from s.ts:
+// a CTA of SPC x RPC groups of T threads, SPC streams x RPC rows.
+template <int LOGN>
+struct WinShape {
+  static constexpr int N = 1 << LOGN, T = N / 16;
+  static constexpr int SPC = T <= 256 ? 4 : 2;      // streams per CTA
+  static constexpr int RPC = T < 256 ? 256 / T : 1;  // rows per CTA
+  static constexpr int THREADS = SPC * RPC * T;
+  static constexpr int BUF = N + N / 16;  // padded FFT buffer (float2) of one group
+  static constexpr size_t SMEM = (size_t)SPC * RPC * BUF * sizeof(float2);
+  static_assert(THREADS == 1024, "one CTA of 1024 threads");
+};
+
+template <int LOGN, int OUT_TC>
+__global__ void __launch_bounds__(1024, 1) window_fft_kernel(
+    const StreamDev *__restrict__ streams, int nstreams, int row0, int nrows, int nrows_total,
+    const float *__restrict__ window, const float2 *__restrict__ tw_rot, int nper, int M, int kpad,
+    void *__restrict__ spec_out, float tc_scale) {
+  using S = WinShape<LOGN>;
+  constexpr int N = S::N, T = S::T, SPC = S::SPC, RPC = S::RPC;
+  extern __shared__ float2 dsm[];
+  const int t = threadIdx.x % T, g = threadIdx.x / T;
+  const int nsg = (nstreams + SPC - 1) / SPC;
+  const int sg = blockIdx.x % nsg, rg = blockIdx.x / nsg;  // stream group fastest
+  const int stream = sg * SPC + g % SPC, rr = rg * RPC + g / SPC;
+  const bool ok = stream < nstreams && rr < nrows;
+  const StreamDev &s = streams[ok ? stream : 0];
+  const float *ts = s.ts + (int64_t)(row0 + rr) * N;  // hop = rot / 2
+  float2 v[16];
+  window_load<T>(v, t, ok, nper, s.flip ? -1.0f : 1.0f, window,
+                 [ts](int i) { return *reinterpret_cast<const float2 *>(ts + i); });
+  // tw_rot holds exp(-2 pi i m / rot) for m < rot, followed by exp(-2 pi i m / N) for m < N.
+  fft_reg<-1, LOGN, true>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, BlockSync());
+#pragma unroll 1
+  for (int r = 0; r < RPC; r++) {
+    const int row = rg * RPC + r;
+    if (row >= nrows) break;
+    store_row<N, SPC, OUT_TC>(dsm + r * SPC * S::BUF, S::BUF, streams, nstreams, sg * SPC, row0 + row, nrows_total,
+                              M, kpad, tw_rot, spec_out, tc_scale, threadIdx.x, S::THREADS);
   }
 }
 
@@ -619,52 +691,40 @@ void launch_extract(const uint8_t *in, int64_t nout, int N, int bits, int nsub, 
   extract_kernel<<<dim3((unsigned)((nout + 255) / 256), nsub), 256, 0, st>>>(in, nout, N, bits, fan_out, tracks, out);
 }
 
-template <int LOGN, int OUT_TC, int SPCMAX>
+template <int LOGN, int OUT_TC>
 static void window_fft_launch(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                               const float *window, const float2 *tw_rot, int nper, int M, int kpad, void *spec,
                               float tc_scale, cudaStream_t st) {
-  using S = WinShape<LOGN, SPCMAX>;
+  using S = WinShape<LOGN>;
   const unsigned grid = (unsigned)((nrows + S::RPC - 1) / S::RPC) * (unsigned)((nstreams + S::SPC - 1) / S::SPC);
-  auto kern = window_fft_kernel<LOGN, OUT_TC, SPCMAX>;
+  auto kern = window_fft_kernel<LOGN, OUT_TC>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
   kern<<<grid, S::THREADS, S::SMEM, st>>>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad,
                                           spec, tc_scale);
 }
 
-template <int OUT_TC>
-static void window_fft_dispatch(int logn, const StreamDev *d_streams, int nstreams, int row0, int nrows,
-                                int nrows_total, const float *window, const float2 *tw_rot, int nper, int M, int kpad,
-                                void *spec, float tc_scale, cudaStream_t st) {
-  // four streams per CTA: a whole 32-byte sector per channel in the TC layout
-  // (two streams per CTA measured the same, one stream 30 % slower)
-  switch (logn) {
-#define SFXC_WIN_CASE(L)                                                                                            \
-  case L:                                                                                                           \
-    window_fft_launch<L, OUT_TC, 4>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad, \
-                                    spec, tc_scale, st);                                                            \
-    break;
-    SFXC_WIN_CASE(8)
-    SFXC_WIN_CASE(9)
-    SFXC_WIN_CASE(10)
-    SFXC_WIN_CASE(11)
-    SFXC_WIN_CASE(12)
-    SFXC_WIN_CASE(13)
-#undef SFXC_WIN_CASE
-    default:
-      break;  // sizes outside 2^9..2^14 samples are rejected by set_parameters
+#define SFXC_LOGN_SWITCH(logn, CALL) \
+  switch (logn) {                    \
+    case 8: CALL(8); break;          \
+    case 9: CALL(9); break;          \
+    case 10: CALL(10); break;        \
+    case 11: CALL(11); break;        \
+    case 12: CALL(12); break;        \
+    case 13: CALL(13); break;        \
+    default: break; /* sizes outside 2^9..2^14 samples are rejected by set_parameters */ \
   }
-}
 
 void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                        const float *window, const float2 *tw_rot, int rot, int nper, int M, int kpad, void *spec,
                        bool tc, float tc_scale, cudaStream_t st) {
   const int logn = 30 - __builtin_clz((unsigned)rot);  // log2(rot / 2)
-  if (tc)
-    window_fft_dispatch<1>(logn, d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad, spec,
-                           tc_scale, st);
-  else
-    window_fft_dispatch<0>(logn, d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad, spec,
-                           tc_scale, st);
+#define SFXC_WIN(L)                                                                                            \
+  (tc ? window_fft_launch<L, 1>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad, \
+                                spec, tc_scale, st)                                                           \
+      : window_fft_launch<L, 0>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad, \
+                                spec, tc_scale, st))
+  SFXC_LOGN_SWITCH(logn, SFXC_WIN)
+#undef SFXC_WIN
 }
 
 void launch_bitstat(const StreamDev *d_streams, const int4 *d_items, int nitems, cudaStream_t st) {
