@@ -159,13 +159,15 @@ __device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, f
 __global__ void __launch_bounds__(256, 4) fstep_block_kernel(const StreamDev *__restrict__ streams,
                                                          const float2 *__restrict__ tw) {
   __shared__ float2 sbuf[16][kNd + kNd / 16];
-  const int t = threadIdx.x & 15, grp = threadIdx.x >> 4;
+  const int t = threadIdx.x & 15, grp = threadIdx.x >> 4, warp = threadIdx.x >> 5;
   const StreamDev &s = streams[blockIdx.y];
-  const int first = blockIdx.x * 32;  // first block of the CTA
-  if (first + (threadIdx.x >> 5) * 4 >= s.n_blocks) return;  // whole warps only (warp barriers)
   float *ts = s.ts;
-  fstep_pair(s, first + grp * 2, t, sbuf[grp], tw,
-             [ts](int bl, int n, float x) { ts[(int64_t)bl * kNd + n] = x; });
+  // 32 blocks per CTA and round, rounds strided over the stream's blocks
+  for (int first = blockIdx.x * 32; first < s.n_blocks; first += gridDim.x * 32) {
+    if (first + warp * 4 >= s.n_blocks) break;  // whole warps only (warp barriers); later rounds lie further out
+    fstep_pair(s, first + grp * 2, t, sbuf[grp], tw,
+               [ts](int bl, int n, float x) { ts[(int64_t)bl * kNd + n] = x; });
+  }
 }
 
 // Per-block FP64 parameters of the F-step, one thread per 256-sample block
@@ -175,34 +177,53 @@ __global__ void __launch_bounds__(256, 4) fstep_block_kernel(const StreamDev *__
 // fractional delay at the block centre, the fringe phase at the block start
 // and its linear step over the block, the amplitude at the centre.  The
 // phases leave FP64 only after reduction to one turn.
-__global__ void block_params_kernel(const StreamDev *__restrict__ streams) {
+__global__ void __launch_bounds__(128) block_params_kernel(const StreamDev *__restrict__ streams) {
   const StreamDev &s = streams[blockIdx.y];
+  const int lane = threadIdx.x & 31;
   const int bl = blockIdx.x * blockDim.x + threadIdx.x;
+  // whole warps stay (neighbour exchange below); lanes past the end compute
+  // their block's times (the spline extrapolates) and store nothing
+  if ((int)(blockIdx.x * blockDim.x + (threadIdx.x & ~31)) >= s.n_blocks) return;
+  constexpr double kInvTick = 1.0 / 512000000.0, kInv2Pi = 0.15915494309189533577;
+  const int64_t ct = s.start_ticks + (int64_t)(s.block0 + bl) * kNd * s.tps;
+  auto delay = [&s](int64_t t) {
+    const double r = spline_eval(s.spline, s.spline_n, 0, (double)(t - s.scan_begin) * kInvTick);
+    return s.no_clock ? r : r + (s.clock_offset + (double)(t - s.clock_epoch) * kInvTick * s.clock_rate);
+  };
+  auto phase = [&s](int64_t t) {
+    return s.phase_zero ? 0.0 : spline_eval(s.spline, s.spline_n, 1, (double)(t - s.scan_begin) * kInvTick);
+  };
+  const double delay_c = delay(ct + s.half_len_ticks);
+  const double delay_0 = delay(ct);
+  const double phase_0 = phase(ct);
+  // the end of a block is the start of the next when a block is a whole
+  // number of ticks: take it from the next lane
+  const bool chained = s.fft_len_ticks == (int64_t)kNd * s.tps;
+  double delay_1 = __shfl_down_sync(0xffffffffu, delay_0, 1);
+  double phase_1 = __shfl_down_sync(0xffffffffu, phase_0, 1);
+  if (!chained || lane == 31) {
+    delay_1 = delay(ct + s.fft_len_ticks);
+    phase_1 = phase(ct + s.fft_len_ticks);
+  }
   if (bl >= s.n_blocks) return;
-  const int b = s.block0 + bl;
-  const int64_t ct = s.start_ticks + (int64_t)b * kNd * s.tps;
-  const double delay_c = stream_delay(s, ct + s.half_len_ticks);
-  const double delay_0 = stream_delay(s, ct);
-  const double delay_1 = stream_delay(s, ct + s.fft_len_ticks);
-  const double phase_0 = s.phase_zero ? 0.0 : stream_phase(s, ct);
-  const double phase_1 = s.phase_zero ? 0.0 : stream_phase(s, ct + s.fft_len_ticks);
-  const double ampl = s.amp_one ? 1.0 : stream_amplitude(s, ct + s.half_len_ticks);
+  const double ampl =
+      s.amp_one ? 1.0 : spline_eval(s.spline, s.spline_n, 2, (double)(ct + s.half_len_ticks - s.scan_begin) * kInvTick);
   const double dis = __dmul_rn(delay_c, (double)s.sample_rate);
   const int integer_delay = (int)floor(__dadd_rn(dis, 0.5));
   const double frac = dis - integer_delay;
-  const double tmp1 = -2.0 * M_PI * frac / s.sample_rate;
-  const double tmp2 = M_PI * (integer_delay & (4 * s.oversamp - 1)) / (2 * s.oversamp);
+  const double tmp1 = frac * (-2.0 * M_PI / s.sample_rate);
+  const double tmp2 = (integer_delay & (4 * s.oversamp - 1)) * (M_PI / (2 * s.oversamp));
   const double cterm = tmp2 - tmp1 * 0.5 * s.bandwidth;
-  const double lterm = tmp1 * ((double)s.sample_rate / kNd);
+  const double lterm = tmp1 * ((double)s.sample_rate * (1.0 / kNd));
   const double mult = -s.sideband * 2.0 * M_PI;
-  const double lo_phase = s.start_phase + s.lo_offset * time_diff_dev(ct, s.start_ticks);
-  double phi = s.center_freq * delay_0 + lo_phase + phase_0 / (2 * M_PI);
+  const double lo_phase = s.start_phase + s.lo_offset * ((double)(ct - s.start_ticks) * kInvTick);
+  double phi = s.center_freq * delay_0 + lo_phase + phase_0 * kInv2Pi;
   const double floor_phi = floor(phi);
   phi = mult * (phi - floor_phi);
-  double phi_end = s.center_freq * delay_1 + lo_phase + s.fft_len_sec * s.lo_offset + phase_1 / (2 * M_PI);
+  double phi_end = s.center_freq * delay_1 + lo_phase + s.fft_len_sec * s.lo_offset + phase_1 * kInv2Pi;
   phi_end = mult * (phi_end - floor_phi);
-  s.bparams[bl] = make_float4((float)(cterm - 2.0 * M_PI * floor(cterm / (2.0 * M_PI))), (float)lterm, (float)phi,
-                              (float)((phi_end - phi) / kNd));
+  s.bparams[bl] = make_float4((float)(cterm - 2.0 * M_PI * floor(cterm * kInv2Pi)), (float)lterm, (float)phi,
+                              (float)((phi_end - phi) * (1.0 / kNd)));
   s.bamp[bl] = (float)ampl;
 }
 
@@ -675,10 +696,22 @@ __global__ void normalize_kernel(const float2 *__restrict__ acc, int kpad, int M
 
 // ------------------------------------------------------------------------
 // launchers
+static int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    n = cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0 ? v : 1;
+  }
+  return n;
+}
+
 void launch_fstep_block(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256,
                         cudaStream_t st) {
   block_params_kernel<<<dim3((max_blocks + 127) / 128, nstreams), 128, 0, st>>>(d_streams);
-  dim3 grid((max_blocks + 31) / 32, nstreams);
+  // about two waves of 4 resident CTAs per SM, each CTA looping over rounds
+  const int per_stream = std::max(1, 8 * sm_count() / nstreams);
+  dim3 grid(std::min((max_blocks + 31) / 32, per_stream), nstreams);
   fstep_block_kernel<<<grid, 256, 0, st>>>(d_streams, tw256);
 }
 
