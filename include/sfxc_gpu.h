@@ -219,6 +219,45 @@ int sfxc_gpu_extract_channels(sfxc_gpu_ctx *ctx, const uint8_t *words, int64_t n
                               int32_t bits_per_sample, int32_t n_subbands, int32_t fan_out, const int32_t *tracks,
                               uint8_t *out);
 
+/* Station recordings read into input-node blocks: the reference's VDIF and
+ * Mark5B readers as Input_data_format_reader_tasklet drives them
+ * (VDIF_reader::open_input_stream / read_new_block / set_parameters,
+ * sfxc/src/vdif_reader.cc:19-36,77-190,202-226; Mark5b_reader, same calls,
+ * sfxc/src/mark5b_reader.cc:23-38,111-162,241-327; fill-pattern runs,
+ * sfxc/src/input_data_format_reader.cc:20-72).  Host only, no GPU needed. */
+#define SFXC_GPU_FORMAT_VDIF 0
+#define SFXC_GPU_FORMAT_MARK5B 1
+/* Input_node_parameters (sfxc/include/control_parameters.h:16-66) as the readers use it. */
+typedef struct {
+  int32_t format;             /* SFXC_GPU_FORMAT_* */
+  int64_t ref_ticks;          /* reference time; its day is the reader's reference MJD */
+  int64_t offset_ticks;       /* subtracted from every block time */
+  int32_t track_bit_rate;     /* samples/s per track (Mark5B: whole Mb/s) */
+  int32_t frame_size;         /* VDIF payload bytes per frame */
+  int32_t n_tracks;           /* VDIF: 0 = one thread per channel; Mark5B: bitstreams */
+  int32_t bits_per_sample;    /* 1 or 2 */
+  int32_t tracks_per_channel; /* sample rate = track_bit_rate * tracks_per_channel / bits_per_sample */
+  int32_t n_channels;
+  const int32_t *first_track; /* per channel: its first track (VDIF thread id when n_tracks == 0) */
+} sfxc_reader_params;
+typedef struct sfxc_gpu_reader sfxc_gpu_reader;
+/* One reader block (Input_node_types::Input_data_frame). */
+typedef struct {
+  const uint8_t *data;    /* payload; valid until the next call on the reader */
+  int32_t size;
+  int32_t channel;        /* VDIF thread's channel, -1 for Mark5B */
+  int64_t start_ticks;
+  int32_t n_invalid;      /* invalid byte runs: invalid[2k] first byte, invalid[2k+1] length */
+  const int32_t *invalid;
+} sfxc_reader_block;
+/* Reader over bytes[0, n), which must stay valid until sfxc_gpu_reader_destroy;
+ * NULL on bad parameters (message from sfxc_gpu_global_error). */
+sfxc_gpu_reader *sfxc_gpu_reader_create(const sfxc_reader_params *params, const uint8_t *bytes, size_t n);
+/* The next block: 1 and *out filled, 0 at the end of the data (or when no
+ * valid block follows within the readers' search limits). */
+int sfxc_gpu_reader_next(sfxc_gpu_reader *reader, sfxc_reader_block *out);
+void sfxc_gpu_reader_destroy(sfxc_gpu_reader *reader);
+
 #ifdef __cplusplus
 }
 #endif

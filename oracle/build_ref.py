@@ -42,6 +42,12 @@ REF_SOURCES = [
     "src/input_node_tasklet.cc",
     "src/channel_extractor_5.cc",
     "src/control_parameters.cc",
+    "src/vdif_reader.cc",
+    "src/mark5b_reader.cc",
+    "src/input_data_format_reader.cc",
+    "src/data_reader.cc",
+    "src/data_reader_file.cc",
+    "src/data_reader_blocking.cc",
     "src/tasklet/tasklet.cc",
     "lib/common/src/align_malloc.cc",
     "lib/common/src/thread.cc",

@@ -122,6 +122,32 @@ def extract(words_bytes, word_bytes, bits, nsamples, tracks, impl="reference"):
         return [raw[i * per:(i + 1) * per] for i in range(len(tracks))]
 
 
+def reader(recording, fmt, *, ref_ticks, offset_ticks=0, track_bit_rate, frame_size=0, n_tracks, bits,
+           channel_tracks, max_blocks=1000000):
+    """Blocks of the reference's VDIF_reader / Mark5b_reader over a recording:
+    dicts {channel, start_ticks, data, invalid [(begin, n)]}.  Only the
+    reference's own classes implement this (there is no restatement)."""
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "rec.bin")
+        open(path, "wb").write(bytes(recording))
+        lines = [("format", fmt), ("file", path), ("ref_ticks", ref_ticks), ("offset_ticks", offset_ticks),
+                 ("track_bit_rate", track_bit_rate), ("frame_size", frame_size), ("n_tracks", n_tracks),
+                 ("bits", bits), ("max_blocks", max_blocks)]
+        lines += [("channel#%d" % c, *tr) for c, tr in enumerate(channel_tracks)]
+        out = os.path.join(d, "out")
+        os.makedirs(out)
+        _run("reader", lines, out, d, "reference")
+        raw = open(os.path.join(out, "data.bin"), "rb").read()
+        blocks, pos = [], 0
+        for line in open(os.path.join(out, "blocks.txt")):
+            v = [int(x) for x in line.split()]
+            ch, ticks, size, inv = v[0], v[1], v[2], v[3:]
+            blocks.append({"channel": ch, "start_ticks": ticks, "data": raw[pos:pos + size],
+                           "invalid": [(inv[k], inv[k + 1]) for k in range(0, len(inv), 2)]})
+            pos += size
+        return blocks
+
+
 def correlate(job, dump=False, impl="reference", precision=32):
     """Run Bit2float_worker -> Delay_correction -> Correlation_core(_pulsar).
 

@@ -34,6 +34,9 @@
 #include "delay_table_akima.h"
 #include "input_node_data_writer.h"
 #include "input_node_tasklet.h"
+#include "data_reader_file.h"
+#include "mark5b_reader.h"
+#include "vdif_reader.h"
 #undef private
 #undef protected
 
@@ -569,14 +572,76 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
   return 0;
 }
 
+// Format readers (VDIF_reader, Mark5b_reader, sfxc/src/vdif_reader.cc,
+// sfxc/src/mark5b_reader.cc) over a file, as Input_data_format_reader_tasklet
+// drives them: open_input_stream, then read_new_block with the frame's
+// invalid list emptied in between.  Per block: channel, start ticks, payload
+// size and invalid byte runs (blocks.txt); payloads back to back (data.bin).
+//   format vdif|mark5b ; file <path> ; ref_ticks ; offset_ticks ;
+//   track_bit_rate ; frame_size ; n_tracks ; bits ; channel#k <tracks...> ;
+//   max_blocks
+static int mode_reader(Kv &kv, const std::string &od) {
+  Input_node_parameters p;
+  p.track_bit_rate = geti(kv, "track_bit_rate");
+  p.frame_size = geti(kv, "frame_size");
+  p.n_tracks = geti(kv, "n_tracks");
+  p.offset = ticks_time(getll(kv, "offset_ticks"));
+  const int nch = count_key(kv, "channel");
+  for (int c = 0; c < nch; c++) {
+    Input_node_parameters::Channel_parameters cp;
+    cp.bits_per_sample = geti(kv, "bits");
+    const std::vector<std::string> &tr = get(kv, idx("channel", c));
+    for (size_t k = 0; k < tr.size(); k++) cp.tracks.push_back(std::atoi(tr[k].c_str()));
+    cp.sideband = 'U';
+    cp.polarisation = 'R';
+    cp.frequency_number = c;
+    p.channels.push_back(cp);
+  }
+  boost::shared_ptr<Data_reader> dr(new Data_reader_file("file://" + get(kv, "file")[0]));
+  Input_node_types::Data_memory_pool &pool = *new Input_node_types::Data_memory_pool(4);  // leaked, see above
+  Input_data_format_reader::Data_frame data;
+  data.buffer = pool.allocate();
+  const Time ref = ticks_time(getll(kv, "ref_ticks"));
+  const std::string fmt = get(kv, "format")[0];
+  Input_data_format_reader *r;
+  if (fmt == "vdif")
+    r = new VDIF_reader(dr, data, ref);
+  else if (fmt == "mark5b")
+    r = new Mark5b_reader(dr, data, ref);
+  else
+    die("unknown format " + fmt);
+  r->set_parameters(p);
+  FILE *bf = std::fopen((od + "/blocks.txt").c_str(), "w");
+  FILE *df = std::fopen((od + "/data.bin").c_str(), "wb");
+  if (!bf || !df) die("cannot write reader output");
+  const int maxb = geti(kv, "max_blocks");
+  bool ok = r->open_input_stream(data);
+  int n = 0;
+  while (ok && n < maxb) {
+    const std::vector<unsigned char> &b = data.buffer->data;
+    std::fprintf(bf, "%d %lld %d", data.channel, (long long)data.start_time.get_clock_ticks(), (int)b.size());
+    for (size_t k = 0; k < data.invalid.size(); k++)
+      std::fprintf(bf, " %d %d", data.invalid[k].invalid_begin, data.invalid[k].nr_invalid);
+    std::fprintf(bf, "\n");
+    if (!b.empty()) std::fwrite(&b[0], 1, b.size(), df);
+    n++;
+    data.invalid.clear();
+    ok = r->read_new_block(data);
+  }
+  std::fclose(bf);
+  std::fclose(df);
+  return 0;
+}
+
 int main(int argc, char **argv) {
-  if (argc != 4) die("usage: ref_harness correlate|delays|protocol|extract <job> <out>");
+  if (argc != 4) die("usage: ref_harness correlate|delays|protocol|extract|reader <job> <out>");
   Kv kv = read_job(argv[2]);
   std::string m(argv[1]);
   if (m == "correlate") return mode_correlate(kv, argv[3]);
   if (m == "delays") return mode_delays(kv, argv[3]);
   if (m == "protocol") return mode_protocol(kv, argv[3]);
   if (m == "extract") return mode_extract(kv, argv[3]);
+  if (m == "reader") return mode_reader(kv, argv[3]);
   die("unknown mode " + m);
   return 2;
 }

@@ -69,3 +69,17 @@ extern "C" int MPI_Comm_rank(MPI_Comm, int *rank) {
   *rank = 0;
   return MPI_SUCCESS;
 }
+
+// Modified Julian Day of a Gregorian calendar date, the helper that
+// sfxc/src/utils.cc:255 provides to the format readers (VDIF epochs).  Own
+// formulation: days since 0000-03-01 of the proleptic Gregorian calendar,
+// minus that count for 1858-11-17.
+int mjd(int day, int month, int year) {
+  const int y = year - (month <= 2 ? 1 : 0);
+  const int era = (y >= 0 ? y : y - 399) / 400;
+  const int yoe = y - era * 400;
+  const int mp = (month + 9) % 12;
+  const int doy = (153 * mp + 2) / 5 + day - 1;
+  const int doe = yoe * 365 + yoe / 4 - yoe / 100 + doy;
+  return era * 146097 + doe - 678881;
+}

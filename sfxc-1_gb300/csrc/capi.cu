@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 
+#include "formats.hpp"
 #include "host.hpp"
 #include "kernels.hpp"
 #include "sfxc_gpu.h"
@@ -246,7 +247,7 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
     s.rot = (int)(((uint64_t)2 * c->M * (uint64_t)ss.sample_rate) / p->sample_rate);
     s.hop = s.rot / 2;
     if (s.rot & (s.rot - 1)) throw Error(SFXC_GPU_EINVAL, "FFT length per stream must be a power of two");
-    if (s.rot > 16384) throw Error(SFXC_GPU_EINVAL, "FFT lengths above 16384 samples are not supported yet");
+    if (s.rot > 32768) throw Error(SFXC_GPU_EINVAL, "FFT lengths above 32768 samples are not supported");
     if (s.rot != 2 * c->M) throw Error(SFXC_GPU_EINVAL, "mixed sample rates within a job are not supported yet");
   }
   c->bl = create_baselines(c->streams, p->reference_station);
@@ -1045,5 +1046,52 @@ int64_t sfxc_gpu_write_protocol(const uint8_t *stream, int32_t n_blocks, const s
     return e.code;
   }
 }
+
+
+struct sfxc_gpu_reader {
+  std::unique_ptr<FormatReader> r;
+  ReaderBlock block;
+};
+
+sfxc_gpu_reader *sfxc_gpu_reader_create(const sfxc_reader_params *p, const uint8_t *bytes, size_t n) {
+  try {
+    if (!p || (n && !bytes)) throw Error(SFXC_GPU_EINVAL, "no reader parameters or data");
+    if (p->n_channels <= 0 || !p->first_track) throw Error(SFXC_GPU_EINVAL, "no channels");
+    ReaderParams rp;
+    rp.format = p->format;
+    rp.ref_ticks = p->ref_ticks;
+    rp.offset_ticks = p->offset_ticks;
+    rp.track_bit_rate = p->track_bit_rate;
+    rp.frame_size = p->frame_size;
+    rp.n_tracks = p->n_tracks;
+    rp.bits_per_sample = p->bits_per_sample;
+    rp.tracks_per_channel = p->tracks_per_channel;
+    rp.first_track.assign(p->first_track, p->first_track + p->n_channels);
+    std::unique_ptr<sfxc_gpu_reader> h(new sfxc_gpu_reader());
+    try {
+      h->r = FormatReader::create(rp, bytes, n);
+    } catch (const std::exception &e) {
+      throw Error(SFXC_GPU_EINVAL, e.what());
+    }
+    return h.release();
+  } catch (const Error &e) {
+    g_error = e.msg;
+    return nullptr;
+  }
+}
+
+int sfxc_gpu_reader_next(sfxc_gpu_reader *h, sfxc_reader_block *out) {
+  if (!h || !out) return SFXC_GPU_EINVAL;
+  if (!h->r->next(h->block)) return 0;
+  out->data = h->block.data.data();
+  out->size = (int32_t)h->block.data.size();
+  out->channel = h->block.channel;
+  out->start_ticks = h->block.start_ticks;
+  out->n_invalid = (int32_t)(h->block.invalid.size() / 2);
+  out->invalid = h->block.invalid.data();
+  return 1;
+}
+
+void sfxc_gpu_reader_destroy(sfxc_gpu_reader *h) { delete h; }
 
 }  // extern "C"

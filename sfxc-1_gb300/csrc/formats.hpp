@@ -1,0 +1,49 @@
+// Station recording formats on the host: VDIF and Mark5B frame readers that
+// turn a recording (bytes in memory) into the reader blocks of the input
+// node -- payload bytes, start time, channel, invalid byte runs -- with the
+// block, skip, restart and resync rules of the reference's readers
+// (VDIF_reader, sfxc/src/vdif_reader.cc; Mark5b_reader,
+// sfxc/src/mark5b_reader.cc; fill-pattern search,
+// sfxc/src/input_data_format_reader.cc:20-72).
+#pragma once
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+namespace sfxc {
+
+enum { FORMAT_VDIF = 0, FORMAT_MARK5B = 1 };
+
+struct ReaderParams {
+  int format = FORMAT_VDIF;
+  int64_t ref_ticks = 0;      // reference time; its day is the reader's reference MJD
+  int64_t offset_ticks = 0;   // Input_node_parameters::offset, subtracted from every time
+  int track_bit_rate = 0;     // samples/s per track
+  int frame_size = 0;         // VDIF payload bytes per frame
+  int n_tracks = 0;           // VDIF: 0 = one thread per channel; Mark5B: bitstreams
+  int bits_per_sample = 2;
+  int tracks_per_channel = 2;
+  std::vector<int> first_track;  // per channel: its first track (the VDIF thread id when n_tracks == 0)
+};
+
+struct ReaderBlock {
+  std::vector<uint8_t> data;
+  int channel = -1;
+  int64_t start_ticks = 0;
+  std::vector<int32_t> invalid;  // (begin, n) byte pairs
+};
+
+// Reads the recording bytes[0, n) (not copied: they must outlive the reader).
+class FormatReader {
+ public:
+  virtual ~FormatReader() {}
+  // The next block; false at the end of the data (or when no valid block can
+  // be found within the readers' search limits).
+  virtual bool next(ReaderBlock &out) = 0;
+  static std::unique_ptr<FormatReader> create(const ReaderParams &p, const uint8_t *bytes, size_t n);
+};
+
+// Modified Julian Day of a Gregorian date (day count from 1858-11-17).
+int mjd_of_date(int day, int month, int year);
+
+}  // namespace sfxc

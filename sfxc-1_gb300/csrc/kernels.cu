@@ -406,7 +406,7 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const Stream
 template <int LOGN>
 struct WinShape {
   static constexpr int N = 1 << LOGN, T = N / 16;
-  static constexpr int SPC = T <= 256 ? 4 : 2;      // streams per CTA
+  static constexpr int SPC = T <= 256 ? 4 : 1024 / T;  // streams per CTA
   static constexpr int RPC = T < 256 ? 256 / T : 1;  // rows per CTA
   static constexpr int THREADS = SPC * RPC * T;
   static constexpr int BUF = N + N / 16;  // padded FFT buffer (float2) of one group
@@ -744,7 +744,8 @@ static void window_fft_launch(const StreamDev *d_streams, int nstreams, int row0
     case 11: CALL(11); break;        \
     case 12: CALL(12); break;        \
     case 13: CALL(13); break;        \
-    default: break; /* sizes outside 2^9..2^14 samples are rejected by set_parameters */ \
+    case 14: CALL(14); break;        \
+    default: break; /* sizes outside 2^9..2^15 samples are rejected by set_parameters */ \
   }
 
 void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,

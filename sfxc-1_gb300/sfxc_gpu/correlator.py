@@ -259,3 +259,36 @@ def write_protocol(blocks, slices, sample_rate, bits, integration_time_us):
         raise L.SfxcError(int(n), lib.sfxc_gpu_global_error().decode())
     raw = bytes(out)[:n]
     return [raw[offs[i]:offs[i + 1]] for i in range(len(slices))]
+
+
+def read_recording(recording, fmt, *, ref_ticks, offset_ticks=0, track_bit_rate, frame_size=0, n_tracks, bits,
+                   channel_tracks, max_blocks=None):
+    """Reader blocks of a VDIF or Mark5B recording (fmt "vdif" / "mark5b"):
+    dicts {channel, start_ticks, data, invalid [(begin, n)]}, as the input
+    node's reader produces them.  channel_tracks: the track list of each
+    channel (its first track is the VDIF thread id when n_tracks == 0)."""
+    lib = L.load()
+    data = np.frombuffer(bytes(recording), dtype=np.uint8)
+    firsts = (C.c_int32 * len(channel_tracks))(*[int(t[0]) for t in channel_tracks])
+    p = L.ReaderParams(L.FORMAT_VDIF if fmt == "vdif" else L.FORMAT_MARK5B, int(ref_ticks), int(offset_ticks),
+                       int(track_bit_rate), int(frame_size), int(n_tracks), int(bits), len(channel_tracks[0]),
+                       len(channel_tracks), firsts)
+    h = lib.sfxc_gpu_reader_create(C.byref(p), data.ctypes.data if data.size else None, data.size)
+    if not h:
+        raise L.SfxcError(L.EINVAL, lib.sfxc_gpu_global_error().decode())
+    blocks = []
+    try:
+        b = L.ReaderBlock()
+        while max_blocks is None or len(blocks) < max_blocks:
+            rc = lib.sfxc_gpu_reader_next(h, C.byref(b))
+            if rc < 0:
+                raise L.SfxcError(rc, "reader failed")
+            if rc == 0:
+                break
+            inv = [(b.invalid[2 * k], b.invalid[2 * k + 1]) for k in range(b.n_invalid)]
+            blocks.append({"channel": b.channel, "start_ticks": b.start_ticks, "data": C.string_at(b.data, b.size),
+                           "invalid": inv})
+    finally:
+        lib.sfxc_gpu_reader_destroy(h)
+    return blocks
+

@@ -18,7 +18,9 @@ EXPORTS = [
     "sfxc_gpu_set_parameters", "sfxc_gpu_push_protocol", "sfxc_gpu_run_integration",
     "sfxc_gpu_copy_unpacked", "sfxc_gpu_copy_spectra", "sfxc_gpu_last_timings", "sfxc_gpu_delay_list",
     "sfxc_gpu_write_protocol", "sfxc_gpu_extract_channels", "sfxc_gpu_copy_spectra_noalloc",
+    "sfxc_gpu_reader_create", "sfxc_gpu_reader_next", "sfxc_gpu_reader_destroy",
 ]
+FORMAT_VDIF, FORMAT_MARK5B = 0, 1
 
 
 class Config(C.Structure):
@@ -67,6 +69,18 @@ class Slice(C.Structure):
                 ("delay_bytes", C.POINTER(C.c_int32)), ("delay_remaining", C.POINTER(C.c_int32))]
 
 
+class ReaderParams(C.Structure):
+    _fields_ = [("format", C.c_int32), ("ref_ticks", C.c_int64), ("offset_ticks", C.c_int64),
+                ("track_bit_rate", C.c_int32), ("frame_size", C.c_int32), ("n_tracks", C.c_int32),
+                ("bits_per_sample", C.c_int32), ("tracks_per_channel", C.c_int32), ("n_channels", C.c_int32),
+                ("first_track", C.POINTER(C.c_int32))]
+
+
+class ReaderBlock(C.Structure):
+    _fields_ = [("data", C.POINTER(C.c_uint8)), ("size", C.c_int32), ("channel", C.c_int32),
+                ("start_ticks", C.c_int64), ("n_invalid", C.c_int32), ("invalid", C.POINTER(C.c_int32))]
+
+
 SINK = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t)
 
 _lib = None
@@ -103,6 +117,10 @@ def load(path=None):
                                             C.c_int64, C.POINTER(C.c_int64)]
     lib.sfxc_gpu_extract_channels.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                               C.c_int32, C.POINTER(C.c_int32), C.c_void_p]
+    lib.sfxc_gpu_reader_create.restype = C.c_void_p
+    lib.sfxc_gpu_reader_create.argtypes = [C.POINTER(ReaderParams), C.c_void_p, C.c_size_t]
+    lib.sfxc_gpu_reader_next.argtypes = [C.c_void_p, C.POINTER(ReaderBlock)]
+    lib.sfxc_gpu_reader_destroy.argtypes = [C.c_void_p]
     _lib = lib
     return lib
 

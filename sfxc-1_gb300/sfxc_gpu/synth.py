@@ -264,3 +264,140 @@ def vdif_file_bytes(words: np.ndarray, *, payload_bytes: int, sample_rate: int, 
                            thread_id, station_id, f in inv)
         out += payload[f].tobytes()
     return bytes(out)
+
+
+# --------------------------------------------------------------------------
+# Recordings with the irregularities the format readers handle
+# --------------------------------------------------------------------------
+VDIF_FILL_WORD = 0x11223344
+
+
+def vdif_recording(nframes: int, *, payload_bytes: int, frames_per_second: int, start_mjd: int,
+                   start_sec_of_day: int, log2_nchan: int, bits: int, legacy: bool = False, threads=(0,),
+                   invalid=(), fill=(), drop=(), first_frame: int = 0, seed: int = 0) -> bytes:
+    """VDIF frames with random payloads.  Frame k belongs to thread
+    threads[k % len(threads)] and is that thread's (first_frame + k //
+    len(threads))-th frame of the recording; `invalid` frames carry the
+    invalid bit, `fill` frames are fill pattern throughout (header and
+    payload), `drop` frames are left out.  Legacy frames have 16-byte headers."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ref_epoch, epoch_mjd = vdif_ref_epoch(start_mjd)
+    sec0 = (start_mjd - epoch_mjd) * 86400 + start_sec_of_day
+    hbytes = 16 if legacy else 32
+    out = bytearray()
+    for k in range(nframes):
+        if k in drop:
+            continue
+        if k in fill:
+            out += struct.pack("<I", VDIF_FILL_WORD) * ((hbytes + payload_bytes) // 4)
+            continue
+        n = first_frame + k // len(threads)
+        h = bytearray(vdif_header(sec0 + n // frames_per_second, n % frames_per_second, ref_epoch,
+                                  payload_bytes + hbytes, log2_nchan, bits, threads[k % len(threads)], 0,
+                                  k in invalid))
+        if legacy:
+            h[3] |= 0x40  # legacy-mode bit (word 0, bit 30)
+        out += bytes(h[:hbytes])
+        out += rng.integers(0, 256, payload_bytes, dtype=np.uint8).tobytes()
+    return bytes(out)
+
+
+MK5B_SYNC = 0xABADDEED
+MK5B_FRAME_BYTES = 10000
+
+
+def _mk5b_crc_table():
+    tab = []
+    for i in range(256):
+        c = (i << 8) & 0xFFFF
+        for _ in range(8):
+            c = ((c << 1) ^ 0x8005) & 0xFFFF if c & 0x8000 else (c << 1) & 0xFFFF
+        tab.append(c)
+    return tab
+
+
+_MK5B_TAB = _mk5b_crc_table()
+
+
+def _mk5b_register(b: bytes) -> int:
+    """Mark5B header check register over words 2-3 (bytes of each word from
+    the most significant), 32-bit and never masked: zero means valid."""
+    crc = 0
+    for word in (2, 3):
+        for i in (3, 2, 1, 0):
+            crc ^= b[word * 4 + i] << 8
+            crc = ((crc << 8) ^ _MK5B_TAB[(crc >> 8) & 0xFF]) & 0xFFFFFFFF
+    return crc
+
+
+_MK5B_SOLVE = None
+
+
+def mk5b_valid_crc(header16: bytes) -> int:
+    """The CRC field value that makes the header check pass.  The register
+    is affine over GF(2) in the 16 CRC bits, so R(x) = R(0) ^ A x with A fixed:
+    tabulate A x once and look up R(0)."""
+    global _MK5B_SOLVE
+    b = bytearray(header16)
+    if _MK5B_SOLVE is None:
+        z = bytearray(16)
+        r0 = _mk5b_register(bytes(z))
+        cols = []
+        for i in range(16):
+            z[12:14] = struct.pack("<H", 1 << i)
+            cols.append(_mk5b_register(bytes(z)) ^ r0)
+        table = {}
+        for x in range(1 << 16):
+            v = 0
+            for i in range(16):
+                if x >> i & 1:
+                    v ^= cols[i]
+            table[v] = x
+        _MK5B_SOLVE = table
+    b[12:14] = b"\0\0"
+    r = _mk5b_register(bytes(b))
+    x = _MK5B_SOLVE.get(r)
+    if x is None:
+        raise ValueError("no CRC value passes the header check")
+    return x
+
+
+def _bcd(value: int, digits: int) -> int:
+    return int("%0*d" % (digits, value), 16)
+
+
+def mark5b_recording(nframes: int, *, mjd: int, sec_of_day: int, frames_per_second: int, seed: int = 0,
+                     first_frame: int = 0, crc: str = "zero", bad_crc=(), bad_sync=(), garbage=None,
+                     fill_runs=(), no_subsec=False) -> bytes:
+    """Mark5B frames (16-byte header + 10000 bytes) with random payloads,
+    frame numbers counting within each second from first_frame.  crc: "zero"
+    (the field left 0, accepted without a check) or "valid" (the value that
+    passes the check); bad_crc frames get a failing value, bad_sync frames a
+    wrong sync word; garbage = {frame: nbytes} inserts random bytes before a
+    frame; fill_runs = [(frame, first word, nwords)] writes the fill word into
+    payloads; no_subsec leaves the fractional-second field zero."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    garbage = garbage or {}
+    out = bytearray()
+    for k in range(nframes):
+        if k in garbage:
+            out += rng.integers(0, 256, garbage[k], dtype=np.uint8).tobytes()
+        n = first_frame + k
+        sec = sec_of_day + n // frames_per_second
+        fn = n % frames_per_second
+        day = mjd + sec // 86400
+        sec %= 86400
+        sub = 0 if no_subsec else (fn * 10000) // frames_per_second  # 0.1 ms units
+        w1 = fn & 0x7FFF
+        w2 = _bcd(day % 1000, 3) << 20 | _bcd(sec, 5)
+        w3 = _bcd(sub, 4) << 16
+        h = bytearray(struct.pack("<IIII", MK5B_SYNC if k not in bad_sync else 0xABADDEEE, w1, w2, w3))
+        if crc == "valid" or k in bad_crc:
+            c = mk5b_valid_crc(bytes(h))
+            h[12:14] = struct.pack("<H", c ^ 0x0101 if k in bad_crc else c)
+        payload = bytearray(rng.integers(0, 256, MK5B_FRAME_BYTES, dtype=np.uint8).tobytes())
+        for (f, w0, nw) in fill_runs:
+            if f == k:
+                payload[4 * w0:4 * (w0 + nw)] = struct.pack("<I", VDIF_FILL_WORD) * nw
+        out += bytes(h) + bytes(payload)
+    return bytes(out)

@@ -121,7 +121,28 @@ def make_extract():
     print("extract done")
 
 
+def make_formats():
+    """Blocks of the reference's VDIF / Mark5B readers for the recordings of
+    tests/format_cases.py (regenerated from their seeds by the tests): per
+    block the channel, start ticks, payload SHA-256 and invalid runs."""
+    import hashlib
+    import json
+    sys.path.insert(0, os.path.dirname(HERE))
+    import format_cases
+    out = {}
+    for name, c in format_cases.cases().items():
+        blocks = jobs.reader(c["rec"], c["fmt"], **c["params"])
+        out[name] = {"recording_sha256": hashlib.sha256(c["rec"]).hexdigest(),
+                     "blocks": [{"channel": b["channel"], "start_ticks": b["start_ticks"], "size": len(b["data"]),
+                                 "sha256": hashlib.sha256(b["data"]).hexdigest(),
+                                 "invalid": [list(r) for r in b["invalid"]]} for b in blocks]}
+    with open(os.path.join(HERE, "formats.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    print("formats done")
+
+
 if __name__ == "__main__":
+    make_formats()
     make_extract()
     for name, sc in scenarios().items():
         make(name, sc)

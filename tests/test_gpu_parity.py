@@ -95,6 +95,23 @@ def test_larger_job_vs_oracle(gpu_node):
     compare_cor(cor, ref["cor"], 4096, FP32_TOL)
 
 
+@pytest.mark.parametrize("nchan", [256, 16384])
+def test_fft_length_extremes_vs_oracle(gpu_node, nchan):
+    """The smallest (512-sample) and largest (32768-sample) windowed FFTs,
+    three stations x two polarisations, against the C restatement."""
+    from oracle import jobs
+    from sfxc_gpu import correlator, scenario
+    st = scenario.cubic_stations(3, seed=77, max_delay=5e-3, max_rate=2e-6)
+    sc = scenario.Scenario(stations=st, pols=("R", "L"), sample_rate=32_000_000, bandwidth=16_000_000, bits=2,
+                           channel_freq=1_400_000_000, nchan=nchan, integration_us=65536, n_integrations=1,
+                           sub_integration_us=32768, lead_us=8000, seed=11, block_bytes=4000)
+    job = scenario.build_job(sc, correlator.delay_list, correlator.write_protocol, fast_random=True)
+    cor, tsys = gpu_node.correlate(job)
+    ref = jobs.correlate(job, impl="oracle")
+    assert tsys == ref["tsys"]
+    compare_cor(cor, ref["cor"], nchan, FP32_TOL)
+
+
 def record_boundaries(data):
     """Offsets at which the correlator-node protocol records end."""
     out, p = [], 0
