@@ -257,6 +257,15 @@ sfxc_gpu_reader *sfxc_gpu_reader_create(const sfxc_reader_params *params, const 
  * valid block follows within the readers' search limits). */
 int sfxc_gpu_reader_next(sfxc_gpu_reader *reader, sfxc_reader_block *out);
 void sfxc_gpu_reader_destroy(sfxc_gpu_reader *reader);
+/* Channel_extractor_tasklet::do_task (sfxc/src/channel_extractor_tasklet.cc:120-220)
+ * for one reader block of word_bytes-byte words: the subbands' bytes as
+ * sfxc_gpu_extract_channels writes them (block->size / word_bytes words), and
+ * the block's invalid runs in bytes of each subband's output
+ * (begin * fan_out / (8 * word_bytes), length likewise) into out_invalid
+ * (2 * block->n_invalid ints). */
+int sfxc_gpu_extract_block(sfxc_gpu_ctx *ctx, const sfxc_reader_block *block, int32_t word_bytes, int32_t bits,
+                           int32_t n_subbands, int32_t fan_out, const int32_t *tracks, uint8_t *out,
+                           int32_t *out_invalid);
 
 #ifdef __cplusplus
 }

@@ -125,6 +125,7 @@ struct sfxc_gpu_ctx {
   // device
   DevBuf streamdev, tw256, window, twrot, ts, spec, acc, out, norms, flagfac, blmap, tiles, blpairs, items, bins,
       offsets, derr;
+  DevBuf xin, xtracks, xout;  // channel extraction
   int tw_rot_n = 0, window_n = 0, window_type = -1;
   std::vector<StreamDev> hsd;
 };
@@ -956,19 +957,34 @@ int sfxc_gpu_extract_channels(sfxc_gpu_ctx *c, const uint8_t *words, int64_t nwo
     if (nwords % spb) throw Error(SFXC_GPU_EINVAL, "word count must be a multiple of 8/fan_out");
     CK(cudaSetDevice(c->device));
     const int64_t nout = nwords / spb;
-    DevBuf din, dtr, dout;
-    upload(din, words, (size_t)(nwords * word_bytes), c->st);
-    upload(dtr, tracks, (size_t)n_subbands * fan_out * 4, c->st);
-    dout.ensure((size_t)(nout * n_subbands));
-    launch_extract(din.as<uint8_t>(), nout, word_bytes, bits, n_subbands, fan_out, dtr.as<int>(), dout.as<uint8_t>(),
-                   c->st);
+    upload(c->xin, words, (size_t)(nwords * word_bytes), c->st);
+    upload(c->xtracks, tracks, (size_t)n_subbands * fan_out * 4, c->st);
+    c->xout.ensure((size_t)(nout * n_subbands));
+    launch_extract(c->xin.as<uint8_t>(), nout, word_bytes, bits, n_subbands, fan_out, c->xtracks.as<int>(),
+                   c->xout.as<uint8_t>(), c->st);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(out, dout.p, (size_t)(nout * n_subbands), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(out, c->xout.p, (size_t)(nout * n_subbands), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     return SFXC_GPU_OK;
   } catch (const Error &e) {
     return fail(c, e);
   }
+}
+
+int sfxc_gpu_extract_block(sfxc_gpu_ctx *c, const sfxc_reader_block *block, int32_t word_bytes, int32_t bits,
+                           int32_t n_subbands, int32_t fan_out, const int32_t *tracks, uint8_t *out,
+                           int32_t *out_invalid) {
+  if (!c) return SFXC_GPU_EINVAL;
+  if (!block || !block->data || block->size <= 0 || word_bytes <= 0 || block->size % word_bytes ||
+      (block->n_invalid > 0 && (!block->invalid || !out_invalid)))
+    return fail(c, Error(SFXC_GPU_EINVAL, "bad reader block"));
+  const int rc = sfxc_gpu_extract_channels(c, block->data, block->size / word_bytes, word_bytes, bits, n_subbands,
+                                           fan_out, tracks, out);
+  if (rc != SFXC_GPU_OK) return rc;
+  // invalid byte runs of the input words, in bytes of each subband's output
+  // (channel_extractor_tasklet.cc:181-194)
+  for (int k = 0; k < 2 * block->n_invalid; k++) out_invalid[k] = block->invalid[k] * fan_out / (8 * word_bytes);
+  return SFXC_GPU_OK;
 }
 
 int sfxc_gpu_last_timings(const sfxc_gpu_ctx *c, float *ms6) {

@@ -165,6 +165,23 @@ class CorrelatorNode:
         return {"unpack_fringe_ms": t[0], "window_fft_ms": t[1], "xstep_ms": t[2], "normalise_ms": t[3],
                 "total_ms": t[4], "launches": int(t[5])}
 
+    def extract_block(self, block, word_bytes, bits, tracks):
+        """One reader block (read_recording's dict) through the channel
+        extractor: ([bytes per subband], invalid runs in subband bytes)."""
+        nsub, fan_out = len(tracks), len(tracks[0])
+        flat = (C.c_int32 * (nsub * fan_out))(*[t for tr in tracks for t in tr])
+        data = np.frombuffer(block["data"], dtype=np.uint8)
+        inv = (C.c_int32 * max(1, 2 * len(block["invalid"])))(*[v for r in block["invalid"] for v in r])
+        b = L.ReaderBlock(data.ctypes.data_as(C.POINTER(C.c_uint8)), data.size, block["channel"],
+                          block["start_ticks"], len(block["invalid"]), inv)
+        per = data.size // word_bytes * fan_out // 8
+        out = np.empty(nsub * per, dtype=np.uint8)
+        oinv = (C.c_int32 * max(1, 2 * len(block["invalid"])))()
+        self._check(self._lib.sfxc_gpu_extract_block(self._h, C.byref(b), word_bytes, bits, nsub, fan_out, flat,
+                                                     out.ctypes.data, oinv))
+        runs = [(oinv[2 * k], oinv[2 * k + 1]) for k in range(len(block["invalid"]))]
+        return [out[i * per:(i + 1) * per].tobytes() for i in range(nsub)], runs
+
     def extract_channels(self, words, word_bytes, bits, tracks):
         """Channel_extractor semantics on the GPU.  tracks: list per subband."""
         nsub, fan_out = len(tracks), len(tracks[0])

@@ -18,7 +18,7 @@ EXPORTS = [
     "sfxc_gpu_set_parameters", "sfxc_gpu_push_protocol", "sfxc_gpu_run_integration",
     "sfxc_gpu_copy_unpacked", "sfxc_gpu_copy_spectra", "sfxc_gpu_last_timings", "sfxc_gpu_delay_list",
     "sfxc_gpu_write_protocol", "sfxc_gpu_extract_channels", "sfxc_gpu_copy_spectra_noalloc",
-    "sfxc_gpu_reader_create", "sfxc_gpu_reader_next", "sfxc_gpu_reader_destroy",
+    "sfxc_gpu_reader_create", "sfxc_gpu_reader_next", "sfxc_gpu_reader_destroy", "sfxc_gpu_extract_block",
 ]
 FORMAT_VDIF, FORMAT_MARK5B = 0, 1
 
@@ -121,6 +121,8 @@ def load(path=None):
     lib.sfxc_gpu_reader_create.argtypes = [C.POINTER(ReaderParams), C.c_void_p, C.c_size_t]
     lib.sfxc_gpu_reader_next.argtypes = [C.c_void_p, C.POINTER(ReaderBlock)]
     lib.sfxc_gpu_reader_destroy.argtypes = [C.c_void_p]
+    lib.sfxc_gpu_extract_block.argtypes = [C.c_void_p, C.POINTER(ReaderBlock), C.c_int32, C.c_int32, C.c_int32,
+                                           C.c_int32, C.POINTER(C.c_int32), C.c_void_p, C.POINTER(C.c_int32)]
     _lib = lib
     return lib
 

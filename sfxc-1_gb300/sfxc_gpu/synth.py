@@ -368,14 +368,15 @@ def _bcd(value: int, digits: int) -> int:
 
 def mark5b_recording(nframes: int, *, mjd: int, sec_of_day: int, frames_per_second: int, seed: int = 0,
                      first_frame: int = 0, crc: str = "zero", bad_crc=(), bad_sync=(), garbage=None,
-                     fill_runs=(), no_subsec=False) -> bytes:
+                     fill_runs=(), no_subsec=False, payload_words=None) -> bytes:
     """Mark5B frames (16-byte header + 10000 bytes) with random payloads,
     frame numbers counting within each second from first_frame.  crc: "zero"
     (the field left 0, accepted without a check) or "valid" (the value that
     passes the check); bad_crc frames get a failing value, bad_sync frames a
     wrong sync word; garbage = {frame: nbytes} inserts random bytes before a
     frame; fill_runs = [(frame, first word, nwords)] writes the fill word into
-    payloads; no_subsec leaves the fractional-second field zero."""
+    payloads; no_subsec leaves the fractional-second field zero; payload_words
+    (uint32, 2500 per frame) replaces the random payloads."""
     rng = np.random.Generator(np.random.PCG64(seed))
     garbage = garbage or {}
     out = bytearray()
@@ -395,7 +396,10 @@ def mark5b_recording(nframes: int, *, mjd: int, sec_of_day: int, frames_per_seco
         if crc == "valid" or k in bad_crc:
             c = mk5b_valid_crc(bytes(h))
             h[12:14] = struct.pack("<H", c ^ 0x0101 if k in bad_crc else c)
-        payload = bytearray(rng.integers(0, 256, MK5B_FRAME_BYTES, dtype=np.uint8).tobytes())
+        if payload_words is not None:
+            payload = bytearray(np.asarray(payload_words[k * 2500:(k + 1) * 2500], dtype="<u4").tobytes())
+        else:
+            payload = bytearray(rng.integers(0, 256, MK5B_FRAME_BYTES, dtype=np.uint8).tobytes())
         for (f, w0, nw) in fill_runs:
             if f == k:
                 payload[4 * w0:4 * (w0 + nw)] = struct.pack("<I", VDIF_FILL_WORD) * nw

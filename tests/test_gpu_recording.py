@@ -1,0 +1,95 @@
+"""The input-node front end on station recordings: VDIF (16 channels x 2 bits
+per 32-bit word, one thread) and Mark5B (32 bitstreams) recordings of a job's
+stations go through the reader, the channel extractor (GPU) and the
+input-node writer.  The channel blocks, the protocol bytes and the correlator
+output must equal those of the same job built from the channel streams
+directly (Input_data_format_reader_tasklet -> Channel_extractor_tasklet ->
+Input_node_data_writer, sfxc/src/input_data_format_reader_tasklet.cc:93-160,
+sfxc/src/channel_extractor_tasklet.cc:120-220,
+sfxc/src/input_node_data_writer.cc:107-229).  A VDIF frame marked invalid
+becomes the same invalid run in both paths."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TRACKS16 = [[2 * c + 1, 2 * c] for c in range(16)]
+
+
+def _job_and_streams(invalid):
+    from sfxc_gpu import correlator, scenario
+    st = scenario.cubic_stations(3, seed=91, max_delay=4e-3, max_rate=1e-6)
+    sc = scenario.Scenario(stations=st, pols=("R", "L"), sample_rate=32_000_000, bandwidth=16_000_000, bits=2,
+                           channel_freq=1_600_000_000, nchan=512, integration_us=31250, n_integrations=1,
+                           sub_integration_us=31250, lead_us=8000, seed=21, block_bytes=invalid["block_bytes"],
+                           invalid=invalid["runs"](st))
+    job = scenario.build_job(sc, correlator.delay_list, correlator.write_protocol, fast_random=True)
+    chans, nsamp = scenario.channel_streams(sc, fast_random=True)
+    return sc, job, chans, nsamp
+
+
+def _words(chans, si, nsamp, seed):
+    """16-channel words of station si: channels 0/1 its R/L streams, the rest noise."""
+    from sfxc_gpu import synth
+    rng = np.random.Generator(np.random.PCG64(seed))
+    codes = [synth.unpack_codes(chans[(si, "R")], 2), synth.unpack_codes(chans[(si, "L")], 2)]
+    codes += [rng.integers(0, 4, nsamp, dtype=np.uint8) for _ in range(14)]
+    return synth.vdif_words_from_codes(codes, 2)
+
+
+def _protocols_from_recordings(gpu_node, sc, recs, fmt, reader_params):
+    from sfxc_gpu import correlator, scenario, timebase
+    dels = scenario.del_tables(sc)
+    rec0, start, tint, slice_samples = scenario.job_timing(sc)
+    protos = []
+    for si in range(len(sc.stations)):
+        blocks = correlator.read_recording(recs[si], fmt, ref_ticks=timebase.ticks_from_mjd_sec(sc.mjd, 0.0),
+                                           channel_tracks=TRACKS16, **reader_params)
+        per_pol = {"R": [], "L": []}
+        for b in blocks:
+            (r, l), inv = gpu_node.extract_block(b, 4, 2, [TRACKS16[0], TRACKS16[1]])
+            per_pol["R"].append((b["start_ticks"], r, inv))
+            per_pol["L"].append((b["start_ticks"], l, inv))
+        slices = [(start, start + tint, slice_samples, correlator.delay_list(dels[si], start, start + tint,
+                                                                              sc.sample_rate, sc.bits))]
+        for pol in sc.pols:
+            # the direct path's blocks, for the block-level comparison
+            direct = scenario.blocks_of(sc, scenario.channel_streams(sc, fast_random=True)[0][(si, pol)], (si, pol))
+            got = per_pol[pol][:len(direct)]
+            assert [(t, d, list(map(tuple, inv))) for t, d, inv in got] == \
+                [(t, d, list(map(tuple, inv))) for t, d, inv in direct], (si, pol)
+            protos.append(correlator.write_protocol(per_pol[pol], slices, sc.sample_rate, sc.bits,
+                                                    sc.integration_us))
+    return protos
+
+
+def test_vdif_recording_path(gpu_node):
+    from sfxc_gpu import synth
+    # frame 5 of station 1 invalid: block 1 (frames 4-7), frame 1 of it ->
+    # channel bytes [500, 1000) of that block
+    sc, job, chans, nsamp = _job_and_streams(dict(
+        block_bytes=2000, runs=lambda st: {(st[1].number, "R"): [(1, 500, 500)], (st[1].number, "L"): [(1, 500, 500)]}))
+    recs = [synth.vdif_file_bytes(_words(chans, si, nsamp, 300 + si), payload_bytes=8000, sample_rate=sc.sample_rate,
+                                  nchan=16, bits=2, start_mjd=sc.mjd, start_sec_of_day=sc.sec0,
+                                  invalid_frames=(5,) if si == 1 else ())
+            for si in range(len(sc.stations))]
+    protos = _protocols_from_recordings(gpu_node, sc, recs, "vdif",
+                                        dict(track_bit_rate=sc.sample_rate, frame_size=8000, n_tracks=32, bits=2))
+    assert protos == job["protocols"]
+    cor_direct, tsys_direct = gpu_node.correlate(job)
+    cor_rec, tsys_rec = gpu_node.correlate(dict(job, protocols=protos))
+    assert cor_rec == cor_direct and tsys_rec == tsys_direct
+
+
+def test_mark5b_recording_path(gpu_node):
+    from sfxc_gpu import synth
+    sc, job, chans, nsamp = _job_and_streams(dict(block_bytes=5000, runs=lambda st: {}))
+    fps = sc.sample_rate * 32 // 80000  # one sample of every channel per 32-bit word
+    recs = []
+    for si in range(len(sc.stations)):
+        w = _words(chans, si, nsamp, 400 + si)
+        recs.append(synth.mark5b_recording(w.size // 2500, mjd=sc.mjd, sec_of_day=sc.sec0, frames_per_second=fps,
+                                           crc="valid", payload_words=w))
+    protos = _protocols_from_recordings(gpu_node, sc, recs, "mark5b",
+                                        dict(track_bit_rate=sc.sample_rate, n_tracks=32, bits=2))
+    assert protos == job["protocols"]
