@@ -123,10 +123,16 @@ struct sfxc_gpu_ctx {
   JobTables jt;
   int M = 0, K = 0, Nd = 0, kpad = 0, nffts = 0, nsub = 0, nbins = 1;
   // device
-  DevBuf streamdev, tw256, window, twrot, ts, spec, acc, out, norms, flagfac, blmap, tiles, blpairs, items, bins,
+  DevBuf streamdev, tw256, ts, spec, acc, out, norms, flagfac, blmap, tiles, blpairs, items, bins,
       offsets, derr;
   DevBuf xin, xtracks, xout;  // channel extraction
-  int tw_rot_n = 0, window_n = 0, window_type = -1;
+  // per windowed-FFT length (streams of different sample rates): window and
+  // twiddle tables, and the stream descriptors grouped by length
+  struct RotTables {
+    DevBuf window, twrot;
+  };
+  std::map<int, RotTables> rot_tables;
+  DevBuf streamdev_grouped;
   std::vector<StreamDev> hsd;
 };
 
@@ -248,8 +254,8 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
     s.rot = (int)(((uint64_t)2 * c->M * (uint64_t)ss.sample_rate) / p->sample_rate);
     s.hop = s.rot / 2;
     if (s.rot & (s.rot - 1)) throw Error(SFXC_GPU_EINVAL, "FFT length per stream must be a power of two");
-    if (s.rot > 32768) throw Error(SFXC_GPU_EINVAL, "FFT lengths above 32768 samples are not supported");
-    if (s.rot != 2 * c->M) throw Error(SFXC_GPU_EINVAL, "mixed sample rates within a job are not supported yet");
+    if (s.rot > 32768 || s.rot < 512)
+      throw Error(SFXC_GPU_EINVAL, "windowed FFT lengths must lie within 512..32768 samples");
   }
   c->bl = create_baselines(c->streams, p->reference_station);
   // stream-pair tiles of the X-step and the map pair -> baseline
@@ -289,13 +295,17 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
   twiddles(tw, 256);
   twiddles(tw, 128);
   upload(c->tw256, tw.data(), tw.size() * sizeof(float2), c->st);
-  const int rot = c->sc[0].rot;
-  std::vector<float2> twr;
-  twiddles(twr, rot);
-  twiddles(twr, rot / 2);
-  upload(c->twrot, twr.data(), twr.size() * sizeof(float2), c->st);
-  std::vector<float> win = make_window(p->window, rot);
-  upload(c->window, win.data(), win.size() * 4, c->st);
+  std::set<int> rots;
+  for (const StreamCtx &s : c->sc) rots.insert(s.rot);
+  for (int rot : rots) {  // one window and twiddle table per FFT length
+    sfxc_gpu_ctx::RotTables &t = c->rot_tables[rot];
+    std::vector<float2> twr;
+    twiddles(twr, rot);
+    twiddles(twr, rot / 2);
+    upload(t.twrot, twr.data(), twr.size() * sizeof(float2), c->st);
+    std::vector<float> win = make_window(p->window, rot);
+    upload(t.window, win.data(), win.size() * 4, c->st);
+  }
   CK(cudaStreamSynchronize(c->st));
   c->current_integration = 0;
   c->have_job = true;
@@ -449,6 +459,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     double sp0 = ss.lo_offset * (dt - std::trunc(dt)) + (ss.lo_offset - std::trunc(ss.lo_offset)) * std::trunc(dt);
     d.start_phase = sp0 - std::floor(sp0);
     d.rot = s.rot;
+    d.slot = i;
     d.flip = c->p.sideband != ss.sideband;
     int64_t delta, freq = ss.channel_freq;  // delay_correction.cc:226-241
     if (c->p.sideband != ss.sideband) freq += (int64_t)d.sideband * ss.bandwidth;
@@ -515,7 +526,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     max_rows = c->nffts;
   }
   int max_blocks = 0;
-  for (int i = 0; i < N; i++) max_blocks = std::max(max_blocks, chunked ? (max_rows + 2) * hop / kNd : c->sc[i].n_blocks);
+  for (int i = 0; i < N; i++)  // each stream's own hop: streams at other rates need more or fewer blocks
+    max_blocks = std::max(max_blocks, chunked ? (max_rows + 2) * c->sc[i].hop / kNd : c->sc[i].n_blocks);
   c->ts.ensure((size_t)N * max_blocks * kNd * sizeof(float));
   // tensor-core X-step for normal correlation of up to 32 inputs; the spectra
   // are scaled by a power of two before the FP16 hi/lo split so that typical
@@ -598,14 +610,29 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       d.n_blocks = b1 - b0;
     }
     upload(c->streamdev, c->hsd.data(), c->hsd.size() * sizeof(StreamDev), st);
+    // the same descriptors grouped by windowed-FFT length (job order within a group)
+    std::vector<StreamDev> grouped;
+    std::vector<std::pair<int, int>> groups;  // (rot, first index in `grouped`)
+    for (auto &rt : c->rot_tables) {
+      const size_t first = grouped.size();
+      for (int i = 0; i < N; i++)
+        if (c->sc[i].rot == rt.first) grouped.push_back(c->hsd[i]);
+      if (grouped.size() > first) groups.push_back({rt.first, (int)first});
+    }
+    upload(c->streamdev_grouped, grouped.data(), grouped.size() * sizeof(StreamDev), st);
     CK(cudaEventRecord(c->evpool[ev], st));
     launch_fstep_block(c->streamdev.as<StreamDev>(), N, max_blocks, c->tw256.as<float2>(), st);
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->evpool[ev + 1], st));
-    const int nper = c->p.window == WINDOW_NONE ? c->sc[0].hop : c->sc[0].rot;
-    launch_window_fft(c->streamdev.as<StreamDev>(), N, 0, nrows, max_rows, c->window.as<float>(),
-                      c->twrot.as<float2>(), c->sc[0].rot, nper, M, kpad, c->spec.p, tc_x, tc_scale, st);
-    CK(cudaGetLastError());
+    for (size_t g = 0; g < groups.size(); g++) {
+      const int rot = groups[g].first, first = groups[g].second;
+      const int count = (g + 1 < groups.size() ? groups[g + 1].second : (int)grouped.size()) - first;
+      const int nper = c->p.window == WINDOW_NONE ? rot / 2 : rot;
+      const sfxc_gpu_ctx::RotTables &t = c->rot_tables.at(rot);
+      launch_window_fft(c->streamdev_grouped.as<StreamDev>() + first, count, 0, nrows, max_rows, t.window.as<float>(),
+                        t.twrot.as<float2>(), rot, nper, M, kpad, c->spec.p, tc_x, tc_scale, st);
+      CK(cudaGetLastError());
+    }
     CK(cudaEventRecord(c->evpool[ev + 2], st));
     if (tc_x) {
       CK(launch_xcorr_tc(c->spec.p, nrows, kpad, K, c->blmap.as<int>(), c->jt.npad, 1.0f / (tc_scale * tc_scale),
@@ -832,6 +859,7 @@ int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n)
     StreamDev d = c->hsd[stream];
     d.block0 = 0;
     d.n_blocks = s.n_blocks;
+    d.slot = 0;  // the only stream of this launch
     DevBuf ts, spec, sd, bp, ba;
     ts.ensure((size_t)s.n_blocks * kNd * sizeof(float));
     spec.ensure(rows * c->kpad * sizeof(float2));
@@ -843,7 +871,8 @@ int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n)
     upload(sd, &d, sizeof(StreamDev), c->st);
     launch_fstep_block(sd.as<StreamDev>(), 1, s.n_blocks, c->tw256.as<float2>(), c->st);
     const int nper = c->p.window == WINDOW_NONE ? s.hop : s.rot;
-    launch_window_fft(sd.as<StreamDev>(), 1, 0, (int)rows, (int)rows, c->window.as<float>(), c->twrot.as<float2>(),
+    const sfxc_gpu_ctx::RotTables &t = c->rot_tables.at(s.rot);
+    launch_window_fft(sd.as<StreamDev>(), 1, 0, (int)rows, (int)rows, t.window.as<float>(), t.twrot.as<float2>(),
                       s.rot, nper, c->M, c->kpad, spec.p, false, 1.0f, c->st);
     CK(cudaGetLastError());
     CK(cudaMemcpy2DAsync(out, K * sizeof(float2), spec.p, c->kpad * sizeof(float2), K * sizeof(float2), rows,
@@ -921,6 +950,7 @@ int sfxc_gpu_copy_spectra_noalloc(sfxc_gpu_ctx *c, int32_t stream, float *out, s
     StreamDev d = c->hsd[stream];
     d.block0 = 0;
     d.n_blocks = s.n_blocks;
+    d.slot = 0;  // the only stream of this launch
     d.ts = reinterpret_cast<float *>(base + kNoallocTsOff);
     d.bparams = reinterpret_cast<float4 *>(base + kNoallocParOff);
     d.bamp = reinterpret_cast<float *>(base + kNoallocAmpOff);
@@ -931,7 +961,8 @@ int sfxc_gpu_copy_spectra_noalloc(sfxc_gpu_ctx *c, int32_t stream, float *out, s
     CK(cudaMemcpyAsync(dd, &d, sizeof(StreamDev), cudaMemcpyHostToDevice, c->st));
     launch_fstep_block(dd, 1, s.n_blocks, c->tw256.as<float2>(), c->st);
     const int nper = c->p.window == WINDOW_NONE ? s.hop : s.rot;
-    launch_window_fft(dd, 1, 0, (int)rows, (int)rows, c->window.as<float>(), c->twrot.as<float2>(), s.rot, nper, c->M,
+    const sfxc_gpu_ctx::RotTables &t = c->rot_tables.at(s.rot);
+    launch_window_fft(dd, 1, 0, (int)rows, (int)rows, t.window.as<float>(), t.twrot.as<float2>(), s.rot, nper, c->M,
                       c->kpad, spec, false, 1.0f, c->st);
     CK(cudaGetLastError());
     CK(cudaMemcpy2DAsync(out, K * sizeof(float2), spec, c->kpad * sizeof(float2), K * sizeof(float2), rows,

@@ -45,8 +45,9 @@ struct StreamDev {
   // channel setup (Delay_correction::set_parameters)
   int32_t sample_rate, bandwidth, oversamp, sideband;  // sideband +1 / -1
   double center_freq, lo_offset, start_phase;
-  // windowed FFT stage
-  int32_t rot, flip, output_offset, temp_fft_offset;
+  // windowed FFT stage; slot: the stream's index in the job (its place in
+  // the spectra layouts), also when the launch covers a subset of streams
+  int32_t rot, flip, output_offset, temp_fft_offset, slot;
   // delay-model shortcuts, exact: an all-zero phase column evaluates to 0.0,
   // an all-one amplitude column to 1.0, a zero clock model to a zero drift
   int32_t phase_zero, amp_one, no_clock;

@@ -327,8 +327,9 @@ __device__ __forceinline__ void window_load(float2 (&v)[16], int t, bool ok, int
   }
 }
 
-// Output row `row` of the NS streams sg0 + j (j < NS) whose transforms are at
-// Z + j * BUF; threads tid = 0..nthr-1 share the channels 0..M.
+// Output row `row` of the NS streams sg0 + j (j < NS) of the launch, whose
+// transforms are at Z + j * BUF; each goes to its slot in the spectra layout.
+// Threads tid = 0..nthr-1 share the channels 0..M.
 template <int N, int NS, int OUT_TC>
 __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const StreamDev *__restrict__ streams,
                                           int nstreams, int sg0, int row, int nrows_total, int M, int kpad,
@@ -349,15 +350,29 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const Stream
     };
 #pragma unroll 1
     for (int j0 = 0; j0 < NS && sg0 + j0 < nstreams; j0 += W) {
-      int shift[W];
+      int shift[W], slot[W];
       bool aligned = M == N;  // every stream's channel i is its bin i
+      bool packed = sg0 + j0 + W <= nstreams;  // W real streams in consecutive, aligned slots
 #pragma unroll
       for (int j = 0; j < W; j++) {
         const int st = min(sg0 + j0 + j, nstreams - 1);
         shift[j] = streams[st].output_offset - streams[st].temp_fft_offset;
+        slot[j] = streams[st].slot;
         aligned = aligned && shift[j] == 0;
+        packed = packed && slot[j] == slot[0] + j;
       }
-      uint2 *dst = reinterpret_cast<uint2 *>(spec_out) + (int64_t)row * kpad * kTcSlots + sg0 + j0;
+      packed = packed && slot[0] % W == 0;
+      uint2 *dst = reinterpret_cast<uint2 *>(spec_out) + (int64_t)row * kpad * kTcSlots;
+      if (!packed) {  // streams of a subset launch: one 8-byte store per stream
+        for (int i = tid; i <= M; i += nthr)
+#pragma unroll
+          for (int j = 0; j < W; j++)
+            if (sg0 + j0 + j < nstreams)
+              dst[(int64_t)i * kTcSlots + slot[j]] =
+                  tc_split(real_bin<N>(Z + (j0 + j) * BUF, tw_rot, shift[j] + i), tc_scale);
+        continue;
+      }
+      dst += slot[0];
       if (aligned) {
         for (int i = tid; i <= N / 2; i += nthr) {
           const float2 w = __ldg(tw_rot + i);
@@ -386,7 +401,7 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const Stream
     for (int j = 0; j < NS && sg0 + j < nstreams; j++) {
       const int st = sg0 + j;
       const int shift = streams[st].output_offset - streams[st].temp_fft_offset;
-      float2 *dst = reinterpret_cast<float2 *>(spec_out) + ((int64_t)st * nrows_total + row) * kpad;
+      float2 *dst = reinterpret_cast<float2 *>(spec_out) + ((int64_t)streams[st].slot * nrows_total + row) * kpad;
       if (shift == 0 && M == N) {
         for (int i = tid; i <= N / 2; i += nthr) {
           float2 xq, xnq;

@@ -57,6 +57,10 @@ class Scenario:
     tsys_freq: int = 80
     reference_station: int = -1
     frequency_nr: int = 0
+    # station number -> (sample rate, bits, start of the station's band minus
+    # the job's channel frequency in Hz); stations not listed record the
+    # job's band at the job's rate (build_job_bulk only)
+    station_modes: dict = field(default_factory=dict)
 
     def streams(self):
         """(station index, pol) in correlator order: stations outer, pols inner."""
@@ -159,25 +163,28 @@ def build_job_bulk(sc: Scenario, alloc=None):
     dels = del_tables(sc)
     rec0, start, tint, slice_samples = job_timing(sc)
     sr, bits = sc.sample_rate, sc.bits
-    tps = timebase.ticks_per_sample(sr)
-    spb_block = sc.block_bytes * 8 // bits
     max_tau = max(abs(float(st.poly.delay(sc.sec0 + sc.lead_us * 1e-6))) for st in sc.stations)
-    span = sc.lead_us * sr // 1_000_000 + sc.n_integrations * (sc.integration_us * sr // 1_000_000)
-    nsamp = span + int(max_tau * sr) + 4 * spb_block
-    nblocks = (nsamp + spb_block - 1) // spb_block
-    starts = rec0 + np.arange(nblocks, dtype=np.int64) * spb_block * tps
     streams, protos = [], []
     for k, (si, pol) in enumerate(sc.streams()):
         st = sc.stations[si]
+        sr_k, bits_k, off_k = sc.station_modes.get(st.number, (sr, bits, 0))
+        bw_k = sc.bandwidth * sr_k // sr
+        tps = timebase.ticks_per_sample(sr_k)
+        spb_block = sc.block_bytes * 8 // bits_k
+        span = sc.lead_us * sr_k // 1_000_000 + sc.n_integrations * (sc.integration_us * sr_k // 1_000_000)
+        nsamp = span + int(max_tau * sr_k) + 4 * spb_block
+        nblocks = (nsamp + spb_block - 1) // spb_block
+        starts = rec0 + np.arange(nblocks, dtype=np.int64) * spb_block * tps
         rng = np.random.Generator(np.random.PCG64(sc.seed * 7919 + k))
         data = rng.integers(0, 256, size=nblocks * sc.block_bytes, dtype=np.uint8)
         slices = []
         for it in range(sc.n_integrations):
             s0 = start + it * tint
-            slices.append((s0, s0 + tint, slice_samples, correlator.delay_list(dels[si], s0, s0 + tint, sr, bits)))
-        protos.append(correlator.write_protocol_stream(data, sc.block_bytes, starts, slices, sr, bits,
+            slices.append((s0, s0 + tint, slice_samples * sr_k // sr,
+                           correlator.delay_list(dels[si], s0, s0 + tint, sr_k, bits_k)))
+        protos.append(correlator.write_protocol_stream(data, sc.block_bytes, starts, slices, sr_k, bits_k,
                                                        sc.integration_us, alloc=alloc))
-        streams.append((st.number, k, sr, sc.channel_freq, sc.bandwidth, sc.sideband, pol, bits, sc.lo_offset,
+        streams.append((st.number, k, sr_k, sc.channel_freq + off_k, bw_k, sc.sideband, pol, bits_k, sc.lo_offset,
                         sc.tsys_freq, si))
     return dict(del_bytes=dels, experiment_start_ticks=rec0, start_ticks=start,
                 integration_time_us=sc.integration_us, sub_integration_time_us=sc.sub_integration_us,
