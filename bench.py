@@ -44,7 +44,9 @@ METRIC = "input Gsamples/s per GB300, TC-FP16 vs FP32 X-step at <=1e-4 vis err v
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
-def workload(args):
+def workload(args, rank=0):
+    """The 8 subband jobs of one timeslice; rank r correlates timeslice r (the
+    jobs of different ranks are independent, as the manager deals them)."""
     from sfxc_gpu import scenario
     st = scenario.cubic_stations(args.stations, seed=4242, max_delay=15e-3, max_rate=3e-6)
     subs = []
@@ -52,8 +54,8 @@ def workload(args):
         subs.append(scenario.Scenario(
             stations=st, pols=("R", "L"), sample_rate=64_000_000, bandwidth=32_000_000, bits=2,
             channel_freq=4_800_000_000 + sb * 32_000_000, nchan=args.nchan, integration_us=args.integration_us,
-            n_integrations=1, sub_integration_us=125000, lead_us=16000, seed=100 + sb, block_bytes=2000,
-            frequency_nr=sb))
+            n_integrations=1, sub_integration_us=125000, lead_us=16000 + rank * args.integration_us,
+            seed=100 + sb + 1000 * rank, block_bytes=2000, frequency_nr=sb))
     return subs
 
 
@@ -149,7 +151,7 @@ def run_gpu(args):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     log = (lambda m: print(m, file=sys.stderr, flush=True)) if rank == 0 else (lambda m: None)
-    subs = workload(args)
+    subs = workload(args, rank)
     total = samples_per_step(subs)
     jobs = build_inputs(subs, log)
     mode = lib.X_TC_HILO if args.x == "tc" else lib.X_FP32
@@ -231,10 +233,8 @@ def run_gpu(args):
     clk = clocks.stop()
     pool.shutdown()
     if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([wall, dev_total], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        wall, dev_total = float(tt[0]), float(tt[1])
+        from sfxc_gpu import sharding
+        wall, dev_total = sharding.max_over_ranks([wall, dev_total])
     if rank != 0:
         return
     value = total * args.steps * world / (dev_total / 1e3) / 1e9
