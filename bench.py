@@ -281,9 +281,18 @@ def roofline(args, per_kernel, total):
     k = max(per_sample, key=lambda n: per_kernel.get(n, 0.0))
     t = per_kernel[k] / args.steps / 1e3
     achieved = per_sample[k] * total / t / 1e9
+    # DRAM bytes per input sample (dram__bytes_read + dram__bytes_write) that
+    # ncu measured for the tensor-core path's kernels on the one-subband,
+    # 4096-channel case; a launch covers one sub-integration chunk of one
+    # subband job, so the per-launch traffic scales with the samples it covers
+    measured = {"window_fft_ms": 11.59, "xstep_ms": 8.27, "unpack_fringe_ms": 3.93}
+    traffic = None
+    if args.x == "tc" and M == 4096 and k in measured:
+        launches = args.subbands * -(-args.integration_us // 125000)
+        traffic = round(measured[k] * total / launches / 1e9, 3)
     return {"kernel": k.replace("_ms", ""), "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None, "peak_source": src,
-            "algorithmic_bytes_per_sample": round(per_sample[k], 4)}
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic, "traffic_unit": "GB per launch",
+            "peak_source": src, "algorithmic_bytes_per_sample": round(per_sample[k], 4)}
 
 
 def cpu_baseline(args, quick):
