@@ -306,24 +306,35 @@ __device__ __forceinline__ void real_bin_pair(const float2 *Z, float2 w, int q, 
   xnq = make_float2(er - owr, owi - ei);
 }
 
-// First-pass inputs v[qq] = complex element t + qq T of the windowed row:
-// samples i = 2 e, 2 e + 1 from sample(i) (a float2), times the window, odd
-// samples negated for a sideband flip, zero from nper on.
-template <int T, class Sample>
-__device__ __forceinline__ void window_load(float2 (&v)[16], int t, bool ok, int nper, float sgn,
-                                            const float *__restrict__ window, Sample sample) {
+// First-pass inputs, in two steps so that the loads of the next row can be in
+// flight while the current row is written out: raw samples v[qq] = (x[2e],
+// x[2e+1]) of complex element e = t + qq T (zero from nper on, or when !ok),
+// then the window and, for a sideband flip, the negated odd samples.
+template <int T>
+__device__ __forceinline__ void window_raw(float2 (&v)[16], int t, bool ok, int nper, const float *ts) {
 #pragma unroll
   for (int qq = 0; qq < 16; qq++) {
     const int i = 2 * (t + qq * T);
     float2 x = make_float2(0.f, 0.f);
-    if (ok && i + 1 < nper) {
-      const float2 a = sample(i);
-      const float2 w = __ldg(reinterpret_cast<const float2 *>(window + i));
-      x = make_float2(a.x * w.x, sgn * (a.y * w.y));
-    } else if (ok && i < nper) {
-      x.x = sample(i).x * window[i];
-    }
+    if (ok && i + 1 < nper)
+      x = *reinterpret_cast<const float2 *>(ts + i);
+    else if (ok && i < nper)
+      x.x = ts[i];
     v[qq] = x;
+  }
+}
+template <int T>
+__device__ __forceinline__ void window_apply(float2 (&v)[16], int t, int nper, float sgn,
+                                             const float *__restrict__ window) {
+#pragma unroll
+  for (int qq = 0; qq < 16; qq++) {
+    const int i = 2 * (t + qq * T);
+    if (i + 1 < nper) {
+      const float2 w = __ldg(reinterpret_cast<const float2 *>(window + i));
+      v[qq] = make_float2(v[qq].x * w.x, sgn * (v[qq].y * w.y));
+    } else if (i < nper) {
+      v[qq] = make_float2(v[qq].x * __ldg(window + i), 0.f);
+    }
   }
 }
 
@@ -417,12 +428,15 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const Stream
 }
 
 // Stage 2 as its own kernel, reading the fringe-stopped samples from s.ts:
-// a CTA of SPC x RPC groups of T threads, SPC streams x RPC rows.
+// a CTA of SPC x RPC groups of T threads transforms SPC streams x RPC rows per
+// step and steps through a run of rows; the next step's samples are loaded
+// into the FFT registers before the current step is written out, so those
+// HBM loads overlap the output stores.
 template <int LOGN>
 struct WinShape {
   static constexpr int N = 1 << LOGN, T = N / 16;
   static constexpr int SPC = T <= 256 ? 4 : 1024 / T;  // streams per CTA
-  static constexpr int RPC = T < 256 ? 256 / T : 1;  // rows per CTA
+  static constexpr int RPC = T < 256 ? 256 / T : 1;    // rows per step
   static constexpr int THREADS = SPC * RPC * T;
   static constexpr int BUF = N + N / 16;  // padded FFT buffer (float2) of one group
   static constexpr size_t SMEM = (size_t)SPC * RPC * BUF * sizeof(float2);
@@ -431,7 +445,7 @@ struct WinShape {
 
 template <int LOGN, int OUT_TC>
 __global__ void __launch_bounds__(1024, 1) window_fft_kernel(
-    const StreamDev *__restrict__ streams, int nstreams, int row0, int nrows, int nrows_total,
+    const StreamDev *__restrict__ streams, int nstreams, int row0, int nrows, int nrows_total, int steps_per_cta,
     const float *__restrict__ window, const float2 *__restrict__ tw_rot, int nper, int M, int kpad,
     void *__restrict__ spec_out, float tc_scale) {
   using S = WinShape<LOGN>;
@@ -439,22 +453,31 @@ __global__ void __launch_bounds__(1024, 1) window_fft_kernel(
   extern __shared__ float2 dsm[];
   const int t = threadIdx.x % T, g = threadIdx.x / T;
   const int nsg = (nstreams + SPC - 1) / SPC;
-  const int sg = blockIdx.x % nsg, rg = blockIdx.x / nsg;  // stream group fastest
-  const int stream = sg * SPC + g % SPC, rr = rg * RPC + g / SPC;
-  const bool ok = stream < nstreams && rr < nrows;
-  const StreamDev &s = streams[ok ? stream : 0];
-  const float *ts = s.ts + (int64_t)(row0 + rr) * N;  // hop = rot / 2
+  const int sg = blockIdx.x % nsg;  // stream group fastest
+  const int nsteps = (nrows + RPC - 1) / RPC;
+  const int k0 = (blockIdx.x / nsg) * steps_per_cta, k1 = min(nsteps, k0 + steps_per_cta);
+  const int stream = sg * SPC + g % SPC;
+  const bool sok = stream < nstreams;
+  const StreamDev &s = streams[sok ? stream : 0];
+  const float sgn = s.flip ? -1.0f : 1.0f;
+  auto row_of = [&](int k) { return k * RPC + g / SPC; };
   float2 v[16];
-  window_load<T>(v, t, ok, nper, s.flip ? -1.0f : 1.0f, window,
-                 [ts](int i) { return *reinterpret_cast<const float2 *>(ts + i); });
-  // tw_rot holds exp(-2 pi i m / rot) for m < rot, followed by exp(-2 pi i m / N) for m < N.
-  fft_reg<-1, LOGN, true>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, BlockSync());
+  if (k0 < k1) window_raw<T>(v, t, sok && row_of(k0) < nrows, nper, s.ts + (int64_t)(row0 + row_of(k0)) * N);
 #pragma unroll 1
-  for (int r = 0; r < RPC; r++) {
-    const int row = rg * RPC + r;
-    if (row >= nrows) break;
-    store_row<N, SPC, OUT_TC>(dsm + r * SPC * S::BUF, S::BUF, streams, nstreams, sg * SPC, row0 + row, nrows_total,
-                              M, kpad, tw_rot, spec_out, tc_scale, threadIdx.x, S::THREADS);
+  for (int k = k0; k < k1; k++) {
+    window_apply<T>(v, t, nper, sgn, window);
+    // tw_rot holds exp(-2 pi i m / rot) for m < rot, followed by exp(-2 pi i m / N) for m < N.
+    fft_reg<-1, LOGN, true>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, BlockSync());
+    if (k + 1 < k1)  // hop = rot / 2
+      window_raw<T>(v, t, sok && row_of(k + 1) < nrows, nper, s.ts + (int64_t)(row0 + row_of(k + 1)) * N);
+#pragma unroll 1
+    for (int r = 0; r < RPC; r++) {
+      const int row = k * RPC + r;
+      if (row >= nrows) break;
+      store_row<N, SPC, OUT_TC>(dsm + r * SPC * S::BUF, S::BUF, streams, nstreams, sg * SPC, row0 + row,
+                                nrows_total, M, kpad, tw_rot, spec_out, tc_scale, threadIdx.x, S::THREADS);
+    }
+    __syncthreads();  // the next step's FFT rewrites the buffers
   }
 }
 
@@ -744,11 +767,15 @@ static void window_fft_launch(const StreamDev *d_streams, int nstreams, int row0
                               const float *window, const float2 *tw_rot, int nper, int M, int kpad, void *spec,
                               float tc_scale, cudaStream_t st) {
   using S = WinShape<LOGN>;
-  const unsigned grid = (unsigned)((nrows + S::RPC - 1) / S::RPC) * (unsigned)((nstreams + S::SPC - 1) / S::SPC);
+  const int nsg = (nstreams + S::SPC - 1) / S::SPC, nsteps = (nrows + S::RPC - 1) / S::RPC;
+  // one CTA per SM: runs of steps so that the CTAs fill two waves
+  const int runs = std::max(1, std::min(nsteps, 2 * sm_count() / nsg));
+  const int steps_per_cta = (nsteps + runs - 1) / runs;
+  const unsigned grid = (unsigned)(nsg * ((nsteps + steps_per_cta - 1) / steps_per_cta));
   auto kern = window_fft_kernel<LOGN, OUT_TC>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
-  kern<<<grid, S::THREADS, S::SMEM, st>>>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad,
-                                          spec, tc_scale);
+  kern<<<grid, S::THREADS, S::SMEM, st>>>(d_streams, nstreams, row0, nrows, nrows_total, steps_per_cta, window, tw_rot,
+                                          nper, M, kpad, spec, tc_scale);
 }
 
 #define SFXC_LOGN_SWITCH(logn, CALL) \
