@@ -477,7 +477,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     d.no_clock = s.sp.clock_offset == 0.0 && s.sp.clock_rate == 0.0;
     for (int r = 0; r < (int)s.plan.stats.size(); r++) {
       const StatRange &sr = s.plan.stats[r];
-      for (int off = 0; off < sr.n; off += 4096) items.push_back(make_int4(i, r, off, std::min(4096, sr.n - off)));
+      for (int off = 0; off < sr.n; off += 65536) items.push_back(make_int4(i, r, off, std::min(65536, sr.n - off)));
     }
     s.pushed = false;
   }

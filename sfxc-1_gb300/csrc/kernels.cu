@@ -32,6 +32,17 @@ namespace sfxc {
 // exp(-i (c + k l)) on k <= 128, upper half zero, inverse 256-point FFT,
 // fringe rotation of the real part.  tw holds exp(-2 pi i m / 256), m < 256.
 //
+// Samples n of the pair's two blocks written as xs[n] and xs[256 + n] by this
+// half warp -> v[r] = (x_b[t + 16 r], x_b+1[t + 16 r]).  Only the half warp
+// synchronises (the other may be on another path).
+__device__ __forceinline__ void pair_from_scratch(float2 (&v)[16], const float *xs, int t) {
+  const unsigned half = (threadIdx.x & 16) ? 0xFFFF0000u : 0x0000FFFFu;
+  __syncwarp(half);
+#pragma unroll
+  for (int r = 0; r < 16; r++) v[r] = make_float2(xs[t + 16 * r], xs[kNd + t + 16 * r]);
+  __syncwarp(half);  // the FFT's first pass writes the scratch
+}
+
 // Pair (bl0, bl0 + 1) of a stream's blocks (indices from the stream's block0)
 // by the 16 threads t = 0..15 of a half warp, with a scratch of
 // kNd + kNd / 16 float2; blocks at or past n_blocks give no output.  The
@@ -68,22 +79,20 @@ __device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, f
             v[r - 16].y = x;
           lo = hi;
         }
-      } else {
-#pragma unroll
+      } else {  // 1-bit: rolled loop through the scratch (small code for the instruction cache)
+        float *xs = reinterpret_cast<float *>(sm);
+#pragma unroll 1
         for (int r = 0; r < 32; r++) {
           const int64_t p = bit0 + t + 16 * r;
-          const float x = ((__ldg(w + (p >> 5)) >> (p & 31)) & 1) ? 5.0f : -5.0f;
-          if (r < 16)
-            v[r].x = x;
-          else
-            v[r - 16].y = x;
+          xs[t + 16 * r] = ((__ldg(w + (p >> 5)) >> (p & 31)) & 1) ? 5.0f : -5.0f;
         }
+        pair_from_scratch(v, xs, t);
       }
-    } else {
-#pragma unroll
-      for (int r = 0; r < 16; r++) v[r].x = ok0 ? gather_sample(s, o0 + t + 16 * r, si) : 0.0f;
-#pragma unroll
-      for (int r = 0; r < 16; r++) v[r].y = ok1 ? gather_sample(s, o0 + kNd + t + 16 * r, si) : 0.0f;
+    } else {  // segment boundaries inside the pair: rare per-sample walk, rolled, through the scratch
+      float *xs = reinterpret_cast<float *>(sm);
+#pragma unroll 1
+      for (int r = 0; r < 32; r++) xs[t + 16 * r] = (r < 16 ? ok0 : ok1) ? gather_sample(s, o0 + t + 16 * r, si) : 0.0f;
+      pair_from_scratch(v, xs, t);
     }
   }
   fft_reg<-1, 8, true>(v, sm, t, tw, WarpSync());
@@ -483,26 +492,43 @@ __global__ void __launch_bounds__(1024, 1) window_fft_kernel(
 
 // ------------------------------------------------------------------------
 // Bit statistics over counted-byte ranges.  Work items: (stream, range, offset).
-__global__ void bitstat_kernel(const StreamDev *__restrict__ streams, const int4 *__restrict__ items, int nitems) {
+__global__ void __launch_bounds__(256) bitstat_kernel(const StreamDev *__restrict__ streams,
+                                                     const int4 *__restrict__ items, int nitems) {
   __shared__ unsigned int h[512];
   for (int i = threadIdx.x; i < 512; i += blockDim.x) h[i] = 0;
   __syncthreads();
   const int4 it = items[blockIdx.x];  // x = stream, y = range index, z = offset in range, w = count
   const StreamDev &s = streams[it.x];
   const DevStatRange rg = s.stats[it.y];
-  for (int j = threadIdx.x; j < it.w; j += blockDim.x) {
-    const int off = it.z + j;
-    const unsigned byte = __ldg(s.src + rg.src_byte + off);
+  const uint8_t *src = s.src + rg.src_byte + it.z;
+  int j = threadIdx.x;
+  if (j < it.w) {
+    // cal-diode state of the thread's first counted byte: it toggles at t0,
+    // t0 + period, ... (one toggle only when period <= 0, none when t0 <= 0);
+    // then advanced boundary by boundary as the thread strides on
+    int64_t c = (int64_t)rg.cidx + it.z + j;
+    const int64_t period = s.tsys_period;
     int on = 1;
+    int64_t next = INT64_MAX;
     if (s.tsys_two_bit) {
-      const int64_t c = (int64_t)rg.cidx + off;
       on = s.tsys_on0;
-      if (s.tsys_t0 > 0 && c >= s.tsys_t0) {
-        const int64_t flips = s.tsys_period > 0 ? 1 + (c - s.tsys_t0) / s.tsys_period : 1;
-        on ^= (int)(flips & 1);
+      if (s.tsys_t0 > 0) {
+        if (c >= s.tsys_t0) {
+          const int64_t flips = period > 0 ? 1 + (c - s.tsys_t0) / period : 1;
+          on ^= (int)(flips & 1);
+          next = period > 0 ? s.tsys_t0 + flips * period : INT64_MAX;
+        } else {
+          next = s.tsys_t0;
+        }
       }
     }
-    atomicAdd(&h[(on ? 0 : 256) + byte], 1u);
+    for (; j < it.w; j += blockDim.x, c += blockDim.x) {
+      while (c >= next) {
+        on ^= 1;
+        next = period > 0 ? next + period : INT64_MAX;
+      }
+      atomicAdd(&h[(on ? 0 : 256) + __ldg(src + j)], 1u);
+    }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < 512; i += blockDim.x)
