@@ -108,6 +108,11 @@ struct WarpSync {
 struct BlockSync {
   __device__ void operator()() const { __syncthreads(); }
 };
+// Named barrier `id` (1..15) over `count` threads (a multiple of 32) of the CTA.
+struct GroupSync {
+  int id, count;
+  __device__ void operator()() const { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory"); }
+};
 
 // 2-bit code -> sample value, the Bit2float_worker table (sfxc/src/bit2float_worker.cc:4-10):
 // 0 -> -7, 1 -> -2, 2 -> +2, 3 -> +7.

@@ -477,7 +477,14 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
   for (int k = k0; k < k1; k++) {
     window_apply<T>(v, t, nper, sgn, window);
     // tw_rot holds exp(-2 pi i m / rot) for m < rot, followed by exp(-2 pi i m / N) for m < N.
-    fft_reg<-1, LOGN, true>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, BlockSync());
+    // Each group's transform synchronises only its own T threads (named
+    // barrier 1 + g) when the groups are whole warps and few enough.
+    if constexpr (T >= 32 && S::THREADS / T <= 15) {
+      fft_reg<-1, LOGN, true>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, GroupSync{1 + g, T});
+      __syncthreads();  // the stores read every group's transform
+    } else {
+      fft_reg<-1, LOGN, true>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, BlockSync());
+    }
     if (k + 1 < k1)  // hop = rot / 2
       window_raw<T>(v, t, sok && row_of(k + 1) < nrows, nper, s.ts + (int64_t)(row0 + row_of(k + 1)) * N);
 #pragma unroll 1
@@ -523,12 +530,22 @@ __global__ void __launch_bounds__(256) bitstat_kernel(const StreamDev *__restric
         }
       }
     }
-    for (; j < it.w; j += blockDim.x, c += blockDim.x) {
-      while (c >= next) {
-        on ^= 1;
-        next = period > 0 ? next + period : INT64_MAX;
+    // four bytes in flight per thread before their counter updates
+    const int step = blockDim.x;
+    for (; j < it.w; j += 4 * step) {
+      unsigned b[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) b[u] = j + u * step < it.w ? __ldg(src + j + u * step) : 0u;
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (j + u * step >= it.w) break;
+        while (c >= next) {
+          on ^= 1;
+          next = period > 0 ? next + period : INT64_MAX;
+        }
+        atomicAdd(&h[(on ? 0 : 256) + b[u]], 1u);
+        c += step;
       }
-      atomicAdd(&h[(on ? 0 : 256) + __ldg(src + j)], 1u);
     }
   }
   __syncthreads();
