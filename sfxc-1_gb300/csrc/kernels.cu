@@ -509,15 +509,14 @@ __global__ void __launch_bounds__(256) bitstat_kernel(const StreamDev *__restric
   const StreamDev &s = streams[it.x];
   const DevStatRange rg = s.stats[it.y];
   const uint8_t *src = s.src + rg.src_byte + it.z;
-  int j = threadIdx.x;
-  if (j < it.w) {
-    // cal-diode state of the thread's first counted byte: it toggles at t0,
-    // t0 + period, ... (one toggle only when period <= 0, none when t0 <= 0);
-    // then advanced boundary by boundary as the thread strides on
-    int64_t c = (int64_t)rg.cidx + it.z + j;
-    const int64_t period = s.tsys_period;
+  const int64_t cfirst = (int64_t)rg.cidx + it.z;  // counted-byte index of src[0]
+  const int64_t period = s.tsys_period;
+  // cal-diode state of counted byte c: toggles at t0, t0 + period, ... (once
+  // when period <= 0, never when t0 <= 0); returns the state and the next
+  // toggle after c, so that later bytes advance it incrementally
+  auto state_at = [&](int64_t c, int64_t &next) {
     int on = 1;
-    int64_t next = INT64_MAX;
+    next = INT64_MAX;
     if (s.tsys_two_bit) {
       on = s.tsys_on0;
       if (s.tsys_t0 > 0) {
@@ -530,22 +529,44 @@ __global__ void __launch_bounds__(256) bitstat_kernel(const StreamDev *__restric
         }
       }
     }
-    // four bytes in flight per thread before their counter updates
-    const int step = blockDim.x;
-    for (; j < it.w; j += 4 * step) {
-      unsigned b[4];
+    return on;
+  };
+  auto count = [&](int64_t c, int &on, int64_t &next, unsigned byte) {
+    while (c >= next) {
+      on ^= 1;
+      next = period > 0 ? next + period : INT64_MAX;
+    }
+    atomicAdd(&h[(on ? 0 : 256) + byte], 1u);
+  };
+  // bytes before the first 16-byte boundary and after the last one, one per
+  // thread; the middle as 16-byte loads, four in flight per thread
+  const int head = (int)min((int64_t)it.w, (int64_t)((16 - ((uintptr_t)src & 15)) & 15));
+  const int nvec = (it.w - head) / 16;
+  const int tail0 = head + 16 * nvec;
+  for (int j = threadIdx.x; j < head + (it.w - tail0); j += blockDim.x) {
+    const int pos = j < head ? j : tail0 + (j - head);
+    int64_t next;
+    int on = state_at(cfirst + pos, next);
+    count(cfirst + pos, on, next, __ldg(src + pos));
+  }
+  const uint4 *vsrc = reinterpret_cast<const uint4 *>(src + head);
+  for (int q0 = threadIdx.x; q0 < nvec; q0 += 4 * blockDim.x) {
+    uint4 w[4];
 #pragma unroll
-      for (int u = 0; u < 4; u++) b[u] = j + u * step < it.w ? __ldg(src + j + u * step) : 0u;
+    for (int u = 0; u < 4; u++) {
+      const int q = q0 + u * blockDim.x;
+      w[u] = q < nvec ? __ldg(vsrc + q) : make_uint4(0u, 0u, 0u, 0u);
+    }
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        if (j + u * step >= it.w) break;
-        while (c >= next) {
-          on ^= 1;
-          next = period > 0 ? next + period : INT64_MAX;
-        }
-        atomicAdd(&h[(on ? 0 : 256) + b[u]], 1u);
-        c += step;
-      }
+    for (int u = 0; u < 4; u++) {
+      const int q = q0 + u * blockDim.x;
+      if (q >= nvec) break;
+      const int64_t c0 = cfirst + head + 16 * (int64_t)q;
+      int64_t next;
+      int on = state_at(c0, next);
+      const unsigned ww[4] = {w[u].x, w[u].y, w[u].z, w[u].w};
+#pragma unroll
+      for (int k = 0; k < 16; k++) count(c0 + k, on, next, (ww[k >> 2] >> (8 * (k & 3))) & 0xFFu);
     }
   }
   __syncthreads();

@@ -4,31 +4,30 @@
 // generation tensor cores.
 //
 // Each spectrum value x is stored as two FP16 numbers, hi = fp16(s*x) and
-// lo = fp16(s*x - hi) (s a power of two), so hi + lo carries ~22 bits.  For
-// one channel, the 128 "rows" of A are the components [hi.re, hi.im] of 32
-// inputs followed by [lo.re, lo.im]; A has one column per FFT (time).  The MMA
-// computes D = A A^T (128x128, FP32 accumulation in TMEM); summing its four
-// 64x64 quadrants gives (hi+lo)(hi+lo)^T exactly as products of the FP16
-// parts, i.e. the compensated product, and the epilogue forms
-//   Re V(a,b) = G[2a][2b] + G[2a+1][2b+1],  Im V(a,b) = G[2a+1][2b] - G[2a][2b+1].
-//
+// lo = fp16(s*x - hi) (s a power of two), so hi + lo carries ~22 bits.
 // Spectra layout (written by the windowed FFT): [row][channel][32 stream
 // slots][hi.re, hi.im, lo.re, lo.im] as FP16, i.e. 256 B per (row, channel),
 // so one channel's K-tile of 64 rows is two 128-byte-wide MN-major atoms
 // (stream slots 0-15 and 16-31), each 64 rows x 128 B.  The M index of a
-// component is 4 * stream + {hi.re, hi.im, lo.re, lo.im}; summing the four
-// hi/lo combinations gives the compensated product, and the epilogue forms
+// component is 4 * stream + {hi.re, hi.im, lo.re, lo.im}.  The MMA computes
+// D = A A^T (128 x 128, FP32 accumulation in TMEM); summing the four hi/lo
+// combinations of a stream pair gives the compensated product, and the
+// epilogue forms
 //   Re V(a,b) = sum over re-re and im-im pairs,  Im V(a,b) = im-re minus re-im
 // with lane shuffles over the 4 TMEM lanes (D rows) of one stream.
 //
-// CTA: 4 channels (4 x 128 TMEM columns), 256 threads, warp-specialised:
-// thread 0 streams K-tiles with TMA (cp.async.bulk.tensor, 128-byte swizzle,
-// 8 boxes of 8 KB per 64 KB stage, 3 stages); thread 32 issues 4 channels x 4
-// MMAs (K = 16) per stage and commits them to the stage's "empty" barrier;
-// after the last tile all 8 warps read TMEM (two channels per warp quarter)
-// and add the visibilities to the accumulator.  Every wait is bounded: on
-// timeout the CTA records an error, waits (bounded) for its loads in flight,
-// skips its output, frees its TMEM and returns.
+// Persistent CTA per SM, 10 warps, warp-specialised, over groups of 2
+// channels: warp 0 streams K-tiles with TMA (cp.async.bulk.tensor, 128-byte
+// swizzle, 4 boxes of 8 KB per 32 KB stage, 6 stages) without stopping at
+// group boundaries; warp 1 issues 2 channels x 4 MMAs (K = 16) per stage into
+// one of two TMEM buffers (2 x 256 columns) and commits each stage to its
+// "empty" barrier and each finished group to the buffer's "full" barrier;
+// warps 2-9 (one per channel and TMEM lane quarter) read the finished buffer,
+// add the visibilities to the accumulator (8 loads in flight per lane) and
+// release the buffer, while the next group accumulates in the other one.  Every wait is bounded: on timeout the
+// CTA records an error and stops, waits (bounded) for its loads and MMAs in
+// flight, frees its TMEM and returns.
+#include <algorithm>
 #include <cstdint>
 #include <cuda.h>
 #include <cuda_fp16.h>
@@ -40,13 +39,14 @@
 namespace sfxc {
 namespace {
 
-constexpr int kChan = 4;        // channels per CTA
+constexpr int kChan = 2;        // channels per group (one TMEM buffer)
 constexpr int kRowsK = 64;      // FFT rows per K-tile
-constexpr int kStages = 3;
-constexpr int kThreads = 256;
+constexpr int kStages = 6;
+constexpr int kThreads = 320;   // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr int kAtomBytes = kRowsK * 128;      // one 64-component atom of a K-tile
 constexpr int kChanTile = 2 * kAtomBytes;     // both atoms (stream slots 0-15, 16-31) of one channel
-constexpr int kStageBytes = kChan * kChanTile;  // 64 KB per stage
+constexpr int kStageBytes = kChan * kChanTile;  // 32 KB per stage
+constexpr uint32_t kBufCols = kChan * 128;      // TMEM columns per buffer
 constexpr unsigned long long kSpinLimit = 200000000ull;
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s
 
@@ -145,17 +145,23 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
       : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
     xcorr_tc_kernel(const __grid_constant__ CUtensorMap tmap, int nrows, int K, int kpad, const int *__restrict__ blmap,
                     int npad, float inv_scale2, float2 *__restrict__ acc, int *__restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);  // 128-byte swizzle wants 1 KB
-  __shared__ uint64_t full[kStages], empty[kStages], done;
+  __shared__ uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], done;
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int k0 = blockIdx.x * kChan;
+  const int ngroups = (K + kChan - 1) / kChan;
   const int nkt = (nrows + kRowsK - 1) / kRowsK;
+  // this CTA's groups: blockIdx.x, blockIdx.x + gridDim.x, ...
+  const int my_groups = blockIdx.x < ngroups ? (ngroups - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&tmem_base))
@@ -166,6 +172,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int s = 0; s < kStages; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 8);  // one arrival per epilogue warp
     }
     mbar_init(&done, 1);
     failed = 0;
@@ -178,24 +188,27 @@ __global__ void __launch_bounds__(kThreads, 1)
   volatile int *vfailed = &failed;
 
   if (tid == 0) {
-    // ---- TMA producer
+    // ---- TMA producer: every K-tile of every group, one stage ring
     int last[kStages];
     for (int s = 0; s < kStages; s++) last[s] = -1;
-    for (int kt = 0; kt < nkt; kt++) {
-      const int s = kt % kStages, n = kt / kStages;
-      if (n > 0 && !mbar_wait(&empty[s], (n - 1) & 1)) {
-        *vfailed = 1;
-        break;
+    int it = 0;
+    for (int i = 0; i < my_groups && !*vfailed; i++) {
+      const int g = blockIdx.x + i * gridDim.x;
+      for (int kt = 0; kt < nkt; kt++, it++) {
+        const int s = it % kStages, n = it / kStages;
+        if ((n > 0 && !mbar_wait(&empty[s], (n - 1) & 1)) || *vfailed) {
+          *vfailed = 1;
+          break;
+        }
+        mbar_expect_tx(&full[s], kStageBytes);
+        uint8_t *st = base + s * kStageBytes;
+#pragma unroll
+        for (int c = 0; c < kChan; c++)
+#pragma unroll
+          for (int a = 0; a < 2; a++)
+            tma_load_3d(st + c * kChanTile + a * kAtomBytes, &tmap, 2 * (g * kChan + c) + a, kt * kRowsK, &full[s]);
+        last[s] = it;
       }
-      if (*vfailed) break;
-      mbar_expect_tx(&full[s], kStageBytes);
-      uint8_t *st = base + s * kStageBytes;
-#pragma unroll
-      for (int c = 0; c < kChan; c++)
-#pragma unroll
-        for (int a = 0; a < 2; a++)
-          tma_load_3d(st + c * kChanTile + a * kAtomBytes, &tmap, 2 * (k0 + c) + a, kt * kRowsK, &full[s]);
-      last[s] = kt;
     }
     // loads still in flight land before the CTA may exit
     for (int s = 0; s < kStages; s++)
@@ -203,43 +216,59 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (tid == 32) {
     // ---- MMA issuer
     const uint32_t idesc = idesc_f16(128, 128);
-    for (int kt = 0; kt < nkt; kt++) {
-      const int s = kt % kStages, n = kt / kStages;
-      if (!mbar_wait(&full[s], n & 1)) {
+    int it = 0;
+    for (int i = 0; i < my_groups && !*vfailed; i++) {
+      const int b = i & 1, u = i >> 1;
+      if (u > 0 && !mbar_wait(&tempty[b], (u - 1) & 1)) {  // the epilogue has read buffer b
         *vfailed = 1;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t st = smem_u32(base + s * kStageBytes);
-#pragma unroll
-      for (int c = 0; c < kChan; c++) {
-#pragma unroll
-        for (int ks = 0; ks < kRowsK / 16; ks++) {
-          // 16 K-rows = two 8-row groups of 1024 B; M atoms kAtomBytes apart
-          const uint64_t d = smem_desc(st + c * kChanTile + ks * 2048, kAtomBytes, 1024);
-          mma_f16(tmem + c * 128, d, d, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
+      bool ok = true;
+      for (int kt = 0; kt < nkt; kt++, it++) {
+        const int s = it % kStages, n = it / kStages;
+        if (!mbar_wait(&full[s], n & 1)) {
+          ok = false;
+          break;
         }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t st = smem_u32(base + s * kStageBytes);
+#pragma unroll
+        for (int c = 0; c < kChan; c++) {
+#pragma unroll
+          for (int ks = 0; ks < kRowsK / 16; ks++) {
+            // 16 K-rows = two 8-row groups of 1024 B; M atoms kAtomBytes apart
+            const uint64_t d = smem_desc(st + c * kChanTile + ks * 2048, kAtomBytes, 1024);
+            mma_f16(tmem + b * kBufCols + c * 128, d, d, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
+          }
+        }
+        mma_commit(&empty[s]);
       }
-      mma_commit(&empty[s]);
+      if (!ok) {
+        *vfailed = 1;
+        break;
+      }
+      mma_commit(&tfull[b]);  // the group's sums are complete when its MMAs are
     }
     mma_commit(&done);  // arrives once every MMA issued above has completed
-  }
-  __syncthreads();
-  if (!mbar_wait(&done, 0)) *vfailed = 1;
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (*vfailed) {
-    if (tid == 0) atomicExch(err, 1);
-  } else if (nkt > 0) {
-    // ---- epilogue: warp quarter q reads D rows 32q..32q+31, two channels per warp
-    const int q = warp & 3, m = q * 32 + lane, a = m >> 2, p = m & 3;
-#pragma unroll 1
-    for (int cc = 0; cc < 2; cc++) {
-      const int c = (warp >> 2) * 2 + cc, k = k0 + c;
+  } else if (warp >= 2) {
+    // ---- epilogue: warp w reads channel (w - 2) / 4 of the group, TMEM lanes
+    // 32 (w % 4) .. + 31 (D rows)
+    const int q = warp & 3, c = (warp - 2) >> 2, m = q * 32 + lane, a = m >> 2, p = m & 3;
+    for (int i = 0; i < my_groups; i++) {
+      const int b = i & 1, u = i >> 1;
+      if (!mbar_wait(&tfull[b], u & 1)) {
+        *vfailed = 1;
+        break;
+      }
+      if (*vfailed) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int k = (blockIdx.x + i * gridDim.x) * kChan + c;
 #pragma unroll 1
       for (int j = 0; j < 4; j++) {
         float v[32];
-        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + c * 128 + j * 32, v);
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + b * kBufCols + c * 128 + j * 32, v);
+        float re8[8], im8[8];
 #pragma unroll
         for (int bb = 0; bb < 8; bb++) {
           const float A = v[4 * bb] + v[4 * bb + 2], B = v[4 * bb + 1] + v[4 * bb + 3];
@@ -249,21 +278,37 @@ __global__ void __launch_bounds__(kThreads, 1)
           im += __shfl_xor_sync(0xffffffffu, im, 1);
           re += __shfl_xor_sync(0xffffffffu, re, 2);
           im += __shfl_xor_sync(0xffffffffu, im, 2);
-          const int b = j * 8 + bb;
-          if (p == 0 && k < K && a < npad && b < npad) {
-            const int mapv = __ldg(blmap + a * npad + b);
-            if (mapv >= 0) {
-              float2 *dst = acc + (int64_t)(mapv >> 1) * kpad + k;
-              float2 o = *dst;
-              o.x += re * inv_scale2;
-              o.y += ((mapv & 1) ? -im : im) * inv_scale2;
-              *dst = o;
+          re8[bb] = re;
+          im8[bb] = im;
+        }
+        if (p == 0 && k < K && a < npad) {
+          // the 8 baselines' accumulator loads in flight together
+          int mv[8];
+          float2 o[8];
+#pragma unroll
+          for (int bb = 0; bb < 8; bb++) mv[bb] = j * 8 + bb < npad ? __ldg(blmap + a * npad + j * 8 + bb) : -1;
+#pragma unroll
+          for (int bb = 0; bb < 8; bb++)
+            if (mv[bb] >= 0) o[bb] = acc[(int64_t)(mv[bb] >> 1) * kpad + k];
+#pragma unroll
+          for (int bb = 0; bb < 8; bb++)
+            if (mv[bb] >= 0) {
+              o[bb].x += re8[bb] * inv_scale2;
+              o[bb].y += ((mv[bb] & 1) ? -im8[bb] : im8[bb]) * inv_scale2;
+              acc[(int64_t)(mv[bb] >> 1) * kpad + k] = o[bb];
             }
-          }
         }
       }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[b]);  // buffer b may be overwritten
     }
   }
+  __syncthreads();
+  if (!mbar_wait(&done, 0)) *vfailed = 1;  // no MMA in flight past this point
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (*vfailed && tid == 0) atomicExch(err, 1);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
@@ -308,8 +353,12 @@ cudaError_t launch_xcorr_tc(const void *spec, int nrows, int kpad, int K, const 
   const size_t smem = xcorr_tc_smem_bytes();
   cudaError_t e = cudaFuncSetAttribute(xcorr_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  xcorr_tc_kernel<<<(K + kChan - 1) / kChan, kThreads, smem, st>>>(map, nrows, K, kpad, blmap, npad, inv_scale2, acc,
-                                                                  err);
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 1;
+  const int ngroups = (K + kChan - 1) / kChan;
+  xcorr_tc_kernel<<<std::min(ngroups, nsm), kThreads, smem, st>>>(map, nrows, K, kpad, blmap, npad, inv_scale2, acc,
+                                                                   err);
   return cudaGetLastError();
 }
 
