@@ -232,6 +232,24 @@ def run_gpu(args):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     pool.shutdown()
+    # ---- the plain FP32 X-step on the same jobs (device time), for the
+    # tensor-core form's speed-up over it
+    compare = None
+    if args.x == "tc" and not args.no_fp32_compare:
+        for n in nodes:
+            n.close()
+        nodes = [correlator.CorrelatorNode(local, lib.X_FP32) for _ in jobs]
+        step_sequential()
+        f_total, f_kernel = 0.0, {}
+        for _ in range(args.steps):
+            f_total += step_sequential()[0]
+            for n in nodes:
+                for k, v in n.timings().items():
+                    f_kernel[k] = f_kernel.get(k, 0.0) + v
+        if world > 1:
+            from sfxc_gpu import sharding
+            f_total = sharding.max_over_ranks([f_total])[0]
+        compare = (f_total, f_kernel)
     if world > 1:
         from sfxc_gpu import sharding
         wall, dev_total = sharding.max_over_ranks([wall, dev_total])
@@ -259,6 +277,14 @@ def run_gpu(args):
         "real_time_factor": round(e2e / (total / (args.integration_us / 1e6) / 1e9), 2),
     }
     line["roofline"] = roofline(args, per_kernel, total)
+    if compare is not None:
+        f_total, f_kernel = compare
+        f_value = total * args.steps * world / (f_total / 1e3) / 1e9
+        line["fp32_x_step"] = {
+            "value": round(f_value, 3), "unit": "Gsamples/s", "ms_per_step": round(f_total / args.steps, 3),
+            "xstep_ms": round(f_kernel.get("xstep_ms", 0.0) / args.steps, 3),
+            "tc_over_fp32": round(value / f_value, 3),
+            "tc_over_fp32_xstep": round(f_kernel.get("xstep_ms", 0.0) / max(per_kernel.get("xstep_ms", 0.0), 1e-9), 2)}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, quick=True)
     print(json.dumps(line), flush=True)
@@ -364,7 +390,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--x", default="fp32", choices=["fp32", "tc"])
+    ap.add_argument("--x", default="tc", choices=["fp32", "tc"])
+    ap.add_argument("--no-fp32-compare", action="store_true",
+                    help="skip the device-time run of the FP32 X-step beside the tensor-core one")
     ap.add_argument("--stations", type=int, default=16)
     ap.add_argument("--subbands", type=int, default=8)
     ap.add_argument("--nchan", type=int, default=4096)

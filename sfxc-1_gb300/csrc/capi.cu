@@ -68,6 +68,29 @@ struct DevBuf {
   }
 };
 
+// Pinned host staging that only grows (asynchronous uploads; freeing pinned
+// memory synchronises the device, so it is kept).
+struct HostBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  HostBuf() = default;
+  HostBuf(const HostBuf &) = delete;
+  HostBuf &operator=(const HostBuf &) = delete;
+  void *ensure(size_t n) {
+    if (n > cap) {
+      if (p) cudaFreeHost(p);
+      p = nullptr;
+      cap = 0;
+      CK(cudaHostAlloc(&p, n, cudaHostAllocDefault));
+      cap = n;
+    }
+    return p;
+  }
+  ~HostBuf() {
+    if (p) cudaFreeHost(p);
+  }
+};
+
 struct StreamCtx {
   std::vector<Record> recs;
   StreamUnpackState ust;
@@ -132,7 +155,7 @@ struct sfxc_gpu_ctx {
     DevBuf window, twrot;
   };
   std::map<int, RotTables> rot_tables;
-  DevBuf streamdev_grouped;
+  HostBuf staging;  // the integration's chunk descriptors, uploaded in one copy
   std::vector<StreamDev> hsd;
 };
 
@@ -423,8 +446,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       spl.insert(spl.end(), s.sp.d[k].begin(), s.sp.d[k].end());
     }
     upload(s.spline, spl.data(), spl.size() * 8, st);
-    s.hist.ensure(512 * 8);
-    CK(cudaMemsetAsync(s.hist.p, 0, 512 * 8, st));
+    s.hist.ensure(8 * 8);
+    CK(cudaMemsetAsync(s.hist.p, 0, 8 * 8, st));
     StreamDev &d = c->hsd[i];
     d.src = s.src.as<uint8_t>();
     d.segs = s.segs.as<DevSegment>();
@@ -475,9 +498,19 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     d.phase_zero = std::all_of(s.sp.y[1].begin(), s.sp.y[1].end(), [](double v) { return v == 0.0; });
     d.amp_one = std::all_of(s.sp.y[2].begin(), s.sp.y[2].end(), [](double v) { return v == 1.0; });
     d.no_clock = s.sp.clock_offset == 0.0 && s.sp.clock_rate == 0.0;
-    for (int r = 0; r < (int)s.plan.stats.size(); r++) {
-      const StatRange &sr = s.plan.stats[r];
-      for (int off = 0; off < sr.n; off += 65536) items.push_back(make_int4(i, r, off, std::min(65536, sr.n - off)));
+    // bit-statistics work: ranges up to 8 KB (one per protocol data block)
+    // packed about 64 KB to an item, longer ones cut into 64 KB pieces
+    const std::vector<StatRange> &st_r = s.plan.stats;
+    for (int r = 0; r < (int)st_r.size();) {
+      if (st_r[r].n > 8192) {
+        for (int off = 0; off < st_r[r].n; off += 65536) items.push_back(make_int4(i, r, 0, off));
+        r++;
+        continue;
+      }
+      const int r0 = r;
+      int64_t bytes = 0;
+      while (r < (int)st_r.size() && st_r[r].n <= 8192 && r - r0 < 64 && bytes < 65536) bytes += st_r[r++].n;
+      items.push_back(make_int4(i, r0, r - r0, 0));
     }
     s.pushed = false;
   }
@@ -501,15 +534,11 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     flagfac[b] = n;
   }
   upload(c->flagfac, flagfac.data(), flagfac.size() * 8, st);
-  upload(c->streamdev, c->hsd.data(), c->hsd.size() * sizeof(StreamDev), st);
   upload(c->items, items.data(), items.size() * sizeof(int4), st);
   // ---- device work
   const size_t accn = (size_t)c->nbins * nbl * kpad;
   c->acc.ensure(accn * sizeof(float2));
   CK(cudaMemsetAsync(c->acc.p, 0, accn * sizeof(float2), st));
-  CK(cudaEventRecord(c->ev[0], st));
-  launch_bitstat(c->streamdev.as<StreamDev>(), c->items.as<int4>(), (int)items.size(), st);
-  CK(cudaGetLastError());
   const bool pulsar = c->nbins > 1;
   std::vector<std::pair<int, int>> ranges;
   if (pulsar)
@@ -594,10 +623,21 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     CK(cudaEventCreate(&e));
     c->evpool.push_back(e);
   }
-  int launches = items.empty() ? 0 : 1;
-  size_t ev = 0;
-  for (auto &rg : ranges) {
-    const int r0 = rg.first, r1 = rg.second, nrows = r1 - r0;
+  // ---- every chunk's stream descriptors, in job order and then grouped by
+  // windowed-FFT length (job order within a group), in one asynchronous
+  // upload from pinned memory: no host wait between the chunks' launches
+  std::vector<int> order;                   // job index of each grouped position
+  std::vector<std::pair<int, int>> groups;  // (rot, first grouped position)
+  for (auto &rt : c->rot_tables) {
+    const size_t first = order.size();
+    for (int i = 0; i < N; i++)
+      if (c->sc[i].rot == rt.first) order.push_back(i);
+    if (order.size() > first) groups.push_back({rt.first, (int)first});
+  }
+  const size_t per_chunk = 2 * (size_t)N;
+  StreamDev *staged = static_cast<StreamDev *>(c->staging.ensure(ranges.size() * per_chunk * sizeof(StreamDev)));
+  for (size_t ch = 0; ch < ranges.size(); ch++) {
+    const int r0 = ranges[ch].first, r1 = ranges[ch].second;
     // block range of each stream for rows [r0, r1) (plus the overlapping half window)
     for (int i = 0; i < N; i++) {
       StreamDev &d = c->hsd[i];
@@ -608,29 +648,33 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       d.bamp = c->sc[i].bamp.as<float>();
       d.block0 = b0;
       d.n_blocks = b1 - b0;
+      staged[ch * per_chunk + i] = d;
     }
-    upload(c->streamdev, c->hsd.data(), c->hsd.size() * sizeof(StreamDev), st);
-    // the same descriptors grouped by windowed-FFT length (job order within a group)
-    std::vector<StreamDev> grouped;
-    std::vector<std::pair<int, int>> groups;  // (rot, first index in `grouped`)
-    for (auto &rt : c->rot_tables) {
-      const size_t first = grouped.size();
-      for (int i = 0; i < N; i++)
-        if (c->sc[i].rot == rt.first) grouped.push_back(c->hsd[i]);
-      if (grouped.size() > first) groups.push_back({rt.first, (int)first});
-    }
-    upload(c->streamdev_grouped, grouped.data(), grouped.size() * sizeof(StreamDev), st);
+    for (int k = 0; k < N; k++) staged[ch * per_chunk + N + k] = c->hsd[order[k]];
+  }
+  c->streamdev.ensure(ranges.size() * per_chunk * sizeof(StreamDev));
+  CK(cudaMemcpyAsync(c->streamdev.p, staged, ranges.size() * per_chunk * sizeof(StreamDev), cudaMemcpyHostToDevice,
+                     st));
+  CK(cudaEventRecord(c->ev[0], st));
+  // bit statistics read only chunk-independent fields (source bytes, ranges, histograms)
+  launch_bitstat(c->streamdev.as<StreamDev>(), c->items.as<int4>(), (int)items.size(), st);
+  CK(cudaGetLastError());
+  int launches = items.empty() ? 0 : 1;
+  size_t ev = 0;
+  for (size_t ch = 0; ch < ranges.size(); ch++) {
+    const int nrows = ranges[ch].second - ranges[ch].first;
+    StreamDev *dchunk = c->streamdev.as<StreamDev>() + ch * per_chunk;
     CK(cudaEventRecord(c->evpool[ev], st));
-    launch_fstep_block(c->streamdev.as<StreamDev>(), N, max_blocks, c->tw256.as<float2>(), st);
+    launch_fstep_block(dchunk, N, max_blocks, c->tw256.as<float2>(), st);
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->evpool[ev + 1], st));
     for (size_t g = 0; g < groups.size(); g++) {
       const int rot = groups[g].first, first = groups[g].second;
-      const int count = (g + 1 < groups.size() ? groups[g + 1].second : (int)grouped.size()) - first;
+      const int count = (g + 1 < groups.size() ? groups[g + 1].second : N) - first;
       const int nper = c->p.window == WINDOW_NONE ? rot / 2 : rot;
       const sfxc_gpu_ctx::RotTables &t = c->rot_tables.at(rot);
-      launch_window_fft(c->streamdev_grouped.as<StreamDev>() + first, count, 0, nrows, max_rows, t.window.as<float>(),
-                        t.twrot.as<float2>(), rot, nper, M, kpad, c->spec.p, tc_x, tc_scale, st);
+      launch_window_fft(dchunk + N + first, count, 0, nrows, max_rows, t.window.as<float>(), t.twrot.as<float2>(), rot,
+                        nper, M, kpad, c->spec.p, tc_x, tc_scale, st);
       CK(cudaGetLastError());
     }
     CK(cudaEventRecord(c->evpool[ev + 2], st));
@@ -665,9 +709,9 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   CK(cudaGetLastError());
   std::vector<float2> vis((size_t)c->nbins * nbl * K);
   CK(cudaMemcpyAsync(vis.data(), c->out.p, vis.size() * sizeof(float2), cudaMemcpyDeviceToHost, st));
-  std::vector<unsigned long long> hist((size_t)N * 512);
+  std::vector<unsigned long long> hist((size_t)N * 8);
   for (int i = 0; i < N; i++)
-    CK(cudaMemcpyAsync(hist.data() + (size_t)i * 512, c->sc[i].hist.p, 512 * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hist.data() + (size_t)i * 8, c->sc[i].hist.p, 8 * 8, cudaMemcpyDeviceToHost, st));
   int dev_err = 0;
   CK(cudaMemcpyAsync(&dev_err, c->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaEventRecord(c->evpool[ev + 1], st));
@@ -694,9 +738,9 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   c->timings[4] = tall;
   for (int i = 0; i < N; i++) {
     BitStats &bs = c->sc[i].stats;
-    for (int k = 0; k < 256; k++) {
-      bs.on[k] = (int64_t)hist[(size_t)i * 512 + k];
-      bs.off[k] = (int64_t)hist[(size_t)i * 512 + 256 + k];
+    for (int k = 0; k < 4; k++) {
+      bs.on[k] = (int64_t)hist[(size_t)i * 8 + k];
+      bs.off[k] = (int64_t)hist[(size_t)i * 8 + 4 + k];
     }
     bs.n_invalid = c->sc[i].plan.n_invalid;
     bs.bits = c->streams[i].bits;

@@ -58,7 +58,7 @@ struct StreamDev {
   float *bamp;
   // outputs
   float *ts;                   // fringe-stopped series, n_blocks*256 floats
-  unsigned long long *hist;    // 512 counters: [on|off][byte]
+  unsigned long long *hist;    // 8 code counters: cal diode on [0..3], off [4..7]
 };
 
 // --------------------------------------------------------------------------

@@ -595,30 +595,19 @@ std::vector<Baseline> create_baselines(const std::vector<StationStream> &s, int 
 }
 
 void BitStats::levels(int out[5]) const {
-  int acc[5] = {0, 0, 0, 0, 0};  // int accumulators as in the reference
-  if (bits == 2) {
-    for (int i = 0; i < 256; i++) {
-      int c = (int)(on[i] + off[i]);
-      for (int k = 0; k < 4; k++) acc[(i >> (2 * k)) & 3] += c;
-    }
-  } else {
-    for (int i = 0; i < 256; i++)
-      for (int k = 0; k < 8; k++) acc[(i >> k) & 1] += (int)(on[i] + off[i]);
-  }
+  // the reference adds every byte bin's count into int accumulators, once per
+  // code of the byte; the same sums from the code counts, wrapped to 32 bits
+  int acc[5] = {0, 0, 0, 0, 0};
+  for (int k = 0; k < (bits == 2 ? 4 : 2); k++) acc[k] = (int)(uint32_t)(uint64_t)(on[k] + off[k]);
   acc[4] += (int)n_invalid;
   for (int i = 0; i < 5; i++)
     out[i] = (int)(((uint64_t)base_sample_rate * (uint64_t)(int64_t)acc[i]) / (uint64_t)sample_rate);
 }
 
 void BitStats::tsys(int out[4]) const {
-  int64_t a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
   out[0] = out[1] = out[2] = out[3] = 0;
   if (bits != 2) return;
-  for (int i = 0; i < 256; i++)
-    for (int k = 0; k < 4; k++) {
-      a[(i >> (2 * k)) & 3] += on[i];
-      b[(i >> (2 * k)) & 3] += off[i];
-    }
+  const int64_t *a = on, *b = off;
   out[0] = (int)(a[1] + a[2]);
   out[1] = (int)(a[0] + a[3]);
   out[2] = (int)(b[1] + b[2]);

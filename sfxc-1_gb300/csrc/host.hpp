@@ -157,7 +157,9 @@ struct Baseline {
 };
 std::vector<Baseline> create_baselines(const std::vector<StationStream> &s, int reference_station);  // 134-171
 struct BitStats {
-  int64_t on[256], off[256];
+  // per-code counts of the counted bytes (2-bit codes 0..3, or bit values 0/1
+  // at indices 0/1), with the cal diode on and off
+  int64_t on[4], off[4];
   int64_t n_invalid;
   int bits, sample_rate, base_sample_rate;
   void levels(int out[5]) const;  // bit_statistics::get_statistics (bit_statistics.cc:81-111)

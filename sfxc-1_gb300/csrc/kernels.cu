@@ -500,23 +500,33 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
 
 // ------------------------------------------------------------------------
 // Bit statistics over counted-byte ranges.  Work items: (stream, range, offset).
-__global__ void __launch_bounds__(256) bitstat_kernel(const StreamDev *__restrict__ streams,
-                                                     const int4 *__restrict__ items, int nitems) {
-  __shared__ unsigned int h[512];
-  for (int i = threadIdx.x; i < 512; i += blockDim.x) h[i] = 0;
-  __syncthreads();
-  const int4 it = items[blockIdx.x];  // x = stream, y = range index, z = offset in range, w = count
-  const StreamDev &s = streams[it.x];
-  const DevStatRange rg = s.stats[it.y];
-  const uint8_t *src = s.src + rg.src_byte + it.z;
-  const int64_t cfirst = (int64_t)rg.cidx + it.z;  // counted-byte index of src[0]
-  const int64_t period = s.tsys_period;
-  // cal-diode state of counted byte c: toggles at t0, t0 + period, ... (once
-  // when period <= 0, never when t0 <= 0); returns the state and the next
-  // toggle after c, so that later bytes advance it incrementally
-  auto state_at = [&](int64_t c, int64_t &next) {
-    int on = 1;
+// Code counts of 8 bits (mask 0x55) or 32 bits (mask 0x55555555): 2-bit
+// codes -> c[code] with code = 2 * high bit + low bit; 1-bit -> c[bit value].
+__device__ __forceinline__ void count_codes(uint32_t x, int nbits, int bits, uint32_t (&c)[4]) {
+  if (bits == 2) {
+    const uint32_t m = nbits == 32 ? 0x55555555u : 0x55u;
+    const uint32_t lo = x & m, hi = (x >> 1) & m;
+    c[3] = __popc(hi & lo);
+    c[2] = __popc(hi & ~lo & m);
+    c[1] = __popc(~hi & lo & m);
+    c[0] = nbits / 2 - c[1] - c[2] - c[3];
+  } else {
+    c[1] = __popc(nbits == 32 ? x : x & 0xFFu);
+    c[0] = nbits - c[1];
+    c[2] = c[3] = 0;
+  }
+}
+
+// Cal-diode state over increasing counted-byte indices: toggles at t0,
+// t0 + period, ... (once when period <= 0, never when t0 <= 0).  at() places
+// the walker with one division, advance() steps it forward without any.
+struct CalWalk {
+  int on;
+  int64_t next, period;
+  __device__ __forceinline__ void at(const StreamDev &s, int64_t c) {
+    on = 1;
     next = INT64_MAX;
+    period = s.tsys_period;
     if (s.tsys_two_bit) {
       on = s.tsys_on0;
       if (s.tsys_t0 > 0) {
@@ -529,49 +539,114 @@ __global__ void __launch_bounds__(256) bitstat_kernel(const StreamDev *__restric
         }
       }
     }
-    return on;
-  };
-  auto count = [&](int64_t c, int &on, int64_t &next, unsigned byte) {
+  }
+  __device__ __forceinline__ void advance(int64_t c) {
     while (c >= next) {
       on ^= 1;
       next = period > 0 ? next + period : INT64_MAX;
     }
-    atomicAdd(&h[(on ? 0 : 256) + byte], 1u);
-  };
-  // bytes before the first 16-byte boundary and after the last one, one per
-  // thread; the middle as 16-byte loads, four in flight per thread
-  const int head = (int)min((int64_t)it.w, (int64_t)((16 - ((uintptr_t)src & 15)) & 15));
-  const int nvec = (it.w - head) / 16;
+  }
+};
+
+struct CodeCounts {
+  uint32_t on[4], off[4];
+  __device__ __forceinline__ void add(uint32_t x, int nbits, int bits, int cal_on) {
+    uint32_t c[4];
+    count_codes(x, nbits, bits, c);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      on[k] += cal_on ? c[k] : 0u;
+      off[k] += cal_on ? 0u : c[k];
+    }
+  }
+};
+
+// Code counts of the counted bytes src[0, n) (counted index cfirst + j for
+// src[j]) by a group of NL threads: bytes before the first 16-byte boundary
+// and after the last one singly, the middle as 16-byte loads (four in flight
+// per thread) counted a word at a time unless a cal-diode toggle falls
+// inside the word.
+template <int NL>
+__device__ __forceinline__ void count_span(const StreamDev &s, const uint8_t *src, int n, int64_t cfirst, int lane,
+                                           CodeCounts &cc) {
+  const int bits = s.bits;
+  const int head = min(n, (int)((16 - ((uintptr_t)src & 15)) & 15));
+  const int nvec = (n - head) / 16;
   const int tail0 = head + 16 * nvec;
-  for (int j = threadIdx.x; j < head + (it.w - tail0); j += blockDim.x) {
+  for (int j = lane; j < head + (n - tail0); j += NL) {
     const int pos = j < head ? j : tail0 + (j - head);
-    int64_t next;
-    int on = state_at(cfirst + pos, next);
-    count(cfirst + pos, on, next, __ldg(src + pos));
+    CalWalk w;
+    w.at(s, cfirst + pos);
+    cc.add(__ldg(src + pos), 8, bits, w.on);
   }
+  if (lane >= nvec) return;
   const uint4 *vsrc = reinterpret_cast<const uint4 *>(src + head);
-  for (int q0 = threadIdx.x; q0 < nvec; q0 += 4 * blockDim.x) {
-    uint4 w[4];
+  const int64_t cvec = cfirst + head;
+  CalWalk w;
+  w.at(s, cvec + 16 * (int64_t)lane);
+  for (int q0 = lane; q0 < nvec; q0 += 4 * NL) {
+    uint4 v[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-      const int q = q0 + u * blockDim.x;
-      w[u] = q < nvec ? __ldg(vsrc + q) : make_uint4(0u, 0u, 0u, 0u);
+      const int q = q0 + u * NL;
+      v[u] = q < nvec ? __ldg(vsrc + q) : make_uint4(0u, 0u, 0u, 0u);
     }
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-      const int q = q0 + u * blockDim.x;
+      const int q = q0 + u * NL;
       if (q >= nvec) break;
-      const int64_t c0 = cfirst + head + 16 * (int64_t)q;
-      int64_t next;
-      int on = state_at(c0, next);
-      const unsigned ww[4] = {w[u].x, w[u].y, w[u].z, w[u].w};
+      const int64_t c0 = cvec + 16 * (int64_t)q;
+      w.advance(c0);
+      const uint32_t ww[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+      if (c0 + 16 <= w.next) {
 #pragma unroll
-      for (int k = 0; k < 16; k++) count(c0 + k, on, next, (ww[k >> 2] >> (8 * (k & 3))) & 0xFFu);
+        for (int k = 0; k < 4; k++) cc.add(ww[k], 32, bits, w.on);
+      } else {
+        for (int b = 0; b < 16; b++) {
+          w.advance(c0 + b);
+          cc.add((ww[b >> 2] >> (8 * (b & 3))) & 0xFFu, 8, bits, w.on);
+        }
+      }
     }
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < 512; i += blockDim.x)
-    if (h[i]) atomicAdd(&s.hist[i], (unsigned long long)h[i]);
+}
+
+// Bit statistics over the counted-byte ranges, as per-code counts split by
+// the cal-diode state: s.hist[0..3] on, [4..7] off (the byte histogram of
+// bit_statistics.cc:36-47 enters the levels and tsys values only through
+// these counts).  Work items (stream, first range, range count, offset):
+// range count > 0 packs that many short ranges, one warp per range; range
+// count 0 is the 64 KB piece at `offset` of one long range, all warps.
+__global__ void __launch_bounds__(256) bitstat_kernel(const StreamDev *__restrict__ streams,
+                                                     const int4 *__restrict__ items, int nitems) {
+  const int4 it = items[blockIdx.x];
+  const StreamDev &s = streams[it.x];
+  CodeCounts cc = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (it.z > 0) {
+    for (int r = it.y + warp; r < it.y + it.z; r += blockDim.x >> 5) {
+      const DevStatRange rg = s.stats[r];
+      count_span<32>(s, s.src + rg.src_byte, rg.n, rg.cidx, lane, cc);
+    }
+  } else {
+    const DevStatRange rg = s.stats[it.y];
+    const int n = min(65536, rg.n - it.w);
+    count_span<256>(s, s.src + rg.src_byte + it.w, n, (int64_t)rg.cidx + it.w, threadIdx.x, cc);
+  }
+  // warp sums, one global update per counter and warp
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    uint32_t a = cc.on[k], b = cc.off[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+      if (a) atomicAdd(&s.hist[k], (unsigned long long)a);
+      if (b) atomicAdd(&s.hist[4 + k], (unsigned long long)b);
+    }
+  }
 }
 
 // ------------------------------------------------------------------------

@@ -162,8 +162,10 @@ class CorrelatorNode:
     def timings(self):
         t = (C.c_float * 6)()
         self._check(self._lib.sfxc_gpu_last_timings(self._h, t))
+        # the bit statistics run first, before the first chunk's events: the
+        # total less the four timed stages
         return {"unpack_fringe_ms": t[0], "window_fft_ms": t[1], "xstep_ms": t[2], "normalise_ms": t[3],
-                "total_ms": t[4], "launches": int(t[5])}
+                "bitstat_ms": max(0.0, t[4] - t[0] - t[1] - t[2] - t[3]), "total_ms": t[4], "launches": int(t[5])}
 
     def extract_block(self, block, word_bytes, bits, tracks):
         """One reader block (read_recording's dict) through the channel
