@@ -9,8 +9,8 @@
 //   window_fft_kernel    window, sideband flip, real FFT of 2M samples, channel
 //                        selection (delay_correction.cc:57-75); M/16 threads per row.
 // Both FFT stages are the register-resident radix-16 transforms of fft_reg.cuh.
-//   bitstat_kernel       byte histograms with cal-diode on/off split
-//                        (bit_statistics.cc:36-47, bit2float_worker.cc:341-346).
+//   bitstat_kernel       per-code sample counts with cal-diode on/off split, from
+//                        popcounts (bit_statistics.cc:36-47, bit2float_worker.cc:341-346).
 //   xcorr_f32_kernel     X-step on CUDA cores, 4x4 stream tiles per thread
 //                        (Correlation_core::integration_step, correlation_core.cc:241-273).
 //   pulsar_bins_kernel / xcorr_f32_pulsar  bin per (FFT, channel) in FP64 and binned
@@ -44,13 +44,14 @@ __device__ __forceinline__ void pair_from_scratch(float2 (&v)[16], const float *
 }
 
 // Pair (bl0, bl0 + 1) of a stream's blocks (indices from the stream's block0)
-// by the 16 threads t = 0..15 of a half warp, with a scratch of
-// kNd + kNd / 16 float2; blocks at or past n_blocks give no output.  The
+// by the 16 threads t = 0..15 of a half warp, with a scratch of kFsScratch
+// float2; blocks at or past n_blocks give no output.  The
 // result goes through store(block, sample, value).  Both half warps of a warp
 // must call this together (warp barriers).
+constexpr int kFsScratch = kNd + kNd / 16 + 9 * 16;
 template <class Store>
 __device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, float2 *sm,
-                                           const float2 *__restrict__ tw, Store store) {
+                                           const float2 *__restrict__ tw, const float4 *ptab, Store store) {
   const bool ok0 = bl0 < s.n_blocks, ok1 = bl0 + 1 < s.n_blocks;
   float2 v[16];
   {  // unpack the two blocks through the plan
@@ -95,71 +96,78 @@ __device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, f
       pair_from_scratch(v, xs, t);
     }
   }
-  fft_reg<-1, 8, true>(v, sm, t, tw, WarpSync());
-
-  // split, halve DC/Nyquist, phase ramp; block 0 into v, block 1 into g1
+  // The pair's forward transform and the two blocks' inverse ones share one
+  // code path (inverse as conj(FFT(conj Y))): h = 0 forward, h = 1, 2 the
+  // inverse of block h - 1.  Block 1's ramped half spectrum waits in the
+  // scratch behind the transform buffer, ext[16 r + t] for r < 9.
+  float2 *ext = sm + kNd + kNd / 16;
   const float4 p0 = ok0 ? s.bparams[bl0] : make_float4(0.f, 0.f, 0.f, 0.f);
   const float4 p1 = ok1 ? s.bparams[bl0 + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
-  float a_s, a_c, as_s, as_c, b_s, b_c, bs_s, bs_c;
-  sincosf(fmaf((float)t, p0.y, p0.x), &a_s, &a_c);
-  sincosf(16.0f * p0.y, &as_s, &as_c);
-  sincosf(fmaf((float)t, p1.y, p1.x), &b_s, &b_c);
-  sincosf(16.0f * p1.y, &bs_s, &bs_c);
-  float2 g1[9];
-#pragma unroll
-  for (int r = 0; r < 9; r++) {
-    const int k = t + 16 * r;
-    float2 f0 = make_float2(0.f, 0.f), f1 = make_float2(0.f, 0.f);
-    if (r < 8 || t == 0) {
-      const float2 xk = sm[padi(k & (kNd - 1))], xm = sm[padi((kNd - k) & (kNd - 1))];
-      const float h = (k == 0 || k == kNd / 2) ? 0.25f : 0.5f;  // 1/2 of the split, DC and Nyquist halved again
-      const float er = h * (xk.x + xm.x), ei = h * (xk.y - xm.y);
-      const float orr = h * (xk.y + xm.y), oi = -h * (xk.x - xm.x);
-      // F * (cos phi, -sin phi)
-      f0 = make_float2(er * a_c + ei * a_s, ei * a_c - er * a_s);
-      f1 = make_float2(orr * b_c + oi * b_s, oi * b_c - orr * b_s);
-    }
-    v[r] = f0;
-    g1[r] = f1;
-    float c2 = a_c * as_c - a_s * as_s;
-    a_s = a_s * as_c + a_c * as_s;
-    a_c = c2;
-    c2 = b_c * bs_c - b_s * bs_s;
-    b_s = b_s * bs_c + b_c * bs_s;
-    b_c = c2;
-  }
-#pragma unroll
-  for (int r = 9; r < 16; r++) v[r] = make_float2(0.f, 0.f);
-  __syncwarp();
-
-  // per block: inverse FFT (result in registers, v[r] = z[t + 16 r]), fringe rotation, store
 #pragma unroll 1
-  for (int h = 0; h < 2; h++) {
-    if (h == 1) {
+  for (int h = 0; h < 3; h++) {
+    if (h == 2) {
 #pragma unroll
-      for (int r = 0; r < 9; r++) v[r] = g1[r];
+      for (int r = 0; r < 9; r++) v[r] = ext[16 * r + t];
 #pragma unroll
       for (int r = 9; r < 16; r++) v[r] = make_float2(0.f, 0.f);
     }
-    fft_reg<+1, 8, false>(v, sm, t, tw, WarpSync());
-    const int bl = bl0 + h;
-    if (bl < s.n_blocks) {
-      const float4 prm = h ? p1 : p0;
-      const float amp = s.bamp[bl];
-      float rs, rc, ss, sc;
-      sincosf(fmaf((float)t, prm.w, prm.z), &rs, &rc);
-      sincosf(16.0f * prm.w, &ss, &sc);
-      rs *= amp;
-      rc *= amp;
+    // v[r] = X[t + 16 r]; the transform's reads of sm are complete on return
+    fft_reg<-1, 8, false>(v, sm, t, tw, ptab, WarpSync());
+    if (h == 0) {
+      // split, halve DC/Nyquist, phase ramp; conj of block 0 into v, of block 1 into ext
 #pragma unroll
-      for (int r = 0; r < 16; r++) {
-        store(bl, t + 16 * r, v[r].x * rc + v[r].y * rs);
-        const float c2 = rc * sc - rs * ss;
-        rs = rs * sc + rc * ss;
-        rc = c2;
+      for (int r = 0; r < 16; r++) sm[padi(t + 16 * r)] = v[r];
+      __syncwarp();
+      float a_s, a_c, as_s, as_c, b_s, b_c, bs_s, bs_c;
+      sincosf(fmaf((float)t, p0.y, p0.x), &a_s, &a_c);
+      sincosf(16.0f * p0.y, &as_s, &as_c);
+      sincosf(fmaf((float)t, p1.y, p1.x), &b_s, &b_c);
+      sincosf(16.0f * p1.y, &bs_s, &bs_c);
+#pragma unroll
+      for (int r = 0; r < 9; r++) {
+        const int k = t + 16 * r;
+        float2 f0 = make_float2(0.f, 0.f), f1 = make_float2(0.f, 0.f);
+        if (r < 8 || t == 0) {
+          const float2 xk = sm[padi(k & (kNd - 1))], xm = sm[padi((kNd - k) & (kNd - 1))];
+          const float hf = (k == 0 || k == kNd / 2) ? 0.25f : 0.5f;  // 1/2 of the split, DC and Nyquist halved again
+          const float er = hf * (xk.x + xm.x), ei = hf * (xk.y - xm.y);
+          const float orr = hf * (xk.y + xm.y), oi = -hf * (xk.x - xm.x);
+          // conj(F * (cos phi, -sin phi))
+          f0 = make_float2(er * a_c + ei * a_s, er * a_s - ei * a_c);
+          f1 = make_float2(orr * b_c + oi * b_s, orr * b_s - oi * b_c);
+        }
+        v[r] = f0;
+        ext[16 * r + t] = f1;
+        float c2 = a_c * as_c - a_s * as_s;
+        a_s = a_s * as_c + a_c * as_s;
+        a_c = c2;
+        c2 = b_c * bs_c - b_s * bs_s;
+        b_s = b_s * bs_c + b_c * bs_s;
+        b_c = c2;
+      }
+#pragma unroll
+      for (int r = 9; r < 16; r++) v[r] = make_float2(0.f, 0.f);
+      __syncwarp();  // the split's reads of sm before the next transform writes it
+    } else {
+      // v = conj(z), z the block's inverse transform: fringe rotation Re(z e^{-i phi}) x amplitude
+      const int bl = bl0 + h - 1;
+      if (bl < s.n_blocks) {
+        const float4 prm = h == 2 ? p1 : p0;
+        const float amp = s.bamp[bl];
+        float rs, rc, ss, sc;
+        sincosf(fmaf((float)t, prm.w, prm.z), &rs, &rc);
+        sincosf(16.0f * prm.w, &ss, &sc);
+        rs *= amp;
+        rc *= amp;
+#pragma unroll
+        for (int r = 0; r < 16; r++) {
+          store(bl, t + 16 * r, v[r].x * rc - v[r].y * rs);
+          const float c2 = rc * sc - rs * ss;
+          rs = rs * sc + rc * ss;
+          rc = c2;
+        }
       }
     }
-    __syncwarp();
   }
 }
 
@@ -167,14 +175,17 @@ __device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, f
 // pairs of blocks per CTA of 256 threads.
 __global__ void __launch_bounds__(256, 4) fstep_block_kernel(const StreamDev *__restrict__ streams,
                                                          const float2 *__restrict__ tw) {
-  __shared__ float2 sbuf[16][kNd + kNd / 16];
+  extern __shared__ __align__(16) float2 sbuf[];  // 16 x kFsScratch
+  __shared__ float4 ptab[2 * pass_table_len<8>()];
   const int t = threadIdx.x & 15, grp = threadIdx.x >> 4, warp = threadIdx.x >> 5;
   const StreamDev &s = streams[blockIdx.y];
   float *ts = s.ts;
+  fill_pass_table<8>(ptab, tw, threadIdx.x, blockDim.x);
+  __syncthreads();
   // 32 blocks per CTA and round, rounds strided over the stream's blocks
   for (int first = blockIdx.x * 32; first < s.n_blocks; first += gridDim.x * 32) {
     if (first + warp * 4 >= s.n_blocks) break;  // whole warps only (warp barriers); later rounds lie further out
-    fstep_pair(s, first + grp * 2, t, sbuf[grp], tw,
+    fstep_pair(s, first + grp * 2, t, sbuf + grp * kFsScratch, tw, ptab,
                [ts](int bl, int n, float x) { ts[(int64_t)bl * kNd + n] = x; });
   }
 }
@@ -332,17 +343,18 @@ __device__ __forceinline__ void window_raw(float2 (&v)[16], int t, bool ok, int 
     v[qq] = x;
   }
 }
-template <int T>
-__device__ __forceinline__ void window_apply(float2 (&v)[16], int t, int nper, float sgn,
-                                             const float *__restrict__ window) {
+// The window is in shared memory (WSMEM) or read through the read-only cache.
+template <int T, bool WSMEM>
+__device__ __forceinline__ void window_apply(float2 (&v)[16], int t, int nper, float sgn, const float *window) {
 #pragma unroll
   for (int qq = 0; qq < 16; qq++) {
     const int i = 2 * (t + qq * T);
     if (i + 1 < nper) {
-      const float2 w = __ldg(reinterpret_cast<const float2 *>(window + i));
+      const float2 w = WSMEM ? *reinterpret_cast<const float2 *>(window + i)
+                             : __ldg(reinterpret_cast<const float2 *>(window + i));
       v[qq] = make_float2(v[qq].x * w.x, sgn * (v[qq].y * w.y));
     } else if (i < nper) {
-      v[qq] = make_float2(v[qq].x * __ldg(window + i), 0.f);
+      v[qq] = make_float2(v[qq].x * (WSMEM ? window[i] : __ldg(window + i)), 0.f);
     }
   }
 }
@@ -448,7 +460,11 @@ struct WinShape {
   static constexpr int RPC = T < 256 ? 256 / T : 1;                   // rows per step
   static constexpr int THREADS = SPC * RPC * T;
   static constexpr int BUF = N + N / 16;  // padded FFT buffer (float2) of one group
-  static constexpr size_t SMEM = (size_t)SPC * RPC * BUF * sizeof(float2);
+  static constexpr size_t FFT_SMEM = (size_t)SPC * RPC * BUF * sizeof(float2);
+  static constexpr int PT = pass_table_len<LOGN>();  // float4 pairs of the pass twiddle table
+  // the window (up to rot = 2N floats) joins the shared tables when it fits
+  static constexpr bool WSMEM = FFT_SMEM + 32 * PT + 8 * N <= 227 * 1024;
+  static constexpr size_t SMEM = FFT_SMEM + 32 * PT + (WSMEM ? 8 * N : 0);
   static_assert(THREADS <= 1024, "at most 1024 threads");
 };
 
@@ -460,7 +476,7 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
     void *__restrict__ spec_out, float tc_scale) {
   using S = WinShape<LOGN, SPCMAX>;
   constexpr int N = S::N, T = S::T, SPC = S::SPC, RPC = S::RPC;
-  extern __shared__ float2 dsm[];
+  extern __shared__ __align__(16) float2 dsm[];
   const int t = threadIdx.x % T, g = threadIdx.x / T;
   const int nsg = (nstreams + SPC - 1) / SPC;
   const int sg = blockIdx.x % nsg;  // stream group fastest
@@ -473,17 +489,27 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
   auto row_of = [&](int k) { return k * RPC + g / SPC; };
   float2 v[16];
   if (k0 < k1) window_raw<T>(v, t, sok && row_of(k0) < nrows, nper, s.ts + (int64_t)(row0 + row_of(k0)) * N);
+  // shared tables behind the FFT buffers: pass twiddles, then the window
+  float4 *ptab = reinterpret_cast<float4 *>(dsm + S::FFT_SMEM / sizeof(float2));
+  fill_pass_table<LOGN>(ptab, tw_rot + 2 * N, threadIdx.x, S::THREADS);
+  const float *win = window;
+  if constexpr (S::WSMEM) {
+    float4 *wsm = ptab + 2 * S::PT;  // nper is a multiple of 4 (rot >= 512)
+    for (int i = threadIdx.x; i < nper / 4; i += S::THREADS) wsm[i] = __ldg(reinterpret_cast<const float4 *>(window) + i);
+    win = reinterpret_cast<const float *>(wsm);
+  }
+  __syncthreads();
 #pragma unroll 1
   for (int k = k0; k < k1; k++) {
-    window_apply<T>(v, t, nper, sgn, window);
+    window_apply<T, S::WSMEM>(v, t, nper, sgn, win);
     // tw_rot holds exp(-2 pi i m / rot) for m < rot, followed by exp(-2 pi i m / N) for m < N.
     // Each group's transform synchronises only its own T threads (named
     // barrier 1 + g) when the groups are whole warps and few enough.
     if constexpr (T >= 32 && S::THREADS / T <= 15) {
-      fft_reg<-1, LOGN, true>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, GroupSync{1 + g, T});
+      fft_reg<-1, LOGN, true>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, ptab, GroupSync{1 + g, T});
       __syncthreads();  // the stores read every group's transform
     } else {
-      fft_reg<-1, LOGN, true>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, BlockSync());
+      fft_reg<-1, LOGN, true>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, ptab, BlockSync());
     }
     if (k + 1 < k1)  // hop = rot / 2
       window_raw<T>(v, t, sok && row_of(k + 1) < nrows, nper, s.ts + (int64_t)(row0 + row_of(k + 1)) * N);
@@ -499,7 +525,7 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
 }
 
 // ------------------------------------------------------------------------
-// Bit statistics over counted-byte ranges.  Work items: (stream, range, offset).
+// Bit statistics.
 // Code counts of 8 bits (mask 0x55) or 32 bits (mask 0x55555555): 2-bit
 // codes -> c[code] with code = 2 * high bit + low bit; 1-bit -> c[bit value].
 __device__ __forceinline__ void count_codes(uint32_t x, int nbits, int bits, uint32_t (&c)[4]) {
@@ -890,7 +916,9 @@ void launch_fstep_block(const StreamDev *d_streams, int nstreams, int max_blocks
   // about two waves of 4 resident CTAs per SM, each CTA looping over rounds
   const int per_stream = std::max(1, 8 * sm_count() / nstreams);
   dim3 grid(std::min((max_blocks + 31) / 32, per_stream), nstreams);
-  fstep_block_kernel<<<grid, 256, 0, st>>>(d_streams, tw256);
+  constexpr int smem = 16 * kFsScratch * sizeof(float2);
+  cudaFuncSetAttribute(fstep_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  fstep_block_kernel<<<grid, 256, smem, st>>>(d_streams, tw256);
 }
 
 void launch_unpack(const StreamDev *d_streams, int nstreams, int max_blocks, float *out, cudaStream_t st) {
