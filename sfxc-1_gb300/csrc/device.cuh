@@ -115,10 +115,12 @@ struct GroupSync {
 };
 
 // 2-bit code -> sample value, the Bit2float_worker table (sfxc/src/bit2float_worker.cc:4-10):
-// 0 -> -7, 1 -> -2, 2 -> +2, 3 -> +7.
+// 0 -> -7, 1 -> -2, 2 -> +2, 3 -> +7.  The four values differ only in their
+// two high bytes (0xC0E0, 0xC000, 0x4000, 0x40E0), so one byte permute picks
+// them from two table words: result byte 3 = {C0,C0,40,40}[c], byte 2 =
+// {E0,00,00,E0}[c], bytes 0-1 a zero byte of the second word.
 __device__ __forceinline__ float code_value2(uint32_t c) {
-  const float mag = ((c ^ (c >> 1)) & 1) ? 2.0f : 7.0f;
-  return (c & 2) ? mag : -mag;
+  return __int_as_float((int)__byte_perm(0x4040C0C0u, 0xE00000E0u, c * 0x1100u + 0x0455u));
 }
 
 // Unpacked sample `o` (index within the integration) through the plan;

@@ -359,87 +359,80 @@ __device__ __forceinline__ void window_apply(float2 (&v)[16], int t, int nper, f
   }
 }
 
-// Output row `row` of the NS streams sg0 + j (j < NS) of the launch, whose
-// transforms are at Z + j * BUF; each goes to its slot in the spectra layout.
-// Threads tid = 0..nthr-1 share the channels 0..M.
+// Output row `row` of the NV <= NS streams of a CTA, whose transforms are at
+// Z + j * BUF; each goes to its slot in the spectra layout.  sinfo[j] =
+// (channel shift output_offset - temp_fft_offset, slot), staged once per CTA.
+// `fast`: four (or NS) streams with no shift in consecutive slots from a
+// multiple of four, M == N.  Threads tid = 0..nthr-1 share the channels 0..M;
+// bins q and N - q come together, so the N/2 + 1 pairs spread evenly (bin N/2
+// goes to the last threads on its own).
 template <int N, int NS, int OUT_TC>
-__device__ __forceinline__ void store_row(const float2 *Z, int BUF, const StreamDev *__restrict__ streams,
-                                          int nstreams, int sg0, int row, int nrows_total, int M, int kpad,
-                                          const float2 *__restrict__ tw_rot, void *__restrict__ spec_out,
-                                          float tc_scale, int tid, int nthr) {
+__device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *sinfo, int NV, bool fast, int row,
+                                          int nrows_total, int M, int kpad, const float2 *__restrict__ tw_rot,
+                                          void *__restrict__ spec_out, float tc_scale, int tid, int nthr) {
+  static_assert(NS <= 4, "at most four streams per CTA");
   if (OUT_TC) {
-    constexpr int W = NS < 4 ? NS : 4;  // streams per store
-    auto put = [](uint2 *p, const uint2 (&o)[W]) {
-      if constexpr (W == 1) {
-        *p = o[0];
-      } else if constexpr (W == 2) {
-        *reinterpret_cast<uint4 *>(p) = make_uint4(o[0].x, o[0].y, o[1].x, o[1].y);
-      } else {
-        asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(o[0].x), "r"(o[0].y),
-                     "r"(o[1].x), "r"(o[1].y), "r"(o[2].x), "r"(o[2].y), "r"(o[3].x), "r"(o[3].y)
-                     : "memory");
-      }
-    };
-#pragma unroll 1
-    for (int j0 = 0; j0 < NS && sg0 + j0 < nstreams; j0 += W) {
-      int shift[W], slot[W];
-      bool aligned = M == N;  // every stream's channel i is its bin i
-      bool packed = sg0 + j0 + W <= nstreams;  // W real streams in consecutive, aligned slots
+    constexpr int W = NS;  // streams per store
+    uint2 *dst = reinterpret_cast<uint2 *>(spec_out) + (int64_t)row * kpad * kTcSlots;
+    if (fast) {
+      auto put = [](uint2 *p, const uint2 (&o)[W]) {
+        if constexpr (W == 1) {
+          *p = o[0];
+        } else if constexpr (W == 2) {
+          *reinterpret_cast<uint4 *>(p) = make_uint4(o[0].x, o[0].y, o[1].x, o[1].y);
+        } else if constexpr (W == 4) {
+          asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(o[0].x), "r"(o[0].y),
+                       "r"(o[1].x), "r"(o[1].y), "r"(o[2].x), "r"(o[2].y), "r"(o[3].x), "r"(o[3].y)
+                       : "memory");
+        } else {
 #pragma unroll
-      for (int j = 0; j < W; j++) {
-        const int st = min(sg0 + j0 + j, nstreams - 1);
-        shift[j] = streams[st].output_offset - streams[st].temp_fft_offset;
-        slot[j] = streams[st].slot;
-        aligned = aligned && shift[j] == 0;
-        packed = packed && slot[j] == slot[0] + j;
-      }
-      packed = packed && slot[0] % W == 0;
-      uint2 *dst = reinterpret_cast<uint2 *>(spec_out) + (int64_t)row * kpad * kTcSlots;
-      if (!packed) {  // streams of a subset launch: one 8-byte store per stream
-        for (int i = tid; i <= M; i += nthr)
-#pragma unroll
-          for (int j = 0; j < W; j++)
-            if (sg0 + j0 + j < nstreams)
-              dst[(int64_t)i * kTcSlots + slot[j]] =
-                  tc_split(real_bin<N>(Z + (j0 + j) * BUF, tw_rot, shift[j] + i), tc_scale);
-        continue;
-      }
-      dst += slot[0];
-      if (aligned) {
-        for (int i = tid; i <= N / 2; i += nthr) {
-          const float2 w = __ldg(tw_rot + i);
-          uint2 a[W], b[W];
-#pragma unroll
-          for (int j = 0; j < W; j++) {
-            float2 xq, xnq;
-            real_bin_pair<N>(Z + (j0 + j) * BUF, w, i, xq, xnq);
-            a[j] = tc_split(xq, tc_scale);
-            b[j] = tc_split(xnq, tc_scale);
-          }
-          put(dst + (int64_t)i * kTcSlots, a);
-          if (i < N / 2) put(dst + (int64_t)(N - i) * kTcSlots, b);
+          for (int j = 0; j < W; j++) p[j] = o[j];
         }
-      } else {
-        for (int i = tid; i <= M; i += nthr) {
-          uint2 o[W];
+      };
+      dst += sinfo[0].y;
+      for (int i = tid; i < N / 2; i += nthr) {
+        const float2 w = __ldg(tw_rot + i);
+        uint2 a[W], b[W];
 #pragma unroll
-          for (int j = 0; j < W; j++) o[j] = tc_split(real_bin<N>(Z + (j0 + j) * BUF, tw_rot, shift[j] + i), tc_scale);
-          put(dst + (int64_t)i * kTcSlots, o);
+        for (int j = 0; j < W; j++) {
+          float2 xq, xnq;
+          real_bin_pair<N>(Z + j * BUF, w, i, xq, xnq);
+          a[j] = tc_split(xq, tc_scale);
+          b[j] = tc_split(xnq, tc_scale);
         }
+        put(dst + (int64_t)i * kTcSlots, a);
+        put(dst + (int64_t)(N - i) * kTcSlots, b);
       }
+      if (tid >= nthr - W) {  // bin N/2, one stream per thread
+        const int j = tid - (nthr - W);
+        float2 xq, xnq;
+        real_bin_pair<N>(Z + j * BUF, __ldg(tw_rot + N / 2), N / 2, xq, xnq);
+        dst[(int64_t)(N / 2) * kTcSlots + j] = tc_split(xq, tc_scale);
+      }
+      return;
     }
+    // shifted channels or scattered slots: one 8-byte store per stream and channel
+    for (int i = tid; i <= M; i += nthr)
+#pragma unroll
+      for (int j = 0; j < NS; j++)
+        if (j < NV)
+          dst[(int64_t)i * kTcSlots + sinfo[j].y] = tc_split(real_bin<N>(Z + j * BUF, tw_rot, sinfo[j].x + i), tc_scale);
   } else {
 #pragma unroll 1
-    for (int j = 0; j < NS && sg0 + j < nstreams; j++) {
-      const int st = sg0 + j;
-      const int shift = streams[st].output_offset - streams[st].temp_fft_offset;
-      float2 *dst = reinterpret_cast<float2 *>(spec_out) + ((int64_t)streams[st].slot * nrows_total + row) * kpad;
+    for (int j = 0; j < NV; j++) {
+      const int shift = sinfo[j].x;
+      float2 *dst = reinterpret_cast<float2 *>(spec_out) + ((int64_t)sinfo[j].y * nrows_total + row) * kpad;
       if (shift == 0 && M == N) {
-        for (int i = tid; i <= N / 2; i += nthr) {
+        for (int i = tid; i < N / 2; i += nthr) {
           float2 xq, xnq;
           real_bin_pair<N>(Z + j * BUF, __ldg(tw_rot + i), i, xq, xnq);
           dst[i] = xq;
-          if (i < N / 2) dst[N - i] = xnq;
+          dst[N - i] = xnq;
+        }
+        if (tid == nthr - 1 - j) {
+          float2 xq, xnq;
+          real_bin_pair<N>(Z + j * BUF, __ldg(tw_rot + N / 2), N / 2, xq, xnq);
+          dst[N / 2] = xq;
         }
       } else {
         for (int i = tid; i <= M; i += nthr) dst[i] = real_bin<N>(Z + j * BUF, tw_rot, shift + i);
@@ -492,6 +485,14 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
   // shared tables behind the FFT buffers: pass twiddles, then the window
   float4 *ptab = reinterpret_cast<float4 *>(dsm + S::FFT_SMEM / sizeof(float2));
   fill_pass_table<LOGN>(ptab, tw_rot + 2 * N, threadIdx.x, S::THREADS);
+  // the CTA's streams: channel shift and slot, and whether the whole-sector path applies
+  __shared__ int2 sinfo[SPC];
+  if (threadIdx.x < SPC) {
+    const int st = sg * SPC + threadIdx.x;
+    sinfo[threadIdx.x] = st < nstreams
+                             ? make_int2(streams[st].output_offset - streams[st].temp_fft_offset, streams[st].slot)
+                             : make_int2(0, -1);
+  }
   const float *win = window;
   if constexpr (S::WSMEM) {
     float4 *wsm = ptab + 2 * S::PT;  // nper is a multiple of 4 (rot >= 512)
@@ -499,6 +500,10 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
     win = reinterpret_cast<const float *>(wsm);
   }
   __syncthreads();
+  const int nv = min(SPC, nstreams - sg * SPC);
+  bool fast = OUT_TC && M == N && nv == SPC && sinfo[0].y % SPC == 0;
+#pragma unroll
+  for (int j = 0; j < SPC; j++) fast = fast && sinfo[j].x == 0 && sinfo[j].y == sinfo[0].y + j;
 #pragma unroll 1
   for (int k = k0; k < k1; k++) {
     window_apply<T, S::WSMEM>(v, t, nper, sgn, win);
@@ -517,8 +522,8 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
     for (int r = 0; r < RPC; r++) {
       const int row = k * RPC + r;
       if (row >= nrows) break;
-      store_row<N, SPC, OUT_TC>(dsm + r * SPC * S::BUF, S::BUF, streams, nstreams, sg * SPC, row0 + row,
-                                nrows_total, M, kpad, tw_rot, spec_out, tc_scale, threadIdx.x, S::THREADS);
+      store_row<N, SPC, OUT_TC>(dsm + r * SPC * S::BUF, S::BUF, sinfo, nv, fast, row0 + row, nrows_total, M, kpad,
+                                tw_rot, spec_out, tc_scale, threadIdx.x, S::THREADS);
     }
     __syncthreads();  // the next step's FFT rewrites the buffers
   }
