@@ -161,7 +161,7 @@ int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t 
  * cannot wait on the allocator, and hosts that carve up GPU memory once at
  * start-up.  Its scratch -- the fringe-stopped samples, the per-block delay
  * parameters, the stream descriptor and the spectra before the copy out --
- * lives in one static device array of 16.2 MiB that every GPU loading the
+ * lives in one static device array of 16.4 MiB that every GPU loading the
  * library holds until the process exits.  Limits: at most 8192 blocks of
  * fft_size_delaycor samples (2,097,152 samples) per stream and integration,
  * and at most 2^20 values of nffts x (fft_size_correlation + 4); larger

@@ -101,15 +101,14 @@ struct StreamCtx {
   BitStats stats{};
   Spline sp;
   int n_blocks = 0, nfft_max = 0, rot = 0, hop = 0;
-  DevBuf src, segs, stat_rng, spline, hist, bparams, bamp;
+  DevBuf src, segs, stat_rng, spline, hist, bpar;
   void take_buffers(StreamCtx &o) {
     src.swap(o.src);
     segs.swap(o.segs);
     stat_rng.swap(o.stat_rng);
     spline.swap(o.spline);
     hist.swap(o.hist);
-    bparams.swap(o.bparams);
-    bamp.swap(o.bamp);
+    bpar.swap(o.bpar);
   }
 };
 
@@ -568,8 +567,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   c->derr.ensure(sizeof(int));
   CK(cudaMemsetAsync(c->derr.p, 0, sizeof(int), st));
   for (int i = 0; i < N; i++) {
-    c->sc[i].bparams.ensure((size_t)max_blocks * sizeof(float4));
-    c->sc[i].bamp.ensure((size_t)max_blocks * sizeof(float));
+    c->sc[i].bpar.ensure((size_t)max_blocks * sizeof(BlockPar));
   }
   float t_f1 = 0, t_f2 = 0, t_x = 0;
   // pulsar setup (Correlation_core_pulsar::set_parameters, correlation_core_pulsar.cc:46-95)
@@ -644,8 +642,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       const int b0 = chunked ? r0 * c->sc[i].hop / kNd : 0;
       const int b1 = chunked ? std::min(c->sc[i].n_blocks, (r1 + 1 + minus) * c->sc[i].hop / kNd) : c->sc[i].n_blocks;
       d.ts = c->ts.as<float>() + (size_t)i * max_blocks * kNd;
-      d.bparams = c->sc[i].bparams.as<float4>();
-      d.bamp = c->sc[i].bamp.as<float>();
+      d.bpar = c->sc[i].bpar.as<BlockPar>();
       d.block0 = b0;
       d.n_blocks = b1 - b0;
       staged[ch * per_chunk + i] = d;
@@ -904,14 +901,12 @@ int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n)
     d.block0 = 0;
     d.n_blocks = s.n_blocks;
     d.slot = 0;  // the only stream of this launch
-    DevBuf ts, spec, sd, bp, ba;
+    DevBuf ts, spec, sd, bp;
     ts.ensure((size_t)s.n_blocks * kNd * sizeof(float));
     spec.ensure(rows * c->kpad * sizeof(float2));
-    bp.ensure((size_t)s.n_blocks * sizeof(float4));
-    ba.ensure((size_t)s.n_blocks * sizeof(float));
+    bp.ensure((size_t)s.n_blocks * sizeof(BlockPar));
     d.ts = ts.as<float>();
-    d.bparams = bp.as<float4>();
-    d.bamp = ba.as<float>();
+    d.bpar = bp.as<BlockPar>();
     upload(sd, &d, sizeof(StreamDev), c->st);
     launch_fstep_block(sd.as<StreamDev>(), 1, s.n_blocks, c->tw256.as<float2>(), c->st);
     const int nper = c->p.window == WINDOW_NONE ? s.hop : s.rot;
@@ -946,10 +941,9 @@ constexpr int kNoallocMaxBlocks = 8192;                 // 2,097,152 samples of 
 constexpr size_t kNoallocMaxSpectra = (size_t)1 << 20;  // rows x (fft_size_correlation + 4) complex values
 constexpr size_t kNoallocTsOff = 0;
 constexpr size_t kNoallocParOff = kNoallocTsOff + (size_t)kNoallocMaxBlocks * kNd * sizeof(float);
-constexpr size_t kNoallocAmpOff = kNoallocParOff + (size_t)kNoallocMaxBlocks * sizeof(float4);
-constexpr size_t kNoallocDescOff = kNoallocAmpOff + (size_t)kNoallocMaxBlocks * sizeof(float);
+constexpr size_t kNoallocDescOff = kNoallocParOff + (size_t)kNoallocMaxBlocks * sizeof(BlockPar);
 constexpr size_t kNoallocSpecOff = kNoallocDescOff + 1024;
-constexpr size_t kNoallocBytes = kNoallocSpecOff + kNoallocMaxSpectra * sizeof(float2);  // 16.2 MiB
+constexpr size_t kNoallocBytes = kNoallocSpecOff + kNoallocMaxSpectra * sizeof(float2);  // 16.4 MiB
 static_assert(sizeof(StreamDev) <= 1024, "stream descriptor slot too small");
 
 // Held by every GPU that loads the library until the process exits.
@@ -996,8 +990,7 @@ int sfxc_gpu_copy_spectra_noalloc(sfxc_gpu_ctx *c, int32_t stream, float *out, s
     d.n_blocks = s.n_blocks;
     d.slot = 0;  // the only stream of this launch
     d.ts = reinterpret_cast<float *>(base + kNoallocTsOff);
-    d.bparams = reinterpret_cast<float4 *>(base + kNoallocParOff);
-    d.bamp = reinterpret_cast<float *>(base + kNoallocAmpOff);
+    d.bpar = reinterpret_cast<BlockPar *>(base + kNoallocParOff);
     StreamDev *dd = reinterpret_cast<StreamDev *>(base + kNoallocDescOff);
     float2 *spec = reinterpret_cast<float2 *>(base + kNoallocSpecOff);
     // every scratch element read below is written first by the same call, so

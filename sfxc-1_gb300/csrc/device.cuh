@@ -21,6 +21,23 @@ struct DevStatRange {
   int32_t n, cidx;
 };
 
+// Per-block record of the F-step, written by block_params_kernel for the
+// blocks of one launch.
+struct BlockPar {
+  // phase-ramp start (rad, [0,2pi)), ramp step per bin, fringe phase at the
+  // block start, fringe phase step per sample
+  float4 ph;
+  // cos and sin of 16 ramp steps, cos and sin of 16 fringe steps (the
+  // per-thread recurrences of the block stage)
+  float4 steps;
+  // bit of the block's first sample in the source when this block and the
+  // next both lie inside one segment of recorded samples, else -1
+  long long src_bit;
+  float amp;  // amplitude at the block centre
+  int32_t pad;
+};
+static_assert(sizeof(BlockPar) == 48, "BlockPar layout");
+
 // Per-stream parameters of the F-step kernels (one integration).
 struct StreamDev {
   const uint8_t *src;          // source bytes (protocol buffer or channel stream)
@@ -51,11 +68,8 @@ struct StreamDev {
   // delay-model shortcuts, exact: an all-zero phase column evaluates to 0.0,
   // an all-one amplitude column to 1.0, a zero clock model to a zero drift
   int32_t phase_zero, amp_one, no_clock;
-  // per-block parameters of this launch's blocks (block_params_kernel):
-  // {phase-ramp start (rad, [0,2pi)), ramp step per bin, fringe phase at the
-  // block start, fringe phase step per sample}, and the amplitude
-  float4 *bparams;
-  float *bamp;
+  // per-block records of this launch's blocks (block_params_kernel)
+  BlockPar *bpar;
   // outputs
   float *ts;                   // fringe-stopped series, n_blocks*256 floats
   unsigned long long *hist;    // 8 code counters: cal diode on [0..3], off [4..7]

@@ -126,45 +126,62 @@ __device__ __forceinline__ void twiddle16(float2 (&v)[16], float2 w1, float2 w2,
   for (int r = 9; r < 16; r++) v[r] = cmulw<SIGN>(v[r], cmul(w8, w[r - 8]));
 }
 
-// Twiddles of the radix-16 passes after the first, in shared memory: the
+// Twiddles of the radix-16 passes after the first, in shared memory.  The
 // pass of stride Ns (16, 256, ...) uses entries e = (Ns - 16) / 15 + k for
-// k < Ns, tab[e] = {W^m, W^2m} and tab[L + e] = {W^4m, W^8m} with
-// m = k N / (16 Ns), W = exp(-2 pi i / N), L = pass_table_len<LOGN>().
-// Consecutive threads read consecutive 16-byte entries (no bank conflicts,
-// where the table tw read by those indices scatters over a stride of 8 m).
+// k < Ns, L = pass_table_len<LOGN>() entries in all; m = k N / (16 Ns) and
+// W = exp(-2 pi i / N).  Two layouts (TWK):
+//   15: tab[(r - 1) L + e] = W^(r m), r = 1..15, 15 L float2: every twiddle
+//       a correctly rounded table value, no products;
+//    4: tab[e] = {W^m, W^2m}, tab[L + e] = {W^4m, W^8m}, 2 L float4: a quarter
+//       of the space, the other eleven twiddles as products of these.
+// Either way consecutive threads read consecutive entries (no bank conflicts).
 template <int LOGN>
 __host__ __device__ constexpr int pass_table_len() {
   int n = 1;
   for (int p = 0; p < LOGN / 4; p++) n *= 16;
   return (n - 16) / 15;
 }
-// Fill the 2 L float4 of the table from tw[j] = exp(-2 pi i j / N) by
-// threads tid = 0..nthr-1 (the caller synchronises before use).
-template <int LOGN>
-__device__ __forceinline__ void fill_pass_table(float4 *tab, const float2 *__restrict__ tw, int tid, int nthr) {
+template <int LOGN, int TWK>
+__host__ __device__ constexpr int pass_table_bytes() {
+  return pass_table_len<LOGN>() * (TWK == 15 ? 15 * 8 : 32);
+}
+// Fill the table from tw[j] = exp(-2 pi i j / N) by threads tid = 0..nthr-1
+// (the caller synchronises before use).
+template <int LOGN, int TWK>
+__device__ __forceinline__ void fill_pass_table(void *tab, const float2 *__restrict__ tw, int tid, int nthr) {
   constexpr int N = 1 << LOGN, L = pass_table_len<LOGN>();
-  for (int e = tid; e < L; e += nthr) {
+  static_assert(TWK == 4 || TWK == 15, "table layout");
+  auto m_of = [](int e) {
     int Ns = 16;
     while (e >= (16 * Ns - 16) / 15) Ns *= 16;
-    const int m = (e - (Ns - 16) / 15) * (N / (16 * Ns));
-    const float2 w1 = __ldg(tw + m), w2 = __ldg(tw + 2 * m), w4 = __ldg(tw + 4 * m), w8 = __ldg(tw + 8 * m);
-    tab[e] = make_float4(w1.x, w1.y, w2.x, w2.y);
-    tab[L + e] = make_float4(w4.x, w4.y, w8.x, w8.y);
+    return (e - (Ns - 16) / 15) * (N / (16 * Ns));
+  };
+  if constexpr (TWK == 15) {
+    float2 *t15 = static_cast<float2 *>(tab);
+    for (int i = tid; i < 15 * L; i += nthr) t15[i] = __ldg(tw + (1 + i / L) * m_of(i % L));  // r m < N
+  } else {
+    float4 *t4 = static_cast<float4 *>(tab);
+    for (int e = tid; e < L; e += nthr) {
+      const int m = m_of(e);
+      const float2 w1 = __ldg(tw + m), w2 = __ldg(tw + 2 * m), w4 = __ldg(tw + 4 * m), w8 = __ldg(tw + 8 * m);
+      t4[e] = make_float4(w1.x, w1.y, w2.x, w2.y);
+      t4[L + e] = make_float4(w4.x, w4.y, w8.x, w8.y);
+    }
   }
 }
 
 // Transform of N = 2^LOGN points by T = N/16 threads (t = 0..T-1).
 // In: v[r] = x[t + r T].  `sm`: this transform's buffer of padi(N) float2.
 // `tw`: exp(-2 pi i j / N) for j < N (final radix-2/4/8 pass); `ptab`: the
-// radix-16 passes' table in shared memory (fill_pass_table).  `sync` is the
+// radix-16 passes' table of layout TWK in shared memory (fill_pass_table).  `sync` is the
 // barrier over all threads sharing the barrier (warp or CTA); every one of
 // them must call this.
 // Out (TO_SMEM): X[k] at sm[padi(k)], visible after the final barrier.
 // Out (!TO_SMEM, LOGN % 4 == 0 only): v[r] = X[t + r T]; sm is free again
 // once every thread has returned (the caller syncs before reusing it).
-template <int SIGN, int LOGN, bool TO_SMEM, typename Sync>
+template <int SIGN, int LOGN, bool TO_SMEM, int TWK, typename Sync>
 __device__ __forceinline__ void fft_reg(float2 (&v)[16], float2 *sm, int t, const float2 *__restrict__ tw,
-                                        const float4 *ptab, Sync sync) {
+                                        const void *ptab, Sync sync) {
   constexpr int N = 1 << LOGN, T = N / 16, NR16 = LOGN / 4, LAST = LOGN % 4;
   static_assert(NR16 >= 1, "at least 16 points");
   static_assert(TO_SMEM || LAST == 0, "register output needs a final radix-16 pass");
@@ -181,8 +198,15 @@ __device__ __forceinline__ void fft_reg(float2 (&v)[16], float2 *sm, int t, cons
       sync();
       constexpr int L = pass_table_len<LOGN>();
       const int e = (Ns - 16) / 15 + (t & (Ns - 1));
-      const float4 a = ptab[e], b = ptab[L + e];
-      twiddle16<SIGN>(v, make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(b.x, b.y), make_float2(b.z, b.w));
+      if constexpr (TWK == 15) {
+        const float2 *pt = static_cast<const float2 *>(ptab) + e;
+#pragma unroll
+        for (int r = 1; r < 16; r++) v[r] = cmulw<SIGN>(v[r], pt[(r - 1) * L]);
+      } else {
+        const float4 a = static_cast<const float4 *>(ptab)[e], b = static_cast<const float4 *>(ptab)[L + e];
+        twiddle16<SIGN>(v, make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(b.x, b.y),
+                        make_float2(b.z, b.w));
+      }
     }
     dft16<SIGN>(v);
     if (p == NR16 - 1 && LAST == 0 && !TO_SMEM) return;  // v[r] = X[t + r T]

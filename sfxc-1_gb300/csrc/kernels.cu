@@ -51,20 +51,17 @@ __device__ __forceinline__ void pair_from_scratch(float2 (&v)[16], const float *
 constexpr int kFsScratch = kNd + kNd / 16 + 9 * 16;
 template <class Store>
 __device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, float2 *sm,
-                                           const float2 *__restrict__ tw, const float4 *ptab, Store store) {
+                                           const float2 *__restrict__ tw, const float2 *ptab, Store store) {
   const bool ok0 = bl0 < s.n_blocks, ok1 = bl0 + 1 < s.n_blocks;
   float2 v[16];
   {  // unpack the two blocks through the plan
-    const int o0 = (s.block0 + bl0) * kNd;
-    int si = ok0 ? find_segment(s, o0) : 0;
-    const DevSegment sg = s.segs[si];
-    if (ok1 && sg.src_bit >= 0 && o0 >= sg.out0 && o0 + 2 * kNd <= sg.out0 + sg.n) {
+    const long long bit0 = ok0 ? s.bpar[bl0].src_bit : -1;
+    if (bit0 >= 0) {
       // common case: both blocks inside one segment of recorded samples, so
       // sample t + 16 r (r < 32 over the pair) sits at bit p + 16 r * bits of
       // the stream; whole 32-bit words and funnel shifts, no segment walk
       // (the input buffer has spare bytes after the last sample)
       const uint32_t *w = reinterpret_cast<const uint32_t *>(s.src);
-      const int64_t bit0 = sg.src_bit + (int64_t)(o0 - sg.out0) * s.bits;
       if (s.bits == 2) {
         const int64_t p = bit0 + 2 * t;
         const int64_t w0 = p >> 5;
@@ -90,6 +87,8 @@ __device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, f
         pair_from_scratch(v, xs, t);
       }
     } else {  // segment boundaries inside the pair: rare per-sample walk, rolled, through the scratch
+      const int o0 = (s.block0 + bl0) * kNd;
+      int si = ok0 ? find_segment(s, o0) : 0;
       float *xs = reinterpret_cast<float *>(sm);
 #pragma unroll 1
       for (int r = 0; r < 32; r++) xs[t + 16 * r] = (r < 16 ? ok0 : ok1) ? gather_sample(s, o0 + t + 16 * r, si) : 0.0f;
@@ -101,8 +100,8 @@ __device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, f
   // inverse of block h - 1.  Block 1's ramped half spectrum waits in the
   // scratch behind the transform buffer, ext[16 r + t] for r < 9.
   float2 *ext = sm + kNd + kNd / 16;
-  const float4 p0 = ok0 ? s.bparams[bl0] : make_float4(0.f, 0.f, 0.f, 0.f);
-  const float4 p1 = ok1 ? s.bparams[bl0 + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 p0 = ok0 ? s.bpar[bl0].ph : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 p1 = ok1 ? s.bpar[bl0 + 1].ph : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
   for (int h = 0; h < 3; h++) {
     if (h == 2) {
@@ -112,17 +111,18 @@ __device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, f
       for (int r = 9; r < 16; r++) v[r] = make_float2(0.f, 0.f);
     }
     // v[r] = X[t + 16 r]; the transform's reads of sm are complete on return
-    fft_reg<-1, 8, false>(v, sm, t, tw, ptab, WarpSync());
+    fft_reg<-1, 8, false, 15>(v, sm, t, tw, ptab, WarpSync());
     if (h == 0) {
       // split, halve DC/Nyquist, phase ramp; conj of block 0 into v, of block 1 into ext
 #pragma unroll
       for (int r = 0; r < 16; r++) sm[padi(t + 16 * r)] = v[r];
       __syncwarp();
-      float a_s, a_c, as_s, as_c, b_s, b_c, bs_s, bs_c;
+      float a_s, a_c, b_s, b_c;
       sincosf(fmaf((float)t, p0.y, p0.x), &a_s, &a_c);
-      sincosf(16.0f * p0.y, &as_s, &as_c);
       sincosf(fmaf((float)t, p1.y, p1.x), &b_s, &b_c);
-      sincosf(16.0f * p1.y, &bs_s, &bs_c);
+      const float4 st0 = ok0 ? s.bpar[bl0].steps : make_float4(1.f, 0.f, 1.f, 0.f);
+      const float4 st1 = ok1 ? s.bpar[bl0 + 1].steps : make_float4(1.f, 0.f, 1.f, 0.f);
+      const float as_c = st0.x, as_s = st0.y, bs_c = st1.x, bs_s = st1.y;
 #pragma unroll
       for (int r = 0; r < 9; r++) {
         const int k = t + 16 * r;
@@ -153,10 +153,11 @@ __device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, f
       const int bl = bl0 + h - 1;
       if (bl < s.n_blocks) {
         const float4 prm = h == 2 ? p1 : p0;
-        const float amp = s.bamp[bl];
-        float rs, rc, ss, sc;
+        const float amp = s.bpar[bl].amp;
+        const float4 st = s.bpar[bl].steps;
+        const float sc = st.z, ss = st.w;
+        float rs, rc;
         sincosf(fmaf((float)t, prm.w, prm.z), &rs, &rc);
-        sincosf(16.0f * prm.w, &ss, &sc);
         rs *= amp;
         rc *= amp;
 #pragma unroll
@@ -176,11 +177,11 @@ __device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, f
 __global__ void __launch_bounds__(256, 4) fstep_block_kernel(const StreamDev *__restrict__ streams,
                                                          const float2 *__restrict__ tw) {
   extern __shared__ __align__(16) float2 sbuf[];  // 16 x kFsScratch
-  __shared__ float4 ptab[2 * pass_table_len<8>()];
+  __shared__ float2 ptab[15 * pass_table_len<8>()];
   const int t = threadIdx.x & 15, grp = threadIdx.x >> 4, warp = threadIdx.x >> 5;
   const StreamDev &s = streams[blockIdx.y];
   float *ts = s.ts;
-  fill_pass_table<8>(ptab, tw, threadIdx.x, blockDim.x);
+  fill_pass_table<8, 15>(ptab, tw, threadIdx.x, blockDim.x);
   __syncthreads();
   // 32 blocks per CTA and round, rounds strided over the stream's blocks
   for (int first = blockIdx.x * 32; first < s.n_blocks; first += gridDim.x * 32) {
@@ -242,9 +243,20 @@ __global__ void __launch_bounds__(128) block_params_kernel(const StreamDev *__re
   phi = mult * (phi - floor_phi);
   double phi_end = s.center_freq * delay_1 + lo_phase + s.fft_len_sec * s.lo_offset + phase_1 * kInv2Pi;
   phi_end = mult * (phi_end - floor_phi);
-  s.bparams[bl] = make_float4((float)(cterm - 2.0 * M_PI * floor(cterm * kInv2Pi)), (float)lterm, (float)phi,
-                              (float)((phi_end - phi) * (1.0 / kNd)));
-  s.bamp[bl] = (float)ampl;
+  BlockPar bp;
+  bp.ph = make_float4((float)(cterm - 2.0 * M_PI * floor(cterm * kInv2Pi)), (float)lterm, (float)phi,
+                      (float)((phi_end - phi) * (1.0 / kNd)));
+  sincosf(16.0f * bp.ph.y, &bp.steps.y, &bp.steps.x);
+  sincosf(16.0f * bp.ph.w, &bp.steps.w, &bp.steps.z);
+  bp.amp = (float)ampl;
+  bp.pad = 0;
+  // unpack source of the pair (bl, bl + 1) when both lie in one recorded segment
+  const int o0 = (s.block0 + bl) * kNd;
+  const DevSegment sg = s.segs[find_segment(s, o0)];
+  bp.src_bit = (bl + 1 < s.n_blocks && sg.src_bit >= 0 && o0 >= sg.out0 && o0 + 2 * kNd <= sg.out0 + sg.n)
+                   ? sg.src_bit + (long long)(o0 - sg.out0) * s.bits
+                   : -1;
+  s.bpar[bl] = bp;
 }
 
 // Unpacked samples only (inspection of the Bit2float_worker output).
@@ -290,9 +302,11 @@ __global__ void extract_kernel(const uint8_t *__restrict__ in, int64_t nout, int
 // streams of a channel as one contiguous piece (a whole 32-byte sector for
 // four streams).
 
-// FP16 hi = fp16(s x), lo = fp16(s x - hi) of a complex value (packed conversions).
+// FP16 hi = fp16(s x), lo = fp16(s x - hi) of a complex value (packed
+// conversions); SCALE false: x already carries the scale s.
+template <bool SCALE>
 __device__ __forceinline__ uint2 tc_split(float2 f, float tc_scale) {
-  const float2 sv = make_float2(f.x * tc_scale, f.y * tc_scale);
+  const float2 sv = SCALE ? make_float2(f.x * tc_scale, f.y * tc_scale) : f;
   const __half2 h = __float22half2_rn(sv);
   const float2 hb = __half22float2(h);
   const __half2 l = __float22half2_rn(make_float2(sv.x - hb.x, sv.y - hb.y));
@@ -366,7 +380,7 @@ __device__ __forceinline__ void window_apply(float2 (&v)[16], int t, int nper, f
 // multiple of four, M == N.  Threads tid = 0..nthr-1 share the channels 0..M;
 // bins q and N - q come together, so the N/2 + 1 pairs spread evenly (bin N/2
 // goes to the last threads on its own).
-template <int N, int NS, int OUT_TC>
+template <int N, int NS, int OUT_TC, bool SCALE>
 __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *sinfo, int NV, bool fast, int row,
                                           int nrows_total, int M, int kpad, const float2 *__restrict__ tw_rot,
                                           void *__restrict__ spec_out, float tc_scale, int tid, int nthr) {
@@ -397,8 +411,8 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
         for (int j = 0; j < W; j++) {
           float2 xq, xnq;
           real_bin_pair<N>(Z + j * BUF, w, i, xq, xnq);
-          a[j] = tc_split(xq, tc_scale);
-          b[j] = tc_split(xnq, tc_scale);
+          a[j] = tc_split<SCALE>(xq, tc_scale);
+          b[j] = tc_split<SCALE>(xnq, tc_scale);
         }
         put(dst + (int64_t)i * kTcSlots, a);
         put(dst + (int64_t)(N - i) * kTcSlots, b);
@@ -407,7 +421,7 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
         const int j = tid - (nthr - W);
         float2 xq, xnq;
         real_bin_pair<N>(Z + j * BUF, __ldg(tw_rot + N / 2), N / 2, xq, xnq);
-        dst[(int64_t)(N / 2) * kTcSlots + j] = tc_split(xq, tc_scale);
+        dst[(int64_t)(N / 2) * kTcSlots + j] = tc_split<SCALE>(xq, tc_scale);
       }
       return;
     }
@@ -416,7 +430,8 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
 #pragma unroll
       for (int j = 0; j < NS; j++)
         if (j < NV)
-          dst[(int64_t)i * kTcSlots + sinfo[j].y] = tc_split(real_bin<N>(Z + j * BUF, tw_rot, sinfo[j].x + i), tc_scale);
+          dst[(int64_t)i * kTcSlots + sinfo[j].y] =
+              tc_split<SCALE>(real_bin<N>(Z + j * BUF, tw_rot, sinfo[j].x + i), tc_scale);
   } else {
 #pragma unroll 1
     for (int j = 0; j < NV; j++) {
@@ -454,10 +469,13 @@ struct WinShape {
   static constexpr int THREADS = SPC * RPC * T;
   static constexpr int BUF = N + N / 16;  // padded FFT buffer (float2) of one group
   static constexpr size_t FFT_SMEM = (size_t)SPC * RPC * BUF * sizeof(float2);
-  static constexpr int PT = pass_table_len<LOGN>();  // float4 pairs of the pass twiddle table
+  // compact pass-twiddle table (a 15-twiddle table measured 5 % slower here:
+  // it takes L1 capacity from the twice-read input rows)
+  static constexpr int TWK = 4;
+  static constexpr size_t PTB = pass_table_bytes<LOGN, TWK>();
   // the window (up to rot = 2N floats) joins the shared tables when it fits
-  static constexpr bool WSMEM = FFT_SMEM + 32 * PT + 8 * N <= 227 * 1024;
-  static constexpr size_t SMEM = FFT_SMEM + 32 * PT + (WSMEM ? 8 * N : 0);
+  static constexpr bool WSMEM = FFT_SMEM + PTB + 8 * N <= 227 * 1024;
+  static constexpr size_t SMEM = FFT_SMEM + PTB + (WSMEM ? 8 * N : 0);
   static_assert(THREADS <= 1024, "at most 1024 threads");
 };
 
@@ -483,8 +501,8 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
   float2 v[16];
   if (k0 < k1) window_raw<T>(v, t, sok && row_of(k0) < nrows, nper, s.ts + (int64_t)(row0 + row_of(k0)) * N);
   // shared tables behind the FFT buffers: pass twiddles, then the window
-  float4 *ptab = reinterpret_cast<float4 *>(dsm + S::FFT_SMEM / sizeof(float2));
-  fill_pass_table<LOGN>(ptab, tw_rot + 2 * N, threadIdx.x, S::THREADS);
+  float2 *ptab = dsm + S::FFT_SMEM / sizeof(float2);
+  fill_pass_table<LOGN, S::TWK>(ptab, tw_rot + 2 * N, threadIdx.x, S::THREADS);
   // the CTA's streams: channel shift and slot, and whether the whole-sector path applies
   __shared__ int2 sinfo[SPC];
   if (threadIdx.x < SPC) {
@@ -493,10 +511,16 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
                              ? make_int2(streams[st].output_offset - streams[st].temp_fft_offset, streams[st].slot)
                              : make_int2(0, -1);
   }
+  // a shared window carries the tensor-core layout's power-of-two scale
+  // (exact), so the output split needs no multiply
   const float *win = window;
   if constexpr (S::WSMEM) {
-    float4 *wsm = ptab + 2 * S::PT;  // nper is a multiple of 4 (rot >= 512)
-    for (int i = threadIdx.x; i < nper / 4; i += S::THREADS) wsm[i] = __ldg(reinterpret_cast<const float4 *>(window) + i);
+    float4 *wsm = reinterpret_cast<float4 *>(ptab + S::PTB / sizeof(float2));  // nper: a multiple of 4 (rot >= 512)
+    const float ws = OUT_TC ? tc_scale : 1.0f;
+    for (int i = threadIdx.x; i < nper / 4; i += S::THREADS) {
+      const float4 w = __ldg(reinterpret_cast<const float4 *>(window) + i);
+      wsm[i] = make_float4(w.x * ws, w.y * ws, w.z * ws, w.w * ws);
+    }
     win = reinterpret_cast<const float *>(wsm);
   }
   __syncthreads();
@@ -511,10 +535,10 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
     // Each group's transform synchronises only its own T threads (named
     // barrier 1 + g) when the groups are whole warps and few enough.
     if constexpr (T >= 32 && S::THREADS / T <= 15) {
-      fft_reg<-1, LOGN, true>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, ptab, GroupSync{1 + g, T});
+      fft_reg<-1, LOGN, true, S::TWK>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, ptab, GroupSync{1 + g, T});
       __syncthreads();  // the stores read every group's transform
     } else {
-      fft_reg<-1, LOGN, true>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, ptab, BlockSync());
+      fft_reg<-1, LOGN, true, S::TWK>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, ptab, BlockSync());
     }
     if (k + 1 < k1)  // hop = rot / 2
       window_raw<T>(v, t, sok && row_of(k + 1) < nrows, nper, s.ts + (int64_t)(row0 + row_of(k + 1)) * N);
@@ -522,8 +546,8 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
     for (int r = 0; r < RPC; r++) {
       const int row = k * RPC + r;
       if (row >= nrows) break;
-      store_row<N, SPC, OUT_TC>(dsm + r * SPC * S::BUF, S::BUF, sinfo, nv, fast, row0 + row, nrows_total, M, kpad,
-                                tw_rot, spec_out, tc_scale, threadIdx.x, S::THREADS);
+      store_row<N, SPC, OUT_TC, !S::WSMEM>(dsm + r * SPC * S::BUF, S::BUF, sinfo, nv, fast, row0 + row, nrows_total,
+                                           M, kpad, tw_rot, spec_out, tc_scale, threadIdx.x, S::THREADS);
     }
     __syncthreads();  // the next step's FFT rewrites the buffers
   }
