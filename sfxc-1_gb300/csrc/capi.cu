@@ -101,13 +101,12 @@ struct StreamCtx {
   BitStats stats{};
   Spline sp;
   int n_blocks = 0, nfft_max = 0, rot = 0, hop = 0;
-  DevBuf src, segs, stat_rng, spline, hist, bpar;
+  DevBuf src, segs, stat_rng, spline, bpar;
   void take_buffers(StreamCtx &o) {
     src.swap(o.src);
     segs.swap(o.segs);
     stat_rng.swap(o.stat_rng);
     spline.swap(o.spline);
-    hist.swap(o.hist);
     bpar.swap(o.bpar);
   }
 };
@@ -155,6 +154,11 @@ struct sfxc_gpu_ctx {
   };
   std::map<int, RotTables> rot_tables;
   HostBuf staging;  // the integration's chunk descriptors, uploaded in one copy
+  // bit-statistics counters of all streams (8 per stream), and the pinned
+  // landing area of an integration's results: visibilities, counters, the
+  // X-step's error flag (one readback copy each)
+  DevBuf hist;
+  HostBuf results;
   std::vector<StreamDev> hsd;
 };
 
@@ -357,7 +361,7 @@ std::vector<std::pair<int, int>> subint_ranges(const sfxc_gpu_ctx *c) {
   return r;
 }
 
-void serialize_integration(sfxc_gpu_ctx *c, const std::vector<float2> &vis, int32_t source_nr,
+void serialize_integration(sfxc_gpu_ctx *c, const float2 *vis, int32_t source_nr,
                            const std::vector<std::pair<int64_t, int64_t>> &nfl, std::vector<uint8_t> &o) {
   const int N = (int)c->streams.size();
   const int nbl = (int)c->bl.size();
@@ -405,7 +409,7 @@ void serialize_integration(sfxc_gpu_ctx *c, const std::vector<float2> &vis, int3
                           ((c->streams[c->bl[b].b].polarisation == 'R' ? 0 : 1) << 1) |
                           ((c->p.sideband == 'U' ? 1 : 0) << 2) | ((c->p.frequency_nr & 31) << 3)));
     o.push_back((uint8_t)' ');
-    const uint8_t *d = reinterpret_cast<const uint8_t *>(vis.data() + (size_t)b * K);
+    const uint8_t *d = reinterpret_cast<const uint8_t *>(vis + (size_t)b * K);
     o.insert(o.end(), d, d + K * sizeof(float2));
   }
 }
@@ -421,6 +425,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   cudaStream_t st = c->st;
   // ---- host planning per stream (Bit2float_worker state machine replica)
   c->hsd.assign(N, StreamDev{});
+  c->hist.ensure((size_t)N * 64);
+  CK(cudaMemsetAsync(c->hist.p, 0, (size_t)N * 64, st));
   std::vector<int4> items;
   for (int i = 0; i < N; i++) {
     StreamCtx &s = c->sc[i];
@@ -445,8 +451,6 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       spl.insert(spl.end(), s.sp.d[k].begin(), s.sp.d[k].end());
     }
     upload(s.spline, spl.data(), spl.size() * 8, st);
-    s.hist.ensure(8 * 8);
-    CK(cudaMemsetAsync(s.hist.p, 0, 8 * 8, st));
     StreamDev &d = c->hsd[i];
     d.src = s.src.as<uint8_t>();
     d.segs = s.segs.as<DevSegment>();
@@ -493,7 +497,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       d.output_offset = 0;
       d.temp_fft_offset = (int)(-delta * 2 * M / c->p.sample_rate);
     }
-    d.hist = s.hist.as<unsigned long long>();
+    d.hist = c->hist.as<unsigned long long>() + (size_t)i * 8;
     d.phase_zero = std::all_of(s.sp.y[1].begin(), s.sp.y[1].end(), [](double v) { return v == 0.0; });
     d.amp_one = std::all_of(s.sp.y[2].begin(), s.sp.y[2].end(), [](double v) { return v == 1.0; });
     d.no_clock = s.sp.clock_offset == 0.0 && s.sp.clock_rate == 0.0;
@@ -704,17 +708,19 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     launch_normalize(c->acc.as<float2>() + (size_t)bin * nbl * kpad, kpad, M, N, nbl, c->blpairs.as<int>(),
                      c->norms.as<double>(), c->flagfac.as<double>(), c->out.as<float2>() + (size_t)bin * nbl * K, st);
   CK(cudaGetLastError());
-  std::vector<float2> vis((size_t)c->nbins * nbl * K);
-  CK(cudaMemcpyAsync(vis.data(), c->out.p, vis.size() * sizeof(float2), cudaMemcpyDeviceToHost, st));
-  std::vector<unsigned long long> hist((size_t)N * 8);
-  for (int i = 0; i < N; i++)
-    CK(cudaMemcpyAsync(hist.data() + (size_t)i * 8, c->sc[i].hist.p, 8 * 8, cudaMemcpyDeviceToHost, st));
-  int dev_err = 0;
-  CK(cudaMemcpyAsync(&dev_err, c->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  const size_t nvis = (size_t)c->nbins * nbl * K;
+  uint8_t *res = static_cast<uint8_t *>(c->results.ensure(nvis * sizeof(float2) + (size_t)N * 64 + 16));
+  const float2 *vis = reinterpret_cast<const float2 *>(res);
+  const unsigned long long *hist = reinterpret_cast<const unsigned long long *>(res + nvis * sizeof(float2));
+  const int *dev_err = reinterpret_cast<const int *>(res + nvis * sizeof(float2) + (size_t)N * 64);
+  CK(cudaMemcpyAsync(res, c->out.p, nvis * sizeof(float2), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(res + nvis * sizeof(float2), c->hist.p, (size_t)N * 64, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(res + nvis * sizeof(float2) + (size_t)N * 64, c->derr.p, sizeof(int), cudaMemcpyDeviceToHost,
+                     st));
   CK(cudaEventRecord(c->evpool[ev + 1], st));
   launches += 2 * c->nbins;
   CK(cudaStreamSynchronize(st));
-  if (dev_err) throw Error(SFXC_GPU_ECUDA, "tensor-core X-step timed out waiting for its MMAs");
+  if (*dev_err) throw Error(SFXC_GPU_ECUDA, "tensor-core X-step timed out waiting for its MMAs");
   for (size_t q = 0; q + 4 <= ev; q += 4) {
     float a, b, x;
     CK(cudaEventElapsedTime(&a, c->evpool[q], c->evpool[q + 1]));
@@ -746,10 +752,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   }
   // ---- output bytes (integration_write per bin) and tsys records
   std::vector<uint8_t> o;
-  for (int bin = 0; bin < c->nbins; bin++) {
-    std::vector<float2> v(vis.begin() + (size_t)bin * nbl * K, vis.begin() + (size_t)(bin + 1) * nbl * K);
-    serialize_integration(c, v, pulsar ? bin : 0, nfl, o);
-  }
+  for (int bin = 0; bin < c->nbins; bin++) serialize_integration(c, vis + (size_t)bin * nbl * K, pulsar ? bin : 0, nfl, o);
   if (sink && sink(user, 0, o.data(), o.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
   for (int i = 0; i < N; i++) {
     std::vector<uint8_t> t;
