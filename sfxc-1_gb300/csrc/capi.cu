@@ -567,7 +567,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   const bool tc_x = c->x_mode == SFXC_GPU_X_TC_HILO && !pulsar;
   const float tc_scale = std::ldexp(1.0f, -(int)std::lround(0.5 * std::log2(2.0 * M * 10.0)));
   // FP32 spectra: [stream][row][kpad]; TC spectra: [row][kpad][32 stream slots], 8 bytes each
-  c->spec.ensure((size_t)(tc_x ? kTcSlots : N) * max_rows * kpad * sizeof(float2));
+  // the tensor-core layout reads rows in groups of 8 (rows past a chunk's end cleared before its X-step)
+  c->spec.ensure((size_t)(tc_x ? kTcSlots : N) * (tc_x ? (max_rows + 7) / 8 * 8 : max_rows) * kpad * sizeof(float2));
   c->derr.ensure(sizeof(int));
   CK(cudaMemsetAsync(c->derr.p, 0, sizeof(int), st));
   for (int i = 0; i < N; i++) {
@@ -680,6 +681,9 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     }
     CK(cudaEventRecord(c->evpool[ev + 2], st));
     if (tc_x) {
+      if (nrows % 8)
+        CK(cudaMemsetAsync(static_cast<char *>(c->spec.p) + (size_t)nrows * kpad * kTcSlots * sizeof(float2), 0,
+                           (size_t)(8 - nrows % 8) * kpad * kTcSlots * sizeof(float2), st));
       CK(launch_xcorr_tc(c->spec.p, nrows, kpad, K, c->blmap.as<int>(), c->jt.npad, 1.0f / (tc_scale * tc_scale),
                          c->acc.as<float2>(), c->derr.as<int>(), st));
     } else if (pulsar) {

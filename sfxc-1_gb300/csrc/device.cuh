@@ -9,6 +9,16 @@ namespace sfxc {
 constexpr int kNd = 256;  // fft_size_delaycor handled by the fused block kernel
 constexpr int kTcSlots = 32;  // stream slots per (row, channel) of the tensor-core spectra layout
 
+// Tensor-core spectra layout, in 8-byte units (one FP16 hi/lo complex value):
+// per row kpad channels x 32 slots; the channels in groups of four, and per
+// group the eight slot quads (slots 4q .. 4q+3) one 128-byte line each,
+// holding the group's four channels x four slots.  So the four streams of a
+// slot quad write whole lines, and one channel's 32 slots are eight 32-byte
+// pieces 128 bytes apart.  kpad is a multiple of 4.
+__host__ __device__ __forceinline__ int64_t tc_index(int64_t row, int kpad, int ch, int slot) {
+  return row * kpad * kTcSlots + (int64_t)(ch >> 2) * 128 + (slot >> 2) * 16 + (ch & 3) * 4 + (slot & 3);
+}
+
 // One plan segment: output samples [out0, out0+n) come from source bit src_bit
 // onward (bits per sample apart); src_bit < 0 means zeros (invalid or an
 // inserted sample).  Same layout as host.hpp's Segment.

@@ -387,7 +387,7 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
   static_assert(NS <= 4, "at most four streams per CTA");
   if (OUT_TC) {
     constexpr int W = NS;  // streams per store
-    uint2 *dst = reinterpret_cast<uint2 *>(spec_out) + (int64_t)row * kpad * kTcSlots;
+    uint2 *dst = reinterpret_cast<uint2 *>(spec_out);
     if (fast) {
       auto put = [](uint2 *p, const uint2 (&o)[W]) {
         if constexpr (W == 1) {
@@ -403,7 +403,8 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
           for (int j = 0; j < W; j++) p[j] = o[j];
         }
       };
-      dst += sinfo[0].y;
+      const int s0 = sinfo[0].y;
+      uint2 *drow = dst + tc_index(row, kpad, 0, s0);  // channel i at drow + (i >> 2) * 128 + (i & 3) * 4
       for (int i = tid; i < N / 2; i += nthr) {
         const float2 w = __ldg(tw_rot + i);
         uint2 a[W], b[W];
@@ -414,14 +415,14 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
           a[j] = tc_split<SCALE>(xq, tc_scale);
           b[j] = tc_split<SCALE>(xnq, tc_scale);
         }
-        put(dst + (int64_t)i * kTcSlots, a);
-        put(dst + (int64_t)(N - i) * kTcSlots, b);
+        put(drow + (i >> 2) * 128 + (i & 3) * 4, a);
+        put(drow + ((N - i) >> 2) * 128 + ((N - i) & 3) * 4, b);
       }
       if (tid >= nthr - W) {  // bin N/2, one stream per thread
         const int j = tid - (nthr - W);
         float2 xq, xnq;
         real_bin_pair<N>(Z + j * BUF, __ldg(tw_rot + N / 2), N / 2, xq, xnq);
-        dst[(int64_t)(N / 2) * kTcSlots + j] = tc_split<SCALE>(xq, tc_scale);
+        dst[tc_index(row, kpad, N / 2, s0 + j)] = tc_split<SCALE>(xq, tc_scale);
       }
       return;
     }
@@ -430,7 +431,7 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
 #pragma unroll
       for (int j = 0; j < NS; j++)
         if (j < NV)
-          dst[(int64_t)i * kTcSlots + sinfo[j].y] =
+          dst[tc_index(row, kpad, i, sinfo[j].y)] =
               tc_split<SCALE>(real_bin<N>(Z + j * BUF, tw_rot, sinfo[j].x + i), tc_scale);
   } else {
 #pragma unroll 1

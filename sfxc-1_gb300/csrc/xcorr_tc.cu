@@ -5,11 +5,14 @@
 //
 // Each spectrum value x is stored as two FP16 numbers, hi = fp16(s*x) and
 // lo = fp16(s*x - hi) (s a power of two), so hi + lo carries ~22 bits.
-// Spectra layout (written by the windowed FFT): [row][channel][32 stream
-// slots][hi.re, hi.im, lo.re, lo.im] as FP16, i.e. 256 B per (row, channel),
-// so one channel's K-tile of 64 rows is two 128-byte-wide MN-major atoms
-// (stream slots 0-15 and 16-31), each 64 rows x 128 B.  The M index of a
-// component is 4 * stream + {hi.re, hi.im, lo.re, lo.im}.  The MMA computes
+// Spectra layout (written by the windowed FFT, tc_index): per row, 32 stream
+// slots x [hi.re, hi.im, lo.re, lo.im] FP16 per channel, stored as one
+// 128-byte line per (group of four channels, slot quad), so a channel's
+// slots are eight 32-byte pieces 128 B apart.  One TMA box per channel and
+// K-tile gathers them, with the 32-byte swizzle, into the canonical MN-major
+// layout: atoms of 8 rows x 32 B (16 components), the eight M atoms 256 B
+// apart, 8-row groups 2 KB apart.  The M index of a component is
+// 4 * stream + {hi.re, hi.im, lo.re, lo.im}.  The MMA computes
 // D = A A^T (128 x 128, FP32 accumulation in TMEM); summing the four hi/lo
 // combinations of a stream pair gives the compensated product, and the
 // epilogue forms
@@ -18,7 +21,7 @@
 //
 // Persistent CTA per SM, 10 warps, warp-specialised, over groups of 2
 // channels: warp 0 streams K-tiles with TMA (cp.async.bulk.tensor, 128-byte
-// swizzle, 4 boxes of 8 KB per 32 KB stage, 6 stages) without stopping at
+// swizzle, 2 boxes of 16 KB per 32 KB stage, 6 stages) without stopping at
 // group boundaries; warp 1 issues 2 channels x 4 MMAs (K = 16) per stage into
 // one of two TMEM buffers (2 x 256 columns) and commits each stage to its
 // "empty" barrier and each finished group to the buffer's "full" barrier;
@@ -43,8 +46,7 @@ constexpr int kChan = 2;        // channels per group (one TMEM buffer)
 constexpr int kRowsK = 64;      // FFT rows per K-tile
 constexpr int kStages = 6;
 constexpr int kThreads = 320;   // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
-constexpr int kAtomBytes = kRowsK * 128;      // one 64-component atom of a K-tile
-constexpr int kChanTile = 2 * kAtomBytes;     // both atoms (stream slots 0-15, 16-31) of one channel
+constexpr int kChanTile = kRowsK * 256;       // one channel's K-tile: 64 rows x 128 components x 2 B
 constexpr int kStageBytes = kChan * kChanTile;  // 32 KB per stage
 constexpr uint32_t kBufCols = kChan * 128;      // TMEM columns per buffer
 constexpr unsigned long long kSpinLimit = 200000000ull;
@@ -56,14 +58,16 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
 
 // SM100 shared-memory matrix descriptor: start >> 4 (bits 0-13), leading
 // byte offset >> 4 (16-29), stride byte offset >> 4 (32-45), version 1
-// (bit 46), base offset 0, layout type SWIZZLE_128B = 2 (bits 61-63).
+// (bit 46), base offset 0, layout type SWIZZLE_32B = 6 (bits 61-63).  For the
+// MN-major operand the leading offset steps between M atoms, the stride
+// offset between 8-row K groups.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
   uint64_t d = 0;
   d |= (uint64_t)((addr >> 4) & 0x3FFF);
   d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
   d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
   d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
+  d |= (uint64_t)6 << 61;
   return d;
 }
 
@@ -136,24 +140,30 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
-// One TMA box {64 halves, 1, 64 rows} = 8 KB at coordinates (0, c1, c2).
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c1, int c2, uint64_t *bar) {
+// One channel's K-tile: TMA box {16 components, 8 rows, 8 slot quads, 8 row
+// groups, 1 channel group} = 16 KB at row group rg and channel group cg.
+__device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *map, int rg, int cg, uint64_t *bar) {
   asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+      "%6}], [%7];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(0), "r"(0), "r"(rg), "r"(cg), "r"(smem_u32(bar))
       : "memory");
 }
+
+// Tensor maps of the four channels of a channel group (base offsets 32 B apart).
+struct TcMaps {
+  CUtensorMap m[4];
+};
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
-    xcorr_tc_kernel(const __grid_constant__ CUtensorMap tmap, int nrows, int K, int kpad, const int *__restrict__ blmap,
+    xcorr_tc_kernel(const __grid_constant__ TcMaps tmaps, int nrows, int K, int kpad, const int *__restrict__ blmap,
                     int npad, float inv_scale2, float2 *__restrict__ acc, int *__restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  uint8_t *base = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);  // 128-byte swizzle wants 1 KB
+  uint8_t *base = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);  // stages 1 KB aligned
   __shared__ uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], done;
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
@@ -203,10 +213,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         mbar_expect_tx(&full[s], kStageBytes);
         uint8_t *st = base + s * kStageBytes;
 #pragma unroll
-        for (int c = 0; c < kChan; c++)
-#pragma unroll
-          for (int a = 0; a < 2; a++)
-            tma_load_3d(st + c * kChanTile + a * kAtomBytes, &tmap, 2 * (g * kChan + c) + a, kt * kRowsK, &full[s]);
+        for (int c = 0; c < kChan; c++) {
+          const int ch = g * kChan + c;
+          tma_load_5d(st + c * kChanTile, &tmaps.m[ch & 3], kt * (kRowsK / 8), ch >> 2, &full[s]);
+        }
         last[s] = it;
       }
     }
@@ -237,8 +247,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int c = 0; c < kChan; c++) {
 #pragma unroll
           for (int ks = 0; ks < kRowsK / 16; ks++) {
-            // 16 K-rows = two 8-row groups of 1024 B; M atoms kAtomBytes apart
-            const uint64_t d = smem_desc(st + c * kChanTile + ks * 2048, kAtomBytes, 1024);
+            // 16 K-rows = two 8-row groups of 2 KB; M atoms 256 B apart
+            const uint64_t d = smem_desc(st + c * kChanTile + ks * 4096, 256, 2048);
             mma_f16(tmem + b * kBufCols + c * 128, d, d, idesc, (kt > 0 || ks > 0) ? 1u : 0u);
           }
         }
@@ -340,16 +350,23 @@ cudaError_t launch_xcorr_tc(const void *spec, int nrows, int kpad, int K, const 
   if (nrows <= 0) return cudaSuccess;
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
   if (!enc) return cudaErrorNotSupported;
-  // halves of one 128-byte atom row; (channel, atom) pairs 128 B apart; rows kpad * 256 B apart
-  alignas(64) CUtensorMap map;
-  const cuuint64_t dims[3] = {64, (cuuint64_t)2 * kpad, (cuuint64_t)nrows};
-  const cuuint64_t strides[2] = {128, (cuuint64_t)kpad * 256};
-  const cuuint32_t box[3] = {64, 1, (cuuint32_t)kRowsK};
-  const cuuint32_t estr[3] = {1, 1, 1};
-  if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<void *>(spec), dims, strides, box, estr,
-          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-    return cudaErrorInvalidValue;
+  // per channel of a group (base + 32 B each): 16 components of a slot quad,
+  // rows within an 8-row group (kpad * 256 B apart), the 8 slot quads (128 B
+  // apart), 8-row groups, channel groups (1 KB apart).  Rows from nrows up to
+  // the next multiple of 8 must be zero in the buffer (the caller clears
+  // them); row groups past the end read as zeros.
+  if (kpad % 4 != 0) return cudaErrorInvalidValue;
+  TcMaps maps;
+  const cuuint64_t R = (cuuint64_t)kpad * 256;
+  const cuuint64_t dims[5] = {16, 8, 8, (cuuint64_t)(nrows + 7) / 8, (cuuint64_t)kpad / 4};
+  const cuuint64_t strides[4] = {R, 128, 8 * R, 1024};
+  const cuuint32_t box[5] = {16, 8, 8, (cuuint32_t)kRowsK / 8, 1};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  for (int cc = 0; cc < 4; cc++)
+    if (enc(&maps.m[cc], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, static_cast<char *>(const_cast<void *>(spec)) + 32 * cc,
+            dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
+            CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
   const size_t smem = xcorr_tc_smem_bytes();
   cudaError_t e = cudaFuncSetAttribute(xcorr_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -357,7 +374,7 @@ cudaError_t launch_xcorr_tc(const void *spec, int nrows, int kpad, int K, const 
   cudaGetDevice(&dev);
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 1;
   const int ngroups = (K + kChan - 1) / kChan;
-  xcorr_tc_kernel<<<std::min(ngroups, nsm), kThreads, smem, st>>>(map, nrows, K, kpad, blmap, npad, inv_scale2, acc,
+  xcorr_tc_kernel<<<std::min(ngroups, nsm), kThreads, smem, st>>>(maps, nrows, K, kpad, blmap, npad, inv_scale2, acc,
                                                                    err);
   return cudaGetLastError();
 }
