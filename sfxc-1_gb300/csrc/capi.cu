@@ -414,6 +414,21 @@ void serialize_integration(sfxc_gpu_ctx *c, const float2 *vis, int32_t source_nr
   }
 }
 
+// Node interval (the device search's answer) of the first block start of a
+// launch; the block kernel walks forward from it.
+int spline_lo_for(const StreamDev &d, const std::vector<double> &x) {
+  const double v = (double)(d.start_ticks + (int64_t)d.block0 * kNd * d.tps - d.scan_begin) * (1.0 / 512000000.0);
+  int lo = 0, hi = (int)x.size() - 1;
+  while (hi > lo + 1) {
+    const int i = (hi + lo) >> 1;
+    if (x[i] > v)
+      hi = i;
+    else
+      lo = i;
+  }
+  return lo;
+}
+
 int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   if (!c->have_job) throw Error(SFXC_GPU_ESTATE, "no parameters set");
   const int N = (int)c->streams.size();
@@ -478,6 +493,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     d.sample_rate = ss.sample_rate;
     d.bandwidth = ss.bandwidth;
     d.oversamp = (int)std::round(ss.sample_rate / (2 * (double)ss.bandwidth));
+    d.frac_scale = -2.0 * M_PI / ss.sample_rate;
+    d.int_phase_q = M_PI / (2 * d.oversamp);
     d.sideband = ss.sideband == 'L' ? -1 : 1;
     d.center_freq = ss.channel_freq + d.sideband * ss.bandwidth * 0.5 + ss.lo_offset;
     d.lo_offset = ss.lo_offset;
@@ -650,6 +667,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       d.bpar = c->sc[i].bpar.as<BlockPar>();
       d.block0 = b0;
       d.n_blocks = b1 - b0;
+      d.spline_lo = spline_lo_for(d, c->sc[i].sp.x);
       staged[ch * per_chunk + i] = d;
     }
     for (int k = 0; k < N; k++) staged[ch * per_chunk + N + k] = c->hsd[order[k]];
@@ -703,6 +721,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   for (int i = 0; i < N; i++) {
     c->hsd[i].block0 = 0;
     c->hsd[i].n_blocks = c->sc[i].n_blocks;
+    c->hsd[i].spline_lo = spline_lo_for(c->hsd[i], c->sc[i].sp.x);
   }
   // ---- normalisation and statistics
   CK(cudaEventRecord(c->evpool[ev], st));

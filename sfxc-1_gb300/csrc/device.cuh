@@ -57,9 +57,11 @@ struct StreamDev {
   const DevStatRange *stats;   // counted-byte ranges
   int32_t nstats;
   int32_t tsys_t0, tsys_period, tsys_on0, tsys_two_bit;
-  // delay model: spline over n nodes: x | (y b c d) x3 columns, 13n doubles
+  // delay model: spline over n nodes: x | (y b c d) x3 columns, 13n doubles;
+  // spline_lo: the node interval of the launch's first block start, from
+  // which the block kernel walks forward (no search per block)
   const double *spline;
-  int32_t spline_n;
+  int32_t spline_n, spline_lo;
   int64_t scan_begin, clock_epoch;
   double clock_offset, clock_rate;
   // time base
@@ -72,6 +74,9 @@ struct StreamDev {
   // channel setup (Delay_correction::set_parameters)
   int32_t sample_rate, bandwidth, oversamp, sideband;  // sideband +1 / -1
   double center_freq, lo_offset, start_phase;
+  // per-stream quotients of Delay_correction::fractional_bit_shift, divided
+  // once here: -2 pi / sample_rate and pi / (2 oversamp)
+  double frac_scale, int_phase_q;
   // windowed FFT stage; slot: the stream's index in the job (its place in
   // the spectra layouts), also when the launch covers a subset of streams
   int32_t rot, flip, output_offset, temp_fft_offset, slot;
@@ -98,6 +103,22 @@ __device__ __forceinline__ int spline_index(const double *x, int n, double v) {
       lo = i;
   }
   return lo;
+}
+// The interval spline_index finds for v, walking forward from lo, an
+// interval at or before it (spline_index is non-decreasing in v).
+__device__ __forceinline__ int spline_walk(const double *x, int n, double v, int lo) {
+  while (lo < n - 2 && x[lo + 1] <= v) lo++;
+  return lo;
+}
+// Evaluation in node interval i (as found by spline_index or spline_walk).
+__device__ __forceinline__ double spline_eval_at(const double *sp, int n, int col, double v, int i) {
+  const double *x = sp;
+  const double *y = sp + n + col * 4 * n;
+  const double *b = y + n, *c = y + 2 * n, *d = y + 3 * n;
+  double dx = __dsub_rn(v, x[i]);
+  double t = __dadd_rn(c[i], __dmul_rn(d[i], dx));
+  t = __dadd_rn(b[i], __dmul_rn(dx, t));
+  return __dadd_rn(y[i], __dmul_rn(dx, t));
 }
 __device__ __forceinline__ double spline_eval(const double *sp, int n, int col, double v) {
   const double *x = sp;

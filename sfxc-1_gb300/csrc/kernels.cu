@@ -207,33 +207,38 @@ __global__ void __launch_bounds__(128) block_params_kernel(const StreamDev *__re
   if ((int)(blockIdx.x * blockDim.x + (threadIdx.x & ~31)) >= s.n_blocks) return;
   constexpr double kInvTick = 1.0 / 512000000.0, kInv2Pi = 0.15915494309189533577;
   const int64_t ct = s.start_ticks + (int64_t)(s.block0 + bl) * kNd * s.tps;
-  auto delay = [&s](int64_t t) {
-    const double r = spline_eval(s.spline, s.spline_n, 0, (double)(t - s.scan_begin) * kInvTick);
+  // node intervals: the times grow with the block, so each is walked forward
+  // from the launch's first interval (or from the previous time's)
+  auto tsec = [&s](int64_t t) { return (double)(t - s.scan_begin) * kInvTick; };
+  auto delay = [&s](int64_t t, double v, int i) {
+    const double r = spline_eval_at(s.spline, s.spline_n, 0, v, i);
     return s.no_clock ? r : r + (s.clock_offset + (double)(t - s.clock_epoch) * kInvTick * s.clock_rate);
   };
-  auto phase = [&s](int64_t t) {
-    return s.phase_zero ? 0.0 : spline_eval(s.spline, s.spline_n, 1, (double)(t - s.scan_begin) * kInvTick);
-  };
-  const double delay_c = delay(ct + s.half_len_ticks);
-  const double delay_0 = delay(ct);
-  const double phase_0 = phase(ct);
+  auto phase = [&s](double v, int i) { return s.phase_zero ? 0.0 : spline_eval_at(s.spline, s.spline_n, 1, v, i); };
+  const double v0 = tsec(ct), vc = tsec(ct + s.half_len_ticks);
+  const int i0 = spline_walk(s.spline, s.spline_n, v0, s.spline_lo);
+  const int ic = spline_walk(s.spline, s.spline_n, vc, i0);
+  const double delay_c = delay(ct + s.half_len_ticks, vc, ic);
+  const double delay_0 = delay(ct, v0, i0);
+  const double phase_0 = phase(v0, i0);
   // the end of a block is the start of the next when a block is a whole
   // number of ticks: take it from the next lane
   const bool chained = s.fft_len_ticks == (int64_t)kNd * s.tps;
   double delay_1 = __shfl_down_sync(0xffffffffu, delay_0, 1);
   double phase_1 = __shfl_down_sync(0xffffffffu, phase_0, 1);
   if (!chained || lane == 31) {
-    delay_1 = delay(ct + s.fft_len_ticks);
-    phase_1 = phase(ct + s.fft_len_ticks);
+    const double v1 = tsec(ct + s.fft_len_ticks);
+    const int i1 = spline_walk(s.spline, s.spline_n, v1, ic);
+    delay_1 = delay(ct + s.fft_len_ticks, v1, i1);
+    phase_1 = phase(v1, i1);
   }
   if (bl >= s.n_blocks) return;
-  const double ampl =
-      s.amp_one ? 1.0 : spline_eval(s.spline, s.spline_n, 2, (double)(ct + s.half_len_ticks - s.scan_begin) * kInvTick);
+  const double ampl = s.amp_one ? 1.0 : spline_eval_at(s.spline, s.spline_n, 2, vc, ic);
   const double dis = __dmul_rn(delay_c, (double)s.sample_rate);
   const int integer_delay = (int)floor(__dadd_rn(dis, 0.5));
   const double frac = dis - integer_delay;
-  const double tmp1 = frac * (-2.0 * M_PI / s.sample_rate);
-  const double tmp2 = (integer_delay & (4 * s.oversamp - 1)) * (M_PI / (2 * s.oversamp));
+  const double tmp1 = frac * s.frac_scale;
+  const double tmp2 = (integer_delay & (4 * s.oversamp - 1)) * s.int_phase_q;
   const double cterm = tmp2 - tmp1 * 0.5 * s.bandwidth;
   const double lterm = tmp1 * ((double)s.sample_rate * (1.0 / kNd));
   const double mult = -s.sideband * 2.0 * M_PI;
