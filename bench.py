@@ -311,7 +311,7 @@ def roofline(args, per_kernel, total):
     # ncu measured for the tensor-core path's kernels on the one-subband,
     # 4096-channel case; a launch covers one sub-integration chunk of one
     # subband job, so the per-launch traffic scales with the samples it covers
-    measured = {"window_fft_ms": 11.59, "xstep_ms": 8.27, "unpack_fringe_ms": 3.93}
+    measured = {"window_fft_ms": 11.87, "xstep_ms": 8.20, "unpack_fringe_ms": 4.26}
     traffic = None
     if args.x == "tc" and M == 4096 and k in measured:
         launches = args.subbands * -(-args.integration_us // 125000)
