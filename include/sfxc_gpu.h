@@ -26,8 +26,11 @@
  * status (SFXC_GPU_E*), with a message from sfxc_gpu_last_error().  Input
  * buffers belong to the caller and are not referenced after a call returns.
  * One host thread drives one context; a context owns one CUDA stream on one
- * device.  The library has no CPU fallback: without a usable GPU,
- * sfxc_gpu_create fails.
+ * device.  Contexts created in one process get successive stream priorities
+ * (cycling through the device's range), so that jobs correlated side by side
+ * on one GPU finish in turn and their host work overlaps each other's kernels.
+ * The library has no CPU fallback: without a usable GPU, sfxc_gpu_create
+ * fails.
  */
 #ifndef SFXC_GPU_H
 #define SFXC_GPU_H

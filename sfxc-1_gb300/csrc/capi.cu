@@ -3,6 +3,7 @@
 // the byte layout of the correlator output (Correlation_core::integration_write,
 // sfxc/src/correlation_core.cc:316-477; headers sfxc/include/output_header.h:100-148).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -810,7 +811,17 @@ sfxc_gpu_ctx *sfxc_gpu_create(const sfxc_gpu_config *config) {
     CK(cudaGetDeviceCount(&n));
     if (c->device < 0 || c->device >= n) throw Error(SFXC_GPU_EINVAL, "no such CUDA device");
     CK(cudaSetDevice(c->device));
-    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    // Contexts of one process take successive stream priorities (cycling
+    // through the device's range): jobs correlated side by side then finish
+    // one after another instead of all together, so each job's host work
+    // (output, next input, planning) overlaps the others' kernels rather than
+    // leaving the GPU idle while every job does it at once.
+    static std::atomic<unsigned> created{0};
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int levels = least - greatest + 1;
+    const int prio = greatest + (int)(created.fetch_add(1) % (unsigned)std::max(levels, 1));
+    CK(cudaStreamCreateWithPriority(&c->st, cudaStreamNonBlocking, prio));
     for (auto &e : c->ev) CK(cudaEventCreate(&e));
   } catch (const Error &e) {
     g_error = e.msg;
