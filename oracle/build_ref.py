@@ -88,7 +88,9 @@ def build(ref_root=None, force=False):
     if not os.path.isdir(sfxc):
         return None
     exe = harness_path()
-    if os.path.exists(exe) and not force:
+    # rebuild when the harness or the shims changed since the last build
+    own = [os.path.join(HERE, "ref_harness.cc")] + [os.path.join(SHIM, f) for f in os.listdir(SHIM)]
+    if os.path.exists(exe) and not force and os.path.getmtime(exe) >= max(os.path.getmtime(f) for f in own):
         return exe
     obj = os.path.join(OUT, "obj")
     inc = os.path.join(OUT, "inc")

@@ -176,6 +176,14 @@ def correlate(job, dump=False, impl="reference", precision=32):
                     f.write(np.uint64(len(chunk)).tobytes())
                     f.write(bytes(chunk))
             lines.append(("protocol", p))
+        # Mask_parameters (spectral reduction): float32 files, and the flag
+        for key in ("mask", "lag_window"):
+            if job.get(key) is not None:
+                p = os.path.join(d, key + ".f32")
+                np.asarray(job[key], dtype=np.float32).tofile(p)
+                lines.append((key, p))
+        if job.get("mask_normalize"):
+            lines.append(("mask_normalize", 1))
         if "pulsar" in job:
             lines.append(("pulsar",) + tuple(job["pulsar"]))
             for pc in job["polyco"]:

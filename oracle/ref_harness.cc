@@ -375,6 +375,29 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
   p.pulsar_binning = has(kv, "pulsar") ? 1 : 0;
   p.pulsar_parameters = 0;
   p.mask_parameters = 0;
+  // Mask_parameters of the ctrl file: float32 files of the mask (M + 1) and
+  // the lag window (2 number_channels), and the normalisation flag
+  Mask_parameters mask_params;
+  if (has(kv, "mask_normalize") || has(kv, "mask") || has(kv, "lag_window")) {
+    mask_params.normalize = has(kv, "mask_normalize") && geti(kv, "mask_normalize") != 0;
+    if (has(kv, "mask")) {
+      const std::vector<char> b = read_file(get(kv, "mask")[0]);
+      for (size_t q = 0; q + 4 <= b.size(); q += 4) {
+        float v;
+        std::memcpy(&v, &b[q], 4);
+        mask_params.mask.push_back(v);
+      }
+    }
+    if (has(kv, "lag_window")) {
+      const std::vector<char> b = read_file(get(kv, "lag_window")[0]);
+      for (size_t q = 0; q + 4 <= b.size(); q += 4) {
+        float v;
+        std::memcpy(&v, &b[q], 4);
+        mask_params.window.push_back(v);
+      }
+    }
+    p.mask_parameters = &mask_params;
+  }
   std::vector<int> stream_station_index;  // delay table per stream
   for (int i = 0; i < nstreams; i++) {
     const std::vector<std::string> &v = get(kv, idx("stream", i));

@@ -654,6 +654,12 @@ typedef struct {
   int npolyco;
   double *polyco; /* per polyco: tmid DM ref_phase ref_freq obs_freq ncoef coef... (packed, stride 32) */
   int dump;
+  /* spectral reduction (number_channels < fft_size_correlation): the
+     Mask_parameters of the ctrl file -- a mask over the M+1 channels, a lag
+     window over 2 number_channels lags, and the per-channel normalisation;
+     NULL / 0 when absent (mask of ones, window from the window type) */
+  double *mask, *lag_window;
+  int mask_normalize;
 } job_t;
 
 /* ------------------------------------------------------------- statistics ---
@@ -1256,6 +1262,88 @@ static void normalize(const job_t *j, const bl_t *bl, int nbl, double *acc, b2f_
   free(norms);
 }
 
+/* ---------------------------------------------------- spectral reduction ---
+ * Correlation_core::integration_write for number_channels < fft size
+ * (sfxc/src/correlation_core.cc:413-439) with create_window (760-810) and
+ * create_mask (812-824): per baseline, optional normalisation to unit
+ * amplitude, the mask, an unnormalised c2r FFT of 2M points (imaginary parts
+ * of DC and Nyquist ignored), the lags folded to 2 nch, the lag window, an
+ * r2c FFT of 2 nch points, and a division by 2M; every step stored in FP32 as
+ * the reference's buffers are. */
+static double lagwin_f(int type, int n, int i) { /* cos / hamming / hann (667-690) */
+  switch (type) {
+    case WINDOW_COS: return sin(M_PI * i / n);
+    case WINDOW_HAMMING: return 0.54 - 0.46 * cos(2 * M_PI * i / n);
+    default: return 0.5 * (1 - cos(2 * M_PI * i / n));
+  }
+}
+static double lagwin_conv(int type, int n, int i) { /* convolve (692-706) */
+  double sum = 0.0;
+  i += n / 2;
+  for (int q = 0; q <= n; q++) {
+    if (i - q < 0 || i - q > n) continue;
+    sum += lagwin_f(type, n, q) * lagwin_f(type, n, i - q);
+  }
+  return sum;
+}
+static double *lag_window_of(const job_t *j) {
+  static double *cache = NULL;
+  static int cn = -1, cm = -1, ct = -1;
+  const int n = 2 * j->number_channels, m = 2 * j->M;
+  if (j->lag_window) return j->lag_window;
+  if (cache && cn == n && cm == m && ct == j->window) return cache;
+  free(cache);
+  cache = xmalloc(n * sizeof(double));
+  cn = n, cm = m, ct = j->window;
+  if (j->window == WINDOW_NONE || j->window == WINDOW_RECT) {
+    cache[0] = 1.;
+    for (int i = 1; i < n / 2; i++) cache[i] = cache[n - i] = st((1. - 2. * i / n) / (1. - 2. * i / m));
+    cache[n / 2] = 0.;
+  } else {
+    const int r = m / n; /* integer ratio, as in the reference */
+    cache[0] = st(r * lagwin_conv(j->window, n, n / 2) / lagwin_conv(j->window, m, m / 2));
+    for (int i = 1; i < n / 2; i++)
+      cache[i] = cache[n - i] = st(r * lagwin_conv(j->window, n, n / 2 + i) / lagwin_conv(j->window, m, m / 2 + i));
+    cache[n / 2] = st(r * lagwin_conv(j->window, n, n) / lagwin_conv(j->window, m, (n + m) / 2));
+  }
+  return cache;
+}
+/* x: M + 1 complex (normalised visibilities), y: nch + 1 complex */
+static void reduce_spectrum(const job_t *j, const double *x, double *y) {
+  const int M = j->M, n2 = 2 * M, nch = j->number_channels, m2 = 2 * nch;
+  static fftplan_t *p2m = NULL, *p2n = NULL;
+  if (!p2m || p2m->n != n2) p2m = fft_plan(n2); /* plans are kept (one job per process) */
+  if (!p2n || p2n->n != m2) p2n = fft_plan(m2);
+  double *re = xmalloc(n2 * 8), *im = xmalloc(n2 * 8);
+  for (int k = 0; k <= M; k++) {
+    double a = x[2 * k], b = x[2 * k + 1];
+    if (j->mask_normalize) {
+      const double mag = st(sqrt(a * a + b * b));
+      if (mag != 0.0) a = st(a / mag), b = st(b / mag);
+    }
+    const double mv = j->mask ? j->mask[k] : 1.0;
+    re[k] = st(a * mv);
+    im[k] = st(b * mv);
+  }
+  im[0] = 0, im[M] = 0;
+  for (int k = M + 1; k < n2; k++) re[k] = re[n2 - k], im[k] = -im[n2 - k];
+  fft_c(p2m, re, im, +1);
+  for (int i = 0; i < n2; i++) re[i] = st(re[i]);
+  double *lag = xmalloc(m2 * 8), *li = xmalloc(m2 * 8);
+  const double *w = lag_window_of(j);
+  for (int q = 0; q < m2; q++) {
+    double v = q < nch ? re[q] : q == nch ? st(st(re[nch] + re[n2 - nch]) / 2) : re[n2 - nch + (q - nch)];
+    lag[q] = st(v * w[q]);
+    li[q] = 0;
+  }
+  fft_c(p2n, lag, li, -1);
+  for (int q = 0; q <= nch; q++) {
+    y[2 * q] = st(st(lag[q]) / (double)(float)n2);
+    y[2 * q + 1] = st(st(li[q]) / (double)(float)n2);
+  }
+  free(re), free(im), free(lag), free(li);
+}
+
 static void write_integration(const job_t *j, const bl_t *bl, int nbl, const double *acc, b2f_t *w,
                               int64_t (*nfl)[2], int nffts, int integration, int32_t sourcenr, bytes_t *out,
                               bytes_t *out64) {
@@ -1306,11 +1394,21 @@ static void write_integration(const job_t *j, const bl_t *bl, int nbl, const dou
     h[3] = ' ';
     bpush(out, &w32, 4);
     bpush(out, h, 4);
-    for (int k = 0; k < K; k++) {
-      float v[2] = {(float)acc[((size_t)b * K + k) * 2], (float)acc[((size_t)b * K + k) * 2 + 1]};
-      bpush(out, v, 8);
-      if (out64) bpush(out64, &acc[((size_t)b * K + k) * 2], 16);
+    const double *x = acc + (size_t)b * K * 2;
+    double *y = NULL;
+    int Ko = K;
+    if (j->number_channels != M) {
+      Ko = j->number_channels + 1;
+      y = xmalloc((size_t)Ko * 16);
+      reduce_spectrum(j, x, y);
+      x = y;
     }
+    for (int k = 0; k < Ko; k++) {
+      float v[2] = {(float)x[2 * k], (float)x[2 * k + 1]};
+      bpush(out, v, 8);
+      if (out64) bpush(out64, &x[2 * k], 16);
+    }
+    free(y);
   }
 }
 
@@ -1580,7 +1678,29 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
   j.n_integrations = (int)kv_ll(k, "n_integrations");
   kv_t *de = kv_get(k, "dump", 0);
   j.dump = de && atoi(de->v[0]);
-  if (j.number_channels != j.M) die("spectral reduction (number_channels != fft size) is not restated");
+  if (j.number_channels < 2 || j.number_channels > j.M || (j.number_channels & (j.number_channels - 1)))
+    die("number_channels must be a power of two no larger than the FFT size");
+  kv_t *mn = kv_get(k, "mask_normalize", 0);
+  j.mask_normalize = mn && atoi(mn->v[0]);
+  /* mask and lag window: files of float32 values */
+  kv_t *mk = kv_get(k, "mask", 0);
+  if (mk) {
+    size_t nb = 0;
+    uint8_t *b = read_all(mk->v[0], &nb);
+    if (nb != (size_t)(j.M + 1) * 4) die("mask needs fft_size_correlation + 1 float32 values");
+    j.mask = xmalloc((j.M + 1) * sizeof(double));
+    for (int q = 0; q <= j.M; q++) j.mask[q] = ((const float *)b)[q];
+    free(b);
+  }
+  kv_t *lw = kv_get(k, "lag_window", 0);
+  if (lw) {
+    size_t nb = 0;
+    uint8_t *b = read_all(lw->v[0], &nb);
+    if (nb != (size_t)(2 * j.number_channels) * 4) die("lag_window needs 2 number_channels float32 values");
+    j.lag_window = xmalloc(2 * j.number_channels * sizeof(double));
+    for (int q = 0; q < 2 * j.number_channels; q++) j.lag_window[q] = ((const float *)b)[q];
+    free(b);
+  }
   j.nstreams = kv_count(k, "stream");
   j.streams = xmalloc(j.nstreams * sizeof(stream_t));
   for (int i = 0; i < j.nstreams; i++) {

@@ -41,6 +41,7 @@ class Scenario:
     sideband: str = "U"
     station_sidebands: dict = field(default_factory=dict)  # station number -> sideband
     nchan: int = 512
+    number_channels: int = 0            # output channels (spectral reduction); 0: nchan
     window: int = 4
     integration_us: int = 15625
     sub_integration_us: int = 125000
@@ -146,7 +147,7 @@ def build_job(sc: Scenario, delay_fn, protocol_fn, fast_random=False):
                         sc.lo_offset, sc.tsys_freq, si))
     return dict(del_bytes=dels, experiment_start_ticks=rec0, start_ticks=start,
                 integration_time_us=sc.integration_us, sub_integration_time_us=sc.sub_integration_us,
-                number_channels=sc.nchan, fft_size_delaycor=256, fft_size_correlation=max(256, sc.nchan),
+                number_channels=sc.number_channels or sc.nchan, fft_size_delaycor=256, fft_size_correlation=max(256, sc.nchan),
                 sample_rate=sc.sample_rate, channel_freq=sc.channel_freq, bandwidth=sc.bandwidth,
                 sideband=sc.sideband, frequency_nr=sc.frequency_nr, polarisation=sc.pols[0],
                 cross_polarize=1 if len(sc.pols) > 1 else 0, reference_station=sc.reference_station,
@@ -188,7 +189,7 @@ def build_job_bulk(sc: Scenario, alloc=None):
                         sc.tsys_freq, si))
     return dict(del_bytes=dels, experiment_start_ticks=rec0, start_ticks=start,
                 integration_time_us=sc.integration_us, sub_integration_time_us=sc.sub_integration_us,
-                number_channels=sc.nchan, fft_size_delaycor=256, fft_size_correlation=max(256, sc.nchan),
+                number_channels=sc.number_channels or sc.nchan, fft_size_delaycor=256, fft_size_correlation=max(256, sc.nchan),
                 sample_rate=sr, channel_freq=sc.channel_freq, bandwidth=sc.bandwidth, sideband=sc.sideband,
                 frequency_nr=sc.frequency_nr, polarisation=sc.pols[0], cross_polarize=1 if len(sc.pols) > 1 else 0,
                 reference_station=sc.reference_station, window=sc.window, source="SRC", integration_nr=0,

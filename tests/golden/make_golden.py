@@ -48,7 +48,34 @@ def scenarios():
     out["pulsar"] = scenario.Scenario(
         stations=stp, sample_rate=32_000_000, bandwidth=16_000_000, bits=2, channel_freq=1_400_000_000,
         nchan=256, integration_us=8000, n_integrations=1, rho=0.05, seed=13, block_bytes=8000)
+    # spectral reduction: 1024-point correlation FFTs reduced to 256 channels,
+    # with the Hann lag window, and with a rectangular window plus a user mask,
+    # lag window and normalisation (Mask_parameters)
+    st2 = scenario.cubic_stations(2, seed=31, max_delay=1e-3, max_rate=1e-5)
+    out["reduced"] = scenario.Scenario(
+        stations=st2, pols=("R", "L"), sample_rate=32_000_000, bandwidth=16_000_000, bits=2,
+        channel_freq=1_600_000_000, nchan=1024, number_channels=256, integration_us=8000, n_integrations=2,
+        rho=0.05, seed=17, block_bytes=8000)
+    out["reduced_mask"] = scenario.Scenario(
+        stations=st2, sample_rate=32_000_000, bandwidth=16_000_000, bits=2, channel_freq=1_600_000_000,
+        nchan=512, number_channels=64, window=0, integration_us=8000, n_integrations=1, rho=0.05, seed=19,
+        block_bytes=8000)
     return out
+
+
+def mask_params(name, job):
+    """User Mask_parameters of the reduced_mask case: a mask with a notch and
+    a taper, a Gaussian lag window, normalisation on."""
+    if name != "reduced_mask":
+        return
+    M, n = job["fft_size_correlation"], job["number_channels"]
+    k = np.arange(M + 1)
+    mask = np.where((k > M // 3) & (k < M // 3 + 9), 0.0, 1.0) * (1.0 - 0.3 * k / M)
+    q = np.arange(2 * n)
+    lag = np.minimum(q, 2 * n - q)
+    job["mask"] = mask.astype(np.float32)
+    job["lag_window"] = np.exp(-0.5 * (lag / (0.4 * n)) ** 2).astype(np.float32)
+    job["mask_normalize"] = 1
 
 
 # two polycos (the closer one is used), non-zero phase polynomial
@@ -67,6 +94,7 @@ def make(name, sc):
     if name == "pulsar":
         job["pulsar"] = (PULSAR["nbins"],) + PULSAR["gate"]
         job["polyco"] = PULSAR["polyco"]
+    mask_params(name, job)
     res = jobs.correlate(job, dump=True)
     keys = sc.streams()
     for k, key in enumerate(keys):
@@ -91,7 +119,10 @@ def make(name, sc):
     rec["cor"] = np.frombuffer(res["cor"], np.uint8)
     rec["tsys"] = np.frombuffer(res["tsys"], np.uint8)
     rec["stats"] = np.frombuffer(res["stats"].encode(), np.uint8)
-    meta = {k: v for k, v in job.items() if k not in ("del_bytes", "protocols")}
+    for key in ("mask", "lag_window"):
+        if key in job:
+            rec[key] = np.asarray(job[key], dtype=np.float32)
+    meta = {k: v for k, v in job.items() if k not in ("del_bytes", "protocols", "mask", "lag_window")}
     meta["block_bytes"] = sc.block_bytes
     meta["rec0"] = rec0
     meta["slice_samples"] = slice_samples

@@ -7,7 +7,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["c1_plain", "multi", "onebit", "pulsar"]
+CASES = ["c1_plain", "multi", "onebit", "pulsar", "reduced", "reduced_mask"]
 
 
 class Golden:
@@ -56,6 +56,9 @@ class Golden:
         m = self.meta
         job = {k: v for k, v in m.items()}
         job["del_bytes"] = self.dels
+        for key in ("mask", "lag_window"):  # Mask_parameters of the spectral-reduction cases
+            if key in self.z.files:
+                job[key] = np.asarray(self.z[key], dtype=np.float32)
         protos = []
         for k in range(self.nstreams):
             s = m["streams"][k]
