@@ -125,6 +125,15 @@ typedef struct {
   double gate_start, gate_stop;    /* Pulsar::interval */
   int32_t n_polyco;
   const sfxc_polyco *polyco;
+  /* spectral reduction, number_channels < fft_size_correlation
+   * (Correlation_core::integration_write, sfxc/src/correlation_core.cc:413-439):
+   * the ctrl file's Mask_parameters -- a mask over fft_size_correlation + 1
+   * channels and a lag window over 2 number_channels lags (NULL: ones, and
+   * the window that create_window derives from `window`), and normalisation
+   * of every channel to unit amplitude before the mask (non-zero: on) */
+  const float *mask;
+  const float *lag_window;
+  int32_t mask_normalize;
 } sfxc_correlation_params;
 
 sfxc_gpu_ctx *sfxc_gpu_create(const sfxc_gpu_config *config);

@@ -3,6 +3,7 @@
 // the byte layout of the correlator output (Correlation_core::integration_write,
 // sfxc/src/correlation_core.cc:316-477; headers sfxc/include/output_header.h:100-148).
 #include <algorithm>
+#include <tuple>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -144,6 +145,10 @@ struct sfxc_gpu_ctx {
   std::vector<Baseline> bl;
   JobTables jt;
   int M = 0, K = 0, Nd = 0, kpad = 0, nffts = 0, nsub = 0, nbins = 1;
+  // spectral reduction: output channels nch (< M when reducing), Kout = nch + 1;
+  // mask (M + 1), lag window (2 nch), exp(-2 pi i k / 2M) (k < 2M), reduced output
+  int nch = 0, Kout = 0, rnorm = 0;
+  DevBuf rmask, rlag, rtw, rout;
   // device
   DevBuf streamdev, tw256, ts, spec, acc, out, norms, flagfac, blmap, tiles, blpairs, items, bins,
       offsets, derr;
@@ -208,11 +213,58 @@ void put(std::vector<uint8_t> &o, const T &v) {
   o.insert(o.end(), p, p + sizeof(T));
 }
 
+// Lag window of the spectral reduction when the ctrl file gives none:
+// Correlation_core::create_window (sfxc/src/correlation_core.cc:760-810) for
+// n = 2 nch lags out of m = 2M, with the cos / hamming / hann functions of
+// (n, i) and convolve (667-706), in FP64, kept in FP32 as the reference
+// keeps it.  The convolutions cost O(n m): kept per (nch, M, window).
+std::vector<float> reduction_window(int nch, int M, int window) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int>, std::vector<float>> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_tuple(nch, M, window);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  const int n = 2 * nch, m = 2 * M;
+  std::vector<double> w(n, 0.0);
+  if (window == WINDOW_NONE || window == WINDOW_RECT) {
+    w[0] = 1.;
+    for (int i = 1; i < n / 2; i++) w[i] = w[n - i] = (1. - 2. * i / n) / (1. - 2. * i / m);
+    w[n / 2] = 0.;
+  } else {
+    auto f = [window](int len, int i) {
+      if (window == WINDOW_COS) return std::sin(M_PI * i / len);
+      if (window == WINDOW_HAMMING) return 0.54 - 0.46 * std::cos(2 * M_PI * i / len);
+      return 0.5 * (1 - std::cos(2 * M_PI * i / len));
+    };
+    std::vector<double> fn(n + 1), fm(m + 1);
+    for (int j = 0; j <= n; j++) fn[j] = f(n, j);
+    for (int j = 0; j <= m; j++) fm[j] = f(m, j);
+    auto conv = [](const std::vector<double> &fv, int len, int i) {  // sum over j of f(j) f(i + len/2 - j)
+      double sum = 0.0;
+      i += len / 2;
+      for (int j = 0; j <= len; j++) {
+        if (i - j < 0 || i - j > len) continue;
+        sum += fv[j] * fv[i - j];
+      }
+      return sum;
+    };
+    const int r = m / n;  // integer ratio, as in the reference
+    w[0] = r * conv(fn, n, n / 2) / conv(fm, m, m / 2);
+    for (int i = 1; i < n / 2; i++) w[i] = w[n - i] = r * conv(fn, n, n / 2 + i) / conv(fm, m, m / 2 + i);
+    w[n / 2] = r * conv(fn, n, n) / conv(fm, m, (n + m) / 2);
+  }
+  std::vector<float> out(w.begin(), w.end());
+  cache.emplace(key, out);
+  return out;
+}
+
 void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
   if (!p || p->n_streams <= 0 || !p->streams) throw Error(SFXC_GPU_EINVAL, "no streams");
   if (p->fft_size_delaycor != kNd) throw Error(SFXC_GPU_EINVAL, "fft_size_delaycor must be 256");
-  if (p->number_channels != p->fft_size_correlation)
-    throw Error(SFXC_GPU_EINVAL, "spectral reduction (number_channels != fft_size_correlation) is not supported");
+  if (p->number_channels < 2 || p->number_channels > p->fft_size_correlation ||
+      (p->number_channels & (p->number_channels - 1)))
+    throw Error(SFXC_GPU_EINVAL, "number_channels must be a power of two no larger than fft_size_correlation");
   if (p->fft_size_correlation < kNd || (p->fft_size_correlation & (p->fft_size_correlation - 1)))
     throw Error(SFXC_GPU_EINVAL, "fft_size_correlation must be a power of two >= 256");
   if (p->window < WINDOW_NONE || p->window > WINDOW_HANN) throw Error(SFXC_GPU_EINVAL, "invalid window");
@@ -220,6 +272,7 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
   c->p = *p;
   c->p.streams = nullptr;
   c->p.delay_tables = nullptr;
+  c->p.mask = c->p.lag_window = nullptr;  // caller-owned; copied below
   c->p.polyco = nullptr;
   c->tables.clear();
   for (int i = 0; i < p->n_delay_tables; i++) {
@@ -259,6 +312,23 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
   }
   c->M = p->fft_size_correlation;
   c->K = c->M + 1;
+  c->nch = p->number_channels;
+  c->Kout = c->nch + 1;
+  if (c->nch < c->M) {  // spectral reduction tables
+    std::vector<float> mk(p->mask ? p->mask : nullptr, p->mask ? p->mask + c->M + 1 : nullptr);
+    if (!p->mask) mk.assign(c->M + 1, 1.0f);
+    std::vector<float> lw = p->lag_window ? std::vector<float>(p->lag_window, p->lag_window + 2 * c->nch)
+                                          : reduction_window(c->nch, c->M, p->window);
+    std::vector<float2> tw(2 * (size_t)c->M);
+    for (size_t k = 0; k < tw.size(); k++) {
+      const double a = -M_PI * (double)k / c->M;
+      tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    upload(c->rmask, mk.data(), mk.size() * sizeof(float), c->st);
+    upload(c->rlag, lw.data(), lw.size() * sizeof(float), c->st);
+    upload(c->rtw, tw.data(), tw.size() * sizeof(float2), c->st);
+    c->rnorm = p->mask_normalize != 0;
+  }
   c->Nd = p->fft_size_delaycor;
   c->kpad = c->M + 4;
   const int nr = nr_ffts_per_integration_slice((double)p->integration_time_us, p->sample_rate, c->M);
@@ -398,7 +468,7 @@ void serialize_integration(sfxc_gpu_ctx *c, const float2 *vis, int32_t source_nr
     for (int k = 0; k < 5; k++) put(o, l[k]);
   }
   const int64_t total = (int64_t)c->nffts * c->M;
-  const size_t K = (size_t)c->M + 1;
+  const size_t K = (size_t)c->Kout;  // output channels + 1
   for (int b = 0; b < nbl; b++) {
     int lv[5];
     c->sc[c->bl[b].a].stats.levels(lv);
@@ -732,12 +802,20 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     launch_normalize(c->acc.as<float2>() + (size_t)bin * nbl * kpad, kpad, M, N, nbl, c->blpairs.as<int>(),
                      c->norms.as<double>(), c->flagfac.as<double>(), c->out.as<float2>() + (size_t)bin * nbl * K, st);
   CK(cudaGetLastError());
-  const size_t nvis = (size_t)c->nbins * nbl * K;
+  const float2 *vsrc = c->out.as<float2>();
+  if (c->nch < M) {
+    c->rout.ensure((size_t)c->nbins * nbl * c->Kout * sizeof(float2));
+    CK(launch_reduce(c->out.as<float2>(), c->nbins * nbl, M, c->nch, c->rmask.as<float>(), c->rlag.as<float>(),
+                     c->rnorm, c->rtw.as<float2>(), c->rout.as<float2>(), st));
+    vsrc = c->rout.as<float2>();
+    launches += 1;
+  }
+  const size_t nvis = (size_t)c->nbins * nbl * c->Kout;
   uint8_t *res = static_cast<uint8_t *>(c->results.ensure(nvis * sizeof(float2) + (size_t)N * 64 + 16));
   const float2 *vis = reinterpret_cast<const float2 *>(res);
   const unsigned long long *hist = reinterpret_cast<const unsigned long long *>(res + nvis * sizeof(float2));
   const int *dev_err = reinterpret_cast<const int *>(res + nvis * sizeof(float2) + (size_t)N * 64);
-  CK(cudaMemcpyAsync(res, c->out.p, nvis * sizeof(float2), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(res, vsrc, nvis * sizeof(float2), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(res + nvis * sizeof(float2), c->hist.p, (size_t)N * 64, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(res + nvis * sizeof(float2) + (size_t)N * 64, c->derr.p, sizeof(int), cudaMemcpyDeviceToHost,
                      st));
@@ -776,7 +854,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   }
   // ---- output bytes (integration_write per bin) and tsys records
   std::vector<uint8_t> o;
-  for (int bin = 0; bin < c->nbins; bin++) serialize_integration(c, vis + (size_t)bin * nbl * K, pulsar ? bin : 0, nfl, o);
+  for (int bin = 0; bin < c->nbins; bin++)
+    serialize_integration(c, vis + (size_t)bin * nbl * c->Kout, pulsar ? bin : 0, nfl, o);
   if (sink && sink(user, 0, o.data(), o.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
   for (int i = 0; i < N; i++) {
     std::vector<uint8_t> t;

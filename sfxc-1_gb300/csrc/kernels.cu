@@ -934,6 +934,94 @@ __global__ void normalize_kernel(const float2 *__restrict__ acc, int kpad, int M
 }
 
 // ------------------------------------------------------------------------
+// Spectral reduction (number_channels < fft_size_correlation):
+// Correlation_core::integration_write, sfxc/src/correlation_core.cc:413-439.
+// One CTA per normalised spectrum X[0..M]: optional normalisation to unit
+// amplitude, the mask, an unnormalised complex-to-real FFT of 2M points (the
+// imaginary parts of DC and Nyquist ignored) as one M-point complex FFT of
+// the even and odd lags, the lags folded to 2 nch (lag nch the mean of +-nch),
+// the lag window, a real FFT of 2 nch points as one nch-point complex FFT and
+// the real split, a division by 2M.  Both transforms are in-place radix-2 in
+// shared memory: the work is one spectrum per baseline per integration.
+
+// in-place radix-2 transform of the 2^logn values a[] in bit-reversed order:
+// sign -1 forward, +1 backward; twiddles exp(-2 pi i j / len) = tw2M[j 2M / len]
+__device__ void smem_fft_radix2(float2 *a, int logn, int sign, const float2 *__restrict__ tw2M, int M) {
+  const int n = 1 << logn;
+  for (int s = 1; s <= logn; s++) {
+    const int len = 1 << s, half = len >> 1, stride = (2 * M) >> s;
+    for (int b = threadIdx.x; b < n / 2; b += blockDim.x) {
+      const int j = b & (half - 1), i = (b - j) * 2 + j;
+      float2 w = __ldg(tw2M + j * stride);
+      if (sign > 0) w.y = -w.y;
+      const float2 u = a[i], x = a[i + half];
+      const float2 v = make_float2(x.x * w.x - x.y * w.y, x.x * w.y + x.y * w.x);
+      a[i] = make_float2(u.x + v.x, u.y + v.y);
+      a[i + half] = make_float2(u.x - v.x, u.y - v.y);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) reduce_kernel(const float2 *__restrict__ in, int M, int logM, int nch,
+                                                     int lognch, const float *__restrict__ mask,
+                                                     const float *__restrict__ lagwin, int normalize,
+                                                     const float2 *__restrict__ tw2M, float2 *__restrict__ out) {
+  extern __shared__ __align__(16) float2 rsm[];
+  float2 *a = rsm;                                   // M complex
+  float *lag = reinterpret_cast<float *>(rsm + M);   // 2 nch lags
+  const float2 *X = in + (size_t)blockIdx.x * (M + 1);
+  auto load = [&](int k) {
+    float2 x = X[k];
+    if (normalize) {
+      const float m = hypotf(x.x, x.y);
+      if (m != 0.0f) x = make_float2(x.x / m, x.y / m);
+    }
+    const float mk = mask[k];
+    return make_float2(x.x * mk, x.y * mk);
+  };
+  // c2r of 2M points: even lags e = IDFT(X[k] + conj X[M-k]), odd lags
+  // o = IDFT((X[k] - conj X[M-k]) e^{i pi k / M}); z = e + i o
+  for (int k = threadIdx.x; k < M; k += blockDim.x) {
+    float2 xk = load(k), xm = load(M - k);
+    if (k == 0) xk.y = xm.y = 0.0f;
+    const float2 e = make_float2(xk.x + xm.x, xk.y - xm.y);
+    const float2 d = make_float2(xk.x - xm.x, xk.y + xm.y);
+    const float2 w = __ldg(tw2M + k);  // exp(-i pi k / M); d * conj(w)
+    const float2 o = make_float2(d.x * w.x + d.y * w.y, d.y * w.x - d.x * w.y);
+    a[__brev((unsigned)k) >> (32 - logM)] = make_float2(e.x - o.y, e.y + o.x);
+  }
+  __syncthreads();
+  smem_fft_radix2(a, logM, +1, tw2M, M);
+  auto lag_at = [&](int q) { return (q & 1) ? a[q >> 1].y : a[q >> 1].x; };  // r[q], q < 2M
+  for (int q = threadIdx.x; q < 2 * nch; q += blockDim.x) {
+    float v;
+    if (q < nch)
+      v = lag_at(q);
+    else if (q == nch)
+      v = (lag_at(nch) + lag_at(2 * M - nch)) / 2;
+    else
+      v = lag_at(2 * M - nch + (q - nch));
+    lag[q] = v * lagwin[q];
+  }
+  __syncthreads();
+  for (int n = threadIdx.x; n < nch; n += blockDim.x)
+    a[__brev((unsigned)n) >> (32 - lognch)] = make_float2(lag[2 * n], lag[2 * n + 1]);
+  __syncthreads();
+  smem_fft_radix2(a, lognch, -1, tw2M, M);
+  // r2c split: A[k] = E + W^k O, W = exp(-2 pi i / 2nch) = tw2M[M / nch]
+  float2 *Y = out + (size_t)blockIdx.x * (nch + 1);
+  const float scale = (float)(2 * M);
+  for (int k = threadIdx.x; k <= nch; k += blockDim.x) {
+    const float2 zk = a[k & (nch - 1)], zc = a[(nch - k) & (nch - 1)];
+    const float er = 0.5f * (zk.x + zc.x), ei = 0.5f * (zk.y - zc.y);
+    const float orr = 0.5f * (zk.y + zc.y), oi = -0.5f * (zk.x - zc.x);
+    const float2 w = __ldg(tw2M + (size_t)k * (M / nch));
+    Y[k] = make_float2((er + (orr * w.x - oi * w.y)) / scale, (ei + (orr * w.y + oi * w.x)) / scale);
+  }
+}
+
+// ------------------------------------------------------------------------
 // launchers
 static int sm_count() {
   static int n = 0;
@@ -1019,6 +1107,17 @@ void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int n
 
 void launch_bitstat(const StreamDev *d_streams, const int4 *d_items, int nitems, cudaStream_t st) {
   if (nitems > 0) bitstat_kernel<<<nitems, 256, 0, st>>>(d_streams, d_items, nitems);
+}
+
+cudaError_t launch_reduce(const float2 *in, int nspec, int M, int nch, const float *mask, const float *lag_window,
+                          int normalize, const float2 *tw2M, float2 *out, cudaStream_t st) {
+  if (nspec <= 0) return cudaSuccess;
+  const int logM = 31 - __builtin_clz((unsigned)M), lognch = 31 - __builtin_clz((unsigned)nch);
+  const size_t smem = (size_t)M * sizeof(float2) + (size_t)2 * nch * sizeof(float);
+  cudaError_t e = cudaFuncSetAttribute(reduce_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  reduce_kernel<<<nspec, 256, smem, st>>>(in, M, logM, nch, lognch, mask, lag_window, normalize, tw2M, out);
+  return cudaGetLastError();
 }
 
 static int xcorr_threads(int ntiles, int tpw) {

@@ -24,10 +24,16 @@ void launch_pulsar(const float2 *spec, int nrows_total, int kpad, int nstreams, 
                    double fft_duration, const double *offsets, double g0, double g1, int nbins, int16_t *bins,
                    float2 *acc, cudaStream_t st);
 size_t xcorr_tc_smem_bytes();
-// TC spectra: [row][channel (kpad)][32 stream slots] of 4 FP16 (hi.re, hi.im, lo.re, lo.im).
+// TC spectra: per row, channels x 32 stream slots of 4 FP16 (hi.re, hi.im, lo.re, lo.im), in the
+// line-complete order of tc_index.
 cudaError_t launch_xcorr_tc(const void *spec, int nrows, int kpad, int K, const int *blmap, int npad,
                             float inv_scale2, float2 *acc, int *err, cudaStream_t st);
 void launch_normalize(const float2 *acc, int kpad, int M, int nstreams, int nbl, const int *bl, double *norms,
                       const double *flagfac, float2 *out, cudaStream_t st);
+// Spectral reduction of nspec normalised spectra of M + 1 channels to nch + 1
+// channels (M, nch powers of two, nch < M); mask: M + 1 values, lag_window:
+// 2 nch values, tw2M: exp(-2 pi i k / 2M) for k < 2M.
+cudaError_t launch_reduce(const float2 *in, int nspec, int M, int nch, const float *mask, const float *lag_window,
+                          int normalize, const float2 *tw2M, float2 *out, cudaStream_t st);
 
 }  // namespace sfxc

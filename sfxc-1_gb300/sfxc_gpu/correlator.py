@@ -104,6 +104,13 @@ class CorrelatorNode:
             p.n_polyco = len(job["polyco"])
             p.polyco = pcs
             keep.append(pcs)
+        # Mask_parameters of the spectral reduction
+        for key in ("mask", "lag_window"):
+            if job.get(key) is not None:
+                arr = np.ascontiguousarray(job[key], dtype=np.float32)
+                setattr(p, key, arr.ctypes.data_as(C.POINTER(C.c_float)))
+                keep.append(arr)
+        p.mask_normalize = int(bool(job.get("mask_normalize", 0)))
         keep += [tables, streams]
         self._check(self._lib.sfxc_gpu_set_parameters(self._h, C.byref(p)))
         self._keep = keep

@@ -55,7 +55,9 @@ class CorrelationParams(C.Structure):
                 ("n_streams", C.c_int32), ("streams", C.POINTER(StationStream)),
                 ("n_delay_tables", C.c_int32), ("delay_tables", C.POINTER(DelayTable)),
                 ("pulsar_nbins", C.c_int32), ("gate_start", C.c_double), ("gate_stop", C.c_double),
-                ("n_polyco", C.c_int32), ("polyco", C.POINTER(Polyco))]
+                ("n_polyco", C.c_int32), ("polyco", C.POINTER(Polyco)),
+                ("mask", C.POINTER(C.c_float)), ("lag_window", C.POINTER(C.c_float)),
+                ("mask_normalize", C.c_int32)]
 
 
 class ChannelBlock(C.Structure):

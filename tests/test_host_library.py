@@ -72,3 +72,18 @@ def test_no_cpu_fallback(sfxc_lib):
     from sfxc_gpu import correlator, lib
     with pytest.raises(lib.SfxcError):
         correlator.CorrelatorNode(0)
+
+
+@pytest.mark.gpu
+def test_reduction_parameters_are_checked(sfxc_lib):
+    """number_channels must be a power of two no larger than the correlation
+    FFT size (spectral reduction); a bad value fails before any device work."""
+    from sfxc_gpu import correlator, lib, scenario
+    sc = scenario.c1_plain(integration_us=15625, n_integrations=1, seed=1)
+    job = scenario.build_job(sc, correlator.delay_list, correlator.write_protocol, fast_random=True)
+    for bad in (3, 0, 1024):
+        j = dict(job, number_channels=bad)
+        node = correlator.CorrelatorNode(0, lib.X_FP32)
+        with pytest.raises(lib.SfxcError, match="number_channels"):
+            node.set_parameters(j)
+        node.close()
