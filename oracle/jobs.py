@@ -184,6 +184,10 @@ def correlate(job, dump=False, impl="reference", precision=32):
                 lines.append((key, p))
         if job.get("mask_normalize"):
             lines.append(("mask_normalize", 1))
+        if int(job.get("n_phase_centers", 1)) > 1:
+            lines.append(("n_phase_centers", int(job["n_phase_centers"])))
+            if job.get("pc_file_index") is not None:
+                lines.append(("pc_file_index",) + tuple(int(x) for x in job["pc_file_index"]))
         if "pulsar" in job:
             lines.append(("pulsar",) + tuple(job["pulsar"]))
             for pc in job["polyco"]:

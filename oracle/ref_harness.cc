@@ -371,7 +371,7 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
   p.window = geti(kv, "window");
   std::memset(p.source, 0, sizeof(p.source));
   std::strncpy(p.source, get(kv, "source")[0].c_str(), 10);
-  p.n_phase_centers = 1;
+  p.n_phase_centers = has(kv, "n_phase_centers") ? geti(kv, "n_phase_centers") : 1;
   p.pulsar_binning = has(kv, "pulsar") ? 1 : 0;
   p.pulsar_parameters = 0;
   p.mask_parameters = 0;
@@ -483,7 +483,7 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
     }
     // Correlator_node::set_parameters (sfxc/src/correlator_node.cc:311-406)
     std::vector<Delay_table_akima> akima(max_stream + 1);
-    std::vector<std::vector<double> > uvw(max_stream + 1, std::vector<double>(3, 0.0));
+    std::vector<std::vector<double> > uvw(max_stream + 1, std::vector<double>(3 * p.n_phase_centers, 0.0));
     for (int i = 0; i < nstreams; i++) {
       int s = p.station_streams[i].station_stream;
       akima[s] = tables[stream_station_index[i]].create_akima_spline(p.start_time, p.integration_time);

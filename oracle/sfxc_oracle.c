@@ -142,8 +142,8 @@ static void deltable_read(deltable_t *t, const char *path) {
     scan_t *s = &t->scans[t->nscans++];
     s->begin = t_from_mjd_sec(mjd, scan_start);
     s->times = s->vals = t->nrows;
-    /* additional phase centre of the same scan: rows overwrite the times
-       (delay_table_akima.cc:330-336); the restatement keeps one centre. */
+    /* an additional phase centre of the same scan is a scan with the same
+       start (delay_table_akima.cc:330-336): its rows repeat the times */
     for (;;) {
       if (line[0] == 0 && line[4] == 0) {
         if (t->nrows - s->times == 1) die("delay table scan with a single row");
@@ -204,8 +204,14 @@ static void akima_coeffs(const double *x, const double *y, int size, double *b, 
   free(mbuf);
 }
 
-/* Delay_table::create_akima_spline (delay_table_akima.cc:431-502) */
+/* Delay_table::create_akima_spline (delay_table_akima.cc:431-502); phase
+   centre pc: the pc-th scan starting with the covering one (an additional
+   phase centre is a scan with the same start, 313-336, 478-494) */
+static void akima_create_pc(akima_t *a, const deltable_t *t, ticks_t start_, ticks_t duration, int pc);
 static void akima_create(akima_t *a, const deltable_t *t, ticks_t start_, ticks_t duration) {
+  akima_create_pc(a, t, start_, duration, 0);
+}
+static void akima_create_pc(akima_t *a, const deltable_t *t, ticks_t start_, ticks_t duration, int pc) {
   int mjd_start = (int)floor(t_get_mjd(start_));
   double seconds_start = floor(t_get_time_usec(start_) / 1000000);
   ticks_t stop = start_ + duration;
@@ -216,7 +222,9 @@ static void akima_create(akima_t *a, const deltable_t *t, ticks_t start_, ticks_
   int sn = 0;
   while (sn < t->nscans && stop > t->scans[sn].end) sn++;
   if (sn == t->nscans) die("time is not in the delay table");
-  const scan_t *s = &t->scans[sn];
+  if (sn + pc >= t->nscans || t->scans[sn + pc].begin != t->scans[sn].begin)
+    die("delay table has fewer phase centres than requested");
+  const scan_t *s = &t->scans[sn + pc];
   if (t_diff(s->end, s->begin) < 4.) die("delay table scan shorter than 4 s");
   ticks_t onesec = t_from_usec(1000000.);
   ticks_t ib = start - t_mul(onesec, 2);
@@ -660,6 +668,10 @@ typedef struct {
      NULL / 0 when absent (mask of ones, window from the window type) */
   double *mask, *lag_window;
   int mask_normalize;
+  /* phase centres (Correlation_parameters::n_phase_centers) and the output
+     file index of each (the manager's source list; 0 when absent) */
+  int n_pc;
+  int *pc_file;
 } job_t;
 
 /* ------------------------------------------------------------- statistics ---
@@ -1344,6 +1356,72 @@ static void reduce_spectrum(const job_t *j, const double *x, double *y) {
   free(re), free(im), free(lag), free(li);
 }
 
+/* -------------------------------------------------- extra phase centres ---
+ * Correlation_core::create_weights (sfxc/src/correlation_core.cc:708-744):
+ * the autocorrelation of the zero-padded window over 2M - 1 points, through
+ * an FP32 r2c / c2r pair of 4M points, normalised at lag 0. */
+static double pc_window_f(int type, int n, int i) { /* rect / cos / hamming / hann (667-690) */
+  switch (type) {
+    case WINDOW_NONE:
+    case WINDOW_RECT: return (i >= n / 4 && i < (3 * n) / 4) ? 1.0 : 0.0;
+    case WINDOW_COS: return sin(M_PI * i / n);
+    case WINDOW_HAMMING: return 0.54 - 0.46 * cos(2 * M_PI * i / n);
+    default: return 0.5 * (1 - cos(2 * M_PI * i / n));
+  }
+}
+static const double *pc_weights(const job_t *j) {
+  static double *w = NULL;
+  if (w) return w;
+  const int n = j->M, n4 = 4 * n;
+  fftplan_t *p = fft_plan(n4);
+  double *re = xmalloc(n4 * 8), *im = xmalloc(n4 * 8);
+  for (int i = 0; i < 2 * n; i++) re[i] = st(pc_window_f(j->window, 2 * n - 1, i));
+  fft_c(p, re, im, -1);
+  for (int q = 0; q <= 2 * n; q++) { /* conj(F) F in FP32 */
+    const double a = st(re[q]), b = st(im[q]);
+    re[q] = st(st(a * a) + st(b * b));
+    im[q] = 0;
+  }
+  for (int q = 2 * n + 1; q < n4; q++) re[q] = re[n4 - q], im[q] = 0;
+  im[0] = im[2 * n] = 0;
+  fft_c(p, re, im, +1);
+  w = xmalloc(n * 8);
+  const double t0 = st(re[0]);
+  for (int i = 0; i < n; i++) w[i] = st(st(re[i]) / t0);
+  free(re), free(im);
+  return w;
+}
+/* Correlation_core::uvshift (sfxc/src/correlation_core.cc:561-593): one
+   baseline's sub-integration spectrum in[K] rotated by the residual delay of
+   an extra phase centre and added to out[K]; FP32 products, FP64 phase
+   recurrence, as the reference. */
+static void uvshift_add(const job_t *j, const double *in, double *out, double dd1, double dd2, double r1,
+                        double r2) {
+  const int K = j->M + 1;
+  const int sb = j->sideband == 'L' ? -1 : 1;
+  const double base_freq = (double)j->channel_freq;
+  const double dfreq = j->sample_rate / (2. * j->M);
+  const double *weights = pc_weights(j);
+  double amplitude = 1;
+  const int lag = abs((int)round((dd1 - dd2) * j->sample_rate));
+  if (lag < j->M && weights[lag] > 1e-4) amplitude = st(1. / weights[lag]);
+  double phi = base_freq * (dd1 * (1 - r1) - dd2 * (1 - r2));
+  phi = 2 * M_PI * sb * (phi - floor(phi));
+  const double delta = 2 * M_PI * dfreq * (dd1 * (1 - r1) - dd2 * (1 - r2));
+  double temp = sin(delta / 2);
+  const double a = 2 * temp * temp, b = sin(delta);
+  double c = cos(phi), s = sin(phi);
+  for (int i = 0; i < K; i++) {
+    const double xr = st(amplitude * in[2 * i]), xi = st(amplitude * in[2 * i + 1]);
+    const double cf = st(c), sf = st(s);
+    out[2 * i] = st(out[2 * i] + st(st(xr * cf) - st(xi * sf)));
+    out[2 * i + 1] = st(out[2 * i + 1] + st(st(xr * sf) + st(xi * cf)));
+    temp = s - (a * s - b * c);
+    c = c - (a * c + b * s);
+    s = temp;
+  }
+}
+
 static void write_integration(const job_t *j, const bl_t *bl, int nbl, const double *acc, b2f_t *w,
                               int64_t (*nfl)[2], int nffts, int integration, int32_t sourcenr, bytes_t *out,
                               bytes_t *out64) {
@@ -1680,6 +1758,15 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
   j.dump = de && atoi(de->v[0]);
   if (j.number_channels < 2 || j.number_channels > j.M || (j.number_channels & (j.number_channels - 1)))
     die("number_channels must be a power of two no larger than the FFT size");
+  kv_t *npc = kv_get(k, "n_phase_centers", 0);
+  j.n_pc = npc ? atoi(npc->v[0]) : 1;
+  if (j.n_pc < 1) die("n_phase_centers must be at least 1");
+  j.pc_file = xmalloc(j.n_pc * sizeof(int));
+  kv_t *pcf = kv_get(k, "pc_file_index", 0);
+  if (pcf) {
+    if (pcf->nv != j.n_pc) die("pc_file_index needs n_phase_centers values");
+    for (int q = 0; q < j.n_pc; q++) j.pc_file[q] = atoi(pcf->v[q]);
+  }
   kv_t *mn = kv_get(k, "mask_normalize", 0);
   j.mask_normalize = mn && atoi(mn->v[0]);
   /* mask and lag window: files of float32 values */
@@ -1765,6 +1852,10 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
     double **rows = xmalloc(j.nstreams * sizeof(double *));
     int *chunk = NULL;
     int nchunks = 0;
+    /* splines of the extra phase centres (index 1..n_pc-1), per stream */
+    akima_t *akp = xmalloc((size_t)j.nstreams * j.n_pc * sizeof(akima_t));
+    for (int i = 0; i < j.nstreams; i++)
+      for (int c = 1; c < j.n_pc; c++) akima_create_pc(&akp[i * j.n_pc + c], &tables[j.streams[i].table], start, tint, c);
     for (int i = 0; i < j.nstreams; i++) {
       stream_t *s = &j.streams[i];
       akima_create(&ak[i], &tables[s->table], start, tint);
@@ -1826,21 +1917,39 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
     find_invalid(&j, bl, nbl, w, nfl);
     if (!j.pulsar) {
       double *acc = xmalloc((size_t)nbl * K * 2 * sizeof(double));
-      double *pc = xmalloc((size_t)nbl * K * 2 * sizeof(double));
-      int cur = 0, next_sub = 1;
+      double *pc = xmalloc((size_t)j.n_pc * nbl * K * 2 * sizeof(double)); /* phase_centers[c][b][k] */
+      const size_t PCS = (size_t)nbl * K * 2;
+      int cur = 0, next_sub = 1, prev = 0;
+      const ticks_t tfft = (ticks_t)M * (ticks_t)(int)round(512000000.0 / j.sample_rate); /* Time(0, sr).inc_samples(M) */
       for (int c = 0; c < nchunks; c++) { /* Correlation_core::do_task per buffer (20-73) */
         xstep_rows(&j, bl, nbl, rows, stride, cur, cur + chunk[c], acc);
         cur += chunk[c];
-        if (cur == nffts || cur >= next_sub * nsub) {
-          for (size_t q = 0; q < (size_t)nbl * K * 2; q++) {
-            pc[q] = st(pc[q] + acc[q]);
-            acc[q] = 0;
+        if (cur == nffts || cur >= next_sub * nsub) { /* sub_integration (516-559) */
+          for (size_t q = 0; q < PCS; q++) pc[q] = st(pc[q] + acc[q]);
+          if (j.n_pc > 1) {
+            const ticks_t tmid = start + t_mul(tfft, prev + (cur - prev) / 2.);
+            for (int c2 = 1; c2 < j.n_pc; c2++) {
+              double *pcc = pc + c2 * PCS;
+              for (size_t q = 0; q < (size_t)j.nstreams * K * 2; q++) pcc[q] = st(pcc[q] + acc[q]); /* autos */
+              for (int b = j.nstreams; b < nbl; b++) {
+                const int s1 = bl[b].a, s2 = bl[b].b;
+                const double d1 = dt_delay(&ak[s1], tmid), d2 = dt_delay(&ak[s2], tmid);
+                const double dd1 = dt_delay(&akp[s1 * j.n_pc + c2], tmid) - d1;
+                const double dd2 = dt_delay(&akp[s2 * j.n_pc + c2], tmid) - d2;
+                uvshift_add(&j, acc + (size_t)b * K * 2, pcc + (size_t)b * K * 2, dd1, dd2, dt_rate(&ak[s1], tmid),
+                            dt_rate(&ak[s2], tmid));
+              }
+            }
           }
+          for (size_t q = 0; q < PCS; q++) acc[q] = 0;
+          prev = cur;
           if (cur != nffts) next_sub++;
         }
       }
-      normalize(&j, bl, nbl, pc, w, nfl, nffts);
-      write_integration(&j, bl, nbl, pc, w, nfl, nffts, it, 0, &cor, &cor64);
+      for (int c2 = 0; c2 < j.n_pc; c2++) {
+        normalize(&j, bl, nbl, pc + c2 * PCS, w, nfl, nffts);
+        write_integration(&j, bl, nbl, pc + c2 * PCS, w, nfl, nffts, it, j.pc_file[c2], &cor, &cor64);
+      }
       free(acc);
       free(pc);
     } else {
@@ -1954,6 +2063,7 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
     for (int i = 0; i < j.nstreams; i++) {
       free(rows[i]);
       akima_free(&ak[i]);
+      for (int c = 1; c < j.n_pc; c++) akima_free(&akp[i * j.n_pc + c]);
     }
     free(rows);
     free(ak);

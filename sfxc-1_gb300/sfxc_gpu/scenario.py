@@ -42,6 +42,8 @@ class Scenario:
     station_sidebands: dict = field(default_factory=dict)  # station number -> sideband
     nchan: int = 512
     number_channels: int = 0            # output channels (spectral reduction); 0: nchan
+    # extra phase centres: per centre, (source name, per-station delay offsets in seconds)
+    extra_centers: list = field(default_factory=list)
     window: int = 4
     integration_us: int = 15625
     sub_integration_us: int = 125000
@@ -69,7 +71,19 @@ class Scenario:
 
 
 def del_tables(sc: Scenario):
-    return [synth.del_file_bytes(st.name[:2], [("SRC", sc.mjd, sc.sec0 - 20, 140, st.poly)]) for st in sc.stations]
+    """One .del per station: the scan of the pointing centre, then one scan
+    per extra phase centre with the same start (its delays offset)."""
+    out = []
+    for si, st in enumerate(sc.stations):
+        scans = [("SRC", sc.mjd, sc.sec0 - 20, 140, st.poly)]
+        for name, offsets in sc.extra_centers:
+            c = list(st.poly.coeffs)
+            c[0] += offsets[si]
+            poly = synth.DelayPoly(coeffs=tuple(c), t0=st.poly.t0, phase_coeffs=st.poly.phase_coeffs,
+                                   amp=st.poly.amp)
+            scans.append((name, sc.mjd, sc.sec0 - 20, 140, poly))
+        out.append(synth.del_file_bytes(st.name[:2], scans))
+    return out
 
 
 def channel_streams(sc: Scenario, fast_random=False):
@@ -152,7 +166,7 @@ def build_job(sc: Scenario, delay_fn, protocol_fn, fast_random=False):
                 sideband=sc.sideband, frequency_nr=sc.frequency_nr, polarisation=sc.pols[0],
                 cross_polarize=1 if len(sc.pols) > 1 else 0, reference_station=sc.reference_station,
                 window=sc.window, source="SRC", integration_nr=0, n_integrations=sc.n_integrations,
-                streams=streams, protocols=protos)
+                n_phase_centers=1 + len(sc.extra_centers), streams=streams, protocols=protos)
 
 
 def build_job_bulk(sc: Scenario, alloc=None):
@@ -193,7 +207,8 @@ def build_job_bulk(sc: Scenario, alloc=None):
                 sample_rate=sr, channel_freq=sc.channel_freq, bandwidth=sc.bandwidth, sideband=sc.sideband,
                 frequency_nr=sc.frequency_nr, polarisation=sc.pols[0], cross_polarize=1 if len(sc.pols) > 1 else 0,
                 reference_station=sc.reference_station, window=sc.window, source="SRC", integration_nr=0,
-                n_integrations=sc.n_integrations, streams=streams, protocols=protos)
+                n_integrations=sc.n_integrations, n_phase_centers=1 + len(sc.extra_centers), streams=streams,
+                protocols=protos)
 
 
 def c1_plain(integration_us=15625, n_integrations=2, seed=1):

@@ -60,6 +60,13 @@ def scenarios():
         stations=st2, sample_rate=32_000_000, bandwidth=16_000_000, bits=2, channel_freq=1_600_000_000,
         nchan=512, number_channels=64, window=0, integration_us=8000, n_integrations=1, rho=0.05, seed=19,
         block_bytes=8000)
+    # two extra phase centres (same scan, residual delays of up to a few samples
+    # between stations), sub-integrations of 2 ms: uvshift at every dump
+    st3 = scenario.cubic_stations(3, seed=41, max_delay=1e-3, max_rate=1e-5)
+    out["phase_centers"] = scenario.Scenario(
+        stations=st3, sample_rate=32_000_000, bandwidth=16_000_000, bits=2, channel_freq=1_600_000_000,
+        nchan=1024, integration_us=8000, sub_integration_us=2000, n_integrations=2, rho=0.05, seed=23,
+        block_bytes=8000, extra_centers=[("SRC2", (2.1e-8, -4.0e-8, 7.5e-8)), ("SRC3", (-1.3e-7, 0.6e-7, 0.0))])
     return out
 
 
