@@ -134,6 +134,14 @@ typedef struct {
   const float *mask;
   const float *lag_window;
   int32_t mask_normalize;
+  /* extra phase centres (Correlation_parameters::n_phase_centers; 0 or 1:
+   * the pointing centre only): each .del table then holds, per scan, that
+   * many scans with the same start, one per source; every centre's
+   * visibilities are written as their own output with the file index given
+   * here (the manager's source list; NULL: 0 for all).  Not with pulsar
+   * binning (Correlator_node::set_parameters, sfxc/src/correlator_node.cc:348-366). */
+  int32_t n_phase_centers;
+  const int32_t *phase_center_file_index;
 } sfxc_correlation_params;
 
 sfxc_gpu_ctx *sfxc_gpu_create(const sfxc_gpu_config *config);

@@ -102,6 +102,7 @@ struct StreamCtx {
   UnpackPlan plan;
   BitStats stats{};
   Spline sp;
+  std::vector<Spline> sp_pc;  // extra phase centres 1.. (host only: the uvshift parameters)
   int n_blocks = 0, nfft_max = 0, rot = 0, hop = 0;
   DevBuf src, segs, stat_rng, spline, bpar;
   void take_buffers(StreamCtx &o) {
@@ -149,6 +150,14 @@ struct sfxc_gpu_ctx {
   // mask (M + 1), lag window (2 nch), exp(-2 pi i k / 2M) (k < 2M), reduced output
   int nch = 0, Kout = 0, rnorm = 0;
   DevBuf rmask, rlag, rtw, rout;
+  // extra phase centres: count (1: the pointing centre only), output file
+  // index per centre, window-autocorrelation weights (create_weights), the
+  // centres' accumulators [centre][baseline][kpad] and the chunks' uvshift
+  // parameters [chunk][centre - 1][baseline]
+  int npc = 1;
+  std::vector<int32_t> pc_file;
+  std::vector<float> pc_weights;
+  DevBuf pcacc, uvp;
   // device
   DevBuf streamdev, tw256, ts, spec, acc, out, norms, flagfac, blmap, tiles, blpairs, items, bins,
       offsets, derr;
@@ -259,6 +268,43 @@ std::vector<float> reduction_window(int nch, int M, int window) {
   return out;
 }
 
+// Amplitude weights of the extra phase centres: Correlation_core::
+// create_weights (sfxc/src/correlation_core.cc:708-744) -- the
+// autocorrelation of the window of 2M - 1 points (rect / cos / hamming /
+// hann of (n, i), 667-690) zero-padded to 4M, normalised at lag 0, for lags
+// below M.  The reference takes it through FP32 FFTs; here an FP64 direct
+// sum (once per (M, window)), rounded to FP32.
+std::vector<float> phase_center_weights(int M, int window) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, std::vector<float>> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find({M, window});
+  if (it != cache.end()) return it->second;
+  const int n = 2 * M - 1;
+  std::vector<double> f(2 * M);
+  for (int i = 0; i < 2 * M; i++) {
+    if (window == WINDOW_NONE || window == WINDOW_RECT)
+      f[i] = (i >= n / 4 && i < (3 * n) / 4) ? 1.0 : 0.0;
+    else if (window == WINDOW_COS)
+      f[i] = std::sin(M_PI * i / n);
+    else if (window == WINDOW_HAMMING)
+      f[i] = 0.54 - 0.46 * std::cos(2 * M_PI * i / n);
+    else
+      f[i] = 0.5 * (1 - std::cos(2 * M_PI * i / n));
+    f[i] = (float)f[i];  // the reference keeps the window in FP32
+  }
+  std::vector<double> r(M);
+  for (int lag = 0; lag < M; lag++) {  // the zero padding makes the circular autocorrelation linear here
+    double sum = 0.0;
+    for (int i = 0; i + lag < 2 * M; i++) sum += f[i] * f[i + lag];
+    r[lag] = sum;
+  }
+  std::vector<float> w(M);
+  for (int lag = 0; lag < M; lag++) w[lag] = (float)(r[lag] / r[0]);
+  cache.emplace(std::make_pair(M, window), w);
+  return w;
+}
+
 void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
   if (!p || p->n_streams <= 0 || !p->streams) throw Error(SFXC_GPU_EINVAL, "no streams");
   if (p->fft_size_delaycor != kNd) throw Error(SFXC_GPU_EINVAL, "fft_size_delaycor must be 256");
@@ -310,10 +356,16 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
     }
     c->nbins = p->pulsar_nbins + 1;
   }
+  c->npc = std::max(1, (int)p->n_phase_centers);
+  if (c->npc > 1 && c->nbins > 1) throw Error(SFXC_GPU_EINVAL, "extra phase centres cannot be combined with pulsar binning");
+  c->pc_file.assign(c->npc, 0);
+  if (p->phase_center_file_index) c->pc_file.assign(p->phase_center_file_index, p->phase_center_file_index + c->npc);
+  c->p.phase_center_file_index = nullptr;
   c->M = p->fft_size_correlation;
   c->K = c->M + 1;
   c->nch = p->number_channels;
   c->Kout = c->nch + 1;
+  if (c->npc > 1) c->pc_weights = phase_center_weights(c->M, p->window);
   if (c->nch < c->M) {  // spectral reduction tables
     std::vector<float> mk(p->mask ? p->mask : nullptr, p->mask ? p->mask + c->M + 1 : nullptr);
     if (!p->mask) mk.assign(c->M + 1, 1.0f);
@@ -518,6 +570,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     StreamCtx &s = c->sc[i];
     const StationStream &ss = c->streams[i];
     s.sp = Spline::create(c->tables[c->stream_table[i]], start, tint);
+    s.sp_pc.clear();
+    for (int pc = 1; pc < c->npc; pc++) s.sp_pc.push_back(Spline::create(c->tables[c->stream_table[i]], start, tint, pc));
     std::vector<Record> recs(s.recs.begin() + (long)s.ust.rec, s.recs.end());
     recs.insert(recs.end(), s.pending.begin(), s.pending.end());
     s.pending.clear();
@@ -631,6 +685,10 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   c->acc.ensure(accn * sizeof(float2));
   CK(cudaMemsetAsync(c->acc.p, 0, accn * sizeof(float2), st));
   const bool pulsar = c->nbins > 1;
+  if (c->npc > 1) {
+    c->pcacc.ensure((size_t)c->npc * nbl * kpad * sizeof(float2));
+    CK(cudaMemsetAsync(c->pcacc.p, 0, (size_t)c->npc * nbl * kpad * sizeof(float2), st));
+  }
   std::vector<std::pair<int, int>> ranges;
   if (pulsar)
     ranges.push_back({0, c->nffts});  // no sub-integrations in Correlation_core_pulsar
@@ -642,6 +700,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   const int hop = c->sc[0].hop;
   const bool chunked = hop % kNd == 0;
   if (!chunked) {
+    if (c->npc > 1)
+      throw Error(SFXC_GPU_EINVAL, "extra phase centres need windowed-FFT hops of whole 256-sample blocks");
     ranges.assign(1, {0, c->nffts});
     max_rows = c->nffts;
   }
@@ -746,6 +806,36 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   c->streamdev.ensure(ranges.size() * per_chunk * sizeof(StreamDev));
   CK(cudaMemcpyAsync(c->streamdev.p, staged, ranges.size() * per_chunk * sizeof(StreamDev), cudaMemcpyHostToDevice,
                      st));
+  // uvshift of every chunk (sub-integration), cross baseline and extra centre:
+  // Correlation_core::sub_integration / uvshift (sfxc/src/correlation_core.cc:
+  // 516-593) in FP64 on the host -- tmid of the sub-integration, residual
+  // delays of the centre against the pointing centre, rates, amplitude from
+  // the window-autocorrelation weight of the residual lag
+  if (c->npc > 1) {
+    const ticks_t tfft = (ticks_t)M * (ticks_t)std::lround(512000000.0 / c->p.sample_rate);
+    const int sbs = c->p.sideband == 'L' ? -1 : 1;
+    const double base_freq = (double)c->p.channel_freq, dfreq = c->p.sample_rate / (2. * M);
+    std::vector<double4> uv(ranges.size() * (size_t)(c->npc - 1) * nbl, make_double4(0, 0, 0, 0));
+    for (size_t ch = 0; ch < ranges.size(); ch++) {
+      const int prev = ranges[ch].first, cur = ranges[ch].second;
+      const ticks_t tmid = start + time_mul(tfft, prev + (cur - prev) / 2.);
+      for (int pc = 1; pc < c->npc; pc++)
+        for (int b = N; b < nbl; b++) {
+          const StreamCtx &s1 = c->sc[c->bl[b].a], &s2 = c->sc[c->bl[b].b];
+          const double delay1 = s1.sp.delay(tmid), delay2 = s2.sp.delay(tmid);
+          const double dd1 = s1.sp_pc[pc - 1].delay(tmid) - delay1, dd2 = s2.sp_pc[pc - 1].delay(tmid) - delay2;
+          const double r1 = s1.sp.rate(tmid), r2 = s2.sp.rate(tmid);
+          float amplitude = 1;
+          const int lag = std::abs((int)std::round((dd1 - dd2) * c->p.sample_rate));
+          if (lag < M && c->pc_weights[lag] > 1e-4) amplitude = (float)(1. / c->pc_weights[lag]);
+          double phi = base_freq * (dd1 * (1 - r1) - dd2 * (1 - r2));
+          phi = 2 * M_PI * sbs * (phi - std::floor(phi));
+          const double delta = 2 * M_PI * dfreq * (dd1 * (1 - r1) - dd2 * (1 - r2));
+          uv[(ch * (c->npc - 1) + (pc - 1)) * nbl + b] = make_double4(phi, delta, amplitude, 0.0);
+        }
+    }
+    upload(c->uvp, uv.data(), uv.size() * sizeof(double4), st);
+  }
   CK(cudaEventRecord(c->ev[0], st));
   // bit statistics read only chunk-independent fields (source bytes, ranges, histograms)
   launch_bitstat(c->streamdev.as<StreamDev>(), c->items.as<int4>(), (int)items.size(), st);
@@ -784,6 +874,12 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
                        c->jt.ntiles, c->blmap.as<int>(), c->acc.as<float2>(), st);
     }
     CK(cudaGetLastError());
+    if (c->npc > 1) {  // the sub-integration into every phase centre
+      launch_pc_dump(c->acc.as<float2>(), c->pcacc.as<float2>(),
+                     c->uvp.as<double4>() + ch * (size_t)(c->npc - 1) * nbl, N, nbl, kpad, K, c->npc, st);
+      CK(cudaGetLastError());
+      launches += 1;
+    }
     CK(cudaEventRecord(c->evpool[ev + 3], st));
     ev += 4;
     launches += pulsar ? 5 : 4;  // parameters, blocks, window FFT, (pulsar bins,) X-step
@@ -797,20 +893,23 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   // ---- normalisation and statistics
   CK(cudaEventRecord(c->evpool[ev], st));
   c->norms.ensure((size_t)N * 8);
-  c->out.ensure((size_t)c->nbins * nbl * K * sizeof(float2));
-  for (int bin = 0; bin < c->nbins; bin++)
-    launch_normalize(c->acc.as<float2>() + (size_t)bin * nbl * kpad, kpad, M, N, nbl, c->blpairs.as<int>(),
-                     c->norms.as<double>(), c->flagfac.as<double>(), c->out.as<float2>() + (size_t)bin * nbl * K, st);
+  // outputs: the pulsar bins, or the phase centres (each normalised on its own)
+  const int nout = pulsar ? c->nbins : c->npc;
+  const float2 *accs = c->npc > 1 ? c->pcacc.as<float2>() : c->acc.as<float2>();
+  c->out.ensure((size_t)nout * nbl * K * sizeof(float2));
+  for (int bin = 0; bin < nout; bin++)
+    launch_normalize(accs + (size_t)bin * nbl * kpad, kpad, M, N, nbl, c->blpairs.as<int>(), c->norms.as<double>(),
+                     c->flagfac.as<double>(), c->out.as<float2>() + (size_t)bin * nbl * K, st);
   CK(cudaGetLastError());
   const float2 *vsrc = c->out.as<float2>();
   if (c->nch < M) {
-    c->rout.ensure((size_t)c->nbins * nbl * c->Kout * sizeof(float2));
-    CK(launch_reduce(c->out.as<float2>(), c->nbins * nbl, M, c->nch, c->rmask.as<float>(), c->rlag.as<float>(),
+    c->rout.ensure((size_t)nout * nbl * c->Kout * sizeof(float2));
+    CK(launch_reduce(c->out.as<float2>(), nout * nbl, M, c->nch, c->rmask.as<float>(), c->rlag.as<float>(),
                      c->rnorm, c->rtw.as<float2>(), c->rout.as<float2>(), st));
     vsrc = c->rout.as<float2>();
     launches += 1;
   }
-  const size_t nvis = (size_t)c->nbins * nbl * c->Kout;
+  const size_t nvis = (size_t)nout * nbl * c->Kout;
   uint8_t *res = static_cast<uint8_t *>(c->results.ensure(nvis * sizeof(float2) + (size_t)N * 64 + 16));
   const float2 *vis = reinterpret_cast<const float2 *>(res);
   const unsigned long long *hist = reinterpret_cast<const unsigned long long *>(res + nvis * sizeof(float2));
@@ -820,7 +919,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   CK(cudaMemcpyAsync(res + nvis * sizeof(float2) + (size_t)N * 64, c->derr.p, sizeof(int), cudaMemcpyDeviceToHost,
                      st));
   CK(cudaEventRecord(c->evpool[ev + 1], st));
-  launches += 2 * c->nbins;
+  launches += 2 * nout;
   CK(cudaStreamSynchronize(st));
   if (*dev_err) throw Error(SFXC_GPU_ECUDA, "tensor-core X-step timed out waiting for its MMAs");
   for (size_t q = 0; q + 4 <= ev; q += 4) {
@@ -854,8 +953,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   }
   // ---- output bytes (integration_write per bin) and tsys records
   std::vector<uint8_t> o;
-  for (int bin = 0; bin < c->nbins; bin++)
-    serialize_integration(c, vis + (size_t)bin * nbl * c->Kout, pulsar ? bin : 0, nfl, o);
+  for (int bin = 0; bin < nout; bin++)
+    serialize_integration(c, vis + (size_t)bin * nbl * c->Kout, pulsar ? bin : c->pc_file[bin], nfl, o);
   if (sink && sink(user, 0, o.data(), o.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
   for (int i = 0; i < N; i++) {
     std::vector<uint8_t> t;

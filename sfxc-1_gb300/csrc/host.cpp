@@ -109,7 +109,7 @@ static void akima_coefficients(const double *x, const double *y, int n, double *
   }
 }
 
-Spline Spline::create(const DelayTable &t, ticks_t start_, ticks_t duration) {
+Spline Spline::create(const DelayTable &t, ticks_t start_, ticks_t duration, int pc) {
   int mjd_start = (int)std::floor(time_mjd(start_));
   double seconds_start = std::floor(time_usec_of_day(start_) / 1000000);
   ticks_t stop = start_ + duration;
@@ -120,7 +120,9 @@ Spline Spline::create(const DelayTable &t, ticks_t start_, ticks_t duration) {
   size_t sn = 0;
   while (sn < t.scans.size() && stop > t.scans[sn].end) sn++;
   if (sn == t.scans.size()) throw Error(-3, "time is not covered by the delay table");
-  const Scan &s = t.scans[sn];
+  if (sn + pc >= t.scans.size() || t.scans[sn + pc].begin != t.scans[sn].begin)
+    throw Error(-3, "the delay table has fewer phase centres than requested");
+  const Scan &s = t.scans[sn + pc];
   if (time_diff(s.end, s.begin) < 4.) throw Error(-3, "delay table scan shorter than 4 s");
   const ticks_t onesec = time_from_usec(1000000.);
   ticks_t ib = start - time_mul(onesec, 2);

@@ -64,7 +64,9 @@ struct Spline {
   std::vector<double> x, y[3], b[3], c[3], d[3];
   ticks_t scan_begin = 0, interval_begin = 0, interval_end = 0, clock_epoch = 0;
   double clock_offset = 0, clock_rate = 0;
-  static Spline create(const DelayTable &t, ticks_t start, ticks_t duration);
+  // pc: phase centre, the pc-th scan starting with the covering one (an
+  // additional phase centre is a scan with the same start, 313-336, 478-494)
+  static Spline create(const DelayTable &t, ticks_t start, ticks_t duration, int pc = 0);
   int index(double x) const;
   double eval(int col, double x) const;
   double deriv(int col, double x) const;

@@ -934,6 +934,36 @@ __global__ void normalize_kernel(const float2 *__restrict__ acc, int kpad, int M
 }
 
 // ------------------------------------------------------------------------
+// Extra phase centres: Correlation_core::sub_integration (sfxc/src/
+// correlation_core.cc:516-559) with uvshift (561-593).  Every channel of
+// every baseline of the sub-integration goes to each centre's accumulator;
+// a cross baseline of centre c >= 1 first gets the amplitude and the phase
+// phi + k delta of its residual delay (FP64 angle, FP32 product, as the
+// reference's FP64 recurrence and complex<float> arithmetic).
+__global__ void pc_dump_kernel(float2 *__restrict__ acc, float2 *__restrict__ pcacc, const double4 *__restrict__ uvp,
+                               int nstreams, int nbl, int kpad, int K, int npc) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+  if (k >= K) return;
+  const size_t i = (size_t)b * kpad + k, cstride = (size_t)nbl * kpad;
+  const float2 x = acc[i];
+  pcacc[i] = make_float2(pcacc[i].x + x.x, pcacc[i].y + x.y);
+  for (int c = 1; c < npc; c++) {
+    float2 &p = pcacc[c * cstride + i];
+    if (b < nstreams) {
+      p = make_float2(p.x + x.x, p.y + x.y);
+    } else {
+      const double4 u = uvp[(size_t)(c - 1) * nbl + b];
+      double sn, cs;
+      sincos(fma((double)k, u.y, u.x), &sn, &cs);
+      const float amp = (float)u.z, cf = (float)cs, sf = (float)sn;
+      const float xr = amp * x.x, xi = amp * x.y;
+      p = make_float2(p.x + (xr * cf - xi * sf), p.y + (xr * sf + xi * cf));
+    }
+  }
+  acc[i] = make_float2(0.f, 0.f);
+}
+
+// ------------------------------------------------------------------------
 // Spectral reduction (number_channels < fft_size_correlation):
 // Correlation_core::integration_write, sfxc/src/correlation_core.cc:413-439.
 // One CTA per normalised spectrum X[0..M]: optional normalisation to unit
@@ -1107,6 +1137,11 @@ void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int n
 
 void launch_bitstat(const StreamDev *d_streams, const int4 *d_items, int nitems, cudaStream_t st) {
   if (nitems > 0) bitstat_kernel<<<nitems, 256, 0, st>>>(d_streams, d_items, nitems);
+}
+
+void launch_pc_dump(float2 *acc, float2 *pcacc, const double4 *uvp, int nstreams, int nbl, int kpad, int K, int npc,
+                    cudaStream_t st) {
+  if (nbl > 0) pc_dump_kernel<<<dim3((K + 255) / 256, nbl), 256, 0, st>>>(acc, pcacc, uvp, nstreams, nbl, kpad, K, npc);
 }
 
 cudaError_t launch_reduce(const float2 *in, int nspec, int M, int nch, const float *mask, const float *lag_window,

@@ -30,6 +30,12 @@ cudaError_t launch_xcorr_tc(const void *spec, int nrows, int kpad, int K, const 
                             float inv_scale2, float2 *acc, int *err, cudaStream_t st);
 void launch_normalize(const float2 *acc, int kpad, int M, int nstreams, int nbl, const int *bl, double *norms,
                       const double *flagfac, float2 *out, cudaStream_t st);
+// Sub-integration dump with extra phase centres: acc[b][k] (b < nbl, k < K,
+// rows kpad apart) added to every centre's accumulator pcacc[c][b][k], rotated
+// for c >= 1 on cross baselines (b >= nstreams) by uvp[(c - 1) nbl + b] =
+// {phase, phase step per channel, amplitude}, then cleared.
+void launch_pc_dump(float2 *acc, float2 *pcacc, const double4 *uvp, int nstreams, int nbl, int kpad, int K, int npc,
+                    cudaStream_t st);
 // Spectral reduction of nspec normalised spectra of M + 1 channels to nch + 1
 // channels (M, nch powers of two, nch < M); mask: M + 1 values, lag_window:
 // 2 nch values, tw2M: exp(-2 pi i k / 2M) for k < 2M.

@@ -111,6 +111,11 @@ class CorrelatorNode:
                 setattr(p, key, arr.ctypes.data_as(C.POINTER(C.c_float)))
                 keep.append(arr)
         p.mask_normalize = int(bool(job.get("mask_normalize", 0)))
+        p.n_phase_centers = int(job.get("n_phase_centers", 1))
+        if job.get("pc_file_index") is not None:
+            fi = (C.c_int32 * len(job["pc_file_index"]))(*[int(x) for x in job["pc_file_index"]])
+            p.phase_center_file_index = fi
+            keep.append(fi)
         keep += [tables, streams]
         self._check(self._lib.sfxc_gpu_set_parameters(self._h, C.byref(p)))
         self._keep = keep

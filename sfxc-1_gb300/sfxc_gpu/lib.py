@@ -57,7 +57,8 @@ class CorrelationParams(C.Structure):
                 ("pulsar_nbins", C.c_int32), ("gate_start", C.c_double), ("gate_stop", C.c_double),
                 ("n_polyco", C.c_int32), ("polyco", C.POINTER(Polyco)),
                 ("mask", C.POINTER(C.c_float)), ("lag_window", C.POINTER(C.c_float)),
-                ("mask_normalize", C.c_int32)]
+                ("mask_normalize", C.c_int32), ("n_phase_centers", C.c_int32),
+                ("phase_center_file_index", C.POINTER(C.c_int32))]
 
 
 class ChannelBlock(C.Structure):
