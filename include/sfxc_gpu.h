@@ -142,6 +142,12 @@ typedef struct {
    * binning (Correlator_node::set_parameters, sfxc/src/correlator_node.cc:348-366). */
   int32_t n_phase_centers;
   const int32_t *phase_center_file_index;
+  /* phased-array core (Correlation_core_phased, sfxc/src/correlation_core_phased.cc;
+   * Correlator_node::Correlator_node, sfxc/src/correlator_node.cc:37-38):
+   * non-zero sums every station's spectra per sub-integration and writes one
+   * spectrum per sub-integration instead of the baselines; no tsys records.
+   * Not with pulsar binning, extra phase centres or spectral reduction. */
+  int32_t phased_array;
 } sfxc_correlation_params;
 
 sfxc_gpu_ctx *sfxc_gpu_create(const sfxc_gpu_config *config);

@@ -34,6 +34,7 @@ REF_SOURCES = [
     "src/delay_correction.cc",
     "src/correlation_core.cc",
     "src/correlation_core_pulsar.cc",
+    "src/correlation_core_phased.cc",
     "src/delay_table_akima.cc",
     "src/correlator_time.cc",
     "src/sfxc_fft_float.cc",

@@ -184,6 +184,8 @@ def correlate(job, dump=False, impl="reference", precision=32):
                 lines.append((key, p))
         if job.get("mask_normalize"):
             lines.append(("mask_normalize", 1))
+        if job.get("phased_array"):
+            lines.append(("phased_array", 1))
         if int(job.get("n_phase_centers", 1)) > 1:
             lines.append(("n_phase_centers", int(job["n_phase_centers"])))
             if job.get("pc_file_index") is not None:

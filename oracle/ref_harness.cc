@@ -27,6 +27,7 @@
 #include "channel_extractor_5.h"
 #include "control_parameters.h"
 #include "correlation_core.h"
+#include "correlation_core_phased.h"
 #include "correlation_core_pulsar.h"
 #include "correlator_node_types.h"
 #include "data_writer.h"
@@ -446,7 +447,10 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
   int max_stream = 0;
   for (int i = 0; i < nstreams; i++) max_stream = std::max(max_stream, (int)p.station_streams[i].station_stream);
   std::vector<Stream_chain> chains(max_stream + 1);
-  boost::shared_ptr<Correlation_core> core_normal(new Correlation_core());
+  // Correlator_node::Correlator_node (sfxc/src/correlator_node.cc:37-38): the phased-array core
+  boost::shared_ptr<Correlation_core> core_normal(has(kv, "phased_array") && geti(kv, "phased_array") != 0
+                                                      ? (Correlation_core *)new Correlation_core_phased()
+                                                      : new Correlation_core());
   boost::shared_ptr<Correlation_core_pulsar> core_pulsar(new Correlation_core_pulsar());
   Correlation_core *core = p.pulsar_binning ? (Correlation_core *)core_pulsar.get() : core_normal.get();
   boost::shared_ptr<Memory_writer> out(new Memory_writer());

@@ -672,6 +672,7 @@ typedef struct {
      file index of each (the manager's source list; 0 when absent) */
   int n_pc;
   int *pc_file;
+  int phased; /* Correlation_core_phased (the phased-array core) */
 } job_t;
 
 /* ------------------------------------------------------------- statistics ---
@@ -1758,6 +1759,8 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
   j.dump = de && atoi(de->v[0]);
   if (j.number_channels < 2 || j.number_channels > j.M || (j.number_channels & (j.number_channels - 1)))
     die("number_channels must be a power of two no larger than the FFT size");
+  kv_t *ph = kv_get(k, "phased_array", 0);
+  j.phased = ph && atoi(ph->v[0]);
   kv_t *npc = kv_get(k, "n_phase_centers", 0);
   j.n_pc = npc ? atoi(npc->v[0]) : 1;
   if (j.n_pc < 1) die("n_phase_centers must be at least 1");
@@ -1915,7 +1918,26 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
     }
     int64_t(*nfl)[2] = xmalloc((size_t)nbl * sizeof(*nfl));
     find_invalid(&j, bl, nbl, w, nfl);
-    if (!j.pulsar) {
+    if (j.phased) {
+      /* Correlation_core_phased (sfxc/src/correlation_core_phased.cc): every
+         FFT's spectra of all streams, in stream order, summed into the
+         buffer of its sub-integration (current_fft / nsub); one "baseline"
+         per buffer, headers from stream 0; no normalisation, no tsys */
+      if (j.pulsar || j.n_pc > 1 || j.number_channels != M) die("phased array with pulsar / phase centres / reduction");
+      const int nsubs = nffts / nsub + 1;
+      double *acc = xmalloc((size_t)nsubs * K * 2 * sizeof(double));
+      for (int r = 0; r < nffts; r++) {
+        double *a = acc + (size_t)(r / nsub) * K * 2;
+        for (int i = 0; i < j.nstreams; i++) {
+          const double *x = rows[i] + (size_t)r * stride * 2;
+          for (int k = 0; k < 2 * K; k++) a[k] = st(a[k] + x[k]);
+        }
+      }
+      bl_t *pb = xmalloc((size_t)nsubs * sizeof(bl_t)); /* (0, 0) pairs */
+      write_integration(&j, pb, nsubs, acc, w, nfl, nffts, it, 0, &cor, &cor64);
+      free(pb);
+      free(acc);
+    } else if (!j.pulsar) {
       double *acc = xmalloc((size_t)nbl * K * 2 * sizeof(double));
       double *pc = xmalloc((size_t)j.n_pc * nbl * K * 2 * sizeof(double)); /* phase_centers[c][b][k] */
       const size_t PCS = (size_t)nbl * K * 2;
@@ -2051,7 +2073,7 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
       free(bins);
       free(offsets);
     }
-    tsys_write(&j, start, w, &tsys);
+    if (!j.phased) tsys_write(&j, start, w, &tsys);
     for (int i = 0; i < j.nstreams; i++) {
       int lv[5], ts[4];
       stats_levels(&w[i].stats, lv);

@@ -156,6 +156,7 @@ struct sfxc_gpu_ctx {
   // parameters [chunk][centre - 1][baseline]
   int npc = 1;
   std::vector<int32_t> pc_file;
+  int phased = 0;  // phased-array core
   std::vector<float> pc_weights;
   DevBuf pcacc, uvp;
   // device
@@ -361,6 +362,10 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
   c->pc_file.assign(c->npc, 0);
   if (p->phase_center_file_index) c->pc_file.assign(p->phase_center_file_index, p->phase_center_file_index + c->npc);
   c->p.phase_center_file_index = nullptr;
+  c->phased = p->phased_array != 0;
+  if (c->phased && (c->nbins > 1 || c->npc > 1 || p->number_channels != p->fft_size_correlation))
+    throw Error(SFXC_GPU_EINVAL,
+                "the phased-array core takes no pulsar binning, extra phase centres or spectral reduction");
   c->M = p->fft_size_correlation;
   c->K = c->M + 1;
   c->nch = p->number_channels;
@@ -484,10 +489,12 @@ std::vector<std::pair<int, int>> subint_ranges(const sfxc_gpu_ctx *c) {
   return r;
 }
 
-void serialize_integration(sfxc_gpu_ctx *c, const float2 *vis, int32_t source_nr,
+// bls: the baselines written (the job's, or the phased core's one (0, 0)
+// entry per sub-integration, Correlation_core_phased::create_baselines).
+void serialize_integration(sfxc_gpu_ctx *c, const std::vector<Baseline> &bls, const float2 *vis, int32_t source_nr,
                            const std::vector<std::pair<int64_t, int64_t>> &nfl, std::vector<uint8_t> &o) {
   const int N = (int)c->streams.size();
-  const int nbl = (int)c->bl.size();
+  const int nbl = (int)bls.size();
   put(o, source_nr);
   std::vector<int> stations;
   std::set<int> seen;
@@ -523,13 +530,13 @@ void serialize_integration(sfxc_gpu_ctx *c, const float2 *vis, int32_t source_nr
   const size_t K = (size_t)c->Kout;  // output channels + 1
   for (int b = 0; b < nbl; b++) {
     int lv[5];
-    c->sc[c->bl[b].a].stats.levels(lv);
-    int64_t w = c->bl[b].a == c->bl[b].b ? total - lv[4] : total - lv[4] - nfl[b].first;
+    c->sc[bls[b].a].stats.levels(lv);
+    int64_t w = bls[b].a == bls[b].b ? total - lv[4] : total - lv[4] - nfl[b].first;
     put(o, (int32_t)std::max<int64_t>(w, 0));
-    o.push_back((uint8_t)c->streams[c->bl[b].a].station_number);
-    o.push_back((uint8_t)c->streams[c->bl[b].b].station_number);
-    o.push_back((uint8_t)((c->streams[c->bl[b].a].polarisation == 'R' ? 0 : 1) |
-                          ((c->streams[c->bl[b].b].polarisation == 'R' ? 0 : 1) << 1) |
+    o.push_back((uint8_t)c->streams[bls[b].a].station_number);
+    o.push_back((uint8_t)c->streams[bls[b].b].station_number);
+    o.push_back((uint8_t)((c->streams[bls[b].a].polarisation == 'R' ? 0 : 1) |
+                          ((c->streams[bls[b].b].polarisation == 'R' ? 0 : 1) << 1) |
                           ((c->p.sideband == 'U' ? 1 : 0) << 2) | ((c->p.frequency_nr & 31) << 3)));
     o.push_back((uint8_t)' ');
     const uint8_t *d = reinterpret_cast<const uint8_t *>(vis + (size_t)b * K);
@@ -681,7 +688,9 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   upload(c->flagfac, flagfac.data(), flagfac.size() * 8, st);
   upload(c->items, items.data(), items.size() * sizeof(int4), st);
   // ---- device work
-  const size_t accn = (size_t)c->nbins * nbl * kpad;
+  // phased array: one buffer per sub-integration (Correlation_core_phased::create_baselines)
+  const int nphs = c->phased ? c->nffts / c->nsub + 1 : 0;
+  const size_t accn = (size_t)std::max(c->nbins * nbl, nphs) * kpad;
   c->acc.ensure(accn * sizeof(float2));
   CK(cudaMemsetAsync(c->acc.p, 0, accn * sizeof(float2), st));
   const bool pulsar = c->nbins > 1;
@@ -712,7 +721,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   // tensor-core X-step for normal correlation of up to 32 inputs; the spectra
   // are scaled by a power of two before the FP16 hi/lo split so that typical
   // magnitudes sit near 1 (|X| ~ sqrt(2M * 0.375 * E[x^2]) for a Hann window)
-  const bool tc_x = c->x_mode == SFXC_GPU_X_TC_HILO && !pulsar;
+  const bool tc_x = c->x_mode == SFXC_GPU_X_TC_HILO && !pulsar && !c->phased;
   const float tc_scale = std::ldexp(1.0f, -(int)std::lround(0.5 * std::log2(2.0 * M * 10.0)));
   // FP32 spectra: [stream][row][kpad]; TC spectra: [row][kpad][32 stream slots], 8 bytes each
   // the tensor-core layout reads rows in groups of 8 (rows past a chunk's end cleared before its X-step)
@@ -859,7 +868,10 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       CK(cudaGetLastError());
     }
     CK(cudaEventRecord(c->evpool[ev + 2], st));
-    if (tc_x) {
+    if (c->phased) {
+      launch_phased(c->spec.as<float2>(), max_rows, kpad, N, ranges[ch].first, nrows, K, c->nsub, c->acc.as<float2>(),
+                    st);
+    } else if (tc_x) {
       if (nrows % 8)
         CK(cudaMemsetAsync(static_cast<char *>(c->spec.p) + (size_t)nrows * kpad * kTcSlots * sizeof(float2), 0,
                            (size_t)(8 - nrows % 8) * kpad * kTcSlots * sizeof(float2), st));
@@ -893,14 +905,20 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   // ---- normalisation and statistics
   CK(cudaEventRecord(c->evpool[ev], st));
   c->norms.ensure((size_t)N * 8);
-  // outputs: the pulsar bins, or the phase centres (each normalised on its own)
+  // outputs: the pulsar bins, or the phase centres (each normalised on its
+  // own); the phased array writes its sub-integration sums as they are
   const int nout = pulsar ? c->nbins : c->npc;
   const float2 *accs = c->npc > 1 ? c->pcacc.as<float2>() : c->acc.as<float2>();
-  c->out.ensure((size_t)nout * nbl * K * sizeof(float2));
-  for (int bin = 0; bin < nout; bin++)
-    launch_normalize(accs + (size_t)bin * nbl * kpad, kpad, M, N, nbl, c->blpairs.as<int>(), c->norms.as<double>(),
-                     c->flagfac.as<double>(), c->out.as<float2>() + (size_t)bin * nbl * K, st);
-  CK(cudaGetLastError());
+  c->out.ensure((size_t)std::max(nout * nbl, nphs) * K * sizeof(float2));
+  if (c->phased) {
+    CK(cudaMemcpy2DAsync(c->out.p, K * sizeof(float2), c->acc.p, kpad * sizeof(float2), K * sizeof(float2), nphs,
+                         cudaMemcpyDeviceToDevice, st));
+  } else {
+    for (int bin = 0; bin < nout; bin++)
+      launch_normalize(accs + (size_t)bin * nbl * kpad, kpad, M, N, nbl, c->blpairs.as<int>(), c->norms.as<double>(),
+                       c->flagfac.as<double>(), c->out.as<float2>() + (size_t)bin * nbl * K, st);
+    CK(cudaGetLastError());
+  }
   const float2 *vsrc = c->out.as<float2>();
   if (c->nch < M) {
     c->rout.ensure((size_t)nout * nbl * c->Kout * sizeof(float2));
@@ -909,7 +927,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     vsrc = c->rout.as<float2>();
     launches += 1;
   }
-  const size_t nvis = (size_t)nout * nbl * c->Kout;
+  const size_t nvis = c->phased ? (size_t)nphs * c->Kout : (size_t)nout * nbl * c->Kout;
   uint8_t *res = static_cast<uint8_t *>(c->results.ensure(nvis * sizeof(float2) + (size_t)N * 64 + 16));
   const float2 *vis = reinterpret_cast<const float2 *>(res);
   const unsigned long long *hist = reinterpret_cast<const unsigned long long *>(res + nvis * sizeof(float2));
@@ -953,10 +971,14 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   }
   // ---- output bytes (integration_write per bin) and tsys records
   std::vector<uint8_t> o;
-  for (int bin = 0; bin < nout; bin++)
-    serialize_integration(c, vis + (size_t)bin * nbl * c->Kout, pulsar ? bin : c->pc_file[bin], nfl, o);
+  if (c->phased) {
+    serialize_integration(c, std::vector<Baseline>(nphs, Baseline{0, 0}), vis, 0, nfl, o);
+  } else {
+    for (int bin = 0; bin < nout; bin++)
+      serialize_integration(c, c->bl, vis + (size_t)bin * nbl * c->Kout, pulsar ? bin : c->pc_file[bin], nfl, o);
+  }
   if (sink && sink(user, 0, o.data(), o.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
-  for (int i = 0; i < N; i++) {
+  for (int i = 0; i < N && !c->phased; i++) {  // the phased core writes no tsys records
     std::vector<uint8_t> t;
     t.push_back((uint8_t)c->streams[i].station_number);
     t.push_back((uint8_t)c->p.frequency_nr);

@@ -934,6 +934,32 @@ __global__ void normalize_kernel(const float2 *__restrict__ acc, int kpad, int M
 }
 
 // ------------------------------------------------------------------------
+// Phased array: Correlation_core_phased::integration_step (sfxc/src/
+// correlation_core_phased.cc:113-126) -- each FFT's spectra of all streams
+// added, in stream order, to the buffer of its sub-integration; one thread
+// per channel keeps the running sum of the current buffer in registers.
+__global__ void phased_kernel(const float2 *__restrict__ spec, int nrows_total, int kpad, int nstreams, int r0,
+                              int nrows, int K, int nsub, float2 *__restrict__ acc) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K || nrows <= 0) return;
+  int s = r0 / nsub;
+  float2 sum = acc[(size_t)s * kpad + k];
+  for (int r = 0; r < nrows; r++) {
+    const int sr = (r0 + r) / nsub;
+    if (sr != s) {
+      acc[(size_t)s * kpad + k] = sum;
+      s = sr;
+      sum = acc[(size_t)s * kpad + k];
+    }
+    for (int i = 0; i < nstreams; i++) {
+      const float2 x = spec[((size_t)i * nrows_total + r) * kpad + k];
+      sum = make_float2(sum.x + x.x, sum.y + x.y);
+    }
+  }
+  acc[(size_t)s * kpad + k] = sum;
+}
+
+// ------------------------------------------------------------------------
 // Extra phase centres: Correlation_core::sub_integration (sfxc/src/
 // correlation_core.cc:516-559) with uvshift (561-593).  Every channel of
 // every baseline of the sub-integration goes to each centre's accumulator;
@@ -1137,6 +1163,11 @@ void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int n
 
 void launch_bitstat(const StreamDev *d_streams, const int4 *d_items, int nitems, cudaStream_t st) {
   if (nitems > 0) bitstat_kernel<<<nitems, 256, 0, st>>>(d_streams, d_items, nitems);
+}
+
+void launch_phased(const float2 *spec, int nrows_total, int kpad, int nstreams, int r0, int nrows, int K, int nsub,
+                   float2 *acc, cudaStream_t st) {
+  phased_kernel<<<(K + 127) / 128, 128, 0, st>>>(spec, nrows_total, kpad, nstreams, r0, nrows, K, nsub, acc);
 }
 
 void launch_pc_dump(float2 *acc, float2 *pcacc, const double4 *uvp, int nstreams, int nbl, int kpad, int K, int npc,

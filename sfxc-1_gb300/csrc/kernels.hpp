@@ -36,6 +36,11 @@ void launch_normalize(const float2 *acc, int kpad, int M, int nstreams, int nbl,
 // {phase, phase step per channel, amplitude}, then cleared.
 void launch_pc_dump(float2 *acc, float2 *pcacc, const double4 *uvp, int nstreams, int nbl, int kpad, int K, int npc,
                     cudaStream_t st);
+// Phased array: acc[(r0 + r) / nsub][k] += spec[i][r][k] over the chunk's rows
+// r < nrows and streams i < nstreams, in that order (FP32 spectra layout,
+// nrows_total rows per stream slot, kpad apart).
+void launch_phased(const float2 *spec, int nrows_total, int kpad, int nstreams, int r0, int nrows, int K, int nsub,
+                   float2 *acc, cudaStream_t st);
 // Spectral reduction of nspec normalised spectra of M + 1 channels to nch + 1
 // channels (M, nch powers of two, nch < M); mask: M + 1 values, lag_window:
 // 2 nch values, tw2M: exp(-2 pi i k / 2M) for k < 2M.

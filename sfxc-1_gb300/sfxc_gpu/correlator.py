@@ -112,6 +112,7 @@ class CorrelatorNode:
                 keep.append(arr)
         p.mask_normalize = int(bool(job.get("mask_normalize", 0)))
         p.n_phase_centers = int(job.get("n_phase_centers", 1))
+        p.phased_array = int(bool(job.get("phased_array", 0)))
         if job.get("pc_file_index") is not None:
             fi = (C.c_int32 * len(job["pc_file_index"]))(*[int(x) for x in job["pc_file_index"]])
             p.phase_center_file_index = fi

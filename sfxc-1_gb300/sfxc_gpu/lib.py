@@ -58,7 +58,7 @@ class CorrelationParams(C.Structure):
                 ("n_polyco", C.c_int32), ("polyco", C.POINTER(Polyco)),
                 ("mask", C.POINTER(C.c_float)), ("lag_window", C.POINTER(C.c_float)),
                 ("mask_normalize", C.c_int32), ("n_phase_centers", C.c_int32),
-                ("phase_center_file_index", C.POINTER(C.c_int32))]
+                ("phase_center_file_index", C.POINTER(C.c_int32)), ("phased_array", C.c_int32)]
 
 
 class ChannelBlock(C.Structure):

@@ -67,6 +67,12 @@ def scenarios():
         stations=st3, sample_rate=32_000_000, bandwidth=16_000_000, bits=2, channel_freq=1_600_000_000,
         nchan=1024, integration_us=8000, sub_integration_us=2000, n_integrations=2, rho=0.05, seed=23,
         block_bytes=8000, extra_centers=[("SRC2", (2.1e-8, -4.0e-8, 7.5e-8)), ("SRC3", (-1.3e-7, 0.6e-7, 0.0))])
+    # phased-array core: 3 stations, sub-integrations of 2 ms (5 sums per 8 ms integration)
+    st4 = scenario.cubic_stations(3, seed=51, max_delay=1e-3, max_rate=1e-5)
+    out["phased"] = scenario.Scenario(
+        stations=st4, sample_rate=32_000_000, bandwidth=16_000_000, bits=2, channel_freq=1_600_000_000,
+        nchan=512, integration_us=8000, sub_integration_us=2000, n_integrations=2, rho=0.05, seed=29,
+        block_bytes=8000)
     return out
 
 
@@ -102,6 +108,8 @@ def make(name, sc):
         job["pulsar"] = (PULSAR["nbins"],) + PULSAR["gate"]
         job["polyco"] = PULSAR["polyco"]
     mask_params(name, job)
+    if name == "phased":
+        job["phased_array"] = 1
     res = jobs.correlate(job, dump=True)
     keys = sc.streams()
     for k, key in enumerate(keys):

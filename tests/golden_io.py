@@ -7,7 +7,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["c1_plain", "multi", "onebit", "pulsar", "reduced", "reduced_mask", "phase_centers"]
+CASES = ["c1_plain", "multi", "onebit", "pulsar", "reduced", "reduced_mask", "phase_centers", "phased"]
 
 
 class Golden:
