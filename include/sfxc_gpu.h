@@ -293,6 +293,43 @@ int sfxc_gpu_extract_block(sfxc_gpu_ctx *ctx, const sfxc_reader_block *block, in
                            int32_t n_subbands, int32_t fan_out, const int32_t *tracks, uint8_t *out,
                            int32_t *out_invalid);
 
+/* Phase-cal extraction of one channel (Input_node_data_writer::do_phasecal,
+ * sfxc/src/input_node_data_writer.cc:230-312, with its parameters from
+ * Input_node_data_writer::set_parameters, 328-346): the channel's samples,
+ * block after block as the input node's writer takes them up, folded into
+ * sample_rate / 10 kHz int32 bins (values -7, -2, 2, 7 for 2-bit codes,
+ * -5, 5 for 1-bit, the samples of a byte LSB first).  A block whose start is
+ * a multiple of integration_ticks ends the running integration (the first
+ * such block starts one; the blocks before it are not counted) and restarts
+ * the fold at bin 0.  Inside a block, an invalid run is skipped (its samples
+ * still advance the bin) when the byte loop reaches its first byte; a run
+ * that begins where the previous skipped run ends, or before it, is not
+ * skipped, and neither are the block's runs after it -- the reference's
+ * loop behaves so and the fold keeps that.  Every finished integration goes
+ * to the sink as kind 2, the packed message of MPI_TAG_OUTPUT_NODE_WRITE_PHASECAL:
+ * uint8 station, frequency number, sideband, polarisation; int64 start ticks;
+ * int64 length in ticks; int32 bin count P; P int32 bins.  The last,
+ * unfinished integration is never sent (the reference's behaviour). */
+typedef struct {
+  int32_t sample_rate;       /* samples/s; P = sample_rate / 10 kHz bins, a multiple of 8 / bits_per_sample */
+  int32_t bits_per_sample;   /* 1 or 2 */
+  int64_t integration_ticks; /* phasecal_integr_time in 512 MHz ticks, > 0 */
+  int32_t station_number, frequency_number;
+  int32_t sideband;          /* 1: upper ('U'), 0: lower, as packed */
+  int32_t polarisation;      /* 1: left ('L'), 0: right, as packed */
+} sfxc_phasecal_params;
+typedef struct sfxc_gpu_phasecal sfxc_gpu_phasecal;
+/* One channel's phase-cal state on ctx's device and stream; NULL on bad
+ * parameters (message from sfxc_gpu_last_error(ctx)). */
+sfxc_gpu_phasecal *sfxc_gpu_phasecal_create(sfxc_gpu_ctx *ctx, const sfxc_phasecal_params *params);
+/* Fold the next n_blocks channel blocks (stored back to back from `stream`,
+ * described as for sfxc_gpu_write_protocol); finished integrations go to
+ * sink(user, 2, message, bytes) in order before the call returns. */
+int sfxc_gpu_phasecal_push(sfxc_gpu_phasecal *pc, const uint8_t *stream, int32_t n_blocks,
+                           const sfxc_channel_block *blocks, sfxc_output_sink sink, void *user);
+/* Frees the state; before or after ctx is destroyed. */
+void sfxc_gpu_phasecal_destroy(sfxc_gpu_phasecal *pc);
+
 #ifdef __cplusplus
 }
 #endif

@@ -69,11 +69,14 @@ def delays(del_bytes, start_ticks, stop_ticks, sample_rate, bits, probes=(), clo
         return dl, pr
 
 
-def protocol(blocks, slices, sample_rate, bits, integr_time_us, station_number=0, impl="reference"):
+def protocol(blocks, slices, sample_rate, bits, integr_time_us, station_number=0, impl="reference",
+             phasecal_ticks=None):
     """Input_node_data_writer protocol bytes for each slice.
 
     blocks: list of (start_ticks, bytes, [(invalid_begin, nr_invalid), ...])
     slices: list of (start_ticks, stop_ticks, nr_samples, delay_list)
+    phasecal_ticks: phase-cal integration time; when given, returns
+    (protocols, phase-cal message bytes) (Input_node_data_writer::do_phasecal)
     """
     with tempfile.TemporaryDirectory() as d:
         blob = os.path.join(d, "blocks.bin")
@@ -98,6 +101,9 @@ def protocol(blocks, slices, sample_rate, bits, integr_time_us, station_number=0
             lines.append(("slice", s0, s1, ns))
             lines.append(("dlist", dpath))
         out = os.path.join(d, "proto.bin")
+        pc_out = os.path.join(d, "pcal.bin")
+        if phasecal_ticks is not None:
+            lines += [("phasecal_ticks", phasecal_ticks), ("phasecal_out", pc_out)]
         _run("protocol", lines, out, d, impl)
         raw = open(out, "rb").read()
         res, p = [], 0
@@ -105,6 +111,8 @@ def protocol(blocks, slices, sample_rate, bits, integr_time_us, station_number=0
             n = int(np.frombuffer(raw[p:p + 8], dtype=np.uint64)[0])
             res.append(raw[p + 8:p + 8 + n])
             p += 8 + n
+        if phasecal_ticks is not None:
+            return res, open(pc_out, "rb").read()
         return res
 
 

@@ -220,6 +220,9 @@ static int mode_protocol(const Kv &kv, const char *outfile) {
   param.track_bit_rate = sample_rate;  // sample_rate() = track_bit_rate * subsamples_per_sample
   param.n_tracks = bps;
   param.frame_size = -1;
+  // phase-cal extraction (Input_node_data_writer::do_phasecal): its messages
+  // (MPI_TAG_OUTPUT_NODE_WRITE_PHASECAL) are written after the slices
+  param.phasecal_integr_time = ticks_time(has(kv, "phasecal_ticks") ? getll(kv, "phasecal_ticks") : 0);
   if (param.sample_rate() != sample_rate || param.bits_per_sample() != bps)
     die("Input_node_parameters accessors disagree with the job");
 
@@ -291,6 +294,13 @@ static int mode_protocol(const Kv &kv, const char *outfile) {
     if (n) std::fwrite(&writers[s]->bytes[0], 1, n, f);
   }
   std::fclose(f);
+  if (has(kv, "phasecal_out")) {
+    FILE *pf = std::fopen(get(kv, "phasecal_out")[0].c_str(), "wb");
+    for (size_t m = 0; m < g_shim_messages.size(); m++)
+      std::fwrite(&g_shim_messages[m].bytes[0], 1, g_shim_messages[m].bytes.size(), pf);
+    std::fclose(pf);
+    g_shim_messages.clear();
+  }
   return 0;
 }
 

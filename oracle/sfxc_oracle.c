@@ -408,9 +408,67 @@ static void pw_data(bytes_t *o, const unsigned char *blk, int n, int off) {
   }
 }
 
-/* Returns per-slice protocol buffers. */
+/* ---------------------------------------------------------- phase cal ---
+ * Input_node_data_writer::do_phasecal (sfxc/src/input_node_data_writer.cc:
+ * 230-312): the samples of every block the writer takes up, folded modulo
+ * sample_rate / 10 kHz into int32 bins; a block starting on a multiple of the
+ * phase-cal integration time sends the bins so far (after the first such
+ * block) and starts again.  The per-byte loop checks one invalid run per
+ * byte, as written. */
+typedef struct {
+  int64_t T; /* integration ticks, 0: off */
+  int sr, bps, P;
+  int32_t *acc;
+  int64_t count;
+  ticks_t time;
+  unsigned char station, freq, sb, pol;
+  bytes_t out;
+  int done; /* blocks processed (input_element.processed) */
+} pcal_t;
+static void pcal_block(pcal_t *pc, const cblock_t *b, int index) {
+  static const int8_t v2[] = {-7, -2, 2, 7}, v1[] = {-5, 5};
+  if (!pc || pc->T == 0 || index < pc->done) return;
+  pc->done = index + 1;
+  const int spb = 8 / pc->bps;
+  if (b->start % pc->T == 0) {
+    if (pc->P == 0) {
+      pc->P = (int)(pc->sr / 10e3);
+      pc->acc = xmalloc(pc->P * sizeof(int32_t));
+    } else {
+      int64_t t0 = pc->time, dt = b->start - pc->time;
+      int32_t ns = pc->P;
+      bpush(&pc->out, &pc->station, 1);
+      bpush(&pc->out, &pc->freq, 1);
+      bpush(&pc->out, &pc->sb, 1);
+      bpush(&pc->out, &pc->pol, 1);
+      bpush(&pc->out, &t0, 8);
+      bpush(&pc->out, &dt, 8);
+      bpush(&pc->out, &ns, 4);
+      bpush(&pc->out, pc->acc, (size_t)pc->P * 4);
+      memset(pc->acc, 0, pc->P * sizeof(int32_t));
+    }
+    pc->count = 0;
+    pc->time = b->start;
+    if (pc->P % spb) die("phase-cal bins not a whole number of bytes");
+  }
+  if (pc->P == 0) return;
+  int iv = 0;
+  for (int i = 0; i < b->size; i++) {
+    if (iv < b->ninv && i == b->inv[iv].begin) {
+      i += b->inv[iv].n;
+      pc->count += (int64_t)b->inv[iv].n * spb;
+      iv++;
+      if (i >= b->size) break;
+    }
+    pc->count %= pc->P;
+    for (int q = 0; q < spb; q++)
+      pc->acc[pc->count++] += pc->bps == 2 ? v2[(b->data[i] >> (2 * q)) & 3] : v1[(b->data[i] >> q) & 1];
+  }
+}
+
+/* Returns per-slice protocol buffers (and feeds pc, if given, as do_task does). */
 static void protocol_write(const cblock_t *blocks, int nblocks, pslice_t *slices, int nslices, int sr,
-                           int bps, double integr_time_us, bytes_t *outs) {
+                           int bps, double integr_time_us, bytes_t *outs, pcal_t *pcal) {
   const int tps = t_sample_rate(sr);
   const ticks_t byte_length = t_from_usec(8 * 1000000. / ((double)sr * bps));
   const ticks_t integration_time = t_from_usec(integr_time_us);
@@ -439,6 +497,7 @@ static void protocol_write(const cblock_t *blocks, int nblocks, pslice_t *slices
     if (bi >= nblocks) break;
     /* do_task */
     const cblock_t *blk = &blocks[bi];
+    pcal_block(pcal, blk, bi);
     bytes_t *o = &outs[writer];
     int64_t byte_offset = 0;
     int delay_size = cur->n;
@@ -1680,7 +1739,16 @@ static int mode_protocol(const kvs_t *k, const char *outp) {
     fclose(f);
   }
   bytes_t *outs = xmalloc(ns * sizeof(bytes_t));
-  protocol_write(blocks, nb, sl, ns, sr, bps, integr, outs);
+  pcal_t pc;
+  memset(&pc, 0, sizeof(pc));
+  kv_t *pt = kv_get(k, "phasecal_ticks", 0);
+  pc.T = pt ? atoll(pt->v[0]) : 0;
+  pc.sr = sr, pc.bps = bps;
+  pc.station = (unsigned char)kv_ll(k, "station_number");
+  pc.sb = 1; /* the job's channel: USB, RCP, frequency 0 */
+  protocol_write(blocks, nb, sl, ns, sr, bps, integr, outs, &pc);
+  kv_t *po = kv_get(k, "phasecal_out", 0);
+  if (po) write_all(po->v[0], pc.out.p, pc.out.n);
   FILE *f = fopen(outp, "wb");
   for (int s = 0; s < ns; s++) {
     uint64_t m = outs[s].n;

@@ -1292,6 +1292,159 @@ int sfxc_gpu_extract_block(sfxc_gpu_ctx *c, const sfxc_reader_block *block, int3
   return SFXC_GPU_OK;
 }
 
+struct sfxc_gpu_phasecal {
+  sfxc_gpu_ctx *ctx = nullptr;
+  int device = 0;
+  sfxc_phasecal_params p{};
+  int P = 0, spb = 4;
+  // fold state (do_phasecal's phasecal, phasecal_count, phasecal_time):
+  // started once the first integration start was seen; row 0 of acc holds
+  // the running integration between calls once live
+  bool started = false, live = false;
+  int64_t count = 0, time = 0;
+  DevBuf data, runs, acc;
+  HostBuf staging;
+};
+
+sfxc_gpu_phasecal *sfxc_gpu_phasecal_create(sfxc_gpu_ctx *c, const sfxc_phasecal_params *p) {
+  if (!c) return nullptr;
+  try {
+    if (!p) throw Error(SFXC_GPU_EINVAL, "null parameters");
+    if (p->bits_per_sample != 1 && p->bits_per_sample != 2) throw Error(SFXC_GPU_EINVAL, "bits_per_sample must be 1 or 2");
+    if (p->integration_ticks <= 0) throw Error(SFXC_GPU_EINVAL, "phase-cal integration time must be positive");
+    // phasecal.resize((size_t)(sample_rate / 10e3)), SFXC_ASSERT(size % samples_per_byte == 0)
+    const int P = (int)(p->sample_rate / 10e3);
+    const int spb = 8 / p->bits_per_sample;
+    if (p->sample_rate <= 0 || P <= 0 || P % spb) throw Error(SFXC_GPU_EINVAL, "sample_rate / 10 kHz bins must be a positive multiple of 8 / bits_per_sample");
+    auto *pc = new sfxc_gpu_phasecal();
+    pc->ctx = c;
+    pc->device = c->device;
+    pc->p = *p;
+    pc->P = P;
+    pc->spb = spb;
+    return pc;
+  } catch (const Error &e) {
+    fail(c, e);
+    return nullptr;
+  }
+}
+
+void sfxc_gpu_phasecal_destroy(sfxc_gpu_phasecal *pc) {
+  if (!pc) return;
+  cudaSetDevice(pc->device);  // its buffers are freed there (cudaFree waits for the device)
+  delete pc;
+}
+
+int sfxc_gpu_phasecal_push(sfxc_gpu_phasecal *pc, const uint8_t *stream, int32_t n_blocks,
+                           const sfxc_channel_block *blocks, sfxc_output_sink sink, void *user) {
+  if (!pc) return SFXC_GPU_EINVAL;
+  sfxc_gpu_ctx *c = pc->ctx;
+  try {
+    if (n_blocks < 0 || (n_blocks && (!blocks || !stream))) throw Error(SFXC_GPU_EINVAL, "bad block list");
+    for (int b = 0; b < n_blocks; b++) {
+      const sfxc_channel_block &k = blocks[b];
+      if (k.size < 0 || k.n_invalid < 0 || (k.n_invalid && !k.invalid)) throw Error(SFXC_GPU_EINVAL, "bad channel block");
+      for (int v = 0; v < 2 * k.n_invalid; v++)
+        if (k.invalid[v] < 0) throw Error(SFXC_GPU_EINVAL, "negative invalid run");
+    }
+    const int P = pc->P, spb = pc->spb, pb = P / spb;
+    const int64_t T = pc->p.integration_ticks;
+    // Host pass over the blocks in order: the integrations they start and end,
+    // and each counted stretch of bytes with the bin of its first byte.  Long
+    // stretches are cut every 64 periods (same first bin) to bound the work of
+    // one thread.
+    const int64_t piece = (int64_t)64 * pb;
+    struct Close { int64_t time, length; };
+    std::vector<Close> closes;
+    std::vector<PcalRun> runs;
+    int row = 0;
+    int64_t off = 0, used_end = 0;
+    auto add_run = [&](int64_t src, int64_t n) {
+      const int bin0 = (int)((pc->count % P) / spb);
+      for (int64_t q = 0; q < n; q += piece)
+        runs.push_back(PcalRun{src + q, (int32_t)std::min(piece, n - q), bin0, row, 0});
+      pc->count = (pc->count + n * spb) % P;
+      used_end = src + n;
+    };
+    for (int b = 0; b < n_blocks; b++) {
+      const sfxc_channel_block &k = blocks[b];
+      if (k.start_ticks % T == 0) {
+        if (pc->started) {
+          closes.push_back(Close{pc->time, k.start_ticks - pc->time});
+          row++;
+        }
+        pc->started = true;
+        pc->count = 0;
+        pc->time = k.start_ticks;
+      }
+      if (pc->started) {
+        // do_phasecal's byte loop as stretches: at byte i an invalid run
+        // beginning there is skipped (its samples advance the bin) and the byte
+        // after it is counted without a check, so the next run is only ever
+        // matched where it begins after that byte
+        const int size = k.size;
+        int64_t i = 0;
+        int iv = 0;
+        while (i < size) {
+          if (iv < k.n_invalid && i == k.invalid[2 * iv]) {
+            const int64_t n = k.invalid[2 * iv + 1];
+            i += n;
+            pc->count = (pc->count + n * spb) % P;
+            iv++;
+            if (i >= size) break;
+          }
+          const int64_t end = (iv < k.n_invalid && k.invalid[2 * iv] > i) ? (int64_t)k.invalid[2 * iv] : (int64_t)size;
+          add_run(off + i, end - i);
+          i = end;
+        }
+      }
+      off += k.size;
+    }
+    const int rows = row + 1;
+    if (!pc->started || (runs.empty() && closes.empty())) return SFXC_GPU_OK;
+    CK(cudaSetDevice(c->device));
+    pc->acc.ensure((size_t)rows * P * 4);
+    // a new integration's row starts from zero; row 0 keeps the running one
+    const int first_clear = pc->live ? 1 : 0;
+    if (rows > first_clear)
+      CK(cudaMemsetAsync(pc->acc.as<int32_t>() + (size_t)first_clear * P, 0, (size_t)(rows - first_clear) * P * 4, c->st));
+    pc->live = true;
+    if (!runs.empty()) {
+      upload(pc->data, stream, (size_t)used_end, c->st);
+      upload(pc->runs, runs.data(), runs.size() * sizeof(PcalRun), c->st);
+      launch_phasecal(pc->data.as<uint8_t>(), pc->runs.as<PcalRun>(), (int)runs.size(), pb, pc->p.bits_per_sample,
+                      pc->acc.as<int32_t>(), c->st);
+      CK(cudaGetLastError());
+    }
+    const size_t nclose = closes.size();
+    int32_t *h = nullptr;
+    if (nclose) {
+      h = (int32_t *)pc->staging.ensure(nclose * P * 4);
+      CK(cudaMemcpyAsync(h, pc->acc.p, nclose * P * 4, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(pc->acc.p, pc->acc.as<int32_t>() + (size_t)row * P, (size_t)P * 4, cudaMemcpyDeviceToDevice,
+                         c->st));
+    }
+    CK(cudaStreamSynchronize(c->st));
+    // MPI_Pack layout of the message (input_node_data_writer.cc:250-265)
+    std::vector<uint8_t> msg(4 + 8 + 8 + 4 + (size_t)P * 4);
+    for (size_t k = 0; k < nclose; k++) {
+      msg[0] = (uint8_t)pc->p.station_number;
+      msg[1] = (uint8_t)pc->p.frequency_number;
+      msg[2] = (uint8_t)pc->p.sideband;
+      msg[3] = (uint8_t)pc->p.polarisation;
+      std::memcpy(&msg[4], &closes[k].time, 8);
+      std::memcpy(&msg[12], &closes[k].length, 8);
+      const int32_t ns = P;
+      std::memcpy(&msg[20], &ns, 4);
+      std::memcpy(&msg[24], h + k * P, (size_t)P * 4);
+      if (sink && sink(user, 2, msg.data(), msg.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
+    }
+    return SFXC_GPU_OK;
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
 int sfxc_gpu_last_timings(const sfxc_gpu_ctx *c, float *ms6) {
   float *ms5 = ms6;
   if (!c || !ms5) return SFXC_GPU_EINVAL;

@@ -1109,6 +1109,52 @@ void launch_extract(const uint8_t *in, int64_t nout, int N, int bits, int nsub, 
   extract_kernel<<<dim3((unsigned)((nout + 255) / 256), nsub), 256, 0, st>>>(in, nout, N, bits, fan_out, tracks, out);
 }
 
+// ------------------------------------------------------------- phase cal ---
+// Phase-cal folding (Input_node_data_writer::do_phasecal,
+// sfxc/src/input_node_data_writer.cc:230-312): byte j of run r, data[off + j],
+// holds the samples of bins ((bin0 + j) mod pb) * spb + q, q < spb = 8 / bits,
+// LSB first, and they go to accumulator row r.row (pb * spb int32 bins).
+// Thread t takes every pb-th byte of the run, those of byte-bin t, so that a
+// warp reads consecutive bytes, and adds its spb sums once: integer sums, so
+// neither the order nor the atomics change the result.
+template <int BITS>
+__global__ void __launch_bounds__(256) phasecal_kernel(const uint8_t *data, const PcalRun *runs, int pb,
+                                                       int32_t *acc) {
+  constexpr int SPB = 8 / BITS;
+  const PcalRun r = runs[blockIdx.y];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= pb) return;
+  int j = t - r.bin0;
+  if (j < 0) j += pb;
+  int sum[SPB] = {};
+  for (; j < r.n; j += pb) {
+    const uint32_t v = __ldg(data + r.off + j);
+#pragma unroll
+    for (int q = 0; q < SPB; q++) {
+      // Bit2float / do_phasecal sample values: 2-bit {-7, -2, 2, 7}, 1-bit {-5, 5}
+      if (BITS == 2)
+        sum[q] += (int)(int8_t)(uint8_t)(0x0702FEF9u >> (8 * ((v >> (2 * q)) & 3)));
+      else
+        sum[q] += ((v >> q) & 1) ? 5 : -5;
+    }
+  }
+  int32_t *a = acc + (int64_t)r.row * pb * SPB + (int64_t)t * SPB;
+#pragma unroll
+  for (int q = 0; q < SPB; q++)
+    if (sum[q]) atomicAdd(a + q, sum[q]);
+}
+
+void launch_phasecal(const uint8_t *data, const PcalRun *runs, int nruns, int pb, int bits, int32_t *acc,
+                     cudaStream_t st) {
+  for (int r0 = 0; r0 < nruns; r0 += 65535) {
+    const dim3 grid((unsigned)((pb + 255) / 256), (unsigned)std::min(65535, nruns - r0));
+    if (bits == 2)
+      phasecal_kernel<2><<<grid, 256, 0, st>>>(data, runs + r0, pb, acc);
+    else
+      phasecal_kernel<1><<<grid, 256, 0, st>>>(data, runs + r0, pb, acc);
+  }
+}
+
 template <int LOGN, int OUT_TC, int SPCMAX>
 static void window_fft_launch_spc(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                                   const float *window, const float2 *tw_rot, int nper, int M, int kpad, void *spec,

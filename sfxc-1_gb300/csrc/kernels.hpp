@@ -46,5 +46,14 @@ void launch_phased(const float2 *spec, int nrows_total, int kpad, int nstreams, 
 // 2 nch values, tw2M: exp(-2 pi i k / 2M) for k < 2M.
 cudaError_t launch_reduce(const float2 *in, int nspec, int M, int nch, const float *mask, const float *lag_window,
                           int normalize, const float2 *tw2M, float2 *out, cudaStream_t st);
+// Phase-cal folding: run k adds the samples of its bytes data[off, off + n)
+// to accumulator row `row` (pb * (8 / bits) int32 bins), byte j to byte-bin
+// (bin0 + j) mod pb.
+struct PcalRun {
+  int64_t off;
+  int32_t n, bin0, row, pad;
+};
+void launch_phasecal(const uint8_t *data, const PcalRun *runs, int nruns, int pb, int bits, int32_t *acc,
+                     cudaStream_t st);
 
 }  // namespace sfxc

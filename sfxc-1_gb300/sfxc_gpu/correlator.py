@@ -210,6 +210,54 @@ class CorrelatorNode:
         return [out[i * per:(i + 1) * per].tobytes() for i in range(nsub)]
 
 
+class PhaseCal:
+    """Phase-cal extraction of one channel on a CorrelatorNode's GPU
+    (Input_node_data_writer::do_phasecal, sfxc/src/input_node_data_writer.cc:230-312).
+    push(blocks) takes the channel blocks the input node's writer takes up,
+    [(start_ticks, bytes, [(invalid_begin, n), ...])], and returns the packed
+    phase-cal messages of the integrations they finish."""
+
+    def __init__(self, node, sample_rate, bits, integration_ticks, station=0, frequency_number=0, sideband=1,
+                 polarisation=0):
+        self._node = node
+        self._lib = node._lib
+        p = L.PhasecalParams(sample_rate, bits, integration_ticks, station, frequency_number, sideband, polarisation)
+        self._h = self._lib.sfxc_gpu_phasecal_create(node._h, C.byref(p))
+        if not self._h:
+            raise L.SfxcError(L.EINVAL, self._lib.sfxc_gpu_last_error(node._h).decode())
+
+    def close(self):
+        if self._h:
+            self._lib.sfxc_gpu_phasecal_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def push(self, blocks):
+        stream = b"".join(bytes(b[1]) for b in blocks)
+        keep = []
+        cb = (L.ChannelBlock * max(1, len(blocks)))()
+        for i, (st, data, inv) in enumerate(blocks):
+            arr = (C.c_int32 * max(1, 2 * len(inv)))(*[x for pr in inv for x in pr])
+            keep.append(arr)
+            cb[i] = L.ChannelBlock(st, len(data), len(inv), arr)
+        msgs = []
+
+        def sink(user, kind, data, n):
+            if kind != 2:
+                return 1
+            msgs.append(C.string_at(data, n))
+            return 0
+
+        self._node._check(self._lib.sfxc_gpu_phasecal_push(self._h, _bytes_ptr(stream), len(blocks), cb,
+                                                            L.SINK(sink), None))
+        return msgs
+
+
 def delay_list(del_bytes, start_ticks, stop_ticks, sample_rate, bits, clock=(0.0, 0.0, 0), capacity=1 << 20):
     lib = L.load()
     buf = _bytes_ptr(del_bytes)

@@ -19,6 +19,7 @@ EXPORTS = [
     "sfxc_gpu_copy_unpacked", "sfxc_gpu_copy_spectra", "sfxc_gpu_last_timings", "sfxc_gpu_delay_list",
     "sfxc_gpu_write_protocol", "sfxc_gpu_extract_channels", "sfxc_gpu_copy_spectra_noalloc",
     "sfxc_gpu_reader_create", "sfxc_gpu_reader_next", "sfxc_gpu_reader_destroy", "sfxc_gpu_extract_block",
+    "sfxc_gpu_phasecal_create", "sfxc_gpu_phasecal_push", "sfxc_gpu_phasecal_destroy",
 ]
 FORMAT_VDIF, FORMAT_MARK5B = 0, 1
 
@@ -84,6 +85,12 @@ class ReaderBlock(C.Structure):
                 ("start_ticks", C.c_int64), ("n_invalid", C.c_int32), ("invalid", C.POINTER(C.c_int32))]
 
 
+class PhasecalParams(C.Structure):
+    _fields_ = [("sample_rate", C.c_int32), ("bits_per_sample", C.c_int32), ("integration_ticks", C.c_int64),
+                ("station_number", C.c_int32), ("frequency_number", C.c_int32), ("sideband", C.c_int32),
+                ("polarisation", C.c_int32)]
+
+
 SINK = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t)
 
 _lib = None
@@ -126,6 +133,11 @@ def load(path=None):
     lib.sfxc_gpu_reader_destroy.argtypes = [C.c_void_p]
     lib.sfxc_gpu_extract_block.argtypes = [C.c_void_p, C.POINTER(ReaderBlock), C.c_int32, C.c_int32, C.c_int32,
                                            C.c_int32, C.POINTER(C.c_int32), C.c_void_p, C.POINTER(C.c_int32)]
+    lib.sfxc_gpu_phasecal_create.restype = C.c_void_p
+    lib.sfxc_gpu_phasecal_create.argtypes = [C.c_void_p, C.POINTER(PhasecalParams)]
+    lib.sfxc_gpu_phasecal_push.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(ChannelBlock), SINK,
+                                           C.c_void_p]
+    lib.sfxc_gpu_phasecal_destroy.argtypes = [C.c_void_p]
     _lib = lib
     return lib
 

@@ -187,7 +187,30 @@ def make_formats():
     print("formats done")
 
 
+def make_phasecal():
+    """Phase-cal messages of the reference's Input_node_data_writer for
+    phasecal_cases(): per case the SHA-256 of each message, in order."""
+    import json
+    sys.path.insert(0, os.path.dirname(HERE))
+    from golden_io import Golden, phasecal_blocks, phasecal_cases
+    out = {}
+    for name, (fx, k, ticks, first, inject) in phasecal_cases().items():
+        g = Golden(fx)
+        m, s = g.meta, g.meta["streams"][k]
+        _, raw = jobs.protocol(phasecal_blocks(g, k, first, inject), g.slices(k), s[2], s[7],
+                               m["integration_time_us"], phasecal_ticks=ticks)
+        P = int(s[2] / 10e3)
+        n = 24 + 4 * P
+        assert len(raw) % n == 0
+        msgs = [raw[i:i + n] for i in range(0, len(raw), n)]
+        out[name] = {"messages": [hashlib.sha256(x).hexdigest() for x in msgs], "message_bytes": n}
+        print(name, len(msgs), "messages")
+    with open(os.path.join(HERE, "phasecal.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+
+
 if __name__ == "__main__":
+    make_phasecal()
     make_formats()
     make_extract()
     for name, sc in scenarios().items():

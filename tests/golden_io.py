@@ -85,6 +85,29 @@ class Golden:
         return bytes(np.asarray(self.z["stats"], dtype=np.uint8)).decode()
 
 
+def phasecal_cases():
+    """Phase-cal extraction cases over the channel blocks of scenario fixtures:
+    (fixture, stream, integration ticks, first block, extra invalid runs per
+    block).  The runs include one that begins where the previous one ends (the
+    reference never skips it), runs reaching or passing the block end, a run
+    past the end and a run covering a whole block."""
+    return {
+        "c1_every_third": ("c1_plain", 0, 6144000, 1,
+                           {2: [(100, 50), (150, 20), (400, 10)], 3: [(0, 10)], 4: [(31990, 10)],
+                            6: [(5, 7), (20, 30)]}),
+        "c1_every_block": ("c1_plain", 1, 2048000, 0, {5: [(1000, 3000), (4000, 8)], 8: [(31000, 5000)]}),
+        "onebit": ("onebit", 1, 1536000, 0, {3: [(100, 50), (150, 20)], 7: [(0, 4000)], 9: [(3999, 1)]}),
+        "multi_scenario_runs": ("multi", 0, 256000, 0, {20: [(1999, 1)], 21: [(2500, 4)]}),
+        "multi_short": ("multi", 2, 192000, 2, {4: [(0, 1), (1, 1), (2, 1)], 11: [(600, 2000)]}),
+    }
+
+
+def phasecal_blocks(g, k, first, inject):
+    """A fixture's channel blocks from block `first` on, with extra invalid runs."""
+    return [(st, d, sorted(list(inv) + [tuple(r) for r in inject.get(b, [])]))
+            for b, (st, d, inv) in enumerate(g.blocks(k)) if b >= first]
+
+
 def parse_cor(data, nchan):
     """Split correlator output bytes into header bytes and visibility arrays.
 
