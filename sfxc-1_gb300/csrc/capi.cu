@@ -1393,7 +1393,9 @@ int sfxc_gpu_phasecal_push(sfxc_gpu_phasecal *pc, const uint8_t *stream, int32_t
             iv++;
             if (i >= size) break;
           }
-          const int64_t end = (iv < k.n_invalid && k.invalid[2 * iv] > i) ? (int64_t)k.invalid[2 * iv] : (int64_t)size;
+          // (a run beginning at or past the block end is never reached)
+          const int64_t end = (iv < k.n_invalid && k.invalid[2 * iv] > i) ? std::min<int64_t>(k.invalid[2 * iv], size)
+                                                                            : (int64_t)size;
           add_run(off + i, end - i);
           i = end;
         }
@@ -1403,7 +1405,16 @@ int sfxc_gpu_phasecal_push(sfxc_gpu_phasecal *pc, const uint8_t *stream, int32_t
     const int rows = row + 1;
     if (!pc->started || (runs.empty() && closes.empty())) return SFXC_GPU_OK;
     CK(cudaSetDevice(c->device));
-    pc->acc.ensure((size_t)rows * P * 4);
+    if ((size_t)rows * P * 4 > pc->acc.cap) {
+      // grow, keeping the running integration of row 0
+      DevBuf grown;
+      grown.ensure((size_t)std::max(rows, 4) * P * 4);
+      if (pc->live) {
+        CK(cudaMemcpyAsync(grown.p, pc->acc.p, (size_t)P * 4, cudaMemcpyDeviceToDevice, c->st));
+        CK(cudaStreamSynchronize(c->st));
+      }
+      pc->acc.swap(grown);
+    }
     // a new integration's row starts from zero; row 0 keeps the running one
     const int first_clear = pc->live ? 1 : 0;
     if (rows > first_clear)
