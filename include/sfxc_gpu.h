@@ -171,6 +171,17 @@ int sfxc_gpu_push_protocol(sfxc_gpu_ctx *ctx, int32_t stream, const uint8_t *byt
  * (the packed message of Correlation_core::tsys_write).  Return 0 to go on. */
 typedef int (*sfxc_output_sink)(void *user, int32_t kind, const void *data, size_t n);
 
+/* UVW coordinates for the timeslice headers of the next and later
+ * integrations (until set again; sfxc_gpu_set_parameters resets them to
+ * zero): n_streams x max(1, n_phase_centers) x 3 doubles, u, v, w of each
+ * stream (params.streams order) and phase centre.  Correlator_node::
+ * set_parameters evaluates its UVW model at the integration's mid-time and
+ * hands these to Correlation_core::set_parameters (sfxc/src/correlator_node.cc:
+ * 327-357); integration_write puts those of the first stream of each station
+ * in the header, for the centre being written (pulsar bins and the phased
+ * array: centre 0) (sfxc/src/correlation_core.cc:350-364). */
+int sfxc_gpu_set_uvw(sfxc_gpu_ctx *ctx, const double *uvw, size_t n_doubles);
+
 /* Correlate the next integration of the job (all streams must have pushed). */
 int sfxc_gpu_run_integration(sfxc_gpu_ctx *ctx, sfxc_output_sink sink, void *user);
 

@@ -192,6 +192,11 @@ def correlate(job, dump=False, impl="reference", precision=32):
                 lines.append((key, p))
         if job.get("mask_normalize"):
             lines.append(("mask_normalize", 1))
+        # UVW for the timeslice headers: float64 [integration][stream][centre][3]
+        if job.get("uvw") is not None:
+            p = os.path.join(d, "uvw.f64")
+            np.asarray(job["uvw"], dtype=np.float64).tofile(p)
+            lines.append(("uvw", p))
         if job.get("phased_array"):
             lines.append(("phased_array", 1))
         if int(job.get("n_phase_centers", 1)) > 1:

@@ -483,6 +483,14 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
     c.protocol_pos = 0;
   }
 
+  // UVW per integration, stream (job order) and phase centre: float64 file
+  std::vector<double> uvw_in;
+  if (has(kv, "uvw")) {
+    const std::vector<char> b = read_file(get(kv, "uvw")[0]);
+    uvw_in.resize(b.size() / sizeof(double));
+    if (!uvw_in.empty()) std::memcpy(&uvw_in[0], &b[0], uvw_in.size() * sizeof(double));
+    if (uvw_in.size() < (size_t)n_int * nstreams * 3 * p.n_phase_centers) die("uvw file too short");
+  }
   std::string od(outdir);
   FILE *tsys_f = std::fopen((od + "/tsys.bin").c_str(), "wb");
   FILE *stats_f = std::fopen((od + "/stats.txt").c_str(), "w");
@@ -501,6 +509,10 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
     for (int i = 0; i < nstreams; i++) {
       int s = p.station_streams[i].station_stream;
       akima[s] = tables[stream_station_index[i]].create_akima_spline(p.start_time, p.integration_time);
+      // the UVW model's values at the integration's mid-time, as given by the job
+      if (!uvw_in.empty())
+        for (int q = 0; q < 3 * p.n_phase_centers; q++)
+          uvw[s][q] = uvw_in[((size_t)it * nstreams + i) * 3 * p.n_phase_centers + q];
     }
     if (p.pulsar_binning)
       core_pulsar->set_parameters(p, pulsar, akima, uvw, 0);

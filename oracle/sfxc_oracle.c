@@ -726,6 +726,11 @@ typedef struct {
      window over 2 number_channels lags, and the per-channel normalisation;
      NULL / 0 when absent (mask of ones, window from the window type) */
   double *mask, *lag_window;
+  /* u, v, w per integration, stream and phase centre for the timeslice
+   * headers (NULL: zeros), as Correlator_node::set_parameters hands them to
+   * the core (sfxc/src/correlator_node.cc:327-357) */
+  double *uvw;
+  size_t n_uvw;
   int mask_normalize;
   /* phase centres (Correlation_parameters::n_phase_centers) and the output
      file index of each (the manager's source list; 0 when absent) */
@@ -1483,21 +1488,29 @@ static void uvshift_add(const job_t *j, const double *in, double *out, double dd
 }
 
 static void write_integration(const job_t *j, const bl_t *bl, int nbl, const double *acc, b2f_t *w,
-                              int64_t (*nfl)[2], int nffts, int integration, int32_t sourcenr, bytes_t *out,
-                              bytes_t *out64) {
+                              int64_t (*nfl)[2], int nffts, int integration, int32_t sourcenr, int centre,
+                              bytes_t *out, bytes_t *out64) {
   const int M = j->M, K = M + 1, N = j->nstreams;
   bpush(out, &sourcenr, 4);
-  int stations[512], nst = 0;
+  /* stations in stream order, with the first stream of each
+   * (Correlation_core::integration_write, sfxc/src/correlation_core.cc:350-364) */
+  int stations[512], first[512], nst = 0;
   for (int i = 0; i < N; i++) {
     int s = j->streams[i].station_number, seen = 0;
     for (int k = 0; k < nst; k++) seen |= stations[k] == s;
-    if (!seen) stations[nst++] = s;
+    if (!seen) first[nst] = i, stations[nst++] = s;
   }
+  const int npc = j->n_pc > 1 ? j->n_pc : 1;
   int32_t ts[4] = {j->integration_nr + integration, nbl, nst, N};
   bpush(out, ts, 16);
   for (int k = 0; k < nst; k++) {
     int32_t h[2] = {stations[k], 0};
     double uvw[3] = {0, 0, 0};
+    if (j->uvw) {
+      const size_t o = (((size_t)integration * N + first[k]) * npc + centre) * 3;
+      if (o + 3 > j->n_uvw) die("uvw file too short");
+      memcpy(uvw, j->uvw + o, sizeof(uvw));
+    }
     bpush(out, h, 8);
     bpush(out, uvw, 24);
   }
@@ -1850,6 +1863,12 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
     for (int q = 0; q <= j.M; q++) j.mask[q] = ((const float *)b)[q];
     free(b);
   }
+  kv_t *uv = kv_get(k, "uvw", 0);
+  if (uv) {
+    size_t nb = 0;
+    j.uvw = (double *)read_all(uv->v[0], &nb);
+    j.n_uvw = nb / sizeof(double);
+  }
   kv_t *lw = kv_get(k, "lag_window", 0);
   if (lw) {
     size_t nb = 0;
@@ -2002,7 +2021,7 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
         }
       }
       bl_t *pb = xmalloc((size_t)nsubs * sizeof(bl_t)); /* (0, 0) pairs */
-      write_integration(&j, pb, nsubs, acc, w, nfl, nffts, it, 0, &cor, &cor64);
+      write_integration(&j, pb, nsubs, acc, w, nfl, nffts, it, 0, 0, &cor, &cor64);
       free(pb);
       free(acc);
     } else if (!j.pulsar) {
@@ -2038,7 +2057,7 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
       }
       for (int c2 = 0; c2 < j.n_pc; c2++) {
         normalize(&j, bl, nbl, pc + c2 * PCS, w, nfl, nffts);
-        write_integration(&j, bl, nbl, pc + c2 * PCS, w, nfl, nffts, it, j.pc_file[c2], &cor, &cor64);
+        write_integration(&j, bl, nbl, pc + c2 * PCS, w, nfl, nffts, it, j.pc_file[c2], c2, &cor, &cor64);
       }
       free(acc);
       free(pc);
@@ -2135,7 +2154,7 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
       for (int bin = 0; bin < nbins; bin++) {
         double *a = acc + (size_t)bin * nbl * K * 2;
         normalize(&j, bl, nbl, a, w, nfl, nffts);
-        write_integration(&j, bl, nbl, a, w, nfl, nffts, it, bin, &cor, &cor64);
+        write_integration(&j, bl, nbl, a, w, nfl, nffts, it, bin, 0, &cor, &cor64);
       }
       free(acc);
       free(bins);

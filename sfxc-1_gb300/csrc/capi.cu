@@ -157,6 +157,8 @@ struct sfxc_gpu_ctx {
   int npc = 1;
   std::vector<int32_t> pc_file;
   int phased = 0;  // phased-array core
+  // UVW per stream and phase centre for the timeslice headers (sfxc_gpu_set_uvw)
+  std::vector<double> uvw;
   std::vector<float> pc_weights;
   DevBuf pcacc, uvp;
   // device
@@ -362,6 +364,7 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
   c->pc_file.assign(c->npc, 0);
   if (p->phase_center_file_index) c->pc_file.assign(p->phase_center_file_index, p->phase_center_file_index + c->npc);
   c->p.phase_center_file_index = nullptr;
+  c->uvw.assign((size_t)p->n_streams * c->npc * 3, 0.0);
   c->phased = p->phased_array != 0;
   if (c->phased && (c->nbins > 1 || c->npc > 1 || p->number_channels != p->fft_size_correlation))
     throw Error(SFXC_GPU_EINVAL,
@@ -492,23 +495,23 @@ std::vector<std::pair<int, int>> subint_ranges(const sfxc_gpu_ctx *c) {
 // bls: the baselines written (the job's, or the phased core's one (0, 0)
 // entry per sub-integration, Correlation_core_phased::create_baselines).
 void serialize_integration(sfxc_gpu_ctx *c, const std::vector<Baseline> &bls, const float2 *vis, int32_t source_nr,
-                           const std::vector<std::pair<int64_t, int64_t>> &nfl, std::vector<uint8_t> &o) {
+                           int centre, const std::vector<std::pair<int64_t, int64_t>> &nfl, std::vector<uint8_t> &o) {
   const int N = (int)c->streams.size();
   const int nbl = (int)bls.size();
   put(o, source_nr);
-  std::vector<int> stations;
+  // stations in stream order, each with its first stream
+  std::vector<std::pair<int, int>> stations;
   std::set<int> seen;
   for (int i = 0; i < N; i++)
-    if (seen.insert(c->streams[i].station_number).second) stations.push_back(c->streams[i].station_number);
+    if (seen.insert(c->streams[i].station_number).second) stations.push_back({c->streams[i].station_number, i});
   put(o, (int32_t)(c->p.integration_nr + c->current_integration));
   put(o, (int32_t)nbl);
   put(o, (int32_t)stations.size());
   put(o, (int32_t)N);
-  for (int s : stations) {
-    put(o, (int32_t)s);
+  for (auto &s : stations) {
+    put(o, (int32_t)s.first);
     put(o, (int32_t)0);
-    const double uvw[3] = {0, 0, 0};  // the UVW model is not part of this path
-    for (double v : uvw) put(o, v);
+    for (int k = 0; k < 3; k++) put(o, c->uvw[((size_t)s.second * c->npc + centre) * 3 + k]);
   }
   for (int i = 0; i < N; i++) {
     o.push_back((uint8_t)c->streams[i].station_number);
@@ -972,10 +975,11 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   // ---- output bytes (integration_write per bin) and tsys records
   std::vector<uint8_t> o;
   if (c->phased) {
-    serialize_integration(c, std::vector<Baseline>(nphs, Baseline{0, 0}), vis, 0, nfl, o);
+    serialize_integration(c, std::vector<Baseline>(nphs, Baseline{0, 0}), vis, 0, 0, nfl, o);
   } else {
     for (int bin = 0; bin < nout; bin++)
-      serialize_integration(c, c->bl, vis + (size_t)bin * nbl * c->Kout, pulsar ? bin : c->pc_file[bin], nfl, o);
+      serialize_integration(c, c->bl, vis + (size_t)bin * nbl * c->Kout, pulsar ? bin : c->pc_file[bin],
+                            pulsar ? 0 : bin, nfl, o);
   }
   if (sink && sink(user, 0, o.data(), o.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
   for (int i = 0; i < N && !c->phased; i++) {  // the phased core writes no tsys records
@@ -1454,6 +1458,14 @@ int sfxc_gpu_phasecal_push(sfxc_gpu_phasecal *pc, const uint8_t *stream, int32_t
   } catch (const Error &e) {
     return fail(c, e);
   }
+}
+
+int sfxc_gpu_set_uvw(sfxc_gpu_ctx *c, const double *uvw, size_t n) {
+  if (!c) return SFXC_GPU_EINVAL;
+  if (!c->have_job) return fail(c, Error(SFXC_GPU_ESTATE, "no parameters set"));
+  if (!uvw || n != c->uvw.size()) return fail(c, Error(SFXC_GPU_EINVAL, "uvw must hold n_streams x phase centres x 3 values"));
+  std::copy(uvw, uvw + n, c->uvw.begin());
+  return SFXC_GPU_OK;
 }
 
 int sfxc_gpu_last_timings(const sfxc_gpu_ctx *c, float *ms6) {

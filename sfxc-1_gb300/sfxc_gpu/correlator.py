@@ -127,6 +127,12 @@ class CorrelatorNode:
         buf = _bytes_ptr(data)
         self._check(self._lib.sfxc_gpu_push_protocol(self._h, stream, buf, len(data)))
 
+    def set_uvw(self, uvw):
+        """u, v, w per stream and phase centre (array [n_streams][centres][3])
+        for the timeslice headers of the next integrations."""
+        u = np.ascontiguousarray(uvw, dtype=np.float64)
+        self._check(self._lib.sfxc_gpu_set_uvw(self._h, u.ctypes.data, u.size))
+
     def run_integration(self):
         """Returns (output bytes (bytes or bytearray), [tsys record bytes per stream])."""
         out, tsys = [], []
@@ -149,6 +155,8 @@ class CorrelatorNode:
         self.set_parameters(job)
         cor, tsys = [], []
         for it in range(int(job["n_integrations"])):
+            if job.get("uvw") is not None:  # [integration][stream][centre][3]
+                self.set_uvw(job["uvw"][it])
             for k in range(self.nstreams):
                 self.push_protocol(k, job["protocols"][k][it])
             o, t = self.run_integration()

@@ -19,7 +19,7 @@ EXPORTS = [
     "sfxc_gpu_copy_unpacked", "sfxc_gpu_copy_spectra", "sfxc_gpu_last_timings", "sfxc_gpu_delay_list",
     "sfxc_gpu_write_protocol", "sfxc_gpu_extract_channels", "sfxc_gpu_copy_spectra_noalloc",
     "sfxc_gpu_reader_create", "sfxc_gpu_reader_next", "sfxc_gpu_reader_destroy", "sfxc_gpu_extract_block",
-    "sfxc_gpu_phasecal_create", "sfxc_gpu_phasecal_push", "sfxc_gpu_phasecal_destroy",
+    "sfxc_gpu_phasecal_create", "sfxc_gpu_phasecal_push", "sfxc_gpu_phasecal_destroy", "sfxc_gpu_set_uvw",
 ]
 FORMAT_VDIF, FORMAT_MARK5B = 0, 1
 
@@ -114,6 +114,7 @@ def load(path=None):
     lib.sfxc_gpu_set_parameters.argtypes = [C.c_void_p, C.POINTER(CorrelationParams)]
     lib.sfxc_gpu_push_protocol.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]
     lib.sfxc_gpu_run_integration.argtypes = [C.c_void_p, SINK, C.c_void_p]
+    lib.sfxc_gpu_set_uvw.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
     lib.sfxc_gpu_copy_unpacked.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]
     lib.sfxc_gpu_copy_spectra.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]
     lib.sfxc_gpu_copy_spectra_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]

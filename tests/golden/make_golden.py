@@ -91,6 +91,18 @@ def mask_params(name, job):
     job["mask_normalize"] = 1
 
 
+def uvw_values(name, job):
+    """UVW header values (what the correlator node's UVW model would give at
+    each integration's mid-time) for some cases: seeded values of baseline-
+    like size, different for each stream, so that the header shows which
+    stream of a station and which phase centre was taken."""
+    if name not in ("multi", "phase_centers", "pulsar", "phased"):
+        return
+    rng = np.random.Generator(np.random.PCG64(len(name) * 1000 + 7))
+    npc = max(1, int(job.get("n_phase_centers", 1)))
+    job["uvw"] = rng.normal(0.0, 3.0e6, size=(int(job["n_integrations"]), len(job["streams"]), npc, 3))
+
+
 # two polycos (the closer one is used), non-zero phase polynomial
 PULSAR = dict(nbins=8, gate=(0.2, 0.9),
               polyco=[(60000.0 + 36000.0 / 86400 - 0.01, 56.8, 0.25, 1 / 0.0334, 1400.0,
@@ -108,6 +120,7 @@ def make(name, sc):
         job["pulsar"] = (PULSAR["nbins"],) + PULSAR["gate"]
         job["polyco"] = PULSAR["polyco"]
     mask_params(name, job)
+    uvw_values(name, job)
     if name == "phased":
         job["phased_array"] = 1
     res = jobs.correlate(job, dump=True)
@@ -137,7 +150,9 @@ def make(name, sc):
     for key in ("mask", "lag_window"):
         if key in job:
             rec[key] = np.asarray(job[key], dtype=np.float32)
-    meta = {k: v for k, v in job.items() if k not in ("del_bytes", "protocols", "mask", "lag_window")}
+    if "uvw" in job:
+        rec["uvw"] = np.asarray(job["uvw"], dtype=np.float64)
+    meta = {k: v for k, v in job.items() if k not in ("del_bytes", "protocols", "mask", "lag_window", "uvw")}
     meta["block_bytes"] = sc.block_bytes
     meta["rec0"] = rec0
     meta["slice_samples"] = slice_samples

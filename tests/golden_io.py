@@ -59,6 +59,8 @@ class Golden:
         for key in ("mask", "lag_window"):  # Mask_parameters of the spectral-reduction cases
             if key in self.z.files:
                 job[key] = np.asarray(self.z[key], dtype=np.float32)
+        if "uvw" in self.z.files:  # UVW header values [integration][stream][centre][3]
+            job["uvw"] = np.asarray(self.z["uvw"], dtype=np.float64)
         protos = []
         for k in range(self.nstreams):
             s = m["streams"][k]

@@ -29,6 +29,8 @@ def run_golden(node, case):
         1 if job["window"] != 0 else 0)
     cor, tsys = [], []
     for it in range(g.nint):
+        if job.get("uvw") is not None:
+            node.set_uvw(job["uvw"][it])
         for k in range(g.nstreams):
             node.push_protocol(k, job["protocols"][k][it])
         o, t = node.run_integration()
@@ -152,3 +154,30 @@ def test_errors_leave_context_usable(gpu_node):
     assert e.value.code == lib.EINVAL
     cor, _ = gpu_node.correlate(job)  # a fresh job on the same context works
     compare_cor(cor, g.cor, 512, FP32_TOL)
+
+
+@pytest.mark.gpu
+def test_uvw_header_values(gpu_node):
+    """UVW values reach the timeslice header for the first stream of each
+    station; a wrong count is refused; a new job starts from zeros."""
+    import struct
+    from sfxc_gpu import correlator, lib
+    g = Golden("multi")
+    job = g.job(correlator.write_protocol)
+    gpu_node.set_parameters(job)
+    with pytest.raises(lib.SfxcError) as e:
+        gpu_node.set_uvw(job["uvw"][0][:2])
+    assert e.value.code == lib.EINVAL
+    cor, _ = gpu_node.correlate(job)
+    hdr = struct.unpack_from("<i4i", cor, 0)
+    nuvw = hdr[3]
+    streams = job["streams"]
+    first = {}
+    for i, s in enumerate(streams):
+        first.setdefault(s[0], i)
+    for k in range(nuvw):
+        station, _, u, v, w = struct.unpack_from("<2i3d", cor, 20 + 32 * k)
+        assert (u, v, w) == tuple(job["uvw"][0][first[station]][0])
+    cor0, _ = gpu_node.correlate(dict(job, uvw=None))
+    for k in range(nuvw):
+        assert struct.unpack_from("<3d", cor0, 28 + 32 * k) == (0.0, 0.0, 0.0)
