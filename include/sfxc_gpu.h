@@ -25,8 +25,9 @@
  * Conventions: plain pointers and sizes; every call returns 0 or a negative
  * status (SFXC_GPU_E*), with a message from sfxc_gpu_last_error().  Input
  * buffers belong to the caller and are not referenced after a call returns.
- * One host thread drives one context; a context owns one CUDA stream on one
- * device.  Contexts created in one process get successive stream priorities
+ * One host thread drives one context; a context owns two CUDA streams on one
+ * device (the second carries per-block parameters ahead of the first).
+ * Contexts created in one process get successive stream priorities
  * (cycling through the device's range), so that jobs correlated side by side
  * on one GPU finish in turn and their host work overlaps each other's kernels.
  * The library has no CPU fallback: without a usable GPU, sfxc_gpu_create
@@ -210,10 +211,11 @@ int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t 
  * race on it.  Arguments and result as sfxc_gpu_copy_spectra. */
 int sfxc_gpu_copy_spectra_noalloc(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
 /* Device time (ms) of the last integration, CUDA events on the context's
- * stream: [0] per-block delay and phase parameters, unpack and fringe
- * stopping, [1] windowed FFT, [2] X-step, [3] normalisation and result
- * copies, [4] total from the first kernel to the last copy; [5] number of
- * kernel launches. */
+ * stream: [0] unpack and fringe stopping (with the first sub-integration
+ * chunk's per-block delay and phase parameters; those of later chunks run on
+ * the context's second stream during the previous chunk's X-step), [1]
+ * windowed FFT, [2] X-step, [3] normalisation and result copies, [4] total
+ * from the first kernel to the last copy; [5] number of kernel launches. */
 int sfxc_gpu_last_timings(const sfxc_gpu_ctx *ctx, float *out6);
 
 /* Integer delay list of one interval (Input_node_tasklet::add_time_interval):

@@ -130,6 +130,9 @@ struct JobTables {
 struct sfxc_gpu_ctx {
   int device = 0, x_mode = 0;
   cudaStream_t st = nullptr;
+  // second stream: the next chunk's per-block parameters (FP64) beside the
+  // current chunk's X-step
+  cudaStream_t st2 = nullptr;
   cudaEvent_t ev[6] = {};
   float timings[6] = {};
   std::vector<cudaEvent_t> evpool;
@@ -181,6 +184,11 @@ struct sfxc_gpu_ctx {
 };
 
 namespace {
+
+// CTAs per SM of the per-block parameter launches beside the X-step (0:
+// uncapped; caps of 1, 2 and 4 measured slower: the launch then runs longer
+// and slows the X-step for longer)
+constexpr int kSideParamCtas = 0;
 
 int fail(sfxc_gpu_ctx *c, const Error &e) {
   if (c) c->err = e.msg;
@@ -731,8 +739,10 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   c->spec.ensure((size_t)(tc_x ? kTcSlots : N) * (tc_x ? (max_rows + 7) / 8 * 8 : max_rows) * kpad * sizeof(float2));
   c->derr.ensure(sizeof(int));
   CK(cudaMemsetAsync(c->derr.p, 0, sizeof(int), st));
+  // two sets of per-block records: chunk ch uses set ch & 1, so the next
+  // chunk's are computed while the current chunk is still transformed
   for (int i = 0; i < N; i++) {
-    c->sc[i].bpar.ensure((size_t)max_blocks * sizeof(BlockPar));
+    c->sc[i].bpar.ensure((size_t)2 * max_blocks * sizeof(BlockPar));
   }
   float t_f1 = 0, t_f2 = 0, t_x = 0;
   // pulsar setup (Correlation_core_pulsar::set_parameters, correlation_core_pulsar.cc:46-95)
@@ -779,8 +789,9 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     upload(c->offsets, off.data(), off.size() * 8, st);
     c->bins.ensure((size_t)max_rows * K * sizeof(int16_t));
   }
-  // four events per chunk (+2 for normalisation), recorded without host syncs
-  const size_t nev = ranges.size() * 4 + 2;
+  // four events per chunk on the main stream and one on the second (+2 for
+  // normalisation), recorded without host syncs
+  const size_t nev = ranges.size() * 5 + 2;
   while (c->evpool.size() < nev) {
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
@@ -807,7 +818,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       const int b0 = chunked ? r0 * c->sc[i].hop / kNd : 0;
       const int b1 = chunked ? std::min(c->sc[i].n_blocks, (r1 + 1 + minus) * c->sc[i].hop / kNd) : c->sc[i].n_blocks;
       d.ts = c->ts.as<float>() + (size_t)i * max_blocks * kNd;
-      d.bpar = c->sc[i].bpar.as<BlockPar>();
+      d.bpar = c->sc[i].bpar.as<BlockPar>() + (ch & 1) * (size_t)max_blocks;
       d.block0 = b0;
       d.n_blocks = b1 - b0;
       d.spline_lo = spline_lo_for(d, c->sc[i].sp.x);
@@ -853,12 +864,21 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   launch_bitstat(c->streamdev.as<StreamDev>(), c->items.as<int4>(), (int)items.size(), st);
   CK(cudaGetLastError());
   int launches = items.empty() ? 0 : 1;
+  // The per-block parameters (block_params_kernel, FP64-pipe bound, few
+  // registers) of chunk ch + 1 run on the second stream once chunk ch's
+  // windowed FFT is done, i.e. beside chunk ch's X-step, whose CTAs leave
+  // registers and issue slots free; chunk ch + 1's transforms wait for them.
+  const size_t ev_side = ranges.size() * 4 + 2;  // the second stream's events, one per chunk
   size_t ev = 0;
   for (size_t ch = 0; ch < ranges.size(); ch++) {
     const int nrows = ranges[ch].second - ranges[ch].first;
     StreamDev *dchunk = c->streamdev.as<StreamDev>() + ch * per_chunk;
     CK(cudaEventRecord(c->evpool[ev], st));
-    launch_fstep_block(dchunk, N, max_blocks, c->tw256.as<float2>(), st);
+    if (ch == 0)
+      launch_block_params(dchunk, N, max_blocks, st);
+    else
+      CK(cudaStreamWaitEvent(st, c->evpool[ev_side + ch], 0));
+    launch_fstep(dchunk, N, max_blocks, c->tw256.as<float2>(), st);
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->evpool[ev + 1], st));
     for (size_t g = 0; g < groups.size(); g++) {
@@ -871,6 +891,13 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       CK(cudaGetLastError());
     }
     CK(cudaEventRecord(c->evpool[ev + 2], st));
+    if (ch + 1 < ranges.size()) {
+      // chunk ch + 1's records go to the other set, last read by chunk ch - 1's transforms
+      CK(cudaStreamWaitEvent(c->st2, c->evpool[ev + 2], 0));
+      launch_block_params(dchunk + per_chunk, N, max_blocks, c->st2, kSideParamCtas);
+      CK(cudaGetLastError());
+      CK(cudaEventRecord(c->evpool[ev_side + ch + 1], c->st2));
+    }
     if (c->phased) {
       launch_phased(c->spec.as<float2>(), max_rows, kpad, N, ranges[ch].first, nrows, K, c->nsub, c->acc.as<float2>(),
                     st);
@@ -1023,9 +1050,13 @@ sfxc_gpu_ctx *sfxc_gpu_create(const sfxc_gpu_config *config) {
     static std::atomic<unsigned> created{0};
     int least = 0, greatest = 0;
     CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    // The second stream sits one level below the first, so that when a
+    // chunk's windowed FFT ends the X-step's CTAs are placed before the next
+    // chunk's parameter CTAs fill the room they leave.
     const int levels = least - greatest + 1;
-    const int prio = greatest + (int)(created.fetch_add(1) % (unsigned)std::max(levels, 1));
+    const int prio = greatest + (int)(created.fetch_add(1) % (unsigned)std::max(levels - 1, 1));
     CK(cudaStreamCreateWithPriority(&c->st, cudaStreamNonBlocking, prio));
+    CK(cudaStreamCreateWithPriority(&c->st2, cudaStreamNonBlocking, std::min(prio + 1, least)));
     for (auto &e : c->ev) CK(cudaEventCreate(&e));
   } catch (const Error &e) {
     g_error = e.msg;
@@ -1038,10 +1069,12 @@ void sfxc_gpu_destroy(sfxc_gpu_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->st) cudaStreamSynchronize(c->st);
+  if (c->st2) cudaStreamSynchronize(c->st2);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
   for (auto &e : c->evpool) cudaEventDestroy(e);
   if (c->st) cudaStreamDestroy(c->st);
+  if (c->st2) cudaStreamDestroy(c->st2);
   delete c;
 }
 

@@ -198,13 +198,23 @@ __global__ void __launch_bounds__(256, 4) fstep_block_kernel(const StreamDev *__
 // fractional delay at the block centre, the fringe phase at the block start
 // and its linear step over the block, the amplitude at the centre.  The
 // phases leave FP64 only after reduction to one turn.
+__device__ __forceinline__ void block_params_one(const StreamDev &s, int bl, int lane);
+
+// CTAs of 128 blocks, strided over the stream's blocks when the grid is
+// smaller than the stream (a capped grid leaves room on the SMs to a
+// kernel running beside it).
 __global__ void __launch_bounds__(128) block_params_kernel(const StreamDev *__restrict__ streams) {
   const StreamDev &s = streams[blockIdx.y];
   const int lane = threadIdx.x & 31;
-  const int bl = blockIdx.x * blockDim.x + threadIdx.x;
-  // whole warps stay (neighbour exchange below); lanes past the end compute
-  // their block's times (the spline extrapolates) and store nothing
-  if ((int)(blockIdx.x * blockDim.x + (threadIdx.x & ~31)) >= s.n_blocks) return;
+  for (int base = blockIdx.x * blockDim.x; base < s.n_blocks; base += gridDim.x * blockDim.x) {
+    // whole warps stay (neighbour exchange below); lanes past the end compute
+    // their block's times (the spline extrapolates) and store nothing
+    if (base + (int)(threadIdx.x & ~31) >= s.n_blocks) break;
+    block_params_one(s, base + threadIdx.x, lane);
+  }
+}
+
+__device__ __forceinline__ void block_params_one(const StreamDev &s, int bl, int lane) {
   constexpr double kInvTick = 1.0 / 512000000.0, kInv2Pi = 0.15915494309189533577;
   const int64_t ct = s.start_ticks + (int64_t)(s.block0 + bl) * kNd * s.tps;
   // node intervals: the times grow with the block, so each is walked forward
@@ -1089,9 +1099,20 @@ static int sm_count() {
   return n;
 }
 
+void launch_block_params(const StreamDev *d_streams, int nstreams, int max_blocks, cudaStream_t st,
+                         int ctas_per_sm) {
+  int x = (max_blocks + 127) / 128;
+  if (ctas_per_sm > 0) x = std::max(1, std::min(x, ctas_per_sm * sm_count() / nstreams));
+  block_params_kernel<<<dim3(x, nstreams), 128, 0, st>>>(d_streams);
+}
+
 void launch_fstep_block(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256,
                         cudaStream_t st) {
-  block_params_kernel<<<dim3((max_blocks + 127) / 128, nstreams), 128, 0, st>>>(d_streams);
+  launch_block_params(d_streams, nstreams, max_blocks, st);
+  launch_fstep(d_streams, nstreams, max_blocks, tw256, st);
+}
+
+void launch_fstep(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256, cudaStream_t st) {
   // about two waves of 4 resident CTAs per SM, each CTA looping over rounds
   const int per_stream = std::max(1, 8 * sm_count() / nstreams);
   dim3 grid(std::min((max_blocks + 31) / 32, per_stream), nstreams);

@@ -7,8 +7,14 @@
 
 namespace sfxc {
 
+// block stage: per-block parameters (block_params_kernel), then the
+// transforms (fstep_block_kernel); launch_fstep_block runs both in order
 void launch_fstep_block(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256_128,
                         cudaStream_t st);
+// ctas_per_sm > 0: at most that many CTAs per SM in all (each striding over its stream's blocks)
+void launch_block_params(const StreamDev *d_streams, int nstreams, int max_blocks, cudaStream_t st,
+                         int ctas_per_sm = 0);
+void launch_fstep(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256, cudaStream_t st);
 void launch_unpack(const StreamDev *d_streams, int nstreams, int max_blocks, float *out, cudaStream_t st);
 void launch_extract(const uint8_t *in, int64_t nout, int N, int bits, int nsub, int fan_out, const int *tracks,
                     uint8_t *out, cudaStream_t st);
