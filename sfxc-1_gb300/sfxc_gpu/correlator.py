@@ -349,6 +349,20 @@ def write_protocol(blocks, slices, sample_rate, bits, integration_time_us):
     return [raw[offs[i]:offs[i + 1]] for i in range(len(slices))]
 
 
+def thread_channel_blocks(blocks, n_channels):
+    """The VDIF path with one channel per thread (Channel_extractor_tasklet_VDIF::
+    do_task, sfxc/src/channel_extractor_tasklet_vdif.cc:25-49): no extraction,
+    each reader block (read_recording's dicts) is its channel's next block as it
+    is, invalid runs included.  Returns, per channel, [(start_ticks, bytes,
+    [(invalid_begin, n), ...])] as write_protocol takes them."""
+    out = [[] for _ in range(n_channels)]
+    for b in blocks:
+        if not 0 <= b["channel"] < n_channels:
+            raise ValueError("block of channel %d outside the %d channels" % (b["channel"], n_channels))
+        out[b["channel"]].append((b["start_ticks"], b["data"], [tuple(r) for r in b["invalid"]]))
+    return out
+
+
 def read_recording(recording, fmt, *, ref_ticks, offset_ticks=0, track_bit_rate, frame_size=0, n_tracks, bits,
                    channel_tracks, max_blocks=None):
     """Reader blocks of a VDIF or Mark5B recording (fmt "vdif" / "mark5b"):

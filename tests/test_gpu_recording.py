@@ -93,3 +93,45 @@ def test_mark5b_recording_path(gpu_node):
     protos = _protocols_from_recordings(gpu_node, sc, recs, "mark5b",
                                         dict(track_bit_rate=sc.sample_rate, n_tracks=32, bits=2))
     assert protos == job["protocols"]
+
+
+def test_vdif_thread_per_channel_path(gpu_node):
+    """VDIF with one thread per channel (threads 0 and 1: a station's R and L
+    streams, frames interleaved): the reader's blocks, one frame each in this
+    mode (VDIF_reader::set_parameters, sfxc/src/vdif_reader.cc:211-218), go to
+    their channels unextracted (Channel_extractor_tasklet_VDIF), and the
+    protocol bytes and correlation equal the direct job's.  Frame 5 of thread 1
+    of station 1 is invalid: the whole of block 5 of its L stream."""
+    from sfxc_gpu import correlator, scenario, synth, timebase
+    sc, job, chans, nsamp = _job_and_streams(dict(
+        block_bytes=8000, runs=lambda st: {(st[1].number, "L"): [(5, 0, 8000)]}))
+    dels = scenario.del_tables(sc)
+    rec0, start, tint, slice_samples = scenario.job_timing(sc)
+    frame = 32 + 8000
+    protos = []
+    for si in range(len(sc.stations)):
+        per_thread = []
+        for th, pol in enumerate(("R", "L")):
+            words = np.frombuffer(bytes(chans[(si, pol)]), dtype=np.uint32)
+            per_thread.append(synth.vdif_file_bytes(words, payload_bytes=8000, sample_rate=sc.sample_rate, nchan=1,
+                                                    bits=2, start_mjd=sc.mjd, start_sec_of_day=sc.sec0,
+                                                    thread_id=th,
+                                                    invalid_frames=(5,) if (si == 1 and pol == "L") else ()))
+        nf = min(len(t) for t in per_thread) // frame
+        rec = b"".join(per_thread[th][f * frame:(f + 1) * frame] for f in range(nf) for th in range(2))
+        blocks = correlator.read_recording(rec, "vdif", ref_ticks=timebase.ticks_from_mjd_sec(sc.mjd, 0.0),
+                                           track_bit_rate=sc.sample_rate, frame_size=8000, n_tracks=0, bits=2,
+                                           channel_tracks=[[0, 1], [1, 0]])
+        per_chan = correlator.thread_channel_blocks(blocks, 2)
+        slices = [(start, start + tint, slice_samples, correlator.delay_list(dels[si], start, start + tint,
+                                                                              sc.sample_rate, sc.bits))]
+        for c, pol in enumerate(sc.pols):
+            direct = scenario.blocks_of(sc, chans[(si, pol)], (si, pol))
+            got = per_chan[c][:len(direct)]
+            assert [(t, bytes(d), list(map(tuple, inv))) for t, d, inv in got] == \
+                [(t, bytes(d), list(map(tuple, inv))) for t, d, inv in direct], (si, pol)
+            protos.append(correlator.write_protocol(per_chan[c], slices, sc.sample_rate, sc.bits, sc.integration_us))
+    assert protos == job["protocols"]
+    cor_direct, tsys_direct = gpu_node.correlate(job)
+    cor_rec, tsys_rec = gpu_node.correlate(dict(job, protocols=protos))
+    assert cor_rec == cor_direct and tsys_rec == tsys_direct
