@@ -211,11 +211,12 @@ int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t 
  * race on it.  Arguments and result as sfxc_gpu_copy_spectra. */
 int sfxc_gpu_copy_spectra_noalloc(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
 /* Device time (ms) of the last integration, CUDA events on the context's
- * stream: [0] unpack and fringe stopping (with the first sub-integration
- * chunk's per-block delay and phase parameters; those of later chunks run on
- * the context's second stream during the previous chunk's X-step), [1]
- * windowed FFT, [2] X-step, [3] normalisation and result copies, [4] total
- * from the first kernel to the last copy; [5] number of kernel launches. */
+ * stream: [0] unpack and fringe stopping, with any wait for the per-block
+ * delay and phase parameters, which run on the context's second stream (the
+ * first sub-integration chunk's beside the bit statistics, later chunks'
+ * during the previous chunk's X-step), [1] windowed FFT, [2] X-step, [3]
+ * normalisation and result copies, [4] total from the first kernel to the
+ * last copy; [5] number of kernel launches. */
 int sfxc_gpu_last_timings(const sfxc_gpu_ctx *ctx, float *out6);
 
 /* Integer delay list of one interval (Input_node_tasklet::add_time_interval):

@@ -860,24 +860,26 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     upload(c->uvp, uv.data(), uv.size() * sizeof(double4), st);
   }
   CK(cudaEventRecord(c->ev[0], st));
+  // The per-block parameters (block_params_kernel, FP64-pipe bound, few
+  // registers) run on the second stream: those of the first chunk beside the
+  // bit statistics (memory bound), those of chunk ch + 1 once chunk ch's
+  // windowed FFT is done, i.e. beside chunk ch's X-step, whose CTAs leave
+  // registers and issue slots free.  Each chunk's transforms wait for them.
+  const size_t ev_side = ranges.size() * 4 + 2;  // the second stream's events, one per chunk
+  CK(cudaStreamWaitEvent(c->st2, c->ev[0], 0));  // the descriptors are on the device
+  launch_block_params(c->streamdev.as<StreamDev>(), N, max_blocks, c->st2);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(c->evpool[ev_side], c->st2));
   // bit statistics read only chunk-independent fields (source bytes, ranges, histograms)
   launch_bitstat(c->streamdev.as<StreamDev>(), c->items.as<int4>(), (int)items.size(), st);
   CK(cudaGetLastError());
   int launches = items.empty() ? 0 : 1;
-  // The per-block parameters (block_params_kernel, FP64-pipe bound, few
-  // registers) of chunk ch + 1 run on the second stream once chunk ch's
-  // windowed FFT is done, i.e. beside chunk ch's X-step, whose CTAs leave
-  // registers and issue slots free; chunk ch + 1's transforms wait for them.
-  const size_t ev_side = ranges.size() * 4 + 2;  // the second stream's events, one per chunk
   size_t ev = 0;
   for (size_t ch = 0; ch < ranges.size(); ch++) {
     const int nrows = ranges[ch].second - ranges[ch].first;
     StreamDev *dchunk = c->streamdev.as<StreamDev>() + ch * per_chunk;
     CK(cudaEventRecord(c->evpool[ev], st));
-    if (ch == 0)
-      launch_block_params(dchunk, N, max_blocks, st);
-    else
-      CK(cudaStreamWaitEvent(st, c->evpool[ev_side + ch], 0));
+    CK(cudaStreamWaitEvent(st, c->evpool[ev_side + ch], 0));
     launch_fstep(dchunk, N, max_blocks, c->tw256.as<float2>(), st);
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->evpool[ev + 1], st));
