@@ -565,7 +565,9 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
       store_row<N, SPC, OUT_TC, !S::WSMEM>(dsm + r * SPC * S::BUF, S::BUF, sinfo, nv, fast, row0 + row, nrows_total,
                                            M, kpad, tw_rot, spec_out, tc_scale, threadIdx.x, S::THREADS);
     }
-    __syncthreads();  // the next step's FFT rewrites the buffers
+    // the next step's FFT rewrites the buffers (placing this barrier inside
+    // that FFT, after its first radix-16 pass, measured 1.7 % slower)
+    __syncthreads();
   }
 }
 
