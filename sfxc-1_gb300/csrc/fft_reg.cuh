@@ -129,9 +129,11 @@ __device__ __forceinline__ void twiddle16(float2 (&v)[16], float2 w1, float2 w2,
 // Twiddles of the radix-16 passes after the first, in shared memory.  The
 // pass of stride Ns (16, 256, ...) uses entries e = (Ns - 16) / 15 + k for
 // k < Ns, L = pass_table_len<LOGN>() entries in all; m = k N / (16 Ns) and
-// W = exp(-2 pi i / N).  Two layouts (TWK):
+// W = exp(-2 pi i / N).  Three layouts (TWK):
 //   15: tab[(r - 1) L + e] = W^(r m), r = 1..15, 15 L float2: every twiddle
 //       a correctly rounded table value, no products;
+//    8: tab[j L + e] = {W^(2j+1)m, W^(2j+2)m}, j < 4, 4 L float4: the first
+//       eight, the other seven as products with W^8m;
 //    4: tab[e] = {W^m, W^2m}, tab[L + e] = {W^4m, W^8m}, 2 L float4: a quarter
 //       of the space, the other eleven twiddles as products of these.
 // Either way consecutive threads read consecutive entries (no bank conflicts).
@@ -143,14 +145,14 @@ __host__ __device__ constexpr int pass_table_len() {
 }
 template <int LOGN, int TWK>
 __host__ __device__ constexpr int pass_table_bytes() {
-  return pass_table_len<LOGN>() * (TWK == 15 ? 15 * 8 : 32);
+  return pass_table_len<LOGN>() * (TWK == 15 ? 15 * 8 : TWK == 8 ? 64 : 32);
 }
 // Fill the table from tw[j] = exp(-2 pi i j / N) by threads tid = 0..nthr-1
 // (the caller synchronises before use).
 template <int LOGN, int TWK>
 __device__ __forceinline__ void fill_pass_table(void *tab, const float2 *__restrict__ tw, int tid, int nthr) {
   constexpr int N = 1 << LOGN, L = pass_table_len<LOGN>();
-  static_assert(TWK == 4 || TWK == 15, "table layout");
+  static_assert(TWK == 4 || TWK == 8 || TWK == 15, "table layout");
   auto m_of = [](int e) {
     int Ns = 16;
     while (e >= (16 * Ns - 16) / 15) Ns *= 16;
@@ -159,6 +161,13 @@ __device__ __forceinline__ void fill_pass_table(void *tab, const float2 *__restr
   if constexpr (TWK == 15) {
     float2 *t15 = static_cast<float2 *>(tab);
     for (int i = tid; i < 15 * L; i += nthr) t15[i] = __ldg(tw + (1 + i / L) * m_of(i % L));  // r m < N
+  } else if constexpr (TWK == 8) {
+    float4 *t8 = static_cast<float4 *>(tab);
+    for (int i = tid; i < 4 * L; i += nthr) {
+      const int j = i / L, m = m_of(i % L);
+      const float2 a = __ldg(tw + (2 * j + 1) * m), b = __ldg(tw + (2 * j + 2) * m);  // 8 m < N
+      t8[i] = make_float4(a.x, a.y, b.x, b.y);
+    }
   } else {
     float4 *t4 = static_cast<float4 *>(tab);
     for (int e = tid; e < L; e += nthr) {
@@ -202,6 +211,20 @@ __device__ __forceinline__ void fft_reg(float2 (&v)[16], float2 *sm, int t, cons
         const float2 *pt = static_cast<const float2 *>(ptab) + e;
 #pragma unroll
         for (int r = 1; r < 16; r++) v[r] = cmulw<SIGN>(v[r], pt[(r - 1) * L]);
+      } else if constexpr (TWK == 8) {
+        const float4 *pt = static_cast<const float4 *>(ptab) + e;
+        float2 w[8];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const float4 q = pt[j * L];
+          w[2 * j] = make_float2(q.x, q.y);
+          w[2 * j + 1] = make_float2(q.z, q.w);
+        }
+        // w[r - 1] = W^(r m), r = 1..8
+#pragma unroll
+        for (int r = 1; r <= 8; r++) v[r] = cmulw<SIGN>(v[r], w[r - 1]);
+#pragma unroll
+        for (int r = 9; r < 16; r++) v[r] = cmulw<SIGN>(v[r], cmul(w[7], w[r - 9]));
       } else {
         const float4 a = static_cast<const float4 *>(ptab)[e], b = static_cast<const float4 *>(ptab)[L + e];
         twiddle16<SIGN>(v, make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(b.x, b.y),
