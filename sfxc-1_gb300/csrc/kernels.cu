@@ -330,13 +330,16 @@ __device__ __forceinline__ uint2 tc_split(float2 f, float tc_scale) {
 
 // Channel i of one transform Z (natural order, padded): the real-FFT split
 // for output bin q = output_offset + i - temp_fft_offset (zero outside 0..N).
-template <int N>
+// HALF: the split's factor 1/2 applied here; else the transform's input
+// carried it (the shared window is scaled by 1/2, which is exact).
+template <int N, bool HALF>
 __device__ __forceinline__ float2 real_bin(const float2 *Z, const float2 *__restrict__ tw_rot, int q) {
   if (q < 0 || q > N) return make_float2(0.f, 0.f);
   const float2 zk = Z[padi(q & (N - 1))];
   const float2 zc = Z[padi((N - q) & (N - 1))];
-  const float er = 0.5f * (zk.x + zc.x), ei = 0.5f * (zk.y - zc.y);
-  const float orr = 0.5f * (zk.y + zc.y), oi = -0.5f * (zk.x - zc.x);
+  constexpr float h = HALF ? 0.5f : 1.0f;
+  const float er = h * (zk.x + zc.x), ei = h * (zk.y - zc.y);
+  const float orr = h * (zk.y + zc.y), oi = -h * (zk.x - zc.x);
   const float2 w = __ldg(tw_rot + q);  // q <= N < rot
   return make_float2(er + (orr * w.x - oi * w.y), ei + (orr * w.y + oi * w.x));
 }
@@ -344,12 +347,13 @@ __device__ __forceinline__ float2 real_bin(const float2 *Z, const float2 *__rest
 // Bins q and N - q of one transform together (0 <= q <= N/2): both read
 // Z[q] and Z[N - q], and with E, O the even and odd parts and w = tw_rot[q],
 // X[q] = E + O w and X[N - q] = conj(E - O w) (tw_rot[N - q] = -conj w).
-template <int N>
+template <int N, bool HALF>
 __device__ __forceinline__ void real_bin_pair(const float2 *Z, float2 w, int q, float2 &xq, float2 &xnq) {
   const float2 zk = Z[padi(q & (N - 1))];
   const float2 zc = Z[padi((N - q) & (N - 1))];
-  const float er = 0.5f * (zk.x + zc.x), ei = 0.5f * (zk.y - zc.y);
-  const float orr = 0.5f * (zk.y + zc.y), oi = -0.5f * (zk.x - zc.x);
+  constexpr float h = HALF ? 0.5f : 1.0f;
+  const float er = h * (zk.x + zc.x), ei = h * (zk.y - zc.y);
+  const float orr = h * (zk.y + zc.y), oi = -h * (zk.x - zc.x);
   const float owr = orr * w.x - oi * w.y, owi = orr * w.y + oi * w.x;
   xq = make_float2(er + owr, ei + owi);
   xnq = make_float2(er - owr, owi - ei);
@@ -394,7 +398,9 @@ __device__ __forceinline__ void window_apply(float2 (&v)[16], int t, int nper, f
 // `fast`: four (or NS) streams with no shift in consecutive slots from a
 // multiple of four, M == N.  Threads tid = 0..nthr-1 share the channels 0..M;
 // bins q and N - q come together, so the N/2 + 1 pairs spread evenly (bin N/2
-// goes to the last threads on its own).
+// goes to the last threads on its own).  SCALE: the window was not the
+// pre-scaled shared copy, so the split's 1/2 and the tensor-core scale are
+// applied here.
 template <int N, int NS, int OUT_TC, bool SCALE>
 __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *sinfo, int NV, bool fast, int row,
                                           int nrows_total, int M, int kpad, const float2 *__restrict__ tw_rot,
@@ -426,7 +432,7 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
 #pragma unroll
         for (int j = 0; j < W; j++) {
           float2 xq, xnq;
-          real_bin_pair<N>(Z + j * BUF, w, i, xq, xnq);
+          real_bin_pair<N, SCALE>(Z + j * BUF, w, i, xq, xnq);
           a[j] = tc_split<SCALE>(xq, tc_scale);
           b[j] = tc_split<SCALE>(xnq, tc_scale);
         }
@@ -436,7 +442,7 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
       if (tid >= nthr - W) {  // bin N/2, one stream per thread
         const int j = tid - (nthr - W);
         float2 xq, xnq;
-        real_bin_pair<N>(Z + j * BUF, __ldg(tw_rot + N / 2), N / 2, xq, xnq);
+        real_bin_pair<N, SCALE>(Z + j * BUF, __ldg(tw_rot + N / 2), N / 2, xq, xnq);
         dst[tc_index(row, kpad, N / 2, s0 + j)] = tc_split<SCALE>(xq, tc_scale);
       }
       return;
@@ -447,7 +453,7 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
       for (int j = 0; j < NS; j++)
         if (j < NV)
           dst[tc_index(row, kpad, i, sinfo[j].y)] =
-              tc_split<SCALE>(real_bin<N>(Z + j * BUF, tw_rot, sinfo[j].x + i), tc_scale);
+              tc_split<SCALE>(real_bin<N, SCALE>(Z + j * BUF, tw_rot, sinfo[j].x + i), tc_scale);
   } else {
 #pragma unroll 1
     for (int j = 0; j < NV; j++) {
@@ -456,17 +462,17 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
       if (shift == 0 && M == N) {
         for (int i = tid; i < N / 2; i += nthr) {
           float2 xq, xnq;
-          real_bin_pair<N>(Z + j * BUF, __ldg(tw_rot + i), i, xq, xnq);
+          real_bin_pair<N, SCALE>(Z + j * BUF, __ldg(tw_rot + i), i, xq, xnq);
           dst[i] = xq;
           dst[N - i] = xnq;
         }
         if (tid == nthr - 1 - j) {
           float2 xq, xnq;
-          real_bin_pair<N>(Z + j * BUF, __ldg(tw_rot + N / 2), N / 2, xq, xnq);
+          real_bin_pair<N, SCALE>(Z + j * BUF, __ldg(tw_rot + N / 2), N / 2, xq, xnq);
           dst[N / 2] = xq;
         }
       } else {
-        for (int i = tid; i <= M; i += nthr) dst[i] = real_bin<N>(Z + j * BUF, tw_rot, shift + i);
+        for (int i = tid; i <= M; i += nthr) dst[i] = real_bin<N, SCALE>(Z + j * BUF, tw_rot, shift + i);
       }
     }
   }
@@ -530,12 +536,13 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
                              ? make_int2(streams[st].output_offset - streams[st].temp_fft_offset, streams[st].slot)
                              : make_int2(0, -1);
   }
-  // a shared window carries the tensor-core layout's power-of-two scale
-  // (exact), so the output split needs no multiply
+  // a shared window carries the tensor-core layout's power-of-two scale and
+  // the real-FFT split's factor 1/2 (both exact), so the output split needs
+  // neither multiply
   const float *win = window;
   if constexpr (S::WSMEM) {
     float4 *wsm = reinterpret_cast<float4 *>(ptab + S::PTB / sizeof(float2));  // nper: a multiple of 4 (rot >= 512)
-    const float ws = OUT_TC ? tc_scale : 1.0f;
+    const float ws = (OUT_TC ? tc_scale : 1.0f) * 0.5f;
     for (int i = threadIdx.x; i < nper / 4; i += S::THREADS) {
       const float4 w = __ldg(reinterpret_cast<const float4 *>(window) + i);
       wsm[i] = make_float4(w.x * ws, w.y * ws, w.z * ws, w.w * ws);
