@@ -363,8 +363,19 @@ __device__ __forceinline__ void real_bin_pair(const float2 *Z, float2 w, int q, 
 // flight while the current row is written out: raw samples v[qq] = (x[2e],
 // x[2e+1]) of complex element e = t + qq T (zero from nper on, or when !ok),
 // then the window and, for a sideband flip, the negated odd samples.
-template <int T>
+// FULL: nper = 2N (every window but NONE), no per-element bounds.
+template <int T, bool FULL>
 __device__ __forceinline__ void window_raw(float2 (&v)[16], int t, bool ok, int nper, const float *ts) {
+  if constexpr (FULL) {
+    if (ok) {
+#pragma unroll
+      for (int qq = 0; qq < 16; qq++) v[qq] = *reinterpret_cast<const float2 *>(ts + 2 * (t + qq * T));
+    } else {
+#pragma unroll
+      for (int qq = 0; qq < 16; qq++) v[qq] = make_float2(0.f, 0.f);
+    }
+    return;
+  }
 #pragma unroll
   for (int qq = 0; qq < 16; qq++) {
     const int i = 2 * (t + qq * T);
@@ -377,8 +388,20 @@ __device__ __forceinline__ void window_raw(float2 (&v)[16], int t, bool ok, int 
   }
 }
 // The window is in shared memory (WSMEM) or read through the read-only cache.
-template <int T, bool WSMEM>
-__device__ __forceinline__ void window_apply(float2 (&v)[16], int t, int nper, float sgn, const float *window) {
+// FULL as for window_raw; FLIP: negate the odd samples.
+template <int T, bool WSMEM, bool FULL, bool FLIP>
+__device__ __forceinline__ void window_apply(float2 (&v)[16], int t, int nper, const float *window) {
+  if constexpr (FULL) {
+#pragma unroll
+    for (int qq = 0; qq < 16; qq++) {
+      const int i = 2 * (t + qq * T);
+      const float2 w = WSMEM ? *reinterpret_cast<const float2 *>(window + i)
+                             : __ldg(reinterpret_cast<const float2 *>(window + i));
+      v[qq] = make_float2(v[qq].x * w.x, FLIP ? -(v[qq].y * w.y) : v[qq].y * w.y);
+    }
+    return;
+  }
+  const float sgn = FLIP ? -1.0f : 1.0f;
 #pragma unroll
   for (int qq = 0; qq < 16; qq++) {
     const int i = 2 * (t + qq * T);
@@ -521,10 +544,20 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
   const int stream = sg * SPC + g % SPC;
   const bool sok = stream < nstreams;
   const StreamDev &s = streams[sok ? stream : 0];
-  const float sgn = s.flip ? -1.0f : 1.0f;
+  const bool flip = s.flip != 0;
+  // every window but NONE covers the whole transform input: no bounds per element
+  const bool full = nper == 2 * N;
   auto row_of = [&](int k) { return k * RPC + g / SPC; };
+  auto load_row = [&](float2(&v)[16], int k) {
+    const bool ok = sok && row_of(k) < nrows;
+    const float *src = s.ts + (int64_t)(row0 + row_of(k)) * N;
+    if (full)
+      window_raw<T, true>(v, t, ok, nper, src);
+    else
+      window_raw<T, false>(v, t, ok, nper, src);
+  };
   float2 v[16];
-  if (k0 < k1) window_raw<T>(v, t, sok && row_of(k0) < nrows, nper, s.ts + (int64_t)(row0 + row_of(k0)) * N);
+  if (k0 < k1) load_row(v, k0);
   // shared tables behind the FFT buffers: pass twiddles, then the window
   float2 *ptab = dsm + S::FFT_SMEM / sizeof(float2);
   fill_pass_table<LOGN, S::TWK>(ptab, tw_rot + 2 * N, threadIdx.x, S::THREADS);
@@ -556,7 +589,17 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
   for (int j = 0; j < SPC; j++) fast = fast && sinfo[j].x == 0 && sinfo[j].y == sinfo[0].y + j;
 #pragma unroll 1
   for (int k = k0; k < k1; k++) {
-    window_apply<T, S::WSMEM>(v, t, nper, sgn, win);
+    if (full) {
+      if (flip)
+        window_apply<T, S::WSMEM, true, true>(v, t, nper, win);
+      else
+        window_apply<T, S::WSMEM, true, false>(v, t, nper, win);
+    } else {
+      if (flip)
+        window_apply<T, S::WSMEM, false, true>(v, t, nper, win);
+      else
+        window_apply<T, S::WSMEM, false, false>(v, t, nper, win);
+    }
     // tw_rot holds exp(-2 pi i m / rot) for m < rot, followed by exp(-2 pi i m / N) for m < N.
     // Each group's transform synchronises only its own T threads (named
     // barrier 1 + g) when the groups are whole warps and few enough.
@@ -566,8 +609,7 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
     } else {
       fft_reg<-1, LOGN, true, S::TWK>(v, dsm + g * S::BUF, t, tw_rot + 2 * N, ptab, BlockSync());
     }
-    if (k + 1 < k1)  // hop = rot / 2
-      window_raw<T>(v, t, sok && row_of(k + 1) < nrows, nper, s.ts + (int64_t)(row0 + row_of(k + 1)) * N);
+    if (k + 1 < k1) load_row(v, k + 1);  // hop = rot / 2
 #pragma unroll 1
     for (int r = 0; r < RPC; r++) {
       const int row = k * RPC + r;
