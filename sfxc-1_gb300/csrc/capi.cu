@@ -638,7 +638,12 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     d.oversamp = (int)std::round(ss.sample_rate / (2 * (double)ss.bandwidth));
     d.frac_scale = -2.0 * M_PI / ss.sample_rate;
     d.int_phase_q = M_PI / (2 * d.oversamp);
+    d.frac_scale_f = (float)d.frac_scale;
+    d.int_phase_q_f = (float)d.int_phase_q;
+    d.half_bw_f = (float)(0.5 * ss.bandwidth);
+    d.rate_per_bin_f = (float)((double)ss.sample_rate / kNd);
     d.sideband = ss.sideband == 'L' ? -1 : 1;
+    d.fringe_mult = -d.sideband * 2.0 * M_PI;
     d.center_freq = ss.channel_freq + d.sideband * ss.bandwidth * 0.5 + ss.lo_offset;
     d.lo_offset = ss.lo_offset;
     const double dt = time_diff(start, c->p.experiment_start_ticks);

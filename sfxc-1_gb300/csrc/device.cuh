@@ -75,8 +75,13 @@ struct StreamDev {
   int32_t sample_rate, bandwidth, oversamp, sideband;  // sideband +1 / -1
   double center_freq, lo_offset, start_phase;
   // per-stream quotients of Delay_correction::fractional_bit_shift, divided
-  // once here: -2 pi / sample_rate and pi / (2 oversamp)
+  // once here: -2 pi / sample_rate and pi / (2 oversamp); the ramp terms
+  // built from them end in FP32 and are computed there: -2 pi / sample_rate,
+  // pi / (2 oversamp), bandwidth / 2 and sample_rate / 256 as floats
   double frac_scale, int_phase_q;
+  float frac_scale_f, int_phase_q_f, half_bw_f, rate_per_bin_f;
+  // -sideband * 2 pi (the fringe phase's turn-to-radian factor)
+  double fringe_mult;
   // windowed FFT stage; slot: the stream's index in the job (its place in
   // the spectra layouts), also when the launch covers a subset of streams
   int32_t rot, flip, output_offset, temp_fft_offset, slot;

@@ -246,20 +246,33 @@ __device__ __forceinline__ void block_params_one(const StreamDev &s, int bl, int
   const double ampl = s.amp_one ? 1.0 : spline_eval_at(s.spline, s.spline_n, 2, vc, ic);
   const double dis = __dmul_rn(delay_c, (double)s.sample_rate);
   const int integer_delay = (int)floor(__dadd_rn(dis, 0.5));
-  const double frac = dis - integer_delay;
-  const double tmp1 = frac * s.frac_scale;
-  const double tmp2 = (integer_delay & (4 * s.oversamp - 1)) * s.int_phase_q;
-  const double cterm = tmp2 - tmp1 * 0.5 * s.bandwidth;
-  const double lterm = tmp1 * ((double)s.sample_rate * (1.0 / kNd));
-  const double mult = -s.sideband * 2.0 * M_PI;
-  const double lo_phase = s.start_phase + s.lo_offset * ((double)(ct - s.start_ticks) * kInvTick);
-  double phi = s.center_freq * delay_0 + lo_phase + phase_0 * kInv2Pi;
+  // the fractional-delay ramp (phase at bin 0 and step per bin) is stored in
+  // FP32 and needs no more: |frac| <= 1/2, the terms stay within a few turns
+  const float frac = (float)(dis - integer_delay);
+  const float tmp1 = frac * s.frac_scale_f;
+  const float tmp2 = (float)(integer_delay & (4 * s.oversamp - 1)) * s.int_phase_q_f;
+  const float cterm = tmp2 - tmp1 * s.half_bw_f;
+  const float lterm = tmp1 * s.rate_per_bin_f;
+  // the fringe phase in FP64 (tens of millions of turns); a zero LO offset or
+  // phase model adds exact zeros, skipped
+  double phi = s.center_freq * delay_0, phi_end = s.center_freq * delay_1;
+  if (s.lo_offset != 0.0) {
+    const double lo_phase = s.start_phase + s.lo_offset * ((double)(ct - s.start_ticks) * kInvTick);
+    phi = phi + lo_phase;
+    phi_end = phi_end + lo_phase + s.fft_len_sec * s.lo_offset;
+  } else {
+    phi = phi + s.start_phase;
+    phi_end = phi_end + s.start_phase;
+  }
+  if (!s.phase_zero) {
+    phi = phi + phase_0 * kInv2Pi;
+    phi_end = phi_end + phase_1 * kInv2Pi;
+  }
   const double floor_phi = floor(phi);
-  phi = mult * (phi - floor_phi);
-  double phi_end = s.center_freq * delay_1 + lo_phase + s.fft_len_sec * s.lo_offset + phase_1 * kInv2Pi;
-  phi_end = mult * (phi_end - floor_phi);
+  phi = s.fringe_mult * (phi - floor_phi);
+  phi_end = s.fringe_mult * (phi_end - floor_phi);
   BlockPar bp;
-  bp.ph = make_float4((float)(cterm - 2.0 * M_PI * floor(cterm * kInv2Pi)), (float)lterm, (float)phi,
+  bp.ph = make_float4(cterm - 6.28318548f * floorf(cterm * 0.159154937f), lterm, (float)phi,
                       (float)((phi_end - phi) * (1.0 / kNd)));
   sincosf(16.0f * bp.ph.y, &bp.steps.y, &bp.steps.x);
   sincosf(16.0f * bp.ph.w, &bp.steps.w, &bp.steps.z);
