@@ -312,7 +312,7 @@ def roofline(args, per_kernel, total):
     # ncu measured for the tensor-core path's kernels on the one-subband,
     # 4096-channel case; a launch covers one sub-integration chunk of one
     # subband job, so the per-launch traffic scales with the samples it covers
-    measured = {"window_fft_ms": 11.87, "xstep_ms": 8.20, "unpack_fringe_ms": 4.26}
+    measured = {"window_fft_ms": 11.87, "xstep_ms": 8.18, "unpack_fringe_ms": 4.27}
     traffic = None
     if args.x == "tc" and M == 4096 and k in measured:
         launches = args.subbands * -(-args.integration_us // 125000)
