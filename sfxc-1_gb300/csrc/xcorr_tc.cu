@@ -44,7 +44,7 @@ namespace {
 
 constexpr int kChan = 2;        // channels per group (one TMEM buffer)
 constexpr int kRowsK = 64;      // FFT rows per K-tile
-constexpr int kStages = 4;   // measured as fast as 6 (129 KB of shared memory)
+constexpr int kStages = 4;   // 129 KB of shared memory; 3 stages measured 17 % slower, 6 stages 3 %
 constexpr int kThreads = 320;   // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr int kChanTile = kRowsK * 256;       // one channel's K-tile: 64 rows x 128 components x 2 B
 constexpr int kStageBytes = kChan * kChanTile;  // 32 KB per stage
