@@ -843,7 +843,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     const ticks_t tfft = (ticks_t)M * (ticks_t)std::lround(512000000.0 / c->p.sample_rate);
     const int sbs = c->p.sideband == 'L' ? -1 : 1;
     const double base_freq = (double)c->p.channel_freq, dfreq = c->p.sample_rate / (2. * M);
-    std::vector<double4> uv(ranges.size() * (size_t)(c->npc - 1) * nbl, make_double4(0, 0, 0, 0));
+    std::vector<UvShift> uv(ranges.size() * (size_t)(c->npc - 1) * nbl, UvShift{0, 0, 0, 0});
     for (size_t ch = 0; ch < ranges.size(); ch++) {
       const int prev = ranges[ch].first, cur = ranges[ch].second;
       const ticks_t tmid = start + time_mul(tfft, prev + (cur - prev) / 2.);
@@ -859,10 +859,10 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
           double phi = base_freq * (dd1 * (1 - r1) - dd2 * (1 - r2));
           phi = 2 * M_PI * sbs * (phi - std::floor(phi));
           const double delta = 2 * M_PI * dfreq * (dd1 * (1 - r1) - dd2 * (1 - r2));
-          uv[(ch * (c->npc - 1) + (pc - 1)) * nbl + b] = make_double4(phi, delta, amplitude, 0.0);
+          uv[(ch * (c->npc - 1) + (pc - 1)) * nbl + b] = UvShift{phi, delta, amplitude, 0.0};
         }
     }
-    upload(c->uvp, uv.data(), uv.size() * sizeof(double4), st);
+    upload(c->uvp, uv.data(), uv.size() * sizeof(UvShift), st);
   }
   CK(cudaEventRecord(c->ev[0], st));
   // The per-block parameters (block_params_kernel, FP64-pipe bound, few
@@ -925,7 +925,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     CK(cudaGetLastError());
     if (c->npc > 1) {  // the sub-integration into every phase centre
       launch_pc_dump(c->acc.as<float2>(), c->pcacc.as<float2>(),
-                     c->uvp.as<double4>() + ch * (size_t)(c->npc - 1) * nbl, N, nbl, kpad, K, c->npc, st);
+                     c->uvp.as<UvShift>() + ch * (size_t)(c->npc - 1) * nbl, N, nbl, kpad, K, c->npc, st);
       CK(cudaGetLastError());
       launches += 1;
     }

@@ -197,6 +197,12 @@ __device__ __forceinline__ int find_segment(const StreamDev &s, int o) {
   return lo;
 }
 
+// uvshift of one extra phase centre and cross baseline in one sub-integration:
+// phase at channel 0, phase step per channel (rad), amplitude.
+struct UvShift {
+  double phi, delta, amp, pad;
+};
+
 // Accumulator element written by the X kernels and read by normalisation.
 struct VisLayout {
   int32_t nbl, kpad;  // baselines, padded channel count

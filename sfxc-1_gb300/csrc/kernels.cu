@@ -387,17 +387,17 @@ __device__ __forceinline__ void window_raw(float2 (&v)[16], int t, bool ok, int 
 #pragma unroll
       for (int qq = 0; qq < 16; qq++) v[qq] = make_float2(0.f, 0.f);
     }
-    return;
-  }
+  } else {
 #pragma unroll
-  for (int qq = 0; qq < 16; qq++) {
-    const int i = 2 * (t + qq * T);
-    float2 x = make_float2(0.f, 0.f);
-    if (ok && i + 1 < nper)
-      x = *reinterpret_cast<const float2 *>(ts + i);
-    else if (ok && i < nper)
-      x.x = ts[i];
-    v[qq] = x;
+    for (int qq = 0; qq < 16; qq++) {
+      const int i = 2 * (t + qq * T);
+      float2 x = make_float2(0.f, 0.f);
+      if (ok && i + 1 < nper)
+        x = *reinterpret_cast<const float2 *>(ts + i);
+      else if (ok && i < nper)
+        x.x = ts[i];
+      v[qq] = x;
+    }
   }
 }
 // The window is in shared memory (WSMEM) or read through the read-only cache.
@@ -412,18 +412,18 @@ __device__ __forceinline__ void window_apply(float2 (&v)[16], int t, int nper, c
                              : __ldg(reinterpret_cast<const float2 *>(window + i));
       v[qq] = make_float2(v[qq].x * w.x, FLIP ? -(v[qq].y * w.y) : v[qq].y * w.y);
     }
-    return;
-  }
-  const float sgn = FLIP ? -1.0f : 1.0f;
+  } else {
+    const float sgn = FLIP ? -1.0f : 1.0f;
 #pragma unroll
-  for (int qq = 0; qq < 16; qq++) {
-    const int i = 2 * (t + qq * T);
-    if (i + 1 < nper) {
-      const float2 w = WSMEM ? *reinterpret_cast<const float2 *>(window + i)
-                             : __ldg(reinterpret_cast<const float2 *>(window + i));
-      v[qq] = make_float2(v[qq].x * w.x, sgn * (v[qq].y * w.y));
-    } else if (i < nper) {
-      v[qq] = make_float2(v[qq].x * (WSMEM ? window[i] : __ldg(window + i)), 0.f);
+    for (int qq = 0; qq < 16; qq++) {
+      const int i = 2 * (t + qq * T);
+      if (i + 1 < nper) {
+        const float2 w = WSMEM ? *reinterpret_cast<const float2 *>(window + i)
+                               : __ldg(reinterpret_cast<const float2 *>(window + i));
+        v[qq] = make_float2(v[qq].x * w.x, sgn * (v[qq].y * w.y));
+      } else if (i < nper) {
+        v[qq] = make_float2(v[qq].x * (WSMEM ? window[i] : __ldg(window + i)), 0.f);
+      }
     }
   }
 }
@@ -1043,7 +1043,7 @@ __global__ void phased_kernel(const float2 *__restrict__ spec, int nrows_total, 
 // a cross baseline of centre c >= 1 first gets the amplitude and the phase
 // phi + k delta of its residual delay (FP64 angle, FP32 product, as the
 // reference's FP64 recurrence and complex<float> arithmetic).
-__global__ void pc_dump_kernel(float2 *__restrict__ acc, float2 *__restrict__ pcacc, const double4 *__restrict__ uvp,
+__global__ void pc_dump_kernel(float2 *__restrict__ acc, float2 *__restrict__ pcacc, const UvShift *__restrict__ uvp,
                                int nstreams, int nbl, int kpad, int K, int npc) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
   if (k >= K) return;
@@ -1055,10 +1055,10 @@ __global__ void pc_dump_kernel(float2 *__restrict__ acc, float2 *__restrict__ pc
     if (b < nstreams) {
       p = make_float2(p.x + x.x, p.y + x.y);
     } else {
-      const double4 u = uvp[(size_t)(c - 1) * nbl + b];
+      const UvShift u = uvp[(size_t)(c - 1) * nbl + b];
       double sn, cs;
-      sincos(fma((double)k, u.y, u.x), &sn, &cs);
-      const float amp = (float)u.z, cf = (float)cs, sf = (float)sn;
+      sincos(fma((double)k, u.delta, u.phi), &sn, &cs);
+      const float amp = (float)u.amp, cf = (float)cs, sf = (float)sn;
       const float xr = amp * x.x, xi = amp * x.y;
       p = make_float2(p.x + (xr * cf - xi * sf), p.y + (xr * sf + xi * cf));
     }
@@ -1304,7 +1304,7 @@ void launch_phased(const float2 *spec, int nrows_total, int kpad, int nstreams, 
   phased_kernel<<<(K + 127) / 128, 128, 0, st>>>(spec, nrows_total, kpad, nstreams, r0, nrows, K, nsub, acc);
 }
 
-void launch_pc_dump(float2 *acc, float2 *pcacc, const double4 *uvp, int nstreams, int nbl, int kpad, int K, int npc,
+void launch_pc_dump(float2 *acc, float2 *pcacc, const UvShift *uvp, int nstreams, int nbl, int kpad, int K, int npc,
                     cudaStream_t st) {
   if (nbl > 0) pc_dump_kernel<<<dim3((K + 255) / 256, nbl), 256, 0, st>>>(acc, pcacc, uvp, nstreams, nbl, kpad, K, npc);
 }

@@ -40,7 +40,7 @@ void launch_normalize(const float2 *acc, int kpad, int M, int nstreams, int nbl,
 // rows kpad apart) added to every centre's accumulator pcacc[c][b][k], rotated
 // for c >= 1 on cross baselines (b >= nstreams) by uvp[(c - 1) nbl + b] =
 // {phase, phase step per channel, amplitude}, then cleared.
-void launch_pc_dump(float2 *acc, float2 *pcacc, const double4 *uvp, int nstreams, int nbl, int kpad, int K, int npc,
+void launch_pc_dump(float2 *acc, float2 *pcacc, const UvShift *uvp, int nstreams, int nbl, int kpad, int K, int npc,
                     cudaStream_t st);
 // Phased array: acc[(r0 + r) / nsub][k] += spec[i][r][k] over the chunk's rows
 // r < nrows and streams i < nstreams, in that order (FP32 spectra layout,
