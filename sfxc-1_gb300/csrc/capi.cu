@@ -899,7 +899,10 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     }
     CK(cudaEventRecord(c->evpool[ev + 2], st));
     if (ch + 1 < ranges.size()) {
-      // chunk ch + 1's records go to the other set, last read by chunk ch - 1's transforms
+      // chunk ch + 1's records go to the other set, last read by chunk ch - 1's
+      // transforms.  (Starting them once chunk ch's transforms are done, to
+      // fill the windowed FFT's tail, measured slower: their CTAs then hold
+      // SMs when the X-step's persistent CTAs are placed.)
       CK(cudaStreamWaitEvent(c->st2, c->evpool[ev + 2], 0));
       launch_block_params(dchunk + per_chunk, N, max_blocks, c->st2, kSideParamCtas);
       CK(cudaGetLastError());
