@@ -349,6 +349,29 @@ def write_protocol(blocks, slices, sample_rate, bits, integration_time_us):
     return [raw[offs[i]:offs[i + 1]] for i in range(len(slices))]
 
 
+def split_output(data, nchan):
+    """Output bytes of run_integration (Correlation_core::integration_write
+    layout) split into (header bytes, [complex64 visibilities of each baseline
+    header, nchan + 1 values]) in file order: per output an int32 file index,
+    the 16-byte timeslice header, 32 bytes per UVW entry, 24 per statistics
+    entry, then per baseline its 8-byte header and visibilities."""
+    hdr, vis, p = bytearray(), [], 0
+    data = bytes(data)
+    while p < len(data):
+        hdr += data[p:p + 20]
+        _, nbl, nuvw, nstat = np.frombuffer(data[p + 4:p + 20], dtype=np.int32)
+        p += 20
+        n = int(nuvw) * 32 + int(nstat) * 24
+        hdr += data[p:p + n]
+        p += n
+        for _ in range(int(nbl)):
+            hdr += data[p:p + 8]
+            p += 8
+            vis.append(np.frombuffer(data[p:p + (nchan + 1) * 8], dtype=np.complex64).copy())
+            p += (nchan + 1) * 8
+    return bytes(hdr), vis
+
+
 def thread_channel_blocks(blocks, n_channels):
     """The VDIF path with one channel per thread (Channel_extractor_tasklet_VDIF::
     do_task, sfxc/src/channel_extractor_tasklet_vdif.cc:25-49): no extraction,

@@ -5,6 +5,7 @@ bit.  No kernel runs here."""
 import os
 import re
 
+import numpy as np
 import pytest
 
 from golden_io import CASES, Golden
@@ -87,3 +88,16 @@ def test_reduction_parameters_are_checked(sfxc_lib):
         with pytest.raises(lib.SfxcError, match="number_channels"):
             node.set_parameters(j)
         node.close()
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_split_output(case):
+    """The package's reader of the output layout agrees with the fixtures' parser."""
+    from golden_io import parse_cor
+    from sfxc_gpu import correlator
+    g = Golden(case)
+    nchan = int(g.meta.get("number_channels") or g.meta["fft_size_correlation"])
+    h1, v1 = parse_cor(g.cor, nchan)
+    h2, v2 = correlator.split_output(g.cor, nchan)
+    assert h1 == h2 and len(v1) == len(v2)
+    assert all(np.array_equal(a, b) for a, b in zip(v1, v2))
