@@ -85,11 +85,31 @@ __device__ __forceinline__ void dft8(float2 *v) {
   v[3] = cadd(e3, o3);
   v[7] = csub(e3, o3);
 }
-// 16-point DFT as 4 x 4: x[n1 + 4 n2] -> X[k1 + 4 k2]
+// 16-point DFT as 4 x 4: x[n1 + 4 n2] -> X[k1 + 4 k2].  upper_zero: the
+// caller guarantees v[9..15] == 0, so the first 4-point stage drops the
+// additions of zeros (same results).
 template <int SIGN>
-__device__ __forceinline__ void dft16(float2 (&v)[16]) {
+__device__ __forceinline__ void dft16(float2 (&v)[16], bool upper_zero = false) {
+  if (upper_zero) {
+    {  // (v0, v4, v8, 0)
+      const float2 t0 = cadd(v[0], v[8]), t1 = csub(v[0], v[8]), t3 = rot90<SIGN>(v[4]);
+      v[8] = csub(t0, v[4]);
+      v[0] = cadd(t0, v[4]);
+      v[4] = cadd(t1, t3);
+      v[12] = csub(t1, t3);
+    }
 #pragma unroll
-  for (int n1 = 0; n1 < 4; n1++) dft4<SIGN>(v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]);
+    for (int n1 = 1; n1 < 4; n1++) {  // (v[n1], v[n1 + 4], 0, 0)
+      const float2 a = v[n1], b = v[n1 + 4], rb = rot90<SIGN>(b);
+      v[n1] = cadd(a, b);
+      v[n1 + 8] = csub(a, b);
+      v[n1 + 4] = cadd(a, rb);
+      v[n1 + 12] = csub(a, rb);
+    }
+  } else {
+#pragma unroll
+    for (int n1 = 0; n1 < 4; n1++) dft4<SIGN>(v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]);
+  }
   // v[n1 + 4 k1] = y[n1][k1]; twiddle W16^(n1 k1)
   v[5] = w16<SIGN, 1>(v[5]);
   v[9] = w16<SIGN, 2>(v[9]);
@@ -188,9 +208,10 @@ __device__ __forceinline__ void fill_pass_table(void *tab, const float2 *__restr
 // Out (TO_SMEM): X[k] at sm[padi(k)], visible after the final barrier.
 // Out (!TO_SMEM, LOGN % 4 == 0 only): v[r] = X[t + r T]; sm is free again
 // once every thread has returned (the caller syncs before reusing it).
+// upper_zero: v[9..15] == 0 on entry (the first pass skips those additions).
 template <int SIGN, int LOGN, bool TO_SMEM, int TWK, typename Sync>
 __device__ __forceinline__ void fft_reg(float2 (&v)[16], float2 *sm, int t, const float2 *__restrict__ tw,
-                                        const void *ptab, Sync sync) {
+                                        const void *ptab, Sync sync, bool upper_zero = false) {
   constexpr int N = 1 << LOGN, T = N / 16, NR16 = LOGN / 4, LAST = LOGN % 4;
   static_assert(NR16 >= 1, "at least 16 points");
   static_assert(TO_SMEM || LAST == 0, "register output needs a final radix-16 pass");
@@ -231,7 +252,7 @@ __device__ __forceinline__ void fft_reg(float2 (&v)[16], float2 *sm, int t, cons
                         make_float2(b.z, b.w));
       }
     }
-    dft16<SIGN>(v);
+    dft16<SIGN>(v, p == 0 && upper_zero);
     if (p == NR16 - 1 && LAST == 0 && !TO_SMEM) return;  // v[r] = X[t + r T]
     const int wbase = padi((t - (t & (Ns - 1))) * 16 + (t & (Ns - 1)));
 #pragma unroll

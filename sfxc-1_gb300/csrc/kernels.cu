@@ -111,7 +111,8 @@ __device__ __forceinline__ void fstep_pair(const StreamDev &s, int bl0, int t, f
       for (int r = 9; r < 16; r++) v[r] = make_float2(0.f, 0.f);
     }
     // v[r] = X[t + 16 r]; the transform's reads of sm are complete on return
-    fft_reg<-1, 8, false, 15>(v, sm, t, tw, ptab, WarpSync());
+    // (the inverse inputs are half spectra: v[9..15] == 0)
+    fft_reg<-1, 8, false, 15>(v, sm, t, tw, ptab, WarpSync(), h != 0);
     if (h == 0) {
       // split, halve DC/Nyquist, phase ramp; conj of block 0 into v, of block 1 into ext
 #pragma unroll
