@@ -191,7 +191,7 @@ def run_gpu(args):
             launches += t["launches"]
         return dev_ms, launches, out_bytes
 
-    # One host thread per job context (each context owns a CUDA stream), each
+    # One host thread per job context (each context owns its CUDA streams), each
     # correlating its job's integration `count` times back to back, as a
     # correlator node does with consecutive time slices: the host side of one
     # job (protocol copies, planning, output bytes) overlaps the kernels of
