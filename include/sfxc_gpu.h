@@ -338,7 +338,8 @@ typedef struct sfxc_gpu_phasecal sfxc_gpu_phasecal;
 sfxc_gpu_phasecal *sfxc_gpu_phasecal_create(sfxc_gpu_ctx *ctx, const sfxc_phasecal_params *params);
 /* Fold the next n_blocks channel blocks (stored back to back from `stream`,
  * described as for sfxc_gpu_write_protocol); finished integrations go to
- * sink(user, 2, message, bytes) in order before the call returns. */
+ * sink(user, 2, message, bytes) in order before the call returns.  After a
+ * failed call the fold state is undefined: destroy it and start again. */
 int sfxc_gpu_phasecal_push(sfxc_gpu_phasecal *pc, const uint8_t *stream, int32_t n_blocks,
                            const sfxc_channel_block *blocks, sfxc_output_sink sink, void *user);
 /* Frees the state; before or after ctx is destroyed. */
