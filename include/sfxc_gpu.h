@@ -345,6 +345,39 @@ int sfxc_gpu_phasecal_push(sfxc_gpu_phasecal *pc, const uint8_t *stream, int32_t
 /* Frees the state; before or after ctx is destroyed. */
 void sfxc_gpu_phasecal_destroy(sfxc_gpu_phasecal *pc);
 
+/* Output node (Output_node, sfxc/src/output_node.cc:68-214): the correlator
+ * output of consecutive time slices into the output files.  Each file starts
+ * with the global header (Output_header_global, sfxc/include/output_header.h:
+ * 70-97, 84 bytes, filled as Manager_node::send_global_header does,
+ * sfxc/src/manager_node.cc:670-703); slices are written in slice order from
+ * slice 0, whatever order they arrive in; a slice's bytes are n_bins equal
+ * parts (pulsar bins or phase centres), each an int32 file index followed by
+ * that output, and each output goes, without its index, to that file.  For
+ * this object the sink's `kind` is the file index. */
+typedef struct {
+  char experiment[32];
+  int32_t start_year, start_day;  /* day of year; both stored as int16 */
+  int32_t start_time;             /* seconds since midnight */
+  int32_t number_channels;
+  int32_t integration_time_us;
+  int32_t correlator_version;
+  int32_t polarisation_type;      /* 0 L, 1 R, 2 L+R, 3 L+R with crosses */
+  char correlator_branch[15];
+  int32_t job_nr, subjob_nr;
+} sfxc_output_global;
+typedef struct sfxc_gpu_output sfxc_gpu_output;
+/* Writes the global header to files 0 .. n_files - 1; NULL on bad arguments
+ * (message from sfxc_gpu_global_error). */
+sfxc_gpu_output *sfxc_gpu_output_create(const sfxc_output_global *global, int32_t n_files, sfxc_output_sink sink,
+                                        void *user);
+/* One slice's bytes (copied); written now if it is the next slice in order,
+ * with any later slices already held. */
+int sfxc_gpu_output_put_slice(sfxc_gpu_output *out, int64_t slice_nr, const uint8_t *bytes, size_t n,
+                              int32_t n_bins);
+/* SFXC_GPU_ESTATE while slices are held for a missing earlier one. */
+int sfxc_gpu_output_finish(sfxc_gpu_output *out);
+void sfxc_gpu_output_destroy(sfxc_gpu_output *out);
+
 #ifdef __cplusplus
 }
 #endif

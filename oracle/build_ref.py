@@ -148,6 +148,21 @@ def build(ref_root=None, force=False):
     return exe
 
 
+def build_output_header(ref_root=None):
+    """oracle/ref_output_header.cc against the reference's output_header.h:
+    prints the bytes of a filled Output_header_global.  None without the checkout."""
+    ref_root = ref_root or os.environ.get("REF_ROOT", "/root/reference")
+    inc = os.path.join(ref_root, "sfxc", "include")
+    if not os.path.isfile(os.path.join(inc, "output_header.h")):
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    exe = os.path.join(OUT, "ref_output_header")
+    src = os.path.join(HERE, "ref_output_header.cc")
+    if not os.path.exists(exe) or os.path.getmtime(exe) < os.path.getmtime(src):
+        _run(["g++", "-O2", "-std=gnu++03", "-I" + inc, src, "-o", exe])
+    return exe
+
+
 if __name__ == "__main__":
     path = build(sys.argv[1] if len(sys.argv) > 1 else None, force=True)
     print(path or "reference checkout absent; nothing built")

@@ -1511,6 +1511,101 @@ int sfxc_gpu_set_uvw(sfxc_gpu_ctx *c, const double *uvw, size_t n) {
   return SFXC_GPU_OK;
 }
 
+// ---- output node (Output_node::start / write_output / write_global_header,
+// sfxc/src/output_node.cc:68-214)
+struct sfxc_gpu_output {
+  int n_files = 0;
+  sfxc_output_sink sink = nullptr;
+  void *user = nullptr;
+  int64_t next_slice = 0;  // curr_slice
+  std::map<int64_t, std::pair<std::vector<uint8_t>, int>> held;  // slice -> (bytes, bins)
+};
+
+namespace {
+// write_output: each of the slice's n_bins equal parts is an int32 file index
+// and the bytes that go to that file
+void output_write_slice(sfxc_gpu_output *o, const std::vector<uint8_t> &b, int bins) {
+  const size_t per = b.size() / (size_t)bins;
+  for (int k = 0; k < bins; k++) {
+    int32_t file;
+    std::memcpy(&file, &b[k * per], 4);
+    if (file < 0 || file >= o->n_files) throw Error(SFXC_GPU_EINVAL, "output file index outside the files");
+    if (o->sink(o->user, file, &b[k * per + 4], per - 4) != 0)
+      throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
+  }
+}
+}  // namespace
+
+sfxc_gpu_output *sfxc_gpu_output_create(const sfxc_output_global *g, int32_t n_files, sfxc_output_sink sink,
+                                        void *user) {
+  try {
+    if (!g || !sink || n_files <= 0) throw Error(SFXC_GPU_EINVAL, "bad output parameters");
+    // Output_header_global, 84 bytes, little-endian, no padding
+    std::vector<uint8_t> h(84, 0);
+    auto put32 = [&](size_t off, int32_t v) { std::memcpy(&h[off], &v, 4); };
+    auto put16 = [&](size_t off, int32_t v) {
+      const int16_t x = (int16_t)v;
+      std::memcpy(&h[off], &x, 2);
+    };
+    put32(0, 84);
+    // strcpy into a zeroed field (the name up to its terminator, at most 31 bytes)
+    std::memcpy(&h[4], g->experiment, strnlen(g->experiment, 31));
+    put16(36, g->start_year);
+    put16(38, g->start_day);
+    put32(40, g->start_time);
+    put32(44, g->number_channels);
+    put32(48, g->integration_time_us);
+    put32(52, 1);  // OUTPUT_FORMAT_VERSION
+    put32(56, g->correlator_version);
+    h[60] = (uint8_t)(int8_t)g->polarisation_type;
+    // strncpy(15) with the last byte cleared
+    std::memcpy(&h[61], g->correlator_branch, strnlen(g->correlator_branch, 14));
+    put32(76, g->job_nr);
+    put32(80, g->subjob_nr);
+    std::unique_ptr<sfxc_gpu_output> o(new sfxc_gpu_output());
+    o->n_files = n_files;
+    o->sink = sink;
+    o->user = user;
+    for (int f = 0; f < n_files; f++)
+      if (sink(user, f, h.data(), h.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
+    return o.release();
+  } catch (const Error &e) {
+    g_error = e.msg;
+    return nullptr;
+  }
+}
+
+int sfxc_gpu_output_put_slice(sfxc_gpu_output *o, int64_t slice_nr, const uint8_t *bytes, size_t n, int32_t bins) {
+  if (!o) return SFXC_GPU_EINVAL;
+  try {
+    if ((n && !bytes) || bins <= 0 || n % (size_t)bins || n / (size_t)bins < 4)
+      throw Error(SFXC_GPU_EINVAL, "slice bytes must be n_bins equal parts of at least 4 bytes");
+    // set_weight_of_input_stream: a slice already written or already held is an error
+    if (slice_nr < o->next_slice || o->held.count(slice_nr)) throw Error(SFXC_GPU_EINVAL, "slice given twice");
+    o->held[slice_nr] = {std::vector<uint8_t>(bytes, bytes + n), bins};
+    for (auto it = o->held.begin(); it != o->held.end() && it->first == o->next_slice; it = o->held.begin()) {
+      output_write_slice(o, it->second.first, it->second.second);
+      o->held.erase(it);
+      o->next_slice++;
+    }
+    return SFXC_GPU_OK;
+  } catch (const Error &e) {
+    g_error = e.msg;
+    return e.code;
+  }
+}
+
+int sfxc_gpu_output_finish(sfxc_gpu_output *o) {
+  if (!o) return SFXC_GPU_EINVAL;
+  if (!o->held.empty()) {
+    g_error = "slices held for a missing slice " + std::to_string(o->next_slice);
+    return SFXC_GPU_ESTATE;
+  }
+  return SFXC_GPU_OK;
+}
+
+void sfxc_gpu_output_destroy(sfxc_gpu_output *o) { delete o; }
+
 int sfxc_gpu_last_timings(const sfxc_gpu_ctx *c, float *ms6) {
   float *ms5 = ms6;
   if (!c || !ms5) return SFXC_GPU_EINVAL;

@@ -349,6 +349,54 @@ def write_protocol(blocks, slices, sample_rate, bits, integration_time_us):
     return [raw[offs[i]:offs[i + 1]] for i in range(len(slices))]
 
 
+class OutputFiles:
+    """The output node (Output_node, sfxc/src/output_node.cc:68-214) into
+    in-memory files: `files[f]` holds file f's bytes, starting with the global
+    header.  global_fields: experiment, start_year, start_day, start_time,
+    number_channels, integration_time_us, correlator_version,
+    polarisation_type, correlator_branch, job_nr, subjob_nr.  Host only."""
+
+    def __init__(self, n_files, **global_fields):
+        self._lib = L.load()
+        g = L.OutputGlobal()
+        sizes = {"experiment": 32, "correlator_branch": 15}
+        for k, v in global_fields.items():
+            setattr(g, k, v.encode()[:sizes[k]] if isinstance(v, str) else v)
+        self.files = [bytearray() for _ in range(n_files)]
+
+        def sink(user, kind, data, n):
+            self.files[kind] += C.string_at(data, n)
+            return 0
+
+        self._sink = L.SINK(sink)  # kept alive with the object
+        self._h = self._lib.sfxc_gpu_output_create(C.byref(g), n_files, self._sink, None)
+        if not self._h:
+            raise L.SfxcError(L.EINVAL, self._lib.sfxc_gpu_global_error().decode())
+
+    def put_slice(self, slice_nr, data, n_bins=1):
+        buf = _bytes_ptr(bytes(data))
+        rc = self._lib.sfxc_gpu_output_put_slice(self._h, slice_nr, buf, len(data), n_bins)
+        if rc < 0:
+            raise L.SfxcError(rc, self._lib.sfxc_gpu_global_error().decode())
+
+    def finish(self):
+        rc = self._lib.sfxc_gpu_output_finish(self._h)
+        if rc < 0:
+            raise L.SfxcError(rc, self._lib.sfxc_gpu_global_error().decode())
+        return [bytes(f) for f in self.files]
+
+    def close(self):
+        if self._h:
+            self._lib.sfxc_gpu_output_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def split_output(data, nchan):
     """Output bytes of run_integration (Correlation_core::integration_write
     layout) split into (header bytes, [complex64 visibilities of each baseline

@@ -20,6 +20,7 @@ EXPORTS = [
     "sfxc_gpu_write_protocol", "sfxc_gpu_extract_channels", "sfxc_gpu_copy_spectra_noalloc",
     "sfxc_gpu_reader_create", "sfxc_gpu_reader_next", "sfxc_gpu_reader_destroy", "sfxc_gpu_extract_block",
     "sfxc_gpu_phasecal_create", "sfxc_gpu_phasecal_push", "sfxc_gpu_phasecal_destroy", "sfxc_gpu_set_uvw",
+    "sfxc_gpu_output_create", "sfxc_gpu_output_put_slice", "sfxc_gpu_output_finish", "sfxc_gpu_output_destroy",
 ]
 FORMAT_VDIF, FORMAT_MARK5B = 0, 1
 
@@ -91,6 +92,13 @@ class PhasecalParams(C.Structure):
                 ("polarisation", C.c_int32)]
 
 
+class OutputGlobal(C.Structure):
+    _fields_ = [("experiment", C.c_char * 32), ("start_year", C.c_int32), ("start_day", C.c_int32),
+                ("start_time", C.c_int32), ("number_channels", C.c_int32), ("integration_time_us", C.c_int32),
+                ("correlator_version", C.c_int32), ("polarisation_type", C.c_int32),
+                ("correlator_branch", C.c_char * 15), ("job_nr", C.c_int32), ("subjob_nr", C.c_int32)]
+
+
 SINK = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t)
 
 _lib = None
@@ -139,6 +147,11 @@ def load(path=None):
     lib.sfxc_gpu_phasecal_push.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(ChannelBlock), SINK,
                                            C.c_void_p]
     lib.sfxc_gpu_phasecal_destroy.argtypes = [C.c_void_p]
+    lib.sfxc_gpu_output_create.restype = C.c_void_p
+    lib.sfxc_gpu_output_create.argtypes = [C.POINTER(OutputGlobal), C.c_int32, SINK, C.c_void_p]
+    lib.sfxc_gpu_output_put_slice.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_size_t, C.c_int32]
+    lib.sfxc_gpu_output_finish.argtypes = [C.c_void_p]
+    lib.sfxc_gpu_output_destroy.argtypes = [C.c_void_p]
     _lib = lib
     return lib
 

@@ -10,6 +10,7 @@ corrected spectra, the correlator output bytes, statistics and tsys records.
 """
 import hashlib
 import os
+import subprocess
 import sys
 
 import numpy as np
@@ -224,7 +225,36 @@ def make_phasecal():
         json.dump(out, f, indent=1, sort_keys=True)
 
 
+OUTPUT_HEADER_CASES = [
+    dict(experiment="N24L1", start_year=2024, start_day=123, start_time=43200, number_channels=4096,
+         integration_time_us=2000000, correlator_version=2048, polarisation_type=3, correlator_branch="trunk",
+         job_nr=17, subjob_nr=2),
+    dict(experiment="EXPERIMENT_NAME_OF_31_CHARACTERS", start_year=2026, start_day=366, start_time=86399,
+         number_channels=64, integration_time_us=125000, correlator_version=0, polarisation_type=0,
+         correlator_branch="a-branch-longer-than-15", job_nr=0, subjob_nr=0),
+]
+
+
+def make_output_header():
+    """Output_header_global bytes from the reference's own struct
+    (oracle/ref_output_header.cc) for OUTPUT_HEADER_CASES."""
+    import json
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build_ref
+    exe = build_ref.build_output_header()
+    out = []
+    for c in OUTPUT_HEADER_CASES:
+        args = [c["experiment"][:31], c["start_year"], c["start_day"], c["start_time"], c["number_channels"],
+                c["integration_time_us"], c["correlator_version"], c["polarisation_type"], c["correlator_branch"],
+                c["job_nr"], c["subjob_nr"]]
+        r = subprocess.run([exe] + [str(a) for a in args], capture_output=True, text=True, check=True)
+        out.append(dict(c, experiment=c["experiment"][:31], header_hex=r.stdout.strip()))
+    with open(os.path.join(HERE, "output_header.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
 if __name__ == "__main__":
+    make_output_header()
     make_phasecal()
     make_formats()
     make_extract()
