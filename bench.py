@@ -25,7 +25,6 @@ bounded sample of the same workload.
 """
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys

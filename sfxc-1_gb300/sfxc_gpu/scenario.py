@@ -14,7 +14,6 @@ node (oracle/jobs.py), the C restatement or this library.
 """
 from __future__ import annotations
 
-import math
 from dataclasses import dataclass, field
 
 import numpy as np

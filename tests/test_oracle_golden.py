@@ -4,8 +4,6 @@ samples bit-exact; statistics, tsys records and output headers byte-exact;
 visibilities within 1e-6 relative L2 (FFT rounding only)."""
 import hashlib
 import os
-import subprocess
-import tempfile
 
 import numpy as np
 import pytest
