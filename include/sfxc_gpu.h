@@ -53,7 +53,11 @@ extern "C" {
 
 /* X-step arithmetic */
 #define SFXC_GPU_X_FP32 0      /* FP32 spectra, FP32 CUDA-core multiply-accumulate */
-#define SFXC_GPU_X_TC_HILO 1   /* FP16 hi+lo spectra, tensor-core products, FP32 accumulation */
+#define SFXC_GPU_X_TC_HILO 1   /* FP16 hi+lo spectra, tensor-core products, FP32 accumulation;
+                                  pulsar binning too; the phased array (sums of spectra, no
+                                  products) keeps FP32 spectra in either mode */
+/* Stream limits per job: FP32 up to 128 streams, tensor-core up to 64;
+ * sfxc_gpu_set_parameters returns SFXC_GPU_EINVAL beyond them. */
 
 typedef struct sfxc_gpu_ctx sfxc_gpu_ctx;
 
@@ -192,23 +196,30 @@ int sfxc_gpu_run_integration(sfxc_gpu_ctx *ctx, sfxc_output_sink sink, void *use
  * fft_size_correlation + 1 complex values, the output of Delay_correction). */
 int sfxc_gpu_copy_unpacked(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
 int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
+/* Pulsar bin of every FFT row and channel of the last integration (the bins
+ * of Correlation_core_pulsar::dedisperse_buffer, sfxc/src/correlation_core_pulsar.cc:
+ * 210-238: 0 off-pulse, 1..nbins on-pulse): nffts x (fft_size_correlation + 1)
+ * int32, row-major; returns the count.  SFXC_GPU_ESTATE without binning. */
+int sfxc_gpu_copy_pulsar_bins(sfxc_gpu_ctx *ctx, int32_t *out, size_t n);
 /* sfxc_gpu_copy_spectra without any allocation.  This call has no
  * counterpart in the reference; it exists for callers that cannot allocate
- * device memory when they inspect a stream: code running while a CUDA graph
- * is captured (cudaMalloc/cudaFree cannot be captured), real-time loops that
- * cannot wait on the allocator, and hosts that carve up GPU memory once at
- * start-up.  Its scratch -- the fringe-stopped samples, the per-block delay
+ * device memory when they inspect a stream: real-time correlator loops that
+ * cannot wait on the allocator (cudaMalloc and cudaFree may synchronise the
+ * whole device, stalling every other job's kernels), and hosts that hand out
+ * the GPU's memory once at start-up under a fixed budget shared with other
+ * processes.  Its scratch -- the fringe-stopped samples, the per-block delay
  * parameters, the stream descriptor and the spectra before the copy out --
  * lives in one static device array of 16.4 MiB that every GPU loading the
  * library holds until the process exits.  Limits: at most 8192 blocks of
  * fft_size_delaycor samples (2,097,152 samples) per stream and integration,
  * and at most 2^20 values of nffts x (fft_size_correlation + 4); larger
  * requests return SFXC_GPU_EINVAL and touch nothing.  The first call on a
- * device resolves the array's device address (cudaGetSymbolAddress) and
- * should come before any stream capture.  All calls share the array and it
- * keeps the last call's contents (each call writes every element it reads);
- * calls that overlap on the GPU -- from different contexts or threads --
- * race on it.  Arguments and result as sfxc_gpu_copy_spectra. */
+ * device resolves the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  The call runs on the context's
+ * own stream and waits for it.  All calls share the array and it keeps the
+ * last call's contents (each call writes every element it reads); calls that
+ * overlap on the GPU -- from different contexts or threads -- race on it.
+ * Arguments and result as sfxc_gpu_copy_spectra. */
 int sfxc_gpu_copy_spectra_noalloc(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
 /* Device time (ms) of the last integration, CUDA events on the context's
  * stream: [0] unpack and fringe stopping, with any wait for the per-block
@@ -377,6 +388,15 @@ int sfxc_gpu_output_put_slice(sfxc_gpu_output *out, int64_t slice_nr, const uint
 /* SFXC_GPU_ESTATE while slices are held for a missing earlier one. */
 int sfxc_gpu_output_finish(sfxc_gpu_output *out);
 void sfxc_gpu_output_destroy(sfxc_gpu_output *out);
+
+/* Compute peaks of `device` for the rooflines (no counterpart in the
+ * reference: a measurement aid).  Times one short kernel of independent FP32
+ * fused multiply-adds on the CUDA cores and one of FP16 tensor-core MMAs with
+ * FP32 accumulation (128 x 256 x 16, operands in shared memory), each the best
+ * of three CUDA-event timings after a warm-up; changes no device setting.
+ * out4: [0] FP32 TFLOP/s, [1] FP16 tensor TFLOP/s, [2] and [3] their kernel
+ * times in ms. */
+int sfxc_gpu_measure_peaks(int32_t device, double *out4);
 
 #ifdef __cplusplus
 }

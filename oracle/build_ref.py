@@ -14,8 +14,9 @@ Flags follow the reference (sfxc/configure.ac:31,98-101): -O2 -ffast-math
 portable (sfxc/include/boost/detail/sp_counted_base.hpp:26-60).
 
 Usage:  python oracle/build_ref.py [reference_root]
-The reference root defaults to the REF_ROOT environment variable, else
-/root/reference.  Returns without building when the checkout is absent.
+The reference root defaults to the REF_ROOT environment variable, else a
+checkout named `reference` beside the repository's own directory.  Returns
+without building when the checkout is absent.
 """
 import os
 import shutil
@@ -26,6 +27,11 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+
+
+def default_root():
+    """REF_ROOT, else the `reference` checkout beside the repository."""
+    return os.environ.get("REF_ROOT") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 SHIM = os.path.join(HERE, "ref_shim")
 
 REF_SOURCES = [
@@ -84,7 +90,7 @@ def harness_path():
 
 
 def build(ref_root=None, force=False):
-    ref_root = ref_root or os.environ.get("REF_ROOT", "/root/reference")
+    ref_root = ref_root or default_root()
     sfxc = os.path.join(ref_root, "sfxc")
     if not os.path.isdir(sfxc):
         return None
@@ -151,7 +157,7 @@ def build(ref_root=None, force=False):
 def build_output_header(ref_root=None):
     """oracle/ref_output_header.cc against the reference's output_header.h:
     prints the bytes of a filled Output_header_global.  None without the checkout."""
-    ref_root = ref_root or os.environ.get("REF_ROOT", "/root/reference")
+    ref_root = ref_root or default_root()
     inc = os.path.join(ref_root, "sfxc", "include")
     if not os.path.isfile(os.path.join(inc, "output_header.h")):
         return None

@@ -156,13 +156,14 @@ def reader(recording, fmt, *, ref_ticks, offset_ticks=0, track_bit_rate, frame_s
         return blocks
 
 
-def correlate(job, dump=False, impl="reference", precision=32):
+def correlate(job, dump=False, impl="reference", precision=32, dump_bins=False):
     """Run Bit2float_worker -> Delay_correction -> Correlation_core(_pulsar).
 
     job: dict with keys of the harness 'correlate' mode (see ref_harness.cc);
     'del_bytes' (list per station), 'protocols' (list per stream of a list of
     per-integration byte strings).  Returns dict with cor bytes, stats lines,
-    tsys bytes and (dump=True) per-integration unpacked/rows arrays.
+    tsys bytes and (dump=True) per-integration unpacked/rows arrays;
+    dump_bins=True (restatement): only the pulsar bin table, res["bins"].
     """
     with tempfile.TemporaryDirectory() as d:
         lines = []
@@ -209,6 +210,8 @@ def correlate(job, dump=False, impl="reference", precision=32):
                 lines.append(("polyco",) + tuple(pc))
         if dump:
             lines.append(("dump", 1))
+        if dump_bins:
+            lines.append(("dump_bins", 1))
         if precision != 32:
             lines.append(("precision", precision))
         outdir = os.path.join(d, "out")
@@ -220,6 +223,12 @@ def correlate(job, dump=False, impl="reference", precision=32):
         p64 = os.path.join(outdir, "out64.bin")
         if os.path.exists(p64):
             res["vis64"] = np.fromfile(p64, dtype=np.complex128)
+        bp = os.path.join(outdir, "bins_i0.i32")
+        if dump_bins and "pulsar" in job and os.path.exists(bp):
+            K = int(job["fft_size_correlation"]) + 1
+            res["bins"] = np.concatenate([
+                np.fromfile(os.path.join(outdir, "bins_i%d.i32" % it), dtype=np.int32).reshape(-1, K)
+                for it in range(int(job["n_integrations"]))])
         if dump:
             un, rows = {}, {}
             for it in range(int(job["n_integrations"])):

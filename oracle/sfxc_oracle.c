@@ -721,6 +721,7 @@ typedef struct {
   int npolyco;
   double *polyco; /* per polyco: tmid DM ref_phase ref_freq obs_freq ncoef coef... (packed, stride 32) */
   int dump;
+  int dump_bins; /* the pulsar bin table only */
   /* spectral reduction (number_channels < fft_size_correlation): the
      Mask_parameters of the ctrl file -- a mask over the M+1 channels, a lag
      window over 2 number_channels lags, and the per-channel normalisation;
@@ -1838,6 +1839,8 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
   j.n_integrations = (int)kv_ll(k, "n_integrations");
   kv_t *de = kv_get(k, "dump", 0);
   j.dump = de && atoi(de->v[0]);
+  kv_t *db = kv_get(k, "dump_bins", 0);
+  j.dump_bins = db && atoi(db->v[0]);
   if (j.number_channels < 2 || j.number_channels > j.M || (j.number_channels & (j.number_channels - 1)))
     die("number_channels must be a power of two no larger than the FFT size");
   kv_t *ph = kv_get(k, "phased_array", 0);
@@ -2111,7 +2114,7 @@ static int mode_correlate(const kvs_t *k, const char *outdir) {
       double *acc = xmalloc((size_t)nbins * nbl * K * 2 * sizeof(double));
       int *bins = xmalloc(K * sizeof(int));
       FILE *binf = NULL;
-      if (j.dump) {
+      if (j.dump || j.dump_bins) {
         snprintf(path, sizeof(path), "%s/bins_i%d.i32", outdir, it);
         binf = fopen(path, "wb");
       }

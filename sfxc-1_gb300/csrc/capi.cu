@@ -167,6 +167,8 @@ struct sfxc_gpu_ctx {
   // device
   DevBuf streamdev, tw256, ts, spec, acc, out, norms, flagfac, blmap, tiles, blpairs, items, bins,
       offsets, derr;
+  DevBuf rowlist, segs;  // pulsar binning on the tensor cores: rows of each channel sorted by bin, and the runs
+  int bins_rows = 0;     // rows of the last integration's bin table (pulsar)
   DevBuf xin, xtracks, xout;  // channel extraction
   // per windowed-FFT length (streams of different sample rates): window and
   // twiddle tables, and the stream descriptors grouped by length
@@ -449,9 +451,10 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
       }
     }
   jt.ntiles = (int)jt.tiles.size() / 2;
-  if (xcorr_tpw(jt.ntiles) < 0) throw Error(SFXC_GPU_EINVAL, "too many streams for the X-step tiling (max 48 tiles)");
-  if (c->x_mode == SFXC_GPU_X_TC_HILO && N > kTcSlots)
-    throw Error(SFXC_GPU_EINVAL, "the tensor-core X-step takes at most 32 streams per job");
+  if (xcorr_f32_plan(jt.ntiles, jt.npad).tpw <= 0)
+    throw Error(SFXC_GPU_EINVAL, "the FP32 X-step takes at most 128 streams per job");
+  if (c->x_mode == SFXC_GPU_X_TC_HILO && N > kTcSlotsWide)
+    throw Error(SFXC_GPU_EINVAL, "the tensor-core X-step takes at most 64 streams per job");
   upload(c->blmap, jt.blmap.data(), jt.blmap.size() * 4, c->st);
   upload(c->tiles, jt.tiles.data(), jt.tiles.size() * 4, c->st);
   upload(c->blpairs, jt.blpairs.data(), jt.blpairs.size() * 4, c->st);
@@ -734,14 +737,18 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   for (int i = 0; i < N; i++)  // each stream's own hop: streams at other rates need more or fewer blocks
     max_blocks = std::max(max_blocks, chunked ? (max_rows + 2) * c->sc[i].hop / kNd : c->sc[i].n_blocks);
   c->ts.ensure((size_t)N * max_blocks * kNd * sizeof(float));
-  // tensor-core X-step for normal correlation of up to 32 inputs; the spectra
-  // are scaled by a power of two before the FP16 hi/lo split so that typical
-  // magnitudes sit near 1 (|X| ~ sqrt(2M * 0.375 * E[x^2]) for a Hann window)
-  const bool tc_x = c->x_mode == SFXC_GPU_X_TC_HILO && !pulsar && !c->phased;
+  // tensor-core X-step (normal correlation and pulsar binning; the phased
+  // array sums spectra and has no products); the spectra are scaled by a
+  // power of two before the FP16 hi/lo split so that typical magnitudes sit
+  // near 1 (|X| ~ sqrt(2M * 0.375 * E[x^2]) for a Hann window)
+  const bool tc_x = c->x_mode == SFXC_GPU_X_TC_HILO && !c->phased;
+  const int tc_slots = tc_x ? (N <= kTcSlots ? kTcSlots : kTcSlotsWide) : 0;
+  // up to 32 streams without binning: the TMA-fed kernel; else the row-gathered one
+  const bool tc_tma = tc_x && !pulsar && tc_slots == kTcSlots;
   const float tc_scale = std::ldexp(1.0f, -(int)std::lround(0.5 * std::log2(2.0 * M * 10.0)));
-  // FP32 spectra: [stream][row][kpad]; TC spectra: [row][kpad][32 stream slots], 8 bytes each
-  // the tensor-core layout reads rows in groups of 8 (rows past a chunk's end cleared before its X-step)
-  c->spec.ensure((size_t)(tc_x ? kTcSlots : N) * (tc_x ? (max_rows + 7) / 8 * 8 : max_rows) * kpad * sizeof(float2));
+  // FP32 spectra: [stream][row][kpad]; TC spectra: [row][kpad][S stream slots], 8 bytes each
+  // the TMA-fed kernel reads rows in groups of 8 (rows past a chunk's end cleared before its X-step)
+  c->spec.ensure((size_t)(tc_x ? tc_slots : N) * (tc_x ? (max_rows + 7) / 8 * 8 : max_rows) * kpad * sizeof(float2));
   c->derr.ensure(sizeof(int));
   CK(cudaMemsetAsync(c->derr.p, 0, sizeof(int), st));
   // two sets of per-block records: chunk ch uses set ch & 1, so the next
@@ -793,6 +800,10 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     }
     upload(c->offsets, off.data(), off.size() * 8, st);
     c->bins.ensure((size_t)max_rows * K * sizeof(int16_t));
+    if (tc_x) {  // per channel the rows sorted by bin (runs padded to 16 rows), and the runs
+      c->rowlist.ensure((size_t)K * (max_rows + 16 * c->nbins) * sizeof(int));
+      c->segs.ensure((size_t)K * c->nbins * sizeof(int2));
+    }
   }
   // four events per chunk on the main stream and one on the second (+2 for
   // normalisation), recorded without host syncs
@@ -894,7 +905,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       const int nper = c->p.window == WINDOW_NONE ? rot / 2 : rot;
       const sfxc_gpu_ctx::RotTables &t = c->rot_tables.at(rot);
       launch_window_fft(dchunk + N + first, count, 0, nrows, max_rows, t.window.as<float>(), t.twrot.as<float2>(), rot,
-                        nper, M, kpad, c->spec.p, tc_x, tc_scale, st);
+                        nper, M, kpad, c->spec.p, tc_slots, tc_scale, st);
       CK(cudaGetLastError());
     }
     CK(cudaEventRecord(c->evpool[ev + 2], st));
@@ -911,19 +922,39 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     if (c->phased) {
       launch_phased(c->spec.as<float2>(), max_rows, kpad, N, ranges[ch].first, nrows, K, c->nsub, c->acc.as<float2>(),
                     st);
-    } else if (tc_x) {
+    } else if (pulsar) {
+      // the bin of every (row, channel), then the binned X-step: tensor cores
+      // over each channel's rows sorted by bin, or CUDA cores in row order
+      launch_pulsar_bins(nrows, K, psr_start_phase, psr_rate, fft_duration, c->offsets.as<double>(), c->p.gate_start,
+                         c->p.gate_stop, c->nbins, c->bins.as<int16_t>(), st);
+      CK(cudaGetLastError());
+      c->bins_rows = nrows;  // one chunk: the whole integration
+      if (tc_x) {
+        const int list_len = max_rows + 16 * c->nbins;
+        launch_pulsar_sort(c->bins.as<int16_t>(), nrows, K, c->nbins, list_len, c->rowlist.as<int>(),
+                           c->segs.as<int2>(), st);
+        CK(cudaGetLastError());
+        CK(launch_xcorr_tc_gather(c->spec.p, tc_slots, nrows, kpad, K, N, c->blmap.as<int>(), c->jt.npad, nbl, c->nbins,
+                                  c->rowlist.as<int>(), list_len, c->segs.as<int2>(), 1.0f / (tc_scale * tc_scale),
+                                  c->acc.as<float2>(), c->derr.as<int>(), st));
+        launches += 1;
+      } else {
+        launch_xcorr_f32(c->spec.as<float2>(), max_rows, kpad, N, c->jt.npad, 0, nrows, K, c->tiles.as<int>(),
+                         c->jt.ntiles, c->blmap.as<int>(), nbl, c->bins.as<int16_t>(), nrows, c->acc.as<float2>(), st);
+      }
+    } else if (tc_tma) {
       if (nrows % 8)
         CK(cudaMemsetAsync(static_cast<char *>(c->spec.p) + (size_t)nrows * kpad * kTcSlots * sizeof(float2), 0,
                            (size_t)(8 - nrows % 8) * kpad * kTcSlots * sizeof(float2), st));
       CK(launch_xcorr_tc(c->spec.p, nrows, kpad, K, c->blmap.as<int>(), c->jt.npad, 1.0f / (tc_scale * tc_scale),
                          c->acc.as<float2>(), c->derr.as<int>(), st));
-    } else if (pulsar) {
-      launch_pulsar(c->spec.as<float2>(), max_rows, kpad, N, c->jt.npad, nrows, K, c->tiles.as<int>(), c->jt.ntiles,
-                    c->blmap.as<int>(), nbl, psr_start_phase, psr_rate, fft_duration, c->offsets.as<double>(),
-                    c->p.gate_start, c->p.gate_stop, c->nbins, c->bins.as<int16_t>(), c->acc.as<float2>(), st);
+    } else if (tc_x) {  // 33 to 64 streams: the row-gathered kernel over rows in order
+      CK(launch_xcorr_tc_gather(c->spec.p, tc_slots, nrows, kpad, K, N, c->blmap.as<int>(), c->jt.npad, nbl, 1, nullptr,
+                                0, nullptr, 1.0f / (tc_scale * tc_scale), c->acc.as<float2>(), c->derr.as<int>(),
+                                st));
     } else {
       launch_xcorr_f32(c->spec.as<float2>(), max_rows, kpad, N, c->jt.npad, 0, nrows, K, c->tiles.as<int>(),
-                       c->jt.ntiles, c->blmap.as<int>(), c->acc.as<float2>(), st);
+                       c->jt.ntiles, c->blmap.as<int>(), nbl, nullptr, 0, c->acc.as<float2>(), st);
     }
     CK(cudaGetLastError());
     if (c->npc > 1) {  // the sub-integration into every phase centre
@@ -1173,6 +1204,24 @@ int sfxc_gpu_copy_unpacked(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n
   }
 }
 
+int sfxc_gpu_copy_pulsar_bins(sfxc_gpu_ctx *c, int32_t *out, size_t n) {
+  if (!c || !c->have_job) return SFXC_GPU_ESTATE;
+  try {
+    if (c->nbins <= 1 || c->bins_rows <= 0) throw Error(SFXC_GPU_ESTATE, "no pulsar bins: binning off or no integration yet");
+    const size_t rows = (size_t)c->bins_rows, K = (size_t)c->K;
+    if (!out || n < rows * K) throw Error(SFXC_GPU_EINVAL, "output buffer too small");
+    CK(cudaSetDevice(c->device));
+    std::vector<int16_t> b(rows * K);  // device table: [channel][row]
+    CK(cudaMemcpyAsync(b.data(), c->bins.p, b.size() * sizeof(int16_t), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (size_t k = 0; k < K; k++)
+      for (size_t r = 0; r < rows; r++) out[r * K + k] = b[k * rows + r];
+    return (int)(rows * K);
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
 int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n) {
   if (!c || !c->have_job) return SFXC_GPU_ESTATE;
   if (stream < 0 || stream >= (int)c->sc.size()) return fail(c, Error(SFXC_GPU_EINVAL, "bad stream index"));
@@ -1184,6 +1233,7 @@ int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n)
     StreamDev d = c->hsd[stream];
     d.block0 = 0;
     d.n_blocks = s.n_blocks;
+    d.spline_lo = spline_lo_for(d, s.sp.x);  // the block kernel walks the spline forward from block 0
     d.slot = 0;  // the only stream of this launch
     DevBuf ts, spec, sd, bp;
     ts.ensure((size_t)s.n_blocks * kNd * sizeof(float));
@@ -1196,7 +1246,7 @@ int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n)
     const int nper = c->p.window == WINDOW_NONE ? s.hop : s.rot;
     const sfxc_gpu_ctx::RotTables &t = c->rot_tables.at(s.rot);
     launch_window_fft(sd.as<StreamDev>(), 1, 0, (int)rows, (int)rows, t.window.as<float>(), t.twrot.as<float2>(),
-                      s.rot, nper, c->M, c->kpad, spec.p, false, 1.0f, c->st);
+                      s.rot, nper, c->M, c->kpad, spec.p, 0, 1.0f, c->st);
     CK(cudaGetLastError());
     CK(cudaMemcpy2DAsync(out, K * sizeof(float2), spec.p, c->kpad * sizeof(float2), K * sizeof(float2), rows,
                          cudaMemcpyDeviceToHost, c->st));
@@ -1212,14 +1262,13 @@ int sfxc_gpu_copy_spectra(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n)
 // ---------------------------------------------------------------------------
 // Allocation-free spectra inspection.  Some callers cannot allocate device
 // memory at the moment they want to look at a stream's delay-corrected
-// spectra: code running while a CUDA graph is being captured on the stream
-// (cudaMalloc/cudaFree are not capturable), real-time correlator loops whose
-// latency budget has no room for allocator synchronisation, and hosts that
-// hand the GPU's memory out once at start-up.  sfxc_gpu_copy_spectra_noalloc
-// does the work of sfxc_gpu_copy_spectra with its scratch (fringe-stopped
-// series, per-block delay parameters, the stream descriptor and the spectra
-// before the copy out) in one file-scope device array of fixed size instead
-// of fresh allocations.
+// spectra: real-time correlator loops whose latency budget has no room for
+// allocator synchronisation (cudaMalloc/cudaFree may wait for the whole
+// device), and hosts that hand the GPU's memory out once at start-up.
+// sfxc_gpu_copy_spectra_noalloc does the work of sfxc_gpu_copy_spectra with
+// its scratch (fringe-stopped series, per-block delay parameters, the stream
+// descriptor and the spectra before the copy out) in one file-scope device
+// array of fixed size instead of fresh allocations.
 namespace {
 constexpr int kNoallocMaxBlocks = 8192;                 // 2,097,152 samples of one stream and integration
 constexpr size_t kNoallocMaxSpectra = (size_t)1 << 20;  // rows x (fft_size_correlation + 4) complex values
@@ -1272,6 +1321,7 @@ int sfxc_gpu_copy_spectra_noalloc(sfxc_gpu_ctx *c, int32_t stream, float *out, s
     StreamDev d = c->hsd[stream];
     d.block0 = 0;
     d.n_blocks = s.n_blocks;
+    d.spline_lo = spline_lo_for(d, s.sp.x);  // the block kernel walks the spline forward from block 0
     d.slot = 0;  // the only stream of this launch
     d.ts = reinterpret_cast<float *>(base + kNoallocTsOff);
     d.bpar = reinterpret_cast<BlockPar *>(base + kNoallocParOff);
@@ -1284,7 +1334,7 @@ int sfxc_gpu_copy_spectra_noalloc(sfxc_gpu_ctx *c, int32_t stream, float *out, s
     const int nper = c->p.window == WINDOW_NONE ? s.hop : s.rot;
     const sfxc_gpu_ctx::RotTables &t = c->rot_tables.at(s.rot);
     launch_window_fft(dd, 1, 0, (int)rows, (int)rows, t.window.as<float>(), t.twrot.as<float2>(), s.rot, nper, c->M,
-                      c->kpad, spec, false, 1.0f, c->st);
+                      c->kpad, spec, 0, 1.0f, c->st);
     CK(cudaGetLastError());
     CK(cudaMemcpy2DAsync(out, K * sizeof(float2), spec, c->kpad * sizeof(float2), K * sizeof(float2), rows,
                          cudaMemcpyDeviceToHost, c->st));
@@ -1519,6 +1569,10 @@ struct sfxc_gpu_output {
   void *user = nullptr;
   int64_t next_slice = 0;  // curr_slice
   std::map<int64_t, std::pair<std::vector<uint8_t>, int>> held;  // slice -> (bytes, bins)
+  // set when a slice's write stopped part way (a refusing sink or a bad file
+  // index): some files already hold part of that slice, so writing it again
+  // would duplicate bytes; every later call fails
+  std::string failed;
 };
 
 namespace {
@@ -1578,13 +1632,20 @@ sfxc_gpu_output *sfxc_gpu_output_create(const sfxc_output_global *g, int32_t n_f
 int sfxc_gpu_output_put_slice(sfxc_gpu_output *o, int64_t slice_nr, const uint8_t *bytes, size_t n, int32_t bins) {
   if (!o) return SFXC_GPU_EINVAL;
   try {
+    if (!o->failed.empty()) throw Error(SFXC_GPU_ESTATE, "output failed earlier: " + o->failed);
     if ((n && !bytes) || bins <= 0 || n % (size_t)bins || n / (size_t)bins < 4)
       throw Error(SFXC_GPU_EINVAL, "slice bytes must be n_bins equal parts of at least 4 bytes");
     // set_weight_of_input_stream: a slice already written or already held is an error
     if (slice_nr < o->next_slice || o->held.count(slice_nr)) throw Error(SFXC_GPU_EINVAL, "slice given twice");
     o->held[slice_nr] = {std::vector<uint8_t>(bytes, bytes + n), bins};
     for (auto it = o->held.begin(); it != o->held.end() && it->first == o->next_slice; it = o->held.begin()) {
-      output_write_slice(o, it->second.first, it->second.second);
+      try {
+        output_write_slice(o, it->second.first, it->second.second);
+      } catch (const Error &e) {
+        o->failed = "slice " + std::to_string(it->first) + ": " + e.msg;
+        o->held.clear();
+        throw;
+      }
       o->held.erase(it);
       o->next_slice++;
     }
@@ -1597,6 +1658,10 @@ int sfxc_gpu_output_put_slice(sfxc_gpu_output *o, int64_t slice_nr, const uint8_
 
 int sfxc_gpu_output_finish(sfxc_gpu_output *o) {
   if (!o) return SFXC_GPU_EINVAL;
+  if (!o->failed.empty()) {
+    g_error = "output failed earlier: " + o->failed;
+    return SFXC_GPU_ESTATE;
+  }
   if (!o->held.empty()) {
     g_error = "slices held for a missing slice " + std::to_string(o->next_slice);
     return SFXC_GPU_ESTATE;

@@ -7,16 +7,18 @@
 namespace sfxc {
 
 constexpr int kNd = 256;  // fft_size_delaycor handled by the fused block kernel
-constexpr int kTcSlots = 32;  // stream slots per (row, channel) of the tensor-core spectra layout
+constexpr int kTcSlots = 32;  // stream slots per (row, channel) of the tensor-core spectra layout, up to 32 streams
+constexpr int kTcSlotsWide = 64;  // the same for jobs of 33 to 64 streams
 
 // Tensor-core spectra layout, in 8-byte units (one FP16 hi/lo complex value):
-// per row kpad channels x 32 slots; the channels in groups of four, and per
-// group the eight slot quads (slots 4q .. 4q+3) one 128-byte line each,
-// holding the group's four channels x four slots.  So the four streams of a
-// slot quad write whole lines, and one channel's 32 slots are eight 32-byte
-// pieces 128 bytes apart.  kpad is a multiple of 4.
-__host__ __device__ __forceinline__ int64_t tc_index(int64_t row, int kpad, int ch, int slot) {
-  return row * kpad * kTcSlots + (int64_t)(ch >> 2) * 128 + (slot >> 2) * 16 + (ch & 3) * 4 + (slot & 3);
+// per row kpad channels x S slots (S = 32, or 64 for jobs of more than 32
+// streams); the channels in groups of four, and per group the S/4 slot quads
+// (slots 4q .. 4q+3) one 128-byte line each, holding the group's four
+// channels x four slots.  So the four streams of a slot quad write whole
+// lines, and one channel's S slots are S/4 32-byte pieces 128 bytes apart.
+// kpad is a multiple of 4.
+__host__ __device__ __forceinline__ int64_t tc_index(int64_t row, int kpad, int ch, int slot, int S = kTcSlots) {
+  return (row * kpad + (ch & ~3)) * S + (slot >> 2) * 16 + (ch & 3) * 4 + (slot & 3);
 }
 
 // One plan segment: output samples [out0, out0+n) come from source bit src_bit

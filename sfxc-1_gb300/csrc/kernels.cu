@@ -441,7 +441,7 @@ __device__ __forceinline__ void window_apply(float2 (&v)[16], int t, int nper, c
 template <int N, int NS, int OUT_TC, bool SCALE>
 __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *sinfo, int NV, bool fast, int row,
                                           int nrows_total, int M, int kpad, const float2 *__restrict__ tw_rot,
-                                          void *__restrict__ spec_out, float tc_scale, int tid, int nthr) {
+                                          void *__restrict__ spec_out, float tc_scale, int S, int tid, int nthr) {
   static_assert(NS <= 4, "at most four streams per CTA");
   if (OUT_TC) {
     constexpr int W = NS;  // streams per store
@@ -462,7 +462,8 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
         }
       };
       const int s0 = sinfo[0].y;
-      uint2 *drow = dst + tc_index(row, kpad, 0, s0);  // channel i at drow + (i >> 2) * 128 + (i & 3) * 4
+      uint2 *drow = dst + tc_index(row, kpad, 0, s0, S);  // channel i at drow + (i >> 2) * 4S + (i & 3) * 4
+      const int gs = 4 * S;
       for (int i = tid; i < N / 2; i += nthr) {
         const float2 w = __ldg(tw_rot + i);
         uint2 a[W], b[W];
@@ -473,14 +474,14 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
           a[j] = tc_split<SCALE>(xq, tc_scale);
           b[j] = tc_split<SCALE>(xnq, tc_scale);
         }
-        put(drow + (i >> 2) * 128 + (i & 3) * 4, a);
-        put(drow + ((N - i) >> 2) * 128 + ((N - i) & 3) * 4, b);
+        put(drow + (i >> 2) * gs + (i & 3) * 4, a);
+        put(drow + ((N - i) >> 2) * gs + ((N - i) & 3) * 4, b);
       }
       if (tid >= nthr - W) {  // bin N/2, one stream per thread
         const int j = tid - (nthr - W);
         float2 xq, xnq;
         real_bin_pair<N, SCALE>(Z + j * BUF, __ldg(tw_rot + N / 2), N / 2, xq, xnq);
-        dst[tc_index(row, kpad, N / 2, s0 + j)] = tc_split<SCALE>(xq, tc_scale);
+        dst[tc_index(row, kpad, N / 2, s0 + j, S)] = tc_split<SCALE>(xq, tc_scale);
       }
       return;
     }
@@ -489,7 +490,7 @@ __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *
 #pragma unroll
       for (int j = 0; j < NS; j++)
         if (j < NV)
-          dst[tc_index(row, kpad, i, sinfo[j].y)] =
+          dst[tc_index(row, kpad, i, sinfo[j].y, S)] =
               tc_split<SCALE>(real_bin<N, SCALE>(Z + j * BUF, tw_rot, sinfo[j].x + i), tc_scale);
   } else {
 #pragma unroll 1
@@ -546,7 +547,7 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
     window_fft_kernel(
     const StreamDev *__restrict__ streams, int nstreams, int row0, int nrows, int nrows_total, int steps_per_cta,
     const float *__restrict__ window, const float2 *__restrict__ tw_rot, int nper, int M, int kpad,
-    void *__restrict__ spec_out, float tc_scale) {
+    void *__restrict__ spec_out, float tc_scale, int tc_slots) {
   using S = WinShape<LOGN, SPCMAX>;
   constexpr int N = S::N, T = S::T, SPC = S::SPC, RPC = S::RPC;
   extern __shared__ __align__(16) float2 dsm[];
@@ -629,7 +630,7 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
       const int row = k * RPC + r;
       if (row >= nrows) break;
       store_row<N, SPC, OUT_TC, !S::WSMEM>(dsm + r * SPC * S::BUF, S::BUF, sinfo, nv, fast, row0 + row, nrows_total,
-                                           M, kpad, tw_rot, spec_out, tc_scale, threadIdx.x, S::THREADS);
+                                           M, kpad, tw_rot, spec_out, tc_scale, tc_slots, threadIdx.x, S::THREADS);
     }
     // the next step's FFT rewrites the buffers (placing this barrier inside
     // that FFT, after its first radix-16 pass, measured 1.7 % slower)
@@ -789,88 +790,143 @@ __global__ void __launch_bounds__(256) bitstat_kernel(const StreamDev *__restric
 }
 
 // ------------------------------------------------------------------------
-// X-step on CUDA cores.  spec: [stream][row][kpad] complex64.  Each thread owns
-// one channel and TPW tiles of 4x4 stream pairs (i in tile row I, j in tile
-// column J, I <= J); blmap[i*npad+j] gives (baseline << 1 | conj) or -1.
-template <int TPW>
-__global__ void __launch_bounds__(384, 1) xcorr_f32_kernel(const float2 *__restrict__ spec, int nrows_total, int kpad,
-                                                        int nstreams, int npad, int r0, int r1, int K,
-                                                        const int *__restrict__ tiles, int ntiles,
-                                                        const int *__restrict__ blmap, float2 *__restrict__ acc) {
-  extern __shared__ float2 xs[];  // [npad][32] for one row
+// X-step on CUDA cores (Correlation_core::integration_step,
+// sfxc/src/correlation_core.cc:241-273; binned: Correlation_core_pulsar::
+// integration_step, sfxc/src/correlation_core_pulsar.cc:101-146).
+// spec: [stream][row][kpad] complex64.  Work items -- (32-channel tile, block
+// of rows, part of the stream-pair tiles) -- are dealt to persistent CTAs.  A
+// CTA stages R rows x npad streams x 32 channels per step through a 4-deep
+// cp.async ring (one barrier per R rows), so the loads of three steps are in
+// flight while one is multiplied; each thread owns one channel and up to TPW
+// tiles of 4x4 stream pairs (i in tile row I, j in tile column J, I <= J) in
+// registers, and adds them to the accumulators with float2 atomics when its
+// item ends, or, binned, when its channel's pulsar bin changes (acc[bin]).
+// blmap[i*npad+j] gives (baseline << 1 | conj) or -1.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+template <int TPW, bool BINNED>
+__global__ void __launch_bounds__(384, 1) xcorr_f32_kernel(const __grid_constant__ F32Args a) {
+  extern __shared__ __align__(16) float2 xs[];  // kF32Stages x [R rows][npad streams][32 channels]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const int k = blockIdx.x * 32 + lane;
-  float2 a[TPW][4][4];
-#pragma unroll
-  for (int t = 0; t < TPW; t++)
-#pragma unroll
-    for (int p = 0; p < 4; p++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) a[t][p][q] = make_float2(0.f, 0.f);
-  int ti[TPW], tj[TPW];
-#pragma unroll
-  for (int t = 0; t < TPW; t++) {
-    const int tile = warp + t * nwarps;
-    ti[t] = tile < ntiles ? tiles[2 * tile] : -1;
-    tj[t] = tile < ntiles ? tiles[2 * tile + 1] : -1;
-  }
-  for (int r = r0; r < r1; r++) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < npad * 32; e += blockDim.x) {
-      const int st = e >> 5, kk = blockIdx.x * 32 + (e & 31);
-      float2 v = make_float2(0.f, 0.f);
-      if (st < nstreams && kk < K) v = spec[((int64_t)st * nrows_total + r) * kpad + kk];
-      xs[e] = v;
-    }
-    __syncthreads();
+  const int nct = (a.K + 31) / 32;
+  const int nrows = a.r1 - a.r0;
+  const int nrb = (nrows + a.rblock - 1) / a.rblock;
+  const int nitems = nct * nrb * a.nparts;
+  const int stage_f2 = a.R * a.npad * 32;  // float2 per stage
+  const int chunks = a.R * a.npad * 16;    // 16-byte copies per stage
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const int part = item % a.nparts, rb = (item / a.nparts) % nrb, ct = item / (a.nparts * nrb);
+    const int k = ct * 32 + lane;
+    const int ra = a.r0 + rb * a.rblock, rz = min(a.r1, ra + a.rblock);
+    const int t_end = min(a.ntiles, (part + 1) * a.tiles_per_part);
+    int ti[TPW], tj[TPW];
+    float2 v[TPW][4][4];
 #pragma unroll
     for (int t = 0; t < TPW; t++) {
-      if (ti[t] < 0) continue;
-      float2 xi[4], xj[4];
-#pragma unroll
-      for (int p = 0; p < 4; p++) {
-        xi[p] = xs[(ti[t] * 4 + p) * 32 + lane];
-        xj[p] = xs[(tj[t] * 4 + p) * 32 + lane];
-      }
+      const int tile = part * a.tiles_per_part + warp + t * nwarps;
+      ti[t] = tile < t_end ? a.tiles[2 * tile] : -1;
+      tj[t] = tile < t_end ? a.tiles[2 * tile + 1] : -1;
 #pragma unroll
       for (int p = 0; p < 4; p++)
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-          // x_i * conj(x_j)
-          a[t][p][q].x += xi[p].x * xj[q].x + xi[p].y * xj[q].y;
-          a[t][p][q].y += xi[p].y * xj[q].x - xi[p].x * xj[q].y;
-        }
+        for (int q = 0; q < 4; q++) v[t][p][q] = make_float2(0.f, 0.f);
     }
-  }
-  if (k >= K) return;
+    // add the register tiles to acc[bin] (bin 0 when not binned) and clear them
+    auto flush = [&](int bin) {
+      if (k >= a.K || bin < 0) return;
 #pragma unroll
-  for (int t = 0; t < TPW; t++) {
-    if (ti[t] < 0) continue;
+      for (int t = 0; t < TPW; t++) {
+        if (ti[t] < 0) continue;
 #pragma unroll
-    for (int p = 0; p < 4; p++)
+        for (int p = 0; p < 4; p++)
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int i = ti[t] * 4 + p, j = tj[t] * 4 + q;
-        const int m = blmap[i * npad + j];
-        if (m < 0) continue;
-        float2 *dst = acc + (int64_t)(m >> 1) * kpad + k;
-        const float2 v = a[t][p][q];
-        float2 o = *dst;
-        o.x += v.x;
-        o.y += (m & 1) ? -v.y : v.y;
-        *dst = o;
+          for (int q = 0; q < 4; q++) {
+            const int m = __ldg(a.blmap + (ti[t] * 4 + p) * a.npad + tj[t] * 4 + q);
+            if (m >= 0) {
+              const float2 x = v[t][p][q];
+              atomicAdd(a.acc + ((int64_t)bin * a.nbl + (m >> 1)) * a.kpad + k,
+                        make_float2(x.x, (m & 1) ? -x.y : x.y));
+            }
+            v[t][p][q] = make_float2(0.f, 0.f);
+          }
       }
+    };
+    const int nsteps = (rz - ra + a.R - 1) / a.R;
+    auto issue = [&](int step) {
+      if (step < nsteps) {
+        float2 *dst = xs + (step % kF32Stages) * stage_f2;
+        const int rs = ra + step * a.R;
+        for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
+          const int rr = c / (a.npad * 16), rem = c - rr * (a.npad * 16), st = rem >> 4, cc = (rem & 15) * 2;
+          const int row = rs + rr, kk = ct * 32 + cc;
+          // channel kk + 1 may be K, which lies inside the padded row (kpad >= K + 3)
+          const bool ok = row < rz && st < a.nstreams && kk < a.K;
+          const float2 *src = ok ? a.spec + ((int64_t)st * a.nrows_total + row) * a.kpad + kk : a.spec;
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst + (rr * a.npad + st) * 32 + cc)),
+                       "l"(src), "r"(ok ? 16 : 0)
+                       : "memory");
+        }
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");  // possibly empty: keeps the group count per step
+    };
+#pragma unroll 1
+    for (int s = 0; s < kF32Stages - 1; s++) issue(s);
+    int cur = -1;
+#pragma unroll 1
+    for (int step = 0; step < nsteps; step++) {
+      asm volatile("cp.async.wait_group %0;" ::"n"(kF32Stages - 2) : "memory");
+      __syncthreads();  // step's rows are in; every thread is done with the slot refilled next
+      issue(step + kF32Stages - 1);
+      const float2 *xst = xs + (step % kF32Stages) * stage_f2;
+#pragma unroll 1
+      for (int rr = 0; rr < a.R; rr++) {
+        const int row = ra + step * a.R + rr;
+        if (row >= rz) break;
+        if constexpr (BINNED) {
+          const int bin = k < a.K ? __ldg(a.bins + (int64_t)k * a.bins_rows + (row - a.r0)) : -1;
+          if (bin != cur) {
+            flush(cur);
+            cur = bin;
+          }
+        }
+        const float2 *xr = xst + rr * a.npad * 32 + lane;
+#pragma unroll
+        for (int t = 0; t < TPW; t++) {
+          if (ti[t] < 0) continue;
+          float2 xi[4], xj[4];
+#pragma unroll
+          for (int p = 0; p < 4; p++) {
+            xi[p] = xr[(ti[t] * 4 + p) * 32];
+            xj[p] = xr[(tj[t] * 4 + p) * 32];
+          }
+#pragma unroll
+          for (int p = 0; p < 4; p++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              // x_i * conj(x_j)
+              v[t][p][q].x = fmaf(xi[p].x, xj[q].x, fmaf(xi[p].y, xj[q].y, v[t][p][q].x));
+              v[t][p][q].y = fmaf(xi[p].y, xj[q].x, fmaf(-xi[p].x, xj[q].y, v[t][p][q].y));
+            }
+        }
+      }
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    flush(BINNED ? cur : 0);
+    __syncthreads();  // the ring is refilled by the next item
   }
 }
 
 // ------------------------------------------------------------------------
 // Pulsar bins (Correlation_core_pulsar::dedisperse_buffer) in FP64, evaluated
-// with the reference's operation order so that every bin matches.
+// with the reference's operation order so that every bin matches; written
+// [channel][row] (row fastest) for the per-channel sort and the binned X-steps.
 __global__ void pulsar_bins_kernel(int nrows, int K, double start_phase, double rate_term, double fft_duration,
                                    const double *__restrict__ offsets, double g0, double g1, int nbins,
                                    int16_t *__restrict__ bins) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int r = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
   if (k >= K || r >= nrows) return;
   const double us_per_day = 86400000000.0;
   // start_phase + (coef[1] + 60 F0) * fft_duration * current_fft * 1440 / us_per_day
@@ -890,87 +946,7 @@ __global__ void pulsar_bins_kernel(int nrows, int K, double start_phase, double 
   } else {
     bin = 0;
   }
-  bins[(int64_t)r * K + k] = (int16_t)bin;
-}
-
-// Binned X-step: like xcorr_f32_kernel, but each thread keeps its register
-// tile while its channel's bin is unchanged and adds it into acc[bin] when
-// the bin changes (each (bin, baseline, channel) has a single owner thread).
-template <int TPW>
-__global__ void __launch_bounds__(384, 1) xcorr_f32_pulsar_kernel(
-    const float2 *__restrict__ spec, int nrows_total, int kpad, int nstreams, int npad, int r0, int r1, int K,
-    const int *__restrict__ tiles, int ntiles, const int *__restrict__ blmap, int nbl, const int16_t *__restrict__ bins,
-    float2 *__restrict__ acc) {
-  extern __shared__ float2 xs[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const int k = blockIdx.x * 32 + lane;
-  float2 a[TPW][4][4];
-  int ti[TPW], tj[TPW];
-#pragma unroll
-  for (int t = 0; t < TPW; t++) {
-    const int tile = warp + t * nwarps;
-    ti[t] = tile < ntiles ? tiles[2 * tile] : -1;
-    tj[t] = tile < ntiles ? tiles[2 * tile + 1] : -1;
-#pragma unroll
-    for (int p = 0; p < 4; p++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) a[t][p][q] = make_float2(0.f, 0.f);
-  }
-  auto flush = [&](int bin) {
-    if (k >= K || bin < 0) return;
-#pragma unroll
-    for (int t = 0; t < TPW; t++) {
-      if (ti[t] < 0) continue;
-#pragma unroll
-      for (int p = 0; p < 4; p++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const int m = blmap[(ti[t] * 4 + p) * npad + tj[t] * 4 + q];
-          if (m >= 0) {
-            float2 *dst = acc + ((int64_t)bin * nbl + (m >> 1)) * kpad + k;
-            float2 o = *dst;
-            o.x += a[t][p][q].x;
-            o.y += (m & 1) ? -a[t][p][q].y : a[t][p][q].y;
-            *dst = o;
-          }
-          a[t][p][q] = make_float2(0.f, 0.f);
-        }
-    }
-  };
-  int cur = -1;
-  for (int r = r0; r < r1; r++) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < npad * 32; e += blockDim.x) {
-      const int st = e >> 5, kk = blockIdx.x * 32 + (e & 31);
-      float2 v = make_float2(0.f, 0.f);
-      if (st < nstreams && kk < K) v = spec[((int64_t)st * nrows_total + r) * kpad + kk];
-      xs[e] = v;
-    }
-    __syncthreads();
-    const int bin = k < K ? bins[(int64_t)r * K + k] : -1;
-    if (bin != cur) {
-      flush(cur);
-      cur = bin;
-    }
-#pragma unroll
-    for (int t = 0; t < TPW; t++) {
-      if (ti[t] < 0) continue;
-      float2 xi[4], xj[4];
-#pragma unroll
-      for (int p = 0; p < 4; p++) {
-        xi[p] = xs[(ti[t] * 4 + p) * 32 + lane];
-        xj[p] = xs[(tj[t] * 4 + p) * 32 + lane];
-      }
-#pragma unroll
-      for (int p = 0; p < 4; p++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          a[t][p][q].x += xi[p].x * xj[q].x + xi[p].y * xj[q].y;
-          a[t][p][q].y += xi[p].y * xj[q].x - xi[p].x * xj[q].y;
-        }
-    }
-  }
-  flush(cur);
+  bins[(int64_t)k * nrows + r] = (int16_t)bin;
 }
 
 // ------------------------------------------------------------------------
@@ -1249,7 +1225,7 @@ void launch_phasecal(const uint8_t *data, const PcalRun *runs, int nruns, int pb
 template <int LOGN, int OUT_TC, int SPCMAX>
 static void window_fft_launch_spc(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                                   const float *window, const float2 *tw_rot, int nper, int M, int kpad, void *spec,
-                                  float tc_scale, cudaStream_t st) {
+                                  float tc_scale, int tc_slots, cudaStream_t st) {
   using S = WinShape<LOGN, SPCMAX>;
   const int nsg = (nstreams + S::SPC - 1) / S::SPC, nsteps = (nrows + S::RPC - 1) / S::RPC;
   // runs of steps so that the CTAs fill two waves
@@ -1261,17 +1237,17 @@ static void window_fft_launch_spc(const StreamDev *d_streams, int nstreams, int 
   auto kern = window_fft_kernel<LOGN, OUT_TC, SPCMAX>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
   kern<<<grid, S::THREADS, S::SMEM, st>>>(d_streams, nstreams, row0, nrows, nrows_total, steps_per_cta, window, tw_rot,
-                                          nper, M, kpad, spec, tc_scale);
+                                          nper, M, kpad, spec, tc_scale, tc_slots);
 }
 
 template <int LOGN, int OUT_TC>
 static void window_fft_launch(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                               const float *window, const float2 *tw_rot, int nper, int M, int kpad, void *spec,
-                              float tc_scale, cudaStream_t st) {
+                              float tc_scale, int tc_slots, cudaStream_t st) {
   // four streams per CTA: a whole 32-byte sector per channel in the TC layout
   // (two streams per CTA, two CTAs per SM, measured 20 % slower)
   window_fft_launch_spc<LOGN, OUT_TC, 4>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad,
-                                         spec, tc_scale, st);
+                                         spec, tc_scale, tc_slots, st);
 }
 
 #define SFXC_LOGN_SWITCH(logn, CALL) \
@@ -1288,13 +1264,13 @@ static void window_fft_launch(const StreamDev *d_streams, int nstreams, int row0
 
 void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                        const float *window, const float2 *tw_rot, int rot, int nper, int M, int kpad, void *spec,
-                       bool tc, float tc_scale, cudaStream_t st) {
+                       int tc_slots, float tc_scale, cudaStream_t st) {
   const int logn = 30 - __builtin_clz((unsigned)rot);  // log2(rot / 2)
 #define SFXC_WIN(L)                                                                                            \
-  (tc ? window_fft_launch<L, 1>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad, \
-                                spec, tc_scale, st)                                                           \
-      : window_fft_launch<L, 0>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad, \
-                                spec, tc_scale, st))
+  (tc_slots ? window_fft_launch<L, 1>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, \
+                                      kpad, spec, tc_scale, tc_slots, st)                                     \
+            : window_fft_launch<L, 0>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, \
+                                      kpad, spec, tc_scale, 0, st))
   SFXC_LOGN_SWITCH(logn, SFXC_WIN)
 #undef SFXC_WIN
 }
@@ -1324,49 +1300,73 @@ cudaError_t launch_reduce(const float2 *in, int nspec, int M, int nch, const flo
   return cudaGetLastError();
 }
 
-static int xcorr_threads(int ntiles, int tpw) {
-  int warps = (ntiles + tpw - 1) / tpw;
-  if (warps < 1) warps = 1;
-  return warps * 32;
+// Work split of the FP32 X-step for ntiles stream-pair tiles: parts of at
+// most 36 tiles (12 warps x 3), the smallest tiles-per-warp that fits a part
+// into 12 warps, rows per step so that a step stages at most 32 KB.
+F32Plan xcorr_f32_plan(int ntiles, int npad) {
+  F32Plan p;
+  if (ntiles <= 0 || npad <= 0 || npad * 256 > kF32StageBytes * 4) return p;
+  p.nparts = (ntiles + 35) / 36;
+  p.tiles_per_part = (ntiles + p.nparts - 1) / p.nparts;
+  for (p.tpw = 1; p.tpw < 3 && (p.tiles_per_part + p.tpw - 1) / p.tpw > 12; p.tpw++) {
+  }
+  p.warps = (p.tiles_per_part + p.tpw - 1) / p.tpw;
+  p.R = std::max(1, kF32StageBytes / (npad * 256));
+  p.smem = (size_t)kF32Stages * p.R * npad * 256;
+  return p;
 }
 
-int xcorr_tpw(int ntiles) {
-  // registers per thread grow with TPW: the smallest TPW that fits 12 warps
-  for (int t = 1; t <= 4; t++)
-    if ((ntiles + t - 1) / t <= 12) return t;
-  return -1;
+template <int TPW>
+static void f32_launch(const F32Args &a, const F32Plan &p, bool binned, cudaStream_t st) {
+  auto kern = binned ? xcorr_f32_kernel<TPW, true> : xcorr_f32_kernel<TPW, false>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem);
+  const int nct = (a.K + 31) / 32, nrows = a.r1 - a.r0;
+  const int nrb = (nrows + a.rblock - 1) / a.rblock;
+  const int nitems = nct * nrb * a.nparts;
+  kern<<<std::min(nitems, sm_count()), p.warps * 32, p.smem, st>>>(a);
 }
 
 void launch_xcorr_f32(const float2 *spec, int nrows_total, int kpad, int nstreams, int npad, int r0, int r1, int K,
-                      const int *tiles, int ntiles, const int *blmap, float2 *acc, cudaStream_t st) {
-  const int tpw = xcorr_tpw(ntiles);
-  const int threads = xcorr_threads(ntiles, tpw);
-  const dim3 grid((K + 31) / 32);
-  const size_t smem = (size_t)npad * 32 * sizeof(float2);
-  switch (tpw) {
-    case 1: xcorr_f32_kernel<1><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, r0, r1, K, tiles, ntiles, blmap, acc); break;
-    case 2: xcorr_f32_kernel<2><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, r0, r1, K, tiles, ntiles, blmap, acc); break;
-    case 3: xcorr_f32_kernel<3><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, r0, r1, K, tiles, ntiles, blmap, acc); break;
-    default: xcorr_f32_kernel<4><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, r0, r1, K, tiles, ntiles, blmap, acc); break;
+                      const int *tiles, int ntiles, const int *blmap, int nbl, const int16_t *bins, int bins_rows,
+                      float2 *acc, cudaStream_t st) {
+  if (r1 <= r0 || K <= 0) return;
+  const F32Plan p = xcorr_f32_plan(ntiles, npad);
+  if (p.tpw <= 0) return;
+  F32Args a;
+  a.spec = spec;
+  a.nrows_total = nrows_total;
+  a.kpad = kpad;
+  a.nstreams = nstreams;
+  a.npad = npad;
+  a.r0 = r0;
+  a.r1 = r1;
+  a.K = K;
+  a.tiles = tiles;
+  a.ntiles = ntiles;
+  a.tiles_per_part = p.tiles_per_part;
+  a.nparts = p.nparts;
+  a.R = p.R;
+  a.blmap = blmap;
+  a.nbl = nbl;
+  a.bins = bins;
+  a.bins_rows = bins_rows;
+  a.acc = acc;
+  // blocks of rows so that about four items per SM keep the CTAs balanced
+  const int nct = (K + 31) / 32, nrows = r1 - r0;
+  const int nrb = std::max(1, std::min((nrows + p.R - 1) / p.R, (4 * sm_count() + nct * p.nparts - 1) / (nct * p.nparts)));
+  a.rblock = ((nrows + nrb - 1) / nrb + p.R - 1) / p.R * p.R;
+  const bool binned = bins != nullptr;
+  switch (p.tpw) {
+    case 1: f32_launch<1>(a, p, binned, st); break;
+    case 2: f32_launch<2>(a, p, binned, st); break;
+    default: f32_launch<3>(a, p, binned, st); break;
   }
 }
 
-void launch_pulsar(const float2 *spec, int nrows_total, int kpad, int nstreams, int npad, int nrows, int K,
-                   const int *tiles, int ntiles, const int *blmap, int nbl, double start_phase, double rate_term,
-                   double fft_duration, const double *offsets, double g0, double g1, int nbins, int16_t *bins,
-                   float2 *acc, cudaStream_t st) {
-  pulsar_bins_kernel<<<dim3((K + 127) / 128, nrows), 128, 0, st>>>(nrows, K, start_phase, rate_term, fft_duration,
+void launch_pulsar_bins(int nrows, int K, double start_phase, double rate_term, double fft_duration,
+                        const double *offsets, double g0, double g1, int nbins, int16_t *bins, cudaStream_t st) {
+  pulsar_bins_kernel<<<dim3((nrows + 127) / 128, K), 128, 0, st>>>(nrows, K, start_phase, rate_term, fft_duration,
                                                                   offsets, g0, g1, nbins, bins);
-  const int tpw = xcorr_tpw(ntiles);
-  const int threads = xcorr_threads(ntiles, tpw);
-  const dim3 grid((K + 31) / 32);
-  const size_t smem = (size_t)npad * 32 * sizeof(float2);
-  switch (tpw) {
-    case 1: xcorr_f32_pulsar_kernel<1><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, 0, nrows, K, tiles, ntiles, blmap, nbl, bins, acc); break;
-    case 2: xcorr_f32_pulsar_kernel<2><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, 0, nrows, K, tiles, ntiles, blmap, nbl, bins, acc); break;
-    case 3: xcorr_f32_pulsar_kernel<3><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, 0, nrows, K, tiles, ntiles, blmap, nbl, bins, acc); break;
-    default: xcorr_f32_pulsar_kernel<4><<<grid, threads, smem, st>>>(spec, nrows_total, kpad, nstreams, npad, 0, nrows, K, tiles, ntiles, blmap, nbl, bins, acc); break;
-  }
 }
 
 void launch_normalize(const float2 *acc, int kpad, int M, int nstreams, int nbl, const int *bl, double *norms,

@@ -18,22 +18,54 @@ void launch_fstep(const StreamDev *d_streams, int nstreams, int max_blocks, cons
 void launch_unpack(const StreamDev *d_streams, int nstreams, int max_blocks, float *out, cudaStream_t st);
 void launch_extract(const uint8_t *in, int64_t nout, int N, int bits, int nsub, int fan_out, const int *tracks,
                     uint8_t *out, cudaStream_t st);
+// tc_slots: slots per (row, channel) of the TC layout (32 or 64); 0 writes the FP32 layout
 void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                        const float *window, const float2 *tw_rot, int rot, int nper, int M, int kpad, void *spec,
-                       bool tc, float tc_scale, cudaStream_t st);
+                       int tc_slots, float tc_scale, cudaStream_t st);
 void launch_bitstat(const StreamDev *d_streams, const int4 *d_items, int nitems, cudaStream_t st);
-int xcorr_tpw(int ntiles);
+// FP32 X-step (xcorr_f32_kernel): launch arguments and work split
+constexpr int kF32Stages = 4;         // cp.async ring depth
+constexpr int kF32StageBytes = 32768;  // rows x streams x 32 channels staged per step, at most
+struct F32Args {
+  const float2 *spec;  // [stream][row][kpad] complex64
+  int nrows_total, kpad, nstreams, npad, r0, r1, K;
+  const int *tiles;    // (I, J) per 4x4 stream-pair tile
+  int ntiles, tiles_per_part, nparts, rblock, R;
+  const int *blmap;
+  int nbl;
+  const int16_t *bins;  // binned (pulsar): [channel][row] with row stride bins_rows, row 0 = r0; else NULL
+  int bins_rows;
+  float2 *acc;          // [bin][baseline][kpad]
+};
+struct F32Plan {
+  int nparts = 0, tiles_per_part = 0, tpw = 0, warps = 0, R = 0;
+  size_t smem = 0;
+};
+// tpw == 0: the streams do not fit (npad x 256 B over 128 KB of staging)
+F32Plan xcorr_f32_plan(int ntiles, int npad);
+// rows [r0, r1) of spec into acc; bins != NULL: binned, acc[bins[k][r - r0]]
 void launch_xcorr_f32(const float2 *spec, int nrows_total, int kpad, int nstreams, int npad, int r0, int r1, int K,
-                      const int *tiles, int ntiles, const int *blmap, float2 *acc, cudaStream_t st);
-void launch_pulsar(const float2 *spec, int nrows_total, int kpad, int nstreams, int npad, int nrows, int K,
-                   const int *tiles, int ntiles, const int *blmap, int nbl, double start_phase, double rate_term,
-                   double fft_duration, const double *offsets, double g0, double g1, int nbins, int16_t *bins,
-                   float2 *acc, cudaStream_t st);
+                      const int *tiles, int ntiles, const int *blmap, int nbl, const int16_t *bins, int bins_rows,
+                      float2 *acc, cudaStream_t st);
+// pulsar bin of every (row, channel), FP64 in the reference's order: bins[k * nrows + r]
+void launch_pulsar_bins(int nrows, int K, double start_phase, double rate_term, double fft_duration,
+                        const double *offsets, double g0, double g1, int nbins, int16_t *bins, cudaStream_t st);
+// rows of each channel sorted stably by bin, each bin's run padded with -1 to a
+// multiple of 16: rowlist[ch * list_len + e], segs[ch * nbins + bin] = (first, entries)
+void launch_pulsar_sort(const int16_t *bins, int nrows, int K, int nbins, int list_len, int *rowlist, int2 *segs,
+                        cudaStream_t st);
 size_t xcorr_tc_smem_bytes();
 // TC spectra: per row, channels x 32 stream slots of 4 FP16 (hi.re, hi.im, lo.re, lo.im), in the
 // line-complete order of tc_index.
 cudaError_t launch_xcorr_tc(const void *spec, int nrows, int kpad, int K, const int *blmap, int npad,
                             float inv_scale2, float2 *acc, int *err, cudaStream_t st);
+// Row-gathered tensor-core X-step over TC spectra with `slots` (32 or 64)
+// slots: rowlist == NULL: rows 0..nrows-1 in order into acc (jobs of up to 64
+// streams); else per channel the rows of rowlist, segment (channel, bin) of
+// segs into acc[bin] (pulsar binning).  Rows need no zero padding.
+cudaError_t launch_xcorr_tc_gather(const void *spec, int slots, int nrows, int kpad, int K, int nstreams,
+                                   const int *blmap, int npad, int nbl, int nbins, const int *rowlist, int list_len,
+                                   const int2 *segs, float inv_scale2, float2 *acc, int *err, cudaStream_t st);
 void launch_normalize(const float2 *acc, int kpad, int M, int nstreams, int nbl, const int *bl, double *norms,
                       const double *flagfac, float2 *out, cudaStream_t st);
 // Sub-integration dump with extra phase centres: acc[b][k] (b < nbl, k < K,

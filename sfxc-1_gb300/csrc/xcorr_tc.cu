@@ -38,9 +38,11 @@
 
 #include "device.cuh"
 #include "kernels.hpp"
+#include "tc_ptx.cuh"
 
 namespace sfxc {
 namespace {
+using namespace tc;
 
 constexpr int kChan = 2;        // channels per group (one TMEM buffer)
 constexpr int kRowsK = 64;      // FFT rows per K-tile
@@ -49,115 +51,16 @@ constexpr int kThreads = 320;   // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr int kChanTile = kRowsK * 256;       // one channel's K-tile: 64 rows x 128 components x 2 B
 constexpr int kStageBytes = kChan * kChanTile;  // 32 KB per stage
 constexpr uint32_t kBufCols = kChan * 128;      // TMEM columns per buffer
-constexpr unsigned long long kSpinLimit = 200000000ull;
-constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-// SM100 shared-memory matrix descriptor: start >> 4 (bits 0-13), leading
-// byte offset >> 4 (16-29), stride byte offset >> 4 (32-45), version 1
-// (bit 46), base offset 0, layout type SWIZZLE_32B = 6 (bits 61-63).  For the
-// MN-major operand the leading offset steps between M atoms, the stride
-// offset between 8-row K groups.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr >> 4) & 0x3FFF);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)6 << 61;
-  return d;
-}
-
-// Instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A and B FP16
-// (formats 0), A and B MN-major (bits 15, 16), N >> 3 at bits 17-22, M >> 4 at
-// bits 24-28.
-__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
-  return (1u << 4) | (1u << 15) | (1u << 16) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ uint64_t globaltimer_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Bounded wait for the phase with the given parity: gives up after kWaitNs of
-// wall time (and after kSpinLimit polls), returning false.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  const uint32_t a = smem_u32(bar);
-  const uint64_t t0 = globaltimer_ns();
-  for (unsigned long long i = 0; i < kSpinLimit; i++) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if ((i & 255) == 255 && globaltimer_ns() - t0 > kWaitNs) return false;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                        uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-
-// 32 lanes x 32 consecutive FP32 columns of the warp's TMEM subpartition.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
 // One channel's K-tile: TMA box {16 components, 8 rows, 8 slot quads, 8 row
 // groups, 1 channel group} = 16 KB at row group rg and channel group cg.
-__device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *map, int rg, int cg, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
-      "%6}], [%7];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(0), "r"(0), "r"(rg), "r"(cg), "r"(smem_u32(bar))
-      : "memory");
+__device__ __forceinline__ void tma_load_tile(void *dst, const CUtensorMap *map, int rg, int cg, uint64_t *bar) {
+  tma_load_5d(dst, map, 0, 0, 0, rg, cg, bar);
 }
 
 // Tensor maps of the four channels of a channel group (base offsets 32 B apart).
 struct TcMaps {
   CUtensorMap m[4];
 };
-
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
 
 __global__ void __launch_bounds__(kThreads, 1)
     xcorr_tc_kernel(const __grid_constant__ TcMaps tmaps, int nrows, int K, int kpad, const int *__restrict__ blmap,
@@ -174,9 +77,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int my_groups = blockIdx.x < ngroups ? (ngroups - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&tmem_base))
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    tmem_alloc(&tmem_base, 512);
   }
   if (tid == 0) {
     for (int s = 0; s < kStages; s++) {
@@ -215,7 +116,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int c = 0; c < kChan; c++) {
           const int ch = g * kChan + c;
-          tma_load_5d(st + c * kChanTile, &tmaps.m[ch & 3], kt * (kRowsK / 8), ch >> 2, &full[s]);
+          tma_load_tile(st + c * kChanTile, &tmaps.m[ch & 3], kt * (kRowsK / 8), ch >> 2, &full[s]);
         }
         last[s] = it;
       }
@@ -323,7 +224,299 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   if (warp == 0) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Row-gathered tensor-core X-step: the same compensated Gram products, with
+// each channel's FFT rows taken in the order of a per-channel row list, cut
+// into segments that go to separate accumulators:
+//   * pulsar binning (Correlation_core_pulsar::integration_step,
+//     sfxc/src/correlation_core_pulsar.cc:101-146 with the bins of 210-238):
+//     each channel's rows sorted by bin (pulsar_sort_kernel), one segment per
+//     bin, the segment's Gram added to acc[bin];
+//   * jobs of 33 to 64 streams (S = 64 slots): rows in order, one segment.
+// Warps 0-3 gather K-tiles of up to 64 listed rows with 16-byte cp.async
+// straight into the 32-byte-swizzled MN-major layout that the TMA kernel's
+// boxes produce (list entries of -1 read as zero rows) and publish each tile
+// after a proxy fence; warp 4 issues the MMAs -- per 16 rows, block I = 0
+// (and 1 for S = 64): M = 128 rows of components from 128 I, N = the
+// components from 128 I to the last stream (FP32 accumulation in the
+// segment's TMEM buffer); warps 5-12 add each finished buffer to its
+// accumulator while the next segments accumulate in the other buffers.
+// Every wait is bounded: on timeout the CTA records an error and stops,
+// waits (bounded) for its copies and MMAs in flight, frees its TMEM and
+// returns.
+template <int S>
+struct GatherShape {
+  static constexpr int kRows = 64;                       // rows per K-tile
+  static constexpr int kGroupBytes = (S / 4) * 256;      // one 8-row K group: S/4 atoms of 8 rows x 32 B
+  static constexpr int kStageBytes = 8 * kGroupBytes;    // 16 KB (S = 32) or 32 KB (S = 64)
+  static constexpr int kStages = 131072 / kStageBytes;   // 128 KB of stages: one CTA per SM
+  static constexpr int kProducers = 128;                 // warps 0-3
+  static constexpr int kThreads = 416;                   // + warp 4 (MMA) + warps 5-12 (epilogue)
+  static constexpr size_t kSmem = (size_t)kStages * kStageBytes + 1024;
+};
+
+struct GatherArgs {
+  const uint8_t *spec;  // TC layout with S slots
+  int nrows;            // rows in the buffer; list entries outside [0, nrows) read as zeros
+  int kpad, K, nstreams, npad, nbl, nbins;
+  const int *rowlist;   // per channel list_len entries (row or -1); NULL: the rows in order
+  int list_len;
+  const int2 *segs;     // per (channel, bin): first list entry, entries (a multiple of 16); NULL: one segment
+  const int *blmap;
+  float inv_scale2;
+  float2 *acc;          // [bin][baseline][kpad]
+  int *err;
+  int n0, n1, col1;     // MMA N of blocks 0 and 1 (n1 = 0: one block), TMEM column of block 1
+  int buf_stride, nbuf; // TMEM columns per buffer, number of buffers
+};
+
+__device__ __forceinline__ int2 gather_seg(const GatherArgs &g, int ch, int bin) {
+  if (!g.segs) return make_int2(0, (g.nrows + 15) & ~15);
+  return g.segs[(size_t)ch * g.nbins + bin];
+}
+
+template <int S>
+__global__ void __launch_bounds__(GatherShape<S>::kThreads, 1) xcorr_tc_gather_kernel(const __grid_constant__ GatherArgs g) {
+  using G = GatherShape<S>;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *base = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);  // stages 1 KB aligned
+  __shared__ uint64_t full[G::kStages], empty[G::kStages], tfull[4], tempty[4], done;
+  __shared__ uint32_t tmem_base;
+  __shared__ int failed;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 4) tmem_alloc(&tmem_base, 512);
+  if (tid == 0) {
+    for (int s = 0; s < G::kStages; s++) {
+      mbar_init(&full[s], G::kProducers);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 4; b++) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 8);  // one arrival per epilogue warp
+    }
+    mbar_init(&done, 1);
+    failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  volatile int *vfailed = &failed;
+
+  if (tid < G::kProducers) {
+    // ---- producers: every K-tile of every segment of this CTA's channels
+    int it = 0;
+    bool stop = false;
+    for (int ch = blockIdx.x; ch < g.K && !stop; ch += gridDim.x) {
+      const int *list = g.rowlist ? g.rowlist + (size_t)ch * g.list_len : nullptr;
+      for (int bin = 0; bin < g.nbins && !stop; bin++) {
+        const int2 sg = gather_seg(g, ch, bin);
+        for (int t0 = 0; t0 < sg.y; t0 += G::kRows, it++) {
+          const int rows = min(G::kRows, sg.y - t0);
+          const int s = it % G::kStages, n = it / G::kStages;
+          if ((n > 0 && !mbar_wait(&empty[s], (n - 1) & 1)) || *vfailed) {
+            *vfailed = 1;
+            stop = true;
+            break;
+          }
+          const uint32_t st = smem_u32(base + s * G::kStageBytes);
+          for (int c = tid; c < rows * (S / 2); c += G::kProducers) {
+            const int j = c / (S / 2), q = (c % (S / 2)) >> 1, h = c & 1;
+            const int e = sg.x + t0 + j;
+            const int row = list ? __ldg(list + e) : e;
+            const bool ok = row >= 0 && row < g.nrows;
+            const uint8_t *src = ok ? g.spec + tc_index(row, g.kpad, ch, 4 * q, S) * 8 + 16 * h : g.spec;
+            cp_async16(st + (j >> 3) * G::kGroupBytes + q * 256 + sw32_offset(j & 7, h), src, ok ? 16u : 0u);
+          }
+          asm volatile("cp.async.commit_group;" ::: "memory");
+          if (it > 0) {  // the previous tile has landed: publish it to the tensor cores
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(&full[(it - 1) % G::kStages]);
+          }
+        }
+      }
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (it > 0) mbar_arrive(&full[(it - 1) % G::kStages]);
+  } else if (tid == 4 * 32) {
+    // ---- MMA issuer
+    const uint32_t id0 = idesc_f16(128, g.n0), id1 = idesc_f16(128, g.n1 > 0 ? g.n1 : 16);
+    int it = 0, sgn = 0;
+    bool stop = false;
+    for (int ch = blockIdx.x; ch < g.K && !stop; ch += gridDim.x) {
+      for (int bin = 0; bin < g.nbins && !stop; bin++) {
+        const int2 sg = gather_seg(g, ch, bin);
+        if (sg.y <= 0) continue;
+        const int b = sgn % g.nbuf, u = sgn / g.nbuf;
+        if ((u > 0 && !mbar_wait(&tempty[b], (u - 1) & 1)) || *vfailed) {  // the epilogue has read buffer b
+          *vfailed = 1;
+          stop = true;
+          break;
+        }
+        fence_after_sync();
+        const uint32_t d0 = tmem + (uint32_t)(b * g.buf_stride);
+        for (int t0 = 0; t0 < sg.y; t0 += G::kRows, it++) {
+          const int rows = min(G::kRows, sg.y - t0);
+          const int s = it % G::kStages, n = it / G::kStages;
+          if (!mbar_wait(&full[s], n & 1)) {
+            stop = true;
+            break;
+          }
+          fence_after_sync();
+          const uint32_t st = smem_u32(base + s * G::kStageBytes);
+          for (int ks = 0; ks < rows / 16; ks++) {
+            const uint32_t acc_flag = (t0 > 0 || ks > 0) ? 1u : 0u;
+            // 16 K rows = two 8-row groups; MN atoms 256 B apart; block 1 starts 8 atoms in
+            const uint64_t a0 = smem_desc(st + ks * 2 * G::kGroupBytes, 256, G::kGroupBytes);
+            mma_f16(d0, a0, a0, id0, acc_flag);
+            if (g.n1 > 0) {
+              const uint64_t a1 = smem_desc(st + ks * 2 * G::kGroupBytes + 2048, 256, G::kGroupBytes);
+              mma_f16(d0 + (uint32_t)g.col1, a1, a1, id1, acc_flag);
+            }
+          }
+          mma_commit(&empty[s]);
+        }
+        if (stop) {
+          *vfailed = 1;
+          break;
+        }
+        mma_commit(&tfull[b]);  // the segment's sums are complete when its MMAs are
+        sgn++;
+      }
+    }
+    mma_commit(&done);  // arrives once every MMA issued above has completed
+  } else if (warp >= 5) {
+    // ---- epilogue: warp w reads TMEM lane quarter q = w % 4 (D rows 32 q ..
+    // 32 q + 31 of each block) and every other 16-column chunk
+    const int q = warp & 3, half = (warp - 5) >> 2;
+    const int m = q * 32 + lane, p = m & 3;
+    int sgn = 0;
+    bool stop = false;
+    for (int ch = blockIdx.x; ch < g.K && !stop; ch += gridDim.x) {
+      for (int bin = 0; bin < g.nbins; bin++) {
+        const int2 sg = gather_seg(g, ch, bin);
+        if (sg.y <= 0) continue;
+        const int b = sgn % g.nbuf, u = sgn / g.nbuf;
+        if (!mbar_wait(&tfull[b], u & 1) || *vfailed) {
+          *vfailed = 1;
+          stop = true;
+          break;
+        }
+        fence_after_sync();
+        float2 *accb = g.acc + (size_t)bin * g.nbl * g.kpad + ch;
+        for (int I = 0; I < (g.n1 > 0 ? 2 : 1); I++) {
+          if (32 * I + 8 * q >= g.nstreams) continue;  // no stream in this lane quarter
+          const int a = 32 * I + (m >> 2);
+          const int nI = I ? g.n1 : g.n0;
+          const uint32_t col = (uint32_t)(b * g.buf_stride + (I ? g.col1 : 0));
+#pragma unroll 1
+          for (int chunk = half; chunk < nI / 16; chunk += 2) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + col + 16 * chunk, v);
+            float re4[4], im4[4];
+#pragma unroll
+            for (int bb = 0; bb < 4; bb++) {
+              const float A = v[4 * bb] + v[4 * bb + 2], B = v[4 * bb + 1] + v[4 * bb + 3];
+              // row component p: 0 hi.re, 1 hi.im, 2 lo.re, 3 lo.im; columns likewise
+              float re = (p & 1) ? B : A, im = (p & 1) ? A : -B;
+              re += __shfl_xor_sync(0xffffffffu, re, 1);
+              im += __shfl_xor_sync(0xffffffffu, im, 1);
+              re += __shfl_xor_sync(0xffffffffu, re, 2);
+              im += __shfl_xor_sync(0xffffffffu, im, 2);
+              re4[bb] = re;
+              im4[bb] = im;
+            }
+            if (p == 0 && a < g.nstreams) {
+              int mv[4];
+#pragma unroll
+              for (int bb = 0; bb < 4; bb++) {
+                const int bs = 32 * I + 4 * chunk + bb;
+                mv[bb] = bs < g.nstreams ? __ldg(g.blmap + a * g.npad + bs) : -1;
+              }
+              float2 o[4];
+#pragma unroll
+              for (int bb = 0; bb < 4; bb++)
+                if (mv[bb] >= 0) o[bb] = accb[(size_t)(mv[bb] >> 1) * g.kpad];
+#pragma unroll
+              for (int bb = 0; bb < 4; bb++)
+                if (mv[bb] >= 0) {
+                  o[bb].x += re4[bb] * g.inv_scale2;
+                  o[bb].y += ((mv[bb] & 1) ? -im4[bb] : im4[bb]) * g.inv_scale2;
+                  accb[(size_t)(mv[bb] >> 1) * g.kpad] = o[bb];
+                }
+            }
+          }
+        }
+        fence_before_sync();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&tempty[b]);  // buffer b may be overwritten
+        sgn++;
+      }
+    }
+  }
+  __syncthreads();
+  if (!mbar_wait(&done, 0)) *vfailed = 1;  // no MMA in flight past this point
+  fence_after_sync();
+  __syncthreads();
+  if (*vfailed && tid == 0) atomicExch(g.err, 1);
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 4) {
+    fence_after_sync();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+// Rows of each channel sorted stably by pulsar bin, each bin's run padded
+// with -1 entries to a multiple of 16 rows: rowlist[ch][list_len] and
+// segs[ch][bin] = (first entry, entries).  bins: [channel][row].  One warp
+// per channel; shared counters per warp.
+__global__ void __launch_bounds__(128) pulsar_sort_kernel(const int16_t *__restrict__ bins, int nrows, int K,
+                                                          int nbins, int list_len, int *__restrict__ rowlist,
+                                                          int2 *__restrict__ segs) {
+  extern __shared__ int cnt[];  // per warp: count[nbins], cursor[nbins]
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ch = blockIdx.x * 4 + w;
+  if (ch >= K) return;  // whole warps
+  int *count = cnt + w * 2 * nbins, *cursor = count + nbins;
+  for (int b = lane; b < nbins; b += 32) count[b] = 0;
+  __syncwarp();
+  const int16_t *br = bins + (size_t)ch * nrows;
+  for (int r = lane; r < nrows; r += 32) atomicAdd(&count[br[r]], 1);
+  __syncwarp();
+  if (lane == 0) {
+    int pos = 0;
+    for (int b = 0; b < nbins; b++) {
+      const int len = (count[b] + 15) & ~15;
+      segs[(size_t)ch * nbins + b] = make_int2(pos, len);
+      cursor[b] = pos;
+      pos += len;
+    }
+  }
+  __syncwarp();
+  int *list = rowlist + (size_t)ch * list_len;
+  for (int b = lane; b < nbins; b += 32)  // padding entries of each run
+    for (int e = cursor[b] + count[b]; e < cursor[b] + ((count[b] + 15) & ~15); e++) list[e] = -1;
+  __syncwarp();
+  for (int r0 = 0; r0 < nrows; r0 += 32) {
+    const int r = r0 + lane;
+    const int b = r < nrows ? br[r] : -1;
+    const unsigned same = __match_any_sync(0xffffffffu, b);
+    const int rank = __popc(same & ((1u << lane) - 1u));
+    const int pos = b >= 0 ? cursor[b] + rank : 0;
+    __syncwarp();
+    if (b >= 0) {
+      list[pos] = r;
+      if (rank == 0) cursor[b] = pos + __popc(same);
+    }
+    __syncwarp();
   }
 }
 
@@ -377,6 +570,60 @@ cudaError_t launch_xcorr_tc(const void *spec, int nrows, int kpad, int K, const 
   xcorr_tc_kernel<<<std::min(ngroups, nsm), kThreads, smem, st>>>(maps, nrows, K, kpad, blmap, npad, inv_scale2, acc,
                                                                    err);
   return cudaGetLastError();
+}
+
+template <int S>
+static cudaError_t launch_gather(const GatherArgs &g, cudaStream_t st) {
+  using G = GatherShape<S>;
+  cudaError_t e = cudaFuncSetAttribute(xcorr_tc_gather_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)G::kSmem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 1;
+  xcorr_tc_gather_kernel<S><<<std::min(g.K, nsm), G::kThreads, G::kSmem, st>>>(g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_xcorr_tc_gather(const void *spec, int slots, int nrows, int kpad, int K, int nstreams,
+                                   const int *blmap, int npad, int nbl, int nbins, const int *rowlist, int list_len,
+                                   const int2 *segs, float inv_scale2, float2 *acc, int *err, cudaStream_t st) {
+  if (nrows <= 0 || K <= 0) return cudaSuccess;
+  if ((slots != kTcSlots && slots != kTcSlotsWide) || nstreams > slots || nstreams <= 0)
+    return cudaErrorInvalidValue;
+  GatherArgs g;
+  g.spec = static_cast<const uint8_t *>(spec);
+  g.nrows = nrows;
+  g.kpad = kpad;
+  g.K = K;
+  g.nstreams = nstreams;
+  g.npad = npad;
+  g.nbl = nbl;
+  g.nbins = rowlist ? nbins : 1;
+  g.rowlist = rowlist;
+  g.list_len = list_len;
+  g.segs = rowlist ? segs : nullptr;
+  g.blmap = blmap;
+  g.inv_scale2 = inv_scale2;
+  g.acc = acc;
+  g.err = err;
+  auto up16 = [](int x) { return (x + 15) & ~15; };
+  auto up32 = [](int x) { return (x + 31) & ~31; };
+  const int comps = 4 * nstreams;
+  g.n0 = up16(std::min(comps, 256));
+  g.n1 = comps > 128 ? up16(comps - 128) : 0;
+  g.col1 = up32(g.n0);
+  g.buf_stride = g.col1 + up32(g.n1);
+  g.nbuf = std::min(4, 512 / g.buf_stride);
+  if (slots == kTcSlots) return launch_gather<kTcSlots>(g, st);
+  return launch_gather<kTcSlotsWide>(g, st);
+}
+
+void launch_pulsar_sort(const int16_t *bins, int nrows, int K, int nbins, int list_len, int *rowlist, int2 *segs,
+                        cudaStream_t st) {
+  const size_t smem = (size_t)4 * 2 * nbins * sizeof(int);
+  if (smem > 48 * 1024) cudaFuncSetAttribute(pulsar_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  pulsar_sort_kernel<<<(K + 3) / 4, 128, smem, st>>>(bins, nrows, K, nbins, list_len, rowlist, segs);
 }
 
 }  // namespace sfxc

@@ -174,6 +174,13 @@ class CorrelatorNode:
         self._check(self._lib.sfxc_gpu_copy_spectra(self._h, stream, out.ctypes.data, out.size * 2))
         return out
 
+    def pulsar_bins(self, nrows, nchan):
+        """Pulsar bin of every FFT row and channel of the last integration:
+        int32 [nrows][nchan + 1] (0 off-pulse)."""
+        out = np.zeros((nrows, nchan + 1), dtype=np.int32)
+        self._check(self._lib.sfxc_gpu_copy_pulsar_bins(self._h, out.ctypes.data, out.size))
+        return out
+
     def spectra_noalloc(self, stream, nrows, nchan):
         """spectra() through the allocation-free entry point (static device scratch)."""
         out = np.empty((nrows, nchan + 1), dtype=np.complex64)
@@ -354,9 +361,11 @@ class OutputFiles:
     in-memory files: `files[f]` holds file f's bytes, starting with the global
     header.  global_fields: experiment, start_year, start_day, start_time,
     number_channels, integration_time_us, correlator_version,
-    polarisation_type, correlator_branch, job_nr, subjob_nr.  Host only."""
+    polarisation_type, correlator_branch, job_nr, subjob_nr.  refuse_files:
+    file indices whose writes the sink refuses after the global header (a
+    full disk, say).  Host only."""
 
-    def __init__(self, n_files, **global_fields):
+    def __init__(self, n_files, refuse_files=(), **global_fields):
         self._lib = L.load()
         g = L.OutputGlobal()
         sizes = {"experiment": 32, "correlator_branch": 15}
@@ -364,7 +373,11 @@ class OutputFiles:
             setattr(g, k, v.encode()[:sizes[k]] if isinstance(v, str) else v)
         self.files = [bytearray() for _ in range(n_files)]
 
+        refuse = set(refuse_files)
+
         def sink(user, kind, data, n):
+            if kind in refuse and len(self.files[kind]) > 0:
+                return 1
             self.files[kind] += C.string_at(data, n)
             return 0
 

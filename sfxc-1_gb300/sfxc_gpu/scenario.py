@@ -168,11 +168,26 @@ def build_job(sc: Scenario, delay_fn, protocol_fn, fast_random=False):
                 n_phase_centers=1 + len(sc.extra_centers), streams=streams, protocols=protos)
 
 
-def build_job_bulk(sc: Scenario, alloc=None):
+def bulk_stream_bytes(sc: Scenario, k=0):
+    """Channel bytes build_job_bulk records for stream k (whole input-node
+    blocks covering the lead, the integrations and the largest delay)."""
+    si, _ = sc.streams()[k]
+    sr_k, bits_k, _ = sc.station_modes.get(sc.stations[si].number, (sc.sample_rate, sc.bits, 0))
+    max_tau = max(abs(float(st.poly.delay(sc.sec0 + sc.lead_us * 1e-6))) for st in sc.stations)
+    spb_block = sc.block_bytes * 8 // bits_k
+    span = sc.lead_us * sr_k // 1_000_000 + sc.n_integrations * (sc.integration_us * sr_k // 1_000_000)
+    nsamp = span + int(max_tau * sr_k) + 4 * spb_block
+    return (nsamp + spb_block - 1) // spb_block * sc.block_bytes
+
+
+def build_job_bulk(sc: Scenario, alloc=None, codes=None):
     """Large jobs: uniformly random 2-bit/1-bit codes generated per stream and
     turned straight into protocol bytes by the library's input-node writer
     (no per-block Python objects).  alloc(n) may supply the protocol buffers
-    (pinned host memory for end-to-end timing).  No invalid runs."""
+    (pinned host memory for end-to-end timing); codes(k, nbytes), if given,
+    supplies stream k's channel bytes instead of the uniform codes (at least
+    nbytes; e.g. the signal model of synth.model_codes_torch).  No invalid
+    runs."""
     from . import correlator
     dels = del_tables(sc)
     rec0, start, tint, slice_samples = job_timing(sc)
@@ -189,8 +204,11 @@ def build_job_bulk(sc: Scenario, alloc=None):
         nsamp = span + int(max_tau * sr_k) + 4 * spb_block
         nblocks = (nsamp + spb_block - 1) // spb_block
         starts = rec0 + np.arange(nblocks, dtype=np.int64) * spb_block * tps
-        rng = np.random.Generator(np.random.PCG64(sc.seed * 7919 + k))
-        data = rng.integers(0, 256, size=nblocks * sc.block_bytes, dtype=np.uint8)
+        if codes is not None:
+            data = np.ascontiguousarray(codes(k, nblocks * sc.block_bytes)[:nblocks * sc.block_bytes])
+        else:
+            rng = np.random.Generator(np.random.PCG64(sc.seed * 7919 + k))
+            data = rng.integers(0, 256, size=nblocks * sc.block_bytes, dtype=np.uint8)
         slices = []
         for it in range(sc.n_integrations):
             s0 = start + it * tint
@@ -234,3 +252,25 @@ def cubic_stations(n, seed, max_delay=15e-3, max_rate=3e-6, t0=36000.0, gains=No
         g = 1.0 if gains is None else gains[i]
         out.append(Station("S%d" % i, i, synth.DelayPoly(coeffs=(c0, c1, c2, c3), t0=t0), g))
     return out
+
+
+def pulsar_params(sc: Scenario, nbins=256, gate=(0.0, 1.0), period=0.0334, dm=56.8, obs_freq=1400.0, n_coef=12):
+    """Pulsar binning of a job (the ctrl file's pulsar block and one polyco):
+    `nbins` on-pulse bins over `gate` plus the off-pulse bin, and one polyco
+    of n_coef coefficients, all zero -- a constant spin frequency 1/period --
+    with its midpoint at the job's first integration.  Returned as the job
+    keys "pulsar" and "polyco"."""
+    tmid = sc.mjd + (sc.sec0 + sc.lead_us * 1e-6) / 86400.0
+    polyco = (tmid, dm, 0.0, 1.0 / period, obs_freq) + (0.0,) * n_coef
+    return {"pulsar": (nbins,) + tuple(gate), "polyco": [polyco]}
+
+
+def c5_pulsar(n_stations=10, integration_us=1_000_000, subband=0, seed=5, n_integrations=1):
+    """The pulsar configuration's subband job: n_stations dual-pol stations at
+    16 MHz (32 MS/s), 2-bit, 2048 channels, sky frequency 1.4 GHz + 16 MHz per
+    subband, cubic delay models."""
+    st = cubic_stations(n_stations, seed=500 + seed, max_delay=1e-2, max_rate=3e-6)
+    return Scenario(stations=st, pols=("R", "L"), sample_rate=32_000_000, bandwidth=16_000_000, bits=2,
+                    channel_freq=1_400_000_000 + subband * 16_000_000, nchan=2048, integration_us=integration_us,
+                    n_integrations=n_integrations, sub_integration_us=125000, lead_us=12000, seed=seed + subband,
+                    block_bytes=2000, frequency_nr=subband)

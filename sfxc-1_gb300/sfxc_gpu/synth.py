@@ -405,3 +405,101 @@ def mark5b_recording(nframes: int, *, mjd: int, sec_of_day: int, frames_per_seco
                 payload[4 * w0:4 * (w0 + nw)] = struct.pack("<I", VDIF_FILL_WORD) * nw
         out += bytes(h) + bytes(payload)
     return bytes(out)
+
+
+# --------------------------------------------------------------------------
+# the same signal model at benchmark sizes, on a GPU with torch
+# --------------------------------------------------------------------------
+@dataclass
+class PulseModel:
+    """A pulsar in the sky signal: amplitude 1 + peak * exp(-(phi - 1/2)^2 / (2 w^2))
+    for pulse phase phi = frac((T - t_ref) / period), its arrival delayed by the
+    dispersion delay 4148.808 DM / f_MHz^2 s at the subband's centre frequency
+    (no sweep within the subband); w from the duty cycle (FWHM)."""
+    period: float = 0.0334
+    duty: float = 0.05
+    peak: float = 20.0
+    dm: float = 56.8
+    t_ref: float = 0.0
+
+
+def model_codes_torch(stations, pols, sample_rate, f_lo, n_samples, start_sec_of_day, rho, seed, tones=(),
+                      pulse: PulseModel | None = None, band_centre_hz=None, device="cuda", chunk=1 << 24):
+    """Yields ((station index, pol), packed 2-bit codes as a numpy uint8 array)
+    for every stream in correlator order, generated on the GPU.
+
+    The model of generate_station_samples -- the analytic sky signal a seen at
+    T with T + tau_i(T) = t, fringe phase -2 pi f_lo tau_i(T) in FP64, gain g_i,
+    correlated fraction rho, common RFI tones (amplitude in units of the
+    unit-variance noise) -- with two simplifications that keep it fast at
+    tens of gigasamples: the sky signal is taken at the nearest sample of T
+    (no fractional interpolation), and a pulsar, if any, modulates the sky
+    signal's amplitude.  2-bit quantisation at +-0.98 sigma of each stream."""
+    import torch
+    sr = float(sample_rate)
+    max_tau = 0.0
+    for st in stations:
+        max_tau = max(max_tau, float(np.max(np.abs(st.poly.delay(
+            np.array([start_sec_of_day, start_sec_of_day + n_samples / sr]))))))
+    margin = int(max_tau * sr) + 1024
+    n_sky = n_samples + 2 * margin
+    n_sky += n_sky & 1
+    gen = torch.Generator(device=device)
+    for pi, pol in enumerate(pols):
+        gen.manual_seed(seed * 100 + pi)
+        sky = torch.randn(n_sky, generator=gen, device=device, dtype=torch.float32)
+        F = torch.fft.rfft(sky)
+        del sky
+        A = torch.zeros(n_sky, dtype=torch.complex64, device=device)
+        A[:F.numel()] = 2.0 * F
+        A[0] = F[0]
+        A[n_sky // 2] = F[n_sky // 2]
+        del F
+        a = torch.fft.ifft(A)  # analytic signal, real part = the sky signal
+        del A
+        for si, st in enumerate(stations):
+            c = torch.tensor(st.poly.coeffs, dtype=torch.float64, device=device)
+
+            def tau(t):
+                x = t - st.poly.t0
+                r = torch.zeros_like(x)
+                for k in range(c.numel() - 1, -1, -1):
+                    r = r * x + c[k]
+                return r
+
+            gen.manual_seed(seed * 1000 + 17 + si * 7 + pi)
+            x = torch.empty(n_samples, dtype=torch.float32, device=device)
+            for c0 in range(0, n_samples, chunk):
+                c1 = min(n_samples, c0 + chunk)
+                t = start_sec_of_day + torch.arange(c0, c1, dtype=torch.float64, device=device) / sr
+                T = t - tau(t)
+                for _ in range(4):
+                    T = t - tau(T)
+                pos = torch.round((T - start_sec_of_day) * sr).to(torch.int64) + margin
+                sig = a[pos]
+                ph = -f_lo * tau(T)
+                ph = (ph - torch.floor(ph)).to(torch.float32) * (2.0 * math.pi)
+                s = sig.real * torch.cos(ph) - sig.imag * torch.sin(ph)
+                if pulse is not None:
+                    fc = (band_centre_hz if band_centre_hz is not None else f_lo) * 1e-6
+                    tp = T - pulse.t_ref - 4148.808 * pulse.dm / (fc * fc)
+                    phi = tp / pulse.period
+                    phi = (phi - torch.floor(phi)).to(torch.float32)
+                    w = pulse.duty / 2.3548
+                    s = s * (1.0 + pulse.peak * torch.exp(-((phi - 0.5) ** 2) / (2 * w * w)))
+                noise = torch.randn(c1 - c0, generator=gen, device=device, dtype=torch.float32)
+                xs = st.gain * (math.sqrt(rho) * s + math.sqrt(1.0 - rho) * noise)
+                for (ftone, amp) in tones:
+                    tph = ftone * (t - start_sec_of_day)
+                    tph = (tph - torch.floor(tph)).to(torch.float32) * (2.0 * math.pi)
+                    xs = xs + amp * torch.cos(tph)
+                x[c0:c1] = xs
+            sigma = float(x.double().std())
+            thr = THRESH_2BIT * sigma
+            codes = (x >= -thr).to(torch.uint8) + (x >= 0).to(torch.uint8) + (x >= thr).to(torch.uint8)
+            del x
+            n4 = codes.numel() // 4 * 4
+            q = codes[:n4].view(-1, 4)
+            packed = q[:, 0] | (q[:, 1] << 2) | (q[:, 2] << 4) | (q[:, 3] << 6)
+            yield (si, pol), packed.cpu().numpy()
+        del a

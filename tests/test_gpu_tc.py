@@ -21,7 +21,7 @@ def tc_node(sfxc_lib):
     node.close()
 
 
-@pytest.mark.parametrize("case", ["c1_plain", "multi", "onebit", "reduced", "reduced_mask", "phase_centers", "phased"])
+@pytest.mark.parametrize("case", ["c1_plain", "multi", "onebit", "pulsar", "reduced", "reduced_mask", "phase_centers", "phased"])
 def test_tc_golden(case, tc_node):
     from sfxc_gpu import correlator
     g = Golden(case)

@@ -90,3 +90,27 @@ def test_errors(sfxc_lib):
     with pytest.raises(lib.SfxcError):
         out.put_slice(0, bytes(bad))
     out.close()
+
+
+def test_sink_refusal_fails_the_output(sfxc_lib):
+    """A sink that refuses one bin's file stops the slice part way: the files
+    before it already hold their part, so the slice is not written again and
+    every later call fails instead of duplicating those bytes."""
+    from sfxc_gpu import correlator, lib
+    g = Golden("pulsar")
+    nbins = int(g.meta["pulsar"][0]) + 1
+    per = len(g.cor) // nbins
+    out = correlator.OutputFiles(nbins, refuse_files=(3,), **_fields(HEADERS[0]))
+    with pytest.raises(lib.SfxcError):
+        out.put_slice(0, g.cor, nbins)
+    with pytest.raises(lib.SfxcError) as e:
+        out.put_slice(1, g.cor, nbins)
+    assert e.value.code == lib.ESTATE
+    with pytest.raises(lib.SfxcError) as e:
+        out.finish()
+    assert e.value.code == lib.ESTATE
+    header = bytes.fromhex(HEADERS[0]["header_hex"])
+    for b in range(nbins):
+        want = header + (g.cor[b * per + 4:(b + 1) * per] if b < 3 else b"")
+        assert bytes(out.files[b]) == want, b
+    out.close()

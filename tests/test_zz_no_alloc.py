@@ -1,9 +1,9 @@
 """The allocation-free spectra entry point (sfxc_gpu_copy_spectra_noalloc).
 
 It serves callers that cannot allocate device memory when they inspect a
-stream -- inside CUDA graph capture, in real-time loops with no time for the
-allocator, or on hosts that hand out GPU memory once at start-up -- by keeping
-its scratch in a fixed static device array.  Through the C ABI it must give
+stream -- real-time loops with no time for the allocator (which may wait for
+the whole device), or hosts that hand out GPU memory once at start-up -- by
+keeping its scratch in a fixed static device array.  Through the C ABI it must give
 the same delay-corrected spectra as sfxc_gpu_copy_spectra, on two calls in a
 row (the array keeps the previous call's contents), and reject requests larger
 than its array.  Collected last so that a stop-at-first-failure run has run
