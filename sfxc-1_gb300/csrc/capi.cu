@@ -168,6 +168,7 @@ struct sfxc_gpu_ctx {
   DevBuf streamdev, tw256, ts, spec, acc, out, norms, flagfac, blmap, tiles, blpairs, items, bins,
       offsets, derr;
   DevBuf rowlist, segs;  // pulsar binning on the tensor cores: rows of each channel sorted by bin, and the runs
+  DevBuf xpart;          // FP32 X-step: partial sums of its row blocks
   int bins_rows = 0;     // rows of the last integration's bin table (pulsar)
   DevBuf xin, xtracks, xout;  // channel extraction
   // per windowed-FFT length (streams of different sample rates): window and
@@ -751,6 +752,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   c->spec.ensure((size_t)(tc_x ? tc_slots : N) * (tc_x ? (max_rows + 7) / 8 * 8 : max_rows) * kpad * sizeof(float2));
   c->derr.ensure(sizeof(int));
   CK(cudaMemsetAsync(c->derr.p, 0, sizeof(int), st));
+  if (!tc_x && !pulsar && !c->phased)
+    c->xpart.ensure(std::max<size_t>(16, xcorr_f32_scratch_bytes(c->jt.ntiles, c->jt.npad, K, max_rows, nbl, kpad)));
   // two sets of per-block records: chunk ch uses set ch & 1, so the next
   // chunk's are computed while the current chunk is still transformed
   for (int i = 0; i < N; i++) {
@@ -940,7 +943,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
         launches += 1;
       } else {
         launch_xcorr_f32(c->spec.as<float2>(), max_rows, kpad, N, c->jt.npad, 0, nrows, K, c->tiles.as<int>(),
-                         c->jt.ntiles, c->blmap.as<int>(), nbl, c->bins.as<int16_t>(), nrows, c->acc.as<float2>(), st);
+                         c->jt.ntiles, c->blmap.as<int>(), nbl, c->bins.as<int16_t>(), nrows, c->acc.as<float2>(),
+                         nullptr, 0, st);
       }
     } else if (tc_tma) {
       if (nrows % 8)
@@ -954,7 +958,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
                                 st));
     } else {
       launch_xcorr_f32(c->spec.as<float2>(), max_rows, kpad, N, c->jt.npad, 0, nrows, K, c->tiles.as<int>(),
-                       c->jt.ntiles, c->blmap.as<int>(), nbl, nullptr, 0, c->acc.as<float2>(), st);
+                       c->jt.ntiles, c->blmap.as<int>(), nbl, nullptr, 0, c->acc.as<float2>(), c->xpart.as<float2>(),
+                       c->xpart.cap, st);
     }
     CK(cudaGetLastError());
     if (c->npc > 1) {  // the sub-integration into every phase centre

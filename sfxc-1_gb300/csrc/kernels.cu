@@ -441,9 +441,10 @@ __device__ __forceinline__ void window_apply(float2 (&v)[16], int t, int nper, c
 template <int N, int NS, int OUT_TC, bool SCALE>
 __device__ __forceinline__ void store_row(const float2 *Z, int BUF, const int2 *sinfo, int NV, bool fast, int row,
                                           int nrows_total, int M, int kpad, const float2 *__restrict__ tw_rot,
-                                          void *__restrict__ spec_out, float tc_scale, int S, int tid, int nthr) {
+                                          void *__restrict__ spec_out, float tc_scale, int tid, int nthr) {
+  constexpr int S = OUT_TC;  // slots of the tensor-core layout (0: FP32 layout)
   static_assert(NS <= 4, "at most four streams per CTA");
-  if (OUT_TC) {
+  if constexpr (OUT_TC != 0) {
     constexpr int W = NS;  // streams per store
     uint2 *dst = reinterpret_cast<uint2 *>(spec_out);
     if (fast) {
@@ -542,12 +543,13 @@ struct WinShape {
   static_assert(THREADS <= 1024, "at most 1024 threads");
 };
 
+// OUT_TC: 0 writes the FP32 layout, 32 or 64 the tensor-core layout with that many slots
 template <int LOGN, int OUT_TC, int SPCMAX>
 __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinShape<LOGN, SPCMAX>::THREADS)
     window_fft_kernel(
     const StreamDev *__restrict__ streams, int nstreams, int row0, int nrows, int nrows_total, int steps_per_cta,
     const float *__restrict__ window, const float2 *__restrict__ tw_rot, int nper, int M, int kpad,
-    void *__restrict__ spec_out, float tc_scale, int tc_slots) {
+    void *__restrict__ spec_out, float tc_scale) {
   using S = WinShape<LOGN, SPCMAX>;
   constexpr int N = S::N, T = S::T, SPC = S::SPC, RPC = S::RPC;
   extern __shared__ __align__(16) float2 dsm[];
@@ -630,7 +632,7 @@ __global__ void __launch_bounds__(WinShape<LOGN, SPCMAX>::THREADS, 1024 / WinSha
       const int row = k * RPC + r;
       if (row >= nrows) break;
       store_row<N, SPC, OUT_TC, !S::WSMEM>(dsm + r * SPC * S::BUF, S::BUF, sinfo, nv, fast, row0 + row, nrows_total,
-                                           M, kpad, tw_rot, spec_out, tc_scale, tc_slots, threadIdx.x, S::THREADS);
+                                           M, kpad, tw_rot, spec_out, tc_scale, threadIdx.x, S::THREADS);
     }
     // the next step's FFT rewrites the buffers (placing this barrier inside
     // that FFT, after its first radix-16 pass, measured 1.7 % slower)
@@ -833,7 +835,10 @@ __global__ void __launch_bounds__(384, 1) xcorr_f32_kernel(const __grid_constant
 #pragma unroll
         for (int q = 0; q < 4; q++) v[t][p][q] = make_float2(0.f, 0.f);
     }
-    // add the register tiles to acc[bin] (bin 0 when not binned) and clear them
+    // add the register tiles to acc[bin] (bin 0 when not binned), or store
+    // them as this row block's partial sums (a.part), and clear them.  Each
+    // (bin, baseline, channel) entry has one writer thread per launch (or per
+    // row block with partial sums), so the results do not depend on timing.
     auto flush = [&](int bin) {
       if (k >= a.K || bin < 0) return;
 #pragma unroll
@@ -846,8 +851,15 @@ __global__ void __launch_bounds__(384, 1) xcorr_f32_kernel(const __grid_constant
             const int m = __ldg(a.blmap + (ti[t] * 4 + p) * a.npad + tj[t] * 4 + q);
             if (m >= 0) {
               const float2 x = v[t][p][q];
-              atomicAdd(a.acc + ((int64_t)bin * a.nbl + (m >> 1)) * a.kpad + k,
-                        make_float2(x.x, (m & 1) ? -x.y : x.y));
+              const float2 y = make_float2(x.x, (m & 1) ? -x.y : x.y);
+              if (a.part) {
+                a.part[((int64_t)rb * a.nbl + (m >> 1)) * a.kpad + k] = y;
+              } else {
+                // the entry's only writer in this launch: its adds land in
+                // program order, so the sum does not depend on timing; the
+                // atomic lets the thread go on without waiting for the load
+                atomicAdd(a.acc + ((int64_t)bin * a.nbl + (m >> 1)) * a.kpad + k, y);
+              }
             }
             v[t][p][q] = make_float2(0.f, 0.f);
           }
@@ -916,6 +928,19 @@ __global__ void __launch_bounds__(384, 1) xcorr_f32_kernel(const __grid_constant
     flush(BINNED ? cur : 0);
     __syncthreads();  // the ring is refilled by the next item
   }
+}
+
+// Partial sums of the row blocks into the accumulators, in row-block order.
+__global__ void f32_part_reduce_kernel(const float2 *__restrict__ part, int nrb, int nbl, int kpad, int K,
+                                       float2 *__restrict__ acc) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+  if (k >= K) return;
+  float2 s = acc[(int64_t)b * kpad + k];
+  for (int r = 0; r < nrb; r++) {
+    const float2 x = part[((int64_t)r * nbl + b) * kpad + k];
+    s = make_float2(s.x + x.x, s.y + x.y);
+  }
+  acc[(int64_t)b * kpad + k] = s;
 }
 
 // ------------------------------------------------------------------------
@@ -1237,7 +1262,7 @@ static void window_fft_launch_spc(const StreamDev *d_streams, int nstreams, int 
   auto kern = window_fft_kernel<LOGN, OUT_TC, SPCMAX>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
   kern<<<grid, S::THREADS, S::SMEM, st>>>(d_streams, nstreams, row0, nrows, nrows_total, steps_per_cta, window, tw_rot,
-                                          nper, M, kpad, spec, tc_scale, tc_slots);
+                                          nper, M, kpad, spec, tc_scale);
 }
 
 template <int LOGN, int OUT_TC>
@@ -1267,10 +1292,14 @@ void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int n
                        int tc_slots, float tc_scale, cudaStream_t st) {
   const int logn = 30 - __builtin_clz((unsigned)rot);  // log2(rot / 2)
 #define SFXC_WIN(L)                                                                                            \
-  (tc_slots ? window_fft_launch<L, 1>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, \
-                                      kpad, spec, tc_scale, tc_slots, st)                                     \
-            : window_fft_launch<L, 0>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, \
-                                      kpad, spec, tc_scale, 0, st))
+  (tc_slots == kTcSlots                                                                                         \
+       ? window_fft_launch<L, kTcSlots>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M,  \
+                                        kpad, spec, tc_scale, tc_slots, st)                                   \
+   : tc_slots == kTcSlotsWide                                                                                    \
+       ? window_fft_launch<L, kTcSlotsWide>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, \
+                                            M, kpad, spec, tc_scale, tc_slots, st)                            \
+       : window_fft_launch<L, 0>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad,    \
+                                 spec, tc_scale, 0, st))
   SFXC_LOGN_SWITCH(logn, SFXC_WIN)
 #undef SFXC_WIN
 }
@@ -1326,12 +1355,42 @@ static void f32_launch(const F32Args &a, const F32Plan &p, bool binned, cudaStre
   kern<<<std::min(nitems, sm_count()), p.warps * 32, p.smem, st>>>(a);
 }
 
+// Row blocks of the unbinned FP32 X-step: about four work items per SM keep
+// the CTAs balanced; each block's partial sums go to scratch and are added in
+// block order.  Binned (pulsar) launches keep all rows in one block.
+static int f32_row_blocks(const F32Plan &p, int K, int nrows) {
+  const int nct = (K + 31) / 32;
+  return std::max(1, std::min((nrows + p.R - 1) / p.R, (4 * sm_count() + nct * p.nparts - 1) / (nct * p.nparts)));
+}
+
+size_t xcorr_f32_scratch_bytes(int ntiles, int npad, int K, int nrows, int nbl, int kpad) {
+  const F32Plan p = xcorr_f32_plan(ntiles, npad);
+  if (p.tpw <= 0 || nrows <= 0) return 0;
+  const int nrb = f32_row_blocks(p, K, nrows);
+  return nrb > 1 ? (size_t)nrb * nbl * kpad * sizeof(float2) : 0;
+}
+
 void launch_xcorr_f32(const float2 *spec, int nrows_total, int kpad, int nstreams, int npad, int r0, int r1, int K,
                       const int *tiles, int ntiles, const int *blmap, int nbl, const int16_t *bins, int bins_rows,
-                      float2 *acc, cudaStream_t st) {
+                      float2 *acc, float2 *scratch, size_t scratch_bytes, cudaStream_t st) {
   if (r1 <= r0 || K <= 0) return;
-  const F32Plan p = xcorr_f32_plan(ntiles, npad);
+  F32Plan p = xcorr_f32_plan(ntiles, npad);
   if (p.tpw <= 0) return;
+  const bool binned = bins != nullptr;
+  if (binned) {
+    // binned launches keep every row of a channel in one work item (each
+    // accumulator entry has one writer); finer parts of the tile set give the
+    // SMs enough items (each part stages the rows again, mostly from L2)
+    const int nct = (K + 31) / 32;
+    const int np = std::min(ntiles, std::max(p.nparts, (2 * sm_count() + nct - 1) / nct));
+    if (np > p.nparts) {
+      p.nparts = np;
+      p.tiles_per_part = (ntiles + np - 1) / np;
+      for (p.tpw = 1; p.tpw < 3 && (p.tiles_per_part + p.tpw - 1) / p.tpw > 12; p.tpw++) {
+      }
+      p.warps = (p.tiles_per_part + p.tpw - 1) / p.tpw;
+    }
+  }
   F32Args a;
   a.spec = spec;
   a.nrows_total = nrows_total;
@@ -1351,16 +1410,20 @@ void launch_xcorr_f32(const float2 *spec, int nrows_total, int kpad, int nstream
   a.bins = bins;
   a.bins_rows = bins_rows;
   a.acc = acc;
-  // blocks of rows so that about four items per SM keep the CTAs balanced
-  const int nct = (K + 31) / 32, nrows = r1 - r0;
-  const int nrb = std::max(1, std::min((nrows + p.R - 1) / p.R, (4 * sm_count() + nct * p.nparts - 1) / (nct * p.nparts)));
+  a.part = nullptr;
+  const int nrows = r1 - r0;
+  int nrb = binned ? 1 : f32_row_blocks(p, K, nrows);
+  if (nrb > 1 && (!scratch || scratch_bytes < (size_t)nrb * nbl * kpad * sizeof(float2))) nrb = 1;
   a.rblock = ((nrows + nrb - 1) / nrb + p.R - 1) / p.R * p.R;
-  const bool binned = bins != nullptr;
+  nrb = (nrows + a.rblock - 1) / a.rblock;
+  if (nrb > 1) a.part = scratch;
   switch (p.tpw) {
     case 1: f32_launch<1>(a, p, binned, st); break;
     case 2: f32_launch<2>(a, p, binned, st); break;
     default: f32_launch<3>(a, p, binned, st); break;
   }
+  if (nrb > 1)
+    f32_part_reduce_kernel<<<dim3((K + 255) / 256, nbl), 256, 0, st>>>(scratch, nrb, nbl, kpad, K, acc);
 }
 
 void launch_pulsar_bins(int nrows, int K, double start_phase, double rate_term, double fft_duration,

@@ -36,6 +36,7 @@ struct F32Args {
   const int16_t *bins;  // binned (pulsar): [channel][row] with row stride bins_rows, row 0 = r0; else NULL
   int bins_rows;
   float2 *acc;          // [bin][baseline][kpad]
+  float2 *part;         // non-NULL: each row block's partial sums [block][baseline][kpad], added later in order
 };
 struct F32Plan {
   int nparts = 0, tiles_per_part = 0, tpw = 0, warps = 0, R = 0;
@@ -43,10 +44,15 @@ struct F32Plan {
 };
 // tpw == 0: the streams do not fit (npad x 256 B over 128 KB of staging)
 F32Plan xcorr_f32_plan(int ntiles, int npad);
-// rows [r0, r1) of spec into acc; bins != NULL: binned, acc[bins[k][r - r0]]
+// Scratch the unbinned FP32 X-step wants for its row blocks' partial sums
+// (0: one block); with less, it runs the rows as one block.
+size_t xcorr_f32_scratch_bytes(int ntiles, int npad, int K, int nrows, int nbl, int kpad);
+// rows [r0, r1) of spec into acc; bins != NULL: binned, acc[bins[k][r - r0]].
+// Deterministic: every accumulator entry has one writer, partial sums are
+// added in a fixed order.
 void launch_xcorr_f32(const float2 *spec, int nrows_total, int kpad, int nstreams, int npad, int r0, int r1, int K,
                       const int *tiles, int ntiles, const int *blmap, int nbl, const int16_t *bins, int bins_rows,
-                      float2 *acc, cudaStream_t st);
+                      float2 *acc, float2 *scratch, size_t scratch_bytes, cudaStream_t st);
 // pulsar bin of every (row, channel), FP64 in the reference's order: bins[k * nrows + r]
 void launch_pulsar_bins(int nrows, int K, double start_phase, double rate_term, double fft_duration,
                         const double *offsets, double g0, double g1, int nbins, int16_t *bins, cudaStream_t st);

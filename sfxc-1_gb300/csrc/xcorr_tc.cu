@@ -272,19 +272,74 @@ struct GatherArgs {
   int *err;
   int n0, n1, col1;     // MMA N of blocks 0 and 1 (n1 = 0: one block), TMEM column of block 1
   int buf_stride, nbuf; // TMEM columns per buffer, number of buffers
+  int accumulate;       // 0: every (bin, channel) segment is the only one of its launch and is stored as it is
 };
+
+constexpr int kMaxBufs = 8;
 
 __device__ __forceinline__ int2 gather_seg(const GatherArgs &g, int ch, int bin) {
   if (!g.segs) return make_int2(0, (g.nrows + 15) & ~15);
   return g.segs[(size_t)ch * g.nbins + bin];
 }
 
+// One K-tile of a segment.
+struct GTile {
+  int ch, bin, e0, rows;  // channel, bin, first list entry, rows (a multiple of 16)
+  bool first, last;       // first / last tile of its segment
+};
+
+// The K-tiles of this CTA in processing order: channel groups of four
+// (group blockIdx.x, then + gridDim.x); within a group bin by bin; within a
+// bin the group's four channels; within a segment 64 rows at a time.  The
+// four channels of a group read the four 32-byte pieces of the same 128-byte
+// spectra lines and write the same 32-byte accumulator sectors close together
+// in time.  Every role of the kernel walks the same sequence.
+struct GWalk {
+  int grp, bin, c, t0;
+  int2 sg;
+  __device__ void init() {
+    grp = blockIdx.x;
+    bin = 0;
+    c = -1;
+    t0 = 0;
+    sg = make_int2(0, 0);
+  }
+  __device__ bool next(const GatherArgs &g, int ngroups, GTile &t) {
+    if (t0 + 64 < sg.y) {  // more rows in the current segment
+      t0 += 64;
+    } else {
+      for (;;) {  // the next non-empty segment
+        if (++c == 4) {
+          c = 0;
+          if (++bin == g.nbins) {
+            bin = 0;
+            grp += gridDim.x;
+          }
+        }
+        if (grp >= ngroups) return false;
+        const int ch = 4 * grp + c;
+        if (ch >= g.K) continue;
+        sg = gather_seg(g, ch, bin);
+        if (sg.y > 0) break;
+      }
+      t0 = 0;
+    }
+    t.ch = 4 * grp + c;
+    t.bin = bin;
+    t.e0 = sg.x + t0;
+    t.rows = min(64, sg.y - t0);
+    t.first = t0 == 0;
+    t.last = t0 + 64 >= sg.y;
+    return true;
+  }
+};
+
 template <int S>
 __global__ void __launch_bounds__(GatherShape<S>::kThreads, 1) xcorr_tc_gather_kernel(const __grid_constant__ GatherArgs g) {
   using G = GatherShape<S>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);  // stages 1 KB aligned
-  __shared__ uint64_t full[G::kStages], empty[G::kStages], tfull[4], tempty[4], done;
+  __shared__ uint64_t full[G::kStages], empty[G::kStages], tfull[kMaxBufs], tempty[kMaxBufs], done;
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -294,7 +349,7 @@ __global__ void __launch_bounds__(GatherShape<S>::kThreads, 1) xcorr_tc_gather_k
       mbar_init(&full[s], G::kProducers);
       mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < 4; b++) {
+    for (int b = 0; b < kMaxBufs; b++) {
       mbar_init(&tfull[b], 1);
       mbar_init(&tempty[b], 8);  // one arrival per epilogue warp
     }
@@ -307,40 +362,64 @@ __global__ void __launch_bounds__(GatherShape<S>::kThreads, 1) xcorr_tc_gather_k
   fence_after_sync();
   const uint32_t tmem = tmem_base;
   volatile int *vfailed = &failed;
+  const int ngroups = (g.K + 3) / 4;
+  GWalk walk;
+  walk.init();
+  GTile t;
 
   if (tid < G::kProducers) {
-    // ---- producers: every K-tile of every segment of this CTA's channels
-    int it = 0;
-    bool stop = false;
-    for (int ch = blockIdx.x; ch < g.K && !stop; ch += gridDim.x) {
-      const int *list = g.rowlist ? g.rowlist + (size_t)ch * g.list_len : nullptr;
-      for (int bin = 0; bin < g.nbins && !stop; bin++) {
-        const int2 sg = gather_seg(g, ch, bin);
-        for (int t0 = 0; t0 < sg.y; t0 += G::kRows, it++) {
-          const int rows = min(G::kRows, sg.y - t0);
-          const int s = it % G::kStages, n = it / G::kStages;
-          if ((n > 0 && !mbar_wait(&empty[s], (n - 1) & 1)) || *vfailed) {
-            *vfailed = 1;
-            stop = true;
-            break;
-          }
-          const uint32_t st = smem_u32(base + s * G::kStageBytes);
-          for (int c = tid; c < rows * (S / 2); c += G::kProducers) {
-            const int j = c / (S / 2), q = (c % (S / 2)) >> 1, h = c & 1;
-            const int e = sg.x + t0 + j;
-            const int row = list ? __ldg(list + e) : e;
-            const bool ok = row >= 0 && row < g.nrows;
-            const uint8_t *src = ok ? g.spec + tc_index(row, g.kpad, ch, 4 * q, S) * 8 + 16 * h : g.spec;
-            cp_async16(st + (j >> 3) * G::kGroupBytes + q * 256 + sw32_offset(j & 7, h), src, ok ? 16u : 0u);
-          }
-          asm volatile("cp.async.commit_group;" ::: "memory");
-          if (it > 0) {  // the previous tile has landed: publish it to the tensor cores
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_arrive(&full[(it - 1) % G::kStages]);
-          }
-        }
+    // ---- producers: thread tid copies, for every row j = j0 + RP i of a
+    // tile, the 16-byte half h of slot quad q (quads one 128-byte line
+    // apart); the row-list entries of the next tile load while the current
+    // tile is issued
+    constexpr int CPR = S / 2;               // 16-byte chunks per row
+    constexpr int RP = G::kProducers / CPR;  // rows per pass
+    constexpr int E = G::kRows / RP;         // rows per thread and tile
+    const int j0 = tid / CPR, q = (tid % CPR) >> 1, h = tid & 1;
+    const uint32_t soff = q * 256;
+    const int64_t rstride = (int64_t)g.kpad * S * 8;  // bytes per row
+    int rcur[E], rnxt[E];
+    auto load_rows = [&](const GTile &x, int(&r)[E]) {
+      const int *list = g.rowlist ? g.rowlist + (size_t)x.ch * g.list_len : nullptr;
+#pragma unroll
+      for (int i = 0; i < E; i++) {
+        const int j = j0 + RP * i;
+        r[i] = j < x.rows ? (list ? __ldg(list + x.e0 + j) : x.e0 + j) : -2;
       }
+    };
+    GTile cur, nxt;
+    bool have = walk.next(g, ngroups, cur);
+    if (have) load_rows(cur, rcur);
+    int it = 0;
+    while (have) {
+      const bool have_next = walk.next(g, ngroups, nxt);
+      if (have_next) load_rows(nxt, rnxt);
+      const int s = it % G::kStages, n = it / G::kStages;
+      if ((n > 0 && !mbar_wait(&empty[s], (n - 1) & 1)) || *vfailed) {
+        *vfailed = 1;
+        break;
+      }
+      const uint32_t st = smem_u32(base + s * G::kStageBytes);
+      const uint8_t *chbase = g.spec + (tc_index(0, g.kpad, cur.ch, 4 * q, S) * 8 + 16 * h);
+#pragma unroll
+      for (int i = 0; i < E; i++) {
+        if (rcur[i] == -2) break;  // past the tile's rows (the rows grow with i)
+        const int j = j0 + RP * i, row = rcur[i];
+        const bool ok = row >= 0 && row < g.nrows;
+        cp_async16(st + (j >> 3) * G::kGroupBytes + soff + sw32_offset(j & 7, h), ok ? chbase + row * rstride : g.spec,
+                   ok ? 16u : 0u);
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      if (it > 0) {  // the previous tile has landed: publish it to the tensor cores
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(&full[(it - 1) % G::kStages]);
+      }
+      it++;
+      cur = nxt;
+#pragma unroll
+      for (int i = 0; i < E; i++) rcur[i] = rnxt[i];
+      have = have_next;
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -349,44 +428,37 @@ __global__ void __launch_bounds__(GatherShape<S>::kThreads, 1) xcorr_tc_gather_k
     // ---- MMA issuer
     const uint32_t id0 = idesc_f16(128, g.n0), id1 = idesc_f16(128, g.n1 > 0 ? g.n1 : 16);
     int it = 0, sgn = 0;
-    bool stop = false;
-    for (int ch = blockIdx.x; ch < g.K && !stop; ch += gridDim.x) {
-      for (int bin = 0; bin < g.nbins && !stop; bin++) {
-        const int2 sg = gather_seg(g, ch, bin);
-        if (sg.y <= 0) continue;
-        const int b = sgn % g.nbuf, u = sgn / g.nbuf;
+    uint32_t d0 = tmem;
+    while (walk.next(g, ngroups, t)) {
+      const int b = sgn % g.nbuf, u = sgn / g.nbuf;
+      if (t.first) {
         if ((u > 0 && !mbar_wait(&tempty[b], (u - 1) & 1)) || *vfailed) {  // the epilogue has read buffer b
           *vfailed = 1;
-          stop = true;
           break;
         }
         fence_after_sync();
-        const uint32_t d0 = tmem + (uint32_t)(b * g.buf_stride);
-        for (int t0 = 0; t0 < sg.y; t0 += G::kRows, it++) {
-          const int rows = min(G::kRows, sg.y - t0);
-          const int s = it % G::kStages, n = it / G::kStages;
-          if (!mbar_wait(&full[s], n & 1)) {
-            stop = true;
-            break;
-          }
-          fence_after_sync();
-          const uint32_t st = smem_u32(base + s * G::kStageBytes);
-          for (int ks = 0; ks < rows / 16; ks++) {
-            const uint32_t acc_flag = (t0 > 0 || ks > 0) ? 1u : 0u;
-            // 16 K rows = two 8-row groups; MN atoms 256 B apart; block 1 starts 8 atoms in
-            const uint64_t a0 = smem_desc(st + ks * 2 * G::kGroupBytes, 256, G::kGroupBytes);
-            mma_f16(d0, a0, a0, id0, acc_flag);
-            if (g.n1 > 0) {
-              const uint64_t a1 = smem_desc(st + ks * 2 * G::kGroupBytes + 2048, 256, G::kGroupBytes);
-              mma_f16(d0 + (uint32_t)g.col1, a1, a1, id1, acc_flag);
-            }
-          }
-          mma_commit(&empty[s]);
+        d0 = tmem + (uint32_t)(b * g.buf_stride);
+      }
+      const int s = it % G::kStages, n = it / G::kStages;
+      if (!mbar_wait(&full[s], n & 1)) {
+        *vfailed = 1;
+        break;
+      }
+      fence_after_sync();
+      const uint32_t st = smem_u32(base + s * G::kStageBytes);
+      for (int ks = 0; ks < t.rows / 16; ks++) {
+        const uint32_t acc_flag = (!t.first || ks > 0) ? 1u : 0u;
+        // 16 K rows = two 8-row groups; MN atoms 256 B apart; block 1 starts 8 atoms in
+        const uint64_t a0 = smem_desc(st + ks * 2 * G::kGroupBytes, 256, G::kGroupBytes);
+        mma_f16(d0, a0, a0, id0, acc_flag);
+        if (g.n1 > 0) {
+          const uint64_t a1 = smem_desc(st + ks * 2 * G::kGroupBytes + 2048, 256, G::kGroupBytes);
+          mma_f16(d0 + (uint32_t)g.col1, a1, a1, id1, acc_flag);
         }
-        if (stop) {
-          *vfailed = 1;
-          break;
-        }
+      }
+      mma_commit(&empty[s]);
+      it++;
+      if (t.last) {
         mma_commit(&tfull[b]);  // the segment's sums are complete when its MMAs are
         sgn++;
       }
@@ -398,67 +470,67 @@ __global__ void __launch_bounds__(GatherShape<S>::kThreads, 1) xcorr_tc_gather_k
     const int q = warp & 3, half = (warp - 5) >> 2;
     const int m = q * 32 + lane, p = m & 3;
     int sgn = 0;
-    bool stop = false;
-    for (int ch = blockIdx.x; ch < g.K && !stop; ch += gridDim.x) {
-      for (int bin = 0; bin < g.nbins; bin++) {
-        const int2 sg = gather_seg(g, ch, bin);
-        if (sg.y <= 0) continue;
-        const int b = sgn % g.nbuf, u = sgn / g.nbuf;
-        if (!mbar_wait(&tfull[b], u & 1) || *vfailed) {
-          *vfailed = 1;
-          stop = true;
-          break;
-        }
-        fence_after_sync();
-        float2 *accb = g.acc + (size_t)bin * g.nbl * g.kpad + ch;
-        for (int I = 0; I < (g.n1 > 0 ? 2 : 1); I++) {
-          if (32 * I + 8 * q >= g.nstreams) continue;  // no stream in this lane quarter
-          const int a = 32 * I + (m >> 2);
-          const int nI = I ? g.n1 : g.n0;
-          const uint32_t col = (uint32_t)(b * g.buf_stride + (I ? g.col1 : 0));
+    while (walk.next(g, ngroups, t)) {
+      if (!t.last) continue;
+      const int b = sgn % g.nbuf, u = sgn / g.nbuf;
+      if (!mbar_wait(&tfull[b], u & 1) || *vfailed) {
+        *vfailed = 1;
+        break;
+      }
+      fence_after_sync();
+      float2 *accb = g.acc + (size_t)t.bin * g.nbl * g.kpad + t.ch;
+      for (int I = 0; I < (g.n1 > 0 ? 2 : 1); I++) {
+        if (32 * I + 8 * q >= g.nstreams) continue;  // no stream in this lane quarter
+        const int a = 32 * I + (m >> 2);
+        const int nI = I ? g.n1 : g.n0;
+        const uint32_t col = (uint32_t)(b * g.buf_stride + (I ? g.col1 : 0));
 #pragma unroll 1
-          for (int chunk = half; chunk < nI / 16; chunk += 2) {
-            float v[16];
-            tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + col + 16 * chunk, v);
-            float re4[4], im4[4];
+        for (int chunk = half; chunk < nI / 16; chunk += 2) {
+          float v[16];
+          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + col + 16 * chunk, v);
+          float re4[4], im4[4];
+#pragma unroll
+          for (int bb = 0; bb < 4; bb++) {
+            const float A = v[4 * bb] + v[4 * bb + 2], B = v[4 * bb + 1] + v[4 * bb + 3];
+            // row component p: 0 hi.re, 1 hi.im, 2 lo.re, 3 lo.im; columns likewise
+            float re = (p & 1) ? B : A, im = (p & 1) ? A : -B;
+            re += __shfl_xor_sync(0xffffffffu, re, 1);
+            im += __shfl_xor_sync(0xffffffffu, im, 1);
+            re += __shfl_xor_sync(0xffffffffu, re, 2);
+            im += __shfl_xor_sync(0xffffffffu, im, 2);
+            re4[bb] = re;
+            im4[bb] = im;
+          }
+          if (p == 0 && a < g.nstreams) {
+            int mv[4];
 #pragma unroll
             for (int bb = 0; bb < 4; bb++) {
-              const float A = v[4 * bb] + v[4 * bb + 2], B = v[4 * bb + 1] + v[4 * bb + 3];
-              // row component p: 0 hi.re, 1 hi.im, 2 lo.re, 3 lo.im; columns likewise
-              float re = (p & 1) ? B : A, im = (p & 1) ? A : -B;
-              re += __shfl_xor_sync(0xffffffffu, re, 1);
-              im += __shfl_xor_sync(0xffffffffu, im, 1);
-              re += __shfl_xor_sync(0xffffffffu, re, 2);
-              im += __shfl_xor_sync(0xffffffffu, im, 2);
-              re4[bb] = re;
-              im4[bb] = im;
+              const int bs = 32 * I + 4 * chunk + bb;
+              mv[bb] = bs < g.nstreams ? __ldg(g.blmap + a * g.npad + bs) : -1;
             }
-            if (p == 0 && a < g.nstreams) {
-              int mv[4];
-#pragma unroll
-              for (int bb = 0; bb < 4; bb++) {
-                const int bs = 32 * I + 4 * chunk + bb;
-                mv[bb] = bs < g.nstreams ? __ldg(g.blmap + a * g.npad + bs) : -1;
-              }
-              float2 o[4];
+            float2 o[4];
+            if (g.accumulate) {
 #pragma unroll
               for (int bb = 0; bb < 4; bb++)
                 if (mv[bb] >= 0) o[bb] = accb[(size_t)(mv[bb] >> 1) * g.kpad];
+            } else {
 #pragma unroll
-              for (int bb = 0; bb < 4; bb++)
-                if (mv[bb] >= 0) {
-                  o[bb].x += re4[bb] * g.inv_scale2;
-                  o[bb].y += ((mv[bb] & 1) ? -im4[bb] : im4[bb]) * g.inv_scale2;
-                  accb[(size_t)(mv[bb] >> 1) * g.kpad] = o[bb];
-                }
+              for (int bb = 0; bb < 4; bb++) o[bb] = make_float2(0.f, 0.f);
             }
+#pragma unroll
+            for (int bb = 0; bb < 4; bb++)
+              if (mv[bb] >= 0) {
+                o[bb].x += re4[bb] * g.inv_scale2;
+                o[bb].y += ((mv[bb] & 1) ? -im4[bb] : im4[bb]) * g.inv_scale2;
+                accb[(size_t)(mv[bb] >> 1) * g.kpad] = o[bb];
+              }
           }
         }
-        fence_before_sync();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&tempty[b]);  // buffer b may be overwritten
-        sgn++;
       }
+      fence_before_sync();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[b]);  // buffer b may be overwritten
+      sgn++;
     }
   }
   __syncthreads();
@@ -581,7 +653,7 @@ static cudaError_t launch_gather(const GatherArgs &g, cudaStream_t st) {
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 1;
-  xcorr_tc_gather_kernel<S><<<std::min(g.K, nsm), G::kThreads, G::kSmem, st>>>(g);
+  xcorr_tc_gather_kernel<S><<<std::min((g.K + 3) / 4, nsm), G::kThreads, G::kSmem, st>>>(g);
   return cudaGetLastError();
 }
 
@@ -614,7 +686,10 @@ cudaError_t launch_xcorr_tc_gather(const void *spec, int slots, int nrows, int k
   g.n1 = comps > 128 ? up16(comps - 128) : 0;
   g.col1 = up32(g.n0);
   g.buf_stride = g.col1 + up32(g.n1);
-  g.nbuf = std::min(4, 512 / g.buf_stride);
+  g.nbuf = std::min(kMaxBufs, 512 / g.buf_stride);
+  // with a row list (pulsar binning: the whole integration in one launch) each
+  // (bin, channel) segment is the only one of its accumulator entries
+  g.accumulate = rowlist ? 0 : 1;
   if (slots == kTcSlots) return launch_gather<kTcSlots>(g, st);
   return launch_gather<kTcSlotsWide>(g, st);
 }
