@@ -418,6 +418,52 @@ def measure(cfg, args, x_mode, log, world=1, rank=0, local=0, e2e=True, compare_
     return res
 
 
+C4_NAME = ("20 stations (12 x 32 MHz 2-bit at 64 MS/s, 6 x 64 MHz 2-bit at 128 MS/s, 2 x 16 MHz 1-bit at 32 MS/s); "
+           "one 2 s timeslice of 8 jobs in one CUDA graph: 4 x 32 MHz subbands of 40 streams, 4096 channels, 2 s "
+           "integration; 2 x 16384 channels (32768-sample FFTs) of 24 streams, 4 x 0.5 s; 2 x 16 MHz subbands of 16 "
+           "streams at up to 4x the job rate, 256 channels, 8 x 0.25 s")
+
+
+def measure_c4(args, log, x_mode="tc"):
+    """The batched uneven configuration: every job of one 2 s timeslice, all
+    their integrations in one CUDA graph per step (sfxc_gpu_batch_run_counts),
+    inputs in host memory pushed through the C ABI each step.  Device time:
+    CUDA events around the graph launch; e2e: wall clock of the whole step."""
+    from sfxc_gpu import correlator, lib, scenario
+    scs = scenario.c4_jobs(scale=1.0)
+    jobs = []
+    for i, sc in enumerate(scs):
+        t = time.time()
+        j = scenario.build_job_bulk(sc)
+        jobs.append(j)
+        log("built C4 job %d (%d streams, %d channels, %d x %d us) in %.1f s"
+            % (i, len(sc.streams()), sc.nchan, sc.n_integrations, sc.integration_us, time.time() - t))
+    # input samples: every stream at its own rate over the timeslice
+    total = sum(sum(sc.station_modes.get(sc.stations[si].number, (sc.sample_rate,))[0] for si, _ in sc.streams())
+                * sc.n_integrations * sc.integration_us // 1_000_000 for sc in scs)
+    mode = lib.X_TC_HILO if x_mode == "tc" else lib.X_FP32
+    nodes = [correlator.CorrelatorNode(0, mode) for _ in jobs]
+    batch = correlator.Batch(nodes)
+    try:
+        for _ in range(args.warmup):
+            batch.correlate(jobs)
+        dev_ms, t0 = 0.0, time.perf_counter()
+        for _ in range(args.steps):
+            batch.correlate(jobs)
+            dev_ms += batch.last_ms()
+        wall = time.perf_counter() - t0
+    finally:
+        batch.close()
+        for n in nodes:
+            n.close()
+    return {"workload": C4_NAME, "x_step": x_mode, "value": round(total * args.steps / (dev_ms / 1e3) / 1e9, 3),
+            "unit": "Gsamples/s", "ms_per_step": round(dev_ms / args.steps, 3), "samples_per_step": total,
+            "e2e": {"value": round(total * args.steps / wall / 1e9, 3), "unit": "Gsamples/s",
+                    "ms_per_step": round(wall * 1e3 / args.steps, 3)},
+            "graph_launches_per_step": 1, "jobs": len(jobs),
+            "data": "seeded uniform 2-bit/1-bit codes, cubic delay models"}
+
+
 def summary(cfg, res, args, x_mode, world=1):
     value = res["total"] * args.steps * world / (res["dev_total"] / 1e3) / 1e9
     d = {"workload": cfg["name"], "value": round(value, 3), "unit": "Gsamples/s",
@@ -469,6 +515,7 @@ def run_gpu(args):
             for m in modes:
                 r = measure(c, args, m, log, e2e=False, compare_fp32=(m == "tc"), peaks=peaks)
                 extra[name] = summary(c, r, args, m)
+        extra["c4"] = measure_c4(args, log)
     if rank != 0:
         return
     total = res["total"]

@@ -389,6 +389,49 @@ int sfxc_gpu_output_put_slice(sfxc_gpu_output *out, int64_t slice_nr, const uint
 int sfxc_gpu_output_finish(sfxc_gpu_output *out);
 void sfxc_gpu_output_destroy(sfxc_gpu_output *out);
 
+/* Batches (no single counterpart in the reference, where each subband job of
+ * a timeslice goes to its own correlator node: Manager_node deals them,
+ * sfxc/src/manager_node.cc:201-257,288-391).  A batch holds several contexts
+ * on one device -- jobs of one timeslice, of any mix of stream counts,
+ * sample rates, bit depths, FFT lengths and integration times -- and
+ * correlates the next integration of every one of them together: the host
+ * plans all jobs first, then their device work goes to the GPU as one CUDA
+ * graph (each job on its own streams, forked from and joined back into the
+ * batch's stream), launched once.  Each context must have its parameters set
+ * and its input pushed, as for sfxc_gpu_run_integration; the results equal
+ * that call's.  The sink gets each job's output in batch order, with
+ * users[i] (NULL: NULL) for job i.  The first integration of a new shape
+ * sizes the jobs' buffers; later ones with the same shapes reuse them and
+ * the executable graph.  A context belongs to at most one batch at a time. */
+typedef struct sfxc_gpu_batch sfxc_gpu_batch;
+/* NULL on bad arguments (message from sfxc_gpu_global_error). */
+sfxc_gpu_batch *sfxc_gpu_batch_create(sfxc_gpu_ctx *const *ctxs, int32_t n);
+int sfxc_gpu_batch_run(sfxc_gpu_batch *batch, sfxc_output_sink sink, void *const *users);
+/* The next counts[i] integrations of context i (0: none), all in the one
+ * graph -- a timeslice's jobs of different integration times (the input of
+ * all of them pushed beforehand); each job's outputs reach the sink in
+ * integration order. */
+int sfxc_gpu_batch_run_counts(sfxc_gpu_batch *batch, const int32_t *counts, sfxc_output_sink sink,
+                              void *const *users);
+/* Device time (ms, CUDA events around the graph launch) of the last run. */
+float sfxc_gpu_batch_last_ms(const sfxc_gpu_batch *batch);
+void sfxc_gpu_batch_destroy(sfxc_gpu_batch *batch);
+
+/* Autotuner (no counterpart in the reference): times the launch-shape
+ * variants of the block stage (CTAs per SM) and of each windowed-FFT length
+ * (waves of resident CTAs) on the last integration's final chunk -- the
+ * launches rewrite that chunk's intermediates with the same values --
+ * `trials` times each (<= 0: 3), and keeps the fastest per job shape in a
+ * plan cache that every context of the process uses from its next
+ * integration on.  Tuned shapes change no result bit.  Returns the number of
+ * shapes tuned, or a negative status (SFXC_GPU_ESTATE before any
+ * integration). */
+int sfxc_gpu_autotune(sfxc_gpu_ctx *ctx, int32_t trials);
+/* The plan cache: up to `capacity` entries of 5 int32 (kernel: 0 block stage,
+ * 1 windowed FFT; two or three shape values; the chosen variant); returns the
+ * number of entries. */
+int sfxc_gpu_plan_cache(int32_t *out, int32_t capacity);
+
 /* Compute peaks of `device` for the rooflines (no counterpart in the
  * reference: a measurement aid).  Times one short kernel of independent FP32
  * fused multiply-adds on the CUDA cores and one of FP16 tensor-core MMAs with

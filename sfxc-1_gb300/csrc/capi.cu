@@ -3,11 +3,13 @@
 // the byte layout of the correlator output (Correlation_core::integration_write,
 // sfxc/src/correlation_core.cc:316-477; headers sfxc/include/output_header.h:100-148).
 #include <algorithm>
+#include <array>
 #include <tuple>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -119,6 +121,76 @@ struct Polyco {
   std::vector<double> coef;
 };
 
+// Device work of one integration, recorded while the host plans it and run
+// afterwards, eagerly or under stream capture (a batch of jobs in one CUDA
+// graph).  Buffers are sized while recording, so running allocates nothing;
+// the payloads of the uploads are kept here and copied into the context's
+// pinned arena before the work runs.
+struct Ops {
+  std::vector<std::function<cudaError_t(const uint8_t *)>> ops;  // argument: the pinned arena
+  std::vector<uint8_t> host;                                     // upload payloads, 16-byte aligned
+  void clear() {
+    ops.clear();
+    host.clear();
+  }
+  void upload(DevBuf &b, const void *src, size_t n, cudaStream_t st) {
+    b.ensure(n ? n : 16);
+    if (!n) return;
+    const size_t off = (host.size() + 15) & ~(size_t)15;
+    host.resize(off + n);
+    std::memcpy(host.data() + off, src, n);
+    void *dst = b.p;
+    ops.push_back([=](const uint8_t *arena) { return cudaMemcpyAsync(dst, arena + off, n, cudaMemcpyHostToDevice, st); });
+  }
+  void memset(void *p, int v, size_t n, cudaStream_t st) {
+    ops.push_back([=](const uint8_t *) { return cudaMemsetAsync(p, v, n, st); });
+  }
+  void record(cudaEvent_t e, cudaStream_t st) {
+    ops.push_back([=](const uint8_t *) { return cudaEventRecord(e, st); });
+  }
+  void wait(cudaStream_t st, cudaEvent_t e) {
+    ops.push_back([=](const uint8_t *) { return cudaStreamWaitEvent(st, e, 0); });
+  }
+  template <class F>
+  void op(F f) {  // f returns a cudaError_t
+    ops.push_back([f](const uint8_t *) { return f(); });
+  }
+  template <class F>
+  void kernel(F f) {  // f launches; the launch error is checked
+    ops.push_back([f](const uint8_t *) {
+      f();
+      return cudaGetLastError();
+    });
+  }
+};
+
+// What finish_integration needs of an enqueued integration.
+struct Pending {
+  ticks_t start = 0;
+  size_t nvis = 0, ev = 0;
+  int nout = 0, nphs = 0, launches = 0;
+  bool pulsar = false;
+  std::vector<std::pair<int64_t, int64_t>> nfl;
+  uint8_t *res = nullptr;
+};
+
+// One integration in flight: its recorded work, the pinned copy of its
+// upload payloads, its pinned results, its timing events and what finishing
+// it needs.  A context has one slot per integration that can be in flight
+// at once (several when a batch runs several integrations of it in one
+// graph).
+struct Slot {
+  Ops q;
+  HostBuf arena, results;
+  Pending pend;
+  std::vector<cudaEvent_t> evs;
+  cudaEvent_t ev0 = nullptr;
+  ~Slot() {
+    for (cudaEvent_t e : evs) cudaEventDestroy(e);
+    if (ev0) cudaEventDestroy(ev0);
+  }
+};
+
 // Host-side per-launch tables uploaded once per job.
 struct JobTables {
   std::vector<int> blmap, tiles, blpairs;
@@ -133,9 +205,7 @@ struct sfxc_gpu_ctx {
   // second stream: the next chunk's per-block parameters (FP64) beside the
   // current chunk's X-step
   cudaStream_t st2 = nullptr;
-  cudaEvent_t ev[6] = {};
   float timings[6] = {};
-  std::vector<cudaEvent_t> evpool;
   std::string err;
   bool have_job = false;
   // job
@@ -177,12 +247,22 @@ struct sfxc_gpu_ctx {
     DevBuf window, twrot;
   };
   std::map<int, RotTables> rot_tables;
-  HostBuf staging;  // the integration's chunk descriptors, uploaded in one copy
+  // integrations in flight (slot 0: the next one)
+  std::vector<std::unique_ptr<Slot>> slots;
+  // the last chunk of the last integration, for the autotuner: its stream
+  // descriptors (block order, then grouped by windowed-FFT length), the
+  // groups (rot, first, count) and the launch sizes
+  struct TuneSpec {
+    StreamDev *dchunk = nullptr;
+    int nstreams = 0, max_blocks = 0, nrows = 0, max_rows = 0, M = 0, kpad = 0, tc_slots = 0, window = 0;
+    float tc_scale = 1.f;
+    void *spec = nullptr;
+    std::vector<std::array<int, 3>> groups;
+  } tune;
   // bit-statistics counters of all streams (8 per stream), and the pinned
   // landing area of an integration's results: visibilities, counters, the
   // X-step's error flag (one readback copy each)
   DevBuf hist;
-  HostBuf results;
   std::vector<StreamDev> hsd;
 };
 
@@ -192,6 +272,34 @@ namespace {
 // uncapped; caps of 1, 2 and 4 measured slower: the launch then runs longer
 // and slows the X-step for longer)
 constexpr int kSideParamCtas = 0;
+
+// ---- plan cache of the autotuner: launch shapes of the F-step kernels per
+// job shape, shared by every context of the process.  Keys: (kernel, and
+// what decides its best shape); values: the variant (0 or absent: the
+// launcher's default).  Only launch shapes that leave every result bit
+// unchanged are tuned.
+enum PlanKnob { kKnobBlockStage = 0, kKnobWindowFft = 1 };
+std::mutex g_plan_mu;
+std::map<std::array<int, 4>, int> g_plan;
+
+int ilog2c(int x) {
+  int l = 0;
+  while ((1 << l) < x) l++;
+  return l;
+}
+std::array<int, 4> block_key(int nstreams, int max_blocks) { return {kKnobBlockStage, nstreams, ilog2c(max_blocks), 0}; }
+std::array<int, 4> window_key(int rot, int nstreams, int nrows) {
+  return {kKnobWindowFft, rot, nstreams, ilog2c(nrows)};
+}
+int plan_get(const std::array<int, 4> &k) {
+  std::lock_guard<std::mutex> lock(g_plan_mu);
+  auto it = g_plan.find(k);
+  return it == g_plan.end() ? 0 : it->second;
+}
+void plan_set(const std::array<int, 4> &k, int v) {
+  std::lock_guard<std::mutex> lock(g_plan_mu);
+  g_plan[k] = v;
+}
 
 int fail(sfxc_gpu_ctx *c, const Error &e) {
   if (c) c->err = e.msg;
@@ -574,11 +682,27 @@ int spline_lo_for(const StreamDev &d, const std::vector<double> &x) {
   return lo;
 }
 
-int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
+// Host planning of the context's next integration, with its device work
+// recorded into slot k (run by run_ops, eagerly or under stream capture) and
+// what finish_integration needs kept there.  Sizes every device buffer
+// and creates every event it uses, so running the work allocates nothing.
+Slot &slot_of(sfxc_gpu_ctx *c, int k) {
+  while ((int)c->slots.size() <= k) {
+    std::unique_ptr<Slot> sl(new Slot());
+    CK(cudaEventCreate(&sl->ev0));
+    c->slots.push_back(std::move(sl));
+  }
+  return *c->slots[k];
+}
+
+void enqueue_integration(sfxc_gpu_ctx *c, int k = 0, bool require_push = true) {
+  Slot &sl = slot_of(c, k);
+  Ops &q = sl.q;
+  q.clear();
   if (!c->have_job) throw Error(SFXC_GPU_ESTATE, "no parameters set");
   const int N = (int)c->streams.size();
   for (int i = 0; i < N; i++)
-    if (!c->sc[i].pushed) throw Error(SFXC_GPU_ESTATE, "a stream has no input for this integration");
+    if (require_push && !c->sc[i].pushed) throw Error(SFXC_GPU_ESTATE, "a stream has no input for this integration");
   const ticks_t tint = time_from_usec((double)c->p.integration_time_us);
   const ticks_t start = c->p.start_ticks + (ticks_t)c->current_integration * tint;
   const int M = c->M, K = c->K, kpad = c->kpad, nbl = (int)c->bl.size();
@@ -586,7 +710,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   // ---- host planning per stream (Bit2float_worker state machine replica)
   c->hsd.assign(N, StreamDev{});
   c->hist.ensure((size_t)N * 64);
-  CK(cudaMemsetAsync(c->hist.p, 0, (size_t)N * 64, st));
+  q.memset(c->hist.p, 0, (size_t)N * 64, st);
   std::vector<int4> items;
   for (int i = 0; i < N; i++) {
     StreamCtx &s = c->sc[i];
@@ -602,8 +726,8 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     s.plan = plan_unpack(s.recs, s.ust, s.n_blocks, s.nfft_max, c->Nd, ss.bits, ss.sample_rate, ss.tsys_freq,
                          s.sp.delay(start));
     if (s.plan.segs.empty()) s.plan.segs.push_back(Segment{0, s.n_blocks * c->Nd, -1});
-    upload(s.segs, s.plan.segs.data(), s.plan.segs.size() * sizeof(Segment), st);
-    upload(s.stat_rng, s.plan.stats.data(), s.plan.stats.size() * sizeof(StatRange), st);
+    q.upload(s.segs, s.plan.segs.data(), s.plan.segs.size() * sizeof(Segment), st);
+    q.upload(s.stat_rng, s.plan.stats.data(), s.plan.stats.size() * sizeof(StatRange), st);
     std::vector<double> spl;
     spl.insert(spl.end(), s.sp.x.begin(), s.sp.x.end());
     for (int k = 0; k < 3; k++) {
@@ -612,7 +736,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       spl.insert(spl.end(), s.sp.c[k].begin(), s.sp.c[k].end());
       spl.insert(spl.end(), s.sp.d[k].begin(), s.sp.d[k].end());
     }
-    upload(s.spline, spl.data(), spl.size() * 8, st);
+    q.upload(s.spline, spl.data(), spl.size() * 8, st);
     StreamDev &d = c->hsd[i];
     d.src = s.src.as<uint8_t>();
     d.segs = s.segs.as<DevSegment>();
@@ -705,18 +829,18 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     if (n < 0.01) n = 1;
     flagfac[b] = n;
   }
-  upload(c->flagfac, flagfac.data(), flagfac.size() * 8, st);
-  upload(c->items, items.data(), items.size() * sizeof(int4), st);
+  q.upload(c->flagfac, flagfac.data(), flagfac.size() * 8, st);
+  q.upload(c->items, items.data(), items.size() * sizeof(int4), st);
   // ---- device work
   // phased array: one buffer per sub-integration (Correlation_core_phased::create_baselines)
   const int nphs = c->phased ? c->nffts / c->nsub + 1 : 0;
   const size_t accn = (size_t)std::max(c->nbins * nbl, nphs) * kpad;
   c->acc.ensure(accn * sizeof(float2));
-  CK(cudaMemsetAsync(c->acc.p, 0, accn * sizeof(float2), st));
+  q.memset(c->acc.p, 0, accn * sizeof(float2), st);
   const bool pulsar = c->nbins > 1;
   if (c->npc > 1) {
     c->pcacc.ensure((size_t)c->npc * nbl * kpad * sizeof(float2));
-    CK(cudaMemsetAsync(c->pcacc.p, 0, (size_t)c->npc * nbl * kpad * sizeof(float2), st));
+    q.memset(c->pcacc.p, 0, (size_t)c->npc * nbl * kpad * sizeof(float2), st);
   }
   std::vector<std::pair<int, int>> ranges;
   if (pulsar)
@@ -751,7 +875,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   // the TMA-fed kernel reads rows in groups of 8 (rows past a chunk's end cleared before its X-step)
   c->spec.ensure((size_t)(tc_x ? tc_slots : N) * (tc_x ? (max_rows + 7) / 8 * 8 : max_rows) * kpad * sizeof(float2));
   c->derr.ensure(sizeof(int));
-  CK(cudaMemsetAsync(c->derr.p, 0, sizeof(int), st));
+  q.memset(c->derr.p, 0, sizeof(int), st);
   if (!tc_x && !pulsar && !c->phased)
     c->xpart.ensure(std::max<size_t>(16, xcorr_f32_scratch_bytes(c->jt.ntiles, c->jt.npad, K, max_rows, nbl, kpad)));
   // two sets of per-block records: chunk ch uses set ch & 1, so the next
@@ -759,7 +883,6 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   for (int i = 0; i < N; i++) {
     c->sc[i].bpar.ensure((size_t)2 * max_blocks * sizeof(BlockPar));
   }
-  float t_f1 = 0, t_f2 = 0, t_x = 0;
   // pulsar setup (Correlation_core_pulsar::set_parameters, correlation_core_pulsar.cc:46-95)
   double psr_start_phase = 0, psr_rate = 0, fft_duration = 0;
   if (pulsar) {
@@ -801,7 +924,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
       const double x = base_freq + i * dfreq;
       off[i] = (4148.808 * pc.dm) * ((1 / (x * x) - inv2) * freq);
     }
-    upload(c->offsets, off.data(), off.size() * 8, st);
+    q.upload(c->offsets, off.data(), off.size() * 8, st);
     c->bins.ensure((size_t)max_rows * K * sizeof(int16_t));
     if (tc_x) {  // per channel the rows sorted by bin (runs padded to 16 rows), and the runs
       c->rowlist.ensure((size_t)K * (max_rows + 16 * c->nbins) * sizeof(int));
@@ -811,10 +934,10 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   // four events per chunk on the main stream and one on the second (+2 for
   // normalisation), recorded without host syncs
   const size_t nev = ranges.size() * 5 + 2;
-  while (c->evpool.size() < nev) {
+  while (sl.evs.size() < nev) {
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
-    c->evpool.push_back(e);
+    sl.evs.push_back(e);
   }
   // ---- every chunk's stream descriptors, in job order and then grouped by
   // windowed-FFT length (job order within a group), in one asynchronous
@@ -828,7 +951,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     if (order.size() > first) groups.push_back({rt.first, (int)first});
   }
   const size_t per_chunk = 2 * (size_t)N;
-  StreamDev *staged = static_cast<StreamDev *>(c->staging.ensure(ranges.size() * per_chunk * sizeof(StreamDev)));
+  std::vector<StreamDev> staged(ranges.size() * per_chunk);
   for (size_t ch = 0; ch < ranges.size(); ch++) {
     const int r0 = ranges[ch].first, r1 = ranges[ch].second;
     // block range of each stream for rows [r0, r1) (plus the overlapping half window)
@@ -845,9 +968,7 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     }
     for (int k = 0; k < N; k++) staged[ch * per_chunk + N + k] = c->hsd[order[k]];
   }
-  c->streamdev.ensure(ranges.size() * per_chunk * sizeof(StreamDev));
-  CK(cudaMemcpyAsync(c->streamdev.p, staged, ranges.size() * per_chunk * sizeof(StreamDev), cudaMemcpyHostToDevice,
-                     st));
+  q.upload(c->streamdev, staged.data(), staged.size() * sizeof(StreamDev), st);
   // uvshift of every chunk (sub-integration), cross baseline and extra centre:
   // Correlation_core::sub_integration / uvshift (sfxc/src/correlation_core.cc:
   // 516-593) in FP64 on the host -- tmid of the sub-integration, residual
@@ -876,101 +997,144 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
           uv[(ch * (c->npc - 1) + (pc - 1)) * nbl + b] = UvShift{phi, delta, amplitude, 0.0};
         }
     }
-    upload(c->uvp, uv.data(), uv.size() * sizeof(UvShift), st);
+    q.upload(c->uvp, uv.data(), uv.size() * sizeof(UvShift), st);
   }
-  CK(cudaEventRecord(c->ev[0], st));
+  q.record(sl.ev0, st);
   // The per-block parameters (block_params_kernel, FP64-pipe bound, few
   // registers) run on the second stream: those of the first chunk beside the
   // bit statistics (memory bound), those of chunk ch + 1 once chunk ch's
   // windowed FFT is done, i.e. beside chunk ch's X-step, whose CTAs leave
   // registers and issue slots free.  Each chunk's transforms wait for them.
   const size_t ev_side = ranges.size() * 4 + 2;  // the second stream's events, one per chunk
-  CK(cudaStreamWaitEvent(c->st2, c->ev[0], 0));  // the descriptors are on the device
-  launch_block_params(c->streamdev.as<StreamDev>(), N, max_blocks, c->st2);
-  CK(cudaGetLastError());
-  CK(cudaEventRecord(c->evpool[ev_side], c->st2));
+  q.wait(c->st2, sl.ev0);  // the descriptors are on the device
+  StreamDev *const sdev = c->streamdev.as<StreamDev>();
+  cudaStream_t st2 = c->st2;
+  q.kernel([=] { launch_block_params(sdev, N, max_blocks, st2); });
+  q.record(sl.evs[ev_side], c->st2);
   // bit statistics read only chunk-independent fields (source bytes, ranges, histograms)
-  launch_bitstat(c->streamdev.as<StreamDev>(), c->items.as<int4>(), (int)items.size(), st);
-  CK(cudaGetLastError());
+  {
+    const int4 *ditems = c->items.as<int4>();
+    const int nitems = (int)items.size();
+    q.kernel([=] { launch_bitstat(sdev, ditems, nitems, st); });
+  }
   int launches = items.empty() ? 0 : 1;
   size_t ev = 0;
   for (size_t ch = 0; ch < ranges.size(); ch++) {
     const int nrows = ranges[ch].second - ranges[ch].first;
-    StreamDev *dchunk = c->streamdev.as<StreamDev>() + ch * per_chunk;
-    CK(cudaEventRecord(c->evpool[ev], st));
-    CK(cudaStreamWaitEvent(st, c->evpool[ev_side + ch], 0));
-    launch_fstep(dchunk, N, max_blocks, c->tw256.as<float2>(), st);
-    CK(cudaGetLastError());
-    CK(cudaEventRecord(c->evpool[ev + 1], st));
+    StreamDev *dchunk = sdev + ch * per_chunk;
+    q.record(sl.evs[ev], st);
+    q.wait(st, sl.evs[ev_side + ch]);
+    {
+      const float2 *tw256 = c->tw256.as<float2>();
+      const int fw = plan_get(block_key(N, max_blocks));
+      q.kernel([=] { launch_fstep(dchunk, N, max_blocks, tw256, st, fw); });
+    }
+    q.record(sl.evs[ev + 1], st);
     for (size_t g = 0; g < groups.size(); g++) {
       const int rot = groups[g].first, first = groups[g].second;
       const int count = (g + 1 < groups.size() ? groups[g + 1].second : N) - first;
       const int nper = c->p.window == WINDOW_NONE ? rot / 2 : rot;
       const sfxc_gpu_ctx::RotTables &t = c->rot_tables.at(rot);
-      launch_window_fft(dchunk + N + first, count, 0, nrows, max_rows, t.window.as<float>(), t.twrot.as<float2>(), rot,
-                        nper, M, kpad, c->spec.p, tc_slots, tc_scale, st);
-      CK(cudaGetLastError());
+      const float *win = t.window.as<float>();
+      const float2 *twr = t.twrot.as<float2>();
+      void *spec = c->spec.p;
+      const int ww = plan_get(window_key(rot, count, nrows));
+      q.kernel([=] {
+        launch_window_fft(dchunk + N + first, count, 0, nrows, max_rows, win, twr, rot, nper, M, kpad, spec, tc_slots,
+                          tc_scale, st, ww);
+      });
     }
-    CK(cudaEventRecord(c->evpool[ev + 2], st));
+    q.record(sl.evs[ev + 2], st);
     if (ch + 1 < ranges.size()) {
       // chunk ch + 1's records go to the other set, last read by chunk ch - 1's
       // transforms.  (Starting them once chunk ch's transforms are done, to
       // fill the windowed FFT's tail, measured slower: their CTAs then hold
       // SMs when the X-step's persistent CTAs are placed.)
-      CK(cudaStreamWaitEvent(c->st2, c->evpool[ev + 2], 0));
-      launch_block_params(dchunk + per_chunk, N, max_blocks, c->st2, kSideParamCtas);
-      CK(cudaGetLastError());
-      CK(cudaEventRecord(c->evpool[ev_side + ch + 1], c->st2));
+      q.wait(c->st2, sl.evs[ev + 2]);
+      q.kernel([=] { launch_block_params(dchunk + per_chunk, N, max_blocks, st2, kSideParamCtas); });
+      q.record(sl.evs[ev_side + ch + 1], c->st2);
     }
-    if (c->phased) {
-      launch_phased(c->spec.as<float2>(), max_rows, kpad, N, ranges[ch].first, nrows, K, c->nsub, c->acc.as<float2>(),
-                    st);
-    } else if (pulsar) {
-      // the bin of every (row, channel), then the binned X-step: tensor cores
-      // over each channel's rows sorted by bin, or CUDA cores in row order
-      launch_pulsar_bins(nrows, K, psr_start_phase, psr_rate, fft_duration, c->offsets.as<double>(), c->p.gate_start,
-                         c->p.gate_stop, c->nbins, c->bins.as<int16_t>(), st);
-      CK(cudaGetLastError());
-      c->bins_rows = nrows;  // one chunk: the whole integration
-      if (tc_x) {
-        const int list_len = max_rows + 16 * c->nbins;
-        launch_pulsar_sort(c->bins.as<int16_t>(), nrows, K, c->nbins, list_len, c->rowlist.as<int>(),
-                           c->segs.as<int2>(), st);
-        CK(cudaGetLastError());
-        CK(launch_xcorr_tc_gather(c->spec.p, tc_slots, nrows, kpad, K, N, c->blmap.as<int>(), c->jt.npad, nbl, c->nbins,
-                                  c->rowlist.as<int>(), list_len, c->segs.as<int2>(), 1.0f / (tc_scale * tc_scale),
-                                  c->acc.as<float2>(), c->derr.as<int>(), st));
-        launches += 1;
+    {
+      // X-step of the chunk (pointers and sizes taken now; the buffers are sized above)
+      const int r0c = ranges[ch].first, nsub = c->nsub, nbins = c->nbins, npad = c->jt.npad, ntiles = c->jt.ntiles;
+      float2 *acc = c->acc.as<float2>();
+      void *specp = c->spec.p;
+      const int *blmap = c->blmap.as<int>(), *tiles = c->tiles.as<int>();
+      int *derr = c->derr.as<int>();
+      const float inv_s2 = 1.0f / (tc_scale * tc_scale);
+      if (c->phased) {
+        q.kernel([=] { launch_phased(static_cast<float2 *>(specp), max_rows, kpad, N, r0c, nrows, K, nsub, acc, st); });
+      } else if (pulsar) {
+        // the bin of every (row, channel), then the binned X-step: tensor cores
+        // over each channel's rows sorted by bin, or CUDA cores in row order
+        const double *offs = c->offsets.as<double>();
+        const double g0 = c->p.gate_start, g1 = c->p.gate_stop;
+        int16_t *bins = c->bins.as<int16_t>();
+        q.kernel([=] { launch_pulsar_bins(nrows, K, psr_start_phase, psr_rate, fft_duration, offs, g0, g1, nbins, bins, st); });
+        c->bins_rows = nrows;  // one chunk: the whole integration
+        if (tc_x) {
+          const int list_len = max_rows + 16 * nbins;
+          int *rowlist = c->rowlist.as<int>();
+          int2 *segs = c->segs.as<int2>();
+          q.kernel([=] { launch_pulsar_sort(bins, nrows, K, nbins, list_len, rowlist, segs, st); });
+          q.op([=] {
+            return launch_xcorr_tc_gather(specp, tc_slots, nrows, kpad, K, N, blmap, npad, nbl, nbins, rowlist,
+                                          list_len, segs, inv_s2, acc, derr, st);
+          });
+          launches += 1;
+        } else {
+          q.kernel([=] {
+            launch_xcorr_f32(static_cast<float2 *>(specp), max_rows, kpad, N, npad, 0, nrows, K, tiles, ntiles, blmap,
+                             nbl, bins, nrows, acc, nullptr, 0, st);
+          });
+        }
+      } else if (tc_tma) {
+        if (nrows % 8)
+          q.memset(static_cast<char *>(specp) + (size_t)nrows * kpad * kTcSlots * sizeof(float2), 0,
+                   (size_t)(8 - nrows % 8) * kpad * kTcSlots * sizeof(float2), st);
+        q.op([=] { return launch_xcorr_tc(specp, nrows, kpad, K, blmap, npad, inv_s2, acc, derr, st); });
+      } else if (tc_x) {  // 33 to 64 streams: the row-gathered kernel over rows in order
+        q.op([=] {
+          return launch_xcorr_tc_gather(specp, tc_slots, nrows, kpad, K, N, blmap, npad, nbl, 1, nullptr, 0, nullptr,
+                                        inv_s2, acc, derr, st);
+        });
       } else {
-        launch_xcorr_f32(c->spec.as<float2>(), max_rows, kpad, N, c->jt.npad, 0, nrows, K, c->tiles.as<int>(),
-                         c->jt.ntiles, c->blmap.as<int>(), nbl, c->bins.as<int16_t>(), nrows, c->acc.as<float2>(),
-                         nullptr, 0, st);
+        float2 *xpart = c->xpart.as<float2>();
+        const size_t xcap = c->xpart.cap;
+        q.kernel([=] {
+          launch_xcorr_f32(static_cast<float2 *>(specp), max_rows, kpad, N, npad, 0, nrows, K, tiles, ntiles, blmap, nbl,
+                           nullptr, 0, acc, xpart, xcap, st);
+        });
       }
-    } else if (tc_tma) {
-      if (nrows % 8)
-        CK(cudaMemsetAsync(static_cast<char *>(c->spec.p) + (size_t)nrows * kpad * kTcSlots * sizeof(float2), 0,
-                           (size_t)(8 - nrows % 8) * kpad * kTcSlots * sizeof(float2), st));
-      CK(launch_xcorr_tc(c->spec.p, nrows, kpad, K, c->blmap.as<int>(), c->jt.npad, 1.0f / (tc_scale * tc_scale),
-                         c->acc.as<float2>(), c->derr.as<int>(), st));
-    } else if (tc_x) {  // 33 to 64 streams: the row-gathered kernel over rows in order
-      CK(launch_xcorr_tc_gather(c->spec.p, tc_slots, nrows, kpad, K, N, c->blmap.as<int>(), c->jt.npad, nbl, 1, nullptr,
-                                0, nullptr, 1.0f / (tc_scale * tc_scale), c->acc.as<float2>(), c->derr.as<int>(),
-                                st));
-    } else {
-      launch_xcorr_f32(c->spec.as<float2>(), max_rows, kpad, N, c->jt.npad, 0, nrows, K, c->tiles.as<int>(),
-                       c->jt.ntiles, c->blmap.as<int>(), nbl, nullptr, 0, c->acc.as<float2>(), c->xpart.as<float2>(),
-                       c->xpart.cap, st);
+      if (c->npc > 1) {  // the sub-integration into every phase centre
+        float2 *pcacc = c->pcacc.as<float2>();
+        const UvShift *uvp = c->uvp.as<UvShift>() + ch * (size_t)(c->npc - 1) * nbl;
+        const int npc = c->npc;
+        q.kernel([=] { launch_pc_dump(acc, pcacc, uvp, N, nbl, kpad, K, npc, st); });
+        launches += 1;
+      }
     }
-    CK(cudaGetLastError());
-    if (c->npc > 1) {  // the sub-integration into every phase centre
-      launch_pc_dump(c->acc.as<float2>(), c->pcacc.as<float2>(),
-                     c->uvp.as<UvShift>() + ch * (size_t)(c->npc - 1) * nbl, N, nbl, kpad, K, c->npc, st);
-      CK(cudaGetLastError());
-      launches += 1;
-    }
-    CK(cudaEventRecord(c->evpool[ev + 3], st));
+    q.record(sl.evs[ev + 3], st);
     ev += 4;
     launches += pulsar ? 5 : 4;  // parameters, blocks, window FFT, (pulsar bins,) X-step
+  }
+  {  // the last chunk, for the autotuner
+    sfxc_gpu_ctx::TuneSpec &ts = c->tune;
+    ts.dchunk = sdev + (ranges.size() - 1) * per_chunk;
+    ts.nstreams = N;
+    ts.max_blocks = max_blocks;
+    ts.nrows = ranges.back().second - ranges.back().first;
+    ts.max_rows = max_rows;
+    ts.M = M;
+    ts.kpad = kpad;
+    ts.tc_slots = tc_slots;
+    ts.tc_scale = tc_scale;
+    ts.window = c->p.window;
+    ts.spec = c->spec.p;
+    ts.groups.clear();
+    for (size_t g = 0; g < groups.size(); g++)
+      ts.groups.push_back({groups[g].first, groups[g].second,
+                           (g + 1 < groups.size() ? groups[g + 1].second : N) - groups[g].second});
   }
   // restore the whole-integration time base for inspection calls
   for (int i = 0; i < N; i++) {
@@ -979,55 +1143,98 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
     c->hsd[i].spline_lo = spline_lo_for(c->hsd[i], c->sc[i].sp.x);
   }
   // ---- normalisation and statistics
-  CK(cudaEventRecord(c->evpool[ev], st));
+  q.record(sl.evs[ev], st);
   c->norms.ensure((size_t)N * 8);
   // outputs: the pulsar bins, or the phase centres (each normalised on its
   // own); the phased array writes its sub-integration sums as they are
   const int nout = pulsar ? c->nbins : c->npc;
   const float2 *accs = c->npc > 1 ? c->pcacc.as<float2>() : c->acc.as<float2>();
   c->out.ensure((size_t)std::max(nout * nbl, nphs) * K * sizeof(float2));
+  float2 *outp = c->out.as<float2>();
   if (c->phased) {
-    CK(cudaMemcpy2DAsync(c->out.p, K * sizeof(float2), c->acc.p, kpad * sizeof(float2), K * sizeof(float2), nphs,
-                         cudaMemcpyDeviceToDevice, st));
+    const void *accp = c->acc.p;
+    q.op([=] {
+      return cudaMemcpy2DAsync(outp, K * sizeof(float2), accp, kpad * sizeof(float2), K * sizeof(float2), nphs,
+                               cudaMemcpyDeviceToDevice, st);
+    });
   } else {
-    for (int bin = 0; bin < nout; bin++)
-      launch_normalize(accs + (size_t)bin * nbl * kpad, kpad, M, N, nbl, c->blpairs.as<int>(), c->norms.as<double>(),
-                       c->flagfac.as<double>(), c->out.as<float2>() + (size_t)bin * nbl * K, st);
-    CK(cudaGetLastError());
+    const int *blp = c->blpairs.as<int>();
+    double *norms = c->norms.as<double>();
+    const double *ff = c->flagfac.as<double>();
+    q.kernel([=] {
+      for (int bin = 0; bin < nout; bin++)
+        launch_normalize(accs + (size_t)bin * nbl * kpad, kpad, M, N, nbl, blp, norms, ff, outp + (size_t)bin * nbl * K,
+                         st);
+    });
   }
-  const float2 *vsrc = c->out.as<float2>();
+  const float2 *vsrc = outp;
   if (c->nch < M) {
     c->rout.ensure((size_t)nout * nbl * c->Kout * sizeof(float2));
-    CK(launch_reduce(c->out.as<float2>(), nout * nbl, M, c->nch, c->rmask.as<float>(), c->rlag.as<float>(),
-                     c->rnorm, c->rtw.as<float2>(), c->rout.as<float2>(), st));
-    vsrc = c->rout.as<float2>();
+    const int nch = c->nch, rnorm = c->rnorm;
+    const float *rmask = c->rmask.as<float>(), *rlag = c->rlag.as<float>();
+    const float2 *rtw = c->rtw.as<float2>();
+    float2 *rout = c->rout.as<float2>();
+    q.op([=] { return launch_reduce(outp, nout * nbl, M, nch, rmask, rlag, rnorm, rtw, rout, st); });
+    vsrc = rout;
     launches += 1;
   }
   const size_t nvis = c->phased ? (size_t)nphs * c->Kout : (size_t)nout * nbl * c->Kout;
-  uint8_t *res = static_cast<uint8_t *>(c->results.ensure(nvis * sizeof(float2) + (size_t)N * 64 + 16));
+  uint8_t *res = static_cast<uint8_t *>(sl.results.ensure(nvis * sizeof(float2) + (size_t)N * 64 + 16));
+  {
+    const void *histp = c->hist.p, *derrp = c->derr.p;
+    q.op([=] { return cudaMemcpyAsync(res, vsrc, nvis * sizeof(float2), cudaMemcpyDeviceToHost, st); });
+    q.op([=] { return cudaMemcpyAsync(res + nvis * sizeof(float2), histp, (size_t)N * 64, cudaMemcpyDeviceToHost, st); });
+    q.op([=] {
+      return cudaMemcpyAsync(res + nvis * sizeof(float2) + (size_t)N * 64, derrp, sizeof(int), cudaMemcpyDeviceToHost,
+                             st);
+    });
+  }
+  q.record(sl.evs[ev + 1], st);
+  launches += 2 * nout;
+  Pending &pd = sl.pend;
+  pd.start = start;
+  pd.nvis = nvis;
+  pd.nout = nout;
+  pd.nphs = nphs;
+  pd.ev = ev;
+  pd.launches = launches;
+  pd.pulsar = pulsar;
+  pd.nfl = std::move(nfl);
+  pd.res = res;
+}
+
+// After the recorded work has run: device error flag, timings, statistics,
+// output bytes to the sink.
+int finish_integration(sfxc_gpu_ctx *c, int k, sfxc_output_sink sink, void *user) {
+  Slot &sl = *c->slots[k];
+  Pending &pd = sl.pend;
+  const int N = (int)c->streams.size(), nbl = (int)c->bl.size();
+  const size_t nvis = pd.nvis, ev = pd.ev;
+  const int nout = pd.nout, nphs = pd.nphs;
+  const bool pulsar = pd.pulsar;
+  const ticks_t start = pd.start;
+  const int launches = pd.launches;
+  const std::vector<std::pair<int64_t, int64_t>> &nfl = pd.nfl;
+  uint8_t *res = pd.res;
   const float2 *vis = reinterpret_cast<const float2 *>(res);
   const unsigned long long *hist = reinterpret_cast<const unsigned long long *>(res + nvis * sizeof(float2));
   const int *dev_err = reinterpret_cast<const int *>(res + nvis * sizeof(float2) + (size_t)N * 64);
-  CK(cudaMemcpyAsync(res, vsrc, nvis * sizeof(float2), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(res + nvis * sizeof(float2), c->hist.p, (size_t)N * 64, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(res + nvis * sizeof(float2) + (size_t)N * 64, c->derr.p, sizeof(int), cudaMemcpyDeviceToHost,
-                     st));
-  CK(cudaEventRecord(c->evpool[ev + 1], st));
-  launches += 2 * nout;
+  cudaStream_t st = c->st;
+  float t_f1 = 0, t_f2 = 0, t_x = 0;
   CK(cudaStreamSynchronize(st));
   if (*dev_err) throw Error(SFXC_GPU_ECUDA, "tensor-core X-step timed out waiting for its MMAs");
   for (size_t q = 0; q + 4 <= ev; q += 4) {
     float a, b, x;
-    CK(cudaEventElapsedTime(&a, c->evpool[q], c->evpool[q + 1]));
-    CK(cudaEventElapsedTime(&b, c->evpool[q + 1], c->evpool[q + 2]));
-    CK(cudaEventElapsedTime(&x, c->evpool[q + 2], c->evpool[q + 3]));
+    CK(cudaEventElapsedTime(&a, sl.evs[q], sl.evs[q + 1]));
+    CK(cudaEventElapsedTime(&b, sl.evs[q + 1], sl.evs[q + 2]));
+    CK(cudaEventElapsedTime(&x, sl.evs[q + 2], sl.evs[q + 3]));
     t_f1 += a;
     t_f2 += b;
     t_x += x;
   }
   float tn, tall;
-  CK(cudaEventElapsedTime(&tn, c->evpool[ev], c->evpool[ev + 1]));
-  CK(cudaEventElapsedTime(&tall, c->ev[0], c->evpool[ev + 1]));
+  CK(cudaEventElapsedTime(&tn, sl.evs[ev], sl.evs[ev + 1]));
+  CK(cudaEventElapsedTime(&tall, sl.ev0, sl.evs[ev + 1]));
   c->timings[5] = (float)launches;
   c->timings[0] = t_f1;
   c->timings[1] = t_f2;
@@ -1071,6 +1278,28 @@ int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
   return SFXC_GPU_OK;
 }
 
+// Copy the recorded uploads' payloads into the pinned arena (may allocate:
+// before any stream capture).
+void stage_ops(sfxc_gpu_ctx *c, int k) {
+  Slot &sl = *c->slots[k];
+  uint8_t *a = static_cast<uint8_t *>(sl.arena.ensure(std::max<size_t>(sl.q.host.size(), 16)));
+  if (!sl.q.host.empty()) std::memcpy(a, sl.q.host.data(), sl.q.host.size());
+}
+
+// Issue the recorded work on the context's streams (allocates nothing).
+void run_ops(sfxc_gpu_ctx *c, int k) {
+  Slot &sl = *c->slots[k];
+  const uint8_t *a = static_cast<const uint8_t *>(sl.arena.p);
+  for (auto &f : sl.q.ops) CK(f(a));
+}
+
+int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
+  enqueue_integration(c, 0);
+  stage_ops(c, 0);
+  run_ops(c, 0);
+  return finish_integration(c, 0, sink, user);
+}
+
 }  // namespace
 
 // ------------------------------------------------------------ C entry points
@@ -1103,7 +1332,6 @@ sfxc_gpu_ctx *sfxc_gpu_create(const sfxc_gpu_config *config) {
     const int prio = greatest + (int)(created.fetch_add(1) % (unsigned)std::max(levels - 1, 1));
     CK(cudaStreamCreateWithPriority(&c->st, cudaStreamNonBlocking, prio));
     CK(cudaStreamCreateWithPriority(&c->st2, cudaStreamNonBlocking, std::min(prio + 1, least)));
-    for (auto &e : c->ev) CK(cudaEventCreate(&e));
   } catch (const Error &e) {
     g_error = e.msg;
     return nullptr;
@@ -1116,9 +1344,7 @@ void sfxc_gpu_destroy(sfxc_gpu_ctx *c) {
   cudaSetDevice(c->device);
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->st2) cudaStreamSynchronize(c->st2);
-  for (auto &e : c->ev)
-    if (e) cudaEventDestroy(e);
-  for (auto &e : c->evpool) cudaEventDestroy(e);
+  c->slots.clear();
   if (c->st) cudaStreamDestroy(c->st);
   if (c->st2) cudaStreamDestroy(c->st2);
   delete c;
@@ -1207,6 +1433,88 @@ int sfxc_gpu_copy_unpacked(sfxc_gpu_ctx *c, int32_t stream, float *out, size_t n
   } catch (const Error &e) {
     return fail(c, e);
   }
+}
+
+int sfxc_gpu_autotune(sfxc_gpu_ctx *c, int32_t trials) {
+  if (!c || !c->have_job) return SFXC_GPU_ESTATE;
+  try {
+    const sfxc_gpu_ctx::TuneSpec &t = c->tune;
+    if (!t.dchunk) throw Error(SFXC_GPU_ESTATE, "no integration run yet");
+    if (trials <= 0) trials = 3;
+    CK(cudaSetDevice(c->device));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    // best of `trials` timings of each candidate, the launches rewriting the
+    // last chunk's own intermediates with the same values
+    auto time_best = [&](auto launch) {
+      float best = 1e30f;
+      launch();
+      for (int r = 0; r < trials; r++) {
+        cudaEventRecord(e0, c->st);
+        launch();
+        cudaEventRecord(e1, c->st);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        best = std::min(best, ms);
+      }
+      return best;
+    };
+    int tuned = 0;
+    {
+      const int cands[] = {4, 8, 12, 16, 24};
+      int best_v = 12;
+      float best_t = 1e30f;
+      for (int v : cands) {
+        const float ms = time_best([&] { launch_fstep(t.dchunk, t.nstreams, t.max_blocks, c->tw256.as<float2>(), c->st, v); });
+        if (ms < best_t) {
+          best_t = ms;
+          best_v = v;
+        }
+      }
+      plan_set(block_key(t.nstreams, t.max_blocks), best_v);
+      tuned++;
+    }
+    for (const auto &g : t.groups) {
+      const int rot = g[0], first = g[1], count = g[2];
+      const int nper = t.window == WINDOW_NONE ? rot / 2 : rot;
+      const sfxc_gpu_ctx::RotTables &rt = c->rot_tables.at(rot);
+      int best_v = 2;
+      float best_t = 1e30f;
+      for (int v : {1, 2, 3, 4}) {
+        const float ms = time_best([&] {
+          launch_window_fft(t.dchunk + t.nstreams + first, count, 0, t.nrows, t.max_rows, rt.window.as<float>(),
+                            rt.twrot.as<float2>(), rot, nper, t.M, t.kpad, t.spec, t.tc_slots, t.tc_scale, c->st, v);
+        });
+        if (ms < best_t) {
+          best_t = ms;
+          best_v = v;
+        }
+      }
+      plan_set(window_key(rot, count, t.nrows), best_v);
+      tuned++;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(cudaGetLastError());
+    return tuned;
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
+int sfxc_gpu_plan_cache(int32_t *out, int32_t capacity) {
+  std::lock_guard<std::mutex> lock(g_plan_mu);
+  int n = 0;
+  for (const auto &kv : g_plan) {
+    if (out && n < capacity) {
+      for (int i = 0; i < 4; i++) out[5 * n + i] = kv.first[i];
+      out[5 * n + 4] = kv.second;
+    }
+    n++;
+  }
+  return n;
 }
 
 int sfxc_gpu_copy_pulsar_bins(sfxc_gpu_ctx *c, int32_t *out, size_t n) {
@@ -1798,5 +2106,151 @@ int sfxc_gpu_reader_next(sfxc_gpu_reader *h, sfxc_reader_block *out) {
 }
 
 void sfxc_gpu_reader_destroy(sfxc_gpu_reader *h) { delete h; }
+
+// ---- batches: the next integration of several jobs in one CUDA graph
+struct sfxc_gpu_batch {
+  std::vector<sfxc_gpu_ctx *> ctx;
+  int device = 0;
+  cudaStream_t origin = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  float last_ms = 0.f;
+  std::string err;
+};
+
+sfxc_gpu_batch *sfxc_gpu_batch_create(sfxc_gpu_ctx *const *ctxs, int32_t n) {
+  try {
+    if (!ctxs || n <= 0) throw Error(SFXC_GPU_EINVAL, "no contexts");
+    std::unique_ptr<sfxc_gpu_batch> b(new sfxc_gpu_batch());
+    for (int i = 0; i < n; i++) {
+      if (!ctxs[i]) throw Error(SFXC_GPU_EINVAL, "null context");
+      for (sfxc_gpu_ctx *o : b->ctx)
+        if (o == ctxs[i]) throw Error(SFXC_GPU_EINVAL, "a context appears twice");
+      if (i > 0 && ctxs[i]->device != ctxs[0]->device) throw Error(SFXC_GPU_EINVAL, "contexts on different devices");
+      b->ctx.push_back(ctxs[i]);
+    }
+    b->device = ctxs[0]->device;
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&b->e0));
+    CK(cudaEventCreate(&b->e1));
+    CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    b->join.resize(n);
+    for (auto &e : b->join) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return b.release();
+  } catch (const Error &e) {
+    g_error = e.msg;
+    return nullptr;
+  }
+}
+
+void sfxc_gpu_batch_destroy(sfxc_gpu_batch *b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->origin) cudaStreamSynchronize(b->origin);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (cudaEvent_t e : {b->e0, b->e1, b->fork})
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : b->join)
+    if (e) cudaEventDestroy(e);
+  if (b->origin) cudaStreamDestroy(b->origin);
+  delete b;
+}
+
+int sfxc_gpu_batch_run_counts(sfxc_gpu_batch *b, const int32_t *counts, sfxc_output_sink sink, void *const *users) {
+  if (!b) return SFXC_GPU_EINVAL;
+  size_t i = 0;
+  const size_t n = b->ctx.size();
+  std::vector<int> cnt(n, 1);
+  try {
+    if (counts)
+      for (size_t k = 0; k < n; k++) {
+        if (counts[k] < 0) throw Error(SFXC_GPU_EINVAL, "negative integration count");
+        cnt[k] = counts[k];
+      }
+    CK(cudaSetDevice(b->device));
+    for (size_t k = 0; k < n; k++) {
+      sfxc_gpu_ctx *c = b->ctx[k];
+      if (!cnt[k]) continue;
+      if (!c->have_job) throw Error(SFXC_GPU_ESTATE, "a context of the batch has no parameters set");
+      for (const StreamCtx &s : c->sc)
+        if (!s.pushed) throw Error(SFXC_GPU_ESTATE, "a stream of the batch has no input for this integration");
+    }
+    // host planning of every integration of every job, its device work
+    // recorded and its upload payloads staged in pinned memory: nothing
+    // below allocates.  A job's later integrations take their input from the
+    // bytes pushed beyond the first one's.
+    for (size_t k = 0; k < n; k++)
+      for (int j = 0; j < cnt[k]; j++) {
+        enqueue_integration(b->ctx[k], j, j == 0);
+        stage_ops(b->ctx[k], j);
+      }
+    // all of it captured into one graph: each job on its own streams, its
+    // integrations in order, forked from and joined back into the batch's
+    // stream
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed));
+    try {
+      CK(cudaEventRecord(b->fork, b->origin));
+      for (size_t k = 0; k < n; k++) {
+        if (!cnt[k]) continue;
+        sfxc_gpu_ctx *c = b->ctx[k];
+        CK(cudaStreamWaitEvent(c->st, b->fork, 0));
+        for (int j = 0; j < cnt[k]; j++) run_ops(c, j);
+        CK(cudaEventRecord(b->join[k], c->st));
+        CK(cudaStreamWaitEvent(b->origin, b->join[k], 0));
+      }
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(b->origin, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    CK(cudaStreamEndCapture(b->origin, &graph));
+    // the previous executable graph takes the new node parameters when the
+    // topology is the same; else instantiate anew
+    bool updated = false;
+    if (b->exec) {
+      cudaGraphExecUpdateResultInfo info;
+      updated = cudaGraphExecUpdate(b->exec, graph, &info) == cudaSuccess;
+      if (!updated) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+      }
+    }
+    if (!updated) {
+      const cudaError_t e = cudaGraphInstantiate(&b->exec, graph, 0);
+      if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        throw CudaError(e, "cudaGraphInstantiate");
+      }
+    }
+    cudaGraphDestroy(graph);
+    CK(cudaEventRecord(b->e0, b->origin));
+    CK(cudaGraphLaunch(b->exec, b->origin));
+    CK(cudaEventRecord(b->e1, b->origin));
+    CK(cudaStreamSynchronize(b->origin));
+    CK(cudaEventElapsedTime(&b->last_ms, b->e0, b->e1));
+    for (i = 0; i < n; i++)
+      for (int j = 0; j < cnt[i]; j++) {
+        const int rc = finish_integration(b->ctx[i], j, sink, users ? users[i] : nullptr);
+        if (rc != SFXC_GPU_OK) return rc;
+      }
+    return SFXC_GPU_OK;
+  } catch (const Error &e) {
+    b->err = e.msg;
+    g_error = e.msg;
+    if (i < n) b->ctx[i]->err = e.msg;
+    return e.code;
+  }
+}
+
+int sfxc_gpu_batch_run(sfxc_gpu_batch *b, sfxc_output_sink sink, void *const *users) {
+  return sfxc_gpu_batch_run_counts(b, nullptr, sink, users);
+}
+
+float sfxc_gpu_batch_last_ms(const sfxc_gpu_batch *b) { return b ? b->last_ms : 0.f; }
 
 }  // extern "C"

@@ -1178,14 +1178,16 @@ void launch_block_params(const StreamDev *d_streams, int nstreams, int max_block
 void launch_fstep_block(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256,
                         cudaStream_t st) {
   launch_block_params(d_streams, nstreams, max_blocks, st);
-  launch_fstep(d_streams, nstreams, max_blocks, tw256, st);
+  launch_fstep(d_streams, nstreams, max_blocks, tw256, st, 0);
 }
 
-void launch_fstep(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256, cudaStream_t st) {
-  // about three waves of 4 resident CTAs per SM, each CTA looping over rounds
-  // (measured against 1, 2, 4 and 6 waves: 2 % faster than two, the others
-  // slower still)
-  const int per_stream = std::max(1, 12 * sm_count() / nstreams);
+void launch_fstep(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256, cudaStream_t st,
+                  int ctas_per_sm) {
+  // by default about three waves of 4 resident CTAs per SM, each CTA looping
+  // over rounds (measured against 1, 2, 4 and 6 waves on the 32-stream,
+  // 4096-channel job: 2 % faster than two, the others slower still); the
+  // autotuner may pick another count per shape
+  const int per_stream = std::max(1, (ctas_per_sm > 0 ? ctas_per_sm : 12) * sm_count() / nstreams);
   dim3 grid(std::min((max_blocks + 31) / 32, per_stream), nstreams);
   constexpr int smem = 16 * kFsScratch * sizeof(float2);
   cudaFuncSetAttribute(fstep_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -1250,13 +1252,14 @@ void launch_phasecal(const uint8_t *data, const PcalRun *runs, int nruns, int pb
 template <int LOGN, int OUT_TC, int SPCMAX>
 static void window_fft_launch_spc(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                                   const float *window, const float2 *tw_rot, int nper, int M, int kpad, void *spec,
-                                  float tc_scale, int tc_slots, cudaStream_t st) {
+                                  float tc_scale, int tc_slots, cudaStream_t st, int waves) {
   using S = WinShape<LOGN, SPCMAX>;
   const int nsg = (nstreams + S::SPC - 1) / S::SPC, nsteps = (nrows + S::RPC - 1) / S::RPC;
-  // runs of steps so that the CTAs fill two waves
+  // runs of steps so that the CTAs fill two waves by default (three or four
+  // waves measured 1 % slower on the 32-stream, 4096-channel job); the
+  // autotuner may pick another count per shape
   const int per_sm = 1024 / S::THREADS;
-  // (three or four waves measured 1 % slower)
-  const int runs = std::max(1, std::min(nsteps, 2 * per_sm * sm_count() / nsg));
+  const int runs = std::max(1, std::min(nsteps, (waves > 0 ? waves : 2) * per_sm * sm_count() / nsg));
   const int steps_per_cta = (nsteps + runs - 1) / runs;
   const unsigned grid = (unsigned)(nsg * ((nsteps + steps_per_cta - 1) / steps_per_cta));
   auto kern = window_fft_kernel<LOGN, OUT_TC, SPCMAX>;
@@ -1268,11 +1271,13 @@ static void window_fft_launch_spc(const StreamDev *d_streams, int nstreams, int 
 template <int LOGN, int OUT_TC>
 static void window_fft_launch(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                               const float *window, const float2 *tw_rot, int nper, int M, int kpad, void *spec,
-                              float tc_scale, int tc_slots, cudaStream_t st) {
+                              float tc_scale, int tc_slots, cudaStream_t st, int waves) {
   // four streams per CTA: a whole 32-byte sector per channel in the TC layout
-  // (two streams per CTA, two CTAs per SM, measured 20 % slower)
+  // (two streams per CTA, two CTAs per SM, measured 20 % slower; each group
+  // writing its own stream's 8-byte pieces, without the CTA-wide barriers,
+  // 74 % slower)
   window_fft_launch_spc<LOGN, OUT_TC, 4>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad,
-                                         spec, tc_scale, tc_slots, st);
+                                         spec, tc_scale, tc_slots, st, waves);
 }
 
 #define SFXC_LOGN_SWITCH(logn, CALL) \
@@ -1289,17 +1294,17 @@ static void window_fft_launch(const StreamDev *d_streams, int nstreams, int row0
 
 void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                        const float *window, const float2 *tw_rot, int rot, int nper, int M, int kpad, void *spec,
-                       int tc_slots, float tc_scale, cudaStream_t st) {
+                       int tc_slots, float tc_scale, cudaStream_t st, int waves) {
   const int logn = 30 - __builtin_clz((unsigned)rot);  // log2(rot / 2)
 #define SFXC_WIN(L)                                                                                            \
   (tc_slots == kTcSlots                                                                                         \
        ? window_fft_launch<L, kTcSlots>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M,  \
-                                        kpad, spec, tc_scale, tc_slots, st)                                   \
+                                        kpad, spec, tc_scale, tc_slots, st, waves)                            \
    : tc_slots == kTcSlotsWide                                                                                    \
        ? window_fft_launch<L, kTcSlotsWide>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, \
-                                            M, kpad, spec, tc_scale, tc_slots, st)                            \
+                                            M, kpad, spec, tc_scale, tc_slots, st, waves)                     \
        : window_fft_launch<L, 0>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad,    \
-                                 spec, tc_scale, 0, st))
+                                 spec, tc_scale, 0, st, waves))
   SFXC_LOGN_SWITCH(logn, SFXC_WIN)
 #undef SFXC_WIN
 }

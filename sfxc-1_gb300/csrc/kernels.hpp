@@ -14,14 +14,17 @@ void launch_fstep_block(const StreamDev *d_streams, int nstreams, int max_blocks
 // ctas_per_sm > 0: at most that many CTAs per SM in all (each striding over its stream's blocks)
 void launch_block_params(const StreamDev *d_streams, int nstreams, int max_blocks, cudaStream_t st,
                          int ctas_per_sm = 0);
-void launch_fstep(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256, cudaStream_t st);
+// ctas_per_sm: grid of the block stage, CTAs per SM over all streams (0: the default, 12)
+void launch_fstep(const StreamDev *d_streams, int nstreams, int max_blocks, const float2 *tw256, cudaStream_t st,
+                  int ctas_per_sm = 0);
 void launch_unpack(const StreamDev *d_streams, int nstreams, int max_blocks, float *out, cudaStream_t st);
 void launch_extract(const uint8_t *in, int64_t nout, int N, int bits, int nsub, int fan_out, const int *tracks,
                     uint8_t *out, cudaStream_t st);
 // tc_slots: slots per (row, channel) of the TC layout (32 or 64); 0 writes the FP32 layout
+// waves: resident-CTA waves the runs of rows are cut into (0: the default, 2)
 void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                        const float *window, const float2 *tw_rot, int rot, int nper, int M, int kpad, void *spec,
-                       int tc_slots, float tc_scale, cudaStream_t st);
+                       int tc_slots, float tc_scale, cudaStream_t st, int waves = 0);
 void launch_bitstat(const StreamDev *d_streams, const int4 *d_items, int nitems, cudaStream_t st);
 // FP32 X-step (xcorr_f32_kernel): launch arguments and work split
 constexpr int kF32Stages = 4;         // cp.async ring depth

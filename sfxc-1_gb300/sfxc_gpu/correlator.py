@@ -174,6 +174,11 @@ class CorrelatorNode:
         self._check(self._lib.sfxc_gpu_copy_spectra(self._h, stream, out.ctypes.data, out.size * 2))
         return out
 
+    def autotune(self, trials=3):
+        """Tune the F-step launch shapes on the last integration (sfxc_gpu_autotune);
+        returns the number of shapes tuned."""
+        return self._check(self._lib.sfxc_gpu_autotune(self._h, trials))
+
     def pulsar_bins(self, nrows, nchan):
         """Pulsar bin of every FFT row and channel of the last integration:
         int32 [nrows][nchan + 1] (0 off-pulse)."""
@@ -354,6 +359,92 @@ def write_protocol(blocks, slices, sample_rate, bits, integration_time_us):
         raise L.SfxcError(int(n), lib.sfxc_gpu_global_error().decode())
     raw = bytes(out)[:n]
     return [raw[offs[i]:offs[i + 1]] for i in range(len(slices))]
+
+
+def plan_cache():
+    """The autotuner's plan cache: [(kernel, shape..., variant)]."""
+    lib = L.load()
+    n = lib.sfxc_gpu_plan_cache(None, 0)
+    out = (C.c_int32 * (5 * max(n, 1)))()
+    n = lib.sfxc_gpu_plan_cache(out, n)
+    return [tuple(out[5 * i:5 * i + 5]) for i in range(n)]
+
+
+class Batch:
+    """Several correlator nodes' jobs (one timeslice: any mix of stream
+    counts, rates, bit depths, FFT lengths and integration times) correlated
+    together, one CUDA graph per integration (sfxc_gpu_batch_*).  Each node
+    needs its parameters set and its input pushed before run()."""
+
+    def __init__(self, nodes):
+        self._lib = L.load()
+        self.nodes = list(nodes)
+        arr = (C.c_void_p * len(self.nodes))(*[n._h for n in self.nodes])
+        self._h = self._lib.sfxc_gpu_batch_create(arr, len(self.nodes))
+        if not self._h:
+            raise L.SfxcError(L.EINVAL, self._lib.sfxc_gpu_global_error().decode())
+
+    def run(self, counts=None):
+        """The next integration (or counts[i] integrations) of every node:
+        [(output bytes, [tsys records])] in node order."""
+        outs = [([], []) for _ in self.nodes]
+
+        def sink(user, kind, data, n):
+            b = bytearray(n)
+            if n:
+                C.memmove((C.c_char * n).from_buffer(b), data, n)
+            o = outs[user or 0]
+            (o[0] if kind == 0 else o[1]).append(bytes(b))
+            return 0
+
+        cb = L.SINK(sink)
+        users = (C.c_void_p * len(self.nodes))(*range(len(self.nodes)))
+        if counts is None:
+            rc = self._lib.sfxc_gpu_batch_run(self._h, cb, users)
+        else:
+            cnt = (C.c_int32 * len(self.nodes))(*counts)
+            rc = self._lib.sfxc_gpu_batch_run_counts(self._h, cnt, cb, users)
+        if rc < 0:
+            raise L.SfxcError(rc, self._lib.sfxc_gpu_global_error().decode())
+        return [(b"".join(o), t) for o, t in outs]
+
+    def last_ms(self):
+        return float(self._lib.sfxc_gpu_batch_last_ms(self._h))
+
+    def correlate(self, jobs, per_run=None):
+        """Every integration of the jobs (one per node; any integration
+        counts): per_run[i] integrations of job i in each graph (default: all
+        of them in one).  Returns [(cor, tsys)] per job."""
+        for n, j in zip(self.nodes, jobs):
+            n.set_parameters(j)
+        left = [int(j["n_integrations"]) for j in jobs]
+        step = per_run or left
+        done = [0] * len(jobs)
+        cor = [[] for _ in jobs]
+        tsys = [[] for _ in jobs]
+        while any(left):
+            counts = [min(s, l) for s, l in zip(step, left)]
+            for n, j, d, c in zip(self.nodes, jobs, done, counts):
+                for it in range(d, d + c):
+                    for k in range(n.nstreams):
+                        n.push_protocol(k, j["protocols"][k][it])
+            for q, (o, t) in enumerate(self.run(counts)):
+                cor[q].append(o)
+                tsys[q] += t
+            done = [d + c for d, c in zip(done, counts)]
+            left = [l - c for l, c in zip(left, counts)]
+        return [(b"".join(c), b"".join(t)) for c, t in zip(cor, tsys)]
+
+    def close(self):
+        if self._h:
+            self._lib.sfxc_gpu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class OutputFiles:

@@ -274,3 +274,46 @@ def c5_pulsar(n_stations=10, integration_us=1_000_000, subband=0, seed=5, n_inte
                     channel_freq=1_400_000_000 + subband * 16_000_000, nchan=2048, integration_us=integration_us,
                     n_integrations=n_integrations, sub_integration_us=125000, lead_us=12000, seed=seed + subband,
                     block_bytes=2000, frequency_nr=subband)
+
+
+def c4_jobs(scale=1.0, seed=11, subbands=(0, 1, 2, 3), fine_subbands=(0, 1), narrow_subbands=(0, 1)):
+    """The batched uneven configuration's jobs of one timeslice (2 s x scale),
+    on 20 stations with cubic delay models: 12 record 32 MHz at 64 MS/s
+    2-bit, 6 record 64 MHz at 128 MS/s 2-bit, 2 record 16 MHz at 32 MS/s
+    1-bit.  Three kinds of job, each its own integration time:
+      A (one per entry of `subbands`): a 32 MHz subband at 64 MS/s with all
+        20 stations dual-pol (40 streams: the 64 MHz stations correlated at
+        twice the job rate, the 16 MHz ones at half of it over their part of
+        the band), 4096 channels, 2 s integrations;
+      B (fine_subbands): the 12 32-MHz stations, 16384 channels (windowed
+        FFTs of 32768 samples), 0.5 s integrations;
+      C (narrow_subbands): a 16 MHz subband at 32 MS/s with the 8 other
+        stations (the 64 MHz ones at four times the job rate), 256 channels,
+        0.25 s integrations.
+    Returns [Scenario]; each job's integrations cover the timeslice."""
+    st = cubic_stations(20, seed=900 + seed, max_delay=1e-2, max_rate=3e-6)
+    span = int(round(2_000_000 * scale))
+    out = []
+    for sb in subbands:
+        modes = {st[i].number: (128_000_000, 2, -32_000_000 if sb % 2 else 0) for i in range(12, 18)}
+        modes.update({st[i].number: (32_000_000, 1, 16_000_000 if sb % 2 else 0) for i in range(18, 20)})
+        iu = span
+        out.append(Scenario(stations=st, pols=("R", "L"), sample_rate=64_000_000, bandwidth=32_000_000, bits=2,
+                            channel_freq=4_800_000_000 + sb * 32_000_000, nchan=4096, integration_us=iu,
+                            n_integrations=max(1, span // iu), sub_integration_us=125000, lead_us=12000,
+                            seed=seed * 10 + sb, block_bytes=2000, frequency_nr=sb, station_modes=modes))
+    for sb in fine_subbands:
+        iu = max(1, span // 4)
+        out.append(Scenario(stations=st[:12], pols=("R", "L"), sample_rate=64_000_000, bandwidth=32_000_000, bits=2,
+                            channel_freq=4_800_000_000 + sb * 32_000_000, nchan=16384, integration_us=iu,
+                            n_integrations=max(1, span // iu), sub_integration_us=125000, lead_us=12000,
+                            seed=seed * 10 + 5 + sb, block_bytes=2000, frequency_nr=8 + sb))
+    for sb in narrow_subbands:
+        iu = max(1, span // 8)
+        modes = {st[i].number: (128_000_000, 2, -16_000_000 * (sb % 4)) for i in range(12, 18)}
+        modes.update({st[i].number: (32_000_000, 1, 0) for i in range(18, 20)})
+        out.append(Scenario(stations=st[12:], pols=("R", "L"), sample_rate=32_000_000, bandwidth=16_000_000, bits=2,
+                            channel_freq=4_800_000_000 + sb * 16_000_000, nchan=256, integration_us=iu,
+                            n_integrations=max(1, span // iu), sub_integration_us=125000, lead_us=12000,
+                            seed=seed * 10 + 7 + sb, block_bytes=2000, frequency_nr=16 + sb, station_modes=modes))
+    return out
