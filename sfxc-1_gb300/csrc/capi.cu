@@ -145,8 +145,14 @@ struct Ops {
   void memset(void *p, int v, size_t n, cudaStream_t st) {
     ops.push_back([=](const uint8_t *) { return cudaMemsetAsync(p, v, n, st); });
   }
+  // a dependency between the context's streams (inside a capture: an edge of the graph)
   void record(cudaEvent_t e, cudaStream_t st) {
     ops.push_back([=](const uint8_t *) { return cudaEventRecord(e, st); });
+  }
+  // a timing mark (inside a capture: an event-record node, so that the
+  // event's time can be read after the graph ran)
+  void mark(cudaEvent_t e, cudaStream_t st) {
+    ops.push_back([=](const uint8_t *) { return cudaEventRecordWithFlags(e, st, cudaEventRecordExternal); });
   }
   void wait(cudaStream_t st, cudaEvent_t e) {
     ops.push_back([=](const uint8_t *) { return cudaStreamWaitEvent(st, e, 0); });
@@ -183,10 +189,12 @@ struct Slot {
   Ops q;
   HostBuf arena, results;
   Pending pend;
-  std::vector<cudaEvent_t> evs;
+  std::vector<cudaEvent_t> evs;   // timing marks
+  std::vector<cudaEvent_t> deps;  // dependencies between the context's two streams
   cudaEvent_t ev0 = nullptr;
   ~Slot() {
     for (cudaEvent_t e : evs) cudaEventDestroy(e);
+    for (cudaEvent_t e : deps) cudaEventDestroy(e);
     if (ev0) cudaEventDestroy(ev0);
   }
 };
@@ -931,13 +939,20 @@ void enqueue_integration(sfxc_gpu_ctx *c, int k = 0, bool require_push = true) {
       c->segs.ensure((size_t)K * c->nbins * sizeof(int2));
     }
   }
-  // four events per chunk on the main stream and one on the second (+2 for
-  // normalisation), recorded without host syncs
-  const size_t nev = ranges.size() * 5 + 2;
+  // four timing marks per chunk (+2 for normalisation), recorded without
+  // host syncs
+  const size_t nev = ranges.size() * 4 + 2;
   while (sl.evs.size() < nev) {
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
     sl.evs.push_back(e);
+  }
+  // the start, each chunk's parameters ready (second stream), each chunk's
+  // windowed FFT done (main stream)
+  while (sl.deps.size() < 1 + 2 * ranges.size()) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    sl.deps.push_back(e);
   }
   // ---- every chunk's stream descriptors, in job order and then grouped by
   // windowed-FFT length (job order within a group), in one asynchronous
@@ -999,18 +1014,18 @@ void enqueue_integration(sfxc_gpu_ctx *c, int k = 0, bool require_push = true) {
     }
     q.upload(c->uvp, uv.data(), uv.size() * sizeof(UvShift), st);
   }
-  q.record(sl.ev0, st);
+  q.mark(sl.ev0, st);
+  q.record(sl.deps[0], st);
   // The per-block parameters (block_params_kernel, FP64-pipe bound, few
   // registers) run on the second stream: those of the first chunk beside the
   // bit statistics (memory bound), those of chunk ch + 1 once chunk ch's
   // windowed FFT is done, i.e. beside chunk ch's X-step, whose CTAs leave
   // registers and issue slots free.  Each chunk's transforms wait for them.
-  const size_t ev_side = ranges.size() * 4 + 2;  // the second stream's events, one per chunk
-  q.wait(c->st2, sl.ev0);  // the descriptors are on the device
+  q.wait(c->st2, sl.deps[0]);  // the descriptors are on the device
   StreamDev *const sdev = c->streamdev.as<StreamDev>();
   cudaStream_t st2 = c->st2;
   q.kernel([=] { launch_block_params(sdev, N, max_blocks, st2); });
-  q.record(sl.evs[ev_side], c->st2);
+  q.record(sl.deps[1], c->st2);
   // bit statistics read only chunk-independent fields (source bytes, ranges, histograms)
   {
     const int4 *ditems = c->items.as<int4>();
@@ -1022,14 +1037,14 @@ void enqueue_integration(sfxc_gpu_ctx *c, int k = 0, bool require_push = true) {
   for (size_t ch = 0; ch < ranges.size(); ch++) {
     const int nrows = ranges[ch].second - ranges[ch].first;
     StreamDev *dchunk = sdev + ch * per_chunk;
-    q.record(sl.evs[ev], st);
-    q.wait(st, sl.evs[ev_side + ch]);
+    q.mark(sl.evs[ev], st);
+    q.wait(st, sl.deps[1 + ch]);
     {
       const float2 *tw256 = c->tw256.as<float2>();
       const int fw = plan_get(block_key(N, max_blocks));
       q.kernel([=] { launch_fstep(dchunk, N, max_blocks, tw256, st, fw); });
     }
-    q.record(sl.evs[ev + 1], st);
+    q.mark(sl.evs[ev + 1], st);
     for (size_t g = 0; g < groups.size(); g++) {
       const int rot = groups[g].first, first = groups[g].second;
       const int count = (g + 1 < groups.size() ? groups[g + 1].second : N) - first;
@@ -1044,15 +1059,16 @@ void enqueue_integration(sfxc_gpu_ctx *c, int k = 0, bool require_push = true) {
                           tc_scale, st, ww);
       });
     }
-    q.record(sl.evs[ev + 2], st);
+    q.mark(sl.evs[ev + 2], st);
+    q.record(sl.deps[1 + ranges.size() + ch], st);
     if (ch + 1 < ranges.size()) {
       // chunk ch + 1's records go to the other set, last read by chunk ch - 1's
       // transforms.  (Starting them once chunk ch's transforms are done, to
       // fill the windowed FFT's tail, measured slower: their CTAs then hold
       // SMs when the X-step's persistent CTAs are placed.)
-      q.wait(c->st2, sl.evs[ev + 2]);
+      q.wait(c->st2, sl.deps[1 + ranges.size() + ch]);
       q.kernel([=] { launch_block_params(dchunk + per_chunk, N, max_blocks, st2, kSideParamCtas); });
-      q.record(sl.evs[ev_side + ch + 1], c->st2);
+      q.record(sl.deps[1 + ch + 1], c->st2);
     }
     {
       // X-step of the chunk (pointers and sizes taken now; the buffers are sized above)
@@ -1114,7 +1130,7 @@ void enqueue_integration(sfxc_gpu_ctx *c, int k = 0, bool require_push = true) {
         launches += 1;
       }
     }
-    q.record(sl.evs[ev + 3], st);
+    q.mark(sl.evs[ev + 3], st);
     ev += 4;
     launches += pulsar ? 5 : 4;  // parameters, blocks, window FFT, (pulsar bins,) X-step
   }
@@ -1143,7 +1159,7 @@ void enqueue_integration(sfxc_gpu_ctx *c, int k = 0, bool require_push = true) {
     c->hsd[i].spline_lo = spline_lo_for(c->hsd[i], c->sc[i].sp.x);
   }
   // ---- normalisation and statistics
-  q.record(sl.evs[ev], st);
+  q.mark(sl.evs[ev], st);
   c->norms.ensure((size_t)N * 8);
   // outputs: the pulsar bins, or the phase centres (each normalised on its
   // own); the phased array writes its sub-integration sums as they are
@@ -1189,7 +1205,7 @@ void enqueue_integration(sfxc_gpu_ctx *c, int k = 0, bool require_push = true) {
                              st);
     });
   }
-  q.record(sl.evs[ev + 1], st);
+  q.mark(sl.evs[ev + 1], st);
   launches += 2 * nout;
   Pending &pd = sl.pend;
   pd.start = start;
