@@ -222,7 +222,8 @@ struct sfxc_gpu_ctx {
   std::vector<DelayTable> tables;
   std::vector<int> stream_table;
   std::vector<Polyco> polyco;
-  int current_integration = 0;
+  int current_integration = 0;  // integrations finished (output written)
+  int planned_integration = 0;  // integrations planned (several may be in flight in a batch)
   std::vector<StreamCtx> sc;
   std::vector<Baseline> bl;
   JobTables jt;
@@ -593,6 +594,7 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
   }
   CK(cudaStreamSynchronize(c->st));
   c->current_integration = 0;
+  c->planned_integration = 0;
   c->have_job = true;
 }
 
@@ -712,7 +714,8 @@ void enqueue_integration(sfxc_gpu_ctx *c, int k = 0, bool require_push = true) {
   for (int i = 0; i < N; i++)
     if (require_push && !c->sc[i].pushed) throw Error(SFXC_GPU_ESTATE, "a stream has no input for this integration");
   const ticks_t tint = time_from_usec((double)c->p.integration_time_us);
-  const ticks_t start = c->p.start_ticks + (ticks_t)c->current_integration * tint;
+  const ticks_t start = c->p.start_ticks + (ticks_t)c->planned_integration * tint;
+  c->planned_integration++;
   const int M = c->M, K = c->K, kpad = c->kpad, nbl = (int)c->bl.size();
   cudaStream_t st = c->st;
   // ---- host planning per stream (Bit2float_worker state machine replica)
@@ -1310,10 +1313,15 @@ void run_ops(sfxc_gpu_ctx *c, int k) {
 }
 
 int run_integration(sfxc_gpu_ctx *c, sfxc_output_sink sink, void *user) {
-  enqueue_integration(c, 0);
-  stage_ops(c, 0);
-  run_ops(c, 0);
-  return finish_integration(c, 0, sink, user);
+  try {
+    enqueue_integration(c, 0);
+    stage_ops(c, 0);
+    run_ops(c, 0);
+    return finish_integration(c, 0, sink, user);
+  } catch (...) {
+    c->planned_integration = c->current_integration;  // the failed integration is not counted
+    throw;
+  }
 }
 
 }  // namespace
@@ -2259,6 +2267,7 @@ int sfxc_gpu_batch_run_counts(sfxc_gpu_batch *b, const int32_t *counts, sfxc_out
     b->err = e.msg;
     g_error = e.msg;
     if (i < n) b->ctx[i]->err = e.msg;
+    for (sfxc_gpu_ctx *c : b->ctx) c->planned_integration = c->current_integration;
     return e.code;
   }
 }
