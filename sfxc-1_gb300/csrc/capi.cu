@@ -152,7 +152,13 @@ struct Ops {
   // a timing mark (inside a capture: an event-record node, so that the
   // event's time can be read after the graph ran)
   void mark(cudaEvent_t e, cudaStream_t st) {
-    ops.push_back([=](const uint8_t *) { return cudaEventRecordWithFlags(e, st, cudaEventRecordExternal); });
+    ops.push_back([=](const uint8_t *) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      const cudaError_t r = cudaStreamIsCapturing(st, &cs);
+      if (r != cudaSuccess) return r;
+      return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(e, st, cudaEventRecordExternal)
+                                                 : cudaEventRecord(e, st);
+    });
   }
   void wait(cudaStream_t st, cudaEvent_t e) {
     ops.push_back([=](const uint8_t *) { return cudaStreamWaitEvent(st, e, 0); });
