@@ -38,6 +38,11 @@ struct CudaError : Error {
     if (e_ != cudaSuccess) throw CudaError(e_, #x); \
   } while (0)
 
+// While a batch plans several integrations whose device work runs later,
+// buffers that grow keep their old allocation alive (work already recorded
+// refers to it) and free it once the batch has run.
+thread_local std::vector<void *> *g_retired = nullptr;
+
 // Device buffer that only grows.  Move-only: freeing device memory
 // synchronises the whole device, so buffers are kept and handed on (swap)
 // rather than freed between jobs.
@@ -57,7 +62,12 @@ struct DevBuf {
   }
   void *ensure(size_t n) {
     if (n > cap) {
-      if (p) cudaFree(p);
+      if (p) {
+        if (g_retired)
+          g_retired->push_back(p);
+        else
+          cudaFree(p);
+      }
       p = nullptr;
       cap = 0;
       CK(cudaMalloc(&p, n));
@@ -68,7 +78,11 @@ struct DevBuf {
   template <class T>
   T *as() const { return reinterpret_cast<T *>(p); }
   ~DevBuf() {
-    if (p) cudaFree(p);
+    if (!p) return;
+    if (g_retired)
+      g_retired->push_back(p);
+    else
+      cudaFree(p);
   }
 };
 
@@ -178,6 +192,7 @@ struct Ops {
 
 // What finish_integration needs of an enqueued integration.
 struct Pending {
+  std::vector<int64_t> n_invalid;  // per stream, of this integration's unpack plan
   ticks_t start = 0;
   size_t nvis = 0, ev = 0;
   int nout = 0, nphs = 0, launches = 0;
@@ -1226,6 +1241,8 @@ void enqueue_integration(sfxc_gpu_ctx *c, int k = 0, bool require_push = true) {
   pd.pulsar = pulsar;
   pd.nfl = std::move(nfl);
   pd.res = res;
+  pd.n_invalid.resize(N);
+  for (int i = 0; i < N; i++) pd.n_invalid[i] = c->sc[i].plan.n_invalid;
 }
 
 // After the recorded work has run: device error flag, timings, statistics,
@@ -1272,7 +1289,7 @@ int finish_integration(sfxc_gpu_ctx *c, int k, sfxc_output_sink sink, void *user
       bs.on[k] = (int64_t)hist[(size_t)i * 8 + k];
       bs.off[k] = (int64_t)hist[(size_t)i * 8 + 4 + k];
     }
-    bs.n_invalid = c->sc[i].plan.n_invalid;
+    bs.n_invalid = pd.n_invalid[i];
     bs.bits = c->streams[i].bits;
     bs.sample_rate = c->streams[i].sample_rate;
     bs.base_sample_rate = c->p.sample_rate;
@@ -2210,12 +2227,23 @@ int sfxc_gpu_batch_run_counts(sfxc_gpu_batch *b, const int32_t *counts, sfxc_out
     // host planning of every integration of every job, its device work
     // recorded and its upload payloads staged in pinned memory: nothing
     // below allocates.  A job's later integrations take their input from the
-    // bytes pushed beyond the first one's.
+    // bytes pushed beyond the first one's.  A buffer that grows for a later
+    // integration keeps its old allocation (earlier work refers to it) until
+    // the batch has run.
+    struct Retire {
+      std::vector<void *> list;
+      Retire() { g_retired = &list; }
+      ~Retire() {
+        g_retired = nullptr;
+        for (void *p : list) cudaFree(p);
+      }
+    } retire;
     for (size_t k = 0; k < n; k++)
       for (int j = 0; j < cnt[k]; j++) {
         enqueue_integration(b->ctx[k], j, j == 0);
         stage_ops(b->ctx[k], j);
       }
+    g_retired = nullptr;  // nothing is allocated below; what grew is freed when the batch returns
     // all of it captured into one graph: each job on its own streams, its
     // integrations in order, forked from and joined back into the batch's
     // stream
