@@ -427,14 +427,21 @@ C4_NAME = ("20 stations (12 x 32 MHz 2-bit at 64 MS/s, 6 x 64 MHz 2-bit at 128 M
 def measure_c4(args, log, x_mode="tc"):
     """The batched uneven configuration: every job of one 2 s timeslice, all
     their integrations in one CUDA graph per step (sfxc_gpu_batch_run_counts),
-    inputs in host memory pushed through the C ABI each step.  Device time:
+    inputs in pinned host memory pushed through the C ABI each step.  Device time:
     CUDA events around the graph launch; e2e: wall clock of the whole step."""
     from sfxc_gpu import correlator, lib, scenario
+    import torch
     scs = scenario.c4_jobs(scale=1.0)
-    jobs = []
+    jobs, keep = [], []
+
+    def alloc(n):  # protocol bytes in pinned host memory, as the headline e2e
+        buf = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+        keep.append(buf)
+        return buf.numpy()
+
     for i, sc in enumerate(scs):
         t = time.time()
-        j = scenario.build_job_bulk(sc)
+        j = scenario.build_job_bulk(sc, alloc=alloc)
         jobs.append(j)
         log("built C4 job %d (%d streams, %d channels, %d x %d us) in %.1f s"
             % (i, len(sc.streams()), sc.nchan, sc.n_integrations, sc.integration_us, time.time() - t))

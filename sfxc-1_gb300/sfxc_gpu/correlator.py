@@ -124,6 +124,10 @@ class CorrelatorNode:
         self.job = job
 
     def push_protocol(self, stream, data):
+        """data: bytes, or a contiguous uint8 numpy array (passed without a copy)."""
+        if isinstance(data, np.ndarray) and data.dtype == np.uint8 and data.flags.c_contiguous:
+            self._check(self._lib.sfxc_gpu_push_protocol(self._h, stream, C.c_void_p(data.ctypes.data), data.size))
+            return
         buf = _bytes_ptr(data)
         self._check(self._lib.sfxc_gpu_push_protocol(self._h, stream, buf, len(data)))
 
