@@ -156,6 +156,61 @@ def reader(recording, fmt, *, ref_ticks, offset_ticks=0, track_bit_rate, frame_s
         return blocks
 
 
+def correlate_lines(job, d, dump=False, precision=32, dump_bins=False):
+    """The job file lines of the 'correlate' mode for a job dict, with its
+    delay tables, protocols and mask files written into directory d (read by
+    the reference harness, the restatement and the adapter driver)."""
+    lines = []
+    for k, db in enumerate(job["del_bytes"]):
+        p = os.path.join(d, "st%d.del" % k)
+        open(p, "wb").write(db)
+        lines.append(("delfile", p))
+    for key in ["experiment_start_ticks", "start_ticks", "integration_time_us",
+                "sub_integration_time_us", "number_channels", "fft_size_delaycor",
+                "fft_size_correlation", "sample_rate", "channel_freq", "bandwidth", "sideband",
+                "frequency_nr", "polarisation", "cross_polarize", "reference_station", "window",
+                "source", "integration_nr", "n_integrations"]:
+        lines.append((key, job[key]))
+    for k, s in enumerate(job["streams"]):
+        lines.append(("stream",) + tuple(s))
+        p = os.path.join(d, "proto%d.bin" % k)
+        with open(p, "wb") as f:
+            for chunk in job["protocols"][k]:
+                f.write(np.uint64(len(chunk)).tobytes())
+                f.write(bytes(chunk))
+        lines.append(("protocol", p))
+    # Mask_parameters (spectral reduction): float32 files, and the flag
+    for key in ("mask", "lag_window"):
+        if job.get(key) is not None:
+            p = os.path.join(d, key + ".f32")
+            np.asarray(job[key], dtype=np.float32).tofile(p)
+            lines.append((key, p))
+    if job.get("mask_normalize"):
+        lines.append(("mask_normalize", 1))
+    # UVW for the timeslice headers: float64 [integration][stream][centre][3]
+    if job.get("uvw") is not None:
+        p = os.path.join(d, "uvw.f64")
+        np.asarray(job["uvw"], dtype=np.float64).tofile(p)
+        lines.append(("uvw", p))
+    if job.get("phased_array"):
+        lines.append(("phased_array", 1))
+    if int(job.get("n_phase_centers", 1)) > 1:
+        lines.append(("n_phase_centers", int(job["n_phase_centers"])))
+        if job.get("pc_file_index") is not None:
+            lines.append(("pc_file_index",) + tuple(int(x) for x in job["pc_file_index"]))
+    if "pulsar" in job:
+        lines.append(("pulsar",) + tuple(job["pulsar"]))
+        for pc in job["polyco"]:
+            lines.append(("polyco",) + tuple(pc))
+    if dump:
+        lines.append(("dump", 1))
+    if dump_bins:
+        lines.append(("dump_bins", 1))
+    if precision != 32:
+        lines.append(("precision", precision))
+    return lines
+
+
 def correlate(job, dump=False, impl="reference", precision=32, dump_bins=False):
     """Run Bit2float_worker -> Delay_correction -> Correlation_core(_pulsar).
 
@@ -166,54 +221,7 @@ def correlate(job, dump=False, impl="reference", precision=32, dump_bins=False):
     dump_bins=True (restatement): only the pulsar bin table, res["bins"].
     """
     with tempfile.TemporaryDirectory() as d:
-        lines = []
-        for k, db in enumerate(job["del_bytes"]):
-            p = os.path.join(d, "st%d.del" % k)
-            open(p, "wb").write(db)
-            lines.append(("delfile", p))
-        for key in ["experiment_start_ticks", "start_ticks", "integration_time_us",
-                    "sub_integration_time_us", "number_channels", "fft_size_delaycor",
-                    "fft_size_correlation", "sample_rate", "channel_freq", "bandwidth", "sideband",
-                    "frequency_nr", "polarisation", "cross_polarize", "reference_station", "window",
-                    "source", "integration_nr", "n_integrations"]:
-            lines.append((key, job[key]))
-        for k, s in enumerate(job["streams"]):
-            lines.append(("stream",) + tuple(s))
-            p = os.path.join(d, "proto%d.bin" % k)
-            with open(p, "wb") as f:
-                for chunk in job["protocols"][k]:
-                    f.write(np.uint64(len(chunk)).tobytes())
-                    f.write(bytes(chunk))
-            lines.append(("protocol", p))
-        # Mask_parameters (spectral reduction): float32 files, and the flag
-        for key in ("mask", "lag_window"):
-            if job.get(key) is not None:
-                p = os.path.join(d, key + ".f32")
-                np.asarray(job[key], dtype=np.float32).tofile(p)
-                lines.append((key, p))
-        if job.get("mask_normalize"):
-            lines.append(("mask_normalize", 1))
-        # UVW for the timeslice headers: float64 [integration][stream][centre][3]
-        if job.get("uvw") is not None:
-            p = os.path.join(d, "uvw.f64")
-            np.asarray(job["uvw"], dtype=np.float64).tofile(p)
-            lines.append(("uvw", p))
-        if job.get("phased_array"):
-            lines.append(("phased_array", 1))
-        if int(job.get("n_phase_centers", 1)) > 1:
-            lines.append(("n_phase_centers", int(job["n_phase_centers"])))
-            if job.get("pc_file_index") is not None:
-                lines.append(("pc_file_index",) + tuple(int(x) for x in job["pc_file_index"]))
-        if "pulsar" in job:
-            lines.append(("pulsar",) + tuple(job["pulsar"]))
-            for pc in job["polyco"]:
-                lines.append(("polyco",) + tuple(pc))
-        if dump:
-            lines.append(("dump", 1))
-        if dump_bins:
-            lines.append(("dump_bins", 1))
-        if precision != 32:
-            lines.append(("precision", precision))
+        lines = correlate_lines(job, d, dump=dump, precision=precision, dump_bins=dump_bins)
         outdir = os.path.join(d, "out")
         os.makedirs(outdir)
         _run("correlate", lines, outdir, d, impl)

@@ -25,6 +25,76 @@ def _bytes_ptr(b):
     return arr
 
 
+def correlation_params(job):
+    """The sfxc_correlation_params of a job dict (the keys of
+    oracle/jobs.correlate: the same dicts drive the reference checker, the C
+    restatement and this library), and the ctypes objects its pointers refer
+    to (keep them alive while the parameters are used)."""
+    keep = []
+    tables = (L.DelayTable * len(job["del_bytes"]))()
+    for k, db in enumerate(job["del_bytes"]):
+        buf = _bytes_ptr(db)
+        keep.append(buf)
+        clock = job.get("clocks", [None] * len(job["del_bytes"]))[k]
+        off, rate, epoch = clock if clock is not None else (0.0, 0.0, 0)
+        tables[k] = L.DelayTable(C.cast(buf, C.POINTER(C.c_uint8)), len(db), off, rate, epoch)
+    streams = (L.StationStream * len(job["streams"]))()
+    for i, s in enumerate(job["streams"]):
+        (station_number, station_stream, sr, cf, bw, sb, pol, bits, lo, tsys_freq, table) = s
+        streams[i] = L.StationStream(station_number, station_stream, sr, bw, bits, tsys_freq, cf,
+                                     sb.encode(), pol.encode(), b"\0\0", table, lo)
+    p = L.CorrelationParams()
+    p.experiment_start_ticks = job["experiment_start_ticks"]
+    p.start_ticks = job["start_ticks"]
+    p.integration_time_us = job["integration_time_us"]
+    p.sub_integration_time_us = job["sub_integration_time_us"]
+    p.number_channels = job["number_channels"]
+    p.fft_size_delaycor = job["fft_size_delaycor"]
+    p.fft_size_correlation = job["fft_size_correlation"]
+    p.sample_rate = job["sample_rate"]
+    p.bandwidth = job["bandwidth"]
+    p.frequency_nr = job["frequency_nr"]
+    p.channel_freq = job["channel_freq"]
+    p.sideband = job["sideband"].encode()
+    p.polarisation = job["polarisation"].encode()
+    p.cross_polarize = job["cross_polarize"]
+    p.reference_station = job["reference_station"]
+    p.window = job["window"]
+    p.integration_nr = job["integration_nr"]
+    p.n_streams = len(job["streams"])
+    p.streams = streams
+    p.n_delay_tables = len(job["del_bytes"])
+    p.delay_tables = tables
+    if "pulsar" in job:
+        nb, g0, g1 = job["pulsar"]
+        p.pulsar_nbins = int(nb)
+        p.gate_start = float(g0)
+        p.gate_stop = float(g1)
+        pcs = (L.Polyco * len(job["polyco"]))()
+        for k, pc in enumerate(job["polyco"]):
+            coef = (C.c_double * (len(pc) - 5))(*pc[5:])
+            keep.append(coef)
+            pcs[k] = L.Polyco(pc[0], pc[1], pc[2], pc[3], pc[4], len(pc) - 5, coef)
+        p.n_polyco = len(job["polyco"])
+        p.polyco = pcs
+        keep.append(pcs)
+    # Mask_parameters of the spectral reduction
+    for key in ("mask", "lag_window"):
+        if job.get(key) is not None:
+            arr = np.ascontiguousarray(job[key], dtype=np.float32)
+            setattr(p, key, arr.ctypes.data_as(C.POINTER(C.c_float)))
+            keep.append(arr)
+    p.mask_normalize = int(bool(job.get("mask_normalize", 0)))
+    p.n_phase_centers = int(job.get("n_phase_centers", 1))
+    p.phased_array = int(bool(job.get("phased_array", 0)))
+    if job.get("pc_file_index") is not None:
+        fi = (C.c_int32 * len(job["pc_file_index"]))(*[int(x) for x in job["pc_file_index"]])
+        p.phase_center_file_index = fi
+        keep.append(fi)
+    keep += [tables, streams]
+    return p, keep
+
+
 class CorrelatorNode:
     """One CUDA context on one device.  x_mode: L.X_FP32 or L.X_TC_HILO."""
 
@@ -56,68 +126,7 @@ class CorrelatorNode:
     def set_parameters(self, job):
         """job: dict with the keys of oracle/jobs.correlate (the same dicts
         drive the reference checker, the C restatement and this library)."""
-        keep = []
-        tables = (L.DelayTable * len(job["del_bytes"]))()
-        for k, db in enumerate(job["del_bytes"]):
-            buf = _bytes_ptr(db)
-            keep.append(buf)
-            clock = job.get("clocks", [None] * len(job["del_bytes"]))[k]
-            off, rate, epoch = clock if clock is not None else (0.0, 0.0, 0)
-            tables[k] = L.DelayTable(C.cast(buf, C.POINTER(C.c_uint8)), len(db), off, rate, epoch)
-        streams = (L.StationStream * len(job["streams"]))()
-        for i, s in enumerate(job["streams"]):
-            (station_number, station_stream, sr, cf, bw, sb, pol, bits, lo, tsys_freq, table) = s
-            streams[i] = L.StationStream(station_number, station_stream, sr, bw, bits, tsys_freq, cf,
-                                         sb.encode(), pol.encode(), b"\0\0", table, lo)
-        p = L.CorrelationParams()
-        p.experiment_start_ticks = job["experiment_start_ticks"]
-        p.start_ticks = job["start_ticks"]
-        p.integration_time_us = job["integration_time_us"]
-        p.sub_integration_time_us = job["sub_integration_time_us"]
-        p.number_channels = job["number_channels"]
-        p.fft_size_delaycor = job["fft_size_delaycor"]
-        p.fft_size_correlation = job["fft_size_correlation"]
-        p.sample_rate = job["sample_rate"]
-        p.bandwidth = job["bandwidth"]
-        p.frequency_nr = job["frequency_nr"]
-        p.channel_freq = job["channel_freq"]
-        p.sideband = job["sideband"].encode()
-        p.polarisation = job["polarisation"].encode()
-        p.cross_polarize = job["cross_polarize"]
-        p.reference_station = job["reference_station"]
-        p.window = job["window"]
-        p.integration_nr = job["integration_nr"]
-        p.n_streams = len(job["streams"])
-        p.streams = streams
-        p.n_delay_tables = len(job["del_bytes"])
-        p.delay_tables = tables
-        if "pulsar" in job:
-            nb, g0, g1 = job["pulsar"]
-            p.pulsar_nbins = int(nb)
-            p.gate_start = float(g0)
-            p.gate_stop = float(g1)
-            pcs = (L.Polyco * len(job["polyco"]))()
-            for k, pc in enumerate(job["polyco"]):
-                coef = (C.c_double * (len(pc) - 5))(*pc[5:])
-                keep.append(coef)
-                pcs[k] = L.Polyco(pc[0], pc[1], pc[2], pc[3], pc[4], len(pc) - 5, coef)
-            p.n_polyco = len(job["polyco"])
-            p.polyco = pcs
-            keep.append(pcs)
-        # Mask_parameters of the spectral reduction
-        for key in ("mask", "lag_window"):
-            if job.get(key) is not None:
-                arr = np.ascontiguousarray(job[key], dtype=np.float32)
-                setattr(p, key, arr.ctypes.data_as(C.POINTER(C.c_float)))
-                keep.append(arr)
-        p.mask_normalize = int(bool(job.get("mask_normalize", 0)))
-        p.n_phase_centers = int(job.get("n_phase_centers", 1))
-        p.phased_array = int(bool(job.get("phased_array", 0)))
-        if job.get("pc_file_index") is not None:
-            fi = (C.c_int32 * len(job["pc_file_index"]))(*[int(x) for x in job["pc_file_index"]])
-            p.phase_center_file_index = fi
-            keep.append(fi)
-        keep += [tables, streams]
+        p, keep = correlation_params(job)
         self._check(self._lib.sfxc_gpu_set_parameters(self._h, C.byref(p)))
         self._keep = keep
         self.nstreams = len(job["streams"])
