@@ -318,6 +318,62 @@ int sfxc_gpu_extract_block(sfxc_gpu_ctx *ctx, const sfxc_reader_block *block, in
                            int32_t n_subbands, int32_t fan_out, const int32_t *tracks, uint8_t *out,
                            int32_t *out_invalid);
 
+/* The same input-node front end with the recording's bytes kept on the
+ * device: the reader (sfxc_gpu_reader_*), the channel extractor
+ * (sfxc_gpu_extract_block) and the writer (sfxc_gpu_write_protocol) over a
+ * whole recording, the frame headers decoded, the Mark5B fill-pattern runs
+ * found, the channels extracted and the protocol bytes assembled by kernels
+ * (the readers' block, skip and resync decisions and the writer's records
+ * stay on the host).  It replaces, per station, Input_data_format_reader_tasklet
+ * -> Channel_extractor_tasklet(_VDIF) -> Input_node_data_writer::do_task
+ * (sfxc/src/input_data_format_reader_tasklet.cc:93-160,
+ * sfxc/src/channel_extractor_tasklet.cc:120-220,
+ * sfxc/src/channel_extractor_tasklet_vdif.cc:25-49,
+ * sfxc/src/input_node_data_writer.cc:107-229) and the transfer of its bytes
+ * into the correlator node's input buffer
+ * (sfxc/src/correlator_node_data_reader_tasklet.cc:28-109).
+ *
+ * create: bytes[0, n) in host memory (copied to the device), or in device
+ * memory of the context's device when bytes_on_device (not copied: it must
+ * stay valid until destroy).  The blocks are those sfxc_gpu_reader_next
+ * returns for the same bytes, except that where a truncated Mark5B recording
+ * ends inside a resync the reader may return one more block whose bytes are
+ * partly left over from its previous block; the walk ends before it.  NULL
+ * on bad parameters (message from sfxc_gpu_last_error(ctx)). */
+typedef struct sfxc_gpu_recording sfxc_gpu_recording;
+sfxc_gpu_recording *sfxc_gpu_recording_create(sfxc_gpu_ctx *ctx, const sfxc_reader_params *params,
+                                               const uint8_t *bytes, size_t n, int32_t bytes_on_device);
+int32_t sfxc_gpu_recording_n_blocks(const sfxc_gpu_recording *rec);
+/* Reader block i (as sfxc_gpu_reader_next fills it; out->invalid valid
+ * until destroy); when data is not NULL, the block's out->size bytes,
+ * assembled from its frames on the device, are copied there (and out->data = data). */
+int sfxc_gpu_recording_block(sfxc_gpu_recording *rec, int32_t i, sfxc_reader_block *out, uint8_t *data);
+/* Channel streams of every block, on the device: subbands as for
+ * sfxc_gpu_extract_block (each frame's payload a whole number of output
+ * bytes), or with word_bytes == 0 one channel per VDIF thread (n_subbands =
+ * the channel count; each block goes to its channel as it is). */
+int sfxc_gpu_recording_extract(sfxc_gpu_recording *rec, int32_t word_bytes, int32_t bits, int32_t n_subbands,
+                               int32_t fan_out, const int32_t *tracks);
+/* Channel `channel`'s blocks after sfxc_gpu_recording_extract (start, size,
+ * invalid runs in its bytes; up to capacity of them into blocks, if not NULL)
+ * and its bytes (into data, if not NULL); returns the block count. */
+int32_t sfxc_gpu_recording_channel(sfxc_gpu_recording *rec, int32_t channel, int32_t capacity,
+                                   sfxc_channel_block *blocks, uint8_t *data);
+/* The writer's protocol for consecutive slices of one channel, as
+ * sfxc_gpu_write_protocol (same slices and arguments) writes it, assembled on
+ * the device and kept there for sfxc_gpu_recording_push; copied to out
+ * (host, capacity bytes) when out is not NULL; slice k's bytes at
+ * out_offsets[k] (n_slices + 1 entries, if not NULL).  Returns the byte count. */
+int64_t sfxc_gpu_recording_protocol(sfxc_gpu_recording *rec, int32_t channel, int32_t n_slices,
+                                    const sfxc_slice *slices, int32_t sample_rate, int32_t bits_per_sample,
+                                    int64_t integration_time_us, uint8_t *out, int64_t capacity,
+                                    int64_t *out_offsets);
+/* sfxc_gpu_push_protocol of slice `slice` of that protocol into stream
+ * `stream` of a correlator context on the same device, device to device. */
+int sfxc_gpu_recording_push(sfxc_gpu_recording *rec, int32_t channel, int32_t slice, sfxc_gpu_ctx *ctx,
+                            int32_t stream);
+void sfxc_gpu_recording_destroy(sfxc_gpu_recording *rec);
+
 /* Phase-cal extraction of one channel (Input_node_data_writer::do_phasecal,
  * sfxc/src/input_node_data_writer.cc:230-312, with its parameters from
  * Input_node_data_writer::set_parameters, 328-346): the channel's samples,

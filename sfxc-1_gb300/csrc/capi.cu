@@ -14,6 +14,7 @@
 #include <memory>
 #include <mutex>
 #include <set>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -1412,6 +1413,22 @@ int sfxc_gpu_set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
   }
 }
 
+namespace {
+// Room for n more protocol bytes in a stream's device input, keeping what
+// this integration already pushed.
+void grow_stream_input(sfxc_gpu_ctx *c, StreamCtx &s, size_t n) {
+  // 8 spare bytes: the unpack reads whole 32-bit words, one past the last sample
+  const size_t need = (size_t)(s.dev_bytes + (int64_t)n) + 8;
+  if (need <= s.src.cap) return;
+  DevBuf grown;
+  grown.ensure(std::max(need, s.src.cap * 3 / 2));
+  if (s.dev_bytes) CK(cudaMemcpyAsync(grown.p, s.src.p, (size_t)s.dev_bytes, cudaMemcpyDeviceToDevice, c->st));
+  std::swap(grown.p, s.src.p);
+  std::swap(grown.cap, s.src.cap);
+  CK(cudaStreamSynchronize(c->st));
+}
+}  // namespace
+
 int sfxc_gpu_push_protocol(sfxc_gpu_ctx *c, int32_t stream, const uint8_t *bytes, size_t n) {
   if (!c) return SFXC_GPU_EINVAL;
   if (!c->have_job) return fail(c, Error(SFXC_GPU_ESTATE, "no parameters set"));
@@ -1420,16 +1437,7 @@ int sfxc_gpu_push_protocol(sfxc_gpu_ctx *c, int32_t stream, const uint8_t *bytes
   StreamCtx &s = c->sc[stream];
   try {
     CK(cudaSetDevice(c->device));
-    // 8 spare bytes: the unpack reads whole 32-bit words, one past the last sample
-    const size_t need = (size_t)(s.dev_bytes + (int64_t)n) + 8;
-    if (need > s.src.cap) {  // grow, keeping what this integration already pushed
-      DevBuf grown;
-      grown.ensure(std::max(need, s.src.cap * 3 / 2));
-      if (s.dev_bytes) CK(cudaMemcpyAsync(grown.p, s.src.p, (size_t)s.dev_bytes, cudaMemcpyDeviceToDevice, c->st));
-      std::swap(grown.p, s.src.p);
-      std::swap(grown.cap, s.src.cap);
-      CK(cudaStreamSynchronize(c->st));
-    }
+    grow_stream_input(c, s, n);
     // the copy runs while the records are parsed; bytes past dev_bytes only
     // count once the parse has succeeded
     if (n) CK(cudaMemcpyAsync(s.src.as<uint8_t>() + s.dev_bytes, bytes, n, cudaMemcpyHostToDevice, c->st));
@@ -2108,6 +2116,23 @@ int64_t sfxc_gpu_write_protocol(const uint8_t *stream, int32_t n_blocks, const s
 }
 
 
+namespace {
+// Input_node_parameters as the readers take them (sfxc_reader_params).
+ReaderParams reader_params(const sfxc_reader_params *p) {
+  ReaderParams rp;
+  rp.format = p->format;
+  rp.ref_ticks = p->ref_ticks;
+  rp.offset_ticks = p->offset_ticks;
+  rp.track_bit_rate = p->track_bit_rate;
+  rp.frame_size = p->frame_size;
+  rp.n_tracks = p->n_tracks;
+  rp.bits_per_sample = p->bits_per_sample;
+  rp.tracks_per_channel = p->tracks_per_channel;
+  rp.first_track.assign(p->first_track, p->first_track + p->n_channels);
+  return rp;
+}
+}  // namespace
+
 struct sfxc_gpu_reader {
   std::unique_ptr<FormatReader> r;
   ReaderBlock block;
@@ -2117,19 +2142,9 @@ sfxc_gpu_reader *sfxc_gpu_reader_create(const sfxc_reader_params *p, const uint8
   try {
     if (!p || (n && !bytes)) throw Error(SFXC_GPU_EINVAL, "no reader parameters or data");
     if (p->n_channels <= 0 || !p->first_track) throw Error(SFXC_GPU_EINVAL, "no channels");
-    ReaderParams rp;
-    rp.format = p->format;
-    rp.ref_ticks = p->ref_ticks;
-    rp.offset_ticks = p->offset_ticks;
-    rp.track_bit_rate = p->track_bit_rate;
-    rp.frame_size = p->frame_size;
-    rp.n_tracks = p->n_tracks;
-    rp.bits_per_sample = p->bits_per_sample;
-    rp.tracks_per_channel = p->tracks_per_channel;
-    rp.first_track.assign(p->first_track, p->first_track + p->n_channels);
     std::unique_ptr<sfxc_gpu_reader> h(new sfxc_gpu_reader());
     try {
-      h->r = FormatReader::create(rp, bytes, n);
+      h->r = FormatReader::create(reader_params(p), bytes, n);
     } catch (const std::exception &e) {
       throw Error(SFXC_GPU_EINVAL, e.what());
     }
@@ -2153,6 +2168,382 @@ int sfxc_gpu_reader_next(sfxc_gpu_reader *h, sfxc_reader_block *out) {
 }
 
 void sfxc_gpu_reader_destroy(sfxc_gpu_reader *h) { delete h; }
+
+// ---- recordings in device memory: the input node's reader, channel
+// extractor and writer with the recording's bytes kept on the device (the
+// headers decoded, the fill runs found, the channels extracted and the
+// protocol bytes assembled by kernels; the readers' block decisions and the
+// writer's records on the host)
+namespace {
+struct DeviceFrames : FrameSource {
+  const uint8_t *rec = nullptr;
+  int64_t n = 0;
+  cudaStream_t st = nullptr;
+  DevBuf info;
+  int64_t size() const override { return n; }
+  void decode(int format, int64_t pos0, int64_t stride, int64_t count, FrameInfo *out) override {
+    if (count <= 0) return;
+    info.ensure((size_t)count * sizeof(FrameInfo));
+    launch_decode_frames(rec, pos0, stride, count, format == FORMAT_MARK5B, info.as<FrameInfo>(), st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, info.p, (size_t)count * sizeof(FrameInfo), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  void fetch(int64_t pos, int64_t len, uint8_t *dst) override {
+    if (len <= 0) return;
+    CK(cudaMemcpyAsync(dst, rec + pos, (size_t)len, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+};
+}  // namespace
+
+struct sfxc_gpu_recording {
+  sfxc_gpu_ctx *ctx = nullptr;
+  ReaderParams p;
+  DevBuf own;  // the recording, when it was passed in host memory
+  const uint8_t *rec = nullptr;
+  int64_t n = 0;
+  std::vector<FrameBlock> blocks;
+  int nf = 0, fb = 0, block_size = 0;
+  DevBuf frames;  // [block][nf] payload offsets in the recording
+  // channel streams: channel c's bytes at chan + chan_off[c], its blocks
+  // (offsets within them) and their invalid runs as (begin, n) pairs
+  DevBuf chan, tracks, list, gathered;
+  std::vector<int64_t> chan_off;
+  std::vector<std::vector<ChannelBlock>> chan_blocks;
+  std::vector<std::vector<std::vector<int32_t>>> chan_runs;
+  // the last protocol of each channel: its bytes on the device and, per
+  // slice, the byte range and the records (DATA payload offsets within the slice's bytes)
+  struct Protocol {
+    DevBuf bytes, recs;
+    std::vector<int64_t> offsets;
+    std::vector<std::vector<Record>> slice_recs;
+  };
+  std::vector<Protocol> proto;
+};
+
+sfxc_gpu_recording *sfxc_gpu_recording_create(sfxc_gpu_ctx *c, const sfxc_reader_params *params,
+                                               const uint8_t *bytes, size_t n, int32_t bytes_on_device) {
+  if (!c) return nullptr;
+  try {
+    if (!params || (n && !bytes)) throw Error(SFXC_GPU_EINVAL, "no reader parameters or data");
+    if (params->n_channels <= 0 || !params->first_track) throw Error(SFXC_GPU_EINVAL, "no channels");
+    CK(cudaSetDevice(c->device));
+    std::unique_ptr<sfxc_gpu_recording> r(new sfxc_gpu_recording());
+    r->ctx = c;
+    r->p = reader_params(params);
+    r->n = (int64_t)n;
+    if (bytes_on_device) {
+      r->rec = bytes;
+    } else {
+      r->own.ensure(n + 16);
+      if (n) CK(cudaMemcpyAsync(r->own.p, bytes, n, cudaMemcpyHostToDevice, c->st));
+      r->rec = r->own.as<uint8_t>();
+    }
+    DeviceFrames src;
+    src.rec = r->rec;
+    src.n = r->n;
+    src.st = c->st;
+    try {
+      r->blocks = walk_frames(r->p, src);
+    } catch (const std::invalid_argument &e) {
+      throw Error(SFXC_GPU_EINVAL, e.what());
+    } catch (const std::logic_error &e) {
+      throw Error(SFXC_GPU_ESTATE, e.what());
+    }
+    if (!r->blocks.empty()) {
+      r->nf = (int)r->blocks[0].frames.size();
+      r->fb = r->blocks[0].frame_bytes;
+      r->block_size = r->blocks[0].size;
+      std::vector<int64_t> fr;
+      fr.reserve(r->blocks.size() * (size_t)r->nf);
+      for (const FrameBlock &b : r->blocks) {
+        if ((int)b.frames.size() != r->nf || b.size != r->block_size) throw Error(SFXC_GPU_ESTATE, "uneven reader blocks");
+        fr.insert(fr.end(), b.frames.begin(), b.frames.end());
+      }
+      upload(r->frames, fr.data(), fr.size() * sizeof(int64_t), c->st);
+      if (r->p.format == FORMAT_MARK5B) {  // fill-pattern runs of every block: count, then write
+        const int nb = (int)r->blocks.size();
+        DevBuf counts, offs, runs;
+        counts.ensure((size_t)nb * 4);
+        launch_fill_runs(r->rec, r->frames.as<int64_t>(), r->nf, r->fb / 4, r->block_size / 4, nb,
+                         counts.as<int32_t>(), nullptr, nullptr, c->st);
+        CK(cudaGetLastError());
+        std::vector<int32_t> cnt(nb);
+        CK(cudaMemcpyAsync(cnt.data(), counts.p, (size_t)nb * 4, cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        std::vector<int64_t> off(nb + 1, 0);
+        for (int b = 0; b < nb; b++) off[b + 1] = off[b] + cnt[b];
+        if (off[nb]) {
+          upload(offs, off.data(), (size_t)nb * 8, c->st);
+          runs.ensure((size_t)off[nb] * 8);
+          launch_fill_runs(r->rec, r->frames.as<int64_t>(), r->nf, r->fb / 4, r->block_size / 4, nb, nullptr,
+                           offs.as<int64_t>(), runs.as<int32_t>(), c->st);
+          CK(cudaGetLastError());
+          std::vector<int32_t> all((size_t)off[nb] * 2);
+          CK(cudaMemcpyAsync(all.data(), runs.p, all.size() * 4, cudaMemcpyDeviceToHost, c->st));
+          CK(cudaStreamSynchronize(c->st));
+          for (int b = 0; b < nb; b++)
+            r->blocks[b].invalid.assign(all.begin() + 2 * off[b], all.begin() + 2 * off[b + 1]);
+        }
+      }
+    }
+    CK(cudaStreamSynchronize(c->st));
+    return r.release();
+  } catch (const Error &e) {
+    fail(c, e);
+    return nullptr;
+  }
+}
+
+void sfxc_gpu_recording_destroy(sfxc_gpu_recording *r) {
+  if (!r) return;
+  cudaSetDevice(r->ctx->device);
+  delete r;
+}
+
+int32_t sfxc_gpu_recording_n_blocks(const sfxc_gpu_recording *r) { return r ? (int32_t)r->blocks.size() : 0; }
+
+int sfxc_gpu_recording_block(sfxc_gpu_recording *r, int32_t i, sfxc_reader_block *out, uint8_t *data) {
+  if (!r) return SFXC_GPU_EINVAL;
+  sfxc_gpu_ctx *c = r->ctx;
+  try {
+    if (!out || i < 0 || i >= (int32_t)r->blocks.size()) throw Error(SFXC_GPU_EINVAL, "bad block index");
+    const FrameBlock &b = r->blocks[i];
+    out->data = data;
+    out->size = b.size;
+    out->channel = b.channel;
+    out->start_ticks = b.start_ticks;
+    out->n_invalid = (int32_t)(b.invalid.size() / 2);
+    out->invalid = b.invalid.data();
+    if (data) {  // the block's bytes, assembled from its frames on the device
+      CK(cudaSetDevice(c->device));
+      upload(r->list, &i, 4, c->st);
+      r->gathered.ensure((size_t)b.size);
+      launch_gather_blocks(r->rec, r->frames.as<int64_t>(), r->nf, r->fb, r->block_size, r->list.as<int32_t>(), 1,
+                           r->gathered.as<uint8_t>(), c->st);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(data, r->gathered.p, (size_t)b.size, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+    }
+    return SFXC_GPU_OK;
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
+int sfxc_gpu_recording_extract(sfxc_gpu_recording *r, int32_t word_bytes, int32_t bits, int32_t n_subbands,
+                               int32_t fan_out, const int32_t *tracks) {
+  if (!r) return SFXC_GPU_EINVAL;
+  sfxc_gpu_ctx *c = r->ctx;
+  try {
+    CK(cudaSetDevice(c->device));
+    const int nb = (int)r->blocks.size();
+    r->chan_blocks.clear();
+    r->chan_runs.clear();
+    r->chan_off.clear();
+    r->proto.clear();
+    if (word_bytes == 0) {
+      // one channel per VDIF thread (Channel_extractor_tasklet_VDIF::do_task,
+      // sfxc/src/channel_extractor_tasklet_vdif.cc:25-49): each block is its
+      // channel's next block as it is
+      const int nch = (int)r->p.first_track.size();
+      if (n_subbands != nch) throw Error(SFXC_GPU_EINVAL, "n_subbands must be the channel count");
+      std::vector<std::vector<int32_t>> lists(nch);
+      for (int b = 0; b < nb; b++) {
+        const int ch = r->blocks[b].channel;
+        if (ch < 0 || ch >= nch) throw Error(SFXC_GPU_EINVAL, "block of a channel outside the channel list");
+        lists[ch].push_back(b);
+      }
+      r->chan_blocks.resize(nch);
+      r->chan_runs.resize(nch);
+      int64_t total = 0;
+      for (int ch = 0; ch < nch; ch++) {
+        r->chan_off.push_back(total);
+        total += (int64_t)lists[ch].size() * r->block_size;
+      }
+      r->chan.ensure((size_t)total + 16);
+      std::vector<int32_t> all;
+      for (auto &l : lists) all.insert(all.end(), l.begin(), l.end());
+      upload(r->list, all.data(), all.size() * 4, c->st);
+      int64_t e0 = 0;
+      for (int ch = 0; ch < nch; ch++) {
+        launch_gather_blocks(r->rec, r->frames.as<int64_t>(), r->nf, r->fb, r->block_size,
+                             r->list.as<int32_t>() + e0, (int)lists[ch].size(),
+                             r->chan.as<uint8_t>() + r->chan_off[ch], c->st);
+        CK(cudaGetLastError());
+        e0 += (int64_t)lists[ch].size();
+        for (size_t j = 0; j < lists[ch].size(); j++) {
+          const FrameBlock &b = r->blocks[lists[ch][j]];
+          ChannelBlock cb;
+          cb.start = b.start_ticks;
+          cb.src_offset = (int64_t)j * r->block_size;
+          cb.size = r->block_size;
+          for (size_t k = 0; k + 1 < b.invalid.size(); k += 2) cb.invalid.push_back(InvalidRun{b.invalid[k], b.invalid[k + 1]});
+          r->chan_blocks[ch].push_back(cb);
+          r->chan_runs[ch].push_back(b.invalid);
+        }
+      }
+    } else {
+      // Channel_extractor_tasklet::do_task (sfxc/src/channel_extractor_tasklet.cc:120-220)
+      // over every block, each block's words read from its frames
+      if (!tracks || word_bytes <= 0 || n_subbands <= 0) throw Error(SFXC_GPU_EINVAL, "bad arguments");
+      if (fan_out <= 0 || fan_out > 8 || 8 % fan_out || (bits != 1 && bits != 2) || fan_out % bits)
+        throw Error(SFXC_GPU_EINVAL, "fan_out must divide 8 and be a multiple of bits_per_sample");
+      for (int i = 0; i < n_subbands * fan_out; i++)
+        if (tracks[i] < 0 || tracks[i] >= word_bytes * 8) throw Error(SFXC_GPU_EINVAL, "track outside the word");
+      const int per_byte = 8 / fan_out * word_bytes;  // input bytes per output byte
+      if (nb && (r->fb % per_byte || r->block_size % per_byte))
+        throw Error(SFXC_GPU_EINVAL, "frame payload is not a whole number of output bytes");
+      const int64_t opb = nb ? r->block_size / per_byte : 0;
+      const int64_t nout = (int64_t)nb * opb;
+      upload(r->tracks, tracks, (size_t)n_subbands * fan_out * 4, c->st);
+      r->chan.ensure((size_t)(nout * n_subbands) + 16);
+      launch_extract_frames(r->rec, r->frames.as<int64_t>(), r->nf, r->fb, opb, nout, word_bytes, bits, n_subbands,
+                            fan_out, r->tracks.as<int>(), r->chan.as<uint8_t>(), c->st);
+      CK(cudaGetLastError());
+      r->chan_blocks.resize(n_subbands);
+      r->chan_runs.resize(n_subbands);
+      for (int sb = 0; sb < n_subbands; sb++) {
+        r->chan_off.push_back((int64_t)sb * nout);
+        for (int b = 0; b < nb; b++) {
+          ChannelBlock cb;
+          cb.start = r->blocks[b].start_ticks;
+          cb.src_offset = (int64_t)b * opb;
+          cb.size = (int32_t)opb;
+          // invalid byte runs in bytes of each subband (channel_extractor_tasklet.cc:181-194)
+          std::vector<int32_t> runs;
+          for (int32_t v : r->blocks[b].invalid) runs.push_back(v * fan_out / (8 * word_bytes));
+          for (size_t k = 0; k + 1 < runs.size(); k += 2) cb.invalid.push_back(InvalidRun{runs[k], runs[k + 1]});
+          r->chan_blocks[sb].push_back(cb);
+          r->chan_runs[sb].push_back(runs);
+        }
+      }
+    }
+    r->proto.resize(r->chan_blocks.size());
+    CK(cudaStreamSynchronize(c->st));
+    return SFXC_GPU_OK;
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
+int32_t sfxc_gpu_recording_channel(sfxc_gpu_recording *r, int32_t channel, int32_t capacity,
+                                   sfxc_channel_block *blocks, uint8_t *data) {
+  if (!r) return SFXC_GPU_EINVAL;
+  sfxc_gpu_ctx *c = r->ctx;
+  try {
+    if (channel < 0 || channel >= (int32_t)r->chan_blocks.size()) throw Error(SFXC_GPU_EINVAL, "bad channel");
+    const auto &cb = r->chan_blocks[channel];
+    const int nb = (int)cb.size();
+    if (blocks) {
+      if (capacity < nb) throw Error(SFXC_GPU_EINVAL, "block array too small");
+      for (int b = 0; b < nb; b++) {
+        blocks[b].start_ticks = cb[b].start;
+        blocks[b].size = cb[b].size;
+        blocks[b].n_invalid = (int32_t)(r->chan_runs[channel][b].size() / 2);
+        blocks[b].invalid = r->chan_runs[channel][b].data();
+      }
+    }
+    if (data && nb) {
+      CK(cudaSetDevice(c->device));
+      const int64_t bytes = cb.back().src_offset + cb.back().size;
+      CK(cudaMemcpyAsync(data, r->chan.as<uint8_t>() + r->chan_off[channel], (size_t)bytes, cudaMemcpyDeviceToHost,
+                         c->st));
+      CK(cudaStreamSynchronize(c->st));
+    }
+    return nb;
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
+int64_t sfxc_gpu_recording_protocol(sfxc_gpu_recording *r, int32_t channel, int32_t n_slices,
+                                    const sfxc_slice *slices, int32_t sample_rate, int32_t bits,
+                                    int64_t integration_time_us, uint8_t *out, int64_t capacity,
+                                    int64_t *out_offsets) {
+  if (!r) return SFXC_GPU_EINVAL;
+  sfxc_gpu_ctx *c = r->ctx;
+  try {
+    if (channel < 0 || channel >= (int32_t)r->chan_blocks.size()) throw Error(SFXC_GPU_EINVAL, "bad channel");
+    if (!slices || n_slices < 0) throw Error(SFXC_GPU_EINVAL, "bad slices");
+    CK(cudaSetDevice(c->device));
+    std::vector<SliceRequest> sl(n_slices);
+    for (int i = 0; i < n_slices; i++) {
+      sl[i].start = slices[i].start_ticks;
+      sl[i].stop = slices[i].stop_ticks;
+      sl[i].nr_samples = slices[i].nr_samples;
+      for (int k = 0; k < slices[i].n_delays; k++)
+        sl[i].delays.push_back(Delay{slices[i].delay_ticks[k], slices[i].delay_bytes[k], slices[i].delay_remaining[k]});
+      if (sl[i].delays.empty()) throw Error(SFXC_GPU_EINVAL, "slice without delays");
+    }
+    // the writer's records (Input_node_data_writer::do_task), then their bytes
+    auto recs = write_protocol(r->chan_blocks[channel], sl, sample_rate, bits, (double)integration_time_us);
+    sfxc_gpu_recording::Protocol &pr = r->proto[channel];
+    pr.offsets.assign(1, 0);
+    pr.slice_recs.assign(n_slices, {});
+    std::vector<ProtoRecord> dev;
+    int64_t total = 0;
+    for (int i = 0; i < n_slices; i++) {
+      const int64_t s0 = total;
+      for (const Record &q : recs[i]) {
+        ProtoRecord d{q.src, total, q.n, q.type, q.rem, 0};
+        dev.push_back(d);
+        Record rel = q;
+        if (q.type == HEADER_DATA) rel.src = total - s0 + 3;
+        pr.slice_recs[i].push_back(rel);
+        total += q.type == HEADER_ENDSTREAM ? 1 : q.type == HEADER_DELAY ? 2 : q.type == HEADER_DATA ? 3 + q.n : 3;
+      }
+      pr.offsets.push_back(total);
+    }
+    if (out_offsets)
+      for (int i = 0; i <= n_slices; i++) out_offsets[i] = pr.offsets[i];
+    upload(pr.recs, dev.data(), dev.size() * sizeof(ProtoRecord), c->st);
+    pr.bytes.ensure((size_t)total + 16);
+    launch_serialize_protocol(pr.recs.as<ProtoRecord>(), (int)dev.size(), r->chan.as<uint8_t>() + r->chan_off[channel],
+                              pr.bytes.as<uint8_t>(), c->st);
+    CK(cudaGetLastError());
+    if (out) {
+      if (total > capacity) throw Error(SFXC_GPU_EINVAL, "output buffer too small");
+      CK(cudaMemcpyAsync(out, pr.bytes.p, (size_t)total, cudaMemcpyDeviceToHost, c->st));
+    }
+    CK(cudaStreamSynchronize(c->st));
+    return total;
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
+
+int sfxc_gpu_recording_push(sfxc_gpu_recording *r, int32_t channel, int32_t slice, sfxc_gpu_ctx *c, int32_t stream) {
+  if (!r || !c) return SFXC_GPU_EINVAL;
+  if (!c->have_job) return fail(c, Error(SFXC_GPU_ESTATE, "no parameters set"));
+  if (stream < 0 || stream >= (int)c->sc.size()) return fail(c, Error(SFXC_GPU_EINVAL, "bad stream index"));
+  try {
+    if (c->device != r->ctx->device) throw Error(SFXC_GPU_EINVAL, "recording and correlator on different devices");
+    if (channel < 0 || channel >= (int32_t)r->proto.size() || slice < 0 ||
+        slice + 1 >= (int32_t)r->proto[channel].offsets.size())
+      throw Error(SFXC_GPU_EINVAL, "no protocol for that channel and slice");
+    CK(cudaSetDevice(c->device));
+    const sfxc_gpu_recording::Protocol &pr = r->proto[channel];
+    const int64_t b0 = pr.offsets[slice], n = pr.offsets[slice + 1] - b0;
+    StreamCtx &s = c->sc[stream];
+    grow_stream_input(c, s, (size_t)n);
+    // the protocol is complete on the recording's stream (its calls return
+    // after it); the copy runs on the correlator's
+    if (n) CK(cudaMemcpyAsync(s.src.as<uint8_t>() + s.dev_bytes, pr.bytes.as<uint8_t>() + b0, (size_t)n,
+                              cudaMemcpyDeviceToDevice, c->st));
+    for (Record q : pr.slice_recs[slice]) {
+      if (q.type == HEADER_DATA) q.src += s.dev_bytes;
+      s.pending.push_back(q);
+    }
+    CK(cudaStreamSynchronize(c->st));
+    s.dev_bytes += n;
+    s.pushed = true;
+    return SFXC_GPU_OK;
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
+}
 
 // ---- batches: the next integration of several jobs in one CUDA graph
 struct sfxc_gpu_batch {

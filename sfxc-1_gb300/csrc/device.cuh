@@ -210,4 +210,27 @@ struct VisLayout {
   int32_t nbl, kpad;  // baselines, padded channel count
 };
 
+// One output byte of channel extraction: spb = 8 / fan_out samples from the
+// spb consecutive N-byte words at w, first sample in the lowest bits; the
+// subband's fan_out tracks are tr[0..fan_out) (bit positions in a word).
+// Bit placement follows Channel_extractor_5 (sfxc/src/channel_extractor_5.cc:40-58,
+// 67-99): track t of a sample lands at low_bit << ((t+1) % bits) with low_bit
+// starting at 1 << (8 - fan_out) and advancing by `bits` per complete sample,
+// and each earlier sample is shifted down by fan_out per later sample.
+__device__ __forceinline__ uint8_t extract_byte(const uint8_t *w, int N, int bits, int fan_out,
+                                                const int *__restrict__ tr) {
+  const int spb = 8 / fan_out;
+  unsigned byte = 0;
+  for (int j = 0; j < spb; j++, w += N) {
+    unsigned v = 0, low_bit = 1u << (8 - fan_out);
+    for (int t = 0; t < fan_out; t++) {
+      const int k = tr[t];
+      if ((w[k >> 3] >> (k & 7)) & 1) v |= low_bit << ((t + 1) % bits);
+      if ((t + 1) % bits == 0) low_bit <<= bits;
+    }
+    byte |= (v >> ((spb - 1 - j) * fan_out)) & 0xffu;
+  }
+  return (uint8_t)byte;
+}
+
 }  // namespace sfxc

@@ -2,6 +2,8 @@
 // reference's reader behaviour; the file:line cites are the reference's.
 #include "formats.hpp"
 
+#include "frames.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -13,8 +15,6 @@ namespace {
 
 constexpr double kClockRate = 512000000.0;  // Time ticks per second (sfxc/include/utils.h:36)
 constexpr int kReferenceMjd = 51544;        // sfxc/include/correlator_time.h:9
-constexpr uint32_t kFill = 0x11223344u;     // MARK5_FILLPATTERN (sfxc/include/utils.h:45)
-constexpr int kFillWords = 65528 / 4;       // MARK5_FILLPATTERN_NWORDS (utils.h:47)
 
 // ---- Time, as the reference's Time class rounds (sfxc/include/correlator_time.h:76-141)
 int64_t ticks_of(int mjd, double sec) {
@@ -64,22 +64,17 @@ uint32_t word_at(const uint8_t *b, int i) {
 // ---- VDIF (sfxc/src/vdif_reader.cc, header sfxc/include/vdif_reader.h:36-61)
 struct VdifHeader {
   uint8_t b[32] = {};
-  uint32_t w(int i) const { return word_at(b, i); }
-  uint32_t sec_from_epoch() const { return w(0) & 0x3FFFFFFFu; }
-  int legacy() const { return (w(0) >> 30) & 1; }
-  int invalid() const { return (w(0) >> 31) & 1; }
-  uint32_t frame_in_second() const { return w(1) & 0xFFFFFFu; }
-  int ref_epoch() const { return (w(1) >> 24) & 0x3F; }
-  uint32_t frame_length8() const { return w(2) & 0xFFFFFFu; }
-  int log2_nchan() const { return (w(2) >> 24) & 0x1F; }
-  int thread_id() const { return (w(3) >> 16) & 0x3FF; }
-  int bits_minus_one() const { return (w(3) >> 26) & 0x1F; }
-  int header_size() const { return 16 + 16 * (1 - legacy()); }
-  int data_size() const { return 8 * (int)frame_length8() - header_size(); }
-  int jday_epoch() const { return mjd_of_date(1, 1 + 6 * (ref_epoch() % 2), 2000 + ref_epoch() / 2); }
-  bool fill() const {
-    return w(0) == kFill || w(1) == kFill || w(2) == kFill || w(3) == kFill;
-  }
+  FrameInfo f() const { return decode_vdif(b); }
+  uint32_t sec_from_epoch() const { return f().seconds; }
+  int legacy() const { return (f().flags & FRAME_LEGACY) ? 1 : 0; }
+  int invalid() const { return (f().flags & FRAME_INVALID) ? 1 : 0; }
+  uint32_t frame_in_second() const { return f().frame_nr; }
+  int log2_nchan() const { return f().log2_nchan; }
+  int thread_id() const { return f().thread; }
+  int bits_minus_one() const { return f().bits_m1; }
+  int data_size() const { return f().data_size; }
+  int jday_epoch() const { return f().epoch_mjd; }
+  bool fill() const { return (f().flags & FRAME_FILL) != 0; }
 };
 
 class VdifReader : public FormatReader {
@@ -211,31 +206,16 @@ constexpr int kMk5bBlock = kMk5bBlockFrames * kMk5bFrame;
 
 struct Mk5bHeader {
   uint8_t b[16] = {};
-  uint32_t sync() const { return word_at(b, 0); }
-  int frame_nr() const { return (int)(word_at(b, 1) & 0x7FFF); }
-  int nib(int byte, int high) const { return high ? b[byte] >> 4 : b[byte] & 0xF; }
-  // BCD fields: word 2 = JJJSSSSS, word 3 = .SSSS (high half) and the CRC
-  int64_t seconds() const {
-    return ((((int64_t)nib(10, 0) * 10 + nib(9, 1)) * 10 + nib(9, 0)) * 10 + nib(8, 1)) * 10 + nib(8, 0);
-  }
-  int64_t microseconds() const {
-    const int64_t sub = ((((int64_t)nib(15, 1) * 10 + nib(15, 0)) * 10 + nib(14, 1)) * 10 + nib(14, 0)) * 100;
-    return 1000000 * seconds() + sub;
-  }
-  int julian_day() const { return (nib(11, 1) * 10 + nib(11, 0)) * 10 + nib(10, 1); }
-  uint16_t crc() const { return (uint16_t)(b[12] | (b[13] << 8)); }
-  bool subsec_zero() const { return b[14] == 0 && b[15] == 0; }
+  FrameInfo f() const { return decode_mk5b(b); }
+  int frame_nr() const { return (int)f().frame_nr; }
+  int64_t seconds() const { return f().seconds; }
+  int64_t microseconds() const { return 1000000 * seconds() + f().epoch_mjd; }
+  int julian_day() const { return f().thread; }
 };
 
 class Mark5bReader : public FormatReader {
  public:
   Mark5bReader(const ReaderParams &p, const uint8_t *bytes, size_t n) : src_(bytes, n) {
-    // CRC-16 table, polynomial 0x8005, 16-bit register (mark5b_reader.cc:195-209)
-    for (int i = 0; i < 256; i++) {
-      uint16_t c = (uint16_t)(i << 8);
-      for (int j = 0; j < 8; j++) c = (c & 0x8000) ? (uint16_t)((c << 1) ^ 0x8005) : (uint16_t)(c << 1);
-      crc_table_[i] = c;
-    }
     current_jday_ = (int)mjd_of_ticks(p.ref_ticks);
     // set_parameters (mark5b_reader.cc:241-252)
     bitstreams_ = p.n_tracks;
@@ -259,26 +239,13 @@ class Mark5bReader : public FormatReader {
 
  private:
   Source src_;
-  uint16_t crc_table_[256];
   int current_jday_ = 0, bitstreams_ = 0, sample_rate_ = 0, frame_nr_ = -1;
   int64_t tbh_ = 0, offset_ = 0;
   bool open_ = false, frame_nr_valid_ = true;
   Mk5bHeader cur_, tmp_, prev_;
 
-  // check_header (mark5b_reader.cc:211-239): the register is a 32-bit
-  // unsigned that is never masked to 16 bits
-  bool check(const Mk5bHeader &h) const {
-    if (h.sync() != 0xABADDEEDu) return false;
-    if (h.crc() == 0) return true;
-    if (h.subsec_zero() && h.frame_nr() != 0) return true;
-    uint32_t crc = 0;
-    for (int word = 2; word <= 3; word++)
-      for (int i = 3; i >= 0; i--) {
-        crc ^= (uint32_t)h.b[word * 4 + i] << 8;
-        crc = (crc << 8) ^ crc_table_[(crc >> 8) & 0xff];
-      }
-    return crc == 0;
-  }
+  // check_header (mark5b_reader.cc:195-239), decoded as the device decodes it
+  static bool check(const Mk5bHeader &h) { return (h.f().flags & FRAME_CHECK) != 0; }
 
   // get_current_time (mark5b_reader.cc:84-105)
   int64_t current_time() {
@@ -384,55 +351,280 @@ class Mark5bReader : public FormatReader {
     return false;
   }
 
-  // Input_data_format_reader::find_fill_pattern (input_data_format_reader.cc:20-72):
-  // galloping search for runs of the fill word, 4-byte granularity
+  // Input_data_format_reader::find_fill_pattern (input_data_format_reader.cc:20-72)
   static void find_fill_pattern(ReaderBlock &out) {
-    const int nw = (int)(out.data.size() / 4);
-    auto w = [&](int i) { return word_at(out.data.data(), i); };
-    int start = 0;
-    while (start < nw) {
-      if (w(start) != kFill) {
-        int step = std::min(kFillWords, nw - start - 1);
-        while (step > 0) {
-          if (w(start + step) != kFill) {
-            start += step;
-            step = std::min(step, nw - start - 1);
-          } else {
-            step /= 2;
-          }
-        }
-        start += 1;
-      }
-      if (start >= nw) break;
-      int end = start;
-      int step = std::min(kFillWords, nw - end - 1);
-      while (step > 0) {
-        if (w(end + step) == kFill) {
-          end += step;
-          step = std::min(step, nw - end - 1);
-        } else {
-          step /= 2;
-        }
-      }
-      out.invalid.push_back(start * 4);
-      out.invalid.push_back((end - start + 1) * 4);
-      start = end + 1;
-    }
+    const uint8_t *d = out.data.data();
+    auto w = [d](int i) { return word_at(d, i); };
+    auto emit = [&out](int begin, int n) {
+      out.invalid.push_back(begin);
+      out.invalid.push_back(n);
+    };
+    fill_pattern_runs(w, (int)(out.data.size() / 4), emit);
   }
 };
 
 }  // namespace
 
-int mjd_of_date(int day, int month, int year) {
-  // days since 0000-03-01 of the proleptic Gregorian calendar, less the
-  // count for 1858-11-17
-  const int y = year - (month <= 2 ? 1 : 0);
-  const int era = (y >= 0 ? y : y - 399) / 400;
-  const int yoe = y - era * 400;
-  const int mp = (month + 9) % 12;
-  const int doy = (153 * mp + 2) / 5 + day - 1;
-  const int doe = yoe * 365 + yoe / 4 - yoe / 100 + doy;
-  return era * 146097 + doe - 678881;
+int mjd_of_date(int day, int month, int year) { return mjd_from_date(day, month, year); }
+
+// ---- The readers over decoded headers (walk_frames).  Each rule below is
+// the corresponding reader's rule above, restated on header records and
+// recording offsets: a header "read" at offset q is the 16 bytes there
+// (q + header size <= size, else end of data), a payload read likewise.
+namespace {
+
+std::vector<FrameBlock> walk_vdif(const ReaderParams &p, FrameSource &src) {
+  if (p.frame_size <= 0) throw std::invalid_argument("VDIF frame size must be positive");
+  const int64_t n = src.size();
+  const int fs = p.frame_size;
+  const int ref_jday = (int)mjd_of_ticks(p.ref_ticks);
+  const double sample_rate = (double)p.track_bit_rate * (p.tracks_per_channel / p.bits_per_sample);
+  std::map<int, int> thread_map;
+  int fpb = std::max(1, 32128 / fs);
+  if (p.n_tracks == 0) {
+    for (size_t i = 0; i < p.first_track.size(); i++) thread_map[p.first_track[i]] = (int)i;
+    fpb = 1;
+  }
+  std::vector<FrameBlock> out;
+  // before the first header: 16-byte candidates, a fill header skips a
+  // non-legacy frame (vdif_reader.cc:84-100)
+  const int64_t cstride = (int64_t)fs + 32;
+  int64_t ncand = 0;
+  while (ncand <= 256 && ncand * cstride + 16 <= n) ncand++;
+  std::vector<FrameInfo> cand((size_t)ncand);
+  if (ncand) src.decode(FORMAT_VDIF, 0, cstride, ncand, cand.data());
+  int restarts = 0;
+  int64_t k = 0;
+  for (;; k++) {
+    if (k >= ncand) return out;
+    if (!(cand[k].flags & FRAME_FILL)) break;
+    if (++restarts > 256) return out;
+  }
+  const FrameInfo first = cand[k];
+  const int64_t p0 = k * cstride;
+  const int hs = (first.flags & FRAME_LEGACY) ? 16 : 32;
+  if (p0 + hs > n) return out;
+  // after it, frames at a fixed stride
+  const int64_t stride = hs + fs;
+  const int64_t nf = (n - p0 - 16) / stride + 1;
+  std::vector<FrameInfo> hdr((size_t)nf);
+  src.decode(FORMAT_VDIF, p0, stride, nf, hdr.data());
+  const int32_t block_size = fpb * std::max(first.data_size, fs);
+  auto time_of = [&](const FrameInfo &h) {  // get_current_time (vdif_reader.cc:63-75)
+    const double seconds = (double)h.seconds - (ref_jday - h.epoch_mjd) * 24 * 60 * 60;
+    double subsec = 0;
+    if (sample_rate > 0) {
+      const int spf = 8 * fs / ((first.bits_m1 + 1) * (1 << first.log2_nchan));
+      subsec = (double)h.frame_nr * spf / sample_rate;
+    }
+    return ticks_of(ref_jday, seconds + subsec) - p.offset_ticks;
+  };
+  auto header_in = [&](int64_t j) { return j < nf && p0 + j * stride + hs <= n; };
+  int64_t j = 0;
+  bool have = true;  // the first header has been read
+  for (;;) {         // read_new_block (vdif_reader.cc:77-190)
+    FrameBlock b;
+    for (;;) {
+      if (!have && !header_in(j)) return out;
+      have = false;
+      const FrameInfo &h = hdr[(size_t)j];
+      const int64_t pos = p0 + j * stride;
+      if ((h.flags & FRAME_FILL) || h.frame_nr % (uint32_t)fpb != 0) {
+        j++;
+        if (++restarts > 256) return out;
+        continue;
+      }
+      if (pos + hs + fs > n) return out;
+      auto it = thread_map.find(h.thread);
+      if (h.flags & FRAME_INVALID) {
+        b.invalid.push_back(0);
+        b.invalid.push_back(fs);
+        b.channel = it != thread_map.end() ? it->second : 0;
+      } else {
+        if (it == thread_map.end()) {
+          if (thread_map.empty()) {
+            thread_map[h.thread] = 0;
+          } else {
+            j++;
+            if (++restarts > 256) return out;
+            continue;
+          }
+        }
+        b.channel = thread_map[h.thread];
+      }
+      b.frames.push_back(pos + hs);
+      j++;
+      for (int i = 1; i < fpb; i++, j++) {
+        if (!header_in(j)) return out;
+        const int64_t q = p0 + j * stride;
+        if (q + hs + fs > n) return out;
+        b.frames.push_back(q + hs);
+        if (hdr[(size_t)j].flags & FRAME_INVALID) {
+          b.invalid.push_back(i * fs);
+          b.invalid.push_back(fs);
+        }
+      }
+      b.start_ticks = time_of(h);
+      b.size = block_size;
+      b.frame_bytes = fs;
+      out.push_back(std::move(b));
+      restarts = 0;
+      break;
+    }
+  }
+}
+
+// Reads of the bytes fetched for one Mark5B resync, with Source's
+// end-of-data rule; any short read ends the walk.
+struct FetchedBytes {
+  std::vector<uint8_t> b;
+  int64_t base = 0, pos = 0, n = 0;  // recording offset of b[0], read position (recording), recording size
+  bool short_read = false;
+  void get(int64_t want, uint8_t *dst) {
+    if (short_read) return;
+    if (pos + want > n) {
+      short_read = true;
+      return;
+    }
+    if (pos + want > base + (int64_t)b.size()) throw std::logic_error("Mark5B resync read beyond the fetched span");
+    if (dst) std::memcpy(dst, b.data() + (pos - base), (size_t)want);
+    pos += want;
+  }
+};
+
+std::vector<FrameBlock> walk_mk5b(const ReaderParams &p, FrameSource &src) {
+  const int64_t n = src.size();
+  int current_jday = (int)mjd_of_ticks(p.ref_ticks);
+  const int bitstreams = p.n_tracks;
+  const int word = bitstreams <= 32 ? 4 : 8;
+  const int tbr = p.track_bit_rate;
+  if (tbr <= 0 || tbr % 1000000) throw std::invalid_argument("Mark5B track bit rate must be whole Mb/s");
+  const int64_t tbh = ticks_of_usec((double)kMk5bBlock / (word * tbr / 1000000));
+  const int sample_rate = p.track_bit_rate * (p.tracks_per_channel / p.bits_per_sample);
+  const int64_t fstride = kMk5bHeader + kMk5bFrame, bstride = kMk5bBlockFrames * fstride;
+  const uint8_t zero[16] = {};
+  FrameInfo cur = decode_mk5b(zero), prev = cur;
+  int frame_nr = -1;
+  bool frame_nr_valid = true;
+  std::vector<FrameBlock> out;
+  auto frame_nr_update = [&]() {  // mark5b_reader.cc:127-131
+    if (bitstreams == 64 && cur.seconds == prev.seconds && frame_nr > (int)cur.frame_nr)
+      frame_nr = (int)cur.frame_nr + 32768;
+    else
+      frame_nr = (int)cur.frame_nr;
+  };
+  auto finish = [&](std::vector<int64_t> &&frames) {  // jday, then get_current_time (mark5b_reader.cc:84-105)
+    if (cur.thread != current_jday % 1000) current_jday++;
+    const double rate = (double)sample_rate * bitstreams;
+    const double subsec = (double)((uint64_t)(int64_t)frame_nr * (8 * kMk5bFrame)) / rate;
+    if (subsec > 1 && frame_nr_valid) frame_nr_valid = false;
+    int64_t t;
+    if (frame_nr_valid) {
+      t = ticks_of(current_jday, (double)cur.seconds + subsec);
+    } else {
+      const int64_t second = ticks_of(current_jday, (double)cur.seconds);
+      const int64_t sub = ticks_of_usec((double)cur.epoch_mjd);
+      const int nframes = (int)std::round((double)sub / tbh);
+      t = second + (int64_t)std::round((double)tbh * nframes);
+    }
+    FrameBlock b;
+    b.start_ticks = t - p.offset_ticks;
+    b.size = kMk5bBlock;
+    b.frame_bytes = kMk5bFrame;
+    b.frames = std::move(frames);
+    out.push_back(std::move(b));
+  };
+  // block-start headers on the grid g0 + k * bstride
+  int64_t g0 = -1;
+  std::vector<FrameInfo> grid;
+  int64_t P = 0;
+  for (;;) {  // read_new_block (mark5b_reader.cc:111-162)
+    if (P + kMk5bHeader > n) return out;
+    if (g0 < 0 || P < g0 || (P - g0) % bstride || (P - g0) / bstride >= (int64_t)grid.size()) {
+      g0 = P;
+      grid.assign((size_t)((n - P - kMk5bHeader) / bstride + 1), FrameInfo{});
+      src.decode(FORMAT_MARK5B, g0, bstride, (int64_t)grid.size(), grid.data());
+    }
+    const FrameInfo h = grid[(size_t)((P - g0) / bstride)];
+    if ((h.flags & FRAME_CHECK) && !(h.frame_nr % kMk5bBlockFrames != 0 && frame_nr_valid)) {
+      prev = cur;
+      cur = h;
+      frame_nr_update();
+      if (P + bstride > n) return out;
+      std::vector<int64_t> frames;
+      for (int i = 0; i < kMk5bBlockFrames; i++) frames.push_back(P + i * fstride + kMk5bHeader);
+      P += bstride;
+      finish(std::move(frames));
+      continue;
+    }
+    // resync_header (mark5b_reader.cc:254-327) on the bytes that follow the
+    // header, fetched once: the scan reads at most 16 blocks plus one frame
+    // before it gives up, and a found block's eight frames after that
+    const int max_read = 16 * kMk5bBlock;
+    FetchedBytes r;
+    r.n = n;
+    r.base = r.pos = P + kMk5bHeader;
+    const int64_t span = std::min<int64_t>(n - r.base, 16 + max_read + 2 * kMk5bFrame + bstride);
+    r.b.resize((size_t)std::max<int64_t>(span, 0));
+    if (span > 0) src.fetch(r.base, span, r.b.data());
+    std::vector<uint8_t> buf(kMk5bFrame, 0);
+    int total = 0;
+    bool found = false, resynced = false;
+    r.get(kMk5bHeader, buf.data());
+    while (total < max_read && !r.short_read) {
+      const int64_t bstart = r.pos;  // recording offset of buf[16]
+      r.get(kMk5bFrame - kMk5bHeader, buf.data() + kMk5bHeader);
+      if (r.short_read) break;
+      total += kMk5bFrame - kMk5bHeader;
+      int pos;
+      for (pos = 0; pos < kMk5bFrame - kMk5bHeader; pos += 4)
+        if (word_at(buf.data() + pos, 0) == kMk5bSync) {
+          found = true;
+          break;
+        }
+      if (!found) {
+        std::memcpy(buf.data(), buf.data() + kMk5bFrame - kMk5bHeader, kMk5bHeader);
+        continue;
+      }
+      // the candidate header is buf[pos, pos + 16); the frame after it is
+      // the rest of the window and the bytes that follow it
+      const FrameInfo t = decode_mk5b(buf.data() + pos);
+      const int frame_start = pos + kMk5bHeader;
+      const int64_t frame0 = bstart + pos;
+      std::memmove(buf.data(), buf.data() + frame_start, kMk5bFrame - frame_start);
+      r.get(frame_start, buf.data() + kMk5bFrame - frame_start);
+      if (r.short_read) break;
+      total += frame_start;
+      if ((t.flags & FRAME_CHECK) && t.frame_nr % kMk5bBlockFrames == 0) {
+        prev = cur;
+        cur = t;
+        std::vector<int64_t> frames{frame0};
+        for (int i = 1; i < kMk5bBlockFrames; i++) {
+          r.get(kMk5bHeader, nullptr);
+          frames.push_back(r.pos);
+          r.get(kMk5bFrame, nullptr);
+        }
+        if (r.short_read) break;
+        frame_nr_update();
+        P = r.pos;
+        finish(std::move(frames));
+        resynced = true;
+        break;
+      }
+    }
+    if (!resynced) return out;
+  }
+}
+
+}  // namespace
+
+std::vector<FrameBlock> walk_frames(const ReaderParams &p, FrameSource &src) {
+  if (p.bits_per_sample != 1 && p.bits_per_sample != 2) throw std::invalid_argument("bits per sample must be 1 or 2");
+  if (p.tracks_per_channel < p.bits_per_sample) throw std::invalid_argument("fewer tracks than bits per sample");
+  if (p.track_bit_rate <= 0) throw std::invalid_argument("track bit rate must be positive");
+  if (p.format == FORMAT_VDIF) return walk_vdif(p, src);
+  if (p.format == FORMAT_MARK5B) return walk_mk5b(p, src);
+  throw std::invalid_argument("unknown recording format");
 }
 
 std::unique_ptr<FormatReader> FormatReader::create(const ReaderParams &p, const uint8_t *bytes, size_t n) {

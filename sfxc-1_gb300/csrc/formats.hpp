@@ -10,6 +10,8 @@
 #include <memory>
 #include <vector>
 
+#include "frames.hpp"
+
 namespace sfxc {
 
 enum { FORMAT_VDIF = 0, FORMAT_MARK5B = 1 };
@@ -45,5 +47,41 @@ class FormatReader {
 
 // Modified Julian Day of a Gregorian date (day count from 1858-11-17).
 int mjd_of_date(int day, int month, int year);
+
+// ---- The same readers over a recording that stays where it is (device
+// memory): the block, skip, restart and resync rules run on decoded frame
+// headers, and each block comes out as the recording offsets of its frames'
+// payloads instead of copied bytes.
+
+// What the walker reads of a recording it does not hold.
+class FrameSource {
+ public:
+  virtual ~FrameSource() {}
+  virtual int64_t size() const = 0;
+  // decoded headers (decode_vdif / decode_mk5b of 16 bytes) of the frames at
+  // pos0 + k * stride, k < count; every such pos + 16 <= size()
+  virtual void decode(int format, int64_t pos0, int64_t stride, int64_t count, FrameInfo *out) = 0;
+  // raw bytes [pos, pos + len), within size(): only the Mark5B sync search reads them
+  virtual void fetch(int64_t pos, int64_t len, uint8_t *dst) = 0;
+};
+
+// One reader block: the reader's data bytes are the frames' payloads,
+// frame_bytes each at block offsets 0, frame_bytes, ..., then zeros up to
+// size.  invalid: the VDIF invalid-frame runs; Mark5B blocks take their
+// fill-pattern runs (fill_pattern_runs over the block bytes) afterwards.
+struct FrameBlock {
+  int channel = -1;
+  int64_t start_ticks = 0;
+  int32_t size = 0;
+  int32_t frame_bytes = 0;
+  std::vector<int64_t> frames;
+  std::vector<int32_t> invalid;
+};
+
+// Every block FormatReader::create(p, ...)->next() returns for the
+// recording, in order.  One difference: where a truncated Mark5B recording
+// ends inside a resync, the reader may still return one block whose bytes
+// are partly left over from the previous block; the walk ends before it.
+std::vector<FrameBlock> walk_frames(const ReaderParams &p, FrameSource &src);
 
 }  // namespace sfxc

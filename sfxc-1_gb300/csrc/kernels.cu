@@ -298,29 +298,13 @@ __global__ void unpack_kernel(const StreamDev *__restrict__ streams, float *__re
 }
 
 // Channel extraction: output byte `ob` of subband s packs spb = 8/fan_out
-// samples, first sample in the lowest bits; sample j reads word ob*spb+j.
-// Bit placement follows Channel_extractor_5 (sfxc/src/channel_extractor_5.cc:40-58,
-// 67-99): track t of a sample lands at low_bit << ((t+1) % bits) with low_bit
-// starting at 1 << (8 - fan_out) and advancing by `bits` per complete sample,
-// and each earlier sample is shifted down by fan_out per later sample.
+// samples (extract_byte); sample j reads word ob*spb+j.
 __global__ void extract_kernel(const uint8_t *__restrict__ in, int64_t nout, int N, int bits, int fan_out,
                                const int *__restrict__ tracks, uint8_t *__restrict__ out) {
   const int64_t ob = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int sb = blockIdx.y;
   if (ob >= nout) return;
-  const int spb = 8 / fan_out;
-  unsigned byte = 0;
-  for (int j = 0; j < spb; j++) {
-    const uint8_t *w = in + (ob * spb + j) * N;
-    unsigned v = 0, low_bit = 1u << (8 - fan_out);
-    for (int t = 0; t < fan_out; t++) {
-      const int tr = tracks[sb * fan_out + t];
-      if ((w[tr >> 3] >> (tr & 7)) & 1) v |= low_bit << ((t + 1) % bits);
-      if ((t + 1) % bits == 0) low_bit <<= bits;
-    }
-    byte |= (v >> ((spb - 1 - j) * fan_out)) & 0xffu;
-  }
-  out[(int64_t)sb * nout + ob] = (uint8_t)byte;
+  out[(int64_t)sb * nout + ob] = extract_byte(in + ob * (8 / fan_out) * N, N, bits, fan_out, tracks + sb * fan_out);
 }
 
 // ------------------------------------------------------------------------

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "device.cuh"
+#include "frames.hpp"
 
 namespace sfxc {
 
@@ -102,5 +103,28 @@ struct PcalRun {
 };
 void launch_phasecal(const uint8_t *data, const PcalRun *runs, int nruns, int pb, int bits, int32_t *acc,
                      cudaStream_t st);
+
+// Recordings in device memory (recording.cu)
+// one protocol record as the input-node writer emits it, with its byte offset in the output
+struct ProtoRecord {
+  int64_t src;  // HEADER_DATA: payload offset in the channel stream
+  int64_t out;  // offset of the record's first byte in the protocol bytes
+  int32_t n;    // HEADER_DATA bytes / HEADER_INVALID samples
+  uint8_t type; // HEADER_*
+  int8_t rem;   // HEADER_DELAY
+  uint16_t pad;
+};
+void launch_decode_frames(const uint8_t *rec, int64_t pos0, int64_t stride, int64_t count, int mk5b, FrameInfo *out,
+                          cudaStream_t st);
+// runs == NULL: counts[b] = number of runs of block b; else runs at 2 * offsets[b]
+void launch_fill_runs(const uint8_t *rec, const int64_t *frames, int nf, int wpf, int nw, int nblocks,
+                      int32_t *counts, const int64_t *offsets, int32_t *runs, cudaStream_t st);
+void launch_gather_blocks(const uint8_t *rec, const int64_t *frames, int nf, int fb, int block_size,
+                          const int32_t *list, int nlist, uint8_t *out, cudaStream_t st);
+void launch_extract_frames(const uint8_t *rec, const int64_t *frames, int nf, int fb, int64_t opb, int64_t nout,
+                           int N, int bits, int nsub, int fan_out, const int *tracks, uint8_t *out,
+                           cudaStream_t st);
+void launch_serialize_protocol(const ProtoRecord *recs, int nrec, const uint8_t *stream, uint8_t *out,
+                               cudaStream_t st);
 
 }  // namespace sfxc

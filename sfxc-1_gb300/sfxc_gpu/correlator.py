@@ -243,6 +243,119 @@ class CorrelatorNode:
         return [out[i * per:(i + 1) * per].tobytes() for i in range(nsub)]
 
 
+def _slices(slices):
+    keep = []
+    sl = (L.Slice * max(1, len(slices)))()
+    for i, (s0, s1, ns, dl) in enumerate(slices):
+        tk = (C.c_int64 * len(dl))(*[d[0] for d in dl])
+        by = (C.c_int32 * len(dl))(*[d[1] for d in dl])
+        rm = (C.c_int32 * len(dl))(*[d[2] for d in dl])
+        keep += [tk, by, rm]
+        sl[i] = L.Slice(s0, s1, ns, len(dl), tk, by, rm)
+    return sl, keep
+
+
+class DeviceRecording:
+    """A station recording read, channel-extracted and turned into the
+    input-node protocol on the GPU of `node` (sfxc_gpu_recording_*): the same
+    blocks as read_recording, channels as extract_block / thread_channel_blocks,
+    protocol bytes as write_protocol.  recording: bytes / uint8 array (host),
+    or a CUDA uint8 torch tensor on the node's device (used in place)."""
+
+    def __init__(self, node, recording, fmt, *, ref_ticks, offset_ticks=0, track_bit_rate, frame_size=0, n_tracks,
+                 bits, channel_tracks):
+        self._lib, self._node = node._lib, node
+        firsts = (C.c_int32 * len(channel_tracks))(*[int(t[0]) for t in channel_tracks])
+        p = L.ReaderParams(L.FORMAT_VDIF if fmt == "vdif" else L.FORMAT_MARK5B, int(ref_ticks), int(offset_ticks),
+                           int(track_bit_rate), int(frame_size), int(n_tracks), int(bits), len(channel_tracks[0]),
+                           len(channel_tracks), firsts)
+        if hasattr(recording, "data_ptr"):
+            self._rec = recording  # kept alive: the library reads it in place
+            ptr, n, on_dev = recording.data_ptr(), recording.numel(), 1
+        else:
+            self._rec = np.ascontiguousarray(np.frombuffer(bytes(recording), dtype=np.uint8))
+            ptr, n, on_dev = (self._rec.ctypes.data if self._rec.size else None), self._rec.size, 0
+        self._h = self._lib.sfxc_gpu_recording_create(node._h, C.byref(p), ptr, n, on_dev)
+        if not self._h:
+            raise L.SfxcError(L.EINVAL, self._lib.sfxc_gpu_last_error(node._h).decode())
+        self._nch = 0
+
+    def close(self):
+        if self._h:
+            self._lib.sfxc_gpu_recording_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        return self._node._check(rc)
+
+    def blocks(self, data=True):
+        """[{channel, start_ticks, data (None unless data), invalid}] per reader block."""
+        out = []
+        b = L.ReaderBlock()
+        for i in range(self._lib.sfxc_gpu_recording_n_blocks(self._h)):
+            self._check(self._lib.sfxc_gpu_recording_block(self._h, i, C.byref(b), None))
+            buf = np.empty(b.size, dtype=np.uint8) if data else None
+            if data:
+                self._check(self._lib.sfxc_gpu_recording_block(self._h, i, C.byref(b), buf.ctypes.data))
+            out.append({"channel": b.channel, "start_ticks": b.start_ticks,
+                        "data": buf.tobytes() if data else None,
+                        "invalid": [(b.invalid[2 * k], b.invalid[2 * k + 1]) for k in range(b.n_invalid)]})
+        return out
+
+    def extract(self, word_bytes, bits, tracks):
+        """Subbands of every block (tracks: list per subband, as extract_block)."""
+        nsub, fan_out = len(tracks), len(tracks[0])
+        flat = (C.c_int32 * (nsub * fan_out))(*[t for tr in tracks for t in tr])
+        self._check(self._lib.sfxc_gpu_recording_extract(self._h, word_bytes, bits, nsub, fan_out, flat))
+        self._nch = nsub
+
+    def extract_threads(self, n_channels):
+        """One channel per VDIF thread, blocks as they are (thread_channel_blocks)."""
+        self._check(self._lib.sfxc_gpu_recording_extract(self._h, 0, 0, n_channels, 0, None))
+        self._nch = n_channels
+
+    def channel(self, c):
+        """Channel c's blocks [(start_ticks, bytes, [(begin, n)])], as write_protocol takes them."""
+        nb = self._check(self._lib.sfxc_gpu_recording_channel(self._h, c, 0, None, None))
+        cb = (L.ChannelBlock * max(1, nb))()
+        total = 0
+        self._check(self._lib.sfxc_gpu_recording_channel(self._h, c, nb, cb, None))
+        total = sum(cb[i].size for i in range(nb))
+        data = np.empty(max(1, total), dtype=np.uint8)
+        self._check(self._lib.sfxc_gpu_recording_channel(self._h, c, nb, cb, data.ctypes.data))
+        out, off = [], 0
+        for i in range(nb):
+            out.append((cb[i].start_ticks, data[off:off + cb[i].size].tobytes(),
+                        [(cb[i].invalid[2 * k], cb[i].invalid[2 * k + 1]) for k in range(cb[i].n_invalid)]))
+            off += cb[i].size
+        return out
+
+    def protocol(self, c, slices, sample_rate, bits, integration_time_us, copy=True):
+        """Channel c's protocol for `slices` ([(start, stop, nr_samples, delays)])
+        assembled on the device; with copy, the bytes of each slice."""
+        sl, keep = _slices(slices)
+        offs = (C.c_int64 * (len(slices) + 1))()
+        need = self._lib.sfxc_gpu_recording_protocol(self._h, c, len(slices), sl, sample_rate, bits,
+                                                     integration_time_us, None, 0, offs)
+        self._check(need)
+        if not copy:
+            return None
+        out = np.empty(max(1, int(need)), dtype=np.uint8)
+        self._check(self._lib.sfxc_gpu_recording_protocol(self._h, c, len(slices), sl, sample_rate, bits,
+                                                          integration_time_us, out.ctypes.data, need, offs))
+        return [out[offs[i]:offs[i + 1]].tobytes() for i in range(len(slices))]
+
+    def push(self, c, slice_index, node, stream):
+        """Slice `slice_index` of channel c's last protocol into a correlator node's stream, device to device."""
+        node._check(self._lib.sfxc_gpu_recording_push(self._h, c, slice_index, node._h, stream))
+
+
 class PhaseCal:
     """Phase-cal extraction of one channel on a CorrelatorNode's GPU
     (Input_node_data_writer::do_phasecal, sfxc/src/input_node_data_writer.cc:230-312).

@@ -8,12 +8,14 @@ No GPU needed (the readers are host code behind the C ABI)."""
 import hashlib
 import json
 import os
+import subprocess
 
 import pytest
 
 import format_cases
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "sfxc-1_gb300", "csrc")
 GOLDEN = json.load(open(os.path.join(HERE, "golden", "formats.json")))
 CASES = format_cases.cases()
 
@@ -69,3 +71,41 @@ def test_reader_rejects_bad_parameters(sfxc_lib):
     with pytest.raises(lib.SfxcError):
         correlator.read_recording(CASES["mark5b_day_rollover"]["rec"], "mark5b", **mk)
     assert correlator.read_recording(b"", "vdif", **c["params"]) == []
+
+
+@pytest.fixture(scope="module")
+def walk_driver(tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("walk") / "walk_driver")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I" + CSRC, os.path.join(HERE, "walk_driver.cc"),
+                    os.path.join(CSRC, "formats.cpp"), "-o", exe], check=True)
+    return exe
+
+
+def walk_blocks(exe, tmp_path, c):
+    """Blocks of the frame walker (walk_frames over headers decoded by the
+    device decode's functions, bytes assembled from the frame offsets)."""
+    rec = tmp_path / "rec"
+    rec.write_bytes(bytes(c["rec"]))
+    pr = c["params"]
+    ct = pr["channel_tracks"]
+    args = [exe, str(rec), str(tmp_path / "out"), "0" if c["fmt"] == "vdif" else "1", str(pr["ref_ticks"]),
+            str(pr.get("offset_ticks", 0)), str(pr["track_bit_rate"]), str(pr.get("frame_size", 0)),
+            str(pr["n_tracks"]), str(pr["bits"]), str(len(ct[0]))] + [str(t[0]) for t in ct]
+    lines = subprocess.run(args, capture_output=True, text=True, check=True).stdout.split("\n")
+    data = (tmp_path / "out").read_bytes()
+    blocks, off = [], 0
+    for line in filter(None, lines):
+        v = list(map(int, line.split()))
+        ch, start, size, nr = v[:4]
+        blocks.append({"channel": ch, "start_ticks": start, "data": data[off:off + size],
+                       "invalid": [(v[4 + 2 * i], v[5 + 2 * i]) for i in range(nr)]})
+        off += size
+    return blocks
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_frame_walk_matches_reference_blocks(name, walk_driver, tmp_path):
+    """The readers restated on decoded frame headers (the block decisions of
+    the device-resident recording path) give the reference readers' blocks."""
+    c = CASES[name]
+    assert _summary(walk_blocks(walk_driver, tmp_path, c)) == GOLDEN[name]["blocks"]

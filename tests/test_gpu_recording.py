@@ -8,10 +8,19 @@ Input_node_data_writer, sfxc/src/input_data_format_reader_tasklet.cc:93-160,
 sfxc/src/channel_extractor_tasklet.cc:120-220,
 sfxc/src/input_node_data_writer.cc:107-229).  A VDIF frame marked invalid
 becomes the same invalid run in both paths."""
+import hashlib
+import json
+import os
+
 import numpy as np
 import pytest
 
+import format_cases
+
 pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = json.load(open(os.path.join(HERE, "golden", "formats.json")))
 
 TRACKS16 = [[2 * c + 1, 2 * c] for c in range(16)]
 
@@ -135,3 +144,156 @@ def test_vdif_thread_per_channel_path(gpu_node):
     cor_direct, tsys_direct = gpu_node.correlate(job)
     cor_rec, tsys_rec = gpu_node.correlate(dict(job, protocols=protos))
     assert cor_rec == cor_direct and tsys_rec == tsys_direct
+
+
+# ---- the same paths with the recording kept on the device
+# (sfxc_gpu_recording_*: headers decoded, fill runs found, channels
+# extracted and protocol bytes assembled by kernels)
+
+def _summary(blocks):
+    return [{"channel": b["channel"], "start_ticks": b["start_ticks"], "size": len(b["data"]),
+             "sha256": hashlib.sha256(b["data"]).hexdigest(), "invalid": [list(r) for r in b["invalid"]]}
+            for b in blocks]
+
+
+@pytest.mark.parametrize("name", sorted(GOLDEN))
+def test_device_reader_matches_reference_blocks(name, gpu_node):
+    """Every block of the reference readers on the format fixtures (misaligned
+    first frames, invalid and fill frames, gaps, unknown threads, legacy
+    headers, CRC failures, lost sync, garbage, fill runs, day roll-over, VLBA
+    time stamps, truncation), from the device-resident recording."""
+    from sfxc_gpu import correlator
+    c = format_cases.cases()[name]
+    rec = correlator.DeviceRecording(gpu_node, c["rec"], c["fmt"], **c["params"])
+    assert _summary(rec.blocks()) == GOLDEN[name]["blocks"]
+    rec.close()
+
+
+def test_device_reader_in_place(gpu_node):
+    """A recording already in device memory is read where it lies."""
+    import torch
+    from sfxc_gpu import correlator
+    c = format_cases.cases()["mark5b_zero_crc_fill"]
+    t = torch.frombuffer(bytearray(c["rec"]), dtype=torch.uint8).cuda()
+    rec = correlator.DeviceRecording(gpu_node, t, c["fmt"], **c["params"])
+    assert _summary(rec.blocks()) == GOLDEN["mark5b_zero_crc_fill"]["blocks"]
+    rec.close()
+
+
+def _device_protocols(gpu_node, sc, recs, fmt, reader_params, chans=None):
+    """Per station: the device recording, its subbands R/L (channels 0, 1 of
+    the 16-channel words) compared block by block with the direct path, and
+    their protocols for the job's slice."""
+    from sfxc_gpu import correlator, scenario, timebase
+    dels = scenario.del_tables(sc)
+    rec0, start, tint, slice_samples = scenario.job_timing(sc)
+    protos, objs = [], []
+    for si in range(len(sc.stations)):
+        r = correlator.DeviceRecording(gpu_node, recs[si], fmt, ref_ticks=timebase.ticks_from_mjd_sec(sc.mjd, 0.0),
+                                       channel_tracks=TRACKS16, **reader_params)
+        r.extract(4, 2, [TRACKS16[0], TRACKS16[1]])
+        slices = [(start, start + tint, slice_samples, correlator.delay_list(dels[si], start, start + tint,
+                                                                              sc.sample_rate, sc.bits))]
+        for c, pol in enumerate(sc.pols):
+            direct = scenario.blocks_of(sc, scenario.channel_streams(sc, fast_random=True)[0][(si, pol)], (si, pol))
+            got = r.channel(c)[:len(direct)]
+            assert [(t, bytes(d), list(map(tuple, inv))) for t, d, inv in got] == \
+                [(t, bytes(d), list(map(tuple, inv))) for t, d, inv in direct], (si, pol)
+            protos.append(r.protocol(c, slices, sc.sample_rate, sc.bits, sc.integration_us))
+        objs.append(r)
+    return protos, objs
+
+
+def _correlate_pushed(node, job, objs, per_station):
+    """The job's single integration with every stream pushed device to device."""
+    node.set_parameters(job)
+    for k in range(len(job["streams"])):
+        objs[k // per_station].push(k % per_station, 0, node, k)
+    o, t = node.run_integration()
+    return bytes(o), b"".join(t)
+
+
+def test_vdif_recording_device_path(gpu_node):
+    from sfxc_gpu import synth
+    sc, job, chans, nsamp = _job_and_streams(dict(
+        block_bytes=2000, runs=lambda st: {(st[1].number, "R"): [(1, 500, 500)], (st[1].number, "L"): [(1, 500, 500)]}))
+    recs = [synth.vdif_file_bytes(_words(chans, si, nsamp, 300 + si), payload_bytes=8000, sample_rate=sc.sample_rate,
+                                  nchan=16, bits=2, start_mjd=sc.mjd, start_sec_of_day=sc.sec0,
+                                  invalid_frames=(5,) if si == 1 else ())
+            for si in range(len(sc.stations))]
+    protos, objs = _device_protocols(gpu_node, sc, recs, "vdif",
+                                     dict(track_bit_rate=sc.sample_rate, frame_size=8000, n_tracks=32, bits=2))
+    # the same bytes as the input-node writer's (SHA-equal per slice)
+    assert [[hashlib.sha256(x).hexdigest() for x in p] for p in protos] == \
+        [[hashlib.sha256(bytes(x)).hexdigest() for x in p] for p in job["protocols"]]
+    cor_direct, tsys_direct = gpu_node.correlate(job)
+    cor_dev, tsys_dev = _correlate_pushed(gpu_node, job, objs, len(sc.pols))
+    assert cor_dev == cor_direct and tsys_dev == tsys_direct
+
+
+def test_mark5b_recording_device_path(gpu_node):
+    from sfxc_gpu import synth
+    sc, job, chans, nsamp = _job_and_streams(dict(block_bytes=5000, runs=lambda st: {}))
+    fps = sc.sample_rate * 32 // 80000
+    recs = []
+    for si in range(len(sc.stations)):
+        w = _words(chans, si, nsamp, 400 + si)
+        recs.append(synth.mark5b_recording(w.size // 2500, mjd=sc.mjd, sec_of_day=sc.sec0, frames_per_second=fps,
+                                           crc="valid", payload_words=w))
+    protos, objs = _device_protocols(gpu_node, sc, recs, "mark5b", dict(track_bit_rate=sc.sample_rate, n_tracks=32,
+                                                                         bits=2))
+    assert protos == [[bytes(x) for x in p] for p in job["protocols"]]
+    cor_direct, tsys_direct = gpu_node.correlate(job)
+    cor_dev, tsys_dev = _correlate_pushed(gpu_node, job, objs, len(sc.pols))
+    assert cor_dev == cor_direct and tsys_dev == tsys_direct
+
+
+def test_vdif_thread_per_channel_device_path(gpu_node):
+    from sfxc_gpu import correlator, scenario, synth, timebase
+    sc, job, chans, nsamp = _job_and_streams(dict(
+        block_bytes=8000, runs=lambda st: {(st[1].number, "L"): [(5, 0, 8000)]}))
+    dels = scenario.del_tables(sc)
+    rec0, start, tint, slice_samples = scenario.job_timing(sc)
+    frame = 32 + 8000
+    protos, objs = [], []
+    for si in range(len(sc.stations)):
+        per_thread = []
+        for th, pol in enumerate(("R", "L")):
+            words = np.frombuffer(bytes(chans[(si, pol)]), dtype=np.uint32)
+            per_thread.append(synth.vdif_file_bytes(words, payload_bytes=8000, sample_rate=sc.sample_rate, nchan=1,
+                                                    bits=2, start_mjd=sc.mjd, start_sec_of_day=sc.sec0,
+                                                    thread_id=th,
+                                                    invalid_frames=(5,) if (si == 1 and pol == "L") else ()))
+        nf = min(len(t) for t in per_thread) // frame
+        rec = b"".join(per_thread[th][f * frame:(f + 1) * frame] for f in range(nf) for th in range(2))
+        r = correlator.DeviceRecording(gpu_node, rec, "vdif", ref_ticks=timebase.ticks_from_mjd_sec(sc.mjd, 0.0),
+                                       track_bit_rate=sc.sample_rate, frame_size=8000, n_tracks=0, bits=2,
+                                       channel_tracks=[[0, 1], [1, 0]])
+        r.extract_threads(2)
+        slices = [(start, start + tint, slice_samples, correlator.delay_list(dels[si], start, start + tint,
+                                                                              sc.sample_rate, sc.bits))]
+        for c, pol in enumerate(sc.pols):
+            direct = scenario.blocks_of(sc, chans[(si, pol)], (si, pol))
+            got = r.channel(c)[:len(direct)]
+            assert [(t, bytes(d), list(map(tuple, inv))) for t, d, inv in got] == \
+                [(t, bytes(d), list(map(tuple, inv))) for t, d, inv in direct], (si, pol)
+            protos.append(r.protocol(c, slices, sc.sample_rate, sc.bits, sc.integration_us))
+        objs.append(r)
+    assert protos == [[bytes(x) for x in p] for p in job["protocols"]]
+    cor_direct, tsys_direct = gpu_node.correlate(job)
+    cor_dev, tsys_dev = _correlate_pushed(gpu_node, job, objs, len(sc.pols))
+    assert cor_dev == cor_direct and tsys_dev == tsys_direct
+
+
+def test_device_recording_errors(gpu_node):
+    """Bad parameters and calls out of order fail with a status, no device work."""
+    from sfxc_gpu import correlator, lib
+    c = format_cases.cases()["vdif_legacy"]
+    with pytest.raises(lib.SfxcError):
+        correlator.DeviceRecording(gpu_node, c["rec"], "vdif", **dict(c["params"], frame_size=0))
+    r = correlator.DeviceRecording(gpu_node, c["rec"], "vdif", **c["params"])
+    with pytest.raises(lib.SfxcError):  # no channels extracted yet
+        r.channel(0)
+    with pytest.raises(lib.SfxcError):  # 8000-byte frames are not whole output bytes of 3-byte words
+        r.extract(3, 2, [[1, 0]])
+    r.close()
