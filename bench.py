@@ -471,6 +471,99 @@ def measure_c4(args, log, x_mode="tc"):
             "data": "seeded uniform 2-bit/1-bit codes, cubic delay models"}
 
 
+F1_NAME = ("station front end: VDIF recording, 16 channels x 2 bits x 32 Ms/s in 32-bit words, 8000-byte "
+           "payloads, 4 s (515 MB); headers decoded, 16 channels extracted, each channel's protocol for three "
+           "1 s slices assembled")
+TRACKS16 = [[2 * c + 1, 2 * c] for c in range(16)]
+
+
+def measure_frontend(args, log):
+    """The input node's front end on the device (sfxc_gpu_recording_*): one
+    station's VDIF recording read (frame headers decoded, blocks found), all
+    16 channels extracted where the frames lie, and every channel's protocol
+    for three 1 s slices (delays from a cubic delay model) assembled on the
+    device.  value: recording bytes per second with the recording resident in
+    HBM; e2e: the same from pinned host memory, its copy to the device inside
+    the timed region.  Host wall clock around the synchronous calls (the
+    header walk and the writer's records run on the host between kernels)."""
+    import torch
+    from sfxc_gpu import correlator, lib, scenario, synth, timebase
+    seconds, sr, nch = 4, 32_000_000, 16
+    st = scenario.cubic_stations(1, seed=5, max_delay=4e-3, max_rate=1e-6)
+    sc = scenario.Scenario(stations=st, pols=("R",), sample_rate=sr, bandwidth=sr // 2, bits=2,
+                           channel_freq=1_600_000_000, nchan=512, integration_us=1_000_000,
+                           n_integrations=seconds - 1, sub_integration_us=1_000_000, lead_us=100_000, seed=3)
+    rng = np.random.Generator(np.random.PCG64(11))
+    words = np.frombuffer(rng.bytes(seconds * sr * nch * 2 // 8), dtype=np.uint32)
+    t = time.time()
+    rec = synth.vdif_file_bytes(words, payload_bytes=8000, sample_rate=sr, nchan=nch, bits=2, start_mjd=sc.mjd,
+                                start_sec_of_day=sc.sec0)
+    pinned = torch.empty(len(rec), dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = np.frombuffer(rec, dtype=np.uint8)
+    del rec
+    log("built the front-end recording (%d bytes) in %.1f s" % (pinned.numel(), time.time() - t))
+    dels = scenario.del_tables(sc)
+    rec0, start, tint, slice_samples = scenario.job_timing(sc)
+    slices = [(start + k * tint, start + (k + 1) * tint, slice_samples,
+               correlator.delay_list(dels[0], start + k * tint, start + (k + 1) * tint, sr, 2))
+              for k in range(sc.n_integrations)]
+    params = dict(ref_ticks=timebase.ticks_from_mjd_sec(sc.mjd, 0.0), track_bit_rate=sr, frame_size=8000,
+                  n_tracks=32, bits=2, channel_tracks=TRACKS16)
+    node = correlator.CorrelatorNode(0, lib.X_FP32)
+    resident = pinned.cuda()
+    nbytes = pinned.numel()
+
+    def step(src, marks=None):
+        t = [time.perf_counter()]
+        r = correlator.DeviceRecording(node, src, "vdif", **params)
+        t.append(time.perf_counter())
+        r.extract(4, 2, TRACKS16)
+        t.append(time.perf_counter())
+        for c in range(nch):
+            r.protocol(c, slices, sr, 2, sc.integration_us, copy=False)
+        t.append(time.perf_counter())
+        n = r.n_blocks()
+        r.close()
+        t.append(time.perf_counter())
+        if marks is not None:
+            marks.update({k: round((t[i + 1] - t[i]) * 1e3, 3) for i, k in enumerate(
+                ("read_ms", "extract_ms", "protocol_ms", "release_ms"))})
+        return n
+
+    out = {}
+    try:
+        for name, src in (("value", resident), ("e2e", pinned.numpy())):
+            for _ in range(args.warmup):
+                nblocks = step(src)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                step(src)
+            torch.cuda.synchronize()
+            out[name] = (time.perf_counter() - t0) / args.steps
+        stages = {}
+        step(resident, stages)  # one more step, split by call (synchronous calls, host clock)
+    finally:
+        node.close()
+    # algorithmic bytes: the recording read once, the channels written,
+    # read back into the protocol, the protocol written (about the channel bytes)
+    chan_bytes = nblocks * 32000
+    algo = nbytes + 3 * chan_bytes
+    hbm, hbm_src = measured_peaks()
+    achieved = algo / out["value"] / 1e9
+    return {"workload": F1_NAME, "value": round(nbytes / out["value"] / 1e9, 3), "unit": "GB/s of recording",
+            "ms_per_step": round(out["value"] * 1e3, 3), "recording_bytes": nbytes, "reader_blocks": nblocks,
+            "real_time_factor": round(seconds / out["value"], 1), "resident_step_split_ms": stages,
+            "e2e": {"value": round(nbytes / out["e2e"] / 1e9, 3), "unit": "GB/s of recording",
+                    "ms_per_step": round(out["e2e"] * 1e3, 3), "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": 0},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
+                         "frac": round(achieved / hbm, 3), "peak_source": hbm_src, "unit": "GB/s",
+                         "algorithmic_bytes_per_step": algo,
+                         "note": "whole front end (host walk and writer records included) against the copy peak"},
+            "data": "seeded uniform random payload words, cubic delay model"}
+
+
 def summary(cfg, res, args, x_mode, world=1):
     value = res["total"] * args.steps * world / (res["dev_total"] / 1e3) / 1e9
     d = {"workload": cfg["name"], "value": round(value, 3), "unit": "Gsamples/s",
@@ -523,6 +616,7 @@ def run_gpu(args):
                 r = measure(c, args, m, log, e2e=False, compare_fp32=(m == "tc"), peaks=peaks)
                 extra[name] = summary(c, r, args, m)
         extra["c4"] = measure_c4(args, log)
+        extra["f1"] = measure_frontend(args, log)
     if rank != 0:
         return
     total = res["total"]
@@ -668,6 +762,8 @@ def main():
     ap.add_argument("--cpu-sample-us", type=int, default=31250,
                     help="integration of each CPU job (a bounded sample of the workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--frontend-only", action="store_true",
+                    help="time only the station front end (recording to protocol on the device)")
     args = ap.parse_args()
     if args.impl == "reference":
         # the CPU arm builds only the restatement: the GPU library is neither
@@ -675,6 +771,10 @@ def main():
         from oracle import build_oracle
         build_oracle.build()
         run_reference(args)
+    elif args.frontend_only:
+        import __graft_entry__
+        __graft_entry__.build()
+        print(json.dumps(measure_frontend(args, lambda m: print(m, file=sys.stderr, flush=True))), flush=True)
     else:
         import __graft_entry__
         __graft_entry__.build()

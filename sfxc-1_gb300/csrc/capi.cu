@@ -227,6 +227,15 @@ struct JobTables {
   int npad = 0, ntiles = 0;
 };
 
+// Device buffers of a recording (sfxc_gpu_recording_*), kept by the
+// context for the next recording once one is destroyed.
+struct RecordingBuffers {
+  DevBuf own, frames, chan, tracks, list, gathered, counts, offs, runs, info;
+  std::vector<DevBuf> proto;           // protocol bytes per channel
+  std::map<int, DevBuf> plan_recs;     // the protocol records of the last plan of each group
+  HostBuf staging;                     // decoded headers on their way to the host
+};
+
 }  // namespace
 
 struct sfxc_gpu_ctx {
@@ -295,6 +304,8 @@ struct sfxc_gpu_ctx {
   // X-step's error flag (one readback copy each)
   DevBuf hist;
   std::vector<StreamDev> hsd;
+  // buffers of destroyed recordings, for the next ones
+  std::vector<std::unique_ptr<RecordingBuffers>> rec_spare;
 };
 
 namespace {
@@ -2179,15 +2190,19 @@ struct DeviceFrames : FrameSource {
   const uint8_t *rec = nullptr;
   int64_t n = 0;
   cudaStream_t st = nullptr;
-  DevBuf info;
+  DevBuf *info = nullptr;
+  HostBuf *staging = nullptr;
   int64_t size() const override { return n; }
   void decode(int format, int64_t pos0, int64_t stride, int64_t count, FrameInfo *out) override {
     if (count <= 0) return;
-    info.ensure((size_t)count * sizeof(FrameInfo));
-    launch_decode_frames(rec, pos0, stride, count, format == FORMAT_MARK5B, info.as<FrameInfo>(), st);
+    const size_t bytes = (size_t)count * sizeof(FrameInfo);
+    info->ensure(bytes);
+    launch_decode_frames(rec, pos0, stride, count, format == FORMAT_MARK5B, info->as<FrameInfo>(), st);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(out, info.p, (size_t)count * sizeof(FrameInfo), cudaMemcpyDeviceToHost, st));
+    staging->ensure(bytes);
+    CK(cudaMemcpyAsync(staging->p, info->p, bytes, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    std::memcpy(out, staging->p, bytes);
   }
   void fetch(int64_t pos, int64_t len, uint8_t *dst) override {
     if (len <= 0) return;
@@ -2197,29 +2212,40 @@ struct DeviceFrames : FrameSource {
 };
 }  // namespace
 
+// The writer's records for one set of slices and their serialised layout:
+// shared by every subband of an extracted recording (same blocks, same
+// invalid runs, payload offsets relative to the channel's bytes).
+struct ProtoPlan {
+  std::vector<int64_t> key;  // the slices and arguments it was made for
+  int group = 0;             // channel (one channel per thread) or -1 (every subband)
+  std::vector<int64_t> offsets;
+  std::vector<std::vector<Record>> slice_recs;  // DATA payload offsets within the slice's bytes
+  std::vector<ProtoRecord> dev_recs;  // also on the device, in the recording's plan buffer of its group
+  int64_t total = 0;
+};
+
 struct sfxc_gpu_recording {
   sfxc_gpu_ctx *ctx = nullptr;
   ReaderParams p;
-  DevBuf own;  // the recording, when it was passed in host memory
+  std::unique_ptr<RecordingBuffers> buf;
   const uint8_t *rec = nullptr;
   int64_t n = 0;
   std::vector<FrameBlock> blocks;
-  int nf = 0, fb = 0, block_size = 0;
-  DevBuf frames;  // [block][nf] payload offsets in the recording
-  // channel streams: channel c's bytes at chan + chan_off[c], its blocks
-  // (offsets within them) and their invalid runs as (begin, n) pairs
-  DevBuf chan, tracks, list, gathered;
+  int nf = 0, fb = 0, block_size = 0;  // frames per block, frame payload bytes, block bytes
+  // channel streams: channel c's bytes at buf->chan + chan_off[c], its
+  // blocks (offsets within them) and their invalid runs as (begin, n) pairs
+  bool per_thread = false;
   std::vector<int64_t> chan_off;
-  std::vector<std::vector<ChannelBlock>> chan_blocks;
-  std::vector<std::vector<std::vector<int32_t>>> chan_runs;
-  // the last protocol of each channel: its bytes on the device and, per
-  // slice, the byte range and the records (DATA payload offsets within the slice's bytes)
-  struct Protocol {
-    DevBuf bytes, recs;
-    std::vector<int64_t> offsets;
-    std::vector<std::vector<Record>> slice_recs;
-  };
-  std::vector<Protocol> proto;
+  // block lists: every subband of an extracted recording shares one, each
+  // VDIF thread's channel has its own; chan_set[c] is channel c's
+  std::vector<int> chan_set;
+  std::vector<std::vector<ChannelBlock>> set_blocks;
+  std::vector<std::vector<std::vector<int32_t>>> set_runs;
+  const std::vector<ChannelBlock> &blocks_of(int c) const { return set_blocks[chan_set[c]]; }
+  int n_channels() const { return (int)chan_set.size(); }
+  // each channel's last protocol (its bytes in buf->proto[c])
+  std::vector<std::shared_ptr<ProtoPlan>> proto;
+  std::shared_ptr<ProtoPlan> last_plan;
 };
 
 sfxc_gpu_recording *sfxc_gpu_recording_create(sfxc_gpu_ctx *c, const sfxc_reader_params *params,
@@ -2233,40 +2259,49 @@ sfxc_gpu_recording *sfxc_gpu_recording_create(sfxc_gpu_ctx *c, const sfxc_reader
     r->ctx = c;
     r->p = reader_params(params);
     r->n = (int64_t)n;
+    if (!c->rec_spare.empty()) {
+      r->buf = std::move(c->rec_spare.back());
+      c->rec_spare.pop_back();
+    } else {
+      r->buf.reset(new RecordingBuffers());
+    }
+    RecordingBuffers &B = *r->buf;
     if (bytes_on_device) {
       r->rec = bytes;
     } else {
-      r->own.ensure(n + 16);
-      if (n) CK(cudaMemcpyAsync(r->own.p, bytes, n, cudaMemcpyHostToDevice, c->st));
-      r->rec = r->own.as<uint8_t>();
+      B.own.ensure(n + 16);
+      if (n) CK(cudaMemcpyAsync(B.own.p, bytes, n, cudaMemcpyHostToDevice, c->st));
+      r->rec = B.own.as<uint8_t>();
     }
     DeviceFrames src;
     src.rec = r->rec;
     src.n = r->n;
     src.st = c->st;
+    src.info = &B.info;
+    src.staging = &B.staging;
+    FrameWalk walk;
     try {
-      r->blocks = walk_frames(r->p, src);
+      walk = walk_frames(r->p, src);
     } catch (const std::invalid_argument &e) {
       throw Error(SFXC_GPU_EINVAL, e.what());
     } catch (const std::logic_error &e) {
       throw Error(SFXC_GPU_ESTATE, e.what());
     }
+    r->blocks = std::move(walk.blocks);
     if (!r->blocks.empty()) {
-      r->nf = (int)r->blocks[0].frames.size();
+      r->nf = r->blocks[0].nframes;
       r->fb = r->blocks[0].frame_bytes;
       r->block_size = r->blocks[0].size;
-      std::vector<int64_t> fr;
-      fr.reserve(r->blocks.size() * (size_t)r->nf);
-      for (const FrameBlock &b : r->blocks) {
-        if ((int)b.frames.size() != r->nf || b.size != r->block_size) throw Error(SFXC_GPU_ESTATE, "uneven reader blocks");
-        fr.insert(fr.end(), b.frames.begin(), b.frames.end());
-      }
-      upload(r->frames, fr.data(), fr.size() * sizeof(int64_t), c->st);
+      for (size_t b = 0; b < r->blocks.size(); b++)
+        if (r->blocks[b].nframes != r->nf || r->blocks[b].size != r->block_size ||
+            r->blocks[b].first != (int64_t)b * r->nf)
+          throw Error(SFXC_GPU_ESTATE, "uneven reader blocks");
+      upload(B.frames, walk.frames.data(), walk.frames.size() * sizeof(int64_t), c->st);
       if (r->p.format == FORMAT_MARK5B) {  // fill-pattern runs of every block: count, then write
         const int nb = (int)r->blocks.size();
-        DevBuf counts, offs, runs;
+        DevBuf &counts = B.counts, &offs = B.offs, &runs = B.runs;
         counts.ensure((size_t)nb * 4);
-        launch_fill_runs(r->rec, r->frames.as<int64_t>(), r->nf, r->fb / 4, r->block_size / 4, nb,
+        launch_fill_runs(r->rec, B.frames.as<int64_t>(), r->nf, r->fb / 4, r->block_size / 4, nb,
                          counts.as<int32_t>(), nullptr, nullptr, c->st);
         CK(cudaGetLastError());
         std::vector<int32_t> cnt(nb);
@@ -2277,7 +2312,7 @@ sfxc_gpu_recording *sfxc_gpu_recording_create(sfxc_gpu_ctx *c, const sfxc_reader
         if (off[nb]) {
           upload(offs, off.data(), (size_t)nb * 8, c->st);
           runs.ensure((size_t)off[nb] * 8);
-          launch_fill_runs(r->rec, r->frames.as<int64_t>(), r->nf, r->fb / 4, r->block_size / 4, nb, nullptr,
+          launch_fill_runs(r->rec, B.frames.as<int64_t>(), r->nf, r->fb / 4, r->block_size / 4, nb, nullptr,
                            offs.as<int64_t>(), runs.as<int32_t>(), c->st);
           CK(cudaGetLastError());
           std::vector<int32_t> all((size_t)off[nb] * 2);
@@ -2299,6 +2334,8 @@ sfxc_gpu_recording *sfxc_gpu_recording_create(sfxc_gpu_ctx *c, const sfxc_reader
 void sfxc_gpu_recording_destroy(sfxc_gpu_recording *r) {
   if (!r) return;
   cudaSetDevice(r->ctx->device);
+  cudaStreamSynchronize(r->ctx->st);
+  r->ctx->rec_spare.push_back(std::move(r->buf));  // its buffers serve the context's next recording
   delete r;
 }
 
@@ -2318,12 +2355,13 @@ int sfxc_gpu_recording_block(sfxc_gpu_recording *r, int32_t i, sfxc_reader_block
     out->invalid = b.invalid.data();
     if (data) {  // the block's bytes, assembled from its frames on the device
       CK(cudaSetDevice(c->device));
-      upload(r->list, &i, 4, c->st);
-      r->gathered.ensure((size_t)b.size);
-      launch_gather_blocks(r->rec, r->frames.as<int64_t>(), r->nf, r->fb, r->block_size, r->list.as<int32_t>(), 1,
-                           r->gathered.as<uint8_t>(), c->st);
+      RecordingBuffers &B = *r->buf;
+      upload(B.list, &i, 4, c->st);
+      B.gathered.ensure((size_t)b.size);
+      launch_gather_blocks(r->rec, B.frames.as<int64_t>(), r->nf, r->fb, r->block_size, B.list.as<int32_t>(), 1,
+                           B.gathered.as<uint8_t>(), c->st);
       CK(cudaGetLastError());
-      CK(cudaMemcpyAsync(data, r->gathered.p, (size_t)b.size, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(data, B.gathered.p, (size_t)b.size, cudaMemcpyDeviceToHost, c->st));
       CK(cudaStreamSynchronize(c->st));
     }
     return SFXC_GPU_OK;
@@ -2339,10 +2377,14 @@ int sfxc_gpu_recording_extract(sfxc_gpu_recording *r, int32_t word_bytes, int32_
   try {
     CK(cudaSetDevice(c->device));
     const int nb = (int)r->blocks.size();
-    r->chan_blocks.clear();
-    r->chan_runs.clear();
+    RecordingBuffers &B = *r->buf;
+    r->chan_set.clear();
+    r->set_blocks.clear();
+    r->set_runs.clear();
     r->chan_off.clear();
     r->proto.clear();
+    r->last_plan.reset();
+    r->per_thread = word_bytes == 0;
     if (word_bytes == 0) {
       // one channel per VDIF thread (Channel_extractor_tasklet_VDIF::do_task,
       // sfxc/src/channel_extractor_tasklet_vdif.cc:25-49): each block is its
@@ -2355,22 +2397,23 @@ int sfxc_gpu_recording_extract(sfxc_gpu_recording *r, int32_t word_bytes, int32_
         if (ch < 0 || ch >= nch) throw Error(SFXC_GPU_EINVAL, "block of a channel outside the channel list");
         lists[ch].push_back(b);
       }
-      r->chan_blocks.resize(nch);
-      r->chan_runs.resize(nch);
+      r->set_blocks.resize(nch);
+      r->set_runs.resize(nch);
+      for (int ch = 0; ch < nch; ch++) r->chan_set.push_back(ch);
       int64_t total = 0;
       for (int ch = 0; ch < nch; ch++) {
         r->chan_off.push_back(total);
         total += (int64_t)lists[ch].size() * r->block_size;
       }
-      r->chan.ensure((size_t)total + 16);
+      B.chan.ensure((size_t)total + 16);
       std::vector<int32_t> all;
       for (auto &l : lists) all.insert(all.end(), l.begin(), l.end());
-      upload(r->list, all.data(), all.size() * 4, c->st);
+      upload(B.list, all.data(), all.size() * 4, c->st);
       int64_t e0 = 0;
       for (int ch = 0; ch < nch; ch++) {
-        launch_gather_blocks(r->rec, r->frames.as<int64_t>(), r->nf, r->fb, r->block_size,
-                             r->list.as<int32_t>() + e0, (int)lists[ch].size(),
-                             r->chan.as<uint8_t>() + r->chan_off[ch], c->st);
+        launch_gather_blocks(r->rec, B.frames.as<int64_t>(), r->nf, r->fb, r->block_size,
+                             B.list.as<int32_t>() + e0, (int)lists[ch].size(),
+                             B.chan.as<uint8_t>() + r->chan_off[ch], c->st);
         CK(cudaGetLastError());
         e0 += (int64_t)lists[ch].size();
         for (size_t j = 0; j < lists[ch].size(); j++) {
@@ -2380,8 +2423,8 @@ int sfxc_gpu_recording_extract(sfxc_gpu_recording *r, int32_t word_bytes, int32_
           cb.src_offset = (int64_t)j * r->block_size;
           cb.size = r->block_size;
           for (size_t k = 0; k + 1 < b.invalid.size(); k += 2) cb.invalid.push_back(InvalidRun{b.invalid[k], b.invalid[k + 1]});
-          r->chan_blocks[ch].push_back(cb);
-          r->chan_runs[ch].push_back(b.invalid);
+          r->set_blocks[ch].push_back(cb);
+          r->set_runs[ch].push_back(b.invalid);
         }
       }
     } else {
@@ -2393,34 +2436,55 @@ int sfxc_gpu_recording_extract(sfxc_gpu_recording *r, int32_t word_bytes, int32_
       for (int i = 0; i < n_subbands * fan_out; i++)
         if (tracks[i] < 0 || tracks[i] >= word_bytes * 8) throw Error(SFXC_GPU_EINVAL, "track outside the word");
       const int per_byte = 8 / fan_out * word_bytes;  // input bytes per output byte
-      if (nb && (r->fb % per_byte || r->block_size % per_byte))
-        throw Error(SFXC_GPU_EINVAL, "frame payload is not a whole number of output bytes");
+      if (nb && (r->fb % word_bytes || r->block_size % per_byte))
+        throw Error(SFXC_GPU_EINVAL, "frames are not whole words, or blocks not whole output bytes");
       const int64_t opb = nb ? r->block_size / per_byte : 0;
       const int64_t nout = (int64_t)nb * opb;
-      upload(r->tracks, tracks, (size_t)n_subbands * fan_out * 4, c->st);
-      r->chan.ensure((size_t)(nout * n_subbands) + 16);
-      launch_extract_frames(r->rec, r->frames.as<int64_t>(), r->nf, r->fb, opb, nout, word_bytes, bits, n_subbands,
-                            fan_out, r->tracks.as<int>(), r->chan.as<uint8_t>(), c->st);
+      B.chan.ensure((size_t)(nout * n_subbands) + 16);
+      // each subband's tracks one bit field, as the extractor orders them
+      // (2-bit samples: track pairs swapped)?  Then its lowest bit is enough.
+      std::vector<int32_t> bases(n_subbands);
+      bool fields = true;
+      for (int sb = 0; sb < n_subbands && fields; sb++) {
+        const int32_t *tr = tracks + sb * fan_out;
+        bases[sb] = tr[bits == 2 ? 1 : 0];
+        for (int q = 0; q < fan_out; q++)
+          if (tr[bits == 2 ? (q ^ 1) : q] != bases[sb] + q) fields = false;
+      }
+      if (fields) {
+        upload(B.tracks, bases.data(), bases.size() * 4, c->st);
+        fields = launch_extract_fields(r->rec, B.frames.as<int64_t>(), r->nf, r->fb, opb, nout, word_bytes, fan_out,
+                                       n_subbands, B.tracks.as<int>(), B.chan.as<uint8_t>(), c->st);
+      }
+      if (!fields) upload(B.tracks, tracks, (size_t)n_subbands * fan_out * 4, c->st);
+      if (!fields && !launch_extract_frames(r->rec, B.frames.as<int64_t>(), r->nf, r->fb, opb, nout, word_bytes, bits,
+                                 n_subbands, fan_out, B.tracks.as<int>(), B.chan.as<uint8_t>(), c->st))
+        throw Error(SFXC_GPU_EINVAL, "more than 1024 tracks in all, or words over 8 bytes across frames");
       CK(cudaGetLastError());
-      r->chan_blocks.resize(n_subbands);
-      r->chan_runs.resize(n_subbands);
+      // every subband: the same blocks at the same offsets in its own bytes
+      r->set_blocks.resize(1);
+      r->set_runs.resize(1);
+      r->set_blocks[0].reserve(nb);
+      r->set_runs[0].reserve(nb);
+      for (int b = 0; b < nb; b++) {
+        ChannelBlock cb;
+        cb.start = r->blocks[b].start_ticks;
+        cb.src_offset = (int64_t)b * opb;
+        cb.size = (int32_t)opb;
+        // invalid byte runs in bytes of each subband (channel_extractor_tasklet.cc:181-194)
+        std::vector<int32_t> runs;
+        for (int32_t v : r->blocks[b].invalid) runs.push_back(v * fan_out / (8 * word_bytes));
+        for (size_t k = 0; k + 1 < runs.size(); k += 2) cb.invalid.push_back(InvalidRun{runs[k], runs[k + 1]});
+        r->set_blocks[0].push_back(std::move(cb));
+        r->set_runs[0].push_back(std::move(runs));
+      }
       for (int sb = 0; sb < n_subbands; sb++) {
         r->chan_off.push_back((int64_t)sb * nout);
-        for (int b = 0; b < nb; b++) {
-          ChannelBlock cb;
-          cb.start = r->blocks[b].start_ticks;
-          cb.src_offset = (int64_t)b * opb;
-          cb.size = (int32_t)opb;
-          // invalid byte runs in bytes of each subband (channel_extractor_tasklet.cc:181-194)
-          std::vector<int32_t> runs;
-          for (int32_t v : r->blocks[b].invalid) runs.push_back(v * fan_out / (8 * word_bytes));
-          for (size_t k = 0; k + 1 < runs.size(); k += 2) cb.invalid.push_back(InvalidRun{runs[k], runs[k + 1]});
-          r->chan_blocks[sb].push_back(cb);
-          r->chan_runs[sb].push_back(runs);
-        }
+        r->chan_set.push_back(0);
       }
     }
-    r->proto.resize(r->chan_blocks.size());
+    r->proto.assign(r->n_channels(), nullptr);
+    if ((int)B.proto.size() < r->n_channels()) B.proto.resize(r->n_channels());
     CK(cudaStreamSynchronize(c->st));
     return SFXC_GPU_OK;
   } catch (const Error &e) {
@@ -2433,23 +2497,24 @@ int32_t sfxc_gpu_recording_channel(sfxc_gpu_recording *r, int32_t channel, int32
   if (!r) return SFXC_GPU_EINVAL;
   sfxc_gpu_ctx *c = r->ctx;
   try {
-    if (channel < 0 || channel >= (int32_t)r->chan_blocks.size()) throw Error(SFXC_GPU_EINVAL, "bad channel");
-    const auto &cb = r->chan_blocks[channel];
+    if (channel < 0 || channel >= r->n_channels()) throw Error(SFXC_GPU_EINVAL, "bad channel");
+    const auto &cb = r->blocks_of(channel);
+    const auto &runs = r->set_runs[r->chan_set[channel]];
     const int nb = (int)cb.size();
     if (blocks) {
       if (capacity < nb) throw Error(SFXC_GPU_EINVAL, "block array too small");
       for (int b = 0; b < nb; b++) {
         blocks[b].start_ticks = cb[b].start;
         blocks[b].size = cb[b].size;
-        blocks[b].n_invalid = (int32_t)(r->chan_runs[channel][b].size() / 2);
-        blocks[b].invalid = r->chan_runs[channel][b].data();
+        blocks[b].n_invalid = (int32_t)(runs[b].size() / 2);
+        blocks[b].invalid = runs[b].data();
       }
     }
     if (data && nb) {
       CK(cudaSetDevice(c->device));
       const int64_t bytes = cb.back().src_offset + cb.back().size;
-      CK(cudaMemcpyAsync(data, r->chan.as<uint8_t>() + r->chan_off[channel], (size_t)bytes, cudaMemcpyDeviceToHost,
-                         c->st));
+      CK(cudaMemcpyAsync(data, r->buf->chan.as<uint8_t>() + r->chan_off[channel], (size_t)bytes,
+                         cudaMemcpyDeviceToHost, c->st));
       CK(cudaStreamSynchronize(c->st));
     }
     return nb;
@@ -2465,50 +2530,67 @@ int64_t sfxc_gpu_recording_protocol(sfxc_gpu_recording *r, int32_t channel, int3
   if (!r) return SFXC_GPU_EINVAL;
   sfxc_gpu_ctx *c = r->ctx;
   try {
-    if (channel < 0 || channel >= (int32_t)r->chan_blocks.size()) throw Error(SFXC_GPU_EINVAL, "bad channel");
+    if (channel < 0 || channel >= r->n_channels()) throw Error(SFXC_GPU_EINVAL, "bad channel");
     if (!slices || n_slices < 0) throw Error(SFXC_GPU_EINVAL, "bad slices");
     CK(cudaSetDevice(c->device));
-    std::vector<SliceRequest> sl(n_slices);
+    std::vector<int64_t> key{sample_rate, bits, integration_time_us, n_slices};
     for (int i = 0; i < n_slices; i++) {
-      sl[i].start = slices[i].start_ticks;
-      sl[i].stop = slices[i].stop_ticks;
-      sl[i].nr_samples = slices[i].nr_samples;
+      key.insert(key.end(), {slices[i].start_ticks, slices[i].stop_ticks, slices[i].nr_samples, slices[i].n_delays});
       for (int k = 0; k < slices[i].n_delays; k++)
-        sl[i].delays.push_back(Delay{slices[i].delay_ticks[k], slices[i].delay_bytes[k], slices[i].delay_remaining[k]});
-      if (sl[i].delays.empty()) throw Error(SFXC_GPU_EINVAL, "slice without delays");
+        key.insert(key.end(), {slices[i].delay_ticks[k], slices[i].delay_bytes[k], slices[i].delay_remaining[k]});
     }
-    // the writer's records (Input_node_data_writer::do_task), then their bytes
-    auto recs = write_protocol(r->chan_blocks[channel], sl, sample_rate, bits, (double)integration_time_us);
-    sfxc_gpu_recording::Protocol &pr = r->proto[channel];
-    pr.offsets.assign(1, 0);
-    pr.slice_recs.assign(n_slices, {});
-    std::vector<ProtoRecord> dev;
-    int64_t total = 0;
-    for (int i = 0; i < n_slices; i++) {
-      const int64_t s0 = total;
-      for (const Record &q : recs[i]) {
-        ProtoRecord d{q.src, total, q.n, q.type, q.rem, 0};
-        dev.push_back(d);
-        Record rel = q;
-        if (q.type == HEADER_DATA) rel.src = total - s0 + 3;
-        pr.slice_recs[i].push_back(rel);
-        total += q.type == HEADER_ENDSTREAM ? 1 : q.type == HEADER_DELAY ? 2 : q.type == HEADER_DATA ? 3 + q.n : 3;
+    // every subband of an extracted recording has the same blocks and
+    // invalid runs: the records of one serve them all
+    const int group = r->per_thread ? channel : -1;
+    std::shared_ptr<ProtoPlan> plan = r->last_plan;
+    if (!plan || plan->group != group || plan->key != key) {
+      std::vector<SliceRequest> sl(n_slices);
+      for (int i = 0; i < n_slices; i++) {
+        sl[i].start = slices[i].start_ticks;
+        sl[i].stop = slices[i].stop_ticks;
+        sl[i].nr_samples = slices[i].nr_samples;
+        for (int k = 0; k < slices[i].n_delays; k++)
+          sl[i].delays.push_back(
+              Delay{slices[i].delay_ticks[k], slices[i].delay_bytes[k], slices[i].delay_remaining[k]});
+        if (sl[i].delays.empty()) throw Error(SFXC_GPU_EINVAL, "slice without delays");
       }
-      pr.offsets.push_back(total);
+      // the writer's records (Input_node_data_writer::do_task), then where their bytes go
+      auto recs = write_protocol(r->blocks_of(channel), sl, sample_rate, bits, (double)integration_time_us);
+      plan = std::make_shared<ProtoPlan>();
+      plan->key = key;
+      plan->group = group;
+      plan->offsets.assign(1, 0);
+      plan->slice_recs.assign(n_slices, {});
+      int64_t total = 0;
+      for (int i = 0; i < n_slices; i++) {
+        const int64_t s0 = total;
+        for (const Record &q : recs[i]) {
+          plan->dev_recs.push_back(ProtoRecord{q.src, total, q.n, q.type, q.rem, 0});
+          Record rel = q;
+          if (q.type == HEADER_DATA) rel.src = total - s0 + 3;
+          plan->slice_recs[i].push_back(rel);
+          total += q.type == HEADER_ENDSTREAM ? 1 : q.type == HEADER_DELAY ? 2 : q.type == HEADER_DATA ? 3 + q.n : 3;
+        }
+        plan->offsets.push_back(total);
+      }
+      plan->total = total;
+      upload(r->buf->plan_recs[group], plan->dev_recs.data(), plan->dev_recs.size() * sizeof(ProtoRecord), c->st);
+      r->last_plan = plan;
     }
     if (out_offsets)
-      for (int i = 0; i <= n_slices; i++) out_offsets[i] = pr.offsets[i];
-    upload(pr.recs, dev.data(), dev.size() * sizeof(ProtoRecord), c->st);
-    pr.bytes.ensure((size_t)total + 16);
-    launch_serialize_protocol(pr.recs.as<ProtoRecord>(), (int)dev.size(), r->chan.as<uint8_t>() + r->chan_off[channel],
-                              pr.bytes.as<uint8_t>(), c->st);
+      for (int i = 0; i <= n_slices; i++) out_offsets[i] = plan->offsets[i];
+    DevBuf &bytes = r->buf->proto[channel];
+    bytes.ensure((size_t)plan->total + 16);
+    launch_serialize_protocol(r->buf->plan_recs[group].as<ProtoRecord>(), (int)plan->dev_recs.size(),
+                              r->buf->chan.as<uint8_t>() + r->chan_off[channel], bytes.as<uint8_t>(), c->st);
     CK(cudaGetLastError());
+    r->proto[channel] = plan;
     if (out) {
-      if (total > capacity) throw Error(SFXC_GPU_EINVAL, "output buffer too small");
-      CK(cudaMemcpyAsync(out, pr.bytes.p, (size_t)total, cudaMemcpyDeviceToHost, c->st));
+      if (plan->total > capacity) throw Error(SFXC_GPU_EINVAL, "output buffer too small");
+      CK(cudaMemcpyAsync(out, bytes.p, (size_t)plan->total, cudaMemcpyDeviceToHost, c->st));
     }
     CK(cudaStreamSynchronize(c->st));
-    return total;
+    return plan->total;
   } catch (const Error &e) {
     return fail(c, e);
   }
@@ -2520,18 +2602,19 @@ int sfxc_gpu_recording_push(sfxc_gpu_recording *r, int32_t channel, int32_t slic
   if (stream < 0 || stream >= (int)c->sc.size()) return fail(c, Error(SFXC_GPU_EINVAL, "bad stream index"));
   try {
     if (c->device != r->ctx->device) throw Error(SFXC_GPU_EINVAL, "recording and correlator on different devices");
-    if (channel < 0 || channel >= (int32_t)r->proto.size() || slice < 0 ||
-        slice + 1 >= (int32_t)r->proto[channel].offsets.size())
+    if (channel < 0 || channel >= (int32_t)r->proto.size() || !r->proto[channel] || slice < 0 ||
+        slice + 1 >= (int32_t)r->proto[channel]->offsets.size())
       throw Error(SFXC_GPU_EINVAL, "no protocol for that channel and slice");
     CK(cudaSetDevice(c->device));
-    const sfxc_gpu_recording::Protocol &pr = r->proto[channel];
+    const ProtoPlan &pr = *r->proto[channel];
+    const uint8_t *pbytes = r->buf->proto[channel].as<uint8_t>();
     const int64_t b0 = pr.offsets[slice], n = pr.offsets[slice + 1] - b0;
     StreamCtx &s = c->sc[stream];
     grow_stream_input(c, s, (size_t)n);
     // the protocol is complete on the recording's stream (its calls return
     // after it); the copy runs on the correlator's
-    if (n) CK(cudaMemcpyAsync(s.src.as<uint8_t>() + s.dev_bytes, pr.bytes.as<uint8_t>() + b0, (size_t)n,
-                              cudaMemcpyDeviceToDevice, c->st));
+    if (n) CK(cudaMemcpyAsync(s.src.as<uint8_t>() + s.dev_bytes, pbytes + b0, (size_t)n, cudaMemcpyDeviceToDevice,
+                              c->st));
     for (Record q : pr.slice_recs[slice]) {
       if (q.type == HEADER_DATA) q.src += s.dev_bytes;
       s.pending.push_back(q);

@@ -373,7 +373,7 @@ int mjd_of_date(int day, int month, int year) { return mjd_from_date(day, month,
 // (q + header size <= size, else end of data), a payload read likewise.
 namespace {
 
-std::vector<FrameBlock> walk_vdif(const ReaderParams &p, FrameSource &src) {
+FrameWalk walk_vdif(const ReaderParams &p, FrameSource &src) {
   if (p.frame_size <= 0) throw std::invalid_argument("VDIF frame size must be positive");
   const int64_t n = src.size();
   const int fs = p.frame_size;
@@ -385,7 +385,7 @@ std::vector<FrameBlock> walk_vdif(const ReaderParams &p, FrameSource &src) {
     for (size_t i = 0; i < p.first_track.size(); i++) thread_map[p.first_track[i]] = (int)i;
     fpb = 1;
   }
-  std::vector<FrameBlock> out;
+  FrameWalk out;
   // before the first header: 16-byte candidates, a fill header skips a
   // non-legacy frame (vdif_reader.cc:84-100)
   const int64_t cstride = (int64_t)fs + 32;
@@ -424,8 +424,12 @@ std::vector<FrameBlock> walk_vdif(const ReaderParams &p, FrameSource &src) {
   bool have = true;  // the first header has been read
   for (;;) {         // read_new_block (vdif_reader.cc:77-190)
     FrameBlock b;
+    b.first = (int64_t)out.frames.size();
     for (;;) {
-      if (!have && !header_in(j)) return out;
+      if (!have && !header_in(j)) {
+        out.frames.resize((size_t)b.first);
+        return out;
+      }
       have = false;
       const FrameInfo &h = hdr[(size_t)j];
       const int64_t pos = p0 + j * stride;
@@ -452,13 +456,15 @@ std::vector<FrameBlock> walk_vdif(const ReaderParams &p, FrameSource &src) {
         }
         b.channel = thread_map[h.thread];
       }
-      b.frames.push_back(pos + hs);
+      out.frames.push_back(pos + hs);
       j++;
       for (int i = 1; i < fpb; i++, j++) {
-        if (!header_in(j)) return out;
         const int64_t q = p0 + j * stride;
-        if (q + hs + fs > n) return out;
-        b.frames.push_back(q + hs);
+        if (!header_in(j) || q + hs + fs > n) {
+          out.frames.resize((size_t)b.first);
+          return out;
+        }
+        out.frames.push_back(q + hs);
         if (hdr[(size_t)j].flags & FRAME_INVALID) {
           b.invalid.push_back(i * fs);
           b.invalid.push_back(fs);
@@ -467,7 +473,8 @@ std::vector<FrameBlock> walk_vdif(const ReaderParams &p, FrameSource &src) {
       b.start_ticks = time_of(h);
       b.size = block_size;
       b.frame_bytes = fs;
-      out.push_back(std::move(b));
+      b.nframes = fpb;
+      out.blocks.push_back(std::move(b));
       restarts = 0;
       break;
     }
@@ -492,7 +499,7 @@ struct FetchedBytes {
   }
 };
 
-std::vector<FrameBlock> walk_mk5b(const ReaderParams &p, FrameSource &src) {
+FrameWalk walk_mk5b(const ReaderParams &p, FrameSource &src) {
   const int64_t n = src.size();
   int current_jday = (int)mjd_of_ticks(p.ref_ticks);
   const int bitstreams = p.n_tracks;
@@ -506,14 +513,14 @@ std::vector<FrameBlock> walk_mk5b(const ReaderParams &p, FrameSource &src) {
   FrameInfo cur = decode_mk5b(zero), prev = cur;
   int frame_nr = -1;
   bool frame_nr_valid = true;
-  std::vector<FrameBlock> out;
+  FrameWalk out;
   auto frame_nr_update = [&]() {  // mark5b_reader.cc:127-131
     if (bitstreams == 64 && cur.seconds == prev.seconds && frame_nr > (int)cur.frame_nr)
       frame_nr = (int)cur.frame_nr + 32768;
     else
       frame_nr = (int)cur.frame_nr;
   };
-  auto finish = [&](std::vector<int64_t> &&frames) {  // jday, then get_current_time (mark5b_reader.cc:84-105)
+  auto finish = [&](const int64_t *frames) {  // jday, then get_current_time (mark5b_reader.cc:84-105)
     if (cur.thread != current_jday % 1000) current_jday++;
     const double rate = (double)sample_rate * bitstreams;
     const double subsec = (double)((uint64_t)(int64_t)frame_nr * (8 * kMk5bFrame)) / rate;
@@ -531,8 +538,10 @@ std::vector<FrameBlock> walk_mk5b(const ReaderParams &p, FrameSource &src) {
     b.start_ticks = t - p.offset_ticks;
     b.size = kMk5bBlock;
     b.frame_bytes = kMk5bFrame;
-    b.frames = std::move(frames);
-    out.push_back(std::move(b));
+    b.first = (int64_t)out.frames.size();
+    b.nframes = kMk5bBlockFrames;
+    out.frames.insert(out.frames.end(), frames, frames + kMk5bBlockFrames);
+    out.blocks.push_back(std::move(b));
   };
   // block-start headers on the grid g0 + k * bstride
   int64_t g0 = -1;
@@ -551,10 +560,10 @@ std::vector<FrameBlock> walk_mk5b(const ReaderParams &p, FrameSource &src) {
       cur = h;
       frame_nr_update();
       if (P + bstride > n) return out;
-      std::vector<int64_t> frames;
-      for (int i = 0; i < kMk5bBlockFrames; i++) frames.push_back(P + i * fstride + kMk5bHeader);
+      int64_t frames[kMk5bBlockFrames];
+      for (int i = 0; i < kMk5bBlockFrames; i++) frames[i] = P + i * fstride + kMk5bHeader;
       P += bstride;
-      finish(std::move(frames));
+      finish(frames);
       continue;
     }
     // resync_header (mark5b_reader.cc:254-327) on the bytes that follow the
@@ -598,16 +607,16 @@ std::vector<FrameBlock> walk_mk5b(const ReaderParams &p, FrameSource &src) {
       if ((t.flags & FRAME_CHECK) && t.frame_nr % kMk5bBlockFrames == 0) {
         prev = cur;
         cur = t;
-        std::vector<int64_t> frames{frame0};
+        int64_t frames[kMk5bBlockFrames] = {frame0};
         for (int i = 1; i < kMk5bBlockFrames; i++) {
           r.get(kMk5bHeader, nullptr);
-          frames.push_back(r.pos);
+          frames[i] = r.pos;
           r.get(kMk5bFrame, nullptr);
         }
         if (r.short_read) break;
         frame_nr_update();
         P = r.pos;
-        finish(std::move(frames));
+        finish(frames);
         resynced = true;
         break;
       }
@@ -618,7 +627,7 @@ std::vector<FrameBlock> walk_mk5b(const ReaderParams &p, FrameSource &src) {
 
 }  // namespace
 
-std::vector<FrameBlock> walk_frames(const ReaderParams &p, FrameSource &src) {
+FrameWalk walk_frames(const ReaderParams &p, FrameSource &src) {
   if (p.bits_per_sample != 1 && p.bits_per_sample != 2) throw std::invalid_argument("bits per sample must be 1 or 2");
   if (p.tracks_per_channel < p.bits_per_sample) throw std::invalid_argument("fewer tracks than bits per sample");
   if (p.track_bit_rate <= 0) throw std::invalid_argument("track bit rate must be positive");

@@ -65,23 +65,29 @@ class FrameSource {
   virtual void fetch(int64_t pos, int64_t len, uint8_t *dst) = 0;
 };
 
-// One reader block: the reader's data bytes are the frames' payloads,
-// frame_bytes each at block offsets 0, frame_bytes, ..., then zeros up to
-// size.  invalid: the VDIF invalid-frame runs; Mark5B blocks take their
-// fill-pattern runs (fill_pattern_runs over the block bytes) afterwards.
+// One reader block: the reader's data bytes are the payloads of its
+// nframes frames, frame_bytes each at block offsets 0, frame_bytes, ...,
+// then zeros up to size.  invalid: the VDIF invalid-frame runs; Mark5B
+// blocks take their fill-pattern runs (fill_pattern_runs over the block
+// bytes) afterwards.
 struct FrameBlock {
   int channel = -1;
   int64_t start_ticks = 0;
   int32_t size = 0;
   int32_t frame_bytes = 0;
-  std::vector<int64_t> frames;
+  int64_t first = 0;  // index of its first frame in FrameWalk::frames
+  int32_t nframes = 0;
   std::vector<int32_t> invalid;
+};
+struct FrameWalk {
+  std::vector<FrameBlock> blocks;
+  std::vector<int64_t> frames;  // payload offsets in the recording, block after block
 };
 
 // Every block FormatReader::create(p, ...)->next() returns for the
 // recording, in order.  One difference: where a truncated Mark5B recording
 // ends inside a resync, the reader may still return one block whose bytes
 // are partly left over from the previous block; the walk ends before it.
-std::vector<FrameBlock> walk_frames(const ReaderParams &p, FrameSource &src);
+FrameWalk walk_frames(const ReaderParams &p, FrameSource &src);
 
 }  // namespace sfxc

@@ -121,9 +121,17 @@ void launch_fill_runs(const uint8_t *rec, const int64_t *frames, int nf, int wpf
                       int32_t *counts, const int64_t *offsets, int32_t *runs, cudaStream_t st);
 void launch_gather_blocks(const uint8_t *rec, const int64_t *frames, int nf, int fb, int block_size,
                           const int32_t *list, int nlist, uint8_t *out, cudaStream_t st);
-void launch_extract_frames(const uint8_t *rec, const int64_t *frames, int nf, int fb, int64_t opb, int64_t nout,
+// false: more than 1024 tracks in all for words of up to 8 bytes, or words
+// over 8 bytes in frames that are not a whole number of output bytes (the
+// caller checked fan_out, bits and that frames are whole words)
+bool launch_extract_frames(const uint8_t *rec, const int64_t *frames, int nf, int fb, int64_t opb, int64_t nout,
                            int N, int bits, int nsub, int fan_out, const int *tracks, uint8_t *out,
                            cudaStream_t st);
+// subbands whose tracks are bit fields (bases[s] = the field's lowest bit);
+// false for words over 8 bytes, more than 1024 subbands or frames that are
+// not a whole number of output bytes: use launch_extract_frames
+bool launch_extract_fields(const uint8_t *rec, const int64_t *frames, int nf, int fb, int64_t opb, int64_t nout,
+                           int N, int fan_out, int nsub, const int *bases, uint8_t *out, cudaStream_t st);
 void launch_serialize_protocol(const ProtoRecord *recs, int nrec, const uint8_t *stream, uint8_t *out,
                                cudaStream_t st);
 

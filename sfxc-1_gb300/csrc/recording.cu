@@ -83,13 +83,133 @@ __global__ void gather_blocks_kernel(const uint8_t *__restrict__ rec, const int6
   }
 }
 
-// Channel extraction of every block at once: output byte ob of subband
-// blockIdx.y is byte r = ob % opb of block ob / opb, made from the spb words
-// at block byte r * spb * N, which lie in one frame (fb is a multiple of
-// spb * N) or past the frames (zero words).
-__global__ void extract_frames_kernel(const uint8_t *__restrict__ rec, const int64_t *__restrict__ frames, int nf,
-                                      int fb, int64_t opb, int64_t nout, int N, int bits, int fan_out,
-                                      const int *__restrict__ tracks, uint8_t *__restrict__ out) {
+// Channel extraction of every block at once: thread ob takes output byte r
+// = ob % opb of block ob / opb in every subband, from the SPB = 8 / fan_out
+// words at block byte r * SPB * N (read once, held as 64-bit values), each
+// in its frame (fb is a multiple of N) or past the frames (zero words).  Bit placement as extract_byte: track t of a sample lands at
+// low_bit << ((t + 1) % BITS), low_bit starting at 1 << (8 - fan_out) and
+// advancing by BITS per complete sample; earlier samples sit lower.
+constexpr int kMaxExtractTracks = 1024;
+template <int SPB, int BITS>
+__global__ void __launch_bounds__(256) extract_frames_kernel(const uint8_t *__restrict__ rec,
+                                                             const int64_t *__restrict__ frames, int nf, int fb,
+                                                             int64_t opb, int64_t nout, int N, int nsub,
+                                                             const int *__restrict__ tracks,
+                                                             uint8_t *__restrict__ out) {
+  constexpr int FAN = 8 / SPB;
+  __shared__ int str[kMaxExtractTracks];
+  for (int i = threadIdx.x; i < nsub * FAN; i += blockDim.x) str[i] = tracks[i];
+  __syncthreads();
+  const int64_t ob = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ob >= nout) return;
+  const int64_t b = ob / opb;
+  const int64_t byte = (ob - b * opb) * SPB * N;
+  const int64_t f = byte / fb, f_last = (byte + (SPB - 1) * N) / fb;
+  uint64_t w[SPB];
+#pragma unroll
+  for (int j = 0; j < SPB; j++) w[j] = 0;
+  const uint8_t *p = f < nf ? rec + frames[b * nf + f] + (byte - f * fb) : nullptr;
+  if (SPB == 4 && N == 4 && f == f_last && f < nf && ((uintptr_t)p & 15) == 0) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
+    w[0] = v.x;
+    w[1 % SPB] = v.y;
+    w[2 % SPB] = v.z;
+    w[3 % SPB] = v.w;
+  } else {
+    // word by word: the SPB words of an output byte may span two frames
+#pragma unroll
+    for (int j = 0; j < SPB; j++) {
+      const int64_t wb = byte + j * N, fj = wb / fb;
+      if (fj < nf) {
+        const uint8_t *q = rec + frames[b * nf + fj] + (wb - fj * fb);
+        for (int i = 0; i < N; i++) w[j] |= (uint64_t)q[i] << (8 * i);
+      }
+    }
+  }
+  for (int sb = 0; sb < nsub; sb++) {
+    int tr[FAN];
+#pragma unroll
+    for (int t = 0; t < FAN; t++) tr[t] = str[sb * FAN + t];
+    unsigned out_byte = 0;
+#pragma unroll
+    for (int j = 0; j < SPB; j++) {
+      unsigned v = 0, low_bit = 1u << (8 - FAN);
+#pragma unroll
+      for (int t = 0; t < FAN; t++) {
+        v |= (unsigned)((w[j] >> tr[t]) & 1u) * (low_bit << ((t + 1) % BITS));
+        if ((t + 1) % BITS == 0) low_bit <<= BITS;
+      }
+      out_byte |= (v >> ((SPB - 1 - j) * FAN)) & 0xffu;
+    }
+    out[(int64_t)sb * nout + ob] = (uint8_t)out_byte;
+  }
+}
+
+// The usual track layouts: every subband's tracks are one bit field of the
+// word, in the order the extractor places them (bits b0 .. b0 + fan_out - 1
+// of sample j land on output bits j * fan_out .. ; for 2-bit samples the
+// extractor swaps each track pair, so tracks {b0 + 1, b0} are the field).
+// Then output byte = OR_j ((word_j >> b0) & mask) << (j * fan_out).  Each
+// thread makes G consecutive output bytes of every subband from G * SPB
+// words (G = 4: 64 bytes for 32-bit words and 2-bit pairs, stored as one
+// 32-bit word per subband; G = 1 where a frame is not a multiple of four
+// output bytes).  T: the word type (uint32_t for words of up to 4 bytes).
+template <int SPB, class T, int G>
+__global__ void __launch_bounds__(256) extract_fields_kernel(const uint8_t *__restrict__ rec,
+                                                             const int64_t *__restrict__ frames, int nf, int fb,
+                                                             int64_t opb, int64_t nout, int N, int nsub,
+                                                             const int *__restrict__ bases,
+                                                             uint8_t *__restrict__ out) {
+  constexpr int FAN = 8 / SPB;
+  constexpr unsigned MASK = (1u << FAN) - 1u;
+  constexpr int NW = G * SPB;
+  __shared__ int sb0[kMaxExtractTracks];
+  for (int i = threadIdx.x; i < nsub; i += blockDim.x) sb0[i] = bases[i];
+  __syncthreads();
+  const int64_t ob = G * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  if (ob >= nout) return;
+  const int64_t b = ob / opb;
+  const int64_t byte = (ob - b * opb) * SPB * N;
+  const int64_t f = byte / fb;
+  T w[NW];
+#pragma unroll
+  for (int j = 0; j < NW; j++) w[j] = 0;
+  if (f < nf) {
+    const uint8_t *p = rec + frames[b * nf + f] + (byte - f * fb);
+    if (sizeof(T) == 4 && N == 4 && NW % 4 == 0 && ((uintptr_t)p & 15) == 0) {
+#pragma unroll
+      for (int v = 0; v < NW / 4; v++) {
+        const uint4 q = __ldg(reinterpret_cast<const uint4 *>(p) + v);
+        w[4 * v] = q.x;
+        w[4 * v + 1] = q.y;
+        w[4 * v + 2] = q.z;
+        w[4 * v + 3] = q.w;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NW; j++)
+        for (int i = 0; i < N; i++) w[j] |= (T)p[j * N + i] << (8 * i);
+    }
+  }
+  for (int sb = 0; sb < nsub; sb++) {
+    const int b0 = sb0[sb];
+    unsigned o = 0;
+#pragma unroll
+    for (int k = 0; k < G; k++)
+#pragma unroll
+      for (int j = 0; j < SPB; j++) o |= ((unsigned)(w[k * SPB + j] >> b0) & MASK) << (8 * k + j * FAN);
+    if (G == 4)
+      *reinterpret_cast<unsigned *>(out + (int64_t)sb * nout + ob) = o;
+    else
+      out[(int64_t)sb * nout + ob] = (uint8_t)o;
+  }
+}
+
+// Words wider than 8 bytes: one thread per output byte and subband
+// (extract_byte on the words where they lie; frames a whole number of output bytes).
+__global__ void extract_frames_wide_kernel(const uint8_t *__restrict__ rec, const int64_t *__restrict__ frames,
+                                           int nf, int fb, int64_t opb, int64_t nout, int N, int bits, int fan_out,
+                                           const int *__restrict__ tracks, uint8_t *__restrict__ out) {
   const int64_t ob = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int sb = blockIdx.y;
   if (ob >= nout) return;
@@ -158,12 +278,60 @@ void launch_gather_blocks(const uint8_t *rec, const int64_t *frames, int nf, int
   gather_blocks_kernel<<<grid, 256, 0, st>>>(rec, frames, nf, fb, block_size, list, total, out);
 }
 
-void launch_extract_frames(const uint8_t *rec, const int64_t *frames, int nf, int fb, int64_t opb, int64_t nout,
+bool launch_extract_frames(const uint8_t *rec, const int64_t *frames, int nf, int fb, int64_t opb, int64_t nout,
                            int N, int bits, int nsub, int fan_out, const int *tracks, uint8_t *out,
                            cudaStream_t st) {
-  if (nout <= 0) return;
-  extract_frames_kernel<<<dim3(blocks_for(nout, 256), nsub), 256, 0, st>>>(rec, frames, nf, fb, opb, nout, N, bits,
-                                                                           fan_out, tracks, out);
+  if (nout <= 0) return true;
+  const unsigned g = blocks_for(nout, 256);
+  if (N > 8) {
+    if (fb % ((8 / fan_out) * N)) return false;
+    extract_frames_wide_kernel<<<dim3(g, nsub), 256, 0, st>>>(rec, frames, nf, fb, opb, nout, N, bits, fan_out,
+                                                              tracks, out);
+    return true;
+  }
+  if (nsub * fan_out > kMaxExtractTracks) return false;
+#define SFXC_EXTRACT(SPB, BITS) \
+  extract_frames_kernel<SPB, BITS><<<g, 256, 0, st>>>(rec, frames, nf, fb, opb, nout, N, nsub, tracks, out)
+  if (fan_out == 1 && bits == 1) SFXC_EXTRACT(8, 1);
+  else if (fan_out == 2 && bits == 1) SFXC_EXTRACT(4, 1);
+  else if (fan_out == 2 && bits == 2) SFXC_EXTRACT(4, 2);
+  else if (fan_out == 4 && bits == 1) SFXC_EXTRACT(2, 1);
+  else if (fan_out == 4 && bits == 2) SFXC_EXTRACT(2, 2);
+  else if (fan_out == 8 && bits == 1) SFXC_EXTRACT(1, 1);
+  else if (fan_out == 8 && bits == 2) SFXC_EXTRACT(1, 2);
+  else return false;
+#undef SFXC_EXTRACT
+  return true;
+}
+
+bool launch_extract_fields(const uint8_t *rec, const int64_t *frames, int nf, int fb, int64_t opb, int64_t nout,
+                           int N, int fan_out, int nsub, const int *bases, uint8_t *out, cudaStream_t st) {
+  if (N > 8 || nsub > kMaxExtractTracks || fb % ((8 / fan_out) * N)) return false;
+  if (nout <= 0) return true;
+  const bool quad = nout % 4 == 0 && opb % 4 == 0 && fb % (4 * (8 / fan_out) * N) == 0;
+  const unsigned g = blocks_for(quad ? nout / 4 : nout, 256);
+#define SFXC_FIELDS(SPB, T)                                                                                    \
+  do {                                                                                                         \
+    if (quad)                                                                                                  \
+      extract_fields_kernel<SPB, T, 4><<<g, 256, 0, st>>>(rec, frames, nf, fb, opb, nout, N, nsub, bases, out); \
+    else                                                                                                       \
+      extract_fields_kernel<SPB, T, 1><<<g, 256, 0, st>>>(rec, frames, nf, fb, opb, nout, N, nsub, bases, out); \
+  } while (0)
+  if (N <= 4) {
+    if (fan_out == 1) SFXC_FIELDS(8, uint32_t);
+    else if (fan_out == 2) SFXC_FIELDS(4, uint32_t);
+    else if (fan_out == 4) SFXC_FIELDS(2, uint32_t);
+    else if (fan_out == 8) SFXC_FIELDS(1, uint32_t);
+    else return false;
+  } else {
+    if (fan_out == 1) SFXC_FIELDS(8, uint64_t);
+    else if (fan_out == 2) SFXC_FIELDS(4, uint64_t);
+    else if (fan_out == 4) SFXC_FIELDS(2, uint64_t);
+    else if (fan_out == 8) SFXC_FIELDS(1, uint64_t);
+    else return false;
+  }
+#undef SFXC_FIELDS
+  return true;
 }
 
 void launch_serialize_protocol(const ProtoRecord *recs, int nrec, const uint8_t *stream, uint8_t *out,

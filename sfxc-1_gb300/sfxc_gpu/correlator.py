@@ -272,6 +272,9 @@ class DeviceRecording:
         if hasattr(recording, "data_ptr"):
             self._rec = recording  # kept alive: the library reads it in place
             ptr, n, on_dev = recording.data_ptr(), recording.numel(), 1
+        elif isinstance(recording, np.ndarray) and recording.dtype == np.uint8 and recording.flags.c_contiguous:
+            self._rec = recording  # host memory (pinned or not), copied to the device by the library
+            ptr, n, on_dev = (recording.ctypes.data if recording.size else None), recording.size, 0
         else:
             self._rec = np.ascontiguousarray(np.frombuffer(bytes(recording), dtype=np.uint8))
             ptr, n, on_dev = (self._rec.ctypes.data if self._rec.size else None), self._rec.size, 0
@@ -293,6 +296,9 @@ class DeviceRecording:
 
     def _check(self, rc):
         return self._node._check(rc)
+
+    def n_blocks(self):
+        return self._lib.sfxc_gpu_recording_n_blocks(self._h)
 
     def blocks(self, data=True):
         """[{channel, start_ticks, data (None unless data), invalid}] per reader block."""

@@ -180,6 +180,31 @@ def test_device_reader_in_place(gpu_node):
     rec.close()
 
 
+@pytest.mark.parametrize("bits,tracks", [
+    (2, TRACKS16),                                            # 16 subbands of 2 tracks (sign, magnitude)
+    (1, [[k] for k in range(32)]),                            # 32 one-bit subbands
+    (2, [[4 * c + 1, 4 * c, 4 * c + 3, 4 * c + 2] for c in range(8)]),  # fan-out 4
+    (1, [[8 * c + t for t in range(8)] for c in range(4)]),   # fan-out 8
+    (2, [[2 * c, 2 * c + 1] for c in range(16)]),             # pairs in the other order (no bit field)
+    (2, [[c, c + 16] for c in range(16)]),                    # scattered tracks
+])
+@pytest.mark.parametrize("case", ["vdif_multichannel", "mark5b_zero_crc_fill"])
+def test_device_extraction_matches_block_extractor(gpu_node, bits, tracks, case):
+    """Every subband of every block, extracted where the frames lie (bit-field
+    layouts and any other), equals the block extractor's output on the
+    reader's blocks (invalid runs included); Mark5B frames are not a multiple
+    of four output bytes, and with fan-out 1 an output byte spans two frames."""
+    from sfxc_gpu import correlator
+    c = format_cases.cases()[case]
+    host_blocks = correlator.read_recording(c["rec"], c["fmt"], **c["params"])
+    per_block = [gpu_node.extract_block(b, 4, bits, tracks) for b in host_blocks]
+    r = correlator.DeviceRecording(gpu_node, c["rec"], c["fmt"], **c["params"])
+    r.extract(4, bits, tracks)
+    for sb in range(len(tracks)):
+        assert r.channel(sb) == [(b["start_ticks"], outs[sb], inv) for b, (outs, inv) in zip(host_blocks, per_block)]
+    r.close()
+
+
 def _device_protocols(gpu_node, sc, recs, fmt, reader_params, chans=None):
     """Per station: the device recording, its subbands R/L (channels 0, 1 of
     the 16-channel words) compared block by block with the direct path, and
@@ -294,6 +319,6 @@ def test_device_recording_errors(gpu_node):
     r = correlator.DeviceRecording(gpu_node, c["rec"], "vdif", **c["params"])
     with pytest.raises(lib.SfxcError):  # no channels extracted yet
         r.channel(0)
-    with pytest.raises(lib.SfxcError):  # 8000-byte frames are not whole output bytes of 3-byte words
+    with pytest.raises(lib.SfxcError):  # 8000-byte frames are not whole 3-byte words
         r.extract(3, 2, [[1, 0]])
     r.close()

@@ -48,12 +48,13 @@ int main(int argc, char **argv) {
   p.bits_per_sample = std::atoi(argv[9]);
   p.tracks_per_channel = std::atoi(argv[10]);
   for (int i = 11; i < argc; i++) p.first_track.push_back(std::atoi(argv[i]));
-  std::vector<FrameBlock> blocks = walk_frames(p, src);
+  FrameWalk walk = walk_frames(p, src);
   std::ofstream out(argv[2], std::ios::binary);
-  for (FrameBlock &blk : blocks) {
+  for (FrameBlock &blk : walk.blocks) {
     std::vector<uint8_t> data((size_t)blk.size, 0);
-    for (size_t i = 0; i < blk.frames.size(); i++)
-      std::memcpy(data.data() + i * blk.frame_bytes, src.b.data() + blk.frames[i], (size_t)blk.frame_bytes);
+    for (int i = 0; i < blk.nframes; i++)
+      std::memcpy(data.data() + (size_t)i * blk.frame_bytes, src.b.data() + walk.frames[(size_t)(blk.first + i)],
+                  (size_t)blk.frame_bytes);
     if (p.format == FORMAT_MARK5B) {
       const uint8_t *d = data.data();
       auto w = [d](int i) {
