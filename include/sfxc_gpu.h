@@ -343,6 +343,19 @@ int sfxc_gpu_extract_block(sfxc_gpu_ctx *ctx, const sfxc_reader_block *block, in
 typedef struct sfxc_gpu_recording sfxc_gpu_recording;
 sfxc_gpu_recording *sfxc_gpu_recording_create(sfxc_gpu_ctx *ctx, const sfxc_reader_params *params,
                                                const uint8_t *bytes, size_t n, int32_t bytes_on_device);
+/* The reader tasklet's blocks instead (Input_data_format_reader_tasklet,
+ * sfxc/src/input_data_format_reader_tasklet.cc:33-260): for the time
+ * intervals intervals[3k] start, [3k+1] stop, [3k+2] leave (ticks; the input
+ * node's reader intervals, Input_node_tasklet::add_time_interval,
+ * sfxc/src/input_node_tasklet.cc:101-128), the blocks it pushes, with
+ * wholly invalid blocks where frames are missing, the data ended or a
+ * stream fell behind (the reference fills those with random bytes marked
+ * invalid).  A block the reference pushes from a data buffer a failed read
+ * wrote into (the data ended inside it) goes out wholly invalid here, and a
+ * block keeps its own bytes where the reference's next read into the same
+ * buffer can replace them before its consumer takes it.  Replaces the
+ * recording's blocks (and any channels extracted). */
+int sfxc_gpu_recording_schedule(sfxc_gpu_recording *rec, int32_t n_intervals, const int64_t *intervals);
 int32_t sfxc_gpu_recording_n_blocks(const sfxc_gpu_recording *rec);
 /* Reader block i (as sfxc_gpu_reader_next fills it; out->invalid valid
  * until destroy); when data is not NULL, the block's out->size bytes,

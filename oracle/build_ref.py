@@ -52,6 +52,8 @@ REF_SOURCES = [
     "src/vdif_reader.cc",
     "src/mark5b_reader.cc",
     "src/input_data_format_reader.cc",
+    "src/input_data_format_reader_tasklet.cc",
+    "src/mark5a_reader.cc",
     "src/data_reader.cc",
     "src/data_reader_file.cc",
     "src/data_reader_blocking.cc",

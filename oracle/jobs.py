@@ -156,6 +156,40 @@ def reader(recording, fmt, *, ref_ticks, offset_ticks=0, track_bit_rate, frame_s
         return blocks
 
 
+def schedule(recording, fmt, *, ref_ticks, offset_ticks=0, track_bit_rate, frame_size=0, n_tracks, bits,
+             channel_tracks, intervals):
+    """Blocks the reference's reader tasklet (Input_data_format_reader_tasklet)
+    pushes for a recording and time intervals [(start, stop, leave) ticks]:
+    dicts {channel, start_ticks, size, data (None for a wholly invalid block),
+    invalid [(begin, n)], buffer (blocks with the same number were pushed in
+    one data buffer and show its last bytes), stale (the buffer's bytes are
+    not a block's: the last read into it failed, or none was made)}.  Only
+    the reference's own classes implement this."""
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "rec.bin")
+        open(path, "wb").write(bytes(recording))
+        lines = [("format", fmt), ("file", path), ("ref_ticks", ref_ticks), ("offset_ticks", offset_ticks),
+                 ("track_bit_rate", track_bit_rate), ("frame_size", frame_size), ("n_tracks", n_tracks),
+                 ("bits", bits)]
+        lines += [("channel#%d" % c, *tr) for c, tr in enumerate(channel_tracks)]
+        lines += [("interval#%d" % k, *iv) for k, iv in enumerate(intervals)]
+        out = os.path.join(d, "out")
+        os.makedirs(out)
+        _run("schedule", lines, out, d, "reference")
+        raw = open(os.path.join(out, "data.bin"), "rb").read()
+        blocks, pos = [], 0
+        for line in open(os.path.join(out, "schedule.txt")):
+            v = [int(x) for x in line.split()]
+            ch, ticks, size, buf, stale, inv = v[0], v[1], v[2], v[3], v[4], v[5:]
+            runs = [(inv[k], inv[k + 1]) for k in range(0, len(inv), 2)]
+            whole = any(b == 0 and n >= size for b, n in runs)
+            blocks.append({"channel": ch, "start_ticks": ticks, "size": size, "invalid": runs, "buffer": buf,
+                           "stale": bool(stale), "data": None if whole else raw[pos:pos + size]})
+            if not whole:
+                pos += size
+        return blocks
+
+
 def correlate_lines(job, d, dump=False, precision=32, dump_bins=False):
     """The job file lines of the 'correlate' mode for a job dict, with its
     delay tables, protocols and mask files written into directory d (read by

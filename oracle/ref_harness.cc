@@ -36,6 +36,7 @@
 #include "input_node_data_writer.h"
 #include "input_node_tasklet.h"
 #include "data_reader_file.h"
+#include "input_data_format_reader_tasklet.h"
 #include "mark5b_reader.h"
 #include "vdif_reader.h"
 #undef private
@@ -682,8 +683,115 @@ static int mode_reader(Kv &kv, const std::string &od) {
   return 0;
 }
 
+// Readers that note, per data buffer, whether the last read into it
+// succeeded (a failed read can leave part of a frame and older bytes there).
+static std::map<const void *, bool> g_last_read_ok;
+class Logged_vdif_reader : public VDIF_reader {
+ public:
+  Logged_vdif_reader(boost::shared_ptr<Data_reader> dr, Data_frame &d, Time ref) : VDIF_reader(dr, d, ref) {}
+  bool read_new_block(Data_frame &d) {
+    const bool ok = VDIF_reader::read_new_block(d);
+    g_last_read_ok[&d.buffer->data] = ok;
+    return ok;
+  }
+};
+class Logged_mark5b_reader : public Mark5b_reader {
+ public:
+  Logged_mark5b_reader(boost::shared_ptr<Data_reader> dr, Data_frame &d, Time ref) : Mark5b_reader(dr, d, ref) {}
+  bool read_new_block(Data_frame &d) {
+    const bool ok = Mark5b_reader::read_new_block(d);
+    g_last_read_ok[&d.buffer->data] = ok;
+    return ok;
+  }
+};
+
+// The reader tasklet (Input_data_format_reader_tasklet,
+// sfxc/src/input_data_format_reader_tasklet.cc) over a file: the reader as in
+// mode_reader, the tasklet given the job's time intervals (start, stop,
+// leave ticks) and run to its end in this thread; per block it pushed:
+// channel, start ticks, size, the number of its data buffer (blocks pushed
+// with the same buffer share its bytes as they were last written), whether
+// the buffer's bytes are not a block's (the last read into it failed, or
+// none was made) and invalid runs (schedule.txt), payloads of blocks that
+// are not wholly invalid back to back (data.bin).
+//   as mode_reader, plus interval#k <start> <stop> <leave>
+static int mode_schedule(Kv &kv, const std::string &od) {
+  Input_node_parameters p;
+  p.track_bit_rate = geti(kv, "track_bit_rate");
+  p.frame_size = geti(kv, "frame_size");
+  p.n_tracks = geti(kv, "n_tracks");
+  p.offset = ticks_time(getll(kv, "offset_ticks"));
+  p.data_modulation = 0;
+  p.exit_on_empty_datastream = false;
+  const int nch = count_key(kv, "channel");
+  for (int c = 0; c < nch; c++) {
+    Input_node_parameters::Channel_parameters cp;
+    cp.bits_per_sample = geti(kv, "bits");
+    const std::vector<std::string> &tr = get(kv, idx("channel", c));
+    for (size_t k = 0; k < tr.size(); k++) cp.tracks.push_back(std::atoi(tr[k].c_str()));
+    cp.sideband = 'U';
+    cp.polarisation = 'R';
+    cp.frequency_number = c;
+    p.channels.push_back(cp);
+  }
+  boost::shared_ptr<Data_reader> dr(new Data_reader_file("file://" + get(kv, "file")[0]));
+  // every pushed block stays in the output queue until the end: a pool large enough for all of them
+  boost::shared_ptr<Input_node_types::Data_memory_pool> pool(new Input_node_types::Data_memory_pool(20000));
+  Input_data_format_reader::Data_frame data;
+  data.buffer = pool->allocate();
+  const Time ref = ticks_time(getll(kv, "ref_ticks"));
+  const std::string fmt = get(kv, "format")[0];
+  boost::shared_ptr<Input_data_format_reader> r;
+  if (fmt == "vdif")
+    r.reset(new Logged_vdif_reader(dr, data, ref));
+  else if (fmt == "mark5b")
+    r.reset(new Logged_mark5b_reader(dr, data, ref));
+  else
+    die("unknown format " + fmt);
+  r->set_parameters(p);
+  Input_data_format_reader_tasklet t(r, pool);
+  t.set_parameters(p);
+  const int niv = count_key(kv, "interval");
+  for (int k = 0; k < niv; k++) {
+    const std::vector<std::string> &v = get(kv, idx("interval", k));
+    Time a = ticks_time(std::atoll(v[0].c_str())), b = ticks_time(std::atoll(v[1].c_str())),
+         c = ticks_time(std::atoll(v[2].c_str()));
+    t.add_time_interval(a, b, c);
+  }
+  t.stop();
+  t.do_execute();
+  FILE *bf = std::fopen((od + "/schedule.txt").c_str(), "w");
+  FILE *df = std::fopen((od + "/data.bin").c_str(), "wb");
+  if (!bf || !df) die("cannot write schedule output");
+  Input_node_types::Input_buffer_ptr q = t.get_output_buffer();
+  std::map<const void *, int> buffers;
+  while (!q->empty()) {
+    Input_node_types::Input_data_frame &e = q->front();
+    const std::vector<unsigned char> &b = e.buffer->data;
+    const void *key = &b;
+    if (!buffers.count(key)) {
+      const int id = (int)buffers.size();
+      buffers[key] = id;
+    }
+    const bool stale = !g_last_read_ok.count(key) || !g_last_read_ok[key];
+    std::fprintf(bf, "%d %lld %d %d %d", e.channel, (long long)e.start_time.get_clock_ticks(), (int)b.size(),
+                 buffers[key], stale ? 1 : 0);
+    bool whole = false;
+    for (size_t k = 0; k < e.invalid.size(); k++) {
+      std::fprintf(bf, " %d %d", e.invalid[k].invalid_begin, e.invalid[k].nr_invalid);
+      if (e.invalid[k].invalid_begin == 0 && e.invalid[k].nr_invalid >= (int)b.size()) whole = true;
+    }
+    std::fprintf(bf, "\n");
+    if (!whole && !b.empty()) std::fwrite(&b[0], 1, b.size(), df);
+    q->pop();
+  }
+  std::fclose(bf);
+  std::fclose(df);
+  return 0;
+}
+
 int main(int argc, char **argv) {
-  if (argc != 4) die("usage: ref_harness correlate|delays|protocol|extract|reader <job> <out>");
+  if (argc != 4) die("usage: ref_harness correlate|delays|protocol|extract|reader|schedule <job> <out>");
   Kv kv = read_job(argv[2]);
   std::string m(argv[1]);
   if (m == "correlate") return mode_correlate(kv, argv[3]);
@@ -691,6 +799,7 @@ int main(int argc, char **argv) {
   if (m == "protocol") return mode_protocol(kv, argv[3]);
   if (m == "extract") return mode_extract(kv, argv[3]);
   if (m == "reader") return mode_reader(kv, argv[3]);
+  if (m == "schedule") return mode_schedule(kv, argv[3]);
   die("unknown mode " + m);
   return 2;
 }

@@ -2248,6 +2248,99 @@ struct sfxc_gpu_recording {
   std::shared_ptr<ProtoPlan> last_plan;
 };
 
+namespace {
+DeviceFrames device_frames(sfxc_gpu_recording *r) {
+  DeviceFrames src;
+  src.rec = r->rec;
+  src.n = r->n;
+  src.st = r->ctx->st;
+  src.info = &r->buf->info;
+  src.staging = &r->buf->staging;
+  return src;
+}
+
+// The recording's blocks: `blocks` in order, each carrying the bytes of a
+// walk block (its frames) or none (filled in: frame offsets -1, wholly
+// invalid).  Mark5B blocks take the fill-pattern runs of their walk block,
+// found on the device.
+void install_blocks(sfxc_gpu_recording *r, const FrameWalk &walk, const std::vector<ScheduledBlock> &blocks) {
+  sfxc_gpu_ctx *c = r->ctx;
+  RecordingBuffers &B = *r->buf;
+  const bool mk5b = r->p.format == FORMAT_MARK5B;
+  r->blocks.clear();
+  r->chan_set.clear();
+  r->set_blocks.clear();
+  r->set_runs.clear();
+  r->chan_off.clear();
+  r->proto.clear();
+  r->last_plan.reset();
+  if (!walk.blocks.empty()) {
+    r->nf = walk.blocks[0].nframes;
+    r->fb = walk.blocks[0].frame_bytes;
+    r->block_size = walk.blocks[0].size;
+  } else if (mk5b) {
+    r->nf = kMk5bBlockFrames;
+    r->fb = kMk5bFrame;
+    r->block_size = kMk5bBlock;
+  } else if (!blocks.empty()) {
+    throw Error(SFXC_GPU_EINVAL, "no VDIF frame header in the recording: no block size for filled-in blocks");
+  }
+  const int nw = (int)walk.blocks.size();
+  for (int b = 0; b < nw; b++)
+    if (walk.blocks[b].nframes != r->nf || walk.blocks[b].size != r->block_size ||
+        walk.blocks[b].first != (int64_t)b * r->nf)
+      throw Error(SFXC_GPU_ESTATE, "uneven reader blocks");
+  // fill-pattern runs of every Mark5B walk block: count, then write
+  std::vector<std::vector<int32_t>> fill(mk5b ? nw : 0);
+  if (mk5b && nw) {
+    upload(B.frames, walk.frames.data(), walk.frames.size() * sizeof(int64_t), c->st);
+    B.counts.ensure((size_t)nw * 4);
+    launch_fill_runs(r->rec, B.frames.as<int64_t>(), r->nf, r->fb / 4, r->block_size / 4, nw, B.counts.as<int32_t>(),
+                     nullptr, nullptr, c->st);
+    CK(cudaGetLastError());
+    std::vector<int32_t> cnt(nw);
+    CK(cudaMemcpyAsync(cnt.data(), B.counts.p, (size_t)nw * 4, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    std::vector<int64_t> off(nw + 1, 0);
+    for (int b = 0; b < nw; b++) off[b + 1] = off[b] + cnt[b];
+    if (off[nw]) {
+      upload(B.offs, off.data(), (size_t)nw * 8, c->st);
+      B.runs.ensure((size_t)off[nw] * 8);
+      launch_fill_runs(r->rec, B.frames.as<int64_t>(), r->nf, r->fb / 4, r->block_size / 4, nw, nullptr,
+                       B.offs.as<int64_t>(), B.runs.as<int32_t>(), c->st);
+      CK(cudaGetLastError());
+      std::vector<int32_t> runs((size_t)off[nw] * 2);
+      CK(cudaMemcpyAsync(runs.data(), B.runs.p, runs.size() * 4, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      for (int b = 0; b < nw; b++) fill[b].assign(runs.begin() + 2 * off[b], runs.begin() + 2 * off[b + 1]);
+    }
+  }
+  std::vector<int64_t> frames;
+  frames.reserve(blocks.size() * (size_t)r->nf);
+  for (const ScheduledBlock &sb : blocks) {
+    FrameBlock fb;
+    fb.channel = sb.channel;
+    fb.start_ticks = sb.start_ticks;
+    fb.size = r->block_size;
+    fb.frame_bytes = r->fb;
+    fb.nframes = r->nf;
+    fb.first = (int64_t)frames.size();
+    if (sb.whole_invalid || sb.block < 0) {
+      frames.insert(frames.end(), (size_t)r->nf, (int64_t)-1);
+      fb.invalid = {0, r->block_size};
+      fb.invalid.insert(fb.invalid.end(), sb.invalid.begin(), sb.invalid.end());
+    } else {
+      const FrameBlock &w = walk.blocks[(size_t)sb.block];
+      frames.insert(frames.end(), walk.frames.begin() + w.first, walk.frames.begin() + w.first + r->nf);
+      fb.invalid = mk5b ? fill[(size_t)sb.block] : sb.invalid;
+    }
+    r->blocks.push_back(std::move(fb));
+  }
+  if (!frames.empty()) upload(B.frames, frames.data(), frames.size() * sizeof(int64_t), c->st);
+  CK(cudaStreamSynchronize(c->st));
+}
+}  // namespace
+
 sfxc_gpu_recording *sfxc_gpu_recording_create(sfxc_gpu_ctx *c, const sfxc_reader_params *params,
                                                const uint8_t *bytes, size_t n, int32_t bytes_on_device) {
   if (!c) return nullptr;
@@ -2273,56 +2366,22 @@ sfxc_gpu_recording *sfxc_gpu_recording_create(sfxc_gpu_ctx *c, const sfxc_reader
       if (n) CK(cudaMemcpyAsync(B.own.p, bytes, n, cudaMemcpyHostToDevice, c->st));
       r->rec = B.own.as<uint8_t>();
     }
-    DeviceFrames src;
-    src.rec = r->rec;
-    src.n = r->n;
-    src.st = c->st;
-    src.info = &B.info;
-    src.staging = &B.staging;
     FrameWalk walk;
-    try {
-      walk = walk_frames(r->p, src);
-    } catch (const std::invalid_argument &e) {
-      throw Error(SFXC_GPU_EINVAL, e.what());
-    } catch (const std::logic_error &e) {
-      throw Error(SFXC_GPU_ESTATE, e.what());
-    }
-    r->blocks = std::move(walk.blocks);
-    if (!r->blocks.empty()) {
-      r->nf = r->blocks[0].nframes;
-      r->fb = r->blocks[0].frame_bytes;
-      r->block_size = r->blocks[0].size;
-      for (size_t b = 0; b < r->blocks.size(); b++)
-        if (r->blocks[b].nframes != r->nf || r->blocks[b].size != r->block_size ||
-            r->blocks[b].first != (int64_t)b * r->nf)
-          throw Error(SFXC_GPU_ESTATE, "uneven reader blocks");
-      upload(B.frames, walk.frames.data(), walk.frames.size() * sizeof(int64_t), c->st);
-      if (r->p.format == FORMAT_MARK5B) {  // fill-pattern runs of every block: count, then write
-        const int nb = (int)r->blocks.size();
-        DevBuf &counts = B.counts, &offs = B.offs, &runs = B.runs;
-        counts.ensure((size_t)nb * 4);
-        launch_fill_runs(r->rec, B.frames.as<int64_t>(), r->nf, r->fb / 4, r->block_size / 4, nb,
-                         counts.as<int32_t>(), nullptr, nullptr, c->st);
-        CK(cudaGetLastError());
-        std::vector<int32_t> cnt(nb);
-        CK(cudaMemcpyAsync(cnt.data(), counts.p, (size_t)nb * 4, cudaMemcpyDeviceToHost, c->st));
-        CK(cudaStreamSynchronize(c->st));
-        std::vector<int64_t> off(nb + 1, 0);
-        for (int b = 0; b < nb; b++) off[b + 1] = off[b] + cnt[b];
-        if (off[nb]) {
-          upload(offs, off.data(), (size_t)nb * 8, c->st);
-          runs.ensure((size_t)off[nb] * 8);
-          launch_fill_runs(r->rec, B.frames.as<int64_t>(), r->nf, r->fb / 4, r->block_size / 4, nb, nullptr,
-                           offs.as<int64_t>(), runs.as<int32_t>(), c->st);
-          CK(cudaGetLastError());
-          std::vector<int32_t> all((size_t)off[nb] * 2);
-          CK(cudaMemcpyAsync(all.data(), runs.p, all.size() * 4, cudaMemcpyDeviceToHost, c->st));
-          CK(cudaStreamSynchronize(c->st));
-          for (int b = 0; b < nb; b++)
-            r->blocks[b].invalid.assign(all.begin() + 2 * off[b], all.begin() + 2 * off[b + 1]);
-        }
+    {
+      DeviceFrames src = device_frames(r.get());
+      try {
+        walk = walk_frames(r->p, src);
+      } catch (const std::invalid_argument &e) {
+        throw Error(SFXC_GPU_EINVAL, e.what());
+      } catch (const std::logic_error &e) {
+        throw Error(SFXC_GPU_ESTATE, e.what());
       }
     }
+    std::vector<ScheduledBlock> all;
+    for (size_t b = 0; b < walk.blocks.size(); b++)
+      all.push_back(ScheduledBlock{walk.blocks[b].start_ticks, walk.blocks[b].channel, (int32_t)b, false,
+                                   walk.blocks[b].invalid});
+    install_blocks(r.get(), walk, all);
     CK(cudaStreamSynchronize(c->st));
     return r.release();
   } catch (const Error &e) {
@@ -2337,6 +2396,31 @@ void sfxc_gpu_recording_destroy(sfxc_gpu_recording *r) {
   cudaStreamSynchronize(r->ctx->st);
   r->ctx->rec_spare.push_back(std::move(r->buf));  // its buffers serve the context's next recording
   delete r;
+}
+
+int sfxc_gpu_recording_schedule(sfxc_gpu_recording *r, int32_t n_intervals, const int64_t *intervals) {
+  if (!r) return SFXC_GPU_EINVAL;
+  sfxc_gpu_ctx *c = r->ctx;
+  try {
+    if (n_intervals < 0 || (n_intervals && !intervals)) throw Error(SFXC_GPU_EINVAL, "bad intervals");
+    CK(cudaSetDevice(c->device));
+    std::vector<TimeInterval> iv;
+    for (int k = 0; k < n_intervals; k++)
+      iv.push_back(TimeInterval{intervals[3 * k], intervals[3 * k + 1], intervals[3 * k + 2]});
+    DeviceFrames src = device_frames(r);
+    Schedule sched;
+    try {
+      sched = schedule_blocks(r->p, src, iv);
+    } catch (const std::invalid_argument &e) {
+      throw Error(SFXC_GPU_EINVAL, e.what());
+    } catch (const std::exception &e) {
+      throw Error(SFXC_GPU_ESTATE, e.what());
+    }
+    install_blocks(r, sched.walk, sched.blocks);
+    return SFXC_GPU_OK;
+  } catch (const Error &e) {
+    return fail(c, e);
+  }
 }
 
 int32_t sfxc_gpu_recording_n_blocks(const sfxc_gpu_recording *r) { return r ? (int32_t)r->blocks.size() : 0; }

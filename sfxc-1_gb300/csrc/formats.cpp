@@ -199,10 +199,6 @@ class VdifReader : public FormatReader {
 };
 
 // ---- Mark5B (sfxc/src/mark5b_reader.cc, header sfxc/include/mark5b_reader.h:33-55)
-constexpr int kMk5bFrame = 2500 * 4;   // SIZE_MK5B_FRAME words of SIZE_MK5B_WORD bytes
-constexpr int kMk5bHeader = 4 * 4;     // SIZE_MK5B_HEADER words
-constexpr int kMk5bBlockFrames = 8;    // N_MK5B_BLOCKS_TO_READ
-constexpr int kMk5bBlock = kMk5bBlockFrames * kMk5bFrame;
 
 struct Mk5bHeader {
   uint8_t b[16] = {};
@@ -373,113 +369,159 @@ int mjd_of_date(int day, int month, int year) { return mjd_from_date(day, month,
 // (q + header size <= size, else end of data), a payload read likewise.
 namespace {
 
-FrameWalk walk_vdif(const ReaderParams &p, FrameSource &src) {
-  if (p.frame_size <= 0) throw std::invalid_argument("VDIF frame size must be positive");
-  const int64_t n = src.size();
-  const int fs = p.frame_size;
-  const int ref_jday = (int)mjd_of_ticks(p.ref_ticks);
-  const double sample_rate = (double)p.track_bit_rate * (p.tracks_per_channel / p.bits_per_sample);
-  std::map<int, int> thread_map;
-  int fpb = std::max(1, 32128 / fs);
-  if (p.n_tracks == 0) {
-    for (size_t i = 0; i < p.first_track.size(); i++) thread_map[p.first_track[i]] = (int)i;
-    fpb = 1;
-  }
+// One reader: read() is one read_new_block call, appending its ReadEvent
+// (and its block) to out.
+class Walker {
+ public:
+  virtual ~Walker() {}
+  virtual void read() = 0;
+  // get_current_time() as when the reader is open; `apply`: with the side
+  // effect the reader's call has (Mark5B: the switch to VLBA time stamps)
+  virtual int64_t now(bool apply) = 0;
+  bool ended() const { return ended_; }
   FrameWalk out;
-  // before the first header: 16-byte candidates, a fill header skips a
-  // non-legacy frame (vdif_reader.cc:84-100)
-  const int64_t cstride = (int64_t)fs + 32;
-  int64_t ncand = 0;
-  while (ncand <= 256 && ncand * cstride + 16 <= n) ncand++;
-  std::vector<FrameInfo> cand((size_t)ncand);
-  if (ncand) src.decode(FORMAT_VDIF, 0, cstride, ncand, cand.data());
-  int restarts = 0;
-  int64_t k = 0;
-  for (;; k++) {
-    if (k >= ncand) return out;
-    if (!(cand[k].flags & FRAME_FILL)) break;
-    if (++restarts > 256) return out;
+
+ protected:
+  bool ended_ = false;
+  void event(int32_t block, bool eof) {
+    if (eof) ended_ = true;
+    out.reads.push_back(ReadEvent{block, eof, now(false)});
   }
-  const FrameInfo first = cand[k];
-  const int64_t p0 = k * cstride;
-  const int hs = (first.flags & FRAME_LEGACY) ? 16 : 32;
-  if (p0 + hs > n) return out;
-  // after it, frames at a fixed stride
-  const int64_t stride = hs + fs;
-  const int64_t nf = (n - p0 - 16) / stride + 1;
-  std::vector<FrameInfo> hdr((size_t)nf);
-  src.decode(FORMAT_VDIF, p0, stride, nf, hdr.data());
-  const int32_t block_size = fpb * std::max(first.data_size, fs);
-  auto time_of = [&](const FrameInfo &h) {  // get_current_time (vdif_reader.cc:63-75)
-    const double seconds = (double)h.seconds - (ref_jday - h.epoch_mjd) * 24 * 60 * 60;
-    double subsec = 0;
-    if (sample_rate > 0) {
-      const int spf = 8 * fs / ((first.bits_m1 + 1) * (1 << first.log2_nchan));
-      subsec = (double)h.frame_nr * spf / sample_rate;
+};
+
+class VdifWalker : public Walker {
+ public:
+  VdifWalker(const ReaderParams &p, FrameSource &src) : p_(p), src_(src) {
+    if (p.frame_size <= 0) throw std::invalid_argument("VDIF frame size must be positive");
+    n_ = src.size();
+    fs_ = p.frame_size;
+    ref_jday_ = (int)mjd_of_ticks(p.ref_ticks);
+    sample_rate_ = (double)p.track_bit_rate * (p.tracks_per_channel / p.bits_per_sample);
+    fpb_ = std::max(1, 32128 / fs_);
+    if (p.n_tracks == 0) {
+      for (size_t i = 0; i < p.first_track.size(); i++) thread_map_[p.first_track[i]] = (int)i;
+      fpb_ = 1;
     }
-    return ticks_of(ref_jday, seconds + subsec) - p.offset_ticks;
-  };
-  auto header_in = [&](int64_t j) { return j < nf && p0 + j * stride + hs <= n; };
-  int64_t j = 0;
-  bool have = true;  // the first header has been read
-  for (;;) {         // read_new_block (vdif_reader.cc:77-190)
-    FrameBlock b;
-    b.first = (int64_t)out.frames.size();
+    cstride_ = (int64_t)fs_ + 32;
+  }
+
+  int64_t now(bool) override {  // get_current_time (vdif_reader.cc:63-75)
+    const double seconds = (double)cur_.seconds - (ref_jday_ - cur_.epoch_mjd) * 24 * 60 * 60;
+    double subsec = 0;
+    if (sample_rate_ > 0) {
+      const int spf = 8 * fs_ / ((first_.bits_m1 + 1) * (1 << first_.log2_nchan));
+      subsec = (double)cur_.frame_nr * spf / sample_rate_;
+    }
+    return ticks_of(ref_jday_, seconds + subsec) - p_.offset_ticks;
+  }
+
+  void read() override {  // read_new_block (vdif_reader.cc:77-190)
+    if (ended_) return event(-1, true);
+    int restarts = 0;
     for (;;) {
-      if (!have && !header_in(j)) {
-        out.frames.resize((size_t)b.first);
-        return out;
+      int64_t pos;
+      if (!first_seen_) {
+        // before the first header: 16-byte candidates fs + 32 apart (a fill
+        // header skips a non-legacy frame, vdif_reader.cc:84-100)
+        pos = k_ * cstride_;
+        if (pos + 16 > n_) return event(-1, true);
+        cur_ = candidate(k_);
+        if (cur_.flags & FRAME_FILL) {
+          k_++;
+          if (++restarts > 256) return event(-1, false);
+          continue;
+        }
+        first_ = cur_;
+        first_seen_ = true;
+        p0_ = pos;
+        hs_ = (first_.flags & FRAME_LEGACY) ? 16 : 32;
+        if (p0_ + hs_ > n_) return event(-1, true);
+        // after it, frames at a fixed stride
+        stride_ = hs_ + fs_;
+        nf_ = (n_ - p0_ - 16) / stride_ + 1;
+        hdr_.resize((size_t)nf_);
+        src_.decode(FORMAT_VDIF, p0_, stride_, nf_, hdr_.data());
+        block_size_ = fpb_ * std::max(first_.data_size, fs_);
+        j_ = 0;
+      } else {
+        if (!header_in(j_)) return event(-1, true);
+        pos = p0_ + j_ * stride_;
+        cur_ = hdr_[(size_t)j_];
       }
-      have = false;
-      const FrameInfo &h = hdr[(size_t)j];
-      const int64_t pos = p0 + j * stride;
-      if ((h.flags & FRAME_FILL) || h.frame_nr % (uint32_t)fpb != 0) {
-        j++;
-        if (++restarts > 256) return out;
+      const FrameInfo h = cur_;
+      if ((h.flags & FRAME_FILL) || h.frame_nr % (uint32_t)fpb_ != 0) {
+        j_++;
+        if (++restarts > 256) return event(-1, false);
         continue;
       }
-      if (pos + hs + fs > n) return out;
-      auto it = thread_map.find(h.thread);
+      if (pos + hs_ + fs_ > n_) return event(-1, true);
+      FrameBlock b;
+      auto it = thread_map_.find(h.thread);
       if (h.flags & FRAME_INVALID) {
         b.invalid.push_back(0);
-        b.invalid.push_back(fs);
-        b.channel = it != thread_map.end() ? it->second : 0;
+        b.invalid.push_back(fs_);
+        b.channel = it != thread_map_.end() ? it->second : 0;
       } else {
-        if (it == thread_map.end()) {
-          if (thread_map.empty()) {
-            thread_map[h.thread] = 0;
+        if (it == thread_map_.end()) {
+          if (thread_map_.empty()) {  // a single thread: its id comes from the data
+            thread_map_[h.thread] = 0;
           } else {
-            j++;
-            if (++restarts > 256) return out;
+            j_++;
+            if (++restarts > 256) return event(-1, false);
             continue;
           }
         }
-        b.channel = thread_map[h.thread];
+        b.channel = thread_map_[h.thread];
       }
-      out.frames.push_back(pos + hs);
-      j++;
-      for (int i = 1; i < fpb; i++, j++) {
-        const int64_t q = p0 + j * stride;
-        if (!header_in(j) || q + hs + fs > n) {
+      b.first = (int64_t)out.frames.size();
+      out.frames.push_back(pos + hs_);
+      j_++;
+      for (int i = 1; i < fpb_; i++, j_++) {
+        const int64_t q = p0_ + j_ * stride_;
+        if (!header_in(j_) || q + hs_ + fs_ > n_) {
           out.frames.resize((size_t)b.first);
-          return out;
+          return event(-1, true);
         }
-        out.frames.push_back(q + hs);
-        if (hdr[(size_t)j].flags & FRAME_INVALID) {
-          b.invalid.push_back(i * fs);
-          b.invalid.push_back(fs);
+        out.frames.push_back(q + hs_);
+        if (hdr_[(size_t)j_].flags & FRAME_INVALID) {
+          b.invalid.push_back(i * fs_);
+          b.invalid.push_back(fs_);
         }
       }
-      b.start_ticks = time_of(h);
-      b.size = block_size;
-      b.frame_bytes = fs;
-      b.nframes = fpb;
+      b.start_ticks = now(false);
+      b.size = block_size_;
+      b.frame_bytes = fs_;
+      b.nframes = fpb_;
       out.blocks.push_back(std::move(b));
-      restarts = 0;
-      break;
+      return event((int32_t)out.blocks.size() - 1, false);
     }
   }
-}
+
+ private:
+  const ReaderParams &p_;
+  FrameSource &src_;
+  int64_t n_ = 0, cstride_ = 0, k_ = 0, p0_ = 0, stride_ = 0, nf_ = 0, j_ = 0;
+  int fs_ = 0, ref_jday_ = 0, fpb_ = 1, hs_ = 32;
+  int32_t block_size_ = 0;
+  double sample_rate_ = 0;
+  bool first_seen_ = false;
+  FrameInfo first_{}, cur_{};  // the first header (zero before it); the header the reader holds as current
+  std::map<int, int> thread_map_;
+  std::vector<FrameInfo> cand_, hdr_;
+
+  bool header_in(int64_t j) const { return j < nf_ && p0_ + j * stride_ + hs_ <= n_; }
+  FrameInfo candidate(int64_t k) {  // decoded as needed
+    while ((int64_t)cand_.size() <= k) {
+      const int64_t k0 = (int64_t)cand_.size();
+      int64_t cnt = 0;
+      while (cnt < 1024 && (k0 + cnt) * cstride_ + 16 <= n_) cnt++;
+      if (cnt == 0) throw std::logic_error("VDIF candidate header past the end");
+      cand_.resize((size_t)(k0 + cnt));
+      src_.decode(FORMAT_VDIF, k0 * cstride_, cstride_, cnt, cand_.data() + k0);
+    }
+    return cand_[(size_t)k];
+  }
+};
 
 // Reads of the bytes fetched for one Mark5B resync, with Source's
 // end-of-data rule; any short read ends the walk.
@@ -499,86 +541,86 @@ struct FetchedBytes {
   }
 };
 
-FrameWalk walk_mk5b(const ReaderParams &p, FrameSource &src) {
-  const int64_t n = src.size();
-  int current_jday = (int)mjd_of_ticks(p.ref_ticks);
-  const int bitstreams = p.n_tracks;
-  const int word = bitstreams <= 32 ? 4 : 8;
-  const int tbr = p.track_bit_rate;
-  if (tbr <= 0 || tbr % 1000000) throw std::invalid_argument("Mark5B track bit rate must be whole Mb/s");
-  const int64_t tbh = ticks_of_usec((double)kMk5bBlock / (word * tbr / 1000000));
-  const int sample_rate = p.track_bit_rate * (p.tracks_per_channel / p.bits_per_sample);
-  const int64_t fstride = kMk5bHeader + kMk5bFrame, bstride = kMk5bBlockFrames * fstride;
-  const uint8_t zero[16] = {};
-  FrameInfo cur = decode_mk5b(zero), prev = cur;
-  int frame_nr = -1;
-  bool frame_nr_valid = true;
-  FrameWalk out;
-  auto frame_nr_update = [&]() {  // mark5b_reader.cc:127-131
-    if (bitstreams == 64 && cur.seconds == prev.seconds && frame_nr > (int)cur.frame_nr)
-      frame_nr = (int)cur.frame_nr + 32768;
-    else
-      frame_nr = (int)cur.frame_nr;
-  };
-  auto finish = [&](const int64_t *frames) {  // jday, then get_current_time (mark5b_reader.cc:84-105)
-    if (cur.thread != current_jday % 1000) current_jday++;
-    const double rate = (double)sample_rate * bitstreams;
-    const double subsec = (double)((uint64_t)(int64_t)frame_nr * (8 * kMk5bFrame)) / rate;
-    if (subsec > 1 && frame_nr_valid) frame_nr_valid = false;
+class Mk5bWalker : public Walker {
+ public:
+  Mk5bWalker(const ReaderParams &p, FrameSource &src) : p_(p), src_(src) {
+    n_ = src.size();
+    current_jday_ = (int)mjd_of_ticks(p.ref_ticks);
+    bitstreams_ = p.n_tracks;
+    const int word = bitstreams_ <= 32 ? 4 : 8;
+    const int tbr = p.track_bit_rate;
+    if (tbr <= 0 || tbr % 1000000) throw std::invalid_argument("Mark5B track bit rate must be whole Mb/s");
+    tbh_ = ticks_of_usec((double)kMk5bBlock / (word * tbr / 1000000));
+    sample_rate_ = p.track_bit_rate * (p.tracks_per_channel / p.bits_per_sample);
+    const uint8_t zero[16] = {};
+    cur_ = prev_ = decode_mk5b(zero);
+  }
+
+  int64_t now(bool apply) override {  // get_current_time (mark5b_reader.cc:84-105)
+    bool valid = frame_nr_valid_;
+    const double rate = (double)sample_rate_ * bitstreams_;
+    const double subsec = (double)((uint64_t)(int64_t)frame_nr_ * (8 * kMk5bFrame)) / rate;
+    if (subsec > 1 && valid) valid = false;
+    if (apply) frame_nr_valid_ = valid;
     int64_t t;
-    if (frame_nr_valid) {
-      t = ticks_of(current_jday, (double)cur.seconds + subsec);
-    } else {
-      const int64_t second = ticks_of(current_jday, (double)cur.seconds);
-      const int64_t sub = ticks_of_usec((double)cur.epoch_mjd);
-      const int nframes = (int)std::round((double)sub / tbh);
-      t = second + (int64_t)std::round((double)tbh * nframes);
+    if (valid) {
+      t = ticks_of(current_jday_, (double)cur_.seconds + subsec);
+    } else {  // VLBA time stamp, rounded to whole blocks
+      const int64_t second = ticks_of(current_jday_, (double)cur_.seconds);
+      const int64_t sub = ticks_of_usec((double)cur_.epoch_mjd);
+      const int nframes = (int)std::round((double)sub / tbh_);
+      t = second + (int64_t)std::round((double)tbh_ * nframes);
     }
-    FrameBlock b;
-    b.start_ticks = t - p.offset_ticks;
-    b.size = kMk5bBlock;
-    b.frame_bytes = kMk5bFrame;
-    b.first = (int64_t)out.frames.size();
-    b.nframes = kMk5bBlockFrames;
-    out.frames.insert(out.frames.end(), frames, frames + kMk5bBlockFrames);
-    out.blocks.push_back(std::move(b));
-  };
-  // block-start headers on the grid g0 + k * bstride
-  int64_t g0 = -1;
-  std::vector<FrameInfo> grid;
-  int64_t P = 0;
-  for (;;) {  // read_new_block (mark5b_reader.cc:111-162)
-    if (P + kMk5bHeader > n) return out;
-    if (g0 < 0 || P < g0 || (P - g0) % bstride || (P - g0) / bstride >= (int64_t)grid.size()) {
-      g0 = P;
-      grid.assign((size_t)((n - P - kMk5bHeader) / bstride + 1), FrameInfo{});
-      src.decode(FORMAT_MARK5B, g0, bstride, (int64_t)grid.size(), grid.data());
+    return t - p_.offset_ticks;
+  }
+
+  void read() override {  // read_new_block (mark5b_reader.cc:111-162)
+    if (ended_) return event(-1, true);
+    if (P_ + kMk5bHeader > n_) return event(-1, true);
+    if (g0_ < 0 || P_ < g0_ || (P_ - g0_) % kBStride || (P_ - g0_) / kBStride >= (int64_t)grid_.size()) {
+      g0_ = P_;  // block-start headers on the grid g0 + k * (8 frames)
+      grid_.assign((size_t)((n_ - P_ - kMk5bHeader) / kBStride + 1), FrameInfo{});
+      src_.decode(FORMAT_MARK5B, g0_, kBStride, (int64_t)grid_.size(), grid_.data());
     }
-    const FrameInfo h = grid[(size_t)((P - g0) / bstride)];
-    if ((h.flags & FRAME_CHECK) && !(h.frame_nr % kMk5bBlockFrames != 0 && frame_nr_valid)) {
-      prev = cur;
-      cur = h;
+    const FrameInfo h = grid_[(size_t)((P_ - g0_) / kBStride)];
+    if ((h.flags & FRAME_CHECK) && !(h.frame_nr % kMk5bBlockFrames != 0 && frame_nr_valid_)) {
+      prev_ = cur_;
+      cur_ = h;
       frame_nr_update();
-      if (P + bstride > n) return out;
+      if (P_ + kBStride > n_) return event(-1, true);
       int64_t frames[kMk5bBlockFrames];
-      for (int i = 0; i < kMk5bBlockFrames; i++) frames[i] = P + i * fstride + kMk5bHeader;
-      P += bstride;
-      finish(frames);
-      continue;
+      for (int i = 0; i < kMk5bBlockFrames; i++) frames[i] = P_ + i * kFStride + kMk5bHeader;
+      P_ += kBStride;
+      return finish(frames);
     }
-    // resync_header (mark5b_reader.cc:254-327) on the bytes that follow the
-    // header, fetched once: the scan reads at most 16 blocks plus one frame
-    // before it gives up, and a found block's eight frames after that
+    resync(P_ + kMk5bHeader);
+  }
+
+  // get_bytes_s without a buffer on a file: nothing once the data has run
+  // out, else the whole skip (a seek may pass the end)
+  int64_t skip(int64_t bytes) {
+    if (ended_) return 0;
+    P_ += bytes;
+    return bytes;
+  }
+  int frame_nr() const { return (int)cur_.frame_nr; }
+  int64_t position() const { return P_; }
+
+  // resync_header (mark5b_reader.cc:254-327) from recording offset q, on the
+  // bytes that follow, fetched once: the scan reads at most 16 blocks plus
+  // one frame before it gives up, and a found block's eight frames after
+  // that.  Returns whether it found a block.
+  bool resync(int64_t q) {
     const int max_read = 16 * kMk5bBlock;
     FetchedBytes r;
-    r.n = n;
-    r.base = r.pos = P + kMk5bHeader;
-    const int64_t span = std::min<int64_t>(n - r.base, 16 + max_read + 2 * kMk5bFrame + bstride);
+    r.n = n_;
+    r.base = r.pos = q;
+    const int64_t span = std::min<int64_t>(n_ - r.base, 16 + max_read + 2 * kMk5bFrame + kBStride);
     r.b.resize((size_t)std::max<int64_t>(span, 0));
-    if (span > 0) src.fetch(r.base, span, r.b.data());
+    if (span > 0) src_.fetch(r.base, span, r.b.data());
     std::vector<uint8_t> buf(kMk5bFrame, 0);
     int total = 0;
-    bool found = false, resynced = false;
+    bool found = false;
     r.get(kMk5bHeader, buf.data());
     while (total < max_read && !r.short_read) {
       const int64_t bstart = r.pos;  // recording offset of buf[16]
@@ -605,8 +647,8 @@ FrameWalk walk_mk5b(const ReaderParams &p, FrameSource &src) {
       if (r.short_read) break;
       total += frame_start;
       if ((t.flags & FRAME_CHECK) && t.frame_nr % kMk5bBlockFrames == 0) {
-        prev = cur;
-        cur = t;
+        prev_ = cur_;
+        cur_ = t;
         int64_t frames[kMk5bBlockFrames] = {frame0};
         for (int i = 1; i < kMk5bBlockFrames; i++) {
           r.get(kMk5bHeader, nullptr);
@@ -615,25 +657,330 @@ FrameWalk walk_mk5b(const ReaderParams &p, FrameSource &src) {
         }
         if (r.short_read) break;
         frame_nr_update();
-        P = r.pos;
+        P_ = r.pos;
         finish(frames);
-        resynced = true;
-        break;
+        return true;
       }
     }
-    if (!resynced) return out;
+    if (r.short_read) {
+      event(-1, true);
+      return false;
+    }
+    P_ = r.pos;  // no block within the search limit; the next read starts where this one stopped
+    event(-1, false);
+    return false;
   }
+
+ private:
+  static constexpr int64_t kFStride = kMk5bHeader + kMk5bFrame, kBStride = kMk5bBlockFrames * kFStride;
+  const ReaderParams &p_;
+  FrameSource &src_;
+  int64_t n_ = 0, tbh_ = 0, P_ = 0, g0_ = -1;
+  int current_jday_ = 0, bitstreams_ = 0, sample_rate_ = 0, frame_nr_ = -1;
+  bool frame_nr_valid_ = true;
+  FrameInfo cur_{}, prev_{};
+  std::vector<FrameInfo> grid_;
+
+  void frame_nr_update() {  // mark5b_reader.cc:127-131
+    if (bitstreams_ == 64 && cur_.seconds == prev_.seconds && frame_nr_ > (int)cur_.frame_nr)
+      frame_nr_ = (int)cur_.frame_nr + 32768;
+    else
+      frame_nr_ = (int)cur_.frame_nr;
+  }
+  void finish(const int64_t *frames) {  // the julian-day step, then the block's time
+    if (cur_.thread != current_jday_ % 1000) current_jday_++;
+    FrameBlock b;
+    b.start_ticks = now(true);
+    b.size = kMk5bBlock;
+    b.frame_bytes = kMk5bFrame;
+    b.first = (int64_t)out.frames.size();
+    b.nframes = kMk5bBlockFrames;
+    out.frames.insert(out.frames.end(), frames, frames + kMk5bBlockFrames);
+    out.blocks.push_back(std::move(b));
+    event((int32_t)out.blocks.size() - 1, false);
+  }
+};
+
+std::unique_ptr<Walker> make_walker(const ReaderParams &p, FrameSource &src) {
+  if (p.bits_per_sample != 1 && p.bits_per_sample != 2) throw std::invalid_argument("bits per sample must be 1 or 2");
+  if (p.tracks_per_channel < p.bits_per_sample) throw std::invalid_argument("fewer tracks than bits per sample");
+  if (p.track_bit_rate <= 0) throw std::invalid_argument("track bit rate must be positive");
+  if (p.format == FORMAT_VDIF) return std::unique_ptr<Walker>(new VdifWalker(p, src));
+  if (p.format == FORMAT_MARK5B) return std::unique_ptr<Walker>(new Mk5bWalker(p, src));
+  throw std::invalid_argument("unknown recording format");
 }
 
 }  // namespace
 
 FrameWalk walk_frames(const ReaderParams &p, FrameSource &src) {
-  if (p.bits_per_sample != 1 && p.bits_per_sample != 2) throw std::invalid_argument("bits per sample must be 1 or 2");
-  if (p.tracks_per_channel < p.bits_per_sample) throw std::invalid_argument("fewer tracks than bits per sample");
-  if (p.track_bit_rate <= 0) throw std::invalid_argument("track bit rate must be positive");
-  if (p.format == FORMAT_VDIF) return walk_vdif(p, src);
-  if (p.format == FORMAT_MARK5B) return walk_mk5b(p, src);
-  throw std::invalid_argument("unknown recording format");
+  std::unique_ptr<Walker> w = make_walker(p, src);
+  while (!w->ended()) w->read();
+  return std::move(w->out);
+}
+
+// ---- Input_data_format_reader_tasklet over a walker
+int64_t reader_tbh(const ReaderParams &p) {
+  // time_between_headers (vdif_reader.cc:211-222, mark5b_reader.cc:245-247), as Time(usec) rounds it
+  const double sample_rate = (double)p.track_bit_rate * (p.tracks_per_channel / p.bits_per_sample);
+  double usec;
+  if (p.format == FORMAT_VDIF) {
+    if (p.n_tracks == 0)
+      usec = p.frame_size * 8.e6 / (sample_rate * p.bits_per_sample);
+    else
+      usec = std::max(1, 32128 / p.frame_size) * p.frame_size * 8.e6 / (sample_rate * p.n_tracks);
+  } else {
+    const int word = p.n_tracks <= 32 ? 4 : 8;
+    usec = (double)kMk5bBlock / (word * p.track_bit_rate / 1000000);
+  }
+  return ticks_of_usec(usec);
+}
+
+namespace {
+constexpr int kSkipFrames = 16;   // NSKIP (input_data_format_reader_tasklet.cc:2)
+constexpr int kSkewFrames = 128;  // NSKEW (input_data_format_reader_tasklet.cc:3)
+
+// The tasklet's current frame (input_element_): the walk block last read
+// into its buffer, its invalid runs, and whether its bytes are not a
+// block's (a new buffer, or a read that failed into it: the reference pushes
+// such bytes as they are, here they go out wholly invalid).
+struct Element {
+  int64_t start = 0;
+  int channel = 0;
+  int32_t block = -1;
+  bool stale = true, whole = false;
+  std::vector<int32_t> runs;
+};
+
+class Tasklet {
+ public:
+  Tasklet(const ReaderParams &p, Walker &w) : w_(w), tbh_(reader_tbh(p)) {
+    if (tbh_ <= 0) throw std::invalid_argument("no time between frame headers");
+    mk5b_ = p.format == FORMAT_MARK5B;
+    not_open_time_ = mk5b_ ? 0 : -p.offset_ticks;
+    thread_mode_ = p.format == FORMAT_VDIF && p.n_tracks == 0;
+    // set_parameters (input_data_format_reader_tasklet.cc:262-297)
+    const int nt = thread_mode_ ? (int)p.first_track.size() : 1;
+    current_.assign(nt, 0);
+    left_.assign(nt, 0);
+    dup_.assign(nt, {});
+    if (thread_mode_)
+      for (int i = 0; i < nt; i++)
+        for (int j = 0; j < nt; j++)
+          if (j != i && p.first_track[j] == p.first_track[i]) dup_[i].push_back(j);
+  }
+
+  std::vector<ScheduledBlock> run(const std::vector<TimeInterval> &intervals) {
+    // do_execute (33-47): an empty interval (stop <= start) ends it
+    size_t next = 0;
+    auto fetch = [&]() -> bool {
+      if (next >= intervals.size() || intervals[next].stop <= intervals[next].start) return false;
+      fetch_interval(intervals[next++]);
+      return true;
+    };
+    if (!fetch()) return out_;
+    for (long guard = 0;; guard++) {
+      if (guard > 50000000L) throw std::runtime_error("reader tasklet did not finish its intervals");
+      if (*std::min_element(current_.begin(), current_.end()) < iv_.stop) {
+        do_task();
+      } else if (!fetch()) {
+        return out_;
+      }
+    }
+  }
+
+ private:
+  Walker &w_;
+  int64_t tbh_, not_open_time_ = 0;
+  bool mk5b_ = false, thread_mode_ = false, open_ = false;
+  TimeInterval iv_{};
+  std::vector<int64_t> current_;
+  std::vector<int> left_;
+  int min_left_ = 0;
+  std::vector<std::vector<int>> dup_;
+  Element e_;
+  std::vector<ScheduledBlock> out_;
+
+  int64_t times(int64_t nframes) const { return (int64_t)std::round((double)tbh_ * (double)nframes); }
+  int frames_between(int64_t a, int64_t b) const { return (int)((double)(b - a) / (double)tbh_); }
+  int64_t reader_now(bool apply = false) { return open_ ? w_.now(apply) : not_open_time_; }
+
+  // read_new_block into the element: VDIF appends the block's invalid runs
+  // to the frame's, Mark5B replaces them (mark5b_reader.cc:157-160)
+  bool read() {
+    w_.read();
+    const ReadEvent &ev = w_.out.reads.back();
+    if (ev.block < 0) {
+      e_.stale = true;
+      return false;
+    }
+    const FrameBlock &b = w_.out.blocks[(size_t)ev.block];
+    e_.block = ev.block;
+    e_.stale = false;
+    e_.start = open_ ? b.start_ticks : not_open_time_;
+    e_.channel = thread_mode_ ? b.channel : 0;
+    if (mk5b_) {
+      e_.whole = false;
+      e_.runs.clear();
+    } else {
+      e_.runs.insert(e_.runs.end(), b.invalid.begin(), b.invalid.end());
+    }
+    return true;
+  }
+  void randomize() {  // randomize_block (342-370): the frame wholly invalid
+    e_.whole = true;
+    e_.runs.clear();
+  }
+  bool open_stream() {  // open_input_stream
+    if (!read()) return false;
+    open_ = true;
+    e_.start = w_.out.blocks[(size_t)e_.block].start_ticks;
+    return true;
+  }
+  int64_t goto_time(int64_t t) {
+    if (!mk5b_) {  // VDIF_reader::goto_time (vdif_reader.cc:51-57)
+      while (t > reader_now())
+        if (!read()) break;
+      return reader_now();
+    }
+    // Mark5b_reader::goto_time on a file (mark5b_reader.cc:44-84): skip a
+    // second's blocks at a time, then the rest, reading the last block of each step
+    Mk5bWalker &m = static_cast<Mk5bWalker &>(w_);
+    const int64_t one_sec = 512000000;
+    if (t > reader_now(true)) {
+      int64_t delta = t - reader_now(true);
+      while (delta >= one_sec) {
+        const int64_t nb = (int64_t)((double)one_sec / (double)tbh_);
+        const int64_t bytes = (nb - 1) * kMk5bBlockFrames * (kMk5bHeader + kMk5bFrame);
+        if (m.skip(bytes) != bytes) return reader_now(true);
+        read();
+        delta = t - reader_now(true);
+      }
+      const int nb = (int)std::round((double)delta / (double)tbh_);
+      if (nb > 0) {
+        const int64_t bytes = (int64_t)(nb - 1) * kMk5bBlockFrames * (kMk5bHeader + kMk5bFrame);
+        if (m.skip(bytes) != bytes) return reader_now(true);
+        read();
+        if (m.frame_nr() % kMk5bBlockFrames != 0) {
+          // the reader returns resync_header's result as a time: 0 or 1 microsecond
+          const size_t before = w_.out.blocks.size();
+          const bool ok = m.resync(m.position());
+          if (ok && w_.out.blocks.size() > before) e_.block = (int32_t)before;
+          return ok ? ticks_of_usec(1.0) : 0;
+        }
+      }
+    }
+    return reader_now(true);
+  }
+
+  void push() {  // push_element (324-337)
+    const int c = e_.channel;
+    // a filled-in frame keeps the runs reads appended to it after (0, size)
+    const bool whole = e_.whole || e_.stale || e_.block < 0;
+    out_.push_back(ScheduledBlock{e_.start, c, e_.block, whole,
+                                  (whole && (e_.stale || !e_.whole)) ? std::vector<int32_t>() : e_.runs});
+    current_[c] += tbh_;
+    left_[c]--;
+    if (left_[c] < min_left_) min_left_ = left_[c];
+  }
+  void push_random(int n, int c) {  // push_random_blocks (230-240)
+    for (int i = 0; i < n; i++) {
+      randomize();
+      e_.start = current_[c];
+      e_.channel = c;
+      push();
+    }
+  }
+
+  // fetch_next_time_interval (175-228)
+  void fetch_interval(const TimeInterval &iv) {
+    iv_ = iv;
+    if (!open_ && !open_stream()) {
+      for (size_t i = 0; i < current_.size(); i++) {
+        current_[i] = iv.start;
+        left_[i] = frames_between(current_[i], iv.stop);
+      }
+      min_left_ = left_[0];
+      return;
+    }
+    int64_t t;
+    if (iv.start <= e_.start) {
+      t = iv.start + times((int64_t)std::round((double)(e_.start - iv.start) / (double)tbh_));
+    } else {
+      e_.start = goto_time(iv.start);  // the element takes the reader's time
+      t = iv.start + times((int64_t)std::round((double)(e_.start - iv.start) / (double)tbh_));
+      if (t < iv.start) t = iv.start;
+    }
+    if (t > iv.stop) {
+      t = iv.stop - tbh_;
+      randomize();
+      e_.start = t;
+      e_.channel = 0;
+    }
+    for (size_t i = 0; i < current_.size(); i++) {
+      current_[i] = t;
+      left_[i] = frames_between(current_[i], iv.stop);
+    }
+    min_left_ = left_[0];
+    push();
+  }
+
+  // do_task (49-160)
+  void do_task() {
+    e_ = Element();  // allocate_element
+    if (w_.ended()) {  // the data reader is at its end
+      for (size_t i = 0; i < current_.size(); i++)
+        if (current_[i] < iv_.stop) push_random(1, (int)i);
+      return;
+    }
+    for (size_t i = 0; i < current_.size(); i++) {
+      const int skew = std::max(0, std::min(2 * kSkewFrames, left_[i] - 1));
+      if (left_[i] > min_left_ + skew) {
+        push_random((left_[i] - min_left_) - skew, (int)i);
+        return;
+      }
+    }
+    if (!read()) {
+      push_random(std::min(kSkipFrames, left_[0]), 0);
+      return;
+    }
+    const int c = e_.channel;
+    if (c < 0 || c >= (int)current_.size()) throw std::runtime_error("block of a channel outside the channel list");
+    if (current_[c] >= iv_.leave) {
+      push_random(std::min(kSkipFrames, left_[0]), c);
+      return;
+    }
+    const int64_t expected = current_[c];
+    if (e_.start != expected) {
+      int64_t missing = (int64_t)((double)(e_.start - expected) / (double)tbh_);
+      missing = std::min(missing, (int64_t)left_[c]);
+      // (the reference also drops a frame from more than 5 s after the host's
+      // clock, a causality check on live data; recorded data is in the past)
+      if (missing > 0) {
+        const Element keep = e_;
+        push_random((int)missing, c);
+        e_ = keep;
+      } else if (missing < 0) {
+        return;  // data from the past: dropped
+      }
+      if (missing >= left_[c]) return;
+    }
+    if (e_.start != current_[c]) throw std::runtime_error("reader block off its channel's time grid");
+    push();
+    for (int j : dup_[c]) {
+      e_.channel = j;
+      push();
+    }
+  }
+};
+}  // namespace
+
+Schedule schedule_blocks(const ReaderParams &p, FrameSource &src, const std::vector<TimeInterval> &intervals) {
+  std::unique_ptr<Walker> w = make_walker(p, src);
+  Tasklet t(p, *w);
+  Schedule s;
+  s.blocks = t.run(intervals);
+  s.walk = std::move(w->out);
+  return s;
 }
 
 std::unique_ptr<FormatReader> FormatReader::create(const ReaderParams &p, const uint8_t *bytes, size_t n) {

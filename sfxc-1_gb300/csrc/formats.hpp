@@ -79,15 +79,62 @@ struct FrameBlock {
   int32_t nframes = 0;
   std::vector<int32_t> invalid;
 };
+// One read_new_block call of the reader: the block it returned (an index
+// into FrameWalk::blocks) or -1 when it failed, whether the data ran out,
+// and the reader's get_current_time() after it, as it reads once the reader
+// is open.
+struct ReadEvent {
+  int32_t block;
+  bool eof;
+  int64_t time;
+};
 struct FrameWalk {
   std::vector<FrameBlock> blocks;
   std::vector<int64_t> frames;  // payload offsets in the recording, block after block
+  std::vector<ReadEvent> reads;  // every read until the data runs out (the last one)
 };
 
-// Every block FormatReader::create(p, ...)->next() returns for the
-// recording, in order.  One difference: where a truncated Mark5B recording
-// ends inside a resync, the reader may still return one block whose bytes
-// are partly left over from the previous block; the walk ends before it.
+// The reader's successive read_new_block calls over the whole recording:
+// the blocks are those FormatReader::create(p, ...)->next() returns, in
+// order, and a failed read (more than 256 frames skipped, a Mark5B resync
+// that found nothing) is followed by the reads after it, as the reader
+// continues.  Differences from the reader: where a truncated Mark5B
+// recording ends inside a resync, the reader may still return one block
+// whose bytes are partly left over from the previous block (the walk ends
+// before it); where the data ends inside a frame header, the reader mixes
+// the partial header into its current one, so its time after that read (the
+// walk keeps the last whole header's) is not defined by the data.
 FrameWalk walk_frames(const ReaderParams &p, FrameSource &src);
+
+// ---- The reader tasklet (Input_data_format_reader_tasklet,
+// sfxc/src/input_data_format_reader_tasklet.cc:33-260) over a walk: for
+// each time interval (start, stop, leave), the blocks it pushes to the
+// channel extractor, with the blocks of missing frames, of data that ended
+// or of streams that fell behind filled in as wholly invalid blocks.
+struct TimeInterval {
+  int64_t start, stop, leave;
+};
+struct ScheduledBlock {
+  int64_t start_ticks;
+  int channel;
+  int32_t block;       // the walk block whose bytes it carries (index into FrameWalk::blocks), or -1
+  bool whole_invalid;  // filled in, or its bytes are not a block's (a read failed into them)
+  // VDIF: its invalid runs, as the reader appended them to the tasklet's
+  // frame (a frame read again by goto_time keeps the runs it had), after
+  // (0, size) when whole_invalid; Mark5B: empty, the block's fill-pattern
+  // runs apply
+  std::vector<int32_t> invalid;
+};
+// The reads the tasklet makes (walk: its blocks and reads, which with
+// Mark5B's skips to a later time are not all of the recording's) and the
+// blocks it pushes.  Throws std::runtime_error where the reference asserts
+// (a block off its channel's time grid) or would not finish.
+struct Schedule {
+  FrameWalk walk;
+  std::vector<ScheduledBlock> blocks;
+};
+Schedule schedule_blocks(const ReaderParams &p, FrameSource &src, const std::vector<TimeInterval> &intervals);
+// the reader's time between block headers (time_between_headers), in ticks
+int64_t reader_tbh(const ReaderParams &p);
 
 }  // namespace sfxc

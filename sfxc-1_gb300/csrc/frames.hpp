@@ -20,6 +20,10 @@ namespace sfxc {
 constexpr uint32_t kFillWord = 0x11223344u;  // MARK5_FILLPATTERN (sfxc/include/utils.h:45)
 constexpr int kFillRunWords = 65528 / 4;     // MARK5_FILLPATTERN_NWORDS (sfxc/include/utils.h:47)
 constexpr uint32_t kMk5bSync = 0xABADDEEDu;
+constexpr int kMk5bFrame = 2500 * 4;  // payload bytes: SIZE_MK5B_FRAME words of SIZE_MK5B_WORD bytes
+constexpr int kMk5bHeader = 4 * 4;    // SIZE_MK5B_HEADER words
+constexpr int kMk5bBlockFrames = 8;   // N_MK5B_BLOCKS_TO_READ
+constexpr int kMk5bBlock = kMk5bBlockFrames * kMk5bFrame;
 
 enum : uint32_t {
   FRAME_FILL = 1,     // VDIF: one of header words 0-3 is the fill word

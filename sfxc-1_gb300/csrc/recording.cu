@@ -36,7 +36,8 @@ __global__ void decode_frames_kernel(const uint8_t *__restrict__ rec, int64_t po
 }
 
 // The 32-bit words of one reader block: nf frames of wpf words at the
-// recording offsets frames[0..nf), zeros after them.
+// recording offsets frames[0..nf), zeros after them.  (A frame offset of -1,
+// a block filled in for missing data, reads as zeros in every kernel here.)
 struct BlockWords {
   const uint8_t *rec;
   const int64_t *frames;
@@ -79,7 +80,8 @@ __global__ void gather_blocks_kernel(const uint8_t *__restrict__ rec, const int6
     const int64_t e = j / block_size;
     const int r = (int)(j - e * block_size);
     const int f = r / fb;
-    out[j] = f < nf ? rec[frames[(int64_t)list[e] * nf + f] + (r - f * fb)] : (uint8_t)0;
+    const int64_t off = f < nf ? frames[(int64_t)list[e] * nf + f] : -1;
+    out[j] = off >= 0 ? rec[off + (r - f * fb)] : (uint8_t)0;
   }
 }
 
@@ -108,8 +110,9 @@ __global__ void __launch_bounds__(256) extract_frames_kernel(const uint8_t *__re
   uint64_t w[SPB];
 #pragma unroll
   for (int j = 0; j < SPB; j++) w[j] = 0;
-  const uint8_t *p = f < nf ? rec + frames[b * nf + f] + (byte - f * fb) : nullptr;
-  if (SPB == 4 && N == 4 && f == f_last && f < nf && ((uintptr_t)p & 15) == 0) {
+  const int64_t off = f < nf ? frames[b * nf + f] : -1;
+  const uint8_t *p = off >= 0 ? rec + off + (byte - f * fb) : nullptr;
+  if (SPB == 4 && N == 4 && f == f_last && p && ((uintptr_t)p & 15) == 0) {
     const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
     w[0] = v.x;
     w[1 % SPB] = v.y;
@@ -120,8 +123,9 @@ __global__ void __launch_bounds__(256) extract_frames_kernel(const uint8_t *__re
 #pragma unroll
     for (int j = 0; j < SPB; j++) {
       const int64_t wb = byte + j * N, fj = wb / fb;
-      if (fj < nf) {
-        const uint8_t *q = rec + frames[b * nf + fj] + (wb - fj * fb);
+      const int64_t offj = fj < nf ? frames[b * nf + fj] : -1;
+      if (offj >= 0) {
+        const uint8_t *q = rec + offj + (wb - fj * fb);
         for (int i = 0; i < N; i++) w[j] |= (uint64_t)q[i] << (8 * i);
       }
     }
@@ -174,8 +178,9 @@ __global__ void __launch_bounds__(256) extract_fields_kernel(const uint8_t *__re
   T w[NW];
 #pragma unroll
   for (int j = 0; j < NW; j++) w[j] = 0;
-  if (f < nf) {
-    const uint8_t *p = rec + frames[b * nf + f] + (byte - f * fb);
+  const int64_t off = f < nf ? frames[b * nf + f] : -1;
+  if (off >= 0) {
+    const uint8_t *p = rec + off + (byte - f * fb);
     if (sizeof(T) == 4 && N == 4 && NW % 4 == 0 && ((uintptr_t)p & 15) == 0) {
 #pragma unroll
       for (int v = 0; v < NW / 4; v++) {
@@ -217,8 +222,8 @@ __global__ void extract_frames_wide_kernel(const uint8_t *__restrict__ rec, cons
   const int64_t byte = (ob - b * opb) * (8 / fan_out) * N;
   const int64_t f = byte / fb;
   uint8_t v = 0;
-  if (f < nf)
-    v = extract_byte(rec + frames[b * nf + f] + (byte - f * fb), N, bits, fan_out, tracks + sb * fan_out);
+  const int64_t off = f < nf ? frames[b * nf + f] : -1;
+  if (off >= 0) v = extract_byte(rec + off + (byte - f * fb), N, bits, fan_out, tracks + sb * fan_out);
   out[(int64_t)sb * nout + ob] = v;
 }
 

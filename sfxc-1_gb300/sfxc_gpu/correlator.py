@@ -297,6 +297,12 @@ class DeviceRecording:
     def _check(self, rc):
         return self._node._check(rc)
 
+    def schedule(self, intervals):
+        """The reader tasklet's blocks for time intervals [(start, stop, leave)
+        ticks] instead of the reader's (sfxc_gpu_recording_schedule)."""
+        flat = (C.c_int64 * max(1, 3 * len(intervals)))(*[int(v) for iv in intervals for v in iv])
+        self._check(self._lib.sfxc_gpu_recording_schedule(self._h, len(intervals), flat))
+
     def n_blocks(self):
         return self._lib.sfxc_gpu_recording_n_blocks(self._h)
 

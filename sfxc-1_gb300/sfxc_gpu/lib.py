@@ -24,7 +24,7 @@ EXPORTS = [
     "sfxc_gpu_reader_create", "sfxc_gpu_reader_next", "sfxc_gpu_reader_destroy", "sfxc_gpu_extract_block",
     "sfxc_gpu_phasecal_create", "sfxc_gpu_phasecal_push", "sfxc_gpu_phasecal_destroy", "sfxc_gpu_set_uvw",
     "sfxc_gpu_output_create", "sfxc_gpu_output_put_slice", "sfxc_gpu_output_finish", "sfxc_gpu_output_destroy",
-    "sfxc_gpu_recording_create", "sfxc_gpu_recording_n_blocks", "sfxc_gpu_recording_block",
+    "sfxc_gpu_recording_create", "sfxc_gpu_recording_schedule", "sfxc_gpu_recording_n_blocks", "sfxc_gpu_recording_block",
     "sfxc_gpu_recording_extract", "sfxc_gpu_recording_channel", "sfxc_gpu_recording_protocol",
     "sfxc_gpu_recording_push", "sfxc_gpu_recording_destroy",
 ]
@@ -162,6 +162,7 @@ def load(path=None):
     lib.sfxc_gpu_recording_create.restype = C.c_void_p
     lib.sfxc_gpu_recording_create.argtypes = [C.c_void_p, C.POINTER(ReaderParams), C.c_void_p, C.c_size_t,
                                               C.c_int32]
+    lib.sfxc_gpu_recording_schedule.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]
     lib.sfxc_gpu_recording_n_blocks.restype = C.c_int32
     lib.sfxc_gpu_recording_n_blocks.argtypes = [C.c_void_p]
     lib.sfxc_gpu_recording_block.argtypes = [C.c_void_p, C.c_int32, C.POINTER(ReaderBlock), C.c_void_p]

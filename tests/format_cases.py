@@ -90,3 +90,56 @@ def cases():
                                    first_frame=3 * fpm),
         params=dict(ref_ticks=_ref_ticks(), **mk))
     return out
+
+
+def schedule_recordings():
+    """Recordings for the reader-tasklet tests besides cases(): a VDIF stream
+    with more than 256 fill frames in a row (a read that fails without the
+    data ending), and one thread per channel with two channels on one thread
+    and a thread that loses frames (skew)."""
+    out = {}
+    fps = 64_000_000 * 2 * 16 // (8000 * 8)
+    out["vdif_long_fill"] = dict(
+        fmt="vdif",
+        rec=synth.vdif_recording(300, payload_bytes=8000, frames_per_second=fps, start_mjd=MJD, start_sec_of_day=10,
+                                 log2_nchan=4, bits=2, fill=tuple(range(8, 8 + 270)), seed=9),
+        params=dict(ref_ticks=_ref_ticks(), track_bit_rate=64_000_000, frame_size=8000, n_tracks=32, bits=2,
+                    channel_tracks=_vdif_tracks(16, 2, 32)))
+    fpst = 16_000_000 * 2 // (1000 * 8)
+    out["vdif_threads_skew"] = dict(
+        fmt="vdif",
+        rec=synth.vdif_recording(60, payload_bytes=1000, frames_per_second=fpst, start_mjd=MJD, start_sec_of_day=200,
+                                 log2_nchan=0, bits=2, threads=(1, 2), drop=tuple(range(21, 41, 2)), seed=10),
+        params=dict(ref_ticks=_ref_ticks(), track_bit_rate=16_000_000, frame_size=1000, n_tracks=0, bits=2,
+                    channel_tracks=[[1, 0], [2, 0], [1, 0]]))
+    return out
+
+
+def schedule_cases(first_ticks, tbh):
+    """Time-interval sets (start, stop, leave ticks) of the reader-tasklet
+    tests, relative to a recording's first block time and frame spacing:
+    data starting inside the interval, a later interval (the reader skips
+    ahead), a leave time before the stop, intervals after the data ended and
+    before it started."""
+    t0, T = first_ticks, tbh
+    return {
+        "covering": [(t0 - 3 * T, t0 + 40 * T, t0 + 40 * T)],
+        "skip_ahead": [(t0 + 2 * T, t0 + 6 * T, t0 + 6 * T), (t0 + 9 * T, t0 + 14 * T, t0 + 14 * T)],
+        "leave_early": [(t0, t0 + 12 * T, t0 + 4 * T)],
+        "before_and_after": [(t0 - 20 * T, t0 - 16 * T, t0 - 16 * T), (t0 + 1 * T, t0 + 5 * T, t0 + 5 * T),
+                             (t0 + 400 * T, t0 + 404 * T, t0 + 404 * T)],
+    }
+
+
+def reader_tbh(c):
+    """The reader's time between block headers in ticks (VDIF_reader /
+    Mark5b_reader::set_parameters, as Time(usec) rounds it)."""
+    p = c["params"]
+    sr = p["track_bit_rate"] * (len(p["channel_tracks"][0]) // p["bits"])
+    if c["fmt"] == "vdif":
+        fs = p["frame_size"]
+        us = fs * 8e6 / (sr * p["bits"]) if p["n_tracks"] == 0 else \
+            max(1, 32128 // fs) * fs * 8e6 / (sr * p["n_tracks"])
+    else:
+        us = 80000 / ((4 if p["n_tracks"] <= 32 else 8) * p["track_bit_rate"] // 1000000)
+    return round(us * 512)

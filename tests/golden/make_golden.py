@@ -203,6 +203,60 @@ def make_formats():
     print("formats done")
 
 
+def make_schedule():
+    """Blocks the reference's reader tasklet (Input_data_format_reader_tasklet)
+    pushes for the recordings of tests/format_cases.py (cases() and
+    schedule_recordings()) and the interval sets of schedule_cases(): per
+    block the channel, start ticks, size, invalid runs and the SHA-256 of its
+    bytes -- null for a wholly invalid block, whose bytes are not defined, and
+    "shared" for a block pushed in the same data buffer as another block that
+    is not wholly invalid: the tasklet reads the next interval's first block
+    into the buffer of the last block it pushed, so that block's bytes depend
+    on whether its consumer took it first; "stale" for a block whose buffer
+    holds no block's bytes (the last read into it failed at the end of the
+    data, or none was made)."""
+    import json
+    sys.path.insert(0, os.path.dirname(HERE))
+    import format_cases
+    recs = dict(format_cases.cases(), **format_cases.schedule_recordings())
+    out = {}
+    for name, c in sorted(recs.items()):
+        first = jobs.reader(c["rec"], c["fmt"], max_blocks=1, **c["params"])
+        if not first:
+            continue
+        for iname, ivs in format_cases.schedule_cases(first[0]["start_ticks"], format_cases.reader_tbh(c)).items():
+            blocks = jobs.schedule(c["rec"], c["fmt"], intervals=ivs, **c["params"])
+            # each buffer's last push: its last block and the blocks of the
+            # other channels of that VDIF thread pushed right before it
+            last_push = set()
+            seen = set()
+            for i in range(len(blocks) - 1, -1, -1):
+                b = blocks[i]
+                if b["data"] is None or b["buffer"] in seen:
+                    continue
+                seen.add(b["buffer"])
+                k = i
+                while k >= 0 and blocks[k]["buffer"] == b["buffer"] and blocks[k]["start_ticks"] == b["start_ticks"] \
+                        and (k == i or blocks[k]["channel"] != blocks[k + 1]["channel"]):
+                    last_push.add(k)
+                    k -= 1
+
+            def digest(i, b):
+                if b["data"] is None:
+                    return None
+                if i not in last_push:
+                    return "shared"  # pushed before its buffer was read into again
+                return "stale" if b["stale"] else hashlib.sha256(b["data"]).hexdigest()
+            out[name + "/" + iname] = {
+                "recording_sha256": hashlib.sha256(c["rec"]).hexdigest(), "intervals": [list(v) for v in ivs],
+                "blocks": [{"channel": b["channel"], "start_ticks": b["start_ticks"], "size": b["size"],
+                            "sha256": digest(i, b), "invalid": [list(r) for r in b["invalid"]]}
+                           for i, b in enumerate(blocks)]}
+            print(name, iname, len(blocks), "blocks")
+    with open(os.path.join(HERE, "schedule.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+
+
 def make_phasecal():
     """Phase-cal messages of the reference's Input_node_data_writer for
     phasecal_cases(): per case the SHA-256 of each message, in order."""
@@ -257,6 +311,7 @@ if __name__ == "__main__":
     make_output_header()
     make_phasecal()
     make_formats()
+    make_schedule()
     make_extract()
     for name, sc in scenarios().items():
         make(name, sc)

@@ -81,25 +81,31 @@ def walk_driver(tmp_path_factory):
     return exe
 
 
-def walk_blocks(exe, tmp_path, c):
+def walk_blocks(exe, tmp_path, c, intervals=()):
     """Blocks of the frame walker (walk_frames over headers decoded by the
-    device decode's functions, bytes assembled from the frame offsets)."""
+    device decode's functions, bytes assembled from the frame offsets), or
+    with time intervals the blocks the reader tasklet pushes (data None for a
+    wholly invalid block)."""
     rec = tmp_path / "rec"
     rec.write_bytes(bytes(c["rec"]))
     pr = c["params"]
     ct = pr["channel_tracks"]
     args = [exe, str(rec), str(tmp_path / "out"), "0" if c["fmt"] == "vdif" else "1", str(pr["ref_ticks"]),
             str(pr.get("offset_ticks", 0)), str(pr["track_bit_rate"]), str(pr.get("frame_size", 0)),
-            str(pr["n_tracks"]), str(pr["bits"]), str(len(ct[0]))] + [str(t[0]) for t in ct]
+            str(pr["n_tracks"]), str(pr["bits"]), str(len(ct[0])), str(len(intervals))]
+    args += [str(v) for iv in intervals for v in iv] + [str(t[0]) for t in ct]
     lines = subprocess.run(args, capture_output=True, text=True, check=True).stdout.split("\n")
     data = (tmp_path / "out").read_bytes()
     blocks, off = [], 0
     for line in filter(None, lines):
         v = list(map(int, line.split()))
         ch, start, size, nr = v[:4]
-        blocks.append({"channel": ch, "start_ticks": start, "data": data[off:off + size],
-                       "invalid": [(v[4 + 2 * i], v[5 + 2 * i]) for i in range(nr)]})
-        off += size
+        inv = [(v[4 + 2 * i], v[5 + 2 * i]) for i in range(nr)]
+        whole = bool(intervals) and any(b == 0 and n >= size for b, n in inv)
+        blocks.append({"channel": ch, "start_ticks": start, "size": size, "invalid": inv,
+                       "data": None if whole else data[off:off + size]})
+        if not whole:
+            off += size
     return blocks
 
 
@@ -109,3 +115,42 @@ def test_frame_walk_matches_reference_blocks(name, walk_driver, tmp_path):
     the device-resident recording path) give the reference readers' blocks."""
     c = CASES[name]
     assert _summary(walk_blocks(walk_driver, tmp_path, c)) == GOLDEN[name]["blocks"]
+
+
+SCHEDULE = json.load(open(os.path.join(HERE, "golden", "schedule.json")))
+SCHED_RECS = dict(CASES, **format_cases.schedule_recordings())
+
+
+def _sched_summary(blocks):
+    return [{"channel": b["channel"], "start_ticks": b["start_ticks"], "size": b["size"],
+             "sha256": None if b["data"] is None else hashlib.sha256(b["data"]).hexdigest(),
+             "invalid": [list(r) for r in b["invalid"]]} for b in blocks]
+
+
+@pytest.mark.parametrize("key", sorted(SCHEDULE))
+def test_reader_tasklet_matches_reference(key, walk_driver, tmp_path):
+    """The reader tasklet's time-interval scheduling over the walk (missing
+    frames, data ending or starting inside an interval, skipping ahead, leave
+    times, a read failing without the data ending, skewed and shared VDIF
+    threads) pushes the blocks the reference's tasklet pushes, wholly invalid
+    blocks where it fills in."""
+    name = key.split("/")[0]
+    c = SCHED_RECS[name]
+    g = SCHEDULE[key]
+    assert hashlib.sha256(c["rec"]).hexdigest() == g["recording_sha256"], "recording generator changed"
+    got = _sched_summary(walk_blocks(walk_driver, tmp_path, c, [tuple(v) for v in g["intervals"]]))
+    # the reference's bytes of a block pushed in a data buffer that a later
+    # block reuses depend on whether its consumer took it first: every field
+    # but those bytes is compared there.  A block whose buffer holds no
+    # block's bytes (a read that failed at the end of the data left part of a
+    # frame over older bytes) goes out wholly invalid here: its channel, time
+    # and size are compared.
+    size = g["blocks"][0]["size"] if g["blocks"] else 0
+    want = []
+    for i, b in enumerate(g["blocks"]):
+        if b["sha256"] == "shared":
+            b = dict(b, sha256=got[i]["sha256"] if i < len(got) and got[i]["sha256"] is not None else "own")
+        elif b["sha256"] == "stale":
+            b = dict(b, sha256=None, invalid=[[0, size]])
+        want.append(b)
+    assert got == want

@@ -322,3 +322,79 @@ def test_device_recording_errors(gpu_node):
     with pytest.raises(lib.SfxcError):  # 8000-byte frames are not whole 3-byte words
         r.extract(3, 2, [[1, 0]])
     r.close()
+
+
+# ---- the reader tasklet's scheduling (gap filling) on the device recording
+SCHEDULE = json.load(open(os.path.join(HERE, "golden", "schedule.json")))
+
+
+@pytest.mark.parametrize("key", sorted(SCHEDULE))
+def test_device_schedule_matches_reference_tasklet(key, gpu_node):
+    """The blocks the reference's reader tasklet pushes for the fixture
+    recordings and time intervals (filled-in blocks for missing frames, data
+    ending or starting inside an interval, skips, leave times, failed reads,
+    skewed and shared VDIF threads), from the device recording.  Bytes the
+    reference's run leaves to its consumer's timing ("shared") or to a failed
+    read ("stale": wholly invalid here) are compared as the CPU test does."""
+    from sfxc_gpu import correlator
+    name = key.split("/")[0]
+    c = dict(format_cases.cases(), **format_cases.schedule_recordings())[name]
+    g = SCHEDULE[key]
+    r = correlator.DeviceRecording(gpu_node, c["rec"], c["fmt"], **c["params"])
+    r.schedule([tuple(v) for v in g["intervals"]])
+    got = []
+    for b in r.blocks():
+        whole = any(x == 0 and n >= len(b["data"]) for x, n in b["invalid"])
+        got.append({"channel": b["channel"], "start_ticks": b["start_ticks"], "size": len(b["data"]),
+                    "sha256": None if whole else hashlib.sha256(b["data"]).hexdigest(),
+                    "invalid": [list(x) for x in b["invalid"]]})
+    r.close()
+    size = g["blocks"][0]["size"] if g["blocks"] else 0
+    want = []
+    for i, b in enumerate(g["blocks"]):
+        if b["sha256"] == "shared":
+            b = dict(b, sha256=got[i]["sha256"] if i < len(got) and got[i]["sha256"] is not None else "own")
+        elif b["sha256"] == "stale":
+            b = dict(b, sha256=None, invalid=[[0, size]])
+        want.append(b)
+    assert got == want
+
+
+def test_vdif_dropped_block_filled_on_device(gpu_node):
+    """Station 1's recording loses a whole block of frames (block 2, frames
+    8-11): the device front end's reader tasklet fills it in, and the
+    protocols and correlation equal the job whose block 2 of station 1 is
+    invalid."""
+    from sfxc_gpu import correlator, scenario, synth, timebase
+    runs = lambda st: {(st[1].number, "R"): [(2, 0, 2000)], (st[1].number, "L"): [(2, 0, 2000)]}  # noqa: E731
+    sc, job, chans, nsamp = _job_and_streams(dict(block_bytes=2000, runs=runs))
+    frame = 32 + 8000
+    recs = []
+    for si in range(len(sc.stations)):
+        rec = synth.vdif_file_bytes(_words(chans, si, nsamp, 300 + si), payload_bytes=8000, sample_rate=sc.sample_rate,
+                                    nchan=16, bits=2, start_mjd=sc.mjd, start_sec_of_day=sc.sec0)
+        if si == 1:
+            rec = rec[:8 * frame] + rec[12 * frame:]
+        recs.append(rec)
+    nblocks = len(recs[0]) // frame // 4
+    rec0 = timebase.ticks_from_mjd_sec(sc.mjd, sc.sec0)
+    tbh = 128000  # 4 frames of 2000 samples per channel at 32 Ms/s
+    dels = scenario.del_tables(sc)
+    _, start, tint, slice_samples = scenario.job_timing(sc)
+    protos, objs = [], []
+    for si in range(len(sc.stations)):
+        r = correlator.DeviceRecording(gpu_node, recs[si], "vdif", ref_ticks=timebase.ticks_from_mjd_sec(sc.mjd, 0.0),
+                                       track_bit_rate=sc.sample_rate, frame_size=8000, n_tracks=32, bits=2,
+                                       channel_tracks=TRACKS16)
+        r.schedule([(rec0, rec0 + nblocks * tbh, rec0 + nblocks * tbh)])
+        assert r.n_blocks() == nblocks
+        r.extract(4, 2, [TRACKS16[0], TRACKS16[1]])
+        slices = [(start, start + tint, slice_samples, correlator.delay_list(dels[si], start, start + tint,
+                                                                              sc.sample_rate, sc.bits))]
+        for c, pol in enumerate(sc.pols):
+            protos.append(r.protocol(c, slices, sc.sample_rate, sc.bits, sc.integration_us))
+        objs.append(r)
+    assert protos == [[bytes(x) for x in p] for p in job["protocols"]]
+    cor_direct, tsys_direct = gpu_node.correlate(job)
+    cor_dev, tsys_dev = _correlate_pushed(gpu_node, job, objs, len(sc.pols))
+    assert cor_dev == cor_direct and tsys_dev == tsys_direct
