@@ -387,6 +387,21 @@ int sfxc_gpu_recording_push(sfxc_gpu_recording *rec, int32_t channel, int32_t sl
                             int32_t stream);
 void sfxc_gpu_recording_destroy(sfxc_gpu_recording *rec);
 
+/* The UVW model of a station (Uvw_model, sfxc/src/uvw_model.cc:79-330): u, v
+ * and w (metres) of a phase centre at a time, from the u, v, w columns of the
+ * station's .del file (Akima splines over the six whole seconds around the
+ * time, rebuilt when a later time leaves the current second, as the
+ * reference's get_uvw does) -- the values Correlator_node::set_parameters
+ * evaluates at each integration's mid-time for sfxc_gpu_set_uvw
+ * (sfxc/src/correlator_node.cc:327-357).  Host only, no GPU needed.  NULL on
+ * a table it cannot read (message from sfxc_gpu_global_error). */
+typedef struct sfxc_gpu_uvw_model sfxc_gpu_uvw_model;
+sfxc_gpu_uvw_model *sfxc_gpu_uvw_create(const uint8_t *del_bytes, size_t n);
+/* phase_center: the phase centre's index among the scans with the covering
+ * scan's start; uvw: 3 doubles.  SFXC_GPU_EINVAL beyond the table. */
+int sfxc_gpu_uvw_get(sfxc_gpu_uvw_model *model, int32_t phase_center, int64_t time_ticks, double *uvw);
+void sfxc_gpu_uvw_destroy(sfxc_gpu_uvw_model *model);
+
 /* Phase-cal extraction of one channel (Input_node_data_writer::do_phasecal,
  * sfxc/src/input_node_data_writer.cc:230-312, with its parameters from
  * Input_node_data_writer::set_parameters, 328-346): the channel's samples,

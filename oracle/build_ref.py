@@ -54,6 +54,7 @@ REF_SOURCES = [
     "src/input_data_format_reader.cc",
     "src/input_data_format_reader_tasklet.cc",
     "src/mark5a_reader.cc",
+    "src/uvw_model.cc",
     "src/data_reader.cc",
     "src/data_reader_file.cc",
     "src/data_reader_blocking.cc",

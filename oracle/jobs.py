@@ -190,6 +190,19 @@ def schedule(recording, fmt, *, ref_ticks, offset_ticks=0, track_bit_rate, frame
         return blocks
 
 
+def uvw(del_bytes, probes):
+    """The reference's Uvw_model over a .del file at probes [(phase centre,
+    ticks)], in order: [(u, v, w)].  Only the reference's own class implements
+    this (the library's restatement is what it pins)."""
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "st.del")
+        open(p, "wb").write(del_bytes)
+        lines = [("delfile", p)] + [("probe#%d" % k, pc, t) for k, (pc, t) in enumerate(probes)]
+        out = os.path.join(d, "uvw.txt")
+        _run("uvw", lines, out, d, "reference")
+        return [tuple(float(x) for x in line.split()) for line in open(out)]
+
+
 def correlate_lines(job, d, dump=False, precision=32, dump_bins=False):
     """The job file lines of the 'correlate' mode for a job dict, with its
     delay tables, protocols and mask files written into directory d (read by

@@ -37,6 +37,7 @@
 #include "input_node_tasklet.h"
 #include "data_reader_file.h"
 #include "input_data_format_reader_tasklet.h"
+#include "uvw_model.h"
 #include "mark5b_reader.h"
 #include "vdif_reader.h"
 #undef private
@@ -790,8 +791,27 @@ static int mode_schedule(Kv &kv, const std::string &od) {
   return 0;
 }
 
+// The reference's UVW model (Uvw_model, sfxc/src/uvw_model.cc) of one .del
+// file evaluated at probes, in order: u v w per line (%.17g).
+//   delfile <path> ; probe#k <phase centre> <ticks>
+static int mode_uvw(Kv &kv, const std::string &out) {
+  Uvw_model m;
+  m.open(get(kv, "delfile")[0].c_str());
+  FILE *f = std::fopen(out.c_str(), "w");
+  if (!f) die("cannot write " + out);
+  const int np = count_key(kv, "probe");
+  for (int k = 0; k < np; k++) {
+    const std::vector<std::string> &v = get(kv, idx("probe", k));
+    double u, vv, w;
+    m.get_uvw(std::atoi(v[0].c_str()), ticks_time(std::atoll(v[1].c_str())), &u, &vv, &w);
+    std::fprintf(f, "%.17g %.17g %.17g\n", u, vv, w);
+  }
+  std::fclose(f);
+  return 0;
+}
+
 int main(int argc, char **argv) {
-  if (argc != 4) die("usage: ref_harness correlate|delays|protocol|extract|reader|schedule <job> <out>");
+  if (argc != 4) die("usage: ref_harness correlate|delays|protocol|extract|reader|schedule|uvw <job> <out>");
   Kv kv = read_job(argv[2]);
   std::string m(argv[1]);
   if (m == "correlate") return mode_correlate(kv, argv[3]);
@@ -800,6 +820,7 @@ int main(int argc, char **argv) {
   if (m == "extract") return mode_extract(kv, argv[3]);
   if (m == "reader") return mode_reader(kv, argv[3]);
   if (m == "schedule") return mode_schedule(kv, argv[3]);
+  if (m == "uvw") return mode_uvw(kv, argv[3]);
   die("unknown mode " + m);
   return 2;
 }

@@ -2712,6 +2712,36 @@ int sfxc_gpu_recording_push(sfxc_gpu_recording *r, int32_t channel, int32_t slic
   }
 }
 
+// ---- the UVW model (host only)
+struct sfxc_gpu_uvw_model {
+  std::unique_ptr<UvwModel> m;
+};
+
+sfxc_gpu_uvw_model *sfxc_gpu_uvw_create(const uint8_t *del_bytes, size_t n) {
+  try {
+    if (!del_bytes || !n) throw Error(SFXC_GPU_EINVAL, "no delay table");
+    std::unique_ptr<sfxc_gpu_uvw_model> h(new sfxc_gpu_uvw_model());
+    h->m.reset(new UvwModel(DelayTable::parse(del_bytes, n)));
+    return h.release();
+  } catch (const Error &e) {
+    g_error = e.msg;
+    return nullptr;
+  }
+}
+
+int sfxc_gpu_uvw_get(sfxc_gpu_uvw_model *h, int32_t phase_center, int64_t time_ticks, double *uvw) {
+  if (!h || !uvw) return SFXC_GPU_EINVAL;
+  try {
+    h->m->get(phase_center, time_ticks, uvw);
+    return SFXC_GPU_OK;
+  } catch (const Error &e) {
+    g_error = e.msg;
+    return SFXC_GPU_EINVAL;
+  }
+}
+
+void sfxc_gpu_uvw_destroy(sfxc_gpu_uvw_model *h) { delete h; }
+
 // ---- batches: the next integration of several jobs in one CUDA graph
 struct sfxc_gpu_batch {
   std::vector<sfxc_gpu_ctx *> ctx;

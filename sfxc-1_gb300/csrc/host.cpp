@@ -59,6 +59,9 @@ DelayTable DelayTable::parse(const uint8_t *p, size_t n) {
         break;
       }
       t.times.push_back(line[0] - scan_start);
+      t.us.push_back(line[1]);
+      t.vs.push_back(line[2]);
+      t.ws.push_back(line[3]);
       t.delays.push_back(line[4]);
       t.phases.push_back(line[5]);
       t.amps.push_back(line[6]);
@@ -135,6 +138,13 @@ Spline Spline::create(const DelayTable &t, ticks_t start_, ticks_t duration, int
     ie = s.end;
     if (time_diff(ie, ib) < 4) ib = ie - time_mul(onesec, 4);
   }
+  const std::vector<double> *const cols[3] = {&t.delays, &t.phases, &t.amps};
+  return build(t, s, ib, ie, cols);
+}
+
+Spline Spline::build(const DelayTable &t, const Scan &s, ticks_t ib, ticks_t ie,
+                     const std::vector<double> *const cols[3]) {
+  const ticks_t onesec = time_from_usec(1000000.);
   Spline sp;
   sp.n = (int)((double)(ie - ib) / (double)onesec + 1);
   int idx = (int)time_diff(ib, s.begin);
@@ -142,7 +152,6 @@ Spline Spline::create(const DelayTable &t, ticks_t start_, ticks_t duration, int
   if (idx < 0 || idx + sp.n > s.nrows) throw Error(-3, "delay-table rows do not cover the spline interval");
   const int r0 = s.first_row + idx;
   sp.x.assign(t.times.begin() + r0, t.times.begin() + r0 + sp.n);
-  const std::vector<double> *cols[3] = {&t.delays, &t.phases, &t.amps};
   for (int k = 0; k < 3; k++) {
     sp.y[k].assign(cols[k]->begin() + r0, cols[k]->begin() + r0 + sp.n);
     sp.b[k].resize(sp.n);
@@ -157,6 +166,61 @@ Spline Spline::create(const DelayTable &t, ticks_t start_, ticks_t duration, int
   sp.clock_offset = t.clock_offset;
   sp.clock_rate = t.clock_rate;
   return sp;
+}
+
+// ---------------------------------------------------------------- UVW model --
+UvwModel::UvwModel(DelayTable t) : t_(std::move(t)) {
+  scan_nr_ = 0;
+  n_sources_ = 0;
+  next_scan();  // open(): the first scan group
+}
+
+// initialise_next_scan (uvw_model.cc:244-257): the next group of scans with one start
+bool UvwModel::next_scan() {
+  if (scan_nr_ >= t_.scans.size() - (size_t)n_sources_) return false;
+  scan_nr_ += (size_t)n_sources_;
+  n_sources_ = 1;
+  while (scan_nr_ + n_sources_ < t_.scans.size() &&
+         t_.scans[scan_nr_ + n_sources_ - 1].begin == t_.scans[scan_nr_ + n_sources_].begin)
+    n_sources_++;
+  return true;
+}
+
+// create_akima_spline (uvw_model.cc:259-310): the second holding t, splines
+// over [-2 s, +3 s] of it clamped to the scan (at least 4 s)
+void UvwModel::create(ticks_t t) {
+  while (t_.scans[scan_nr_].end < t)
+    if (!next_scan()) throw Error(-3, "UVW model ends before the requested time");
+  const int mjd_start = (int)std::floor(time_mjd(t));
+  const double seconds_start = std::floor(time_usec_of_day(t) / 1000000);
+  const ticks_t start = time_from_mjd_sec(mjd_start, seconds_start);
+  const ticks_t onesec = time_from_usec(1000000.);
+  interval_begin_ = start;
+  interval_end_ = start + onesec;
+  ticks_t ib = start - time_mul(onesec, 2), ie = start + time_mul(onesec, 3);
+  const Scan &s0 = t_.scans[scan_nr_];
+  if (ib < s0.begin) {
+    ib = s0.begin;
+    if (time_diff(ie, ib) < 4) ie = ib + time_mul(onesec, 4);
+  }
+  if (ie > s0.end) {
+    ie = s0.end;
+    if (time_diff(ie, ib) < 4) ib = ie - time_mul(onesec, 4);
+  }
+  const std::vector<double> *const cols[3] = {&t_.us, &t_.vs, &t_.ws};
+  splines_.clear();
+  for (int i = 0; i < n_sources_; i++) {
+    Spline sp = Spline::build(t_, t_.scans[scan_nr_ + i], ib, ie, cols);
+    sp.scan_begin = s0.begin;
+    splines_.push_back(std::move(sp));
+  }
+}
+
+void UvwModel::get(int pc, ticks_t t, double out[3]) {
+  if (t > interval_end_) create(t);
+  if (pc < 0 || pc >= (int)splines_.size()) throw Error(-1, "no such phase centre in the UVW model's scan");
+  const double sec = time_diff(t, t_.scans[scan_nr_].begin);
+  for (int k = 0; k < 3; k++) out[k] = splines_[(size_t)pc].eval(k, sec);
 }
 
 // Interval search as GSL's gsl_interp_bsearch; the device uses the same rule.

@@ -49,6 +49,7 @@ struct Scan {
 struct DelayTable {
   std::vector<Scan> scans;
   std::vector<double> times, delays, phases, amps;  // row columns; times relative to scan start
+  std::vector<double> us, vs, ws;                    // the u, v, w columns (metres)
   double clock_offset = 0, clock_rate = 0;
   ticks_t clock_epoch = 0;
   static DelayTable parse(const uint8_t *bytes, size_t n);
@@ -67,6 +68,9 @@ struct Spline {
   // pc: phase centre, the pc-th scan starting with the covering one (an
   // additional phase centre is a scan with the same start, 313-336, 478-494)
   static Spline create(const DelayTable &t, ticks_t start, ticks_t duration, int pc = 0);
+  // the spline of three columns of scan s's rows over [ib, ie] (whole seconds from the scan start)
+  static Spline build(const DelayTable &t, const Scan &s, ticks_t ib, ticks_t ie,
+                      const std::vector<double> *const cols[3]);
   int index(double x) const;
   double eval(int col, double x) const;
   double deriv(int col, double x) const;
@@ -74,6 +78,26 @@ struct Spline {
   double rate(ticks_t t) const;        // ::rate (128-136)
   double phase(ticks_t t) const;       // ::phase (148-156)
   double amplitude(ticks_t t) const;   // ::amplitude (158-166)
+};
+
+// ---- UVW model (Uvw_model, sfxc/src/uvw_model.cc:79-330): Akima splines of
+// a delay table's u, v, w columns over the six whole seconds around a time,
+// rebuilt when a later time leaves the current second, one per phase
+// centre of the scan (scans with the same start).
+class UvwModel {
+ public:
+  explicit UvwModel(DelayTable t);
+  // get_uvw (312-325): u, v, w of phase centre pc at time t
+  void get(int pc, ticks_t t, double out[3]);
+
+ private:
+  DelayTable t_;
+  size_t scan_nr_ = 0;
+  int n_sources_ = 0;
+  ticks_t interval_begin_ = 0, interval_end_ = 0;
+  std::vector<Spline> splines_;
+  bool next_scan();
+  void create(ticks_t t);
 };
 
 // ---- Integer delays (Input_node_tasklet::get_delay/get_delays, sfxc/src/input_node_tasklet.cc:235-282)

@@ -368,6 +368,36 @@ class DeviceRecording:
         node._check(self._lib.sfxc_gpu_recording_push(self._h, c, slice_index, node._h, stream))
 
 
+class UvwModel:
+    """A station's UVW model from its .del bytes (sfxc_gpu_uvw_*): get(pc,
+    ticks) -> (u, v, w) in metres, as the reference's Uvw_model::get_uvw."""
+
+    def __init__(self, del_bytes):
+        self._lib = L.load()
+        self._buf = bytes(del_bytes)
+        self._h = self._lib.sfxc_gpu_uvw_create(self._buf, len(self._buf))
+        if not self._h:
+            raise L.SfxcError(L.EINVAL, self._lib.sfxc_gpu_global_error().decode())
+
+    def get(self, phase_center, ticks):
+        out = (C.c_double * 3)()
+        rc = self._lib.sfxc_gpu_uvw_get(self._h, phase_center, int(ticks), out)
+        if rc < 0:
+            raise L.SfxcError(rc, self._lib.sfxc_gpu_global_error().decode())
+        return out[0], out[1], out[2]
+
+    def close(self):
+        if self._h:
+            self._lib.sfxc_gpu_uvw_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class PhaseCal:
     """Phase-cal extraction of one channel on a CorrelatorNode's GPU
     (Input_node_data_writer::do_phasecal, sfxc/src/input_node_data_writer.cc:230-312).

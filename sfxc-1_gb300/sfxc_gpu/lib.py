@@ -27,6 +27,7 @@ EXPORTS = [
     "sfxc_gpu_recording_create", "sfxc_gpu_recording_schedule", "sfxc_gpu_recording_n_blocks", "sfxc_gpu_recording_block",
     "sfxc_gpu_recording_extract", "sfxc_gpu_recording_channel", "sfxc_gpu_recording_protocol",
     "sfxc_gpu_recording_push", "sfxc_gpu_recording_destroy",
+    "sfxc_gpu_uvw_create", "sfxc_gpu_uvw_get", "sfxc_gpu_uvw_destroy",
 ]
 FORMAT_VDIF, FORMAT_MARK5B = 0, 1
 
@@ -177,6 +178,10 @@ def load(path=None):
                                                 C.POINTER(C.c_int64)]
     lib.sfxc_gpu_recording_push.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32]
     lib.sfxc_gpu_recording_destroy.argtypes = [C.c_void_p]
+    lib.sfxc_gpu_uvw_create.restype = C.c_void_p
+    lib.sfxc_gpu_uvw_create.argtypes = [C.c_void_p, C.c_size_t]
+    lib.sfxc_gpu_uvw_get.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double)]
+    lib.sfxc_gpu_uvw_destroy.argtypes = [C.c_void_p]
     lib.sfxc_gpu_phasecal_create.restype = C.c_void_p
     lib.sfxc_gpu_phasecal_create.argtypes = [C.c_void_p, C.POINTER(PhasecalParams)]
     lib.sfxc_gpu_phasecal_push.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(ChannelBlock), SINK,

@@ -58,20 +58,40 @@ class DelayPoly:
 
 
 def del_file_bytes(station: str, scans) -> bytes:
-    """scans: list of (source, mjd, sec_start, n_rows, DelayPoly) with 1-s row spacing."""
+    """scans: list of (source, mjd, sec_start, n_rows, DelayPoly[, uvw]) with
+    1-s row spacing; uvw(sec) -> (u, v, w) in metres fills those columns
+    (zero without it)."""
     out = bytearray()
     name = station.encode()[:2].ljust(2, b"\0") + b"\0"
     out += struct.pack("<i", 3) + name
-    for source, mjd, sec_start, n_rows, poly in scans:
+    for scan in scans:
+        source, mjd, sec_start, n_rows, poly = scan[:5]
+        uvw = scan[5] if len(scan) > 5 else None
         src = source.encode()[:80].ljust(80, b" ") + b"\0"
         out += src + struct.pack("<i", mjd)
         for k in range(n_rows):
             sec = float(sec_start + k)
             d = float(poly.delay(sec))
             ph = float(poly.phase(sec))
-            out += struct.pack("<7d", sec, 0.0, 0.0, 0.0, d, ph, poly.amp)
+            u, v, w = (float(x) for x in uvw(sec)) if uvw else (0.0, 0.0, 0.0)
+            out += struct.pack("<7d", sec, u, v, w, d, ph, poly.amp)
         out += struct.pack("<7d", *([0.0] * 7))
     return bytes(out)
+
+
+def earth_rotation_uvw(baseline_m, dec, h0):
+    """u, v, w (metres) of a station `baseline_m` (x, y, z) from the array
+    centre towards a source at declination dec (rad), hour angle h0 + Earth
+    rotation at sec 0: the textbook projection, as a smooth test model."""
+    bx, by, bz = baseline_m
+
+    def f(sec):
+        h = h0 + 7.2921150e-5 * sec
+        u = bx * math.sin(h) + by * math.cos(h)
+        v = -bx * math.sin(dec) * math.cos(h) + by * math.sin(dec) * math.sin(h) + bz * math.cos(dec)
+        w = bx * math.cos(dec) * math.cos(h) - by * math.cos(dec) * math.sin(h) + bz * math.sin(dec)
+        return u, v, w
+    return f
 
 
 # --------------------------------------------------------------------------

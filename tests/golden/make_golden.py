@@ -257,6 +257,40 @@ def make_schedule():
         json.dump(out, f, indent=1, sort_keys=True)
 
 
+def uvw_cases():
+    """.del tables with u, v, w columns (a two-centre scan, then a later
+    scan) and probes (phase centre, ticks) in order: fractional and whole
+    seconds, the first and last seconds of a scan (clamped windows), a later
+    scan, and a step back in time (the model keeps its spline)."""
+    from sfxc_gpu import timebase
+    mjd, sec0 = 60200, 43000
+    poly = synth.DelayPoly(coeffs=(1e-3, 2e-7, 0.0, 0.0), t0=sec0, phase_coeffs=(0.0,), amp=1.0)
+    tables = {}
+    for name, (b, dec, h0) in {"near": ((1200.0, -800.0, 300.0), 0.6, 0.3),
+                               "far": ((-5.1e6, 2.2e6, 3.3e6), -0.2, 1.1)}.items():
+        scans = [("SRC1", mjd, sec0, 20, poly, synth.earth_rotation_uvw(b, dec, h0)),
+                 ("SRC2", mjd, sec0, 20, poly, synth.earth_rotation_uvw(b, dec + 0.01, h0 - 0.02)),
+                 ("SRC3", mjd, sec0 + 40, 15, poly, synth.earth_rotation_uvw(b, dec - 0.3, h0 + 0.5))]
+        tables[name] = synth.del_file_bytes("Xx", scans)
+    t = lambda s: timebase.ticks_from_mjd_sec(mjd, s)  # noqa: E731
+    probes = [(0, t(sec0 + 0.25)), (1, t(sec0 + 0.25)), (0, t(sec0 + 1.0)), (0, t(sec0 + 1.5)),
+              (1, t(sec0 + 7.125)), (0, t(sec0 + 7.875)), (0, t(sec0 + 7.5)), (0, t(sec0 + 12.0)),
+              (1, t(sec0 + 18.5)), (0, t(sec0 + 19.0)), (0, t(sec0 + 41.75)), (0, t(sec0 + 47.0625)),
+              (0, t(sec0 + 54.0))]
+    return tables, probes
+
+
+def make_uvw():
+    """u, v, w of the reference's Uvw_model for uvw_cases()."""
+    import json
+    tables, probes = uvw_cases()
+    out = {name: {"del_sha256": hashlib.sha256(db).hexdigest(), "probes": probes,
+                  "uvw": [list(v) for v in jobs.uvw(db, probes)]} for name, db in tables.items()}
+    with open(os.path.join(HERE, "uvw.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    print("uvw done")
+
+
 def make_phasecal():
     """Phase-cal messages of the reference's Input_node_data_writer for
     phasecal_cases(): per case the SHA-256 of each message, in order."""
@@ -312,6 +346,7 @@ if __name__ == "__main__":
     make_phasecal()
     make_formats()
     make_schedule()
+    make_uvw()
     make_extract()
     for name, sc in scenarios().items():
         make(name, sc)
