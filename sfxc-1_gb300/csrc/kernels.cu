@@ -978,19 +978,24 @@ __global__ void norm_autos_kernel(const float2 *__restrict__ acc, int kpad, int 
 }
 
 // out[b][k] (compact M+1) = normalised visibility; flagfac[b] = N1*N2 (crosses).
+// A cross baseline's FP64 norm is the same for all its channels: one thread
+// of the CTA (all of whose threads share the baseline) computes it.
 __global__ void normalize_kernel(const float2 *__restrict__ acc, int kpad, int M, int nstreams, int nbl,
                                  const int *__restrict__ bl, const double *__restrict__ norms,
                                  const double *__restrict__ flagfac, float2 *__restrict__ out) {
   const int b = blockIdx.y;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ float cross_norm;
+  if (b >= nstreams && threadIdx.x == 0)
+    cross_norm = (float)sqrt(flagfac[b] * norms[bl[2 * b]] * norms[bl[2 * b + 1]]);
+  __syncthreads();
   if (k > M) return;
   const float2 v = acc[(int64_t)b * kpad + k];
   float2 o;
   if (b < nstreams) {
     o = make_float2((float)((double)v.x / norms[b]), 0.f);
   } else {
-    const double n = flagfac[b];
-    const float norm = (float)sqrt(n * norms[bl[2 * b]] * norms[bl[2 * b + 1]]);
+    const float norm = cross_norm;
     o = make_float2(v.x / norm, v.y / norm);
   }
   out[(int64_t)b * (M + 1) + k] = o;
