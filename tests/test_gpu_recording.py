@@ -398,3 +398,43 @@ def test_vdif_dropped_block_filled_on_device(gpu_node):
     cor_direct, tsys_direct = gpu_node.correlate(job)
     cor_dev, tsys_dev = _correlate_pushed(gpu_node, job, objs, len(sc.pols))
     assert cor_dev == cor_direct and tsys_dev == tsys_direct
+
+
+def test_mark5b_dropped_block_filled_on_device(gpu_node):
+    """Station 2's Mark5B recording loses block 1 (frames 8-15): the device
+    front end's reader tasklet fills it in, and the protocols and correlation
+    equal the job whose block 1 of station 2 is invalid."""
+    from sfxc_gpu import correlator, scenario, synth, timebase
+    runs = lambda st: {(st[2].number, "R"): [(1, 0, 5000)], (st[2].number, "L"): [(1, 0, 5000)]}  # noqa: E731
+    sc, job, chans, nsamp = _job_and_streams(dict(block_bytes=5000, runs=runs))
+    fps = sc.sample_rate * 32 // 80000
+    frame = 16 + 10000
+    recs = []
+    for si in range(len(sc.stations)):
+        w = _words(chans, si, nsamp, 400 + si)
+        rec = synth.mark5b_recording(w.size // 2500, mjd=sc.mjd, sec_of_day=sc.sec0, frames_per_second=fps,
+                                     crc="valid", payload_words=w)
+        if si == 2:
+            rec = rec[:8 * frame] + rec[16 * frame:]
+        recs.append(rec)
+    nblocks = len(recs[0]) // frame // 8
+    rec0 = timebase.ticks_from_mjd_sec(sc.mjd, sc.sec0)
+    tbh = 320000  # 8 frames of 10000 bytes at 32 bitstreams x 32 Mb/s: 625 us
+    dels = scenario.del_tables(sc)
+    _, start, tint, slice_samples = scenario.job_timing(sc)
+    protos, objs = [], []
+    for si in range(len(sc.stations)):
+        r = correlator.DeviceRecording(gpu_node, recs[si], "mark5b", ref_ticks=timebase.ticks_from_mjd_sec(sc.mjd, 0.0),
+                                       track_bit_rate=sc.sample_rate, n_tracks=32, bits=2, channel_tracks=TRACKS16)
+        r.schedule([(rec0, rec0 + nblocks * tbh, rec0 + nblocks * tbh)])
+        assert r.n_blocks() == nblocks
+        r.extract(4, 2, [TRACKS16[0], TRACKS16[1]])
+        slices = [(start, start + tint, slice_samples, correlator.delay_list(dels[si], start, start + tint,
+                                                                              sc.sample_rate, sc.bits))]
+        for c, pol in enumerate(sc.pols):
+            protos.append(r.protocol(c, slices, sc.sample_rate, sc.bits, sc.integration_us))
+        objs.append(r)
+    assert protos == [[bytes(x) for x in p] for p in job["protocols"]]
+    cor_direct, tsys_direct = gpu_node.correlate(job)
+    cor_dev, tsys_dev = _correlate_pushed(gpu_node, job, objs, len(sc.pols))
+    assert cor_dev == cor_direct and tsys_dev == tsys_direct
