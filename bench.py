@@ -455,9 +455,12 @@ def measure_c4(args, log, x_mode="tc"):
         for _ in range(args.warmup):
             batch.correlate(jobs)
         dev_ms, t0 = 0.0, time.perf_counter()
+        split = {}
         for _ in range(args.steps):
             batch.correlate(jobs)
             dev_ms += batch.last_ms()
+            for k, v in batch.last_host_ms().items():
+                split[k] = split.get(k, 0.0) + v / args.steps
         wall = time.perf_counter() - t0
     finally:
         batch.close()
@@ -466,7 +469,8 @@ def measure_c4(args, log, x_mode="tc"):
     return {"workload": C4_NAME, "x_step": x_mode, "value": round(total * args.steps / (dev_ms / 1e3) / 1e9, 3),
             "unit": "Gsamples/s", "ms_per_step": round(dev_ms / args.steps, 3), "samples_per_step": total,
             "e2e": {"value": round(total * args.steps / wall / 1e9, 3), "unit": "Gsamples/s",
-                    "ms_per_step": round(wall * 1e3 / args.steps, 3)},
+                    "ms_per_step": round(wall * 1e3 / args.steps, 3),
+                    "batch_call_split_ms": {k: round(v, 3) for k, v in split.items()}},
             "graph_launches_per_step": 1, "jobs": len(jobs),
             "data": "seeded uniform 2-bit/1-bit codes, cubic delay models"}
 

@@ -499,6 +499,11 @@ int sfxc_gpu_batch_run_counts(sfxc_gpu_batch *batch, const int32_t *counts, sfxc
                               void *const *users);
 /* Device time (ms, CUDA events around the graph launch) of the last run. */
 float sfxc_gpu_batch_last_ms(const sfxc_gpu_batch *batch);
+/* Host wall time (ms) of the last run's phases: [0] planning every
+ * integration (host tables, upload payloads staged), [1] graph capture and
+ * update (or instantiation), [2] launch to completion, [3] outputs to the
+ * sink (statistics, output bytes, tsys records). */
+int sfxc_gpu_batch_last_host_ms(const sfxc_gpu_batch *batch, float *out4);
 void sfxc_gpu_batch_destroy(sfxc_gpu_batch *batch);
 
 /* Autotuner (no counterpart in the reference): times the launch-shape

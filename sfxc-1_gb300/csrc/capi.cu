@@ -4,6 +4,7 @@
 // sfxc/src/correlation_core.cc:316-477; headers sfxc/include/output_header.h:100-148).
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <tuple>
 #include <atomic>
 #include <cmath>
@@ -2751,6 +2752,7 @@ struct sfxc_gpu_batch {
   cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr;
   std::vector<cudaEvent_t> join;
   float last_ms = 0.f;
+  float host_ms[4] = {};  // the last run: planning, graph capture and update, launch to completion, outputs
   std::string err;
 };
 
@@ -2826,11 +2828,18 @@ int sfxc_gpu_batch_run_counts(sfxc_gpu_batch *b, const int32_t *counts, sfxc_out
         for (void *p : list) cudaFree(p);
       }
     } retire;
+    using clock = std::chrono::steady_clock;
+    auto ms_since = [](clock::time_point t) {
+      return std::chrono::duration<float, std::milli>(clock::now() - t).count();
+    };
+    clock::time_point t0 = clock::now();
     for (size_t k = 0; k < n; k++)
       for (int j = 0; j < cnt[k]; j++) {
         enqueue_integration(b->ctx[k], j, j == 0);
         stage_ops(b->ctx[k], j);
       }
+    b->host_ms[0] = ms_since(t0);
+    t0 = clock::now();
     g_retired = nullptr;  // nothing is allocated below; what grew is freed when the batch returns
     // all of it captured into one graph: each job on its own streams, its
     // integrations in order, forked from and joined back into the batch's
@@ -2874,16 +2883,21 @@ int sfxc_gpu_batch_run_counts(sfxc_gpu_batch *b, const int32_t *counts, sfxc_out
       }
     }
     cudaGraphDestroy(graph);
+    b->host_ms[1] = ms_since(t0);
+    t0 = clock::now();
     CK(cudaEventRecord(b->e0, b->origin));
     CK(cudaGraphLaunch(b->exec, b->origin));
     CK(cudaEventRecord(b->e1, b->origin));
     CK(cudaStreamSynchronize(b->origin));
     CK(cudaEventElapsedTime(&b->last_ms, b->e0, b->e1));
+    b->host_ms[2] = ms_since(t0);
+    t0 = clock::now();
     for (i = 0; i < n; i++)
       for (int j = 0; j < cnt[i]; j++) {
         const int rc = finish_integration(b->ctx[i], j, sink, users ? users[i] : nullptr);
         if (rc != SFXC_GPU_OK) return rc;
       }
+    b->host_ms[3] = ms_since(t0);
     return SFXC_GPU_OK;
   } catch (const Error &e) {
     b->err = e.msg;
@@ -2899,5 +2913,11 @@ int sfxc_gpu_batch_run(sfxc_gpu_batch *b, sfxc_output_sink sink, void *const *us
 }
 
 float sfxc_gpu_batch_last_ms(const sfxc_gpu_batch *b) { return b ? b->last_ms : 0.f; }
+
+int sfxc_gpu_batch_last_host_ms(const sfxc_gpu_batch *b, float *out4) {
+  if (!b || !out4) return SFXC_GPU_EINVAL;
+  for (int k = 0; k < 4; k++) out4[k] = b->host_ms[k];
+  return SFXC_GPU_OK;
+}
 
 }  // extern "C"

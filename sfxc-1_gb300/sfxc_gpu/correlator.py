@@ -14,6 +14,7 @@ expose Input_node_tasklet::get_delays, Input_node_data_writer and the channel
 extractor through the same library.
 """
 import ctypes as C
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -579,6 +580,13 @@ class Batch:
     def last_ms(self):
         return float(self._lib.sfxc_gpu_batch_last_ms(self._h))
 
+    def last_host_ms(self):
+        """Host wall time of the last run's phases: planning, graph capture and
+        update, launch to completion, outputs (sfxc_gpu_batch_last_host_ms)."""
+        out = (C.c_float * 4)()
+        self._lib.sfxc_gpu_batch_last_host_ms(self._h, out)
+        return {"plan_ms": out[0], "graph_ms": out[1], "run_ms": out[2], "outputs_ms": out[3]}
+
     def correlate(self, jobs, per_run=None):
         """Every integration of the jobs (one per node; any integration
         counts): per_run[i] integrations of job i in each graph (default: all
@@ -590,17 +598,24 @@ class Batch:
         done = [0] * len(jobs)
         cor = [[] for _ in jobs]
         tsys = [[] for _ in jobs]
+        def push(n, j, d, c):
+            for it in range(d, d + c):
+                for k in range(n.nstreams):
+                    n.push_protocol(k, j["protocols"][k][it])
+
+        pool = ThreadPoolExecutor(max_workers=len(self.nodes))
         while any(left):
             counts = [min(s, l) for s, l in zip(step, left)]
-            for n, j, d, c in zip(self.nodes, jobs, done, counts):
-                for it in range(d, d + c):
-                    for k in range(n.nstreams):
-                        n.push_protocol(k, j["protocols"][k][it])
+            # each node's pushes from its own thread: the copies of different
+            # contexts run at the same time (the library call drops the GIL)
+            for f in [pool.submit(push, n, j, d, c) for n, j, d, c in zip(self.nodes, jobs, done, counts)]:
+                f.result()
             for q, (o, t) in enumerate(self.run(counts)):
                 cor[q].append(o)
                 tsys[q] += t
             done = [d + c for d, c in zip(done, counts)]
             left = [l - c for l, c in zip(left, counts)]
+        pool.shutdown()
         return [(b"".join(c), b"".join(t)) for c, t in zip(cor, tsys)]
 
     def close(self):

@@ -20,7 +20,7 @@ EXPORTS = [
     "sfxc_gpu_write_protocol", "sfxc_gpu_extract_channels", "sfxc_gpu_copy_spectra_noalloc",
     "sfxc_gpu_copy_pulsar_bins", "sfxc_gpu_measure_peaks", "sfxc_gpu_batch_create", "sfxc_gpu_batch_run",
     "sfxc_gpu_batch_run_counts", "sfxc_gpu_autotune", "sfxc_gpu_plan_cache",
-    "sfxc_gpu_batch_last_ms", "sfxc_gpu_batch_destroy",
+    "sfxc_gpu_batch_last_ms", "sfxc_gpu_batch_last_host_ms", "sfxc_gpu_batch_destroy",
     "sfxc_gpu_reader_create", "sfxc_gpu_reader_next", "sfxc_gpu_reader_destroy", "sfxc_gpu_extract_block",
     "sfxc_gpu_phasecal_create", "sfxc_gpu_phasecal_push", "sfxc_gpu_phasecal_destroy", "sfxc_gpu_set_uvw",
     "sfxc_gpu_output_create", "sfxc_gpu_output_put_slice", "sfxc_gpu_output_finish", "sfxc_gpu_output_destroy",
@@ -143,6 +143,7 @@ def load(path=None):
     lib.sfxc_gpu_plan_cache.argtypes = [C.c_void_p, C.c_int32]
     lib.sfxc_gpu_batch_last_ms.restype = C.c_float
     lib.sfxc_gpu_batch_last_ms.argtypes = [C.c_void_p]
+    lib.sfxc_gpu_batch_last_host_ms.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     lib.sfxc_gpu_batch_destroy.argtypes = [C.c_void_p]
     lib.sfxc_gpu_last_timings.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     lib.sfxc_gpu_delay_list.argtypes = [C.POINTER(DelayTable), C.c_int64, C.c_int64, C.c_int32, C.c_int32,
