@@ -17,6 +17,7 @@
 #include <set>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "formats.hpp"
@@ -2833,11 +2834,41 @@ int sfxc_gpu_batch_run_counts(sfxc_gpu_batch *b, const int32_t *counts, sfxc_out
       return std::chrono::duration<float, std::milli>(clock::now() - t).count();
     };
     clock::time_point t0 = clock::now();
-    for (size_t k = 0; k < n; k++)
-      for (int j = 0; j < cnt[k]; j++) {
-        enqueue_integration(b->ctx[k], j, j == 0);
-        stage_ops(b->ctx[k], j);
-      }
+    {
+      // the jobs planned at the same time, one host thread per context (a
+      // job's integrations in order); each thread keeps its own list of
+      // grown buffers, taken over by the batch's
+      std::vector<std::vector<void *>> grown(n);
+      std::vector<int> codes(n, SFXC_GPU_OK);
+      std::vector<std::string> msgs(n);
+      auto plan_job = [&](size_t k) {
+        g_retired = &grown[k];
+        try {
+          CK(cudaSetDevice(b->device));
+          for (int j = 0; j < cnt[k]; j++) {
+            enqueue_integration(b->ctx[k], j, j == 0);
+            stage_ops(b->ctx[k], j);
+          }
+        } catch (const Error &e) {
+          codes[k] = e.code;
+          msgs[k] = e.msg;
+        } catch (const std::exception &e) {
+          codes[k] = SFXC_GPU_ESTATE;
+          msgs[k] = e.what();
+        }
+        g_retired = nullptr;
+      };
+      std::vector<std::thread> threads;
+      for (size_t k = 0; k < n; k++)
+        if (cnt[k]) threads.emplace_back(plan_job, k);
+      for (std::thread &t : threads) t.join();
+      for (auto &l : grown) retire.list.insert(retire.list.end(), l.begin(), l.end());
+      for (size_t k = 0; k < n; k++)
+        if (codes[k] != SFXC_GPU_OK) {
+          i = k;
+          throw Error(codes[k], msgs[k]);
+        }
+    }
     b->host_ms[0] = ms_since(t0);
     t0 = clock::now();
     g_retired = nullptr;  // nothing is allocated below; what grew is freed when the batch returns

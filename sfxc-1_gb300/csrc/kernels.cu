@@ -1148,12 +1148,11 @@ __global__ void __launch_bounds__(256) reduce_kernel(const float2 *__restrict__ 
 // ------------------------------------------------------------------------
 // launchers
 static int sm_count() {
-  static int n = 0;
-  if (!n) {
+  static const int n = [] {  // initialised once, also when contexts are planned from several threads
     int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    n = cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0 ? v : 1;
-  }
+    return cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0 ? v : 1;
+  }();
   return n;
 }
 

@@ -555,7 +555,7 @@ class Batch:
 
     def run(self, counts=None):
         """The next integration (or counts[i] integrations) of every node:
-        [(output bytes, [tsys records])] in node order."""
+        [(output bytes (bytes or bytearray), [tsys records])] in node order."""
         outs = [([], []) for _ in self.nodes]
 
         def sink(user, kind, data, n):
@@ -563,7 +563,7 @@ class Batch:
             if n:
                 C.memmove((C.c_char * n).from_buffer(b), data, n)
             o = outs[user or 0]
-            (o[0] if kind == 0 else o[1]).append(bytes(b))
+            (o[0] if kind == 0 else o[1]).append(b)
             return 0
 
         cb = L.SINK(sink)
@@ -575,7 +575,8 @@ class Batch:
             rc = self._lib.sfxc_gpu_batch_run_counts(self._h, cnt, cb, users)
         if rc < 0:
             raise L.SfxcError(rc, self._lib.sfxc_gpu_global_error().decode())
-        return [(b"".join(o), t) for o, t in outs]
+        # one output buffer is passed on as it is (bytearray); several are joined
+        return [(o[0] if len(o) == 1 else b"".join(o), [bytes(x) for x in t]) for o, t in outs]
 
     def last_ms(self):
         return float(self._lib.sfxc_gpu_batch_last_ms(self._h))
@@ -590,7 +591,7 @@ class Batch:
     def correlate(self, jobs, per_run=None):
         """Every integration of the jobs (one per node; any integration
         counts): per_run[i] integrations of job i in each graph (default: all
-        of them in one).  Returns [(cor, tsys)] per job."""
+        of them in one).  Returns [(cor (bytes or bytearray), tsys)] per job."""
         for n, j in zip(self.nodes, jobs):
             n.set_parameters(j)
         left = [int(j["n_integrations"]) for j in jobs]
@@ -616,7 +617,7 @@ class Batch:
             done = [d + c for d, c in zip(done, counts)]
             left = [l - c for l, c in zip(left, counts)]
         pool.shutdown()
-        return [(b"".join(c), b"".join(t)) for c, t in zip(cor, tsys)]
+        return [(c[0] if len(c) == 1 else b"".join(c), b"".join(t)) for c, t in zip(cor, tsys)]
 
     def close(self):
         if self._h:
