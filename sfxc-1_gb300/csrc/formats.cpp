@@ -778,10 +778,15 @@ class Tasklet {
       return true;
     };
     if (!fetch()) return out_;
-    for (long guard = 0;; guard++) {
-      if (guard > 50000000L) throw std::runtime_error("reader tasklet did not finish its intervals");
+    // every step pushes a block, reads one or takes the next interval; steps
+    // that do none of these in a row mean the reference would not finish
+    int idle = 0;
+    for (;;) {
+      const size_t pushed = out_.size(), reads = w_.out.reads.size();
       if (*std::min_element(current_.begin(), current_.end()) < iv_.stop) {
         do_task();
+        idle = (out_.size() == pushed && w_.out.reads.size() == reads) ? idle + 1 : 0;
+        if (idle > 1000) throw std::runtime_error("reader tasklet makes no progress in its interval");
       } else if (!fetch()) {
         return out_;
       }
