@@ -402,6 +402,32 @@ sfxc_gpu_uvw_model *sfxc_gpu_uvw_create(const uint8_t *del_bytes, size_t n);
 int sfxc_gpu_uvw_get(sfxc_gpu_uvw_model *model, int32_t phase_center, int64_t time_ticks, double *uvw);
 void sfxc_gpu_uvw_destroy(sfxc_gpu_uvw_model *model);
 
+/* The correlation set-up of a control file and a VEX file: what
+ * Control_parameters derives from them (sfxc/src/control_parameters.cc:
+ * 29-230 defaults, 1483-1555 reader parameters, 1867-2022 job parameters)
+ * and how the manager deals out the jobs (Manager_node::initialise,
+ * initialise_scan, start, start_next_timeslice_on_node, send_global_header;
+ * sfxc/src/manager_node.cc:150-391,402-683).  Host only, no GPU needed.
+ * NULL on a file it cannot read or parse, or a set-up the reference refuses
+ * (message from sfxc_gpu_global_error). */
+typedef struct sfxc_gpu_control sfxc_gpu_control;
+sfxc_gpu_control *sfxc_gpu_control_open(const char *ctrl_path, const char *vex_path);
+/* The input node's current time (clock ticks) of control-file station
+ * `station` when the manager starts scan number `scan` of the plan; the
+ * manager moves the scan's first slice to the latest of these. */
+typedef int64_t (*sfxc_station_time_fn)(void *user, int32_t station, int32_t scan);
+/* Works out the whole plan and keeps it as JSON text: the global output
+ * header, the output files, per scan its stations (delay table, clock model,
+ * reader parameters with their track lists, stop time) and channel numbers,
+ * and every job in output slice order (its Correlation_parameters and the
+ * station channels feeding its streams); also "ctrl" (the control file with
+ * its defaults), "pulsars" (polyco files read) and "mask".  station_time may
+ * be NULL.  Returns the text's length, or a negative status. */
+int64_t sfxc_gpu_control_plan(sfxc_gpu_control *control, sfxc_station_time_fn station_time, void *user);
+/* The text of the last plan (NUL-terminated, owned by the handle). */
+const char *sfxc_gpu_control_plan_text(const sfxc_gpu_control *control);
+void sfxc_gpu_control_close(sfxc_gpu_control *control);
+
 /* Phase-cal extraction of one channel (Input_node_data_writer::do_phasecal,
  * sfxc/src/input_node_data_writer.cc:230-312, with its parameters from
  * Input_node_data_writer::set_parameters, 328-346): the channel's samples,

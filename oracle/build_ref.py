@@ -5,7 +5,8 @@ own source files for the correlator-node hot path where they lie under the
 reference checkout, plus the GSL 1.9 interpolation sources from the tarball the
 reference vendors (sfxc/lib/gsl/gsl-1.9.tar.gz), and links them with
 oracle/ref_harness.cc and the shims in oracle/ref_shim/ (config.h, an FFTW3
-API over a double-precision FFT, an in-process MPI stand-in).  Every output
+API over a double-precision FFT, an in-process MPI stand-in, and the VEX grammar restated in
+vex_grammar.cc because flex and bison are absent).  Every output
 goes to oracle/_ref/ (git-ignored).  The reference's own build system is not
 used.
 
@@ -68,6 +69,11 @@ REF_SOURCES = [
     "lib/common/src/backtrace.cc",
     "lib/common/src/demangler.cc",
     "lib/containers/src/default_allocator.cc",
+    "lib/vex_parser/vex_parser/src/Vexpp_node.cc",
+    "lib/vex_parser/vex_parser/src/Vex++.cc",
+    "lib/jsoncpp/src/json_reader.cpp",
+    "lib/jsoncpp/src/json_value.cpp",
+    "lib/jsoncpp/src/json_writer.cpp",
 ]
 GSL_SOURCES = [
     "interpolation/accel.c",
@@ -148,6 +154,9 @@ def build(ref_root=None, force=False):
     for s in ["fftw_shim.cc", "sfxc_stubs.cc"]:
         jobs.append(["g++", "-O2", "-I" + SHIM, "-ffunction-sections", "-fdata-sections",
                      "-c", os.path.join(SHIM, s), "-o", os.path.join(obj, "shim_" + s + ".o")])
+    # the VEX grammar, restated (no flex/bison here), over the reference's Vexpp_node
+    jobs.append(cxx + ["-I" + os.path.join(sfxc, "lib/vex_parser/vex_parser/src"),
+                       "-c", os.path.join(SHIM, "vex_grammar.cc"), "-o", os.path.join(obj, "shim_vex_grammar.o")])
     jobs.append(cxx + ["-c", os.path.join(HERE, "ref_harness.cc"),
                        "-o", os.path.join(obj, "harness.o")])
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:

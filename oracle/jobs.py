@@ -203,6 +203,25 @@ def uvw(del_bytes, probes):
         return [tuple(float(x) for x in line.split()) for line in open(out)]
 
 
+def control(ctrl_path, vex_path, workdir, station_times=()):
+    """The reference's Control_parameters over a control file and a VEX file,
+    with the manager's dealing of the jobs: the plan as a dict, or None when
+    the reference refuses the set-up (returns false or aborts).  Runs in
+    workdir, which relative paths of the control file are taken from, as the
+    reference takes them from its working directory.  station_times:
+    [(station, scan, ticks)]."""
+    job = os.path.join(workdir, "control.job")
+    _write_job(job, [("ctrl", ctrl_path), ("vex", vex_path)] +
+               [("station_time", s, sc, t) for s, sc, t in station_times])
+    out = os.path.join(workdir, "control.json")
+    r = subprocess.run([harness(), "control", job, out], capture_output=True, text=True, cwd=workdir)
+    if r.returncode != 0:
+        return None
+    import json
+    plan = json.load(open(out))
+    return None if "error" in plan else plan
+
+
 def correlate_lines(job, d, dump=False, precision=32, dump_bins=False):
     """The job file lines of the 'correlate' mode for a job dict, with its
     delay tables, protocols and mask files written into directory d (read by

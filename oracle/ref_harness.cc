@@ -50,6 +50,8 @@
 #include <map>
 #include <new>
 #include <sstream>
+#include <set>
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -810,8 +812,457 @@ static int mode_uvw(Kv &kv, const std::string &out) {
   return 0;
 }
 
+// ---- control: the reference's Control_parameters over a control file and a
+// VEX file, with Manager_node's dealing of the jobs restated around it (the
+// manager itself needs MPI).  Writes the plan as JSON in the form
+// Json plan_json() of the library writes.
+//   ctrl <path> ; vex <path> ; station_time#k <station> <scan> <ticks>
+
+struct Jw {  // a small JSON writer
+  std::string s;
+  std::vector<int> count;  // items written so far in each open container
+  bool after_key;
+  Jw() : after_key(false) {}
+  void pre() {
+    if (after_key) {
+      after_key = false;
+      return;
+    }
+    if (!count.empty() && count.back()++) s += ",";
+  }
+  void key(const char *k) {
+    if (!count.empty() && count.back()++) s += ",";
+    s += "\"";
+    s += k;
+    s += "\":";
+    after_key = true;
+  }
+  void val(const std::string &raw) {
+    pre();
+    s += raw;
+  }
+  void open(char c) {
+    pre();
+    s += c;
+    count.push_back(0);
+  }
+  void close(char c) {
+    count.pop_back();
+    s += c;
+  }
+  void str(const std::string &v) {
+    std::string q = "\"";
+    for (size_t i = 0; i < v.size(); i++) {
+      unsigned char c = v[i];
+      if (c == '"' || c == '\\') {
+        q += '\\';
+        q += (char)c;
+      } else if (c < 0x20) {
+        char b[8];
+        std::snprintf(b, sizeof b, "\\u%04x", c);
+        q += b;
+      } else {
+        q += (char)c;
+      }
+    }
+    val(q + "\"");
+  }
+  void num(long long v) {
+    char b[32];
+    std::snprintf(b, sizeof b, "%lld", v);
+    val(b);
+  }
+  void dbl(double v) {
+    char b[40];
+    std::snprintf(b, sizeof b, "%.17g", v);
+    val(b);
+  }
+  void boolean(bool v) { val(v ? "true" : "false"); }
+  void chr(char c) { str(c ? std::string(1, c) : std::string()); }
+};
+
+static void put_input(Jw &w, const Input_node_parameters &p, const std::string &fmt) {
+  w.open('{');
+  w.key("data_format"); w.str(fmt);
+  w.key("n_tracks"); w.num(p.n_tracks);
+  w.key("track_bit_rate"); w.num(p.track_bit_rate);
+  w.key("frame_size"); w.num(p.frame_size);
+  w.key("fft_size"); w.num(p.fft_size);
+  w.key("data_modulation"); w.num(p.data_modulation);
+  w.key("integr_time"); w.num(p.integr_time.get_clock_ticks());
+  w.key("offset"); w.num(p.offset.get_clock_ticks());
+  w.key("phasecal_integr_time"); w.num(p.phasecal_integr_time.get_clock_ticks());
+  w.key("exit_on_empty_datastream"); w.boolean(p.exit_on_empty_datastream);
+  w.key("channels");
+  w.open('[');
+  for (size_t i = 0; i < p.channels.size(); i++) {
+    const Input_node_parameters::Channel_parameters &c = p.channels[i];
+    w.open('{');
+    w.key("bits_per_sample"); w.num(c.bits_per_sample);
+    w.key("sideband"); w.chr(c.sideband);
+    w.key("polarisation"); w.chr(c.polarisation);
+    w.key("frequency_number"); w.num(c.frequency_number);
+    w.key("tracks");
+    w.open('[');
+    for (size_t k = 0; k < c.tracks.size(); k++) w.num(c.tracks[k]);
+    w.close(']');
+    w.close('}');
+  }
+  w.close(']');
+  w.close('}');
+}
+
+static int mode_control(Kv &kv, const std::string &out) {
+  Control_parameters cp;
+  if (!cp.initialise(get(kv, "ctrl")[0].c_str(), get(kv, "vex")[0].c_str(), std::cerr)) {
+    write_file(out, "{\"error\":\"initialise\"}", 22);
+    return 0;
+  }
+  const Vex &vex = cp.get_vex();
+  const int nst = (int)cp.number_stations();
+  std::map<std::string, int> to_input;
+  for (int s = 0; s < nst; s++) to_input[cp.station(s)] = s;
+  std::map<std::pair<int, int>, long long> station_time;
+  for (int k = 0; k < count_key(kv, "station_time"); k++) {
+    const std::vector<std::string> &v = get(kv, idx("station_time", k));
+    station_time[std::make_pair(std::atoi(v[0].c_str()), std::atoi(v[1].c_str()))] = std::atoll(v[2].c_str());
+  }
+  Time start = cp.get_start_time(), stop = cp.get_stop_time();
+  Time tint = cp.integration_time();
+  Jw w;
+  w.open('{');
+  w.key("start"); w.num(start.get_clock_ticks());
+  w.key("stop"); w.num(stop.get_clock_ticks());
+  // Manager_node::initialise (manager_node.cc:402-418)
+  int current_scan = cp.scan(start.date_string());
+  if (current_scan == -1) die("no scan at the start time");
+  // output files (420-472)
+  std::vector<std::string> files, sources;
+  std::string base = cp.get_output_file();
+  if (cp.pulsar_binning()) {
+    Pulsar_parameters pp(std::cerr);
+    if (!cp.get_pulsar_parameters(pp)) die("pulsar parameters");
+    int max_nbins = 2;
+    for (std::map<std::string, Pulsar_parameters::Pulsar>::iterator it = pp.pulsars.begin(); it != pp.pulsars.end(); it++)
+      max_nbins = std::max(it->second.nbins + 1, max_nbins);
+    for (int b = 0; b < max_nbins; b++) {
+      std::ostringstream f;
+      f << base << ".bin" << b;
+      files.push_back(f.str());
+    }
+  } else if (cp.multi_phase_center()) {
+    Vex::Date st(cp.get_start_time().date_string()), sp(cp.get_stop_time().date_string());
+    std::string first = vex.get_scan_name(st);
+    Vex::Node::const_iterator it = vex.get_root_node()["SCHED"][first];
+    std::set<std::string> srcs;
+    while (it != vex.get_root_node()["SCHED"]->end() && vex.start_of_scan(it.key()) < sp) {
+      for (Vex::Node::const_iterator si = it->begin("source"); si != it->end("source"); si++) srcs.insert(si->to_string());
+      it++;
+    }
+    for (std::set<std::string>::iterator si = srcs.begin(); si != srcs.end(); si++) {
+      sources.push_back(*si);
+      files.push_back(base + "_" + *si);
+    }
+  } else {
+    files.push_back(base);
+  }
+  w.key("output_files");
+  w.open('[');
+  for (size_t i = 0; i < files.size(); i++) w.str(files[i]);
+  w.close(']');
+  w.key("sources");
+  w.open('[');
+  for (size_t i = 0; i < sources.size(); i++) w.str(sources[i]);
+  w.close(']');
+  // send_global_header (660-683)
+  {
+    int y, d;
+    start.get_date(y, d);
+    w.key("header");
+    w.open('{');
+    w.key("experiment"); w.str(cp.get_exper_name());
+    w.key("start_year"); w.num(y);
+    w.key("start_day"); w.num(d);
+    w.key("start_time"); w.num((int)start.get_time());
+    w.key("number_channels"); w.num(cp.number_channels());
+    w.key("integration_time"); w.num((int)tint.get_time_usec());
+    w.key("polarisation_type"); w.num(cp.polarisation_type_for_global_output_header(vex.get_mode(cp.scan(current_scan))));
+    w.key("job_nr"); w.num(cp.job_nr());
+    w.key("subjob_nr"); w.num(cp.subjob_nr());
+    w.close('}');
+  }
+  // the state machine of Manager_node::start (150-277) and
+  // start_next_timeslice_on_node (284-391)
+  Jw jobs;
+  jobs.open('[');
+  w.key("scans");
+  w.open('[');
+  int slice = 0, out_slice = 0, scan_index = 0;
+  const int nch = (int)cp.number_frequency_channels();
+  bool done = false;
+  while (!done) {
+    // initialise_scan (493-626)
+    const std::string scan = cp.scan(current_scan);
+    Vex::Date sos = vex.start_of_scan(scan), eos = vex.stop_of_scan(scan);
+    Time scan_start(mjd(1, 1, sos.year) + sos.day - 1, sos.to_miliseconds() / 1000.);
+    if (start + tint * slice < scan_start) {
+      Time iv = scan_start - start;
+      slice = (int)(iv / tint);
+      if ((iv % tint) != Time()) slice++;
+    }
+    Time stop_scan(mjd(1, 1, eos.year) + eos.day - 1, eos.to_miliseconds() / 1000.);
+    if (stop < stop_scan) stop_scan = stop;
+    stop_scan -= (stop_scan - start) % tint;
+    const std::string mode = vex.get_mode(scan);
+    Jw sw;  // this scan's entry (written only if the scan is correlated)
+    sw.open('{');
+    sw.key("name"); sw.str(scan);
+    sw.key("mode"); sw.str(mode);
+    sw.key("source"); sw.str(cp.scan_source(scan));
+    sw.key("n_sources"); sw.num(vex.n_sources(scan));
+    sw.key("start"); sw.num(scan_start.get_clock_ticks());
+    sw.key("stop"); sw.num(stop_scan.get_clock_ticks());
+    sw.key("stations");
+    sw.open('[');
+    const Vex::Node &root = vex.get_root_node();
+    for (int s = 0; s < nst; s++) {
+      const std::string name = cp.station(s);
+      if (!cp.station_in_scan(scan, name)) continue;
+      std::string delay_file = cp.get_delay_table_name(name);
+      // clock (532-576)
+      Vex::Node::const_iterator clock = root["STATION"][name]["CLOCK"];
+      const std::string clock_name = clock->to_string();
+      Time cstart, epoch;
+      double offset = 0.0, rate = 0.0;
+      for (clock = root["CLOCK"][clock_name]->begin("clock_early"); clock != root["CLOCK"][clock_name]->end("clock_early"); clock++) {
+        if (scan_start < Time(clock[0]->to_string())) continue;
+        if (cstart > Time(clock[0]->to_string())) continue;
+        cstart = Time(clock[0]->to_string());
+        offset = clock[1]->to_double_amount("sec");
+        rate = 0.0;
+        if (clock->size() > 3) {
+          if (clock[3]->to_string().find_first_of("\t ") != std::string::npos)
+            rate = clock[3]->to_double_amount("sec/sec");
+          else
+            rate = clock[3]->to_double() * 1e-6;
+          epoch = Time(clock[2]->to_string());
+        }
+      }
+      if (cstart == Time()) die("clock does not cover the scan");
+      double reader_offset = round(offset / 1.0) * 1.0;
+      offset = offset - reader_offset;
+      cp.set_reader_offset(name, Time(reader_offset * 1e6));
+      Input_node_parameters ip = cp.get_input_node_parameters(mode, name);
+      sw.open('{');
+      sw.key("station"); sw.num(s);
+      sw.key("name"); sw.str(name);
+      sw.key("delay_file"); sw.str(delay_file);
+      sw.key("clock_offset"); sw.dbl(offset);
+      sw.key("clock_rate"); sw.dbl(rate);
+      sw.key("clock_start"); sw.num(cstart.get_clock_ticks());
+      sw.key("clock_epoch"); sw.num(epoch.get_clock_ticks());
+      sw.key("reader_offset"); sw.num(Time(reader_offset * 1e6).get_clock_ticks());
+      sw.key("stop_time"); sw.num(cp.stop_time(scan, name).get_clock_ticks());
+      sw.key("input");
+      put_input(sw, ip, cp.data_format(name));
+      sw.close('}');
+    }
+    sw.close(']');
+    std::vector<std::vector<int> > chs(nch, std::vector<int>(nst, -1));
+    std::vector<int> last(nst, -1);
+    for (int i = 0; i < nch; i++)
+      for (int s = 0; s < nst; s++)
+        if (cp.station_in_scan(scan, cp.station(s)) && !cp.frequency_channel(i, mode, cp.station(s)).empty())
+          chs[i][s] = ++last[s];
+    sw.key("ch_number_in_scan");
+    sw.open('[');
+    for (int i = 0; i < nch; i++) {
+      sw.open('[');
+      for (int s = 0; s < nst; s++) sw.num(chs[i][s]);
+      sw.close(']');
+    }
+    sw.close(']');
+    // START_NEW_SCAN (164-208)
+    for (int s = 0; s < nst; s++) {
+      bool in = false;
+      for (int i = 0; i < nch; i++) in = in || chs[i][s] >= 0;
+      if (!in) continue;
+      std::map<std::pair<int, int>, long long>::iterator t = station_time.find(std::make_pair(s, scan_index));
+      if (t == station_time.end()) continue;
+      Time st = ticks_time(t->second);
+      if (st > start + tint * slice) slice = (int)((st - start) / tint);
+    }
+    if (stop <= start + tint * slice) break;
+    sw.key("first_slice_start"); sw.num((start + tint * slice).get_clock_ticks());
+    sw.close('}');
+    w.val(sw.s.substr(0));
+    // time slices
+    const bool xpol = cp.cross_polarize();
+    for (;;) {
+      int ch = 0;
+      while (ch < nch) {
+        int xch = xpol ? cp.cross_channel(ch, mode) : -1;
+        Correlation_parameters c = cp.get_correlation_parameters(scan, ch, to_input);
+        c.start_time = start + tint * slice;
+        c.stop_time = start + tint * (slice + 1);
+        c.integration_nr = slice;
+        c.slice_nr = out_slice;
+        strncpy(c.source, cp.scan_source(scan).c_str(), 11);
+        c.pulsar_binning = cp.pulsar_binning();
+        c.n_phase_centers = cp.multi_phase_center() ? vex.n_sources(scan) : 1;
+        jobs.open('{');
+        jobs.key("scan"); jobs.num(scan_index);
+        jobs.key("channel"); jobs.num(ch);
+        jobs.key("cross_channel"); jobs.num(xch);
+        jobs.key("experiment_start"); jobs.num(c.experiment_start.get_clock_ticks());
+        jobs.key("start_time"); jobs.num(c.start_time.get_clock_ticks());
+        jobs.key("stop_time"); jobs.num(c.stop_time.get_clock_ticks());
+        jobs.key("integration_time"); jobs.num(c.integration_time.get_clock_ticks());
+        jobs.key("sub_integration_time"); jobs.num(c.sub_integration_time.get_clock_ticks());
+        jobs.key("number_channels"); jobs.num(c.number_channels);
+        jobs.key("fft_size_delaycor"); jobs.num(c.fft_size_delaycor);
+        jobs.key("fft_size_correlation"); jobs.num(c.fft_size_correlation);
+        jobs.key("window"); jobs.num(c.window);
+        jobs.key("integration_nr"); jobs.num(c.integration_nr);
+        jobs.key("slice_nr"); jobs.num(c.slice_nr);
+        jobs.key("slice_offset"); jobs.num(c.slice_offset);
+        jobs.key("sample_rate"); jobs.num(c.sample_rate);
+        jobs.key("bandwidth"); jobs.num(c.bandwidth);
+        jobs.key("frequency_nr"); jobs.num(c.frequency_nr);
+        jobs.key("channel_freq"); jobs.num(c.channel_freq);
+        jobs.key("sideband"); jobs.chr(c.sideband);
+        jobs.key("polarisation"); jobs.chr(c.polarisation);
+        jobs.key("cross_polarize"); jobs.boolean(c.cross_polarize);
+        jobs.key("reference_station"); jobs.num(c.reference_station);
+        jobs.key("n_phase_centers"); jobs.num(c.n_phase_centers);
+        jobs.key("pulsar_binning"); jobs.boolean(c.pulsar_binning != 0);
+        jobs.key("source"); jobs.str(std::string(c.source, strnlen(c.source, 11)));
+        jobs.key("stations");
+        jobs.open('[');
+        for (size_t k = 0; k < c.station_streams.size(); k++) {
+          const Correlation_parameters::Station_parameters &p = c.station_streams[k];
+          jobs.open('{');
+          jobs.key("station_number"); jobs.num(p.station_number);
+          jobs.key("station_stream"); jobs.num(p.station_stream);
+          jobs.key("start_time"); jobs.num(p.start_time.get_clock_ticks());
+          jobs.key("stop_time"); jobs.num(p.stop_time.get_clock_ticks());
+          jobs.key("sample_rate"); jobs.num(p.sample_rate);
+          jobs.key("channel_freq"); jobs.num(p.channel_freq);
+          jobs.key("bandwidth"); jobs.num(p.bandwidth);
+          jobs.key("sideband"); jobs.chr(p.sideband);
+          jobs.key("polarisation"); jobs.chr(p.polarisation);
+          jobs.key("bits_per_sample"); jobs.num(p.bits_per_sample);
+          jobs.key("lo_offset"); jobs.dbl(p.LO_offset);
+          jobs.key("tsys_freq"); jobs.num(p.tsys_freq);
+          jobs.close('}');
+        }
+        jobs.close(']');
+        jobs.key("inputs");
+        jobs.open('[');
+        for (int s = 0; s < nst; s++) {
+          int stream = 0;
+          if (chs[ch][s] >= 0) {
+            jobs.open('{');
+            jobs.key("station"); jobs.num(s);
+            jobs.key("channel_in_scan"); jobs.num(chs[ch][s]);
+            jobs.key("stream"); jobs.num(s);
+            jobs.close('}');
+            stream = 1;
+          }
+          if (xch != -1 && chs[xch][s] >= 0) {
+            jobs.open('{');
+            jobs.key("station"); jobs.num(s);
+            jobs.key("channel_in_scan"); jobs.num(chs[xch][s]);
+            jobs.key("stream"); jobs.num(stream ? s + nst : s);
+            jobs.close('}');
+          }
+        }
+        jobs.close(']');
+        jobs.close('}');
+        out_slice++;
+        ch++;
+        if (xpol) {
+          int x = cp.cross_channel(ch, mode);
+          while (ch < nch && x >= 0 && x < ch) {
+            ch++;
+            x = cp.cross_channel(ch, mode);
+          }
+        }
+      }
+      slice++;
+      if (start + tint * (slice + 1) > stop) {
+        done = true;
+        break;
+      }
+      if (start + tint * (slice + 1) > stop_scan) {
+        if (++current_scan == (int)cp.number_scans()) done = true;
+        break;
+      }
+    }
+    scan_index++;
+  }
+  w.close(']');
+  jobs.close(']');
+  w.key("jobs");
+  w.val(jobs.s);
+  // pulsars and the mask
+  w.key("pulsars");
+  w.open('[');
+  if (cp.pulsar_binning()) {
+    Pulsar_parameters pp(std::cerr);
+    cp.get_pulsar_parameters(pp);
+    for (std::map<std::string, Pulsar_parameters::Pulsar>::iterator it = pp.pulsars.begin(); it != pp.pulsars.end(); it++) {
+      const Pulsar_parameters::Pulsar &ps = it->second;
+      w.open('{');
+      w.key("name"); w.str(std::string(ps.name, strnlen(ps.name, 11)));
+      w.key("nbins"); w.num(ps.nbins);
+      w.key("gate_start"); w.dbl(ps.interval.start);
+      w.key("gate_stop"); w.dbl(ps.interval.stop);
+      w.key("polyco");
+      w.open('[');
+      for (size_t k = 0; k < ps.polyco_params.size(); k++) {
+        const Pulsar_parameters::Polyco_params &pc = ps.polyco_params[k];
+        w.open('{');
+        w.key("name"); w.str(std::string(pc.name, strnlen(pc.name, 11)));
+        w.key("tmid"); w.dbl(pc.tmid);
+        w.key("dm"); w.dbl(pc.DM);
+        w.key("ref_phase"); w.dbl(pc.ref_phase);
+        w.key("ref_freq"); w.dbl(pc.ref_freq);
+        w.key("obs_freq"); w.dbl(pc.obs_freq);
+        w.key("data_span"); w.num(pc.data_span);
+        w.key("coef");
+        w.open('[');
+        for (size_t q = 0; q < pc.coef.size(); q++) w.dbl(pc.coef[q]);
+        w.close(']');
+        w.close('}');
+      }
+      w.close(']');
+      w.close('}');
+    }
+  }
+  w.close(']');
+  Mask_parameters mp;
+  if (cp.get_mask_parameters(mp)) {
+    w.key("mask");
+    w.open('{');
+    w.key("normalize"); w.boolean(mp.normalize);
+    w.key("mask");
+    w.open('[');
+    for (size_t k = 0; k < mp.mask.size(); k++) w.dbl(mp.mask[k]);
+    w.close(']');
+    w.key("window");
+    w.open('[');
+    for (size_t k = 0; k < mp.window.size(); k++) w.dbl(mp.window[k]);
+    w.close(']');
+    w.close('}');
+  }
+  w.close('}');
+  write_file(out, w.s.data(), w.s.size());
+  return 0;
+}
+
 int main(int argc, char **argv) {
-  if (argc != 4) die("usage: ref_harness correlate|delays|protocol|extract|reader|schedule|uvw <job> <out>");
+  if (argc != 4) die("usage: ref_harness correlate|delays|protocol|extract|reader|schedule|uvw|control <job> <out>");
   Kv kv = read_job(argv[2]);
   std::string m(argv[1]);
   if (m == "correlate") return mode_correlate(kv, argv[3]);
@@ -821,6 +1272,7 @@ int main(int argc, char **argv) {
   if (m == "reader") return mode_reader(kv, argv[3]);
   if (m == "schedule") return mode_schedule(kv, argv[3]);
   if (m == "uvw") return mode_uvw(kv, argv[3]);
+  if (m == "control") return mode_control(kv, argv[3]);
   die("unknown mode " + m);
   return 2;
 }

@@ -20,6 +20,7 @@
 #include <thread>
 #include <vector>
 
+#include "control.hpp"
 #include "formats.hpp"
 #include "host.hpp"
 #include "kernels.hpp"
@@ -2743,6 +2744,85 @@ int sfxc_gpu_uvw_get(sfxc_gpu_uvw_model *h, int32_t phase_center, int64_t time_t
 }
 
 void sfxc_gpu_uvw_destroy(sfxc_gpu_uvw_model *h) { delete h; }
+
+// ---- correlation set-up from the control file and the VEX file
+
+struct sfxc_gpu_control {
+  Control c;
+  std::string plan;
+};
+
+sfxc_gpu_control *sfxc_gpu_control_open(const char *ctrl_path, const char *vex_path) {
+  try {
+    if (!ctrl_path || !vex_path) throw Error(SFXC_GPU_EINVAL, "no control or vex file");
+    std::unique_ptr<sfxc_gpu_control> h(new sfxc_gpu_control());
+    h->c.initialise(ctrl_path, vex_path);
+    return h.release();
+  } catch (const Error &e) {
+    g_error = e.msg;
+  } catch (const std::exception &e) {
+    g_error = e.what();
+  }
+  return nullptr;
+}
+
+int64_t sfxc_gpu_control_plan(sfxc_gpu_control *h, sfxc_station_time_fn station_time, void *user) {
+  if (!h) return SFXC_GPU_EINVAL;
+  try {
+    std::function<ticks_t(int, int)> st;
+    if (station_time) st = [station_time, user](int s, int scan) { return (ticks_t)station_time(user, s, scan); };
+    Json j = plan_json(make_plan(h->c, st));
+    j.set("ctrl", h->c.ctrl());
+    Json ps = Json::parse("[]");
+    for (const PulsarSpec &p : h->c.pulsars()) {
+      Json x;
+      x.set("name", Json::of_string(p.name));
+      x.set("nbins", Json::of_int(p.nbins));
+      x.set("gate_start", Json::of_double(p.gate_start));
+      x.set("gate_stop", Json::of_double(p.gate_stop));
+      Json pcs = Json::parse("[]");
+      for (const PolycoBlock &pc : p.polyco) {
+        Json y;
+        y.set("name", Json::of_string(pc.name));
+        y.set("tmid", Json::of_double(pc.tmid));
+        y.set("dm", Json::of_double(pc.dm));
+        y.set("ref_phase", Json::of_double(pc.ref_phase));
+        y.set("ref_freq", Json::of_double(pc.ref_freq));
+        y.set("obs_freq", Json::of_double(pc.obs_freq));
+        y.set("data_span", Json::of_int(pc.data_span));
+        Json co = Json::parse("[]");
+        for (double v : pc.coef) co.append(Json::of_double(v));
+        y.set("coef", co);
+        pcs.append(y);
+      }
+      x.set("polyco", pcs);
+      ps.append(x);
+    }
+    j.set("pulsars", ps);
+    bool norm = false;
+    std::vector<double> mask, window;
+    if (h->c.mask(norm, mask, window)) {
+      Json m, a = Json::parse("[]"), w = Json::parse("[]");
+      for (double v : mask) a.append(Json::of_double(v));
+      for (double v : window) w.append(Json::of_double(v));
+      m.set("normalize", Json::of_bool(norm));
+      m.set("mask", a);
+      m.set("window", w);
+      j.set("mask", m);
+    }
+    h->plan = j.dump();
+    return (int64_t)h->plan.size();
+  } catch (const Error &e) {
+    g_error = e.msg;
+  } catch (const std::exception &e) {
+    g_error = e.what();
+  }
+  return SFXC_GPU_EINVAL;
+}
+
+const char *sfxc_gpu_control_plan_text(const sfxc_gpu_control *h) { return h ? h->plan.c_str() : ""; }
+
+void sfxc_gpu_control_close(sfxc_gpu_control *h) { delete h; }
 
 // ---- batches: the next integration of several jobs in one CUDA graph
 struct sfxc_gpu_batch {

@@ -28,6 +28,7 @@ EXPORTS = [
     "sfxc_gpu_recording_extract", "sfxc_gpu_recording_channel", "sfxc_gpu_recording_protocol",
     "sfxc_gpu_recording_push", "sfxc_gpu_recording_destroy",
     "sfxc_gpu_uvw_create", "sfxc_gpu_uvw_get", "sfxc_gpu_uvw_destroy",
+    "sfxc_gpu_control_open", "sfxc_gpu_control_plan", "sfxc_gpu_control_plan_text", "sfxc_gpu_control_close",
 ]
 FORMAT_VDIF, FORMAT_MARK5B = 0, 1
 
@@ -107,6 +108,7 @@ class OutputGlobal(C.Structure):
 
 
 SINK = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t)
+STATION_TIME = C.CFUNCTYPE(C.c_int64, C.c_void_p, C.c_int32, C.c_int32)
 
 _lib = None
 
@@ -183,6 +185,13 @@ def load(path=None):
     lib.sfxc_gpu_uvw_create.argtypes = [C.c_void_p, C.c_size_t]
     lib.sfxc_gpu_uvw_get.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double)]
     lib.sfxc_gpu_uvw_destroy.argtypes = [C.c_void_p]
+    lib.sfxc_gpu_control_open.restype = C.c_void_p
+    lib.sfxc_gpu_control_open.argtypes = [C.c_char_p, C.c_char_p]
+    lib.sfxc_gpu_control_plan.restype = C.c_int64
+    lib.sfxc_gpu_control_plan.argtypes = [C.c_void_p, STATION_TIME, C.c_void_p]
+    lib.sfxc_gpu_control_plan_text.restype = C.c_char_p
+    lib.sfxc_gpu_control_plan_text.argtypes = [C.c_void_p]
+    lib.sfxc_gpu_control_close.argtypes = [C.c_void_p]
     lib.sfxc_gpu_phasecal_create.restype = C.c_void_p
     lib.sfxc_gpu_phasecal_create.argtypes = [C.c_void_p, C.POINTER(PhasecalParams)]
     lib.sfxc_gpu_phasecal_push.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(ChannelBlock), SINK,

@@ -341,7 +341,29 @@ def make_output_header():
         json.dump(out, f, indent=1)
 
 
+def make_control():
+    """The reference's plans for control_cases() (control.json.gz): per case the plan
+    (Control_parameters and the manager's dealing, oracle/ref_harness.cc
+    mode `control`) with the case directory written as <dir>, or null for a
+    set-up the reference refuses."""
+    import json
+    import tempfile
+    sys.path.insert(0, os.path.dirname(HERE))
+    import control_cases
+    out = {}
+    for name, case in control_cases.cases().items():
+        with tempfile.TemporaryDirectory() as d:
+            ctrl, vex = control_cases.write_case(case, d)
+            plan = jobs.control(ctrl, vex, d, control_cases.station_times(case))
+            out[name] = json.loads(json.dumps(plan).replace(d, "<dir>")) if plan else None
+        print(name, "refused" if plan is None else "%d jobs" % len(plan["jobs"]))
+    import gzip
+    with gzip.open(os.path.join(HERE, "control.json.gz"), "wt") as f:
+        json.dump(out, f, indent=None, sort_keys=True, separators=(",", ":"))
+
+
 if __name__ == "__main__":
+    make_control()
     make_output_header()
     make_phasecal()
     make_formats()
