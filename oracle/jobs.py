@@ -231,6 +231,9 @@ def correlate_lines(job, d, dump=False, precision=32, dump_bins=False):
         p = os.path.join(d, "st%d.del" % k)
         open(p, "wb").write(db)
         lines.append(("delfile", p))
+    if job.get("clocks") is not None:  # Delay_table::set_clock_offset per table: offset, rate, epoch ticks
+        for c in job["clocks"]:
+            lines.append(("clock",) + tuple(c if c is not None else (0.0, 0.0, 0)))
     for key in ["experiment_start_ticks", "start_ticks", "integration_time_us",
                 "sub_integration_time_us", "number_channels", "fft_size_delaycor",
                 "fft_size_correlation", "sample_rate", "channel_freq", "bandwidth", "sideband",

@@ -1,0 +1,117 @@
+"""A small synthetic experiment for the single-GPU driver (sfxc_gpu.run): a VEX
+schedule, a control file, the stations' delay tables and their recordings,
+written into a directory.
+
+Three stations record 2 frequencies x R/L at 4 MS/s, 2 bits, each in its own
+format: Ef VDIF with four channels in one thread, Wb VDIF with one channel per
+thread (and a clock more than a second off, so that its reader time is
+shifted by whole seconds), On Mark5B with eight bitstreams.  Two scans with a
+gap between them; the recordings run from before the first to after the
+last.  Cross-polarised correlation of the first frequency, 1 s integrations.
+tests/golden/driver.npz holds what the reference's own classes make of it,
+stage by stage (tests/golden/make_golden.py: its plan, reader tasklet,
+channel extractor, delays, input-node writer and correlation core)."""
+import json
+import os
+
+import numpy as np
+
+import control_cases
+from sfxc_gpu import synth
+
+MJD = 60409  # 2024y100d
+SR = 4_000_000
+T0 = 43198            # recordings start at 11:59:58
+T1 = 43211            # and end at 12:00:11
+STATIONS = ["Ef", "Wb", "On"]
+WB_CLOCK = 1.0000021  # seconds: the reader takes 1 s of it
+
+
+def vex_text():
+    freqs = [control_cases._freq_def("f4", control_cases._chans_rl(2, 2.0, f0=4974.49), 4.0)]
+    das = [("vdif_dbbc", "Mark5C", "DBBC"), ("mk5b", "Mark5B", "DBBC")]
+    thr_ef = ("t_ef", [(0, 32.0, 4, 2, 8000)], [("CH%02d" % (k + 1), 0, k) for k in range(4)])
+    thr_wb = ("t_wb", [(k, 8.0, 1, 2, 8000) for k in range(4)], [("CH%02d" % (k + 1), k, 0) for k in range(4)])
+    bs_on = ("bs_on", [("CH%02d" % (k + 1), sm, 2 * k + (sm == "mag"), 2 * k + (sm == "mag"))
+                       for k in range(4) for sm in ("sign", "mag")])
+    mode = [("FREQ", "f4", STATIONS), ("IF", "ifs", STATIONS), ("BBC", "bbcs", STATIONS),
+            ("THREADS", "t_ef", ["Ef"]), ("THREADS", "t_wb", ["Wb"]), ("BITSTREAMS", "bs_on", ["On"])]
+    clocks = [("Ef", ["2024y099d00h00m00s : 0.85 usec : 2024y100d12h00m00s : 1.0e-6"]),
+              ("Wb", ["2024y099d00h00m00s : %.7f sec : 2024y100d12h00m00s : 0.0" % WB_CLOCK]),
+              ("On", ["2024y099d00h00m00s : -1.25 usec"])]
+    scans = [("No0001", "2024y100d12h00m00s", "sess", ["SRC1"], [(s, 0, 4) for s in STATIONS]),
+             ("No0002", "2024y100d12h00m06s", "sess", ["SRC2"], [(s, 0, 3) for s in STATIONS])]
+    return control_cases._base([("Ef", "vdif_dbbc"), ("Wb", "vdif_dbbc"), ("On", "mk5b")], das, mode, freqs,
+                               threads=[thr_ef, thr_wb], bitstreams=[bs_on], scans=scans, clocks=clocks, nbbc=4)
+
+
+def ctrl_dict():
+    return {"exper_name": "N24X1", "stations": STATIONS, "start": "2024y100d12h00m00s",
+            "stop": "2024y100d12h00m09s", "integr_time": 1.0, "number_channels": 256, "cross_polarize": True,
+            "channels": ["CH01", "CH02"], "output_file": "file://out/n24x1.cor", "delay_directory": "file://delays",
+            "data_sources": {"Ef": ["file://data/ef.vdif"], "Wb": ["file://data/wb_a.vdif", "file://data/wb_b.vdif"],
+                             "On": ["file://data/on.m5b"]}}
+
+
+def del_bytes(station):
+    """Delay table of a station: one .del scan per VEX scan, rows from 5 s
+    before to 5 s after it; a smooth delay and u, v, w.  The delays (clock
+    included) stay negative: a slice of 1 s at 4 MS/s is exactly its 15625
+    FFTs of 256 samples, and the reader tasklet reads up to its interval's
+    stop time, so with a positive delay the last slice of a scan would lack
+    its last samples (the reference's input-node writer then waits for data
+    that never comes)."""
+    k = STATIONS.index(station)
+    poly = synth.DelayPoly(coeffs=(-2.0e-5 * (k + 1), 2.0e-7 * (1 + k), -1.0e-11), t0=43200.0)
+    uvw = synth.earth_rotation_uvw((4.0e5 * (k - 1), 2.5e5 * k, 1.0e5), 0.6, 0.3)
+    return synth.del_file_bytes(station, [("SRC1", MJD, 43195, 14, poly, uvw), ("SRC2", MJD, 43201, 13, poly, uvw)])
+
+
+def recordings():
+    """name -> bytes of each data file."""
+    n = T1 - T0
+    ef = synth.vdif_recording(n * 500, payload_bytes=8000, frames_per_second=500, start_mjd=MJD,
+                              start_sec_of_day=T0, log2_nchan=2, bits=2, invalid=(1711,), seed=701)
+    # Wb: one thread per channel, 125 frames/s each, its time stamps 1 s late (the clock);
+    # two files, the second starting where the first ends, one frame lost
+    wb = synth.vdif_recording(n * 500, payload_bytes=8000, frames_per_second=125, start_mjd=MJD,
+                              start_sec_of_day=T0 + 1, log2_nchan=0, bits=2, threads=(0, 1, 2, 3),
+                              drop=(2222,), seed=702)
+    cut = 8032 * 1000
+    on = synth.mark5b_recording(n * 400, mjd=MJD, sec_of_day=T0, frames_per_second=400, seed=703)
+    return {"data/ef.vdif": ef, "data/wb_a.vdif": wb[:cut], "data/wb_b.vdif": wb[cut:], "data/on.m5b": on}
+
+
+def write_experiment(d):
+    """Writes the experiment into directory d; returns (ctrl path, vex path)."""
+    os.makedirs(os.path.join(d, "delays"), exist_ok=True)
+    os.makedirs(os.path.join(d, "data"), exist_ok=True)
+    vex = os.path.join(d, "n24x1.vex")
+    with open(vex, "w") as f:
+        f.write(vex_text())
+    ctrl = os.path.join(d, "n24x1.ctrl")
+    with open(ctrl, "w") as f:
+        json.dump(ctrl_dict(), f, indent=2)
+    for s in STATIONS:
+        with open(os.path.join(d, "delays", "N24X1_%s.del" % s), "wb") as f:
+            f.write(del_bytes(s))
+    for name, b in recordings().items():
+        with open(os.path.join(d, name), "wb") as f:
+            f.write(b)
+    return ctrl, vex
+
+
+def split_slices(cor, nchan):
+    """A .cor file (global header, then slices) as (global header, [slice
+    header bytes], [complex64 visibilities per baseline of each slice])."""
+    from sfxc_gpu import correlator
+    (hs,) = np.frombuffer(cor[:4], dtype=np.int32)
+    g, p, hdrs, vis = cor[:hs], int(hs), [], []
+    while p < len(cor):  # the output node writes each slice without its file index
+        nbl, nuvw, nstat = np.frombuffer(cor[p + 4:p + 16], dtype=np.int32)
+        n = 16 + int(nuvw) * 32 + int(nstat) * 24 + int(nbl) * (8 + (nchan + 1) * 8)
+        h, v = correlator.split_output(b"\0\0\0\0" + cor[p:p + n], nchan)
+        hdrs.append(h[4:])
+        vis.append(v)
+        p += n
+    return g, hdrs, vis

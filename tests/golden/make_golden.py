@@ -362,8 +362,145 @@ def make_control():
         json.dump(out, f, indent=None, sort_keys=True, separators=(",", ":"))
 
 
+def make_driver():
+    """The reference's own stages over driver_cases' experiment (driver.npz):
+    its plan (Control_parameters and the manager's dealing), for each station
+    the reader tasklet's blocks over the scan intervals, Channel_extractor_5
+    on them (a block whose buffer the tasklet reused for its next read keeps
+    its own bytes, the reader's block of that time; invalid runs rescaled as
+    Channel_extractor_tasklet::do_task does,
+    sfxc/src/channel_extractor_tasklet.cc:173-194; VDIF with one
+    channel per thread takes the blocks as they are), Input_node_tasklet's
+    delays per scan interval and Input_node_data_writer's protocol per slice,
+    then each job's Correlation_core output (with its file index) and u, v, w.
+    The glue between the stages restates Input_node and Correlator_node."""
+    import json
+    import tempfile
+    sys.path.insert(0, os.path.dirname(HERE))
+    import driver_cases
+    from sfxc_gpu import timebase
+    with tempfile.TemporaryDirectory() as d:
+        ctrl_path, vex_path = driver_cases.write_experiment(d)
+        ctrl = json.load(open(ctrl_path))
+        plan0 = jobs.control(ctrl_path, vex_path, d)
+        per = {}
+        for sci, sc in enumerate(plan0["scans"]):
+            for e in sc["stations"]:
+                per.setdefault(e["station"], []).append((sci, e))
+        recs, params = {}, {}
+        start = plan0["jobs"][0]["experiment_start"]
+        for s, scans in per.items():
+            e = scans[0][1]
+            ip = e["input"]
+            rec = b"".join(open(os.path.join(d, u[7:]), "rb").read() for u in ctrl["data_sources"][e["name"]])
+            chans = [c for c in ip["channels"] if not (ip["n_tracks"] == 0 and c["tracks"][0] < 0)]
+            recs[s] = rec
+            params[s] = dict(ref_ticks=start, offset_ticks=e["reader_offset"], track_bit_rate=ip["track_bit_rate"],
+                             frame_size=ip["frame_size"] if ip["data_format"] == "VDIF" else 0,
+                             n_tracks=ip["n_tracks"], bits=chans[0]["bits_per_sample"],
+                             channel_tracks=[c["tracks"] for c in chans])
+        fmt = {s: "vdif" if per[s][0][1]["input"]["data_format"] == "VDIF" else "mark5b" for s in per}
+        # the input node's current time at its first scan: its reader's first block
+        first = {s: jobs.reader(recs[s], fmt[s], max_blocks=1, **params[s])[0]["start_ticks"] for s in per}
+        times = [(s, per[s][0][0], first[s]) for s in per]
+        plan = jobs.control(ctrl_path, vex_path, d, times)
+        per = {}
+        for sci, sc in enumerate(plan["scans"]):
+            for e in sc["stations"]:
+                per.setdefault(e["station"], []).append((sci, e))
+        dels = {s: open(os.path.join(d, per[s][0][1]["delay_file"]), "rb").read() for s in per}
+        integr_us = int(round(ctrl["integr_time"] * 1e6))
+        slice_bytes = {}  # (station, channel in scan) -> [protocol bytes per slice]
+        for s, scans in per.items():
+            p = params[s]
+            ip = scans[0][1]["input"]
+            iv = [(plan["scans"][sci]["first_slice_start"], plan["scans"][sci]["stop"], e["stop_time"])
+                  for sci, e in scans]
+            blocks = jobs.schedule(recs[s], fmt[s], intervals=iv, **p)
+            # A block whose data buffer the tasklet reused for a later read
+            # (the next interval's first block) shows that read's bytes in the
+            # dump; it carries its own, the reader's block of the same time
+            thread_mode = ip["n_tracks"] == 0
+            own = {(b["channel"] if thread_mode else 0, b["start_ticks"]): b["data"]
+                   for b in jobs.reader(recs[s], fmt[s], **p)}
+            last_of_buffer = {b["buffer"]: k for k, b in enumerate(blocks)}
+            for k, b in enumerate(blocks):
+                if b["data"] is not None and last_of_buffer[b["buffer"]] != k:
+                    b["data"] = own[(b["channel"] if thread_mode else 0, b["start_ticks"])]
+            nch = len(p["channel_tracks"])
+            chan_blocks = [[] for _ in range(nch)]
+            if ip["n_tracks"] == 0:  # one channel per VDIF thread: the blocks as they are
+                for b in blocks:
+                    data = b["data"] if b["data"] is not None else bytes(b["size"])
+                    chan_blocks[b["channel"]].append((b["start_ticks"], data, b["invalid"]))
+            else:
+                word = 4 if ip["n_tracks"] <= 32 else 8
+                fan_out = len(p["channel_tracks"][0])
+                words = b"".join(b["data"] if b["data"] is not None else bytes(b["size"]) for b in blocks)
+                outs = jobs.extract(words, word, p["bits"], len(words) // word, p["channel_tracks"])
+                pos = 0
+                for b in blocks:
+                    n = b["size"] * fan_out // (8 * word)
+                    inv = [(bb * fan_out // (8 * word), nn * fan_out // (8 * word)) for bb, nn in b["invalid"]]
+                    for c in range(nch):
+                        chan_blocks[c].append((b["start_ticks"], outs[c][pos:pos + n], inv))
+                    pos += n
+            sr = ip["track_bit_rate"] * len(p["channel_tracks"][0]) // p["bits"]
+            delays = {}
+            for sci, e in scans:
+                sc = plan["scans"][sci]
+                delays[sci] = jobs.delays(dels[s], sc["first_slice_start"], sc["stop"], sr, p["bits"],
+                                          clock=(e["clock_offset"], e["clock_rate"], e["clock_epoch"]))[0]
+            fft = ip["fft_size"]
+            size = timebase.nr_ffts_per_integration_slice(integr_us, sr, fft) * fft
+            for c in range(nch):
+                sl = [(j["start_time"], j["stop_time"], size, delays[j["scan"]]) for j in plan["jobs"]
+                      if any(i["station"] == s and i["channel_in_scan"] == c for i in j["inputs"])]
+                if sl:
+                    slice_bytes[(s, c)] = jobs.protocol(chan_blocks[c], sl, sr, p["bits"], integr_us)
+            print("station", s, len(blocks), "blocks")
+        outs, used = [], {}
+        for j in plan["jobs"]:
+            n_st = len(ctrl["stations"])
+            tables, clocks, table_of, streams, protos, uvws = [], [], {}, [], [], []
+            sc_st = {e["station"]: e for e in plan["scans"][j["scan"]]["stations"]}
+            by_stream = {i["stream"]: i for i in j["inputs"]}
+            tmid = j["start_time"] + j["integration_time"] // 2
+            for sp in j["stations"]:
+                s = sp["station_stream"] % n_st
+                if s not in table_of:
+                    table_of[s] = len(tables)
+                    tables.append(dels[s])
+                    e = sc_st[s]
+                    clocks.append((e["clock_offset"], e["clock_rate"], e["clock_epoch"]))
+                streams.append((sp["station_number"], sp["station_stream"], sp["sample_rate"], sp["channel_freq"],
+                                sp["bandwidth"], sp["sideband"], sp["polarisation"], sp["bits_per_sample"],
+                                sp["lo_offset"], sp["tsys_freq"], table_of[s]))
+                i = by_stream[sp["station_stream"]]
+                key = (i["station"], i["channel_in_scan"])
+                k = used.get(key, 0)
+                used[key] = k + 1
+                protos.append([slice_bytes[key][k]])
+                uvws.append([jobs.uvw(dels[s], [(0, tmid)])[0]])
+            job = dict(experiment_start_ticks=j["experiment_start"], start_ticks=j["start_time"],
+                       integration_time_us=integr_us, sub_integration_time_us=int(round(j["sub_integration_time"] / 512)),
+                       number_channels=j["number_channels"], fft_size_delaycor=j["fft_size_delaycor"],
+                       fft_size_correlation=j["fft_size_correlation"], sample_rate=j["sample_rate"],
+                       channel_freq=j["channel_freq"], bandwidth=j["bandwidth"], sideband=j["sideband"],
+                       frequency_nr=j["frequency_nr"], polarisation=j["polarisation"],
+                       cross_polarize=int(j["cross_polarize"]), reference_station=j["reference_station"],
+                       window=j["window"], source=j["source"], integration_nr=j["integration_nr"], n_integrations=1,
+                       streams=streams, del_bytes=tables, clocks=clocks, protocols=protos, uvw=[uvws])
+            outs.append(np.frombuffer(jobs.correlate(job)["cor"], dtype=np.uint8))
+            print("job", j["slice_nr"], "integration", j["integration_nr"], len(outs[-1]), "bytes")
+        header = plan["header"]
+    np.savez_compressed(os.path.join(HERE, "driver.npz"), header=json.dumps(header),
+                        slices=np.array(len(outs)), **{"slice%d" % k: o for k, o in enumerate(outs)})
+
+
 if __name__ == "__main__":
     make_control()
+    make_driver()
     make_output_header()
     make_phasecal()
     make_formats()

@@ -1,0 +1,101 @@
+"""The single-GPU driver (sfxc_gpu.run: control file + VEX file -> .cor file)
+on a small experiment of three stations in three recording formats
+(tests/driver_cases.py), against the reference's own classes stage by stage
+(tests/golden/driver.npz: its plan, reader tasklet, channel extractor, delays,
+input-node writer and correlation core, composed as its nodes compose them):
+the global header's fields, every slice's headers byte for byte, the
+visibilities within the FP32 tolerance (1e-5 relative L2 per baseline; 1e-4
+for the tensor-core X-step)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import driver_cases
+from sfxc_gpu import lib as L
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden", "driver.npz")
+NCHAN = 256
+
+
+def _run(tmp_path, x_mode):
+    from sfxc_gpu import run
+    d = str(tmp_path)
+    ctrl, vex = driver_cases.write_experiment(d)
+    old = os.getcwd()
+    os.chdir(d)  # the delay directory of the control file is relative to the working directory
+    try:
+        files = run.correlate(ctrl, vex, x_mode=x_mode)
+    finally:
+        os.chdir(old)
+    assert list(files) == [os.path.join(d, "out", "n24x1.cor")]
+    return files[os.path.join(d, "out", "n24x1.cor")]
+
+
+def _global_fields(g):
+    (size,) = np.frombuffer(g[:4], dtype=np.int32)
+    year, day = np.frombuffer(g[36:40], dtype=np.int16)
+    start, nchan, tint, fmt_version, version = np.frombuffer(g[40:60], dtype=np.int32)
+    pol = g[60]
+    job, subjob = np.frombuffer(g[76:84], dtype=np.int32)
+    return dict(header_size=int(size), experiment=g[4:36].split(b"\0")[0].decode(), start_year=int(year),
+                start_day=int(day), start_time=int(start), number_channels=int(nchan), integration_time=int(tint),
+                polarisation_type=int(pol), job_nr=int(job), subjob_nr=int(subjob))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("x_mode,tol", [(L.X_FP32, 1e-5), (L.X_TC_HILO, 1e-4)])
+def test_driver_matches_reference_stages(tmp_path, x_mode, tol):
+    from sfxc_gpu import correlator
+    cor = _run(tmp_path, x_mode)
+    g = np.load(GOLDEN)
+    want = json.loads(str(g["header"]))
+    head, hdrs, vis = driver_cases.split_slices(cor, NCHAN)
+    fields = _global_fields(head)
+    assert fields["header_size"] == 84
+    for k in ("experiment", "start_year", "start_day", "start_time", "number_channels", "integration_time",
+              "polarisation_type", "job_nr", "subjob_nr"):
+        assert fields[k] == want[k], k
+    n = int(g["slices"])
+    assert len(hdrs) == n == 7  # 4 + 3 one-second slices of the two scans
+    for k in range(n):
+        rh, rv = correlator.split_output(g["slice%d" % k].tobytes(), NCHAN)
+        assert rh[:4] == b"\0\0\0\0"  # file index 0: the output node strips it
+        assert hdrs[k] == rh[4:], "slice %d headers" % k
+        assert len(vis[k]) == len(rv) == 18  # 6 streams: 6 autos + 12 crosses between stations
+        for b, (x, y) in enumerate(zip(vis[k], rv)):
+            err = np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-30)
+            assert err <= tol, "slice %d baseline %d: %.3g" % (k, b, err)
+
+
+def test_driver_refuses_what_it_does_not_run(tmp_path, sfxc_lib):
+    """Mark4 recordings (no Mark5A reader) and the phased array stop the
+    driver before it takes a GPU."""
+    import control_cases
+    from sfxc_gpu import run
+    case = control_cases.cases()["mark4_tracks"]
+    ctrl, vex = control_cases.write_case(case, str(tmp_path / "mk4"))
+    with pytest.raises(run.DriverError, match="Mark4 recordings are not read"):
+        run.correlate(ctrl, vex)
+    case = dict(control_cases.cases()["vdif_multichannel"])
+    case["ctrl"] = dict(case["ctrl"], phased_array=True)
+    ctrl, vex = control_cases.write_case(case, str(tmp_path / "pa"))
+    with pytest.raises(run.DriverError, match="phased array"):
+        run.correlate(ctrl, vex)
+
+
+def test_driver_plan_of_the_experiment(tmp_path, sfxc_lib):
+    """The experiment's plan: seven jobs, cross-polarised, Wb's reader one
+    second off, each station in its own format."""
+    from sfxc_gpu import control
+    d = str(tmp_path)
+    ctrl, vex = driver_cases.write_experiment(d)
+    p = control.plan(ctrl, vex)
+    assert [j["integration_nr"] for j in p["jobs"]] == [0, 1, 2, 3, 6, 7, 8]
+    assert all(j["cross_polarize"] and len(j["stations"]) == 6 for j in p["jobs"])
+    st = {e["name"]: e for e in p["scans"][0]["stations"]}
+    assert st["Wb"]["reader_offset"] == 512_000_000 and st["Ef"]["reader_offset"] == 0
+    assert {n: (e["input"]["data_format"], e["input"]["n_tracks"]) for n, e in st.items()} == \
+        {"Ef": ("VDIF", 8), "Wb": ("VDIF", 0), "On": ("Mark5B", 8)}
