@@ -70,13 +70,15 @@ def delays(del_bytes, start_ticks, stop_ticks, sample_rate, bits, probes=(), clo
 
 
 def protocol(blocks, slices, sample_rate, bits, integr_time_us, station_number=0, impl="reference",
-             phasecal_ticks=None):
+             phasecal_ticks=None, channel=None):
     """Input_node_data_writer protocol bytes for each slice.
 
     blocks: list of (start_ticks, bytes, [(invalid_begin, nr_invalid), ...])
     slices: list of (start_ticks, stop_ticks, nr_samples, delay_list)
     phasecal_ticks: phase-cal integration time; when given, returns
     (protocols, phase-cal message bytes) (Input_node_data_writer::do_phasecal)
+    channel: the channel's {sideband, polarisation, frequency_number} for
+    those messages (default U, R, 0)
     """
     with tempfile.TemporaryDirectory() as d:
         blob = os.path.join(d, "blocks.bin")
@@ -90,6 +92,9 @@ def protocol(blocks, slices, sample_rate, bits, integr_time_us, station_number=0
         lines = [("sample_rate", sample_rate), ("bits_per_sample", bits),
                  ("integr_time_us", integr_time_us), ("station_number", station_number),
                  ("blockfile", blob)]
+        if channel is not None:
+            lines.append(("channel_params", channel["sideband"], channel["polarisation"],
+                          channel["frequency_number"]))
         for st, pos, n, inv in offs:
             flat = [x for pair in inv for x in pair]
             lines.append(("block", st, pos, n, *flat))

@@ -205,6 +205,7 @@ static int mode_delays(const Kv &kv, const char *outfile) {
 // -------------------------------------------------------------- protocol ---
 // Input_node_data_writer over in-memory channel blocks.
 //   sample_rate, bits_per_sample, integr_time_us, station_number
+//   [channel_params <sideband> <polarisation> <frequency number>]
 //   blockfile <path> ; blocks "block#k start_ticks offset size [inv_begin n]..."
 //   delays <path to delay list from mode_delays>
 //   slice#k start_ticks stop_ticks nr_samples
@@ -219,6 +220,12 @@ static int mode_protocol(const Kv &kv, const char *outfile) {
   ch.sideband = 'U';
   ch.polarisation = 'R';
   ch.frequency_number = 0;
+  if (has(kv, "channel_params")) {  // sideband, polarisation, frequency number of the phase-cal messages
+    const std::vector<std::string> &c = get(kv, "channel_params");
+    ch.sideband = c[0][0];
+    ch.polarisation = c[1][0];
+    ch.frequency_number = std::atoi(c[2].c_str());
+  }
   for (int b = 0; b < bps; b++) ch.tracks.push_back(b);
   param.channels.push_back(ch);
   param.track_bit_rate = sample_rate;  // sample_rate() = track_bit_rate * subsamples_per_sample

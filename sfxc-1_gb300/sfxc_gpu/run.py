@@ -13,7 +13,8 @@ schedule), its channels, and each channel's input-node protocol for every
 time slice it feeds are made on the device; each job's streams are pushed
 device to device into one correlator context, which writes the output
 slices; the output node writes them in slice order to the output file(s)
-with the global header.  Delay tables are the stations' .del files (the
+with the global header, and the tsys and phase-cal records to their files
+when the control file names them.  Delay tables are the stations' .del files (the
 manager's delay_directory); the delay model generator is not run.
 
 Set-ups the reference correlates that this driver refuses: Mark4 and VLBA
@@ -66,6 +67,36 @@ def _del_scans(del_bytes):
     return out
 
 
+_TICKS_PER_DAY = 86400 * 512_000_000
+
+
+def _mjd_secs(ticks):
+    """The uint32 MJD and seconds of day the output node writes for a time
+    (Time::get_mjd and get_time truncated, sfxc/src/correlator_time.cc:50-66)."""
+    return 51544 + ticks // _TICKS_PER_DAY, (ticks % _TICKS_PER_DAY) // 512_000_000
+
+
+def tsys_record(msg):
+    """The tsys file record of a correlator's tsys message (four uint8
+    station, frequency number, sideband, polarisation; int64 start ticks; four
+    int64 counts): the ids, uint32 MJD, uint32 seconds, the counts as uint64
+    (Output_node_controller, sfxc/src/output_node_controller.cc:171-205)."""
+    (t,) = struct.unpack_from("<q", msg, 4)
+    return bytes(msg[:4]) + struct.pack("<II", *_mjd_secs(t)) + bytes(msg[12:44])
+
+
+def phasecal_record(msg):
+    """The phase-cal file record of an input node's phase-cal message (four
+    uint8 ids; int64 start and length ticks; int32 bin count P; P int32 bins):
+    the ids, uint32 MJD, uint32 seconds, uint32 length in seconds, uint32 P,
+    the bins (sfxc/src/output_node_controller.cc:110-155)."""
+    t, length = struct.unpack_from("<qq", msg, 4)
+    (p,) = struct.unpack_from("<i", msg, 20)
+    mjd, secs = _mjd_secs(t)
+    return bytes(msg[:4]) + struct.pack("<IIII", mjd, secs, (length % _TICKS_PER_DAY) // 512_000_000, p) + \
+        bytes(msg[24:24 + 4 * p])
+
+
 class _Station:
     """One station's recording on the device and its per-scan set-up."""
 
@@ -106,7 +137,9 @@ class _Station:
 
 
 def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
-    """Runs the whole correlation; returns {output path: bytes written}."""
+    """Runs the whole correlation; returns {path: bytes written} of the
+    output file(s) and, when the control file names them, the tsys and
+    phase-cal files."""
     log = log or (lambda *a: None)
     ctrl_path, vex_path = os.path.abspath(ctrl_path), os.path.abspath(vex_path)
     ctrl_dir = os.path.dirname(ctrl_path)
@@ -183,6 +216,23 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
             st.rec.protocol(c, [x for _, x in sl], st.sample_rate, st.bits, integration_us, copy=False)
         log("station %s: %d channel streams" % (st.name, len(st.slices)))
 
+    # phase-cal of every channel the writers take up (Input_node_data_writer::do_phasecal)
+    station_number = {sp["station_stream"] % n_st: sp["station_number"] for j in jobs for sp in j["stations"]}
+    pcal = []
+    if ctrl.get("phasecal_file") and per_station:
+        for s in sorted(per_station):
+            st = stations[s]
+            ticks = st.input["phasecal_integr_time"]
+            if ticks <= 0:
+                continue
+            for c in sorted(st.slices):
+                ch = st.channels[c]
+                pc = correlator.PhaseCal(node, st.sample_rate, st.bits, ticks, station_number.get(s, 0),
+                                         ch["frequency_number"], 1 if ch["sideband"] == "U" else 0,
+                                         1 if ch["polarisation"] == "L" else 0)
+                pcal += pc.push(st.rec.channel(c))
+                pc.close()
+
     # the correlator node, job after job; the output node
     pulsars = {p["name"]: p for p in plan.get("pulsars", [])}
     mask = plan.get("mask")
@@ -194,6 +244,7 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
                                  correlator_version=0, polarisation_type=h["polarisation_type"],
                                  correlator_branch="gb300", job_nr=h["job_nr"], subjob_nr=h["subjob_nr"])
     slice_index = {}  # (station, channel) -> next slice of its protocol
+    tsys_msgs = []
     for ji, j in enumerate(jobs):
         sc = plan["scans"][j["scan"]]
         sc_station = {e["station"]: e for e in sc["stations"]}
@@ -249,8 +300,9 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
             i = slice_index.get(key, 0)
             slice_index[key] = i + 1
             stations[inp["station"]].rec.push(inp["channel_in_scan"], i, node, k)
-        data, _tsys = node.run_integration()
+        data, tsys = node.run_integration()
         out.put_slice(j["slice_nr"], data, n_bins)
+        tsys_msgs += tsys
         log("slice %d: %s channel %d integration %d" % (j["slice_nr"], sc["name"], j["channel"],
                                                         j["integration_nr"]))
     files = out.finish()
@@ -261,6 +313,15 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
         with open(path, "wb") as f:
             f.write(b)
         written[path] = b
+    side = [("tsys_file", [tsys_record(m) for m in tsys_msgs]), ("phasecal_file", [phasecal_record(m) for m in pcal])]
+    for key, records in side:
+        if ctrl.get(key):
+            path = _path(ctrl[key], ctrl_dir)
+            os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+            b = b"".join(records)
+            with open(path, "wb") as f:
+                f.write(b)
+            written[path] = b
     out.close()
     for st in stations.values():
         st.rec.close()

@@ -49,6 +49,7 @@ def ctrl_dict():
     return {"exper_name": "N24X1", "stations": STATIONS, "start": "2024y100d12h00m00s",
             "stop": "2024y100d12h00m09s", "integr_time": 1.0, "number_channels": 256, "cross_polarize": True,
             "channels": ["CH01", "CH02"], "output_file": "file://out/n24x1.cor", "delay_directory": "file://delays",
+            "tsys_file": "file://out/n24x1.tsys", "phasecal_file": "file://out/n24x1.pcal", "phasecal_integr_time": 1,
             "data_sources": {"Ef": ["file://data/ef.vdif"], "Wb": ["file://data/wb_a.vdif", "file://data/wb_b.vdif"],
                              "On": ["file://data/on.m5b"]}}
 

@@ -411,6 +411,9 @@ def make_driver():
         dels = {s: open(os.path.join(d, per[s][0][1]["delay_file"]), "rb").read() for s in per}
         integr_us = int(round(ctrl["integr_time"] * 1e6))
         slice_bytes = {}  # (station, channel in scan) -> [protocol bytes per slice]
+        pcal = {}  # (station, channel in scan) -> phase-cal message bytes
+        n_st = len(ctrl["stations"])
+        station_nr = {sp["station_stream"] % n_st: sp["station_number"] for j in plan["jobs"] for sp in j["stations"]}
         for s, scans in per.items():
             p = params[s]
             ip = scans[0][1]["input"]
@@ -428,6 +431,7 @@ def make_driver():
                 if b["data"] is not None and last_of_buffer[b["buffer"]] != k:
                     b["data"] = own[(b["channel"] if thread_mode else 0, b["start_ticks"])]
             nch = len(p["channel_tracks"])
+            chan_params = [c for c in ip["channels"] if not (ip["n_tracks"] == 0 and c["tracks"][0] < 0)]
             chan_blocks = [[] for _ in range(nch)]
             if ip["n_tracks"] == 0:  # one channel per VDIF thread: the blocks as they are
                 for b in blocks:
@@ -457,9 +461,13 @@ def make_driver():
                 sl = [(j["start_time"], j["stop_time"], size, delays[j["scan"]]) for j in plan["jobs"]
                       if any(i["station"] == s and i["channel_in_scan"] == c for i in j["inputs"])]
                 if sl:
-                    slice_bytes[(s, c)] = jobs.protocol(chan_blocks[c], sl, sr, p["bits"], integr_us)
+                    slice_bytes[(s, c)], msgs = jobs.protocol(chan_blocks[c], sl, sr, p["bits"], integr_us,
+                                                              station_number=station_nr[s],
+                                                              phasecal_ticks=ip["phasecal_integr_time"],
+                                                              channel=chan_params[c])
+                    pcal[(s, c)] = msgs
             print("station", s, len(blocks), "blocks")
-        outs, used = [], {}
+        outs, tsys, used = [], [], {}
         for j in plan["jobs"]:
             n_st = len(ctrl["stations"])
             tables, clocks, table_of, streams, protos, uvws = [], [], {}, [], [], []
@@ -491,11 +499,15 @@ def make_driver():
                        cross_polarize=int(j["cross_polarize"]), reference_station=j["reference_station"],
                        window=j["window"], source=j["source"], integration_nr=j["integration_nr"], n_integrations=1,
                        streams=streams, del_bytes=tables, clocks=clocks, protocols=protos, uvw=[uvws])
-            outs.append(np.frombuffer(jobs.correlate(job)["cor"], dtype=np.uint8))
+            res = jobs.correlate(job)
+            outs.append(np.frombuffer(res["cor"], dtype=np.uint8))
+            tsys.append(np.frombuffer(res["tsys"], dtype=np.uint8))
             print("job", j["slice_nr"], "integration", j["integration_nr"], len(outs[-1]), "bytes")
         header = plan["header"]
+    pc = {"pcal_%d_%d" % k: np.frombuffer(v, dtype=np.uint8) for k, v in pcal.items()}
     np.savez_compressed(os.path.join(HERE, "driver.npz"), header=json.dumps(header),
-                        slices=np.array(len(outs)), **{"slice%d" % k: o for k, o in enumerate(outs)})
+                        slices=np.array(len(outs)), **{"slice%d" % k: o for k, o in enumerate(outs)},
+                        **{"tsys%d" % k: t for k, t in enumerate(tsys)}, **pc)
 
 
 if __name__ == "__main__":

@@ -5,7 +5,8 @@ on a small experiment of three stations in three recording formats
 input-node writer and correlation core, composed as its nodes compose them):
 the global header's fields, every slice's headers byte for byte, the
 visibilities within the FP32 tolerance (1e-5 relative L2 per baseline; 1e-4
-for the tensor-core X-step)."""
+for the tensor-core X-step), and the tsys and phase-cal files made of the
+reference's own messages."""
 import json
 import os
 
@@ -30,8 +31,9 @@ def _run(tmp_path, x_mode):
         files = run.correlate(ctrl, vex, x_mode=x_mode)
     finally:
         os.chdir(old)
-    assert list(files) == [os.path.join(d, "out", "n24x1.cor")]
-    return files[os.path.join(d, "out", "n24x1.cor")]
+    out = os.path.join(d, "out", "n24x1")
+    assert sorted(files) == [out + ".cor", out + ".pcal", out + ".tsys"]
+    return files[out + ".cor"], files[out + ".tsys"], files[out + ".pcal"]
 
 
 def _global_fields(g):
@@ -48,8 +50,8 @@ def _global_fields(g):
 @pytest.mark.gpu
 @pytest.mark.parametrize("x_mode,tol", [(L.X_FP32, 1e-5), (L.X_TC_HILO, 1e-4)])
 def test_driver_matches_reference_stages(tmp_path, x_mode, tol):
-    from sfxc_gpu import correlator
-    cor = _run(tmp_path, x_mode)
+    from sfxc_gpu import correlator, run
+    cor, tsys, pcal = _run(tmp_path, x_mode)
     g = np.load(GOLDEN)
     want = json.loads(str(g["header"]))
     head, hdrs, vis = driver_cases.split_slices(cor, NCHAN)
@@ -68,6 +70,18 @@ def test_driver_matches_reference_stages(tmp_path, x_mode, tol):
         for b, (x, y) in enumerate(zip(vis[k], rv)):
             err = np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-30)
             assert err <= tol, "slice %d baseline %d: %.3g" % (k, b, err)
+    # side files: the correlation core's tsys messages of every job, the input
+    # nodes' phase-cal messages of every station channel, as the output node
+    # writes them
+    msgs = [g["tsys%d" % k].tobytes() for k in range(n)]
+    assert tsys == b"".join(run.tsys_record(m[i:i + 44]) for m in msgs for i in range(0, len(m), 44))
+    want = b""
+    for key in sorted(k for k in g.files if k.startswith("pcal_")):
+        m = g[key].tobytes()
+        p = 24 + 4 * 400
+        assert len(m) % p == 0 and len(m) // p == 6  # seven seconds of data, the last integration unfinished
+        want += b"".join(run.phasecal_record(m[i:i + p]) for i in range(0, len(m), p))
+    assert pcal == want
 
 
 def test_driver_refuses_what_it_does_not_run(tmp_path, sfxc_lib):
@@ -99,3 +113,14 @@ def test_driver_plan_of_the_experiment(tmp_path, sfxc_lib):
     assert st["Wb"]["reader_offset"] == 512_000_000 and st["Ef"]["reader_offset"] == 0
     assert {n: (e["input"]["data_format"], e["input"]["n_tracks"]) for n, e in st.items()} == \
         {"Ef": ("VDIF", 8), "Wb": ("VDIF", 0), "On": ("Mark5B", 8)}
+
+
+def test_side_file_records():
+    """The output node's tsys and phase-cal records of known messages."""
+    import struct
+    from sfxc_gpu import run
+    t = ((60409 - 51544) * 86400 + 43201) * 512_000_000 + 12345  # 2024y100d12h00m01s and a bit
+    msg = bytes([2, 1, 1, 0]) + struct.pack("<q4q", t, 10, 20, 30, 40)
+    assert run.tsys_record(msg) == bytes([2, 1, 1, 0]) + struct.pack("<II4Q", 60409, 43201, 10, 20, 30, 40)
+    msg = bytes([0, 3, 0, 1]) + struct.pack("<qqi", t, 2 * 512_000_000, 3) + struct.pack("<3i", -5, 0, 7)
+    assert run.phasecal_record(msg) == bytes([0, 3, 0, 1]) + struct.pack("<IIII3i", 60409, 43201, 2, 3, -5, 0, 7)
