@@ -272,6 +272,10 @@ def correlate_lines(job, d, dump=False, precision=32, dump_bins=False):
         lines.append(("n_phase_centers", int(job["n_phase_centers"])))
         if job.get("pc_file_index") is not None:
             lines.append(("pc_file_index",) + tuple(int(x) for x in job["pc_file_index"]))
+    if job.get("source_list"):
+        lines.append(("source_list",) + tuple(job["source_list"]))
+    if job.get("pulsar_mode"):
+        lines.append(("pulsar_mode", 1))
     if "pulsar" in job:
         lines.append(("pulsar",) + tuple(job["pulsar"]))
         for pc in job["polyco"]:

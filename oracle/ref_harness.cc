@@ -394,7 +394,11 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
   std::memset(p.source, 0, sizeof(p.source));
   std::strncpy(p.source, get(kv, "source")[0].c_str(), 10);
   p.n_phase_centers = has(kv, "n_phase_centers") ? geti(kv, "n_phase_centers") : 1;
-  p.pulsar_binning = has(kv, "pulsar") ? 1 : 0;
+  // the pulsar core for a pulsar source; pulsar mode for any other source of
+  // a pulsar-binning run (Correlator_node::set_parameters,
+  // sfxc/src/correlator_node.cc:351-361): the normal core, file index 1
+  const bool pulsar_core = has(kv, "pulsar");
+  p.pulsar_binning = pulsar_core || (has(kv, "pulsar_mode") && geti(kv, "pulsar_mode") != 0) ? 1 : 0;
   p.pulsar_parameters = 0;
   p.mask_parameters = 0;
   // Mask_parameters of the ctrl file: float32 files of the mask (M + 1) and
@@ -440,7 +444,7 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
   }
 
   Pulsar_parameters::Pulsar pulsar;
-  if (p.pulsar_binning) {
+  if (pulsar_core) {
     const std::vector<std::string> &v = get(kv, "pulsar");  // nbins gate_start gate_stop
     std::memset(pulsar.name, 0, sizeof(pulsar.name));
     std::strncpy(pulsar.name, p.source, 10);
@@ -473,7 +477,16 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
                                                       ? (Correlation_core *)new Correlation_core_phased()
                                                       : new Correlation_core());
   boost::shared_ptr<Correlation_core_pulsar> core_pulsar(new Correlation_core_pulsar());
-  Correlation_core *core = p.pulsar_binning ? (Correlation_core *)core_pulsar.get() : core_normal.get();
+  Correlation_core *core = pulsar_core ? (Correlation_core *)core_pulsar.get() : core_normal.get();
+  // the manager's source list of a multiple-phase-centre run
+  // (correlator_node_controller.cc:76-82): each centre's output then carries
+  // its source's place in the list as file index (correlation_core.cc:55-58)
+  if (has(kv, "source_list")) {
+    const std::vector<std::string> &v = get(kv, "source_list");
+    std::map<std::string, int> m;
+    for (size_t q = 0; q < v.size(); q++) m[v[q]] = (int)q;
+    core_normal->add_source_list(m);
+  }
   boost::shared_ptr<Memory_writer> out(new Memory_writer());
   core->set_data_writer(out);
   const size_t ring_size = has(kv, "ring_bytes") ? (size_t)getll(kv, "ring_bytes") : (size_t)37100000;
@@ -525,7 +538,7 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
         for (int q = 0; q < 3 * p.n_phase_centers; q++)
           uvw[s][q] = uvw_in[((size_t)it * nstreams + i) * 3 * p.n_phase_centers + q];
     }
-    if (p.pulsar_binning)
+    if (pulsar_core)
       core_pulsar->set_parameters(p, pulsar, akima, uvw, 0);
     else
       core_normal->set_parameters(p, akima, uvw, 0);
@@ -599,7 +612,7 @@ static int mode_correlate(const Kv &kv, const char *outdir) {
         write_file(b.str(), c.rows.empty() ? 0 : &c.rows[0], c.rows.size() * 8);
       }
     }
-    if (dump && p.pulsar_binning) {
+    if (dump && pulsar_core) {
       // The reference's own bin table of this integration: dedisperse_buffer()
       // recomputed per FFT after the integration (its scratch buffer is zero,
       // so the accumulators are unchanged), plus its phase constants.

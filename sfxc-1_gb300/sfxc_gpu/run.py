@@ -279,7 +279,7 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
                 job["polyco"] = [[pc["tmid"], pc["dm"], pc["ref_phase"], pc["ref_freq"], pc["obs_freq"]] + pc["coef"]
                                  for pc in p["polyco"]]
                 n_bins = p["nbins"] + 1
-        elif j["n_phase_centers"] > 1:
+        elif sources:  # multiple phase centres: every output carries its source's file index
             job["n_phase_centers"] = j["n_phase_centers"]
             job["pc_file_index"] = _phase_centre_files(_del_scans(tables[0]), j, sources)
             n_bins = j["n_phase_centers"]

@@ -362,8 +362,9 @@ def make_control():
         json.dump(out, f, indent=None, sort_keys=True, separators=(",", ":"))
 
 
-def make_driver():
-    """The reference's own stages over driver_cases' experiment (driver.npz):
+def make_driver(variant="plain"):
+    """The reference's own stages over driver_cases' experiment (driver.npz,
+    driver_<variant>.npz for the other variants):
     its plan (Control_parameters and the manager's dealing), for each station
     the reader tasklet's blocks over the scan intervals, Channel_extractor_5
     on them (a block whose buffer the tasklet reused for its next read keeps
@@ -372,15 +373,18 @@ def make_driver():
     sfxc/src/channel_extractor_tasklet.cc:173-194; VDIF with one
     channel per thread takes the blocks as they are), Input_node_tasklet's
     delays per scan interval and Input_node_data_writer's protocol per slice,
-    then each job's Correlation_core output (with its file index) and u, v, w.
-    The glue between the stages restates Input_node and Correlator_node."""
+    then each job's Correlation_core(_pulsar) output (with its file index)
+    and u, v, w: the pulsar core for the pulsar's scan and file index 1 for
+    other sources of a pulsar run, the manager's source list for extra phase
+    centres (the core gives each centre its source's file index).  The glue
+    between the stages restates Input_node and Correlator_node."""
     import json
     import tempfile
     sys.path.insert(0, os.path.dirname(HERE))
     import driver_cases
     from sfxc_gpu import timebase
     with tempfile.TemporaryDirectory() as d:
-        ctrl_path, vex_path = driver_cases.write_experiment(d)
+        ctrl_path, vex_path = driver_cases.write_experiment(d, variant)
         ctrl = json.load(open(ctrl_path))
         plan0 = jobs.control(ctrl_path, vex_path, d)
         per = {}
@@ -489,7 +493,8 @@ def make_driver():
                 k = used.get(key, 0)
                 used[key] = k + 1
                 protos.append([slice_bytes[key][k]])
-                uvws.append([jobs.uvw(dels[s], [(0, tmid)])[0]])
+                npc = max(1, j["n_phase_centers"])
+                uvws.append(jobs.uvw(dels[s], [(pc, tmid) for pc in range(npc)]))
             job = dict(experiment_start_ticks=j["experiment_start"], start_ticks=j["start_time"],
                        integration_time_us=integr_us, sub_integration_time_us=int(round(j["sub_integration_time"] / 512)),
                        number_channels=j["number_channels"], fft_size_delaycor=j["fft_size_delaycor"],
@@ -499,20 +504,35 @@ def make_driver():
                        cross_polarize=int(j["cross_polarize"]), reference_station=j["reference_station"],
                        window=j["window"], source=j["source"], integration_nr=j["integration_nr"], n_integrations=1,
                        streams=streams, del_bytes=tables, clocks=clocks, protocols=protos, uvw=[uvws])
+            if ctrl.get("pulsar_binning"):
+                ps = {x["name"]: x for x in plan["pulsars"]}
+                if j["source"] in ps:
+                    x = ps[j["source"]]
+                    job["pulsar"] = (x["nbins"], x["gate_start"], x["gate_stop"])
+                    job["polyco"] = [[c["tmid"], c["dm"], c["ref_phase"], c["ref_freq"], c["obs_freq"]] + c["coef"]
+                                     for c in x["polyco"]]
+                else:
+                    job["pulsar_mode"] = 1
+            if plan["sources"]:
+                job["source_list"] = plan["sources"]
+                job["n_phase_centers"] = j["n_phase_centers"]
             res = jobs.correlate(job)
             outs.append(np.frombuffer(res["cor"], dtype=np.uint8))
             tsys.append(np.frombuffer(res["tsys"], dtype=np.uint8))
             print("job", j["slice_nr"], "integration", j["integration_nr"], len(outs[-1]), "bytes")
         header = plan["header"]
+        plan["output_files"] = [f.replace(d, "<dir>") for f in plan["output_files"]]
     pc = {"pcal_%d_%d" % k: np.frombuffer(v, dtype=np.uint8) for k, v in pcal.items()}
-    np.savez_compressed(os.path.join(HERE, "driver.npz"), header=json.dumps(header),
+    name = "driver.npz" if variant == "plain" else "driver_%s.npz" % variant
+    np.savez_compressed(os.path.join(HERE, name), header=json.dumps(header), files=json.dumps(plan["output_files"]),
                         slices=np.array(len(outs)), **{"slice%d" % k: o for k, o in enumerate(outs)},
                         **{"tsys%d" % k: t for k, t in enumerate(tsys)}, **pc)
 
 
 if __name__ == "__main__":
     make_control()
-    make_driver()
+    for v in ("plain", "pulsar", "phase_centres"):
+        make_driver(v)
     make_output_header()
     make_phasecal()
     make_formats()

@@ -21,16 +21,20 @@ GOLDEN = os.path.join(HERE, "golden", "driver.npz")
 NCHAN = 256
 
 
-def _run(tmp_path, x_mode):
+def _correlate(d, x_mode, variant="plain"):
     from sfxc_gpu import run
-    d = str(tmp_path)
-    ctrl, vex = driver_cases.write_experiment(d)
+    ctrl, vex = driver_cases.write_experiment(d, variant)
     old = os.getcwd()
     os.chdir(d)  # the delay directory of the control file is relative to the working directory
     try:
-        files = run.correlate(ctrl, vex, x_mode=x_mode)
+        return run.correlate(ctrl, vex, x_mode=x_mode)
     finally:
         os.chdir(old)
+
+
+def _run(tmp_path, x_mode):
+    d = str(tmp_path)
+    files = _correlate(d, x_mode)
     out = os.path.join(d, "out", "n24x1")
     assert sorted(files) == [out + ".cor", out + ".pcal", out + ".tsys"]
     return files[out + ".cor"], files[out + ".tsys"], files[out + ".pcal"]
@@ -82,6 +86,37 @@ def test_driver_matches_reference_stages(tmp_path, x_mode, tol):
         assert len(m) % p == 0 and len(m) // p == 6  # seven seconds of data, the last integration unfinished
         want += b"".join(run.phasecal_record(m[i:i + p]) for i in range(0, len(m), p))
     assert pcal == want
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", ["pulsar", "phase_centres"])
+@pytest.mark.parametrize("x_mode,tol", [(L.X_FP32, 1e-5), (L.X_TC_HILO, 1e-4)])
+def test_driver_variants_match_reference_stages(tmp_path, variant, x_mode, tol):
+    """Pulsar binning (the pulsar's scan in 4 + 1 bins, one file per bin;
+    the other scan's source as file 1) and extra phase centres (the first
+    scan's two sources, one file per source): every output file's slices
+    against the reference's core outputs routed by their file index."""
+    from sfxc_gpu import correlator
+    d = str(tmp_path)
+    files = _correlate(d, x_mode, variant)
+    g = np.load(os.path.join(HERE, "golden", "driver_%s.npz" % variant))
+    names = [f.replace("<dir>", d)[7:] for f in json.loads(str(g["files"]))]
+    assert sorted(files) == sorted(names)
+    want = {k: [] for k in range(len(names))}
+    for k in range(int(g["slices"])):
+        for fi, part in driver_cases.output_parts(g["slice%d" % k].tobytes(), NCHAN):
+            want[fi].append(part)
+    assert all(want.values())  # every file has slices
+    for fi, name in enumerate(names):
+        head, hdrs, vis = driver_cases.split_slices(files[name], NCHAN)
+        assert _global_fields(head)["header_size"] == 84
+        assert len(hdrs) == len(want[fi]), name
+        for k, part in enumerate(want[fi]):
+            rh, rv = correlator.split_output(b"\0\0\0\0" + part, NCHAN)
+            assert hdrs[k] == rh[4:], "%s slice %d headers" % (name, k)
+            for b, (x, y) in enumerate(zip(vis[k], rv)):
+                err = np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-30)
+                assert err <= tol, "%s slice %d baseline %d: %.3g" % (name, k, b, err)
 
 
 def test_driver_refuses_what_it_does_not_run(tmp_path, sfxc_lib):
