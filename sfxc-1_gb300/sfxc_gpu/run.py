@@ -18,8 +18,8 @@ when the control file names them.  Delay tables are the stations' .del files (th
 manager's delay_directory); the delay model generator is not run.
 
 Set-ups the reference correlates that this driver refuses: Mark4 and VLBA
-recordings (no Mark5A reader), the phased array, and a station whose reader
-parameters change between scans.
+recordings (no Mark5A reader) and a station whose reader parameters change
+between scans.
 """
 import argparse
 import os
@@ -145,8 +145,6 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
     ctrl_dir = os.path.dirname(ctrl_path)
     plan = control.plan(ctrl_path, vex_path)
     ctrl = plan["ctrl"]
-    if ctrl.get("phased_array"):
-        raise DriverError("the phased array is not run by this driver")
     if not plan["jobs"]:
         raise DriverError("nothing to correlate between the start and stop times")
     names = ctrl["stations"]
@@ -268,7 +266,7 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
                    channel_freq=j["channel_freq"], sideband=j["sideband"], polarisation=j["polarisation"],
                    cross_polarize=int(j["cross_polarize"]), reference_station=j["reference_station"],
                    window=j["window"], integration_nr=j["integration_nr"], streams=streams, del_bytes=tables,
-                   clocks=clocks, n_integrations=1)
+                   clocks=clocks, n_integrations=1, phased_array=int(bool(ctrl.get("phased_array"))))
         n_bins = 1
         if j["pulsar_binning"]:
             p = pulsars.get(j["source"])

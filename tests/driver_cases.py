@@ -8,8 +8,8 @@ thread (and a clock more than a second off, so that its reader time is
 shifted by whole seconds), On Mark5B with eight bitstreams.  Two scans with a
 gap between them; the recordings run from before the first to after the
 last.  Cross-polarised correlation of the first frequency, 1 s integrations.
-Two variants take two of the stations for pulsar binning and for extra phase
-centres.  tests/golden/driver*.npz hold what the reference's own classes make of them,
+Three variants take two of the stations for pulsar binning, extra phase
+centres and the phased array.  tests/golden/driver*.npz hold what the reference's own classes make of them,
 stage by stage (tests/golden/make_golden.py: its plan, reader tasklet,
 channel extractor, delays, input-node writer and correlation core)."""
 import json
@@ -28,17 +28,17 @@ STATIONS = ["Ef", "Wb", "On"]
 WB_CLOCK = 1.0000021  # seconds: the reader takes 1 s of it
 
 
-VARIANTS = ("plain", "pulsar", "phase_centres")
+VARIANTS = ("plain", "pulsar", "phase_centres", "phased")
 PULSAR = "B0329+54"
 
 
 def _stations(variant):
-    return {"plain": STATIONS, "pulsar": ["Ef", "On"], "phase_centres": ["Ef", "Wb"]}[variant]
+    return {"plain": STATIONS, "pulsar": ["Ef", "On"], "phase_centres": ["Ef", "Wb"], "phased": ["Ef", "On"]}[variant]
 
 
 def _scan_sources(variant):
     return {"plain": (["SRC1"], ["SRC2"]), "pulsar": ([PULSAR], ["SRC2"]),
-            "phase_centres": (["SRC1", "SRC3"], ["SRC2"])}[variant]
+            "phase_centres": (["SRC1", "SRC3"], ["SRC2"]), "phased": (["SRC1"], ["SRC2"])}[variant]
 
 
 def vex_text(variant="plain"):
@@ -65,7 +65,8 @@ def ctrl_dict(variant="plain"):
     """plain: three stations cross-polarised, with the tsys and phase-cal
     files; pulsar: Ef and On, R only, the first scan on a pulsar (4 bins
     between pulse phases 0.1 and 0.9), the second on an ordinary source;
-    phase_centres: Ef and Wb, R only, the first scan with two sources."""
+    phase_centres: Ef and Wb, R only, the first scan with two sources;
+    phased: Ef and On summed as a phased array, R and L."""
     sts = _stations(variant)
     c = {"exper_name": "N24X1", "stations": sts, "start": "2024y100d12h00m00s",
          "stop": "2024y100d12h00m09s", "integr_time": 1.0, "number_channels": 256,
@@ -79,8 +80,10 @@ def ctrl_dict(variant="plain"):
     elif variant == "pulsar":
         c.update(channels=["CH01"], pulsar_binning=True,
                  pulsars={PULSAR: {"polyco_file": "file://b0329.polyco", "nbins": 4, "interval": [0.1, 0.9]}})
-    else:
+    elif variant == "phase_centres":
         c.update(channels=["CH01"], fft_size_correlation=256)
+    else:
+        c.update(channels=["CH01", "CH02"], phased_array=True)
     return c
 
 

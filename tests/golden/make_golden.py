@@ -513,6 +513,8 @@ def make_driver(variant="plain"):
                                      for c in x["polyco"]]
                 else:
                     job["pulsar_mode"] = 1
+            if ctrl.get("phased_array"):
+                job["phased_array"] = 1
             if plan["sources"]:
                 job["source_list"] = plan["sources"]
                 job["n_phase_centers"] = j["n_phase_centers"]
@@ -531,7 +533,7 @@ def make_driver(variant="plain"):
 
 if __name__ == "__main__":
     make_control()
-    for v in ("plain", "pulsar", "phase_centres"):
+    for v in ("plain", "pulsar", "phase_centres", "phased"):
         make_driver(v)
     make_output_header()
     make_phasecal()

@@ -89,13 +89,14 @@ def test_driver_matches_reference_stages(tmp_path, x_mode, tol):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("variant", ["pulsar", "phase_centres"])
+@pytest.mark.parametrize("variant", ["pulsar", "phase_centres", "phased"])
 @pytest.mark.parametrize("x_mode,tol", [(L.X_FP32, 1e-5), (L.X_TC_HILO, 1e-4)])
 def test_driver_variants_match_reference_stages(tmp_path, variant, x_mode, tol):
     """Pulsar binning (the pulsar's scan in 4 + 1 bins, one file per bin;
-    the other scan's source as file 1) and extra phase centres (the first
-    scan's two sources, one file per source): every output file's slices
-    against the reference's core outputs routed by their file index."""
+    the other scan's source as file 1), extra phase centres (the first
+    scan's two sources, one file per source) and the phased array (one summed
+    spectrum per sub-integration): every output file's slices against the
+    reference's core outputs routed by their file index."""
     from sfxc_gpu import correlator
     d = str(tmp_path)
     files = _correlate(d, x_mode, variant)
@@ -120,18 +121,13 @@ def test_driver_variants_match_reference_stages(tmp_path, variant, x_mode, tol):
 
 
 def test_driver_refuses_what_it_does_not_run(tmp_path, sfxc_lib):
-    """Mark4 recordings (no Mark5A reader) and the phased array stop the
-    driver before it takes a GPU."""
+    """Mark4 recordings (no Mark5A reader) stop the driver before it takes a
+    GPU."""
     import control_cases
     from sfxc_gpu import run
     case = control_cases.cases()["mark4_tracks"]
     ctrl, vex = control_cases.write_case(case, str(tmp_path / "mk4"))
     with pytest.raises(run.DriverError, match="Mark4 recordings are not read"):
-        run.correlate(ctrl, vex)
-    case = dict(control_cases.cases()["vdif_multichannel"])
-    case["ctrl"] = dict(case["ctrl"], phased_array=True)
-    ctrl, vex = control_cases.write_case(case, str(tmp_path / "pa"))
-    with pytest.raises(run.DriverError, match="phased array"):
         run.correlate(ctrl, vex)
 
 
