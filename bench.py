@@ -568,6 +568,82 @@ def measure_frontend(args, log):
             "data": "seeded uniform random payload words, cubic delay model"}
 
 
+DRIVER_NAME = ("sfxc <ctrl> <vex> on one GPU (sfxc_gpu.run): 8 stations, VDIF 16 channels x 2 bits x 64 MS/s, "
+               "8 x 32 MHz dual pol cross-polarised, 4096 channels, one 2 s scan, 1 s integrations")
+
+
+def measure_driver(args, log):
+    """The single-GPU driver on a synthetic experiment written to files
+    (tmpfs where the host has one): the control file and VEX schedule
+    planned, each station's 768 MB VDIF recording read from its file into
+    device memory, channelled and turned into protocol there, the 16 jobs
+    (8 subbands x 2 integrations, 16 streams each) correlated and the .cor
+    file written.  value: input samples correlated per second of the whole
+    run (host wall clock from the files to the written output)."""
+    import shutil
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import control_cases
+    from sfxc_gpu import lib, run, synth
+    names = ["Ef", "Wb", "On", "Mc", "Nt", "Tr", "Jb", "Hh"]
+    mjd, sr, nch, t0, secs = 60409, 64_000_000, 16, 43199, 3
+    base = "/dev/shm" if os.path.isdir("/dev/shm") else None
+    d = tempfile.mkdtemp(dir=base)
+    try:
+        t = time.time()
+        os.makedirs(os.path.join(d, "delays"))
+        os.makedirs(os.path.join(d, "data"))
+        mode = [("FREQ", "f32", names), ("IF", "ifs", names), ("BBC", "bbcs", names), ("THREADS", "t16", names)]
+        thr = ("t16", [(0, 2048.0, 16, 2, 8000)], [("CH%02d" % (k + 1), 0, k) for k in range(16)])
+        vex = control_cases._base([(n, "dbbc") for n in names], [("dbbc", "Mark5C", "DBBC")], mode,
+                                  [control_cases._freq_def("f32", control_cases._chans_rl(8, 32.0), 64.0)],
+                                  threads=[thr], nbbc=16,
+                                  scans=[("No0001", "2024y100d12h00m00s", "sess", ["SRC1"], [(n, 0, 2) for n in names])])
+        ctrl = {"stations": names, "start": "2024y100d12h00m00s", "stop": "2024y100d12h00m02s", "integr_time": 1.0,
+                "number_channels": 4096, "cross_polarize": True, "output_file": "file://out/bench.cor",
+                "delay_directory": "file://delays", "data_sources": {n: ["file://data/%s.vdif" % n] for n in names}}
+        with open(os.path.join(d, "bench.vex"), "w") as f:
+            f.write(vex)
+        with open(os.path.join(d, "bench.ctrl"), "w") as f:
+            json.dump(ctrl, f)
+        for k, n in enumerate(names):
+            poly = synth.DelayPoly(coeffs=(-1.0e-3 * (k + 1) / 8, 1.0e-6 * (k - 4) / 4, 1.0e-11), t0=43200.0)
+            with open(os.path.join(d, "delays", "N24X1_%s.del" % n), "wb") as f:
+                f.write(synth.del_file_bytes(n, [("SRC1", mjd, t0 - 4, secs + 8, poly)]))
+            rng = np.random.Generator(np.random.PCG64(900 + k))
+            words = np.frombuffer(rng.bytes(secs * sr * nch * 2 // 8), dtype=np.uint32)
+            synth.vdif_frames_array(words, payload_bytes=8000, sample_rate=sr, nchan=nch, bits=2, start_mjd=mjd,
+                                    start_sec_of_day=t0).tofile(os.path.join(d, "data", "%s.vdif" % n))
+        log("wrote the driver experiment (%d stations) in %.1f s" % (len(names), time.time() - t))
+        cwd = os.getcwd()
+        os.chdir(d)
+        try:
+            x_mode = lib.X_TC_HILO if args.x == "tc" else lib.X_FP32
+            for _ in range(max(1, min(args.warmup, 2))):
+                run.correlate("bench.ctrl", "bench.vex", x_mode=x_mode)
+            runs = []
+            for _ in range(max(1, args.steps)):
+                st = {}
+                t1 = time.perf_counter()
+                files = run.correlate("bench.ctrl", "bench.vex", x_mode=x_mode, stats=st)
+                st["wall_s"] = time.perf_counter() - t1
+                runs.append(st)
+        finally:
+            os.chdir(cwd)
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    best = min(runs, key=lambda r: r["wall_s"])
+    samples = best["samples"]
+    return {"workload": DRIVER_NAME, "metric": "input Gsamples/s through sfxc <ctrl> <vex>",
+            "value": round(samples / best["wall_s"] / 1e9, 3), "unit": "Gsamples/s",
+            "ms_per_run": round(best["wall_s"] * 1e3, 1), "runs": len(runs), "samples_per_run": samples,
+            "recording_bytes": best["recording_bytes"], "x_step": args.x,
+            "real_time_factor": round(2.0 / best["wall_s"], 2),
+            "phase_s": {k[:-2]: v for k, v in best.items() if k.endswith("_s") and k != "wall_s"},
+            "output_bytes": sum(len(b) for b in files.values()),
+            "data": "seeded uniform random VDIF payloads on tmpfs; cubic delay models; best of the timed runs"}
+
+
 def summary(cfg, res, args, x_mode, world=1):
     value = res["total"] * args.steps * world / (res["dev_total"] / 1e3) / 1e9
     d = {"workload": cfg["name"], "value": round(value, 3), "unit": "Gsamples/s",
@@ -768,6 +844,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--frontend-only", action="store_true",
                     help="time only the station front end (recording to protocol on the device)")
+    ap.add_argument("--driver", action="store_true",
+                    help="time only the single-GPU driver on a synthetic experiment written to files")
     args = ap.parse_args()
     if args.impl == "reference":
         # the CPU arm builds only the restatement: the GPU library is neither
@@ -775,6 +853,10 @@ def main():
         from oracle import build_oracle
         build_oracle.build()
         run_reference(args)
+    elif args.driver:
+        import __graft_entry__
+        __graft_entry__.build()
+        print(json.dumps(measure_driver(args, lambda m: print(m, file=sys.stderr, flush=True))), flush=True)
     elif args.frontend_only:
         import __graft_entry__
         __graft_entry__.build()

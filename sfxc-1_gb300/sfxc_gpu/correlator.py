@@ -307,6 +307,12 @@ class DeviceRecording:
     def n_blocks(self):
         return self._lib.sfxc_gpu_recording_n_blocks(self._h)
 
+    def block_start(self, i):
+        """Start time (ticks) of reader block i."""
+        b = L.ReaderBlock()
+        self._check(self._lib.sfxc_gpu_recording_block(self._h, i, C.byref(b), None))
+        return b.start_ticks
+
     def blocks(self, data=True):
         """[{channel, start_ticks, data (None unless data), invalid}] per reader block."""
         out = []

@@ -10,9 +10,10 @@ the manager's dealing of the jobs).  Each station's recording (its
 data_sources, VDIF or Mark5B) is read into device memory once; the reader
 tasklet's blocks for every scan the station takes part in (sfxc_gpu_recording_
 schedule), its channels, and each channel's input-node protocol for every
-time slice it feeds are made on the device; each job's streams are pushed
-device to device into one correlator context, which writes the output
-slices; the output node writes them in slice order to the output file(s)
+time slice it feeds are made on the device (stations side by side, each on
+its own library context and host thread); the jobs of a time slice run side
+by side on correlator contexts of their own, their streams pushed device to
+device; the output node writes them in slice order to the output file(s)
 with the global header, and the tsys and phase-cal records to their files
 when the control file names them.  Delay tables are the stations' .del files (the
 manager's delay_directory); the delay model generator is not run.
@@ -25,6 +26,7 @@ import argparse
 import os
 import struct
 import sys
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -124,8 +126,7 @@ class _Station:
         self.slices = {}  # channel -> [(job index, slice)]
 
     def first_time(self):
-        b = self.rec.blocks(data=False)
-        return b[0]["start_ticks"] if b else None
+        return self.rec.block_start(0) if self.rec.n_blocks() > 0 else None
 
     def read(self, intervals):
         self.rec.schedule(intervals)
@@ -136,11 +137,20 @@ class _Station:
             self.rec.extract(word, self.bits, [c["tracks"] for c in self.channels])
 
 
-def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
+def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None, stats=None):
     """Runs the whole correlation; returns {path: bytes written} of the
     output file(s) and, when the control file names them, the tsys and
-    phase-cal files."""
+    phase-cal files.  stats (a dict), if given, receives the wall-clock
+    seconds of each phase and the samples correlated."""
+    import time
     log = log or (lambda *a: None)
+    clock = [time.perf_counter()]
+
+    def lap(name):
+        if stats is not None:
+            t = time.perf_counter()
+            stats[name + "_s"] = round(t - clock[0], 4)
+            clock[0] = t
     ctrl_path, vex_path = os.path.abspath(ctrl_path), os.path.abspath(vex_path)
     ctrl_dir = os.path.dirname(ctrl_path)
     plan = control.plan(ctrl_path, vex_path)
@@ -159,13 +169,25 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
         if fmt not in ("VDIF", "Mark5B"):
             raise DriverError("station %s: %s recordings are not read (no Mark5A reader)" % (names[s], fmt))
 
-    node = correlator.CorrelatorNode(device, x_mode)
-    # every station's recording, read once
+    # one library context per station (its input node) and per concurrent
+    # job (a correlator node): the contexts are driven from their own threads
+    workers = max(1, min(16, os.cpu_count() or 4))
+    station_nodes = {s: correlator.CorrelatorNode(device, x_mode) for s in sorted(per_station)}
+    lap("plan")
+
+    def open_station(s):  # read the recording files, put them on the device
+        parts = [np.fromfile(_path(u, ctrl_dir), dtype=np.uint8) for u in ctrl["data_sources"][names[s]]]
+        data = parts[0] if len(parts) == 1 else np.concatenate(parts)
+        return s, _Station(station_nodes[s], s, names[s], per_station[s], data, experiment_start), data.size
+
     stations = {}
-    for s, scans in sorted(per_station.items()):
-        data = b"".join(open(_path(u, ctrl_dir), "rb").read() for u in ctrl["data_sources"][names[s]])
-        stations[s] = _Station(node, s, names[s], scans, data, experiment_start)
-        log("station %s: %d bytes of %s" % (names[s], len(data), stations[s].fmt))
+    with ThreadPoolExecutor(workers) as ex:
+        for s, st, n in ex.map(open_station, sorted(per_station)):
+            stations[s] = st
+            log("station %s: %d bytes of %s" % (names[s], n, st.fmt))
+            if stats is not None:
+                stats["recording_bytes"] = stats.get("recording_bytes", 0) + n
+    lap("read")
 
     # the manager moves a scan's first slice to the latest input node time
     # (its reader's first frame, at the first scan a station is in)
@@ -189,10 +211,17 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
         del_bytes[s] = open(path, "rb").read()
     uvw = {s: correlator.UvwModel(b) for s, b in del_bytes.items()}
 
-    # the input nodes: reader blocks for each scan interval, channels, delays, protocols
+    # the input nodes: reader blocks for each scan interval, channels, delays,
+    # protocols, and the phase-cal of every channel the writers take up
+    # (Input_node_data_writer::do_phasecal); each station on its own context
     integration_us = int(round(ctrl["integr_time"] * 1e6))
-    for s, scans in per_station.items():
-        st = stations[s]
+    station_number = {sp["station_stream"] % n_st: sp["station_number"] for j in jobs for sp in j["stations"]}
+    for ji, j in enumerate(jobs):
+        for inp in j["inputs"]:
+            stations[inp["station"]].slices.setdefault(inp["channel_in_scan"], []).append((ji, j))
+
+    def input_node(s):
+        st, scans = stations[s], per_station[s]
         st.read([(plan["scans"][sci]["first_slice_start"], plan["scans"][sci]["stop"], e["stop_time"])
                  for sci, e in scans])
         delays = {}
@@ -203,47 +232,53 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
                 clock=(e["clock_offset"], e["clock_rate"], e["clock_epoch"]))
         fft = st.input["fft_size"]
         size_slice = timebase.nr_ffts_per_integration_slice(integration_us, st.sample_rate, fft) * fft
-        for ji, j in enumerate(jobs):
-            for inp in j["inputs"]:
-                if inp["station"] == s:
-                    st.slices.setdefault(inp["channel_in_scan"], []).append(
-                        (ji, (j["start_time"], j["stop_time"], size_slice, delays[j["scan"]])))
         for c, sl in st.slices.items():
             if not 0 <= c < len(st.channels):
                 raise DriverError("station %s: channel %d of the scan is not in its recording set-up" % (st.name, c))
-            st.rec.protocol(c, [x for _, x in sl], st.sample_rate, st.bits, integration_us, copy=False)
-        log("station %s: %d channel streams" % (st.name, len(st.slices)))
-
-    # phase-cal of every channel the writers take up (Input_node_data_writer::do_phasecal)
-    station_number = {sp["station_stream"] % n_st: sp["station_number"] for j in jobs for sp in j["stations"]}
-    pcal = []
-    if ctrl.get("phasecal_file") and per_station:
-        for s in sorted(per_station):
-            st = stations[s]
-            ticks = st.input["phasecal_integr_time"]
-            if ticks <= 0:
-                continue
+            st.rec.protocol(c, [(j["start_time"], j["stop_time"], size_slice, delays[j["scan"]]) for _, j in sl],
+                            st.sample_rate, st.bits, integration_us, copy=False)
+        msgs = []
+        ticks = st.input["phasecal_integr_time"]
+        if ctrl.get("phasecal_file") and ticks > 0:
             for c in sorted(st.slices):
                 ch = st.channels[c]
-                pc = correlator.PhaseCal(node, st.sample_rate, st.bits, ticks, station_number.get(s, 0),
+                pc = correlator.PhaseCal(station_nodes[s], st.sample_rate, st.bits, ticks, station_number.get(s, 0),
                                          ch["frequency_number"], 1 if ch["sideband"] == "U" else 0,
                                          1 if ch["polarisation"] == "L" else 0)
-                pcal += pc.push(st.rec.channel(c))
+                msgs += pc.push(st.rec.channel(c))
                 pc.close()
+        return msgs
 
-    # the correlator node, job after job; the output node
+    with ThreadPoolExecutor(workers) as ex:
+        pcal = [m for msgs in ex.map(input_node, sorted(per_station)) for m in msgs]
+    log("input nodes: %d channel streams" % sum(len(st.slices) for st in stations.values()))
+    lap("input_nodes")
+
+    # the correlator nodes: the jobs of one time slice side by side, each on
+    # its own context; the output node takes their slices in order
     pulsars = {p["name"]: p for p in plan.get("pulsars", [])}
     mask = plan.get("mask")
     sources = plan["sources"]
+    phased = int(bool(ctrl.get("phased_array")))
     h = plan["header"]
     out = correlator.OutputFiles(len(plan["output_files"]), experiment=h["experiment"], start_year=h["start_year"],
                                  start_day=h["start_day"], start_time=h["start_time"],
                                  number_channels=h["number_channels"], integration_time_us=h["integration_time"],
                                  correlator_version=0, polarisation_type=h["polarisation_type"],
                                  correlator_branch="gb300", job_nr=h["job_nr"], subjob_nr=h["subjob_nr"])
-    slice_index = {}  # (station, channel) -> next slice of its protocol
-    tsys_msgs = []
+    slice_of = {}  # job index -> the protocol slice of each of its streams
+    used = {}
     for ji, j in enumerate(jobs):
+        by_stream = {inp["stream"]: inp for inp in j["inputs"]}
+        pushes = []
+        for sp in j["stations"]:
+            inp = by_stream[sp["station_stream"]]
+            key = (inp["station"], inp["channel_in_scan"])
+            pushes.append((inp["station"], inp["channel_in_scan"], used.get(key, 0)))
+            used[key] = used.get(key, 0) + 1
+        slice_of[ji] = pushes
+
+    def job_of(j):
         sc = plan["scans"][j["scan"]]
         sc_station = {e["station"]: e for e in sc["stations"]}
         streams, tables, clocks, table_of = [], [], [], {}
@@ -266,7 +301,7 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
                    channel_freq=j["channel_freq"], sideband=j["sideband"], polarisation=j["polarisation"],
                    cross_polarize=int(j["cross_polarize"]), reference_station=j["reference_station"],
                    window=j["window"], integration_nr=j["integration_nr"], streams=streams, del_bytes=tables,
-                   clocks=clocks, n_integrations=1, phased_array=int(bool(ctrl.get("phased_array"))))
+                   clocks=clocks, n_integrations=1, phased_array=phased)
         n_bins = 1
         if j["pulsar_binning"]:
             p = pulsars.get(j["source"])
@@ -287,22 +322,48 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
             if mask["window"]:
                 job["lag_window"] = np.asarray(mask["window"], dtype=np.float32)
             job["mask_normalize"] = int(mask["normalize"])
-        node.set_parameters(job)
+        # u, v, w at the integration's mid-time (the models keep state: here, in job order)
         tmid = j["start_time"] + tint // 2
         npc = max(1, j["n_phase_centers"])
-        node.set_uvw([[uvw[sp["station_stream"] % n_st].get(pc, tmid) for pc in range(npc)] for sp in j["stations"]])
-        by_stream = {inp["stream"]: inp for inp in j["inputs"]}
-        for k, sp in enumerate(j["stations"]):
-            inp = by_stream[sp["station_stream"]]
-            key = (inp["station"], inp["channel_in_scan"])
-            i = slice_index.get(key, 0)
-            slice_index[key] = i + 1
-            stations[inp["station"]].rec.push(inp["channel_in_scan"], i, node, k)
-        data, tsys = node.run_integration()
-        out.put_slice(j["slice_nr"], data, n_bins)
-        tsys_msgs += tsys
-        log("slice %d: %s channel %d integration %d" % (j["slice_nr"], sc["name"], j["channel"],
-                                                        j["integration_nr"]))
+        job["uvw_now"] = [[uvw[sp["station_stream"] % n_st].get(pc, tmid) for pc in range(npc)]
+                          for sp in j["stations"]]
+        return job, n_bins
+
+    def correlate_one(args):
+        node, ji, job = args
+        node.set_parameters(job)
+        node.set_uvw(job["uvw_now"])
+        for k, (s, c, i) in enumerate(slice_of[ji]):
+            stations[s].rec.push(c, i, node, k)
+        return node.run_integration()
+
+    groups = []  # runs of jobs of one time slice
+    for ji, j in enumerate(jobs):
+        if groups and (jobs[groups[-1][0]]["scan"], jobs[groups[-1][0]]["integration_nr"]) == (j["scan"],
+                                                                                               j["integration_nr"]):
+            groups[-1].append(ji)
+        else:
+            groups.append([ji])
+    n_nodes = min(max(len(g) for g in groups), workers)
+    nodes = [correlator.CorrelatorNode(device, x_mode) for _ in range(n_nodes)]
+    tsys_msgs = []
+    with ThreadPoolExecutor(n_nodes) as ex:
+        for g in groups:
+            for k0 in range(0, len(g), n_nodes):
+                part = g[k0:k0 + n_nodes]
+                built = [job_of(jobs[ji]) for ji in part]
+                results = list(ex.map(correlate_one, [(nodes[k], ji, built[k][0]) for k, ji in enumerate(part)]))
+                for k, ji in enumerate(part):
+                    j = jobs[ji]
+                    data, tsys = results[k]
+                    out.put_slice(j["slice_nr"], data, built[k][1])
+                    tsys_msgs += tsys
+                    if stats is not None:
+                        n = sum(sp["sample_rate"] for sp in j["stations"]) * j["integration_time"] // 512_000_000
+                        stats["samples"] = stats.get("samples", 0) + n
+                    log("slice %d: %s channel %d integration %d" % (
+                        j["slice_nr"], plan["scans"][j["scan"]]["name"], j["channel"], j["integration_nr"]))
+    lap("correlate")
     files = out.finish()
     written = {}
     for url, b in zip(plan["output_files"], files):
@@ -323,7 +384,9 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None):
     out.close()
     for st in stations.values():
         st.rec.close()
-    node.close()
+    for n in nodes + list(station_nodes.values()):
+        n.close()
+    lap("output")
     return written
 
 

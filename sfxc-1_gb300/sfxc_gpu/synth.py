@@ -286,6 +286,26 @@ def vdif_file_bytes(words: np.ndarray, *, payload_bytes: int, sample_rate: int, 
     return bytes(out)
 
 
+def vdif_frames_array(words: np.ndarray, *, payload_bytes: int, sample_rate: int, nchan: int, bits: int,
+                      start_mjd: int, start_sec_of_day: int) -> np.ndarray:
+    """vdif_file_bytes without invalid frames, built with whole-array
+    operations (for recordings of gigabytes): a uint8 array of the frames."""
+    ref_epoch, epoch_mjd = vdif_ref_epoch(start_mjd)
+    wpf = payload_bytes // 4
+    fps = sample_rate // (payload_bytes * 8 // (bits * nchan))
+    nframes = words.size // wpf
+    f = np.arange(nframes, dtype=np.int64)
+    sec0 = (start_mjd - epoch_mjd) * 86400 + start_sec_of_day
+    out = np.zeros((nframes, 8 + wpf), dtype=np.uint32)
+    out[:, 0] = ((sec0 + f // fps) & 0x3FFFFFFF).astype(np.uint32)
+    out[:, 1] = ((f % fps) & 0xFFFFFF).astype(np.uint32) | np.uint32((ref_epoch & 0x3F) << 24)
+    out[:, 2] = np.uint32((((payload_bytes + VDIF_HEADER_BYTES) // 8) & 0xFFFFFF) |
+                          ((int(round(math.log2(nchan))) & 0x1F) << 24))
+    out[:, 3] = np.uint32(((bits - 1) & 0x1F) << 26)
+    out[:, 8:] = words[:nframes * wpf].reshape(nframes, wpf)
+    return out.reshape(-1).view(np.uint8)
+
+
 # --------------------------------------------------------------------------
 # Recordings with the irregularities the format readers handle
 # --------------------------------------------------------------------------
