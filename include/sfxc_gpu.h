@@ -510,7 +510,10 @@ void sfxc_gpu_output_destroy(sfxc_gpu_output *out);
  * batch's stream), launched once.  Each context must have its parameters set
  * and its input pushed, as for sfxc_gpu_run_integration; the results equal
  * that call's.  The sink gets each job's output in batch order, with
- * users[i] (NULL: NULL) for job i.  The first integration of a new shape
+ * users[i] (NULL: NULL) for job i, after every job's output bytes have been
+ * made (one host thread per context); a sink that refuses data stops the
+ * delivery there, the later jobs' integrations having run without their
+ * output reaching the sink.  The first integration of a new shape
  * sizes the jobs' buffers; later ones with the same shapes reuse them and
  * the executable graph.  A context belongs to at most one batch at a time. */
 typedef struct sfxc_gpu_batch sfxc_gpu_batch;

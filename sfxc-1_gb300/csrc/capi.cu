@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <functional>
 #include <map>
 #include <memory>
@@ -1262,7 +1263,14 @@ void enqueue_integration(sfxc_gpu_ctx *c, int k = 0, bool require_push = true) {
 
 // After the recorded work has run: device error flag, timings, statistics,
 // output bytes to the sink.
-int finish_integration(sfxc_gpu_ctx *c, int k, sfxc_output_sink sink, void *user) {
+// The host side of a finished integration: its output bytes and tsys
+// records, made before any of them goes to the sink.
+struct IntegrationOut {
+  std::vector<uint8_t> cor;
+  std::vector<std::vector<uint8_t>> tsys;
+};
+
+void prepare_outputs(sfxc_gpu_ctx *c, int k, IntegrationOut &out) {
   Slot &sl = *c->slots[k];
   Pending &pd = sl.pend;
   const int N = (int)c->streams.size(), nbl = (int)c->bl.size();
@@ -1310,7 +1318,11 @@ int finish_integration(sfxc_gpu_ctx *c, int k, sfxc_output_sink sink, void *user
     bs.base_sample_rate = c->p.sample_rate;
   }
   // ---- output bytes (integration_write per bin) and tsys records
-  std::vector<uint8_t> o;
+  std::vector<uint8_t> &o = out.cor;
+  {
+    const size_t per_out = 20 + (size_t)N * (32 + 24) + (size_t)std::max(nbl, nphs) * (8 + (size_t)c->Kout * 8);
+    o.reserve(per_out * (size_t)std::max(1, nout));
+  }
   if (c->phased) {
     serialize_integration(c, std::vector<Baseline>(nphs, Baseline{0, 0}), vis, 0, 0, nfl, o);
   } else {
@@ -1318,9 +1330,9 @@ int finish_integration(sfxc_gpu_ctx *c, int k, sfxc_output_sink sink, void *user
       serialize_integration(c, c->bl, vis + (size_t)bin * nbl * c->Kout, pulsar ? bin : c->pc_file[bin],
                             pulsar ? 0 : bin, nfl, o);
   }
-  if (sink && sink(user, 0, o.data(), o.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
   for (int i = 0; i < N && !c->phased; i++) {  // the phased core writes no tsys records
-    std::vector<uint8_t> t;
+    out.tsys.emplace_back();
+    std::vector<uint8_t> &t = out.tsys.back();
     t.push_back((uint8_t)c->streams[i].station_number);
     t.push_back((uint8_t)c->p.frequency_nr);
     t.push_back((uint8_t)(c->p.sideband == 'L' ? 0 : 1));
@@ -1329,9 +1341,21 @@ int finish_integration(sfxc_gpu_ctx *c, int k, sfxc_output_sink sink, void *user
     c->sc[i].stats.tsys(ts);
     put(t, (int64_t)start);
     for (int k = 0; k < 4; k++) put(t, (int64_t)ts[k]);
-    if (sink && sink(user, 1, t.data(), t.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
   }
   c->current_integration++;
+}
+
+void deliver_outputs(const IntegrationOut &o, sfxc_output_sink sink, void *user) {
+  if (!sink) return;
+  if (sink(user, 0, o.cor.data(), o.cor.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
+  for (const std::vector<uint8_t> &t : o.tsys)
+    if (sink(user, 1, t.data(), t.size()) != 0) throw Error(SFXC_GPU_EINVAL, "output sink refused the data");
+}
+
+int finish_integration(sfxc_gpu_ctx *c, int k, sfxc_output_sink sink, void *user) {
+  IntegrationOut o;
+  prepare_outputs(c, k, o);
+  deliver_outputs(o, sink, user);
   return SFXC_GPU_OK;
 }
 
@@ -3003,11 +3027,30 @@ int sfxc_gpu_batch_run_counts(sfxc_gpu_batch *b, const int32_t *counts, sfxc_out
     CK(cudaEventElapsedTime(&b->last_ms, b->e0, b->e1));
     b->host_ms[2] = ms_since(t0);
     t0 = clock::now();
+    // every job's output bytes made side by side (one host thread per
+    // context, its integrations in order), then handed to the sink in job
+    // order as one thread would
+    std::vector<std::vector<IntegrationOut>> outs(n);
+    std::vector<std::exception_ptr> errs(n);
+    {
+      auto prepare_job = [&](int k) {
+        try {
+          CK(cudaSetDevice(b->ctx[k]->device));
+          outs[k].resize(cnt[k]);
+          for (int j = 0; j < cnt[k]; j++) prepare_outputs(b->ctx[k], j, outs[k][j]);
+        } catch (...) {
+          errs[k] = std::current_exception();
+        }
+      };
+      std::vector<std::thread> threads;
+      for (int k = 0; k < n; k++)
+        if (cnt[k]) threads.emplace_back(prepare_job, k);
+      for (std::thread &t : threads) t.join();
+    }
     for (i = 0; i < n; i++)
-      for (int j = 0; j < cnt[i]; j++) {
-        const int rc = finish_integration(b->ctx[i], j, sink, users ? users[i] : nullptr);
-        if (rc != SFXC_GPU_OK) return rc;
-      }
+      if (errs[i]) std::rethrow_exception(errs[i]);
+    for (i = 0; i < n; i++)
+      for (int j = 0; j < cnt[i]; j++) deliver_outputs(outs[i][j], sink, users ? users[i] : nullptr);
     b->host_ms[3] = ms_since(t0);
     return SFXC_GPU_OK;
   } catch (const Error &e) {
