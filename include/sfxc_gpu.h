@@ -69,7 +69,8 @@ typedef struct {
 /* Correlation_parameters::Station_parameters (sfxc/include/control_parameters.h:125-142) */
 typedef struct {
   int32_t station_number;
-  int32_t station_stream;
+  int32_t station_stream; /* the node's input number: distinct per stream (gaps allowed); the
+                             streams are taken in array order */
   int32_t sample_rate;
   int32_t bandwidth;
   int32_t bits_per_sample;

@@ -505,7 +505,13 @@ void set_parameters(sfxc_gpu_ctx *c, const sfxc_correlation_params *p) {
     if (s.bits_per_sample != 1 && s.bits_per_sample != 2) throw Error(SFXC_GPU_EINVAL, "bits_per_sample must be 1 or 2");
     if (s.sample_rate <= 0 || s.bandwidth <= 0) throw Error(SFXC_GPU_EINVAL, "bad stream sample rate or bandwidth");
     if (s.delay_table < 0 || s.delay_table >= p->n_delay_tables) throw Error(SFXC_GPU_EINVAL, "bad delay table index");
-    if (s.station_stream != i) throw Error(SFXC_GPU_EINVAL, "station_stream must equal the stream's position");
+    // the node's input number of the stream (a station's second polarisation
+    // numbered after every station's first; a station missing from the scan
+    // leaves a gap): streams are taken in array order, the numbers only
+    // have to be distinct
+    if (s.station_stream < 0) throw Error(SFXC_GPU_EINVAL, "station_stream must not be negative");
+    for (int j = 0; j < i; j++)
+      if (p->streams[j].station_stream == s.station_stream) throw Error(SFXC_GPU_EINVAL, "station_stream repeated");
     if (s.bits_per_sample == 2 && s.tsys_freq <= 0) throw Error(SFXC_GPU_EINVAL, "tsys_freq must be positive");
     StationStream ss{s.station_number, s.station_stream, s.sample_rate, s.bandwidth, s.bits_per_sample, s.tsys_freq,
                      s.channel_freq, s.sideband, s.polarisation, s.lo_offset};

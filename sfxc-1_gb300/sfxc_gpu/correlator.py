@@ -106,9 +106,20 @@ class CorrelatorNode:
         if not self._h:
             raise L.SfxcError(L.ECUDA, self._lib.sfxc_gpu_global_error().decode())
         self._keep = []
+        # recordings and phase-cal folds made on this context, held here so
+        # that closing the context closes them first, whatever order the
+        # objects are collected in (the library wants them destroyed before
+        # their context)
+        self._dependents = []
+
+    def _adopt(self, obj):
+        self._dependents = [d for d in self._dependents if d._h] + [obj]
 
     def close(self):
         if self._h:
+            for obj in self._dependents:
+                obj.close()
+            self._dependents = []
             self._lib.sfxc_gpu_destroy(self._h)
             self._h = None
 
@@ -282,6 +293,7 @@ class DeviceRecording:
         self._h = self._lib.sfxc_gpu_recording_create(node._h, C.byref(p), ptr, n, on_dev)
         if not self._h:
             raise L.SfxcError(L.EINVAL, self._lib.sfxc_gpu_last_error(node._h).decode())
+        node._adopt(self)
         self._nch = 0
 
     def close(self):
@@ -420,6 +432,7 @@ class PhaseCal:
         self._h = self._lib.sfxc_gpu_phasecal_create(node._h, C.byref(p))
         if not self._h:
             raise L.SfxcError(L.EINVAL, self._lib.sfxc_gpu_last_error(node._h).decode())
+        node._adopt(self)
 
     def close(self):
         if self._h:

@@ -171,8 +171,19 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None, stats=No
 
     # one library context per station (its input node) and per concurrent
     # job (a correlator node): the contexts are driven from their own threads
-    workers = max(1, min(16, os.cpu_count() or 4))
     station_nodes = {s: correlator.CorrelatorNode(device, x_mode) for s in sorted(per_station)}
+    nodes = []
+    try:
+        return _run(plan, ctrl, ctrl_path, vex_path, ctrl_dir, names, n_st, experiment_start, per_station,
+                    station_nodes, nodes, device, x_mode, log, stats, lap)
+    finally:
+        for n in nodes + list(station_nodes.values()):  # each closes its recordings first
+            n.close()
+
+
+def _run(plan, ctrl, ctrl_path, vex_path, ctrl_dir, names, n_st, experiment_start, per_station, station_nodes,
+         nodes, device, x_mode, log, stats, lap):
+    workers = max(1, min(16, os.cpu_count() or 4))
     lap("plan")
 
     def open_station(s):  # read the recording files, put them on the device
@@ -345,7 +356,7 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None, stats=No
         else:
             groups.append([ji])
     n_nodes = min(max(len(g) for g in groups), workers)
-    nodes = [correlator.CorrelatorNode(device, x_mode) for _ in range(n_nodes)]
+    nodes += [correlator.CorrelatorNode(device, x_mode) for _ in range(n_nodes)]
     tsys_msgs = []
     with ThreadPoolExecutor(n_nodes) as ex:
         for g in groups:
@@ -382,9 +393,7 @@ def correlate(ctrl_path, vex_path, device=0, x_mode=L.X_FP32, log=None, stats=No
                 f.write(b)
             written[path] = b
     out.close()
-    for st in stations.values():
-        st.rec.close()
-    for n in nodes + list(station_nodes.values()):
+    for n in nodes + list(station_nodes.values()):  # each closes its recordings first
         n.close()
     lap("output")
     return written

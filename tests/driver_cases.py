@@ -9,7 +9,8 @@ shifted by whole seconds), On Mark5B with eight bitstreams.  Two scans with a
 gap between them; the recordings run from before the first to after the
 last.  Cross-polarised correlation of the first frequency, 1 s integrations.
 Three variants take two of the stations for pulsar binning, extra phase
-centres and the phased array.  tests/golden/driver*.npz hold what the reference's own classes make of them,
+centres and the phased array; a fourth has a station leave a scan and
+another start recording late.  tests/golden/driver*.npz hold what the reference's own classes make of them,
 stage by stage (tests/golden/make_golden.py: its plan, reader tasklet,
 channel extractor, delays, input-node writer and correlation core)."""
 import json
@@ -28,17 +29,19 @@ STATIONS = ["Ef", "Wb", "On"]
 WB_CLOCK = 1.0000021  # seconds: the reader takes 1 s of it
 
 
-VARIANTS = ("plain", "pulsar", "phase_centres", "phased")
+VARIANTS = ("plain", "pulsar", "phase_centres", "phased", "scans")
 PULSAR = "B0329+54"
 
 
 def _stations(variant):
-    return {"plain": STATIONS, "pulsar": ["Ef", "On"], "phase_centres": ["Ef", "Wb"], "phased": ["Ef", "On"]}[variant]
+    return {"plain": STATIONS, "pulsar": ["Ef", "On"], "phase_centres": ["Ef", "Wb"], "phased": ["Ef", "On"],
+            "scans": STATIONS}[variant]
 
 
 def _scan_sources(variant):
     return {"plain": (["SRC1"], ["SRC2"]), "pulsar": ([PULSAR], ["SRC2"]),
-            "phase_centres": (["SRC1", "SRC3"], ["SRC2"]), "phased": (["SRC1"], ["SRC2"])}[variant]
+            "phase_centres": (["SRC1", "SRC3"], ["SRC2"]), "phased": (["SRC1"], ["SRC2"]),
+            "scans": (["SRC1"], ["SRC2"])}[variant]
 
 
 def vex_text(variant="plain"):
@@ -55,8 +58,9 @@ def vex_text(variant="plain"):
               ("On", ["2024y099d00h00m00s : -1.25 usec"])]
     src1, src2 = _scan_sources(variant)
     sts = _stations(variant)
+    sts2 = [s for s in sts if not (variant == "scans" and s == "Wb")]  # Wb leaves the second scan
     scans = [("No0001", "2024y100d12h00m00s", "sess", src1, [(s, 0, 4) for s in sts]),
-             ("No0002", "2024y100d12h00m06s", "sess", src2, [(s, 0, 3) for s in sts])]
+             ("No0002", "2024y100d12h00m06s", "sess", src2, [(s, 0, 3) for s in sts2])]
     return control_cases._base([("Ef", "vdif_dbbc"), ("Wb", "vdif_dbbc"), ("On", "mk5b")], das, mode, freqs,
                                threads=[thr_ef, thr_wb], bitstreams=[bs_on], scans=scans, clocks=clocks, nbbc=4)
 
@@ -66,7 +70,9 @@ def ctrl_dict(variant="plain"):
     files; pulsar: Ef and On, R only, the first scan on a pulsar (4 bins
     between pulse phases 0.1 and 0.9), the second on an ordinary source;
     phase_centres: Ef and Wb, R only, the first scan with two sources;
-    phased: Ef and On summed as a phased array, R and L."""
+    phased: Ef and On summed as a phased array, R and L; scans: all three,
+    R only, Wb not in the second scan and Ef's recording starting a second
+    into the first (the manager starts that scan's correlation later)."""
     sts = _stations(variant)
     c = {"exper_name": "N24X1", "stations": sts, "start": "2024y100d12h00m00s",
          "stop": "2024y100d12h00m09s", "integr_time": 1.0, "number_channels": 256,
@@ -82,6 +88,8 @@ def ctrl_dict(variant="plain"):
                  pulsars={PULSAR: {"polyco_file": "file://b0329.polyco", "nbins": 4, "interval": [0.1, 0.9]}})
     elif variant == "phase_centres":
         c.update(channels=["CH01"], fft_size_correlation=256)
+    elif variant == "scans":
+        c.update(channels=["CH01"])
     else:
         c.update(channels=["CH01", "CH02"], phased_array=True)
     return c
@@ -110,11 +118,12 @@ def del_bytes(station, variant="plain"):
     return synth.del_file_bytes(station, scans)
 
 
-def recordings():
+def recordings(variant="plain"):
     """name -> bytes of each data file."""
     n = T1 - T0
-    ef = synth.vdif_recording(n * 500, payload_bytes=8000, frames_per_second=500, start_mjd=MJD,
-                              start_sec_of_day=T0, log2_nchan=2, bits=2, invalid=(1711,), seed=701)
+    late = 3 if variant == "scans" else 0  # Ef's data from 12:00:01
+    ef = synth.vdif_recording((n - late) * 500, payload_bytes=8000, frames_per_second=500, start_mjd=MJD,
+                              start_sec_of_day=T0 + late, log2_nchan=2, bits=2, invalid=(1711,), seed=701)
     # Wb: one thread per channel, 125 frames/s each, its time stamps 1 s late (the clock);
     # two files, the second starting where the first ends, one frame lost
     wb = synth.vdif_recording(n * 500, payload_bytes=8000, frames_per_second=125, start_mjd=MJD,
@@ -140,7 +149,7 @@ def write_experiment(d, variant="plain"):
         with open(os.path.join(d, "delays", "N24X1_%s.del" % s), "wb") as f:
             f.write(del_bytes(s, variant))
     files = {u[7:] for s in c["stations"] for u in c["data_sources"][s]}
-    for name, b in recordings().items():
+    for name, b in recordings(variant).items():
         if name in files:
             with open(os.path.join(d, name), "wb") as f:
                 f.write(b)

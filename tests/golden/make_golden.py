@@ -533,7 +533,7 @@ def make_driver(variant="plain"):
 
 if __name__ == "__main__":
     make_control()
-    for v in ("plain", "pulsar", "phase_centres", "phased"):
+    for v in ("plain", "pulsar", "phase_centres", "phased", "scans"):
         make_driver(v)
     make_output_header()
     make_phasecal()

@@ -89,14 +89,15 @@ def test_driver_matches_reference_stages(tmp_path, x_mode, tol):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("variant", ["pulsar", "phase_centres", "phased"])
+@pytest.mark.parametrize("variant", ["pulsar", "phase_centres", "phased", "scans"])
 @pytest.mark.parametrize("x_mode,tol", [(L.X_FP32, 1e-5), (L.X_TC_HILO, 1e-4)])
 def test_driver_variants_match_reference_stages(tmp_path, variant, x_mode, tol):
     """Pulsar binning (the pulsar's scan in 4 + 1 bins, one file per bin;
     the other scan's source as file 1), extra phase centres (the first
-    scan's two sources, one file per source) and the phased array (one summed
-    spectrum per sub-integration): every output file's slices against the
-    reference's core outputs routed by their file index."""
+    scan's two sources, one file per source), the phased array (one summed
+    spectrum per sub-integration), and a station leaving a scan while another
+    starts late: every output file's slices against the reference's core
+    outputs routed by their file index."""
     from sfxc_gpu import correlator
     d = str(tmp_path)
     files = _correlate(d, x_mode, variant)
