@@ -271,6 +271,22 @@ def cases():
         ctrl=_ctrl(sts, stop="end", exper_name="N24X1", job=7, subjob=3, window_function="COSINE",
                    fft_size_delaycor=512, number_channels=256))
 
+    # two modes: the second scan in another set-up (16 MHz channels, another
+    # thread layout), which changes the reader parameters and the channels'
+    # frequencies from one scan to the next
+    sts2 = ["Ef", "Wb"]
+    f16 = _freq_def("f16b", _chans_rl(4, 16.0, f0=4974.49), 32.0)
+    thr8 = ("thr8", [(0, 256.0, 8, 2, 8000)], [("CH%02d" % (k + 1), 0, k) for k in range(8)])
+    modes = [("wide", [("FREQ", "f32", sts2), ("IF", "ifs", sts2), ("BBC", "bbcs", sts2), ("THREADS", "thr16", sts2)]),
+             ("narrow", [("FREQ", "f16b", sts2), ("IF", "ifs", sts2), ("BBC", "bbcs", sts2), ("THREADS", "thr8", sts2)])]
+    scans = [("No0001", "2024y100d12h00m00s", "wide", ["SRC1"], [(x, 0, 20) for x in sts2]),
+             ("No0002", "2024y100d12h00m30s", "narrow", ["SRC2"], [(x, 0, 20) for x in sts2])]
+    out["two_modes"] = dict(
+        vex=_vex("N24X1", [(x, "dbbc_mk5c", x) for x in sts2], modes, [_freq_def("f32", _chans_rl(8, 32.0), 64.0), f16],
+                 [_ifs_rl()], [_bbcs(16)], threads=[_vdif16_threads(), thr8], scans=scans,
+                 clocks=[(x, ["2024y100d00h00m00s : 1.0 usec"]) for x in sts2], das=das),
+        ctrl=_ctrl(sts2, channels=["CH01", "CH02", "CH03", "CH04"], cross_polarize=True))
+
     # refused set-ups
     out["error_pulsar_multi_phase"] = dict(
         vex=_base([(s, "dbbc_mk5c") for s in sts], das, vdif_mode, freqs, threads=[_vdif16_threads()]),
