@@ -611,23 +611,25 @@ class Batch:
         """Every integration of the jobs (one per node; any integration
         counts): per_run[i] integrations of job i in each graph (default: all
         of them in one).  Returns [(cor (bytes or bytearray), tsys)] per job."""
-        for n, j in zip(self.nodes, jobs):
-            n.set_parameters(j)
+        pool = ThreadPoolExecutor(max_workers=len(self.nodes))
+        # each node's set-up and pushes from its own thread: the host work and
+        # the copies of different contexts run at the same time (the library
+        # calls drop the GIL)
+        for f in [pool.submit(n.set_parameters, j) for n, j in zip(self.nodes, jobs)]:
+            f.result()
         left = [int(j["n_integrations"]) for j in jobs]
         step = per_run or left
         done = [0] * len(jobs)
         cor = [[] for _ in jobs]
         tsys = [[] for _ in jobs]
+
         def push(n, j, d, c):
             for it in range(d, d + c):
                 for k in range(n.nstreams):
                     n.push_protocol(k, j["protocols"][k][it])
 
-        pool = ThreadPoolExecutor(max_workers=len(self.nodes))
         while any(left):
             counts = [min(s, l) for s, l in zip(step, left)]
-            # each node's pushes from its own thread: the copies of different
-            # contexts run at the same time (the library call drops the GIL)
             for f in [pool.submit(push, n, j, d, c) for n, j, d, c in zip(self.nodes, jobs, done, counts)]:
                 f.result()
             for q, (o, t) in enumerate(self.run(counts)):
