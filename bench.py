@@ -340,6 +340,14 @@ def roofline(cfg, per_kernel, total, steps, peaks, x_mode, nbl_per_stream):
                       "flops_per_sample": round(w["flops"], 1)})
         kernels[name.replace("_ms", "")] = e
     out["kernels"] = kernels
+    stages = sum(per_kernel.get(n, 0.0) for n in ("unpack_fringe_ms", "window_fft_ms", "xstep_ms", "normalise_ms",
+                                                    "bitstat_ms"))
+    if "total_ms" in per_kernel and stages > 1.02 * per_kernel["total_ms"]:
+        # the X-step on the context's third stream beside the next chunk's
+        # F-step: both kernels' times are their elapsed times while sharing SMs
+        out["stages_overlap"] = ("each chunk's X-step runs beside the next chunk's F-step; stage times are elapsed "
+                                 "times while they share the SMs (sum %.1f ms, step %.1f ms)"
+                                 % (stages / steps, per_kernel["total_ms"] / steps))
     if peaks and work[k]["flops"]:
         tf = work[k]["flops"] * total / t / 1e12
         out["compute"] = {"bound": "fp32", "achieved": round(tf, 2), "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",

@@ -223,13 +223,19 @@ int sfxc_gpu_copy_pulsar_bins(sfxc_gpu_ctx *ctx, int32_t *out, size_t n);
  * Arguments and result as sfxc_gpu_copy_spectra. */
 int sfxc_gpu_copy_spectra_noalloc(sfxc_gpu_ctx *ctx, int32_t stream, float *out, size_t n_floats);
 /* Device time (ms) of the last integration, CUDA events on the context's
- * stream: [0] unpack and fringe stopping, with any wait for the per-block
+ * streams: [0] unpack and fringe stopping, with any wait for the per-block
  * delay and phase parameters, which run on the context's second stream (the
  * first sub-integration chunk's beside the bit statistics, later chunks'
  * during the previous chunk's X-step), [1] windowed FFT, [2] X-step, [3]
  * normalisation and result copies, [4] total from the first kernel to the
- * last copy; [5] number of kernel launches. */
+ * last copy; [5] number of kernel launches.  Where a chunk's X-step runs on
+ * the context's third stream beside the next chunk's F-step (every X-step
+ * but the TMA-fed tensor-core one), [0] and [2] overlap and [0] to [3] add
+ * up to more than [4]. */
 int sfxc_gpu_last_timings(const sfxc_gpu_ctx *ctx, float *out6);
+/* The same times and, as [6], the bit statistics (which run before the first
+ * chunk); writes the first min(n, 7) entries. */
+int sfxc_gpu_last_timings_n(const sfxc_gpu_ctx *ctx, float *out, int32_t n);
 
 /* Integer delay list of one interval (Input_node_tasklet::add_time_interval):
  * writes up to `capacity` entries (ticks, bytes, remaining samples) and

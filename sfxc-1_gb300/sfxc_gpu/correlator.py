@@ -218,12 +218,12 @@ class CorrelatorNode:
         return out
 
     def timings(self):
-        t = (C.c_float * 6)()
-        self._check(self._lib.sfxc_gpu_last_timings(self._h, t))
-        # the bit statistics run first, before the first chunk's events: the
-        # total less the four timed stages
+        t = (C.c_float * 7)()
+        self._check(self._lib.sfxc_gpu_last_timings_n(self._h, t, 7))
+        # stage times overlap where the X-step runs beside the next chunk's
+        # F-step: each is its own kernels' elapsed time
         return {"unpack_fringe_ms": t[0], "window_fft_ms": t[1], "xstep_ms": t[2], "normalise_ms": t[3],
-                "bitstat_ms": max(0.0, t[4] - t[0] - t[1] - t[2] - t[3]), "total_ms": t[4], "launches": int(t[5])}
+                "bitstat_ms": t[6], "total_ms": t[4], "launches": int(t[5])}
 
     def extract_block(self, block, word_bytes, bits, tracks):
         """One reader block (read_recording's dict) through the channel

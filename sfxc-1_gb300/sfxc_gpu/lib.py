@@ -16,7 +16,8 @@ X_FP32, X_TC_HILO = 0, 1
 EXPORTS = [
     "sfxc_gpu_create", "sfxc_gpu_destroy", "sfxc_gpu_last_error", "sfxc_gpu_global_error",
     "sfxc_gpu_set_parameters", "sfxc_gpu_push_protocol", "sfxc_gpu_run_integration",
-    "sfxc_gpu_copy_unpacked", "sfxc_gpu_copy_spectra", "sfxc_gpu_last_timings", "sfxc_gpu_delay_list",
+    "sfxc_gpu_copy_unpacked", "sfxc_gpu_copy_spectra", "sfxc_gpu_last_timings", "sfxc_gpu_last_timings_n",
+    "sfxc_gpu_delay_list",
     "sfxc_gpu_write_protocol", "sfxc_gpu_extract_channels", "sfxc_gpu_copy_spectra_noalloc",
     "sfxc_gpu_copy_pulsar_bins", "sfxc_gpu_measure_peaks", "sfxc_gpu_batch_create", "sfxc_gpu_batch_run",
     "sfxc_gpu_batch_run_counts", "sfxc_gpu_autotune", "sfxc_gpu_plan_cache",
@@ -148,6 +149,7 @@ def load(path=None):
     lib.sfxc_gpu_batch_last_host_ms.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     lib.sfxc_gpu_batch_destroy.argtypes = [C.c_void_p]
     lib.sfxc_gpu_last_timings.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+    lib.sfxc_gpu_last_timings_n.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int32]
     lib.sfxc_gpu_delay_list.argtypes = [C.POINTER(DelayTable), C.c_int64, C.c_int64, C.c_int32, C.c_int32,
                                         C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                         C.c_int32]
