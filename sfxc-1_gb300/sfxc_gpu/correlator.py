@@ -607,16 +607,18 @@ class Batch:
         self._lib.sfxc_gpu_batch_last_host_ms(self._h, out)
         return {"plan_ms": out[0], "graph_ms": out[1], "run_ms": out[2], "outputs_ms": out[3]}
 
-    def correlate(self, jobs, per_run=None):
+    def correlate(self, jobs, per_run=None, setup_lock=None):
         """Every integration of the jobs (one per node; any integration
         counts): per_run[i] integrations of job i in each graph (default: all
-        of them in one).  Returns [(cor (bytes or bytearray), tsys)] per job."""
+        of them in one).  Returns [(cor (bytes or bytearray), tsys)] per job.
+        setup_lock (a threading.Lock), when given, is held while the jobs are
+        set up and their inputs pushed before each graph: consecutive
+        timeslices correlated from several threads on other batches then set
+        up one at a time, each beside the others' graphs, instead of all at
+        once with the GPU idle."""
+        import contextlib
+        guard = setup_lock if setup_lock is not None else contextlib.nullcontext()
         pool = ThreadPoolExecutor(max_workers=len(self.nodes))
-        # each node's set-up and pushes from its own thread: the host work and
-        # the copies of different contexts run at the same time (the library
-        # calls drop the GIL)
-        for f in [pool.submit(n.set_parameters, j) for n, j in zip(self.nodes, jobs)]:
-            f.result()
         left = [int(j["n_integrations"]) for j in jobs]
         step = per_run or left
         done = [0] * len(jobs)
@@ -628,10 +630,19 @@ class Batch:
                 for k in range(n.nstreams):
                     n.push_protocol(k, j["protocols"][k][it])
 
+        first = True
         while any(left):
             counts = [min(s, l) for s, l in zip(step, left)]
-            for f in [pool.submit(push, n, j, d, c) for n, j, d, c in zip(self.nodes, jobs, done, counts)]:
-                f.result()
+            with guard:
+                if first:
+                    # each node's set-up and pushes from its own thread: the host
+                    # work and the copies of different contexts run at the same
+                    # time (the library calls drop the GIL)
+                    for f in [pool.submit(n.set_parameters, j) for n, j in zip(self.nodes, jobs)]:
+                        f.result()
+                    first = False
+                for f in [pool.submit(push, n, j, d, c) for n, j, d, c in zip(self.nodes, jobs, done, counts)]:
+                    f.result()
             for q, (o, t) in enumerate(self.run(counts)):
                 cor[q].append(o)
                 tsys[q] += t

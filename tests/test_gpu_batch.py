@@ -4,7 +4,8 @@ work one CUDA graph per run (sfxc_gpu_batch_*), and the autotuner.
 
 Bars: a batch gives byte-identical output to the same jobs run one by one
 through sfxc_gpu_run_integration, on both X-step forms, also with several
-integrations of one job in one graph; on the batched uneven configuration's
+integrations of one job in one graph, and with timeslices in flight on
+two batches from two host threads; on the batched uneven configuration's
 shape (20 stations: 32 MHz 2-bit, 64 MHz 2-bit at twice the job rate, 16 MHz
 1-bit at half of it; 4096-, 16384- and 256-channel jobs with integration
 times in the ratio 8:2:1) every job's visibilities are within relative L2
@@ -94,6 +95,45 @@ def test_batch_equals_single_runs(mode, c4_case, sfxc_lib):
                 n.close()
         assert outs == single
         assert outs2 == single
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_batches_in_flight_equal_single_runs(mode, c4_case, sfxc_lib):
+    """Consecutive timeslices on two batches from two host threads (set-ups
+    one at a time under a shared lock, each graph captured and run beside the
+    other batch's): every timeslice byte for byte equal to the jobs run one
+    by one."""
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+    from sfxc_gpu import correlator
+    built, _ = c4_case
+    single = []
+    for job in built:
+        node = correlator.CorrelatorNode(0, _mode(mode))
+        try:
+            single.append(node.correlate(job))
+        finally:
+            node.close()
+    sets = [[correlator.CorrelatorNode(0, _mode(mode)) for _ in built] for _ in range(2)]
+    batches = [correlator.Batch(nodes) for nodes in sets]
+    lock = threading.Lock()
+    try:
+        with ThreadPoolExecutor(max_workers=2) as ex:
+            futs, outs = [], []
+            for i in range(6):  # timeslice i on batch i % 2, once timeslice i - 2 is done
+                if len(futs) == 2:
+                    outs.append(futs.pop(0).result())
+                futs.append(ex.submit(batches[i % 2].correlate, built, [1] * len(built) if i % 3 == 2 else None,
+                                      lock))
+            outs += [f.result() for f in futs]
+    finally:
+        for b in batches:
+            b.close()
+        for nodes in sets:
+            for n in nodes:
+                n.close()
+    for i, o in enumerate(outs):
+        assert o == single, "timeslice %d" % i
 
 
 def test_autotune_keeps_every_byte(sfxc_lib):
