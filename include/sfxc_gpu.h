@@ -25,8 +25,9 @@
  * Conventions: plain pointers and sizes; every call returns 0 or a negative
  * status (SFXC_GPU_E*), with a message from sfxc_gpu_last_error().  Input
  * buffers belong to the caller and are not referenced after a call returns.
- * One host thread drives one context; a context owns two CUDA streams on one
- * device (the second carries per-block parameters ahead of the first).
+ * One host thread drives one context; a context owns three CUDA streams on
+ * one device (the second carries per-block parameters ahead of the first, the
+ * third a sub-integration chunk's X-step beside the next chunk's F-step).
  * Contexts created in one process get successive stream priorities
  * (cycling through the device's range), so that jobs correlated side by side
  * on one GPU finish in turn and their host work overlaps each other's kernels.
