@@ -3079,8 +3079,8 @@ int sfxc_gpu_batch_run_counts(sfxc_gpu_batch *b, const int32_t *counts, sfxc_out
         }
       };
       std::vector<std::thread> threads;
-      for (int k = 0; k < n; k++)
-        if (cnt[k]) threads.emplace_back(prepare_job, k);
+      for (size_t k = 0; k < n; k++)
+        if (cnt[k]) threads.emplace_back(prepare_job, (int)k);
       for (std::thread &t : threads) t.join();
     }
     for (i = 0; i < n; i++)

@@ -1274,7 +1274,7 @@ void launch_phasecal(const uint8_t *data, const PcalRun *runs, int nruns, int pb
 template <int LOGN, int OUT_TC, int SPCMAX>
 static void window_fft_launch_spc(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                                   const float *window, const float2 *tw_rot, int nper, int M, int kpad, void *spec,
-                                  float tc_scale, int tc_slots, cudaStream_t st, int waves) {
+                                  float tc_scale, cudaStream_t st, int waves) {
   using S = WinShape<LOGN, SPCMAX>;
   const int nsg = (nstreams + S::SPC - 1) / S::SPC, nsteps = (nrows + S::RPC - 1) / S::RPC;
   // runs of steps so that the CTAs fill two waves by default (three or four
@@ -1293,13 +1293,13 @@ static void window_fft_launch_spc(const StreamDev *d_streams, int nstreams, int 
 template <int LOGN, int OUT_TC>
 static void window_fft_launch(const StreamDev *d_streams, int nstreams, int row0, int nrows, int nrows_total,
                               const float *window, const float2 *tw_rot, int nper, int M, int kpad, void *spec,
-                              float tc_scale, int tc_slots, cudaStream_t st, int waves) {
+                              float tc_scale, cudaStream_t st, int waves) {
   // four streams per CTA: a whole 32-byte sector per channel in the TC layout
   // (two streams per CTA, two CTAs per SM, measured 20 % slower; each group
   // writing its own stream's 8-byte pieces, without the CTA-wide barriers,
   // 74 % slower)
   window_fft_launch_spc<LOGN, OUT_TC, 4>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad,
-                                         spec, tc_scale, tc_slots, st, waves);
+                                         spec, tc_scale, st, waves);
 }
 
 #define SFXC_LOGN_SWITCH(logn, CALL) \
@@ -1321,12 +1321,12 @@ void launch_window_fft(const StreamDev *d_streams, int nstreams, int row0, int n
 #define SFXC_WIN(L)                                                                                            \
   (tc_slots == kTcSlots                                                                                         \
        ? window_fft_launch<L, kTcSlots>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M,  \
-                                        kpad, spec, tc_scale, tc_slots, st, waves)                            \
+                                        kpad, spec, tc_scale, st, waves)                                      \
    : tc_slots == kTcSlotsWide                                                                                    \
        ? window_fft_launch<L, kTcSlotsWide>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, \
-                                            M, kpad, spec, tc_scale, tc_slots, st, waves)                     \
+                                            M, kpad, spec, tc_scale, st, waves)                               \
        : window_fft_launch<L, 0>(d_streams, nstreams, row0, nrows, nrows_total, window, tw_rot, nper, M, kpad,    \
-                                 spec, tc_scale, 0, st, waves))
+                                 spec, tc_scale, st, waves))
   SFXC_LOGN_SWITCH(logn, SFXC_WIN)
 #undef SFXC_WIN
 }
