@@ -1088,9 +1088,10 @@ void enqueue_integration(sfxc_gpu_ctx *c, int k = 0, bool require_push = true) {
   // times then overlap: each is its own kernels' elapsed time).  Measured
   // at 4096 channels: the FP32 X-step path 5-6 % faster overall (16- and
   // 32-stream jobs), a batch with row-gathered tensor-core X-steps (40-stream
-  // jobs) 5 %; the TMA-fed X-step 1.3 % slower (its channel groups are split
-  // over one CTA per SM in advance, so the slowest SM sets its time), so it
-  // stays on the main stream.
+  // jobs) 5 %; the TMA-fed X-step 1.3-3 % slower, whatever its CTA count
+  // (with 129 KB of shared memory it leaves room for one of the F-step's four
+  // CTAs per SM, so the F-step's time grows by about what the X-step takes),
+  // so it stays on the main stream.
   const size_t R = ranges.size();
   cudaStream_t xs = tc_tma ? st : c->st3;
   for (size_t ch = 0; ch < R; ch++) {
