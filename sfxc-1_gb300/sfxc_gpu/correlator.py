@@ -631,24 +631,26 @@ class Batch:
                     n.push_protocol(k, j["protocols"][k][it])
 
         first = True
-        while any(left):
-            counts = [min(s, l) for s, l in zip(step, left)]
-            with guard:
-                if first:
-                    # each node's set-up and pushes from its own thread: the host
-                    # work and the copies of different contexts run at the same
-                    # time (the library calls drop the GIL)
-                    for f in [pool.submit(n.set_parameters, j) for n, j in zip(self.nodes, jobs)]:
+        try:
+            while any(left):
+                counts = [min(s, l) for s, l in zip(step, left)]
+                with guard:
+                    if first:
+                        # each node's set-up and pushes from its own thread: the host
+                        # work and the copies of different contexts run at the same
+                        # time (the library calls drop the GIL)
+                        for f in [pool.submit(n.set_parameters, j) for n, j in zip(self.nodes, jobs)]:
+                            f.result()
+                        first = False
+                    for f in [pool.submit(push, n, j, d, c) for n, j, d, c in zip(self.nodes, jobs, done, counts)]:
                         f.result()
-                    first = False
-                for f in [pool.submit(push, n, j, d, c) for n, j, d, c in zip(self.nodes, jobs, done, counts)]:
-                    f.result()
-            for q, (o, t) in enumerate(self.run(counts)):
-                cor[q].append(o)
-                tsys[q] += t
-            done = [d + c for d, c in zip(done, counts)]
-            left = [l - c for l, c in zip(left, counts)]
-        pool.shutdown()
+                for q, (o, t) in enumerate(self.run(counts)):
+                    cor[q].append(o)
+                    tsys[q] += t
+                done = [d + c for d, c in zip(done, counts)]
+                left = [l - c for l, c in zip(left, counts)]
+        finally:
+            pool.shutdown()  # after a failed call too: no worker threads left behind
         return [(c[0] if len(c) == 1 else b"".join(c), b"".join(t)) for c, t in zip(cor, tsys)]
 
     def close(self):
