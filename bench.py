@@ -757,7 +757,7 @@ def run_gpu(args):
     if "fp32_x_step" in s:
         line["fp32_x_step"] = s["fp32_x_step"]
     line.update(extra)
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and world == 1:  # rank 0 at one GPU only
         line["cpu_baseline"] = cpu_baseline(cfg, args.cpu_sample_us)
     print(json.dumps(line), flush=True)
 
