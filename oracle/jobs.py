@@ -35,10 +35,10 @@ def _write_job(path, lines):
             f.write(key + " " + " ".join(str(v) for v in vals) + "\n")
 
 
-def _run(mode, lines, out, workdir, impl):
+def _run(mode, lines, out, workdir, impl, timeout=None):
     job = os.path.join(workdir, mode + ".job")
     _write_job(job, lines)
-    r = subprocess.run([_EXE[impl](), mode, job, out], capture_output=True, text=True)
+    r = subprocess.run([_EXE[impl](), mode, job, out], capture_output=True, text=True, timeout=timeout)
     if r.returncode != 0:
         raise RuntimeError("%s %s failed (%d): %s%s" % (impl, mode, r.returncode, r.stdout, r.stderr))
 
@@ -136,10 +136,11 @@ def extract(words_bytes, word_bytes, bits, nsamples, tracks, impl="reference"):
 
 
 def reader(recording, fmt, *, ref_ticks, offset_ticks=0, track_bit_rate, frame_size=0, n_tracks, bits,
-           channel_tracks, max_blocks=1000000):
+           channel_tracks, max_blocks=1000000, timeout=None):
     """Blocks of the reference's VDIF_reader / Mark5b_reader over a recording:
     dicts {channel, start_ticks, data, invalid [(begin, n)]}.  Only the
-    reference's own classes implement this (there is no restatement)."""
+    reference's own classes implement this (there is no restatement).
+    timeout (s): subprocess.TimeoutExpired when the reader runs longer."""
     with tempfile.TemporaryDirectory() as d:
         path = os.path.join(d, "rec.bin")
         open(path, "wb").write(bytes(recording))
@@ -149,7 +150,7 @@ def reader(recording, fmt, *, ref_ticks, offset_ticks=0, track_bit_rate, frame_s
         lines += [("channel#%d" % c, *tr) for c, tr in enumerate(channel_tracks)]
         out = os.path.join(d, "out")
         os.makedirs(out)
-        _run("reader", lines, out, d, "reference")
+        _run("reader", lines, out, d, "reference", timeout=timeout)
         raw = open(os.path.join(out, "data.bin"), "rb").read()
         blocks, pos = [], 0
         for line in open(os.path.join(out, "blocks.txt")):
