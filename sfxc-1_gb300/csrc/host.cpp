@@ -220,7 +220,7 @@ void UvwModel::get(int pc, ticks_t t, double out[3]) {
   if (t > interval_end_) create(t);
   if (pc < 0 || pc >= (int)splines_.size()) throw Error(-1, "no such phase centre in the UVW model's scan");
   const double sec = time_diff(t, t_.scans[scan_nr_].begin);
-  for (int k = 0; k < 3; k++) out[k] = splines_[(size_t)pc].eval(k, sec);
+  for (int k = 0; k < 3; k++) out[k] = splines_[(size_t)pc].eval_extended(k, sec);
 }
 
 // Interval search as GSL's gsl_interp_bsearch; the device uses the same rule.
@@ -238,6 +238,17 @@ int Spline::index(double v) const {
 }
 double Spline::eval(int col, double v) const {
   int i = index(v);
+  const double dx = v - x[i];
+  return y[col][i] + dx * (b[col][i] + dx * (c[col][i] + d[col][i] * dx));
+}
+// gsl_spline_eval as GSL 1.9 has it (interpolation/interp.c, gsl_interp_eval)
+// checks no domain: outside the nodes its interval search returns the first
+// or the last interval and akima_eval extends that interval's cubic.
+// Uvw_model::get_uvw evaluates this way when a time steps back before its
+// spline's window (the spline is only rebuilt for later times) or lies past a
+// scan's last row.
+double Spline::eval_extended(int col, double v) const {
+  const int i = v < x[0] ? 0 : v > x[n - 1] ? n - 2 : index(v);
   const double dx = v - x[i];
   return y[col][i] + dx * (b[col][i] + dx * (c[col][i] + d[col][i] * dx));
 }

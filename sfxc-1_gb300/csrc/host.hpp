@@ -73,6 +73,7 @@ struct Spline {
                       const std::vector<double> *const cols[3]);
   int index(double x) const;
   double eval(int col, double x) const;
+  double eval_extended(int col, double x) const;  // no domain check, as GSL 1.9's gsl_spline_eval
   double deriv(int col, double x) const;
   double delay(ticks_t t) const;       // Delay_table_akima::delay (114-126)
   double rate(ticks_t t) const;        // ::rate (128-136)
